@@ -1,0 +1,143 @@
+/*
+ * justpic_gb300.h -- C ABI of the GB300-native JustPIC particle-in-cell hot path.
+ *
+ * One handle (`jp_particles`) carries the geometry part of JustPIC's
+ * `Particles` struct (src/particles.jl:17-46): dimension, cell counts, the
+ * vertex grid `xvi`, the staggered velocity grids `xi_vel`, their spacings and
+ * `nxcell/max_xcell/min_xcell`. The per-slot data (coordinates, the occupancy
+ * `index`, particle fields) stay owned by the caller as plain device pointers
+ * laid out like the reference's GPU CellArrays (blocklength 0,
+ * ext/JustPICCUDAExt.jl:29): slot s (0-based) of cell c (0-based, column-major,
+ * x fastest) is element c + ncells * s. The index is one byte per slot
+ * (Julia Bool). Grid fields (velocity components, vertex fields) are
+ * column-major device arrays with x fastest.
+ *
+ * Every mutating entry point replaces one exported Julia function of the
+ * reference and keeps its semantics: it works in place, returns JP_OK (0) or a
+ * negative JP_ERR_* code (the Julia side turns it into an exception), and is
+ * synchronous by default like the reference's `launch!` (src/launch.jl:65-69).
+ * Kernels run on the stream given to jp_set_stream (default: the legacy
+ * default stream). The handle is not thread-safe.
+ *
+ * Limits: ndim 2 or 3; 1 <= max_xcell <= 64; at most JP_MAX_ARGS particle
+ * fields per call; grids strictly increasing.
+ */
+#ifndef JUSTPIC_GB300_H
+#define JUSTPIC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JP_OK 0
+#define JP_ERR_INVALID_ARGUMENT (-1) /* ArgumentError in the reference */
+#define JP_ERR_CUDA (-2)             /* a CUDA runtime call failed */
+#define JP_ERR_OUT_OF_MEMORY (-3)
+#define JP_ERR_BISECTION_LIMIT (-4)  /* a cell search hit its iteration cap */
+#define JP_ERR_NOT_BUILT (-5)
+
+#define JP_MAX_ARGS 16
+
+/* warning bits (jp_get_warnings): conditions the reference does not report */
+#define JP_WARN_FAR_MOVE 0x2     /* a particle moved more than one cell; it was dropped */
+#define JP_WARN_NO_NEIGHBOUR 0x4 /* an injected particle had no live neighbour to copy fields from */
+
+/* integrators, src/Advection/types.jl:17-49 */
+#define JP_EULER 0
+#define JP_RUNGE_KUTTA2 1
+#define JP_RUNGE_KUTTA4 2
+
+typedef struct jp_particles jp_particles;
+
+/*
+ * Grid description: the staggered velocity grids of init_particles
+ * (src/Particles/particles_utils.jl:30-35). xi_vel[c][d] is the coordinate
+ * vector (host memory) of velocity component c along axis d, of length
+ * n_vel[c][d]. The vertex grid is xi_vel[d][d], so the cell count along d is
+ * n_vel[d][d] - 1. `uniform` selects the spacing rule: 1 = range grids (one
+ * spacing x[1] - x[0] per axis, particles_utils.jl:137-139), 0 = vector grids
+ * (per-interval diff, particles_utils.jl:76-79).
+ */
+typedef struct jp_grid_desc {
+    int32_t ndim;
+    int32_t uniform;
+    const double* xi_vel[3][3];
+    int64_t n_vel[3][3];
+} jp_grid_desc;
+
+/*
+ * Create a container. Replaces the geometry part of init_particles
+ * (src/Particles/particles_utils.jl:48-106 and :108-166): nxcell is rounded up
+ * to a multiple of 2^ndim and max_xcell raised to at least that. `seed` keys
+ * the counter RNG used by jp_init_particles and jp_inject_particles.
+ */
+int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nxcell,
+                        int32_t max_xcell, int32_t min_xcell, uint64_t seed);
+int jp_particles_destroy(jp_particles* p);
+
+/* Read back the derived sizes (the fields of Particles, src/particles.jl:17-29). */
+int jp_particles_info(const jp_particles* p, int32_t* ndim, int64_t ncells[3], int32_t* nxcell,
+                      int32_t* max_xcell, int32_t* min_xcell, int64_t* np);
+
+int jp_set_stream(jp_particles* p, void* cuda_stream);
+/* 1 (default): every call synchronizes and reports device-side errors, like
+   launch! (src/launch.jl:65-69). 0: calls only enqueue; jp_synchronize reports. */
+int jp_set_synchronous(jp_particles* p, int32_t synchronous);
+int jp_synchronize(jp_particles* p);
+/* Sticky warning bits (JP_WARN_*) since the last call with clear = 1. */
+int jp_get_warnings(jp_particles* p, uint32_t* bits, int32_t clear);
+/* Number of inject calls so far: the `call` word of the injection RNG counter. */
+int jp_get_rng_counter(const jp_particles* p, uint64_t* counter);
+int jp_set_rng_counter(jp_particles* p, uint64_t counter);
+/* Message of the last failing call on this thread. */
+const char* jp_last_error(void);
+
+/*
+ * Seed particles: fill_coords_index! (src/Particles/particles_utils.jl:168-194).
+ * Writes every slot: np_quadrant random points per quadrant/octant in slots
+ * 0..nxcell-1 (index 1), NaN and index 0 elsewhere.
+ */
+int jp_init_particles(jp_particles* p, double* const coords[3], uint8_t* index);
+
+/*
+ * advection! (src/Particles/Advection/advection.jl:35-62): advect every live
+ * particle through the staggered velocity components V[0..ndim-1] (device,
+ * sized n_vel[c][0] x n_vel[c][1] (x n_vel[c][2])). method = JP_EULER,
+ * JP_RUNGE_KUTTA2 (alpha in (0, 1)) or JP_RUNGE_KUTTA4.
+ */
+int jp_advection(jp_particles* p, int32_t method, double alpha, const double* const V[3],
+                 double dt, double* const coords[3], const uint8_t* index);
+
+/*
+ * move_particles! (src/Particles/move_safe.jl:21-125): relocate particles that
+ * left their cell, carrying the nargs particle fields args[0..nargs-1]. Slot
+ * allocation reproduces the reference's colour passes exactly.
+ */
+int jp_move_particles(jp_particles* p, double* const coords[3], uint8_t* index,
+                      double* const* args, int32_t nargs);
+
+/*
+ * inject_particles! (src/Particles/injection.jl:19-131): reseed quadrants of
+ * under-populated cells; new particles copy the fields of their nearest
+ * neighbour.
+ */
+int jp_inject_particles(jp_particles* p, double* const coords[3], uint8_t* index,
+                        double* const* args, int32_t nargs);
+
+/* grid2particle! (src/Interpolations/grid_to_particle.jl:26-45): vertex field F
+   (n0+1 x n1+1 (x n2+1)) to the live slots of Fp. */
+int jp_grid2particle(jp_particles* p, double* Fp, const double* F, const double* const coords[3],
+                     const uint8_t* index);
+
+/* particle2grid! (src/Interpolations/particle_to_grid.jl:23-151): inverse
+   squared distance average of Fp onto the vertex field F. */
+int jp_particle2grid(jp_particles* p, double* F, const double* Fp, const double* const coords[3],
+                     const uint8_t* index);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JUSTPIC_GB300_H */

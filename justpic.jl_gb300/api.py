@@ -1,0 +1,164 @@
+"""The hot-path functions of JustPIC.jl, one native call each.
+
+Julia's in-place ``f!`` becomes ``f_`` here (PyTorch's in-place convention):
+
+=====================  ===============================================
+Python                 reference
+=====================  ===============================================
+``advection_``         ``advection!`` (src/Particles/Advection/advection.jl:21)
+``move_particles_``    ``move_particles!`` (src/Particles/move_safe.jl:21)
+``inject_particles_``  ``inject_particles!`` (src/Particles/injection.jl:19)
+``grid2particle_``     ``grid2particle!`` (src/Interpolations/grid_to_particle.jl:26)
+``particle2grid_``     ``particle2grid!`` (src/Interpolations/particle_to_grid.jl:23)
+=====================  ===============================================
+
+Calls are synchronous (like the reference's ``launch!``) unless
+``set_synchronous(particles, False)`` was called; kernels run on PyTorch's
+current CUDA stream.
+"""
+from __future__ import annotations
+
+import ctypes
+import warnings
+
+import numpy as np
+import torch
+
+from . import _native
+from ._native import JP_MAX_ARGS, JP_WARN_FAR_MOVE, JP_WARN_NO_NEIGHBOUR, ArgumentError, P3, check
+from .integrators import AbstractAdvectionIntegrator
+from .particles import CellArray, Particles
+
+
+def _bind_stream(p: Particles) -> None:
+    s = torch.cuda.current_stream()
+    _native.load().jp_set_stream(p.handle, s.cuda_stream)
+
+
+def _warn_bits(bits: int) -> None:
+    if bits & JP_WARN_FAR_MOVE:
+        warnings.warn("move_particles!: a particle moved more than one cell in one step and was dropped "
+                      "(the reference's colour passes race in this case)", RuntimeWarning, stacklevel=3)
+    if bits & JP_WARN_NO_NEIGHBOUR:
+        warnings.warn("inject_particles!: an injected particle had no live neighbour; its fields were left "
+                      "unchanged", RuntimeWarning, stacklevel=3)
+
+
+def _finish(p: Particles, rc: int, what: str) -> None:
+    check(rc, what)
+    if p._synchronous:
+        bits = ctypes.c_uint32(0)
+        check(_native.load().jp_get_warnings(p.handle, ctypes.byref(bits), 1))
+        if bits.value:
+            _warn_bits(bits.value)
+
+
+Particles._synchronous = True
+
+
+def set_synchronous(p: Particles, synchronous: bool) -> None:
+    """Toggle the per-call synchronisation (default on, as ``launch!``)."""
+    check(_native.load().jp_set_synchronous(p.handle, 1 if synchronous else 0))
+    p._synchronous = bool(synchronous)
+
+
+def synchronize(p: Particles) -> None:
+    """Wait for queued work and raise any device-side error."""
+    check(_native.load().jp_synchronize(p.handle))
+    bits = ctypes.c_uint32(0)
+    check(_native.load().jp_get_warnings(p.handle, ctypes.byref(bits), 1))
+    if bits.value:
+        _warn_bits(bits.value)
+
+
+def _coords(p: Particles) -> P3:
+    return P3(*[c.data_ptr() for c in p.coords], *([None] * (3 - p.ndim)))
+
+
+def _check_cellarray(p: Particles, A: CellArray, what: str) -> None:
+    if not isinstance(A, CellArray):
+        raise ArgumentError(f"{what} must be a CellArray")
+    if A.data.dtype != torch.float64 or not A.data.is_cuda:
+        raise ArgumentError(f"{what} must hold float64 CUDA data")
+    if A.ni != p.ni or A.ncap != p.max_xcell:
+        raise ArgumentError(f"{what} does not have the particle layout {p.max_xcell} x {p.ni}")
+
+
+def _check_grid(t: torch.Tensor, shape, what: str) -> None:
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64:
+        raise ArgumentError(f"{what} must be a float64 CUDA tensor")
+    if tuple(t.shape) != tuple(shape):
+        raise ArgumentError(f"{what} has shape {tuple(t.shape)}, expected {tuple(shape)}")
+    expected = tuple(int(np.prod(shape[:d])) for d in range(len(shape)))
+    if tuple(t.stride()) != expected:
+        raise ArgumentError(f"{what} must be column-major (Julia layout); use TA(backend)(array)")
+
+
+def _args(p: Particles, args):
+    args = tuple(args) if args is not None else ()
+    if len(args) > JP_MAX_ARGS:
+        raise ArgumentError(f"at most {JP_MAX_ARGS} particle fields are supported")
+    for k, a in enumerate(args):
+        _check_cellarray(p, a, f"args[{k}]")
+    arr = (ctypes.c_void_p * max(1, len(args)))(*[a.data_ptr() for a in args])
+    return arr, len(args)
+
+
+def advection_(particles: Particles, method: AbstractAdvectionIntegrator, V, dt) -> None:
+    """``advection!(particles, method, V, dt)``: advect every live particle
+    through the staggered velocity components ``V`` (one per axis)."""
+    if not isinstance(method, AbstractAdvectionIntegrator):
+        raise ArgumentError("method must be Euler(), RungeKutta2(α) or RungeKutta4()")
+    N = particles.ndim
+    V = tuple(V)
+    if len(V) != N:
+        raise ArgumentError(f"V must have {N} components")
+    for c in range(N):
+        _check_grid(V[c], tuple(len(x) for x in particles.xi_vel[c]), f"V[{c}]")
+    _bind_stream(particles)
+    vp = P3(*[v.data_ptr() for v in V], *([None] * (3 - N)))
+    rc = _native.load().jp_advection(particles.handle, method.code, float(method.alpha), vp, float(dt),
+                                     _coords(particles), particles.index.data_ptr())
+    _finish(particles, rc, "advection!")
+
+
+def move_particles_(particles: Particles, args=()) -> None:
+    """``move_particles!(particles, args)``: relocate particles that left their
+    cell, carrying the per-particle fields ``args``."""
+    arr, n = _args(particles, args)
+    _bind_stream(particles)
+    rc = _native.load().jp_move_particles(particles.handle, _coords(particles), particles.index.data_ptr(), arr, n)
+    _finish(particles, rc, "move_particles!")
+
+
+def inject_particles_(particles: Particles, args=()) -> None:
+    """``inject_particles!(particles, args)``: reseed under-populated cells."""
+    arr, n = _args(particles, args)
+    _bind_stream(particles)
+    rc = _native.load().jp_inject_particles(particles.handle, _coords(particles), particles.index.data_ptr(),
+                                            arr, n)
+    _finish(particles, rc, "inject_particles!")
+
+
+def _vertex_shape(p: Particles):
+    return tuple(n + 1 for n in p.ni)
+
+
+def grid2particle_(Fp: CellArray, F: torch.Tensor, particles: Particles) -> None:
+    """``grid2particle!(Fp, F, particles)``: vertex field -> particles."""
+    _check_cellarray(particles, Fp, "Fp")
+    _check_grid(F, _vertex_shape(particles), "F")
+    _bind_stream(particles)
+    rc = _native.load().jp_grid2particle(particles.handle, Fp.data_ptr(), F.data_ptr(), _coords(particles),
+                                         particles.index.data_ptr())
+    _finish(particles, rc, "grid2particle!")
+
+
+def particle2grid_(F: torch.Tensor, Fp: CellArray, particles: Particles) -> None:
+    """``particle2grid!(F, Fp, particles)``: particles -> vertex field."""
+    _check_cellarray(particles, Fp, "Fp")
+    _check_grid(F, _vertex_shape(particles), "F")
+    _bind_stream(particles)
+    rc = _native.load().jp_particle2grid(particles.handle, F.data_ptr(), Fp.data_ptr(), _coords(particles),
+                                         particles.index.data_ptr())
+    _finish(particles, rc, "particle2grid!")

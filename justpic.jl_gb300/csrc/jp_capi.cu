@@ -1,0 +1,293 @@
+// jp_capi.cu -- the extern "C" boundary: container life cycle, argument
+// checks, error reporting and dispatch to the kernel launchers.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "jp_internal.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where)
+{
+    return fail(e == cudaErrorMemoryAllocation ? JP_ERR_OUT_OF_MEMORY : JP_ERR_CUDA,
+                std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+bool strictly_increasing(const double* x, int64_t n)
+{
+    for (int64_t i = 1; i < n; ++i)
+        if (!(x[i] > x[i - 1])) return false;
+    return true;
+}
+
+// After a launch: in synchronous mode wait, fold the device error word into a
+// status code and the sticky warnings.
+int finish(jp_particles* P, cudaError_t launch_err, const char* what)
+{
+    if (launch_err != cudaSuccess) return cuda_fail(launch_err, what);
+    if (!P->synchronous) return JP_OK;
+    return jp_synchronize(P);
+}
+
+bool check_coords(const jp_particles* P, const void* const* c)
+{
+    for (int d = 0; d < P->g.ndim; ++d)
+        if (c == nullptr || c[d] == nullptr) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* jp_last_error(void) { return g_last_error.c_str(); }
+
+int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nxcell,
+                        int32_t max_xcell, int32_t min_xcell, uint64_t seed)
+{
+    if (!out || !grid) return fail(JP_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    const int N = grid->ndim;
+    if (N != 2 && N != 3) return fail(JP_ERR_INVALID_ARGUMENT, "ndim must be 2 or 3");
+    if (nxcell <= 0) return fail(JP_ERR_INVALID_ARGUMENT, "nxcell must be positive");
+    for (int c = 0; c < N; ++c)
+        for (int d = 0; d < N; ++d) {
+            if (!grid->xi_vel[c][d] || grid->n_vel[c][d] < 2)
+                return fail(JP_ERR_INVALID_ARGUMENT, "The velocity grid cannot be empty");
+            if (!strictly_increasing(grid->xi_vel[c][d], grid->n_vel[c][d]))
+                return fail(JP_ERR_INVALID_ARGUMENT, "velocity grids must be strictly increasing");
+        }
+    // particles_utils.jl:86-91: quadrant rounding of nxcell, max_xcell >= nxcell
+    const int NQ = 1 << N;
+    const int npq = (nxcell + NQ - 1) / NQ;
+    const int nx_r = npq * NQ;
+    const int mx = max_xcell > nx_r ? max_xcell : nx_r;
+    if (mx > 64) return fail(JP_ERR_INVALID_ARGUMENT, "max_xcell above 64 is not supported");
+
+    auto* P = new jp_particles();
+    jp::DevGrid& g = P->g;
+    g.ndim = N;
+    g.uniform = grid->uniform ? 1 : 0;
+    g.np_quadrant = npq;
+    g.nxcell = nx_r;
+    g.max_xcell = mx;
+    g.min_xcell = min_xcell;
+    g.seed = seed;
+    g.ncells = 1;
+    for (int d = 0; d < 3; ++d) g.n[d] = 1;
+    for (int d = 0; d < N; ++d) {
+        g.n[d] = grid->n_vel[d][d] - 1;
+        g.ncells *= g.n[d];
+    }
+    // host staging of every grid vector: xv, dxv, xvel, dxvel
+    std::vector<double> host;
+    size_t off_xv[3], off_dxv[3], off_xvel[3][3], off_dxvel[3][3];
+    auto push = [&](const double* x, int64_t n) {
+        size_t o = host.size();
+        host.insert(host.end(), x, x + n);
+        return o;
+    };
+    auto push_spacing = [&](const double* x, int64_t n) {
+        size_t o = host.size();
+        for (int64_t i = 0; i + 1 < n; ++i)
+            host.push_back(grid->uniform ? x[1] - x[0] : x[i + 1] - x[i]);
+        return o;
+    };
+    for (int d = 0; d < N; ++d) {
+        const double* x = grid->xi_vel[d][d];
+        off_xv[d] = push(x, g.n[d] + 1);
+        off_dxv[d] = push_spacing(x, g.n[d] + 1);
+        double lo = x[0], hi = x[0];
+        for (int64_t i = 0; i <= g.n[d]; ++i) {
+            lo = x[i] < lo ? x[i] : lo;
+            hi = x[i] > hi ? x[i] : hi;
+        }
+        g.dom_lo[d] = lo;
+        g.dom_hi[d] = hi;
+    }
+    for (int c = 0; c < N; ++c)
+        for (int d = 0; d < N; ++d) {
+            const double* x = grid->xi_vel[c][d];
+            const int64_t n = grid->n_vel[c][d];
+            off_xvel[c][d] = push(x, n);
+            off_dxvel[c][d] = push_spacing(x, n);
+            g.nvel[c][d] = n;
+            g.lim_lo[c][d] = x[0];  // inner_limits: first/last (src/Advection/advection.jl:73-81)
+            g.lim_hi[c][d] = x[n - 1];
+        }
+    cudaError_t e = cudaMalloc(&P->dev_block, host.size() * sizeof(double));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(P->dev_block, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&P->d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(P->d_err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&P->h_err, sizeof(int));
+    if (e != cudaSuccess) {
+        int rc = cuda_fail(e, "jp_particles_create");
+        jp_particles_destroy(P);
+        return rc;
+    }
+    for (int d = 0; d < N; ++d) {
+        g.xv[d] = P->dev_block + off_xv[d];
+        g.dxv[d] = P->dev_block + off_dxv[d];
+        for (int c = 0; c < N; ++c) {
+            g.xvel[c][d] = P->dev_block + off_xvel[c][d];
+            g.dxvel[c][d] = P->dev_block + off_dxvel[c][d];
+        }
+    }
+    *out = P;
+    return JP_OK;
+}
+
+int jp_particles_destroy(jp_particles* P)
+{
+    if (!P) return JP_OK;
+    cudaFree(P->dev_block);
+    cudaFree(P->d_err);
+    if (P->h_err) cudaFreeHost(P->h_err);
+    cudaFree(P->move.L0);  // one allocation holds all move scratch
+    cudaFree(P->inject.flag);
+    delete P;
+    return JP_OK;
+}
+
+int jp_particles_info(const jp_particles* P, int32_t* ndim, int64_t ncells[3], int32_t* nxcell,
+                      int32_t* max_xcell, int32_t* min_xcell, int64_t* np)
+{
+    if (!P) return fail(JP_ERR_INVALID_ARGUMENT, "null container");
+    if (ndim) *ndim = P->g.ndim;
+    if (ncells)
+        for (int d = 0; d < 3; ++d) ncells[d] = P->g.n[d];
+    if (nxcell) *nxcell = P->g.nxcell;
+    if (max_xcell) *max_xcell = P->g.max_xcell;
+    if (min_xcell) *min_xcell = P->g.min_xcell;
+    if (np) *np = (int64_t)P->g.max_xcell * P->g.ncells;
+    return JP_OK;
+}
+
+int jp_set_stream(jp_particles* P, void* s)
+{
+    if (!P) return fail(JP_ERR_INVALID_ARGUMENT, "null container");
+    P->stream = (cudaStream_t)s;
+    return JP_OK;
+}
+
+int jp_set_synchronous(jp_particles* P, int32_t sync)
+{
+    if (!P) return fail(JP_ERR_INVALID_ARGUMENT, "null container");
+    P->synchronous = sync ? 1 : 0;
+    return JP_OK;
+}
+
+int jp_synchronize(jp_particles* P)
+{
+    if (!P) return fail(JP_ERR_INVALID_ARGUMENT, "null container");
+    cudaError_t e = cudaMemcpyAsync(P->h_err, P->d_err, sizeof(int), cudaMemcpyDeviceToHost, P->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "jp_synchronize");
+    const int bits = *P->h_err;
+    if (bits) {
+        e = cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "jp_synchronize");
+    }
+    P->warnings |= (uint32_t)(bits & (jp::kWarnFarMove | jp::kWarnNoNeighbour));
+    if (bits & jp::kErrBisection)
+        return fail(JP_ERR_BISECTION_LIMIT, "cell search exceeded its iteration cap (NaN or out-of-grid position)");
+    return JP_OK;
+}
+
+int jp_get_warnings(jp_particles* P, uint32_t* bits, int32_t clear)
+{
+    if (!P || !bits) return fail(JP_ERR_INVALID_ARGUMENT, "null argument");
+    *bits = P->warnings;
+    if (clear) P->warnings = 0;
+    return JP_OK;
+}
+
+int jp_get_rng_counter(const jp_particles* P, uint64_t* counter)
+{
+    if (!P || !counter) return fail(JP_ERR_INVALID_ARGUMENT, "null argument");
+    *counter = P->inject_calls;
+    return JP_OK;
+}
+
+int jp_set_rng_counter(jp_particles* P, uint64_t counter)
+{
+    if (!P) return fail(JP_ERR_INVALID_ARGUMENT, "null container");
+    P->inject_calls = counter;
+    return JP_OK;
+}
+
+int jp_init_particles(jp_particles* P, double* const coords[3], uint8_t* index)
+{
+    if (!P || !index || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_init_particles: null pointer");
+    return finish(P, jp::launch_init(P, coords, index), "jp_init_particles");
+}
+
+int jp_advection(jp_particles* P, int32_t method, double alpha, const double* const V[3], double dt,
+                 double* const coords[3], const uint8_t* index)
+{
+    if (!P || !index || !check_coords(P, (const void* const*)coords) ||
+        !check_coords(P, (const void* const*)V))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection: null pointer");
+    if (method != JP_EULER && method != JP_RUNGE_KUTTA2 && method != JP_RUNGE_KUTTA4)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection: unknown integrator");
+    if (method == JP_RUNGE_KUTTA2 && !(0.0 < alpha && alpha < 1.0))
+        return fail(JP_ERR_INVALID_ARGUMENT, "Only 0 < α < 1 is supported");
+    return finish(P, jp::launch_advection(P, method, alpha, V, dt, coords, index), "jp_advection");
+}
+
+int jp_move_particles(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
+                      int32_t nargs)
+{
+    if (!P || !index || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles: null pointer");
+    if (nargs < 0 || nargs > JP_MAX_ARGS || (nargs > 0 && !args))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles: bad particle field list");
+    for (int k = 0; k < nargs; ++k)
+        if (!args[k]) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles: null field");
+    return finish(P, jp::launch_move(P, coords, index, args, nargs), "jp_move_particles");
+}
+
+int jp_inject_particles(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
+                        int32_t nargs)
+{
+    if (!P || !index || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_particles: null pointer");
+    if (nargs < 0 || nargs > JP_MAX_ARGS || (nargs > 0 && !args))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_particles: bad particle field list");
+    for (int k = 0; k < nargs; ++k)
+        if (!args[k]) return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_particles: null field");
+    const uint32_t call = (uint32_t)P->inject_calls;
+    P->inject_calls += 1;
+    return finish(P, jp::launch_inject(P, coords, index, args, nargs, call), "jp_inject_particles");
+}
+
+int jp_grid2particle(jp_particles* P, double* Fp, const double* F, const double* const coords[3],
+                     const uint8_t* index)
+{
+    if (!P || !Fp || !F || !index || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_grid2particle: null pointer");
+    return finish(P, jp::launch_g2p(P, Fp, F, coords, index), "jp_grid2particle");
+}
+
+int jp_particle2grid(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
+                     const uint8_t* index)
+{
+    if (!P || !Fp || !F || !index || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid: null pointer");
+    return finish(P, jp::launch_p2g(P, F, Fp, coords, index), "jp_particle2grid");
+}
+
+}  // extern "C"

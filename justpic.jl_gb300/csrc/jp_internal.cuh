@@ -1,0 +1,234 @@
+// jp_internal.cuh -- shared device helpers and the container state of the
+// GB300 particle-in-cell library (all kernels compile for sm_103a with
+// -fmad=false: every fused multiply-add below is an explicit fma()).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/justpic_gb300.h"
+#include "../../include/justpic_gb300_rng.h"
+
+namespace jp {
+
+// device-side error / warning bits (one int word per container)
+constexpr int kErrBisection = 0x1;
+constexpr int kWarnFarMove = 0x2;
+constexpr int kWarnNoNeighbour = 0x4;
+
+constexpr int kBisectCap = 256;
+constexpr int kThreads = 256;
+
+// move_particles! destination codes: neighbour code (0..3^N-1) in bits 0..4,
+// bit 6 = the particle is not strictly inside its new cell (it will be
+// re-examined as a mover when that cell is walked), 0x3F = leaves / dropped.
+constexpr uint8_t kCodeExit = 0x3F;
+constexpr uint8_t kCodeUnstable = 0x40;
+
+// Geometry of a container, passed to kernels by value.
+struct DevGrid {
+    int ndim;
+    int max_xcell;
+    int nxcell;
+    int min_xcell;
+    int np_quadrant;
+    int uniform;
+    int64_t n[3];
+    int64_t ncells;
+    uint64_t seed;
+    const double* xv[3];        // vertex grid, n[d]+1
+    const double* dxv[3];       // vertex spacing per cell, n[d]
+    const double* xvel[3][3];   // velocity grid of component c along axis d
+    const double* dxvel[3][3];  // its spacing per interval
+    int64_t nvel[3][3];
+    double dom_lo[3], dom_hi[3];  // extrema of the vertex grid
+    double lim_lo[3][3], lim_hi[3][3];  // first/last of every velocity grid
+};
+
+// Scratch owned by a container for move_particles! (allocated on first use).
+struct MoveScratch {
+    uint64_t* L0 = nullptr;   // occupancy before the move
+    uint64_t* L = nullptr;    // occupancy, updated by the colour passes
+    uint64_t* M = nullptr;    // movers found by the classify pass
+    uint64_t* R = nullptr;    // slots refilled during this move
+    uint64_t* U = nullptr;    // refilled slots whose particle is not strictly inside
+    uint8_t* code = nullptr;  // destination code per mover slot
+    uint16_t* orig = nullptr; // origin tag per refilled slot
+    double* shadow = nullptr; // movers' coordinates and fields, per component
+    int shadow_comps = 0;
+    size_t bytes = 0;
+};
+
+struct InjectScratch {
+    uint8_t* flag = nullptr;  // cell needs the sequential injection walk
+};
+
+}  // namespace jp
+
+struct jp_particles {
+    jp::DevGrid g;
+    double* dev_block = nullptr;  // all grid vectors in one allocation
+    int* d_err = nullptr;         // device error/warning word
+    int* h_err = nullptr;         // pinned mirror
+    cudaStream_t stream = nullptr;
+    int synchronous = 1;
+    uint32_t warnings = 0;
+    uint64_t inject_calls = 0;
+    jp::MoveScratch move;
+    jp::InjectScratch inject;
+};
+
+namespace jp {
+
+__device__ __forceinline__ void cell_coords(const DevGrid& g, int64_t c, int64_t I[3])
+{
+    I[0] = c % g.n[0];
+    I[1] = (c / g.n[0]) % g.n[1];
+    I[2] = g.ndim == 3 ? c / (g.n[0] * g.n[1]) : 0;
+}
+
+template <int DIM>
+__device__ __forceinline__ int64_t cell_linear(const DevGrid& g, const int64_t I[3])
+{
+    if (DIM == 2) return I[0] + g.n[0] * I[1];
+    return I[0] + g.n[0] * (I[1] + g.n[1] * I[2]);
+}
+
+__device__ __forceinline__ double ldg(const double* p) { return __ldg(p); }
+
+// lerp(t, v0, v1) = muladd(t, v1, muladd(-t, v0, v0)) (src/Interpolations/ndlerp.jl:15)
+__device__ __forceinline__ double lerp1(double t, double v0, double v1)
+{
+    return fma(t, v1, fma(-t, v0, v0));
+}
+
+template <int DIM>
+__device__ __forceinline__ double lerpN(const double* v, const double* t)
+{
+    if (DIM == 2) return lerp1(t[1], lerp1(t[0], v[0], v[1]), lerp1(t[0], v[2], v[3]));
+    return lerp1(t[2], lerp1(t[1], lerp1(t[0], v[0], v[1]), lerp1(t[0], v[2], v[3])),
+                 lerp1(t[1], lerp1(t[0], v[4], v[5]), lerp1(t[0], v[6], v[7])));
+}
+
+// find_parent_cell_bisection (src/Utils.jl:117-130), 0-based, bounded.
+// Result: s with x[s] <= px <= x[s+1]. When px lies strictly between two
+// nodes that s is unique, so a short local walk from the seed finds it; only a
+// px that sits exactly on a node (two valid answers) replays the reference's
+// bisection step by step to get the same pick.
+__device__ __forceinline__ int64_t bisect_exact(double px, const double* x, int64_t len,
+                                                int64_t seed, int* errs)
+{
+    int64_t lo = 0, hi = len - 1, s = seed;
+    for (int it = 0; it < kBisectCap; ++it) {
+        const double a = ldg(x + s), b = ldg(x + s + 1);
+        if (a <= px && px <= b) return s;
+        if (a < px) {
+            lo = s;
+            s = (hi + s) / 2;
+        } else {
+            hi = s;
+            s = (lo + s) / 2;
+        }
+    }
+    *errs |= kErrBisection;
+    return s;
+}
+
+__device__ __forceinline__ int64_t find_cell(double px, const double* x, int64_t len, int64_t seed,
+                                             int* errs)
+{
+    double a = ldg(x + seed), b = ldg(x + seed + 1);
+    if (a <= px && px <= b) return seed;  // the reference's first test
+    int64_t k = seed;
+    if (px < a) {
+#pragma unroll 1
+        for (int it = 0; it < 4 && k > 0; ++it) {
+            --k;
+            b = a;
+            a = ldg(x + k);
+            if (a <= px && px <= b) {
+                if (px == a || px == b) return bisect_exact(px, x, len, seed, errs);
+                return k;
+            }
+        }
+    } else if (px > b) {
+#pragma unroll 1
+        for (int it = 0; it < 4 && k + 2 < len; ++it) {
+            ++k;
+            a = b;
+            b = ldg(x + k + 1);
+            if (a <= px && px <= b) {
+                if (px == a || px == b) return bisect_exact(px, x, len, seed, errs);
+                return k;
+            }
+        }
+    }
+    return bisect_exact(px, x, len, seed, errs);
+}
+
+template <int DIM>
+__device__ __forceinline__ bool isincell(const double* p, const double* corner, const double* dx)
+{
+    bool in = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) in = in & (corner[d] < p[d]) & (p[d] < corner[d] + dx[d]);
+    return in;
+}
+
+template <int DIM>
+__host__ __device__ constexpr int self_code()
+{
+    return DIM == 2 ? 4 : 13;
+}
+
+template <int DIM>
+__device__ __forceinline__ int nb_code(const int off[3])
+{
+    return DIM == 2 ? (off[0] + 1) + 3 * (off[1] + 1)
+                    : (off[0] + 1) + 3 * (off[1] + 1) + 9 * (off[2] + 1);
+}
+
+template <int DIM>
+__device__ __forceinline__ void nb_offset(int code, int off[3])
+{
+    off[0] = code % 3 - 1;
+    off[1] = (code / 3) % 3 - 1;
+    off[2] = DIM == 3 ? code / 9 - 1 : 0;
+}
+
+__device__ __forceinline__ void raise_err(int* d_err, int bits)
+{
+    if (bits) atomicOr(d_err, bits);
+}
+
+inline unsigned grid_blocks(int64_t n, int threads = kThreads)
+{
+    return (unsigned)((n + threads - 1) / threads);
+}
+
+// launchers (one translation unit each)
+cudaError_t launch_init(jp_particles* P, double* const coords[3], uint8_t* index);
+cudaError_t launch_advection(jp_particles* P, int method, double alpha, const double* const V[3],
+                             double dt, double* const coords[3], const uint8_t* index);
+cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index,
+                        double* const* args, int nargs);
+cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* index,
+                          double* const* args, int nargs, uint32_t call);
+cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const double* const coords[3],
+                       const uint8_t* index);
+cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
+                       const uint8_t* index);
+
+// argument blocks passed by value
+struct Coords {
+    double* c[3];
+};
+struct CCoords {
+    const double* c[3];
+};
+struct Args {
+    double* a[JP_MAX_ARGS];
+    int n;
+};
+
+}  // namespace jp

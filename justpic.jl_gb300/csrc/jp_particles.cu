@@ -1,0 +1,409 @@
+// jp_particles.cu -- per-cell kernels: particle seeding, advection!,
+// grid2particle! and particle2grid!.
+//
+// Layout: one thread per cell (or per vertex column for particle2grid!), a warp
+// covers 32 consecutive cells along x, so every per-slot load and store of the
+// blocklength-0 CellArray (element c + ncells*s) is one coalesced 256-byte
+// (FP64) or 32-byte (index) transaction per warp.
+#include <math_constants.h>
+
+#include "jp_internal.cuh"
+
+namespace jp {
+
+struct CVel {
+    const double* v[3];
+};
+
+// ------------------------------------------------------------- seeding
+// fill_coords_index!: src/Particles/particles_utils.jl:168-194
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) init_kernel(DevGrid g, Coords X, uint8_t* __restrict__ index)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    const int64_t nc = g.ncells;
+    double x0[3], dx[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        x0[d] = ldg(g.xv[d] + I[d]);
+        dx[d] = ldg(g.dxv[d] + I[d]);
+    }
+    int l = 0;
+    for (int iq = 0; iq < (1 << DIM); ++iq) {
+        double xc[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xc[d] = x0[d] + (dx[d] * (double)((iq >> d) & 1)) / 2.0;
+        for (int q = 0; q < g.np_quadrant; ++q, ++l) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const double r = jp_rand_uniform(g.seed, JP_RNG_STREAM_INIT, 0u, (uint64_t)c, (uint32_t)l,
+                                                 (uint32_t)d);
+                X.c[d][c + nc * l] = xc[d] + (dx[d] / 2.0) * r;
+            }
+            index[c + nc * l] = 1;
+        }
+    }
+    for (; l < g.max_xcell; ++l) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) X.c[d][c + nc * l] = CUDART_NAN;
+        index[c + nc * l] = 0;
+    }
+}
+
+// ----------------------------------------------------------- advection
+// interp_velocity2particle for component `comp`
+// (src/Particles/Advection/advection.jl:93-148, src/Advection/advection.jl:3-47)
+template <int DIM>
+__device__ __forceinline__ double interp_component(const DevGrid& g, int comp, const double* p,
+                                                   const int64_t* I, const double* __restrict__ V,
+                                                   int* errs)
+{
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+        if (!(g.lim_lo[comp][d] <= p[d] && p[d] <= g.lim_hi[comp][d])) return CUDART_INF;
+    int64_t idx[3];
+    double t[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const double* x = g.xvel[comp][d];
+        idx[d] = find_cell(p[d], x, g.nvel[comp][d], I[d], errs);
+        const double xc = ldg(x + idx[d]);
+        const double dx = ldg(g.dxvel[comp][d] + idx[d]);
+        t[d] = (p[d] - xc) * (1.0 / dx);
+    }
+    const int64_t L0 = g.nvel[comp][0];
+    double v[8];
+    if (DIM == 2) {
+        const double* b = V + idx[0] + L0 * idx[1];
+        v[0] = ldg(b);
+        v[1] = ldg(b + 1);
+        v[2] = ldg(b + L0);
+        v[3] = ldg(b + L0 + 1);
+    } else {
+        const int64_t L1 = g.nvel[comp][1];
+        const int64_t sz = L0 * L1;
+        const double* b = V + idx[0] + L0 * (idx[1] + L1 * idx[2]);
+        v[0] = ldg(b);
+        v[1] = ldg(b + 1);
+        v[2] = ldg(b + L0);
+        v[3] = ldg(b + L0 + 1);
+        v[4] = ldg(b + sz);
+        v[5] = ldg(b + sz + 1);
+        v[6] = ldg(b + sz + L0);
+        v[7] = ldg(b + sz + L0 + 1);
+    }
+    return lerpN<DIM>(v, t);
+}
+
+template <int DIM>
+__device__ __forceinline__ void interp_velocity(const DevGrid& g, const CVel& V, const double* p,
+                                                const int64_t* I, double* v, int* errs)
+{
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) v[c] = interp_component<DIM>(g, c, p, I, V.v[c], errs);
+}
+
+// advect_particle: RK2 src/Particles/Advection/advection.jl:154-179 with
+// first/second_stage of src/Advection/RK2.jl; RK4 :261-279; Euler :348-367.
+template <int DIM, int METHOD>
+__device__ __forceinline__ void advect_particle(const DevGrid& g, const CVel& V, double alpha, double dt,
+                                                const int64_t* I, const double* p0, double* p, int* errs)
+{
+    if (METHOD == JP_RUNGE_KUTTA2) {
+        double v0[3], v1[3], p1[3];
+        interp_velocity<DIM>(g, V, p0, I, v0, errs);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) p1[d] = fma(1.0, (alpha * dt) * v0[d], p0[d]);
+        interp_velocity<DIM>(g, V, p1, I, v1, errs);
+        if (alpha == 0.5) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, dt * v1[d], p0[d]);
+        } else {
+            const double ia = 1.0 / alpha;
+            const double a = fma(-0.5, ia, 1.0);
+            const double b = 0.5 * ia;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, dt * fma(a, v0[d], b * v1[d]), p0[d]);
+        }
+    } else if (METHOD == JP_RUNGE_KUTTA4) {
+        double k1[3], k2[3], k3[3], k4[3], q[3];
+        interp_velocity<DIM>(g, V, p0, I, k1, errs);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) q[d] = p0[d] + (dt * k1[d]) / 2.0;
+        interp_velocity<DIM>(g, V, q, I, k2, errs);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) q[d] = p0[d] + (dt * k2[d]) / 2.0;
+        interp_velocity<DIM>(g, V, q, I, k3, errs);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) q[d] = p0[d] + dt * k3[d];
+        interp_velocity<DIM>(g, V, q, I, k4, errs);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            p[d] = p0[d] + (dt * (((k1[d] + 2.0 * k2[d]) + 2.0 * k3[d]) + k4[d])) / 6.0;
+    } else {
+        double v0[3];
+        interp_velocity<DIM>(g, V, p0, I, v0, errs);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, dt * v0[d], p0[d]);
+    }
+}
+
+// advection_kernel!: src/Particles/Advection/advection.jl:66-91
+template <int DIM, int METHOD>
+__global__ void __launch_bounds__(kThreads)
+    advect_kernel(DevGrid g, CVel V, double alpha, double dt, Coords X, const uint8_t* __restrict__ index,
+                  int* d_err)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    const int64_t nc = g.ncells;
+    int errs = 0;
+    for (int s = 0; s < g.max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        if (!index[a]) continue;
+        double p0[3], p[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) p0[d] = X.c[d][a];
+        advect_particle<DIM, METHOD>(g, V, alpha, dt, I, p0, p, &errs);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) X.c[d][a] = p[d];
+    }
+    raise_err(d_err, errs);
+}
+
+// ------------------------------------------------------- grid2particle!
+// _grid2particle_classic!: src/Interpolations/grid_to_particle.jl:64-82
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    g2p_kernel(DevGrid g, double* __restrict__ Fp, const double* __restrict__ F, CCoords X,
+               const uint8_t* __restrict__ index)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    const int64_t nc = g.ncells;
+    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
+    double x0[3], idx_[3], v[8];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        x0[d] = ldg(g.xv[d] + I[d]);
+        idx_[d] = 1.0 / ldg(g.dxv[d] + I[d]);
+    }
+    const double* b = F + I[0] + V0 * (I[1] + (DIM == 3 ? V1 * I[2] : 0));
+    v[0] = ldg(b);
+    v[1] = ldg(b + 1);
+    v[2] = ldg(b + V0);
+    v[3] = ldg(b + V0 + 1);
+    if (DIM == 3) {
+        const int64_t sz = V0 * V1;
+        v[4] = ldg(b + sz);
+        v[5] = ldg(b + sz + 1);
+        v[6] = ldg(b + sz + V0);
+        v[7] = ldg(b + sz + V0 + 1);
+    }
+    for (int s = 0; s < g.max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        if (!index[a]) continue;
+        double t[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) t[d] = (X.c[d][a] - x0[d]) * idx_[d];
+        Fp[a] = lerpN<DIM>(v, t);
+    }
+}
+
+// ------------------------------------------------------- particle2grid!
+// src/Interpolations/particle_to_grid.jl:37-68 (2D), :113-151 (3D).
+// One thread per vertex column marching along the last axis over `chunk`
+// vertex rows: the cells of row r are read once and feed both vertex r (its
+// upper half of the stencil) and vertex r+1 (its lower half), so every
+// vertex accumulates its cells in the reference's order (offsets of the last
+// axis outermost, x innermost, slots in order) and the sums are bit-identical.
+template <int DIM>
+__device__ __forceinline__ void p2g_cell(const DevGrid& g, int64_t c, const double* q_cur, const double* q_nxt,
+                                         bool has_next, const double* __restrict__ Fp, const CCoords& X,
+                                         const uint8_t* __restrict__ index, double& w_c, double& wF_c,
+                                         double& w_n, double& wF_n)
+{
+    const int64_t nc = g.ncells;
+    for (int s = 0; s < g.max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        if (!index[a]) continue;
+        double p[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) p[d] = X.c[d][a];
+        const double f = Fp[a];
+        {
+            double ss;
+            const double dx = q_cur[0] - p[0], dy = q_cur[1] - p[1];
+            if (DIM == 2) {
+                ss = dx * dx + dy * dy;
+            } else {
+                const double dz = q_cur[2] - p[2];
+                ss = (dx * dx + dy * dy) + dz * dz;
+            }
+            const double dist = sqrt(ss);
+            const double wi = 1.0 / (dist * dist);
+            w_c += wi;
+            wF_c = fma(wi, f, wF_c);
+        }
+        if (has_next) {
+            double ss;
+            const double dx = q_nxt[0] - p[0], dy = q_nxt[1] - p[1];
+            if (DIM == 2) {
+                ss = dx * dx + dy * dy;
+            } else {
+                const double dz = q_nxt[2] - p[2];
+                ss = (dx * dx + dy * dy) + dz * dz;
+            }
+            const double dist = sqrt(ss);
+            const double wi = 1.0 / (dist * dist);
+            w_n += wi;
+            wF_n = fma(wi, f, wF_n);
+        }
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    p2g_kernel(DevGrid g, double* __restrict__ F, const double* __restrict__ Fp, CCoords X,
+               const uint8_t* __restrict__ index, int chunk)
+{
+    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    constexpr int LAST = DIM - 1;
+    const int64_t nlast = g.n[LAST];  // cells along the marching axis
+    const int64_t cols = DIM == 2 ? V0 : V0 * V1;
+    const int64_t col = t % cols;
+    const int64_t q = t / cols;
+    const int64_t r0 = q * chunk;
+    if (r0 > nlast) return;  // vertex rows along the last axis: 0..nlast
+    const int64_t r1 = min(r0 + (int64_t)chunk, nlast + 1);
+    const int64_t i = col % V0;
+    const int64_t j = DIM == 3 ? col / V0 : 0;
+    double qv[3];
+    qv[0] = ldg(g.xv[0] + i);
+    if (DIM == 3) qv[1] = ldg(g.xv[1] + j);
+
+    // the (up to) 2^(DIM-1) cells of one row/layer, in reference order
+    int64_t cells[4];
+    int ncell_row = 0;
+    auto row_cells = [&](int64_t r) {
+        ncell_row = 0;
+        if (DIM == 2) {
+            for (int io = -1; io <= 0; ++io) {
+                const int64_t ic = i + io;
+                if (0 <= ic && ic < g.n[0]) cells[ncell_row++] = ic + g.n[0] * r;
+            }
+        } else {
+            for (int jo = -1; jo <= 0; ++jo) {
+                const int64_t jc = j + jo;
+                if (!(0 <= jc && jc < g.n[1])) continue;
+                for (int io = -1; io <= 0; ++io) {
+                    const int64_t ic = i + io;
+                    if (0 <= ic && ic < g.n[0]) cells[ncell_row++] = ic + g.n[0] * (jc + g.n[1] * r);
+                }
+            }
+        }
+    };
+
+    double w_c = 0.0, wF_c = 0.0;
+    double q_cur[3], q_nxt[3];
+    q_cur[0] = q_nxt[0] = qv[0];
+    if (DIM == 3) q_cur[1] = q_nxt[1] = qv[1];
+    if (r0 >= 1) {  // prologue: row r0-1 is the lower half of vertex r0's stencil
+        q_nxt[LAST] = ldg(g.xv[LAST] + r0);
+        row_cells(r0 - 1);
+        double w_d = 0.0, wF_d = 0.0;
+        for (int k = 0; k < ncell_row; ++k)
+            p2g_cell<DIM>(g, cells[k], q_nxt, q_nxt, false, Fp, X, index, w_c, wF_c, w_d, wF_d);
+    }
+    for (int64_t r = r0; r < r1; ++r) {
+        const bool has_next = r + 1 < r1;
+        q_cur[LAST] = ldg(g.xv[LAST] + r);
+        if (has_next) q_nxt[LAST] = ldg(g.xv[LAST] + r + 1);
+        double w_n = 0.0, wF_n = 0.0;
+        if (r < nlast) {
+            row_cells(r);
+            for (int k = 0; k < ncell_row; ++k)
+                p2g_cell<DIM>(g, cells[k], q_cur, q_nxt, has_next, Fp, X, index, w_c, wF_c, w_n, wF_n);
+        }
+        const int64_t v = DIM == 2 ? i + V0 * r : i + V0 * (j + V1 * r);
+        F[v] = DIM == 2 ? wF_c / w_c : wF_c * (1.0 / w_c);
+        w_c = w_n;
+        wF_c = wF_n;
+    }
+}
+
+// ------------------------------------------------------------ launchers
+cudaError_t launch_init(jp_particles* P, double* const coords[3], uint8_t* index)
+{
+    Coords X{{coords[0], coords[1], P->g.ndim == 3 ? coords[2] : nullptr}};
+    const unsigned nb = grid_blocks(P->g.ncells);
+    if (P->g.ndim == 2)
+        init_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, X, index);
+    else
+        init_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, X, index);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advection(jp_particles* P, int method, double alpha, const double* const V[3], double dt,
+                             double* const coords[3], const uint8_t* index)
+{
+    const bool d3 = P->g.ndim == 3;
+    Coords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
+    CVel Vv{{V[0], V[1], d3 ? V[2] : nullptr}};
+    const unsigned nb = grid_blocks(P->g.ncells);
+    cudaStream_t s = P->stream;
+#define JP_ADV(D, M) advect_kernel<D, M><<<nb, kThreads, 0, s>>>(P->g, Vv, alpha, dt, X, index, P->d_err)
+    if (!d3) {
+        if (method == JP_RUNGE_KUTTA2) JP_ADV(2, JP_RUNGE_KUTTA2);
+        else if (method == JP_RUNGE_KUTTA4) JP_ADV(2, JP_RUNGE_KUTTA4);
+        else JP_ADV(2, JP_EULER);
+    } else {
+        if (method == JP_RUNGE_KUTTA2) JP_ADV(3, JP_RUNGE_KUTTA2);
+        else if (method == JP_RUNGE_KUTTA4) JP_ADV(3, JP_RUNGE_KUTTA4);
+        else JP_ADV(3, JP_EULER);
+    }
+#undef JP_ADV
+    return cudaGetLastError();
+}
+
+cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const double* const coords[3],
+                       const uint8_t* index)
+{
+    const bool d3 = P->g.ndim == 3;
+    CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
+    const unsigned nb = grid_blocks(P->g.ncells);
+    if (!d3)
+        g2p_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, X, index);
+    else
+        g2p_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, X, index);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
+                       const uint8_t* index)
+{
+    const bool d3 = P->g.ndim == 3;
+    CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
+    const int64_t V0 = P->g.n[0] + 1, V1 = P->g.n[1] + 1;
+    const int64_t cols = d3 ? V0 * V1 : V0;
+    const int64_t nlast = P->g.n[d3 ? 2 : 1];
+    // about four threads' worth of work per SM lane: columns x row chunks
+    int chunk = 8;
+    const int64_t nchunks = (nlast + 1 + chunk - 1) / chunk;
+    const unsigned nb = grid_blocks(cols * nchunks);
+    if (!d3)
+        p2g_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk);
+    else
+        p2g_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk);
+    return cudaGetLastError();
+}
+
+}  // namespace jp

@@ -1,0 +1,636 @@
+/*
+ * jp_oracle.c -- FP64 CPU restatement of JustPIC.jl's particle-in-cell hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the correctness oracle for the CUDA library and the
+ * CPU baseline that bench.py times. Nothing in the product links or calls it.
+ *
+ * Every function follows the cited Julia lines of the reference (paths are
+ * relative to the JustPIC.jl repository), keeping its operation order:
+ *   - `muladd` / `@muladd` sites become C99 fma(); every other product and sum
+ *     is rounded separately (compile with -ffp-contract=off);
+ *   - @muladd of a product of more than two factors splits it as
+ *     muladd(first factor, product of the rest, addend) (MuladdMacro 0.2);
+ *   - colour passes, slot walks, the `starting_point` carry of
+ *     move_particles! and the `break` of inject_particles! are kept;
+ *   - the in-kernel rand() calls are replaced by the shared Philox4x32-10
+ *     counter RNG of include/justpic_gb300_rng.h.
+ * Two cases where the reference is undefined get a defined result that the
+ * CUDA library shares: a particle that moved more than one cell in one step
+ * (the reference's colour passes race) is dropped and JPO_ERR_FAR_MOVE is
+ * raised; an injected particle with no live neighbour in its 3^N block (the
+ * reference reads slot 0, out of bounds) keeps its field values and raises
+ * JPO_ERR_NO_NEIGHBOUR.
+ */
+#include "jp_oracle.h"
+#include "../include/justpic_gb300_rng.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int g_threads = 0;
+
+void jpo_set_threads(int nthreads) { g_threads = nthreads; }
+
+static int nthreads(void)
+{
+#ifdef _OPENMP
+    return g_threads > 0 ? g_threads : omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+#define JPO_BISECT_CAP 256
+
+/* ---------------------------------------------------------------- helpers */
+
+static inline void cell_coords(const jpo_grid* g, int64_t c, int64_t I[3])
+{
+    I[0] = c % g->n[0];
+    I[1] = (c / g->n[0]) % g->n[1];
+    I[2] = g->ndim == 3 ? c / (g->n[0] * g->n[1]) : 0;
+}
+
+static inline int64_t cell_linear(const jpo_grid* g, const int64_t I[3])
+{
+    return I[0] + g->n[0] * (I[1] + (g->ndim == 3 ? g->n[1] * I[2] : 0));
+}
+
+/* lerp(t, v0, v1) = muladd(t, v1, muladd(-t, v0, v0)): src/Interpolations/ndlerp.jl:15 */
+static inline double lerp1(double t, double v0, double v1)
+{
+    return fma(t, v1, fma(-t, v0, v0));
+}
+
+/* recursive N-linear lerp, x first then y then z: src/Interpolations/ndlerp.jl:11-14 */
+static inline double lerpN(int n, const double* v, const double* t)
+{
+    if (n == 1) return lerp1(t[0], v[0], v[1]);
+    if (n == 2) return lerp1(t[1], lerp1(t[0], v[0], v[1]), lerp1(t[0], v[2], v[3]));
+    return lerp1(t[2],
+                 lerp1(t[1], lerp1(t[0], v[0], v[1]), lerp1(t[0], v[2], v[3])),
+                 lerp1(t[1], lerp1(t[0], v[4], v[5]), lerp1(t[0], v[6], v[7])));
+}
+
+double jpo_lerp(int n, const double* v, const double* t) { return lerpN(n, v, t); }
+
+/*
+ * find_parent_cell_bisection (src/Utils.jl:117-130), 0-based: returns s with
+ * x[s] <= px <= x[s+1], starting from `seed`, lo = 0, hi = len - 1. The
+ * reference loop is unbounded; here it stops after JPO_BISECT_CAP steps.
+ */
+int64_t jpo_bisection(double px, const double* x, int64_t len, int64_t seed, int* err)
+{
+    int64_t lo = 0, hi = len - 1, s = seed;
+    for (int it = 0; it < JPO_BISECT_CAP; ++it) {
+        if (x[s] <= px && px <= x[s + 1]) return s;
+        if (x[s] < px) {
+            lo = s;
+            s = (hi + s) / 2;
+        } else {
+            hi = s;
+            s = (lo + s) / 2;
+        }
+    }
+    *err |= JPO_ERR_BISECTION_LIMIT;
+    return s;
+}
+
+/* isincell: xv < px < xv + dx on every axis, src/Particles/utils.jl:7-15 */
+static inline int isincell(int n, const double* p, const double* corner, const double* dx)
+{
+    int in = 1;
+    for (int d = 0; d < n; ++d) in &= (corner[d] < p[d]) & (p[d] < corner[d] + dx[d]);
+    return in;
+}
+
+/* --------------------------------------------------------- init_particles */
+
+void jpo_init_particles(const jpo_grid* g, double* const coords[3], uint8_t* index)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int NQ = 1 << N;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t c = 0; c < nc; ++c) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        double x0[3], dx[3];
+        for (int d = 0; d < N; ++d) {
+            x0[d] = g->xv[d][I[d]];
+            dx[d] = g->dxv[d][I[d]];
+        }
+        for (int s = 0; s < M; ++s) {
+            for (int d = 0; d < N; ++d) coords[d][c + nc * s] = NAN;
+            index[c + nc * s] = 0;
+        }
+        /* fill_coords_index!: src/Particles/particles_utils.jl:168-194 */
+        int l = 0;
+        for (int iq = 0; iq < NQ; ++iq) {
+            double xc[3];
+            for (int d = 0; d < N; ++d) xc[d] = x0[d] + (dx[d] * (double)((iq >> d) & 1)) / 2.0;
+            for (int q = 0; q < g->np_quadrant; ++q) {
+                for (int d = 0; d < N; ++d) {
+                    double r = jp_rand_uniform(g->seed, JP_RNG_STREAM_INIT, 0u, (uint64_t)c,
+                                               (uint32_t)l, (uint32_t)d);
+                    coords[d][c + nc * l] = xc[d] + (dx[d] / 2.0) * r;
+                }
+                index[c + nc * l] = 1;
+                ++l;
+            }
+        }
+    }
+}
+
+/* -------------------------------------------------------------- advection */
+
+/*
+ * interp_velocity2particle for one component (src/Particles/Advection/advection.jl:93-148,
+ * src/Advection/advection.jl:3-47): Inf outside the component grid's limits,
+ * else bisection seeded by the cell index, corner values and N-linear lerp.
+ */
+static double interp_component(const jpo_grid* g, int comp, const double* p, const int64_t* I,
+                               const double* V, int* err)
+{
+    const int N = g->ndim;
+    for (int d = 0; d < N; ++d) {
+        const double* x = g->xvel[comp][d];
+        const int64_t L = g->nvel[comp][d];
+        if (!(x[0] <= p[d] && p[d] <= x[L - 1])) return INFINITY;
+    }
+    int64_t idx[3] = {0, 0, 0};
+    double t[3];
+    for (int d = 0; d < N; ++d) {
+        const double* x = g->xvel[comp][d];
+        idx[d] = jpo_bisection(p[d], x, g->nvel[comp][d], I[d], err);
+        const double xc = x[idx[d]];
+        const double dx = g->dxvel[comp][d][idx[d]];
+        t[d] = (p[d] - xc) * (1.0 / dx);
+    }
+    const int64_t L0 = g->nvel[comp][0], L1 = g->nvel[comp][1];
+    double v[8];
+    if (N == 2) {
+        const int64_t b = idx[0] + L0 * idx[1];
+        v[0] = V[b];
+        v[1] = V[b + 1];
+        v[2] = V[b + L0];
+        v[3] = V[b + L0 + 1];
+    } else {
+        const int64_t b = idx[0] + L0 * (idx[1] + L1 * idx[2]);
+        const int64_t sz = L0 * L1;
+        v[0] = V[b];
+        v[1] = V[b + 1];
+        v[2] = V[b + L0];
+        v[3] = V[b + L0 + 1];
+        v[4] = V[b + sz];
+        v[5] = V[b + sz + 1];
+        v[6] = V[b + sz + L0];
+        v[7] = V[b + sz + L0 + 1];
+    }
+    return lerpN(N, v, t);
+}
+
+static void interp_velocity(const jpo_grid* g, const double* p, const int64_t* I,
+                            const double* const V[3], double* v, int* err)
+{
+    for (int c = 0; c < g->ndim; ++c) v[c] = interp_component(g, c, p, I, V[c], err);
+}
+
+void jpo_first_stage(int method, double alpha, double dt, int n, const double* v,
+                     const double* p, double* out)
+{
+    /* src/Advection/Euler.jl:1-6 and src/Advection/RK2.jl:7-20:
+       muladd(sign, (alpha*dt)*v, p) with sign = 1 */
+    for (int d = 0; d < n; ++d) {
+        if (method == JPO_EULER)
+            out[d] = fma(1.0, dt * v[d], p[d]);
+        else
+            out[d] = fma(1.0, (alpha * dt) * v[d], p[d]);
+    }
+}
+
+void jpo_second_stage(double alpha, double dt, int n, const double* v0, const double* v1,
+                      const double* p, double* out)
+{
+    /* src/Advection/RK2.jl:22-44 */
+    if (alpha == 0.5) {
+        for (int d = 0; d < n; ++d) out[d] = fma(1.0, dt * v1[d], p[d]);
+    } else {
+        const double ia = 1.0 / alpha;
+        const double a = fma(-0.5, ia, 1.0);
+        const double b = 0.5 * ia;
+        for (int d = 0; d < n; ++d) {
+            const double x = fma(a, v0[d], b * v1[d]);
+            out[d] = fma(1.0, dt * x, p[d]);
+        }
+    }
+}
+
+static void advect_particle(const jpo_grid* g, int method, double alpha, const double* const V[3],
+                            double dt, const int64_t* I, const double* p0, double* pout, int* err)
+{
+    const int N = g->ndim;
+    if (method == JPO_RK2) {
+        /* src/Particles/Advection/advection.jl:154-179 */
+        double v0[3], v1[3], p1[3];
+        interp_velocity(g, p0, I, V, v0, err);
+        jpo_first_stage(JPO_RK2, alpha, dt, N, v0, p0, p1);
+        interp_velocity(g, p1, I, V, v1, err);
+        jpo_second_stage(alpha, dt, N, v0, v1, p0, pout);
+    } else if (method == JPO_RK4) {
+        /* src/Particles/Advection/advection.jl:261-279 (no muladd) */
+        double k1[3], k2[3], k3[3], k4[3], q[3];
+        interp_velocity(g, p0, I, V, k1, err);
+        for (int d = 0; d < N; ++d) q[d] = p0[d] + (dt * k1[d]) / 2.0;
+        interp_velocity(g, q, I, V, k2, err);
+        for (int d = 0; d < N; ++d) q[d] = p0[d] + (dt * k2[d]) / 2.0;
+        interp_velocity(g, q, I, V, k3, err);
+        for (int d = 0; d < N; ++d) q[d] = p0[d] + dt * k3[d];
+        interp_velocity(g, q, I, V, k4, err);
+        for (int d = 0; d < N; ++d)
+            pout[d] = p0[d] + (dt * (((k1[d] + 2.0 * k2[d]) + 2.0 * k3[d]) + k4[d])) / 6.0;
+    } else {
+        /* src/Particles/Advection/advection.jl:348-367 */
+        double v0[3];
+        interp_velocity(g, p0, I, V, v0, err);
+        jpo_first_stage(JPO_EULER, alpha, dt, N, v0, p0, pout);
+    }
+}
+
+int jpo_advection(const jpo_grid* g, int method, double alpha, const double* const V[3],
+                  double dt, double* const coords[3], const uint8_t* index)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    int err = 0;
+#pragma omp parallel for schedule(static) num_threads(nthreads()) reduction(| : err)
+    for (int64_t c = 0; c < nc; ++c) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        /* advection_kernel!: src/Particles/Advection/advection.jl:66-91 */
+        for (int s = 0; s < M; ++s) {
+            if (!index[c + nc * s]) continue;
+            double p0[3], p[3];
+            for (int d = 0; d < N; ++d) p0[d] = coords[d][c + nc * s];
+            advect_particle(g, method, alpha, V, dt, I, p0, p, &err);
+            for (int d = 0; d < N; ++d) coords[d][c + nc * s] = p[d];
+        }
+    }
+    return err;
+}
+
+/* -------------------------------------------------------- move_particles! */
+
+static void move_cell(const jpo_grid* g, const int64_t* idx, double* const coords[3],
+                      uint8_t* index, double* const* args, int nargs, const double* dom_lo,
+                      const double* dom_hi, int* err)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int64_t c = cell_linear(g, idx);
+    double corner[3], dx[3];
+    for (int d = 0; d < N; ++d) {
+        corner[d] = g->xv[d][idx[d]];
+        dx[d] = g->dxv[d][idx[d]];
+    }
+    /* move_kernel!: src/Particles/move_safe.jl:72-125 */
+    int sp = 0; /* starting_point */
+    for (int ip = 0; ip < M; ++ip) {
+        const int64_t a = c + nc * ip;
+        if (!index[a]) continue;
+        double p[3];
+        for (int d = 0; d < N; ++d) p[d] = coords[d][a];
+        if (isincell(N, p, corner, dx)) continue;
+        /* indomain: strict, src/Particles/move_safe.jl:199-206 */
+        int inside = 1;
+        for (int d = 0; d < N; ++d) inside &= (dom_lo[d] < p[d]) & (p[d] < dom_hi[d]);
+        if (!inside) {
+            index[a] = 0;
+            for (int d = 0; d < N; ++d) coords[d][a] = NAN;
+            for (int k = 0; k < nargs; ++k) args[k][a] = NAN;
+            continue;
+        }
+        int64_t T[3] = {0, 0, 0};
+        int far = 0;
+        for (int d = 0; d < N; ++d) {
+            T[d] = jpo_bisection(p[d], g->xv[d], g->n[d] + 1, idx[d], err);
+            if (T[d] - idx[d] > 1 || idx[d] - T[d] > 1) far = 1;
+        }
+        double cached[64];
+        for (int k = 0; k < nargs; ++k) cached[k] = args[k][a];
+        index[a] = 0;
+        for (int d = 0; d < N; ++d) coords[d][a] = NAN;
+        for (int k = 0; k < nargs; ++k) args[k][a] = NAN;
+        if (far) {
+            *err |= JPO_ERR_FAR_MOVE;
+            continue;
+        }
+        const int64_t t = cell_linear(g, T);
+        int free_idx = -1;
+        for (int i = sp; i < M; ++i) { /* find_free_memory: move_safe.jl:192-197 */
+            if (!index[t + nc * i]) {
+                free_idx = i;
+                break;
+            }
+        }
+        if (free_idx < 0) continue;
+        sp = free_idx;
+        const int64_t b = t + nc * free_idx;
+        index[b] = 1;
+        for (int d = 0; d < N; ++d) coords[d][b] = p[d];
+        for (int k = 0; k < nargs; ++k) args[k][b] = cached[k];
+    }
+}
+
+int jpo_move_particles(const jpo_grid* g, double* const coords[3], uint8_t* index,
+                       double* const* args, int nargs)
+{
+    const int N = g->ndim;
+    int err = 0;
+    double lo[3], hi[3];
+    int64_t ncol[3] = {1, 1, 1};
+    for (int d = 0; d < N; ++d) {
+        /* domain_limits = extrema.(grid): src/Particles/move_safe.jl:27 */
+        lo[d] = g->xv[d][0];
+        hi[d] = g->xv[d][0];
+        for (int64_t i = 0; i <= g->n[d]; ++i) {
+            const double x = g->xv[d][i];
+            if (x < lo[d]) lo[d] = x;
+            if (x > hi[d]) hi[d] = x;
+        }
+        ncol[d] = (g->n[d] + 2) / 3;
+    }
+    const int npass = N == 2 ? 9 : 27;
+    const int64_t ntot = ncol[0] * ncol[1] * ncol[2];
+    for (int pass = 0; pass < npass; ++pass) {
+        /* offsets loop: i outermost, last axis innermost (move_safe.jl:32,39) */
+        int64_t off[3];
+        if (N == 2) {
+            off[0] = pass / 3;
+            off[1] = pass % 3;
+            off[2] = 0;
+        } else {
+            off[0] = pass / 9;
+            off[1] = (pass / 3) % 3;
+            off[2] = pass % 3;
+        }
+#pragma omp parallel for schedule(static) num_threads(nthreads()) reduction(| : err)
+        for (int64_t w = 0; w < ntot; ++w) {
+            int64_t J[3] = {w % ncol[0], (w / ncol[0]) % ncol[1], w / (ncol[0] * ncol[1])};
+            int64_t idx[3] = {0, 0, 0};
+            int ok = 1;
+            for (int d = 0; d < N; ++d) {
+                idx[d] = 3 * J[d] + off[d];
+                if (idx[d] >= g->n[d]) ok = 0;
+            }
+            if (ok) move_cell(g, idx, coords, index, args, nargs, lo, hi, &err);
+        }
+    }
+    return err;
+}
+
+/* ------------------------------------------------------ inject_particles! */
+
+/* index_min_distance: src/Particles/injection.jl:330-393 */
+static int nearest_particle(const jpo_grid* g, double* const coords[3], const uint8_t* index,
+                            const double* pn, int cur_slot, const int64_t* I, int64_t* best_a)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    double dmin = INFINITY;
+    int found = 0;
+    const int kr = N == 3 ? 1 : 0;
+    for (int64_t k = I[2] - kr; k <= I[2] + kr; ++k) {
+        for (int64_t j = I[1] - 1; j <= I[1] + 1; ++j) {
+            for (int64_t i = I[0] - 1; i <= I[0] + 1; ++i) {
+                if (i < 0 || j < 0 || k < 0) continue;
+                if (i >= g->n[0] || j >= g->n[1] || (N == 3 && k >= g->n[2])) continue;
+                const int64_t J[3] = {i, j, k};
+                const int64_t c = cell_linear(g, J);
+                const int self = (i == I[0] && j == I[1] && k == I[2]);
+                for (int ip = 0; ip < M; ++ip) {
+                    if (self && ip == cur_slot) continue;
+                    const int64_t a = c + nc * ip;
+                    if (!index[a]) continue;
+                    double s;
+                    if (N == 2) {
+                        const double px = coords[0][a], py = coords[1][a];
+                        if (isnan(px) || isnan(py)) continue;
+                        const double dxx = px - pn[0], dyy = py - pn[1];
+                        s = dxx * dxx + dyy * dyy;
+                    } else {
+                        const double dxx = coords[0][a] - pn[0];
+                        const double dyy = coords[1][a] - pn[1];
+                        const double dzz = coords[2][a] - pn[2];
+                        s = (dxx * dxx + dyy * dyy) + dzz * dzz;
+                    }
+                    const double dist = sqrt(s);
+                    if (dist < dmin) {
+                        dmin = dist;
+                        *best_a = a;
+                        found = 1;
+                    }
+                }
+            }
+        }
+    }
+    return found;
+}
+
+static void inject_cell(const jpo_grid* g, const int64_t* idx, double* const coords[3],
+                        uint8_t* index, double* const* args, int nargs, uint32_t call, int* err)
+{
+    /* _inject_particles!: src/Particles/injection.jl:68-131 */
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int NQ = 1 << N;
+    const int64_t c = cell_linear(g, idx);
+    double corner[3], dq[3];
+    for (int d = 0; d < N; ++d) {
+        corner[d] = g->xv[d][idx[d]];
+        dq[d] = g->dxv[d][idx[d]] / 2.0;
+    }
+    const int min_xq = (g->min_xcell + NQ - 1) / NQ; /* cld(min_xcell, 2^N) */
+    for (int q = 0; q < NQ; ++q) {
+        double qc[3];
+        for (int d = 0; d < N; ++d) qc[d] = corner[d] + dq[d] * (double)((q >> d) & 1);
+        int count = 0;
+        for (int i = 0; i < M; ++i) {
+            const int64_t a = c + nc * i;
+            if (!index[a]) continue;
+            double p[3];
+            for (int d = 0; d < N; ++d) p[d] = coords[d][a];
+            if (isincell(N, p, qc, dq)) ++count;
+        }
+        if (count >= min_xq) break;
+        for (int i = 0; i < M; ++i) {
+            const int64_t a = c + nc * i;
+            if (index[a]) continue;
+            ++count;
+            double pn[3];
+            for (int d = 0; d < N; ++d) {
+                /* new_particle: src/Particles/injection.jl:411-417 */
+                const double r = jp_rand_uniform(g->seed, JP_RNG_STREAM_INJECT, call,
+                                                 (uint64_t)c, (uint32_t)i, (uint32_t)d);
+                pn[d] = qc[d] + dq[d] * fma(0.95, r, 0.05);
+            }
+            for (int d = 0; d < N; ++d) coords[d][a] = pn[d];
+            index[a] = 1;
+            int64_t src = 0;
+            if (nearest_particle(g, coords, index, pn, i, idx, &src)) {
+                for (int k = 0; k < nargs; ++k) args[k][a] = args[k][src];
+            } else if (nargs > 0) {
+                *err |= JPO_ERR_NO_NEIGHBOUR;
+            }
+            if (count >= min_xq) break;
+        }
+    }
+}
+
+int jpo_inject_particles(const jpo_grid* g, double* const coords[3], uint8_t* index,
+                         double* const* args, int nargs, uint32_t call)
+{
+    const int N = g->ndim;
+    int err = 0;
+    int64_t ncol[3] = {1, 1, 1};
+    for (int d = 0; d < N; ++d) ncol[d] = (g->n[d] + 1) / 2; /* ceil(n*0.5) */
+    const int npass = 1 << N;
+    const int64_t ntot = ncol[0] * ncol[1] * ncol[2];
+    for (int pass = 0; pass < npass; ++pass) {
+        /* offsets loop: i outermost, last axis innermost (injection.jl:31,38) */
+        int64_t off[3];
+        if (N == 2) {
+            off[0] = pass / 2;
+            off[1] = pass % 2;
+            off[2] = 0;
+        } else {
+            off[0] = pass / 4;
+            off[1] = (pass / 2) % 2;
+            off[2] = pass % 2;
+        }
+#pragma omp parallel for schedule(static) num_threads(nthreads()) reduction(| : err)
+        for (int64_t w = 0; w < ntot; ++w) {
+            int64_t J[3] = {w % ncol[0], (w / ncol[0]) % ncol[1], w / (ncol[0] * ncol[1])};
+            int64_t idx[3] = {0, 0, 0};
+            int ok = 1;
+            for (int d = 0; d < N; ++d) {
+                idx[d] = 2 * J[d] + off[d];
+                if (idx[d] >= g->n[d]) ok = 0;
+            }
+            if (ok) inject_cell(g, idx, coords, index, args, nargs, call, &err);
+        }
+    }
+    return err;
+}
+
+/* ---------------------------------------------------------- grid2particle! */
+
+void jpo_grid2particle(const jpo_grid* g, double* Fp, const double* F,
+                       const double* const coords[3], const uint8_t* index)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int64_t V0 = g->n[0] + 1, V1 = g->n[1] + 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t c = 0; c < nc; ++c) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        /* _grid2particle_classic!: src/Interpolations/grid_to_particle.jl:64-82 */
+        double x0[3], dx[3], v[8];
+        for (int d = 0; d < N; ++d) {
+            x0[d] = g->xv[d][I[d]];
+            dx[d] = g->dxv[d][I[d]];
+        }
+        const int64_t b = I[0] + V0 * (I[1] + (N == 3 ? V1 * I[2] : 0));
+        v[0] = F[b];
+        v[1] = F[b + 1];
+        v[2] = F[b + V0];
+        v[3] = F[b + V0 + 1];
+        if (N == 3) {
+            const int64_t sz = V0 * V1;
+            v[4] = F[b + sz];
+            v[5] = F[b + sz + 1];
+            v[6] = F[b + sz + V0];
+            v[7] = F[b + sz + V0 + 1];
+        }
+        for (int s = 0; s < M; ++s) {
+            const int64_t a = c + nc * s;
+            if (!index[a]) continue;
+            double t[3];
+            for (int d = 0; d < N; ++d) t[d] = (coords[d][a] - x0[d]) * (1.0 / dx[d]);
+            Fp[a] = lerpN(N, v, t);
+        }
+    }
+}
+
+/* ---------------------------------------------------------- particle2grid! */
+
+void jpo_particle2grid(const jpo_grid* g, double* F, const double* Fp,
+                       const double* const coords[3], const uint8_t* index)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int64_t V0 = g->n[0] + 1, V1 = g->n[1] + 1, V2 = N == 3 ? g->n[2] + 1 : 1;
+    const int64_t nv = V0 * V1 * V2;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t v = 0; v < nv; ++v) {
+        const int64_t i = v % V0, j = (v / V0) % V1, k = v / (V0 * V1);
+        const double xq = g->xv[0][i], yq = g->xv[1][j], zq = N == 3 ? g->xv[2][k] : 0.0;
+        double w = 0.0, wF = 0.0;
+        /* src/Interpolations/particle_to_grid.jl:37-68 (2D), :113-151 (3D) */
+        const int kmin = N == 3 ? -1 : 0;
+        for (int ko = kmin; ko <= 0; ++ko) {
+            const int64_t kc = k + ko;
+            if (N == 3 && !(0 <= kc && kc < g->n[2])) continue;
+            for (int jo = -1; jo <= 0; ++jo) {
+                const int64_t jc = j + jo;
+                if (!(0 <= jc && jc < g->n[1])) continue;
+                for (int io = -1; io <= 0; ++io) {
+                    const int64_t ic = i + io;
+                    if (!(0 <= ic && ic < g->n[0])) continue;
+                    const int64_t c = ic + g->n[0] * (jc + g->n[1] * (N == 3 ? kc : 0));
+                    for (int s = 0; s < M; ++s) {
+                        const int64_t a = c + nc * s;
+                        if (!index[a]) continue;
+                        double ss;
+                        const double ddx = xq - coords[0][a];
+                        const double ddy = yq - coords[1][a];
+                        if (N == 2) {
+                            ss = ddx * ddx + ddy * ddy;
+                        } else {
+                            const double ddz = zq - coords[2][a];
+                            ss = (ddx * ddx + ddy * ddy) + ddz * ddz;
+                        }
+                        const double dist = sqrt(ss);
+                        const double wi = 1.0 / (dist * dist);
+                        w += wi;
+                        wF = fma(wi, Fp[a], wF);
+                    }
+                }
+            }
+        }
+        F[v] = N == 2 ? wF / w : wF * (1.0 / w);
+    }
+}
+
+double jpo_rand(uint64_t seed, uint32_t stream, uint32_t call, uint64_t cell, uint32_t slot,
+                uint32_t dim)
+{
+    return jp_rand_uniform(seed, stream, call, cell, slot, dim);
+}
+
+void jpo_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    jp_philox4x32_10(ctr, key, out);
+}

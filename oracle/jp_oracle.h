@@ -1,0 +1,91 @@
+/*
+ * jp_oracle.h -- CPU restatement of JustPIC.jl's particle-in-cell hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This is the correctness oracle that the CUDA
+ * library is checked against (and the timed CPU baseline of bench.py). No
+ * product code path links, loads or calls it.
+ *
+ * Data layout is the reference's GPU CellArray layout (blocklength 0,
+ * ext/JustPICCUDAExt.jl:29): a per-slot quantity q of slot s (0-based) in cell c
+ * (0-based, column-major, x fastest) lives at q[c + ncells * s]. Grid fields
+ * (velocity components, vertex fields) are column-major with x fastest.
+ *
+ * Parity status: pinned against the reference's own known-answer tests
+ * (test/test_integrators.jl, test/test_interpolation_kernels.jl,
+ * test/test_2D.jl) that need no Julia; the reference itself (Julia) cannot run
+ * in this container, so the slot-level semantics follow the cited source lines.
+ */
+#ifndef JP_ORACLE_H
+#define JP_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct jpo_grid {
+    int32_t ndim;            /* 2 or 3 */
+    int64_t n[3];            /* cells per dimension */
+    int64_t ncells;
+    int32_t nxcell;          /* already rounded to a multiple of 2^ndim */
+    int32_t max_xcell;
+    int32_t min_xcell;
+    int32_t np_quadrant;
+    uint64_t seed;
+    const double* xv[3];     /* vertex coordinates, length n[d] + 1 */
+    const double* dxv[3];    /* vertex spacing per cell, length n[d] */
+    const double* xvel[3][3];  /* velocity grid of component c along dim d */
+    const double* dxvel[3][3]; /* its spacing per interval, length nvel - 1 */
+    int64_t nvel[3][3];
+} jpo_grid;
+
+/* error bits returned by the mutating calls (0 = clean) */
+#define JPO_ERR_BISECTION_LIMIT 0x1
+#define JPO_ERR_FAR_MOVE 0x2
+#define JPO_ERR_NO_NEIGHBOUR 0x4
+
+#define JPO_EULER 0
+#define JPO_RK2 1
+#define JPO_RK4 2
+
+void jpo_set_threads(int nthreads);
+
+/* particle seeding: src/Particles/particles_utils.jl:168-194 */
+void jpo_init_particles(const jpo_grid* g, double* const coords[3], uint8_t* index);
+
+/* advection!: src/Particles/Advection/advection.jl:35-91 */
+int jpo_advection(const jpo_grid* g, int method, double alpha, const double* const V[3],
+                  double dt, double* const coords[3], const uint8_t* index);
+
+/* move_particles!: src/Particles/move_safe.jl:21-125 */
+int jpo_move_particles(const jpo_grid* g, double* const coords[3], uint8_t* index,
+                       double* const* args, int nargs);
+
+/* inject_particles!: src/Particles/injection.jl:19-131 */
+int jpo_inject_particles(const jpo_grid* g, double* const coords[3], uint8_t* index,
+                         double* const* args, int nargs, uint32_t call);
+
+/* grid2particle!: src/Interpolations/grid_to_particle.jl:26-82 */
+void jpo_grid2particle(const jpo_grid* g, double* Fp, const double* F,
+                       const double* const coords[3], const uint8_t* index);
+
+/* particle2grid!: src/Interpolations/particle_to_grid.jl:23-151 */
+void jpo_particle2grid(const jpo_grid* g, double* F, const double* Fp,
+                       const double* const coords[3], const uint8_t* index);
+
+/* known-answer helpers (test/test_integrators.jl, test_interpolation_kernels.jl) */
+void jpo_first_stage(int method, double alpha, double dt, int n, const double* v,
+                     const double* p, double* out);
+void jpo_second_stage(double alpha, double dt, int n, const double* v0, const double* v1,
+                      const double* p, double* out);
+double jpo_lerp(int n, const double* v, const double* t);
+int64_t jpo_bisection(double px, const double* x, int64_t len, int64_t seed, int* err);
+void jpo_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+double jpo_rand(uint64_t seed, uint32_t stream, uint32_t call, uint64_t cell, uint32_t slot,
+                uint32_t dim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

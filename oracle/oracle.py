@@ -1,0 +1,240 @@
+"""ctypes front end of the CPU oracle (jp_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` leg of bench.py to check (or time beside) the CUDA library. The
+product package never imports it.
+
+Arrays use the layouts of the reference's GPU path:
+  * per-slot arrays: numpy ``(max_xcell, ncells)`` C-order, i.e. element
+    ``[s, c]`` at ``c + ncells * s`` (CellArray blocklength 0,
+    ext/JustPICCUDAExt.jl:29), cell index column-major (x fastest);
+  * grid fields: numpy arrays in Fortran order with the Julia shape, e.g. a
+    vertex field of an nx x ny grid has shape ``(nx + 1, ny + 1)``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libjp_oracle.so")
+
+EULER, RK2, RK4 = 0, 1, 2
+ERR_BISECTION_LIMIT, ERR_FAR_MOVE, ERR_NO_NEIGHBOUR = 0x1, 0x2, 0x4
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class _Grid(ctypes.Structure):
+    _fields_ = [
+        ("ndim", ctypes.c_int32),
+        ("n", ctypes.c_int64 * 3),
+        ("ncells", ctypes.c_int64),
+        ("nxcell", ctypes.c_int32),
+        ("max_xcell", ctypes.c_int32),
+        ("min_xcell", ctypes.c_int32),
+        ("np_quadrant", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+        ("xv", _dp * 3),
+        ("dxv", _dp * 3),
+        ("xvel", (_dp * 3) * 3),
+        ("dxvel", (_dp * 3) * 3),
+        ("nvel", (ctypes.c_int64 * 3) * 3),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library with its Makefile (gcc, OpenMP)."""
+    src = os.path.join(_HERE, "jp_oracle.c")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE, "-B" if force else "all"], check=True)
+    return _LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        G = ctypes.POINTER(_Grid)
+        P3 = ctypes.c_void_p * 3
+        L.jpo_set_threads.argtypes = [ctypes.c_int]
+        L.jpo_init_particles.argtypes = [G, P3, ctypes.c_void_p]
+        L.jpo_advection.argtypes = [G, ctypes.c_int, ctypes.c_double, P3, ctypes.c_double, P3, ctypes.c_void_p]
+        L.jpo_advection.restype = ctypes.c_int
+        L.jpo_move_particles.argtypes = [G, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.jpo_move_particles.restype = ctypes.c_int
+        L.jpo_inject_particles.argtypes = [G, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32]
+        L.jpo_inject_particles.restype = ctypes.c_int
+        L.jpo_grid2particle.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]
+        L.jpo_particle2grid.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]
+        L.jpo_first_stage.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                      _dp, _dp, _dp]
+        L.jpo_second_stage.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp, _dp]
+        L.jpo_lerp.argtypes = [ctypes.c_int, _dp, _dp]
+        L.jpo_lerp.restype = ctypes.c_double
+        L.jpo_bisection.argtypes = [ctypes.c_double, _dp, ctypes.c_int64, ctypes.c_int64,
+                                    ctypes.POINTER(ctypes.c_int)]
+        L.jpo_bisection.restype = ctypes.c_int64
+        L.jpo_rand.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                               ctypes.c_uint32, ctypes.c_uint32]
+        L.jpo_rand.restype = ctypes.c_double
+        L.jpo_philox.argtypes = [ctypes.c_uint32 * 4, ctypes.c_uint32 * 2, ctypes.c_uint32 * 4]
+        _lib = L
+    return _lib
+
+
+def set_threads(n: int) -> None:
+    lib().jpo_set_threads(int(n))
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def _spacing(x: np.ndarray, uniform: bool) -> np.ndarray:
+    """di of init_particles: scalar x[2]-x[1] for ranges (particles_utils.jl:137-139),
+    diff(x) for vector grids (particles_utils.jl:76-79), stored per interval."""
+    if uniform:
+        return np.full(len(x) - 1, x[1] - x[0], dtype=np.float64)
+    return np.ascontiguousarray(np.diff(x), dtype=np.float64)
+
+
+class OracleParticles:
+    """The geometry part of a ``Particles`` container (particles.jl:17-46) plus the
+    per-slot arrays, all on the host."""
+
+    def __init__(self, xi_vel, nxcell, max_xcell, min_xcell, uniform=True, seed=0x4A50):
+        ndim = len(xi_vel)
+        assert ndim in (2, 3)
+        self.ndim = ndim
+        self.xi_vel = tuple(tuple(np.ascontiguousarray(a, dtype=np.float64) for a in comp) for comp in xi_vel)
+        self.xvi = tuple(self.xi_vel[d][d] for d in range(ndim))
+        self.n = tuple(len(x) - 1 for x in self.xvi)
+        self.ncells = int(np.prod(self.n))
+        nq = 2 ** ndim
+        self.np_quadrant = -(-int(nxcell) // nq)
+        self.nxcell = self.np_quadrant * nq
+        self.max_xcell = max(self.nxcell, int(max_xcell))
+        self.min_xcell = int(min_xcell)
+        self.seed = int(seed)
+        self.uniform = bool(uniform)
+        self.dxv = tuple(_spacing(x, uniform) for x in self.xvi)
+        self.dxvel = tuple(tuple(_spacing(x, uniform) for x in comp) for comp in self.xi_vel)
+        g = _Grid()
+        g.ndim = ndim
+        for d in range(3):
+            g.n[d] = self.n[d] if d < ndim else 1
+        g.ncells = self.ncells
+        g.nxcell, g.max_xcell, g.min_xcell = self.nxcell, self.max_xcell, self.min_xcell
+        g.np_quadrant = self.np_quadrant
+        g.seed = self.seed
+        for d in range(ndim):
+            g.xv[d] = _dptr(self.xvi[d])
+            g.dxv[d] = _dptr(self.dxv[d])
+            for c in range(ndim):
+                g.xvel[c][d] = _dptr(self.xi_vel[c][d])
+                g.dxvel[c][d] = _dptr(self.dxvel[c][d])
+                g.nvel[c][d] = len(self.xi_vel[c][d])
+        self._g = g
+        shape = (self.max_xcell, self.ncells)
+        self.coords = tuple(np.full(shape, np.nan) for _ in range(ndim))
+        self.index = np.zeros(shape, dtype=np.uint8)
+        self.inject_calls = 0
+
+    # -- helpers ---------------------------------------------------------
+    def _p3(self, arrs):
+        P3 = ctypes.c_void_p * 3
+        v = [None, None, None]
+        for i, a in enumerate(arrs):
+            assert a.flags.c_contiguous or a.flags.f_contiguous
+            v[i] = a.ctypes.data
+        return P3(*v)
+
+    def _args(self, args):
+        args = tuple(args)
+        arr = (ctypes.c_void_p * max(1, len(args)))(*[a.ctypes.data for a in args])
+        return arr, len(args)
+
+    def cell_array(self, fill=0.0):
+        return np.full((self.max_xcell, self.ncells), fill, dtype=np.float64)
+
+    # -- the hot path ----------------------------------------------------
+    def init_particles(self):
+        lib().jpo_init_particles(ctypes.byref(self._g), self._p3(self.coords), _ptr(self.index))
+
+    def advection(self, method, alpha, V, dt):
+        V = [np.asfortranarray(v, dtype=np.float64) for v in V]
+        self._keep = V
+        return lib().jpo_advection(ctypes.byref(self._g), int(method), float(alpha), self._p3(V), float(dt),
+                                   self._p3(self.coords), _ptr(self.index))
+
+    def move_particles(self, args=()):
+        a, n = self._args(args)
+        return lib().jpo_move_particles(ctypes.byref(self._g), self._p3(self.coords), _ptr(self.index), a, n)
+
+    def inject_particles(self, args=()):
+        a, n = self._args(args)
+        err = lib().jpo_inject_particles(ctypes.byref(self._g), self._p3(self.coords), _ptr(self.index), a, n,
+                                         self.inject_calls)
+        self.inject_calls += 1
+        return err
+
+    def grid2particle(self, Fp, F):
+        F = np.asfortranarray(F, dtype=np.float64)
+        lib().jpo_grid2particle(ctypes.byref(self._g), _ptr(Fp), _ptr(F), self._p3(self.coords), _ptr(self.index))
+
+    def particle2grid(self, F, Fp):
+        assert F.flags.f_contiguous and F.dtype == np.float64
+        lib().jpo_particle2grid(ctypes.byref(self._g), _ptr(F), _ptr(Fp), self._p3(self.coords), _ptr(self.index))
+
+
+# -- known-answer helpers (test/test_integrators.jl, test_interpolation_kernels.jl)
+def first_stage(method, alpha, dt, v, p):
+    v = np.asarray(v, dtype=np.float64)
+    p = np.asarray(p, dtype=np.float64)
+    out = np.empty_like(p)
+    lib().jpo_first_stage(method, alpha, dt, len(p), _dptr(v), _dptr(p), _dptr(out))
+    return tuple(out)
+
+
+def second_stage(alpha, dt, v0, v1, p):
+    v0, v1, p = (np.asarray(a, dtype=np.float64) for a in (v0, v1, p))
+    out = np.empty_like(p)
+    lib().jpo_second_stage(alpha, dt, len(p), _dptr(v0), _dptr(v1), _dptr(p), _dptr(out))
+    return tuple(out)
+
+
+def lerp(v, t):
+    v = np.asarray(v, dtype=np.float64)
+    t = np.asarray(t, dtype=np.float64)
+    return lib().jpo_lerp(len(t), _dptr(v), _dptr(t))
+
+
+def bisection(px, x, seed):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    err = ctypes.c_int(0)
+    r = lib().jpo_bisection(float(px), _dptr(x), len(x), int(seed), ctypes.byref(err))
+    return r, err.value
+
+
+def rand(seed, stream, call, cell, slot, dim):
+    return lib().jpo_rand(seed, stream, call, cell, slot, dim)
+
+
+def philox4x32_10(ctr, key):
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    lib().jpo_philox(c, k, o)
+    return tuple(o)

@@ -1,0 +1,190 @@
+"""The CPU oracle against the reference's own known-answer and tolerance tests
+(test/test_integrators.jl, test/test_interpolation_kernels.jl, test/test_2D.jl,
+test/test_3D.jl). These pin the restatement without running Julia."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from justpic_gb300 import workloads as W
+import justpic_gb300 as jp
+
+
+# --- test/test_integrators.jl ------------------------------------------------
+def test_rk2_first_stage_exact_2d():
+    assert O.first_stage(O.RK2, 0.5, 0.1, (3.0, 4.0), (1.0, 2.0)) == (1.15, 2.2)  # :17-18
+
+
+def test_rk2_second_stage_2d():
+    p1 = O.first_stage(O.RK2, 0.5, 0.1, (3.0, 4.0), (1.0, 2.0))
+    np.testing.assert_allclose(O.second_stage(0.5, 0.1, (3.0, 4.0), (3.1, 4.1), p1), (1.46, 2.61))  # :19
+    p1 = O.first_stage(O.RK2, 2 / 3, 0.1, (3.0, 4.0), (1.0, 2.0))
+    np.testing.assert_allclose(p1, (1.2, 2.266666666))  # :23
+    np.testing.assert_allclose(O.second_stage(2 / 3, 0.1, (3.0, 4.0), (3.1, 4.1), p1), (1.5075, 2.67416666))  # :24
+
+
+def test_euler_first_stage_exact():
+    assert O.first_stage(O.EULER, 0.5, 0.1, (3.0, 4.0), (1.0, 2.0)) == (1.3, 2.4)  # :39
+    assert O.first_stage(O.EULER, 0.5, 0.1, (3.0, 4.0, 5.0), (1.0, 2.0, 3.0)) == (1.3, 2.4, 3.5)  # :78
+
+
+def test_rk2_3d():
+    p1 = O.first_stage(O.RK2, 0.5, 0.1, (3.0, 4.0, 5.0), (1.0, 2.0, 3.0))
+    assert p1 == (1.15, 2.2, 3.25)  # :57
+    np.testing.assert_allclose(O.second_stage(0.5, 0.1, (3.0, 4.0, 5.0), (3.1, 4.1, 5.1), p1), (1.46, 2.61, 3.76))
+    p1 = O.first_stage(O.RK2, 2 / 3, 0.1, (3.0, 4.0, 5.0), (1.0, 2.0, 3.0))
+    np.testing.assert_allclose(p1, (1.2, 2.266666666, 3.3333333333333335))  # :62
+    np.testing.assert_allclose(O.second_stage(2 / 3, 0.1, (3.0, 4.0, 5.0), (3.1, 4.1, 5.1), p1),
+                               (1.5075, 2.67416666, 3.8408333333333333))  # :63
+
+
+def test_integrator_argument_errors():
+    with pytest.raises(jp.ArgumentError):
+        jp.RungeKutta2(1.1)
+    with pytest.raises(jp.ArgumentError):
+        jp.RungeKutta2(-0.1)
+    assert jp.RungeKutta2().alpha == 0.5 and jp.RungeKutta2(2 / 3).alpha == 2 / 3
+    assert isinstance(jp.Euler("potato"), jp.Euler)
+
+
+# --- test/test_interpolation_kernels.jl:47-60 ----------------------------------
+def test_lerp_exact():
+    assert O.lerp((1.0, 2.0), (0.5,)) == 1.5
+    assert O.lerp((1.0, 2.0, 1.0, 2.0), (0.5, 0.5)) == 1.5
+    assert O.lerp((1.0, 2.0, 1.0, 2.0, 1.0, 2.0, 1.0, 2.0), (0.5, 0.5, 0.5)) == 1.5
+
+
+# --- src/Utils.jl:108-130 bisection semantics -----------------------------------
+def test_bisection_closed_interval_and_ties():
+    x = np.linspace(0.0, 1.0, 11)
+    rng = np.random.default_rng(1)
+    for seed in range(10):
+        for px in rng.uniform(0, 1, 50):
+            s, err = O.bisection(px, x, seed)
+            assert err == 0 and x[s] <= px <= x[s + 1]
+    # a point on a node: the seed's own interval wins when it holds it
+    assert O.bisection(x[4], x, 4)[0] == 4
+    assert O.bisection(x[4], x, 3)[0] == 3
+
+
+def test_bisection_is_bounded():
+    x = np.linspace(0.0, 1.0, 11)
+    s, err = O.bisection(float("nan"), x, 3)
+    assert err == O.ERR_BISECTION_LIMIT
+
+
+# --- counter RNG (Philox4x32-10, published known answers) ---------------------
+@pytest.mark.parametrize("ctr,key,out", [
+    ((0, 0, 0, 0), (0, 0), (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+    ((0xffffffff,) * 4, (0xffffffff,) * 2, (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+    ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+     (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1)),
+])
+def test_philox_known_answers(ctr, key, out):
+    # known-answer vectors of the Philox4x32-10 publication (Random123 distribution)
+    assert O.philox4x32_10(ctr, key) == out
+
+
+def test_rng_uniform_range_and_determinism():
+    vals = [O.rand(7, 1, 2, c, s, d) for c in range(5) for s in range(3) for d in range(2)]
+    assert all(0.0 <= v < 1.0 for v in vals)
+    assert vals == [O.rand(7, 1, 2, c, s, d) for c in range(5) for s in range(3) for d in range(2)]
+    assert len(set(vals)) == len(vals)
+
+
+# --- interpolation tests (test_interpolation_kernels.jl:62-116, :118-180) ------
+def _oracle_particles(g, nxcell, max_xcell, min_xcell, seed=0x4A50):
+    grids = tuple(tuple(np.asarray(x) for x in comp) for comp in g["grid_v"])
+    P = O.OracleParticles(grids, nxcell, max_xcell, min_xcell, uniform=True, seed=seed)
+    P.init_particles()
+    return P
+
+
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_g2p_linear_field_and_p2g_error(ndim):
+    g = W.grid((4,) * ndim)
+    P = _oracle_particles(g, 5 if ndim == 2 else 12, 5 if ndim == 2 else 12, 1)
+    axis = ndim - 1
+    T = W.linear_T(g, axis)
+    pT = P.cell_array()
+    P.grid2particle(pT, T)
+    live = P.index.astype(bool)
+    np.testing.assert_allclose(pT[live], P.coords[axis][live], rtol=1e-12)  # pT ≈ coords
+    T2 = np.asfortranarray(np.zeros_like(T))
+    P.particle2grid(T2, pT)
+    assert np.linalg.norm(T2 - T) / T.size < 0.1
+
+
+def test_init_particles_layout():
+    g = W.grid((6, 5))
+    P = _oracle_particles(g, 24, 48, 12)
+    assert P.nxcell == 24 and P.max_xcell == 48 and P.np_quadrant == 6
+    assert P.index[:24].all() and not P.index[24:].any()
+    # quadrant-stratified: slot l of quadrant q lies in that quadrant
+    xv, yv = (np.asarray(a) for a in g["xv"])
+    for c in range(P.ncells):
+        i, j = c % 6, c // 6
+        for l in range(24):
+            q = l // 6
+            x, y = P.coords[0][l, c], P.coords[1][l, c]
+            hx, hy = (xv[i + 1] - xv[i]) / 2, (yv[j + 1] - yv[j]) / 2
+            x0, y0 = xv[i] + hx * (q & 1), yv[j] + hy * (q >> 1)
+            assert x0 <= x <= x0 + hx and y0 <= y <= y0 + hy
+    # nxcell is rounded up to a multiple of 2^N and max_xcell follows
+    P2 = _oracle_particles(g, 25, 20, 10)
+    assert P2.nxcell == 28 and P2.max_xcell == 28
+
+
+# --- miniapps with their tolerances (test/test_2D.jl:482-653) -----------------
+def _miniapp(g, V, T, dt, nsteps, alpha, nxcell=25, max_xcell=50, min_xcell=10, uniform=True):
+    grids = tuple(tuple(np.asarray(x) for x in comp) for comp in g["grid_v"])
+    P = O.OracleParticles(grids, nxcell, max_xcell, min_xcell, uniform=uniform)
+    P.init_particles()
+    pT = P.cell_array()
+    T = np.asfortranarray(T.copy())
+    P.grid2particle(pT, T)
+    sumT = T.sum()
+    for _ in range(nsteps):
+        P.particle2grid(T, pT)
+        P.advection(O.RK2, alpha, V, dt)
+        P.move_particles((pT,))
+        P.inject_particles((pT,))
+        P.grid2particle(pT, T)
+    return abs(sumT - T.sum()) / sumT
+
+
+def test_advection_2d_miniapp():
+    g = W.grid((64, 64))
+    V = W.stream_velocity(g)
+    err = _miniapp(g, V, W.linear_T(g, 1), W.cfl_dt(g, V, 0.5), 25, 2 / 3)
+    assert err < 1e-2  # test_2D.jl:540-545
+
+
+def test_advection_2d_refined_miniapp():
+    from _harness import refined_grid
+    xv = np.array([0.0, 0.05, 0.12, 0.21, 0.32, 0.45, 0.6, 0.77, 0.91, 1.0])
+    yv = np.array([0.0, 0.04, 0.1, 0.18, 0.29, 0.43, 0.58, 0.74, 0.89, 1.0])
+    from _harness import expand_vector
+    xc, yc = 0.5 * (xv[1:] + xv[:-1]), 0.5 * (yv[1:] + yv[:-1])
+    g = {"ndim": 2, "ni": (9, 9), "xv": (xv, yv), "grid_v": ((xv, expand_vector(yc)), (expand_vector(xc), yv)),
+         "dx": (np.min(np.diff(xv)), np.min(np.diff(yv)))}
+    V = W.stream_velocity(g)
+    T = W.on_grid(lambda x, y: y + 0 * x, (xv, yv))
+    err = _miniapp(g, V, T, W.cfl_dt(g, V, 0.5), 25, 2 / 3, uniform=False)
+    assert err < 1e-1  # test_2D.jl:592-597
+    assert refined_grid  # imported helper used by the GPU tests too
+
+
+def test_rotating_circle_miniapp():
+    # test_2D.jl:599-653 (rotation of a disc; 100 steps of dt = 200)
+    n = 256
+    g = W.grid((n - 1, n - 1))
+    vi = lambda x: np.pi * 1e-5 * (x - 0.5)  # noqa: E731
+    Vx = W.on_grid(lambda x, y: -vi(y) + 0 * x, g["grid_v"][0])
+    Vy = W.on_grid(lambda x, y: vi(x) + 0 * y, g["grid_v"][1])
+    dx = g["dx"][0]
+    R = 6 * dx
+    T = W.on_grid(lambda x, y: (((x - 0.25) ** 2 + (y - 0.25) ** 2) <= R ** 2) * 1.0, g["xv"])
+    tmax = 1 / (np.pi * 1e-5 / (2 * np.pi)) / 10
+    nsteps = int(tmax // 200) + 1
+    err = _miniapp(g, (Vx, Vy), T, 200.0, nsteps, 0.5)
+    assert err < 1e-1
