@@ -153,7 +153,7 @@ def run_ours(args):
         torch.cuda.set_device(0)
     jp._native.load()
 
-    cfg = W.setup(WORKLOAD)
+    cfg = W.setup(WORKLOAD, args.ni and (args.ni, args.ni))
     g = cfg["grid"]
     Vx, Vy = cfg["V"]
     dt = cfg["dt"]
@@ -411,6 +411,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ni", type=int, default=None,
+                    help="cells per axis instead of 1024 (small cases for ncu captures; not a bench line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

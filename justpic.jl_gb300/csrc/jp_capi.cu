@@ -90,24 +90,29 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
         g.n[d] = grid->n_vel[d][d] - 1;
         g.ncells *= g.n[d];
     }
-    // host staging of every grid vector: xv, dxv, xvel, dxvel
+    // host staging of every grid vector: coordinates, spacings (the
+    // reference's di) and their inverses (its _di = inv.(di), computed once
+    // here with the same IEEE division the kernels would use)
     std::vector<double> host;
-    size_t off_xv[3], off_dxv[3], off_xvel[3][3], off_dxvel[3][3];
+    size_t off_xv[3], off_dxv[3], off_ixv[3], off_xvel[3][3], off_dxvel[3][3], off_ixvel[3][3];
     auto push = [&](const double* x, int64_t n) {
         size_t o = host.size();
         host.insert(host.end(), x, x + n);
         return o;
     };
-    auto push_spacing = [&](const double* x, int64_t n) {
+    auto push_spacing = [&](const double* x, int64_t n, bool inverse) {
         size_t o = host.size();
-        for (int64_t i = 0; i + 1 < n; ++i)
-            host.push_back(grid->uniform ? x[1] - x[0] : x[i + 1] - x[i]);
+        for (int64_t i = 0; i + 1 < n; ++i) {
+            const double dx = grid->uniform ? x[1] - x[0] : x[i + 1] - x[i];
+            host.push_back(inverse ? 1.0 / dx : dx);
+        }
         return o;
     };
     for (int d = 0; d < N; ++d) {
         const double* x = grid->xi_vel[d][d];
         off_xv[d] = push(x, g.n[d] + 1);
-        off_dxv[d] = push_spacing(x, g.n[d] + 1);
+        off_dxv[d] = push_spacing(x, g.n[d] + 1, false);
+        off_ixv[d] = push_spacing(x, g.n[d] + 1, true);
         double lo = x[0], hi = x[0];
         for (int64_t i = 0; i <= g.n[d]; ++i) {
             lo = x[i] < lo ? x[i] : lo;
@@ -121,7 +126,8 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
             const double* x = grid->xi_vel[c][d];
             const int64_t n = grid->n_vel[c][d];
             off_xvel[c][d] = push(x, n);
-            off_dxvel[c][d] = push_spacing(x, n);
+            off_dxvel[c][d] = push_spacing(x, n, false);
+            off_ixvel[c][d] = push_spacing(x, n, true);
             g.nvel[c][d] = n;
             g.lim_lo[c][d] = x[0];  // inner_limits: first/last (src/Advection/advection.jl:73-81)
             g.lim_hi[c][d] = x[n - 1];
@@ -140,9 +146,11 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
     for (int d = 0; d < N; ++d) {
         g.xv[d] = P->dev_block + off_xv[d];
         g.dxv[d] = P->dev_block + off_dxv[d];
+        g.ixv[d] = P->dev_block + off_ixv[d];
         for (int c = 0; c < N; ++c) {
             g.xvel[c][d] = P->dev_block + off_xvel[c][d];
             g.dxvel[c][d] = P->dev_block + off_dxvel[c][d];
+            g.ixvel[c][d] = P->dev_block + off_ixvel[c][d];
         }
     }
     *out = P;
@@ -156,7 +164,7 @@ int jp_particles_destroy(jp_particles* P)
     cudaFree(P->d_err);
     if (P->h_err) cudaFreeHost(P->h_err);
     cudaFree(P->move.L0);  // one allocation holds all move scratch
-    cudaFree(P->inject.flag);
+    cudaFree(P->inject.counts);  // counters and lists share one allocation
     delete P;
     return JP_OK;
 }

@@ -38,8 +38,10 @@ struct DevGrid {
     uint64_t seed;
     const double* xv[3];        // vertex grid, n[d]+1
     const double* dxv[3];       // vertex spacing per cell, n[d]
+    const double* ixv[3];       // 1/spacing per cell (the reference's inv(di), computed once)
     const double* xvel[3][3];   // velocity grid of component c along axis d
     const double* dxvel[3][3];  // its spacing per interval
+    const double* ixvel[3][3];  // 1/spacing per interval
     int64_t nvel[3][3];
     double dom_lo[3], dom_hi[3];  // extrema of the vertex grid
     double lim_lo[3][3], lim_hi[3][3];  // first/last of every velocity grid
@@ -60,7 +62,8 @@ struct MoveScratch {
 };
 
 struct InjectScratch {
-    uint8_t* flag = nullptr;  // cell needs the sequential injection walk
+    int* counts = nullptr;  // flagged cells per colour (8 counters), then the lists
+    int* list = nullptr;    // flagged cells, one region per colour
 };
 
 }  // namespace jp
@@ -200,6 +203,90 @@ __device__ __forceinline__ void raise_err(int* d_err, int bits)
 {
     if (bits) atomicOr(d_err, bits);
 }
+
+// ---- exact IEEE comparisons on the integer pipe ------------------------
+// GB300 issues FP64 instructions (compares included) at a small fraction of
+// its integer rate, so range tests use an order-preserving integer key of
+// the double: for non-NaN x, y,  x <= y  <=>  okey(x) <= okey(y)  and
+// x < y  <=>  okey(x) < okey(y)  (-0.0 maps to the key of +0.0). A NaN
+// compares false with everything, exactly like the FP64 comparison.
+__device__ __forceinline__ long long okey(double x)
+{
+    long long b = __double_as_longlong(x);
+    b = (b == (long long)0x8000000000000000ull) ? 0ll : b;
+    return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+
+__device__ __forceinline__ bool is_nan_bits(double x)
+{
+    return (__double_as_longlong(x) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+
+// ---- warp-level compaction of live slots -------------------------------
+// A warp owns 32 consecutive cells. `mask[s]` holds, per slot s, the lanes
+// whose cell has slot s live; `pre[s]` is the number of live slots before s.
+// Live slot number k (slot-major order) belongs to slot s with
+// pre[s] <= k < pre[s+1] and to the lane of the (k - pre[s])-th set bit of
+// mask[s]. Work then runs with all 32 lanes busy instead of one lane per cell
+// stepping through mostly empty slots.
+struct SlotList {
+    uint32_t mask[64];
+    int pre[65];
+};
+
+__device__ __forceinline__ int nth_set_bit(uint32_t m, int n)
+{
+    int pos = 0, c;
+    c = __popc(m & 0xFFFFu);
+    if (n >= c) { n -= c; m >>= 16; pos += 16; }
+    c = __popc(m & 0xFFu);
+    if (n >= c) { n -= c; m >>= 8; pos += 8; }
+    c = __popc(m & 0xFu);
+    if (n >= c) { n -= c; m >>= 4; pos += 4; }
+    c = __popc(m & 0x3u);
+    if (n >= c) { n -= c; m >>= 2; pos += 2; }
+    if (n >= (int)(m & 1u)) pos += 1;
+    return pos;
+}
+
+// Builds the list for cells c0 .. c0+31 (lanes past ncells own no cell) and
+// returns the number of live slots. Also returns the lane's own 64-bit live mask.
+__device__ __forceinline__ int build_slot_list(SlotList& Lst, const uint8_t* __restrict__ index, int64_t c0,
+                                               int64_t nc, int M, int lane, uint64_t* own_live)
+{
+    const bool valid = c0 + lane < nc;
+    int K = 0;
+    uint64_t mine = 0;
+#pragma unroll 4
+    for (int s = 0; s < M; ++s) {
+        const bool live = valid && index[c0 + lane + nc * s] != 0;
+        const uint32_t m = __ballot_sync(0xffffffffu, live);
+        if (lane == 0) {
+            Lst.mask[s] = m;
+            Lst.pre[s] = K;
+        }
+        mine |= (uint64_t)live << s;
+        K += __popc(m);
+    }
+    if (lane == 0) Lst.pre[M] = K;
+    __syncwarp();
+    *own_live = mine;
+    return K;
+}
+
+__device__ __forceinline__ void slot_item(const SlotList& Lst, int M, int k, int* slot, int* lane)
+{
+    int lo = 0, hi = M;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (Lst.pre[mid] <= k) lo = mid;
+        else hi = mid;
+    }
+    *slot = lo;
+    *lane = nth_set_bit(Lst.mask[lo], k - Lst.pre[lo]);
+}
+
+constexpr int kWarpsPerBlock = 8;
 
 inline unsigned grid_blocks(int64_t n, int threads = kThreads)
 {

@@ -5,9 +5,9 @@
 // slot at or after `starting_point`, which carries over between target cells)
 // decides which particles survive a full cell. It is reproduced exactly in
 // three stages:
-//   1. classify (all cells, one coalesced pass): which live slots left their
-//      cell, where they go (one of the 3^N neighbours, or out), and a copy of
-//      the movers' coordinates and fields into a shadow array;
+//   1. classify (all cells, one pass over the live slots): which particles left
+//      their cell, where they go (one of the 3^N neighbours, or out), and a
+//      copy of the movers' coordinates and fields into a shadow array;
 //   2. allocate (3^N colour launches): the reference's walk, replayed on
 //      64-bit occupancy masks only (L2-resident), recording for every refilled
 //      slot the origin of its particle;
@@ -18,9 +18,13 @@
 //
 // inject_particles! (src/Particles/injection.jl:19-131) only changes a cell
 // whose first quadrant is under-populated (the `break` at injection.jl:100
-// ends the walk otherwise), and that test depends on the cell alone. A
-// coalesced flag pass finds those cells; the 2^N colour passes then run the
-// reference's sequential walk for flagged cells only.
+// ends the walk otherwise), and that test depends on the cell alone. A flag
+// pass over all cells appends those cells to one work list per colour; each of
+// the 2^N colour passes then gives every listed cell a warp that stages the
+// cell's 3^N neighbourhood in shared memory and runs the reference's
+// sequential walk with warp-wide counts and nearest-neighbour searches. Cells
+// of one colour are independent, so the list order (set by atomics) does not
+// change any result.
 #include <math_constants.h>
 
 #include "jp_internal.cuh"
@@ -39,67 +43,124 @@ struct MoveView {
     int64_t nslots;
 };
 
+// find_parent_cell_bisection with integer-key comparisons (px not NaN):
+// the local walk of find_cell, ties replayed by bisect_exact.
+__device__ __forceinline__ int64_t find_cell_key(double px, long long kp, const double* x, int64_t len,
+                                                 int64_t seed, int* errs)
+{
+    long long ka = okey(ldg(x + seed)), kb = okey(ldg(x + seed + 1));
+    if (ka <= kp && kp <= kb) return seed;
+    int64_t k = seed;
+    if (kp < ka) {
+#pragma unroll 1
+        for (int it = 0; it < 4 && k > 0; ++it) {
+            --k;
+            kb = ka;
+            ka = okey(ldg(x + k));
+            if (ka <= kp && kp <= kb) return (kp == ka || kp == kb) ? bisect_exact(px, x, len, seed, errs) : k;
+        }
+    } else {
+#pragma unroll 1
+        for (int it = 0; it < 4 && k + 2 < len; ++it) {
+            ++k;
+            ka = kb;
+            kb = okey(ldg(x + k + 1));
+            if (ka <= kp && kp <= kb) return (kp == ka || kp == kb) ? bisect_exact(px, x, len, seed, errs) : k;
+        }
+    }
+    return bisect_exact(px, x, len, seed, errs);
+}
+
 // -------------------------------------------------------------- classify
 template <int DIM>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
     move_classify(DevGrid g, Coords X, const uint8_t* __restrict__ index, Args A, MoveView S, int* d_err)
 {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.ncells) return;
-    int64_t I[3];
-    cell_coords(g, c, I);
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ long long cellk[kWarpsPerBlock][32][2 * DIM];  // keys of corner and corner + dx
+    __shared__ int cellI[kWarpsPerBlock][32][3];
+    __shared__ unsigned long long movers[kWarpsPerBlock][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
     const int64_t nc = g.ncells;
-    double corner[3], dx[3];
+    const int M = g.max_xcell;
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            const double lo = ldg(g.xv[d] + I[d]);
+            cellk[w][lane][d] = okey(lo);
+            cellk[w][lane][DIM + d] = okey(lo + ldg(g.dxv[d] + I[d]));  // xv + dx (isincell)
+            cellI[w][lane][d] = (int)I[d];
+        }
+        movers[w][lane] = 0;
+    }
+    long long kdlo[3], kdhi[3];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        corner[d] = ldg(g.xv[d] + I[d]);
-        dx[d] = ldg(g.dxv[d] + I[d]);
+        kdlo[d] = okey(g.dom_lo[d]);
+        kdhi[d] = okey(g.dom_hi[d]);
     }
-    uint64_t L = 0, Mv = 0;
+    uint64_t L;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &L);
     int errs = 0;
-    for (int s = 0; s < g.max_xcell; ++s) {
-        const int64_t a = c + nc * s;
-        if (!index[a]) continue;
-        const uint64_t bit = 1ull << s;
-        L |= bit;
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
         double p[3];
+        long long kp[3];
+        bool pnan = false;
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) p[d] = X.c[d][a];
-        if (isincell<DIM>(p, corner, dx)) continue;  // move_safe.jl:93
-        Mv |= bit;
-        bool inside = true;  // indomain, strict (move_safe.jl:199-206)
+        for (int d = 0; d < DIM; ++d) {
+            p[d] = X.c[d][a];
+            kp[d] = okey(p[d]);
+            pnan |= is_nan_bits(p[d]);
+        }
+        bool in = !pnan;  // isincell, strict (src/Particles/utils.jl:7-15)
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) inside = inside & (g.dom_lo[d] < p[d]) & (p[d] < g.dom_hi[d]);
+        for (int d = 0; d < DIM; ++d) in = in & (cellk[w][l][d] < kp[d]) & (kp[d] < cellk[w][l][DIM + d]);
+        if (in) continue;  // move_safe.jl:93
+        atomicOr(&movers[w][l], 1ull << s);
+        bool inside = !pnan;  // indomain, strict (move_safe.jl:199-206)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) inside = inside & (kdlo[d] < kp[d]) & (kp[d] < kdhi[d]);
         uint8_t code = kCodeExit;
         if (inside) {
             int off[3] = {0, 0, 0};
-            double cT[3], dT[3];
-            bool far = false;
+            bool far = false, inT = true;
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
-                const int64_t T = find_cell(p[d], g.xv[d], g.n[d] + 1, I[d], &errs);
-                off[d] = (int)(T - I[d]);
+                const int I = cellI[w][l][d];
+                const int64_t T = find_cell_key(p[d], kp[d], g.xv[d], g.n[d] + 1, I, &errs);
+                off[d] = (int)(T - I);
                 far |= (off[d] > 1) | (off[d] < -1);
-                cT[d] = ldg(g.xv[d] + T);
-                dT[d] = ldg(g.dxv[d] + T);
+                const double lo = ldg(g.xv[d] + T);
+                inT = inT & (okey(lo) < kp[d]) & (kp[d] < okey(lo + ldg(g.dxv[d] + T)));
             }
             if (far) {
                 errs |= kWarnFarMove;
             } else {
                 code = (uint8_t)nb_code<DIM>(off);
-                if (!isincell<DIM>(p, cT, dT)) code |= kCodeUnstable;
+                if (!inT) code |= kCodeUnstable;
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) S.shadow[d * S.nslots + a] = p[d];
-                for (int k = 0; k < A.n; ++k) S.shadow[(DIM + k) * S.nslots + a] = A.a[k][a];
+                for (int j = 0; j < A.n; ++j) S.shadow[(DIM + j) * S.nslots + a] = A.a[j][a];
             }
         }
         S.code[a] = code;
     }
-    S.L0[c] = L;
-    S.L[c] = L;
-    S.M[c] = Mv;
-    S.R[c] = 0;
-    S.U[c] = 0;
+    __syncwarp();
+    const int64_t c = c0 + lane;
+    if (c < nc) {
+        S.L0[c] = L;
+        S.L[c] = L;
+        S.M[c] = movers[w][lane];
+        S.R[c] = 0;
+        S.U[c] = 0;
+    }
     raise_err(d_err, errs);
 }
 
@@ -230,124 +291,165 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------- injection
-// first quadrant occupancy test (injection.jl:81-100 for the first vertex)
+struct InjectLists {
+    int* counts;     // [8]
+    int* list;       // ncells entries
+    int64_t off[8];  // start of each colour's region in `list`
+};
+
+template <int DIM>
+__device__ __forceinline__ int colour_of(const int64_t* I)
+{
+    return (int)(I[0] & 1) + 2 * (int)(I[1] & 1) + (DIM == 3 ? 4 * (int)(I[2] & 1) : 0);
+}
+
+// first-quadrant occupancy test (injection.jl:81-100 for the first vertex);
+// flagged cells are appended to their colour's list.
 template <int DIM>
 __global__ void __launch_bounds__(kThreads)
-    inject_flag(DevGrid g, CCoords X, const uint8_t* __restrict__ index, uint8_t* __restrict__ flag)
+    inject_flag(DevGrid g, CCoords X, const uint8_t* __restrict__ index, InjectLists Ls)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.ncells) return;
+    const int lane = threadIdx.x & 31;
+    bool flag = false;
+    int col = 0;
+    if (c < g.ncells) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        col = colour_of<DIM>(I);
+        const int64_t nc = g.ncells;
+        long long klo[3], khi[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            const double lo = ldg(g.xv[d] + I[d]);
+            klo[d] = okey(lo);
+            khi[d] = okey(lo + ldg(g.dxv[d] + I[d]) / 2.0);  // quadrant corner + dx/2
+        }
+        const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
+        int count = 0;
+        for (int s = 0; s < g.max_xcell && count < min_xq; ++s) {
+            const int64_t a = c + nc * s;
+            if (!index[a]) continue;
+            bool in = true;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const double x = X.c[d][a];
+                const long long k = okey(x);
+                in = in & !is_nan_bits(x) & (klo[d] < k) & (k < khi[d]);
+            }
+            count += in ? 1 : 0;
+        }
+        flag = count < min_xq;
+    }
+    const unsigned active = __ballot_sync(0xffffffffu, flag);
+    if (flag) {
+        const unsigned grp = __match_any_sync(active, col);
+        const int leader = __ffs(grp) - 1;
+        const int rank = __popc(grp & ((1u << lane) - 1u));
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&Ls.counts[col], __popc(grp));
+        base = __shfl_sync(grp, base, leader);
+        Ls.list[Ls.off[col] + base + rank] = (int)c;
+    }
+}
+
+__device__ __forceinline__ double warp_min(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Per-warp shared-memory image of a cell's 3^N neighbourhood: coordinates
+// and occupancy of every candidate slot, plus the squared distances of the
+// current search.
+template <int DIM>
+struct Hood {
+    double* x[DIM];
+    double* ss;
+    uint8_t* live;
+};
+
+template <int DIM>
+__host__ __device__ __forceinline__ size_t hood_bytes(int M)
+{
+    const int n = (DIM == 2 ? 9 : 27) * M;
+    const size_t bytes = (size_t)n * (DIM * sizeof(double) + sizeof(double) + 1);
+    return (bytes + 15) & ~(size_t)15;  // keep every warp's doubles 16-byte aligned
+}
+
+// _inject_particles! (src/Particles/injection.jl:68-131) for one cell, by one warp.
+// The nearest-neighbour result of index_min_distance (injection.jl:330-393) is
+// the first candidate, in the reference's k -> j -> i -> slot order, whose
+// distance sqrt(ss) equals the minimum: the lanes find the minimum ss over
+// the staged candidates, then only candidates within rounding of it
+// evaluate sqrt.
+template <int DIM>
+__device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __restrict__ index, const Args& A,
+                                 uint32_t call, int64_t c, const Hood<DIM>& H, int lane, int* errs)
+{
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    constexpr int NB = DIM == 2 ? 9 : 27;
+    constexpr int CENTER = DIM == 2 ? 4 : 13;
+    const int ncand = NB * M;
     int64_t I[3];
     cell_coords(g, c, I);
-    const int64_t nc = g.ncells;
-    double qc[3], dq[3];
+    // stage the neighbourhood
+    for (int o = lane; o < ncand; o += 32) {
+        const int nb = o / M, s = o - nb * M;
+        const int64_t J[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1, DIM == 3 ? I[2] + nb / 9 - 1 : 0};
+        bool ok = J[0] >= 0 && J[1] >= 0 && J[0] < g.n[0] && J[1] < g.n[1] &&
+                  (DIM == 2 || (J[2] >= 0 && J[2] < g.n[2]));
+        uint8_t live = 0;
+        if (ok) {
+            const int64_t a = cell_linear<DIM>(g, J) + nc * s;
+            live = index[a];
+            if (live) {
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-        qc[d] = ldg(g.xv[d] + I[d]);
-        dq[d] = ldg(g.dxv[d] + I[d]) / 2.0;
-    }
-    const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
-    int count = 0;
-    for (int s = 0; s < g.max_xcell && count < min_xq; ++s) {
-        const int64_t a = c + nc * s;
-        if (!index[a]) continue;
-        double p[3];
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) p[d] = X.c[d][a];
-        count += isincell<DIM>(p, qc, dq) ? 1 : 0;
-    }
-    flag[c] = count < min_xq ? 1 : 0;
-}
-
-// index_min_distance: src/Particles/injection.jl:330-393
-template <int DIM>
-__device__ bool nearest_particle(const DevGrid& g, const Coords& X, const uint8_t* __restrict__ index,
-                                 const double* pn, int cur_slot, const int64_t* I, int64_t* best)
-{
-    const int64_t nc = g.ncells;
-    double dmin = CUDART_INF;
-    bool found = false;
-    const int kr = DIM == 3 ? 1 : 0;
-    for (int64_t k = I[2] - kr; k <= I[2] + kr; ++k) {
-        for (int64_t j = I[1] - 1; j <= I[1] + 1; ++j) {
-            for (int64_t i = I[0] - 1; i <= I[0] + 1; ++i) {
-                if (i < 0 || j < 0 || k < 0) continue;
-                if (i >= g.n[0] || j >= g.n[1] || (DIM == 3 && k >= g.n[2])) continue;
-                const int64_t J[3] = {i, j, k};
-                const int64_t cc = cell_linear<DIM>(g, J);
-                const bool self = (i == I[0]) && (j == I[1]) && (k == I[2]);
-                for (int ip = 0; ip < g.max_xcell; ++ip) {
-                    if (self && ip == cur_slot) continue;
-                    const int64_t a = cc + nc * ip;
-                    if (!index[a]) continue;
-                    double ss;
-                    if (DIM == 2) {
-                        const double px = X.c[0][a], py = X.c[1][a];
-                        if (isnan(px) || isnan(py)) continue;
-                        const double dxx = px - pn[0], dyy = py - pn[1];
-                        ss = dxx * dxx + dyy * dyy;
-                    } else {
-                        const double dxx = X.c[0][a] - pn[0];
-                        const double dyy = X.c[1][a] - pn[1];
-                        const double dzz = X.c[2][a] - pn[2];
-                        ss = (dxx * dxx + dyy * dyy) + dzz * dzz;
-                    }
-                    const double dist = sqrt(ss);
-                    if (dist < dmin) {
-                        dmin = dist;
-                        *best = a;
-                        found = true;
-                    }
-                }
+                for (int d = 0; d < DIM; ++d) H.x[d][o] = X.c[d][a];
             }
         }
+        H.live[o] = live;
     }
-    return found;
-}
-
-// _inject_particles!: src/Particles/injection.jl:68-131, for flagged cells
-template <int DIM>
-__global__ void __launch_bounds__(kThreads)
-    inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, const uint8_t* __restrict__ flag,
-                uint32_t call, int o0, int o1, int o2, int64_t m0, int64_t m1, int64_t m2, int* d_err)
-{
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= m0 * m1 * m2) return;
-    int64_t idx[3];
-    idx[0] = 2 * (t % m0) + o0;
-    idx[1] = 2 * ((t / m0) % m1) + o1;
-    idx[2] = DIM == 3 ? 2 * (t / (m0 * m1)) + o2 : 0;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d)
-        if (idx[d] >= g.n[d]) return;
-    const int64_t c = cell_linear<DIM>(g, idx);
-    if (!flag[c]) return;
-    const int64_t nc = g.ncells;
+    __syncwarp();
     double corner[3], dq[3];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        corner[d] = ldg(g.xv[d] + idx[d]);
-        dq[d] = ldg(g.dxv[d] + idx[d]) / 2.0;
+        corner[d] = ldg(g.xv[d] + I[d]);
+        dq[d] = ldg(g.dxv[d] + I[d]) / 2.0;
     }
     const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
-    int errs = 0;
+    const int base = CENTER * M;
     for (int q = 0; q < (1 << DIM); ++q) {
         double qc[3];
+        long long klo[3], khi[3];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) qc[d] = corner[d] + dq[d] * (double)((q >> d) & 1);
-        int count = 0;
-        for (int i = 0; i < g.max_xcell; ++i) {
-            const int64_t a = c + nc * i;
-            if (!index[a]) continue;
-            double p[3];
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) p[d] = X.c[d][a];
-            count += isincell<DIM>(p, qc, dq) ? 1 : 0;
+        for (int d = 0; d < DIM; ++d) {
+            qc[d] = corner[d] + dq[d] * (double)((q >> d) & 1);
+            klo[d] = okey(qc[d]);
+            khi[d] = okey(qc[d] + dq[d]);  // isincell(p, vertex, di_quadrant)
         }
-        if (count >= min_xq) break;
-        for (int i = 0; i < g.max_xcell; ++i) {
-            const int64_t a = c + nc * i;
-            if (index[a]) continue;
+        int cnt = 0;
+        for (int s = lane; s < M; s += 32) {
+            if (!H.live[base + s]) continue;
+            bool in = true;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const double x = H.x[d][base + s];
+                const long long k = okey(x);
+                in = in & !is_nan_bits(x) & (klo[d] < k) & (k < khi[d]);
+            }
+            cnt += in ? 1 : 0;
+        }
+        int count = __reduce_add_sync(0xffffffffu, cnt);
+        if (count >= min_xq) break;  // injection.jl:100
+        const bool f0 = lane < M && !H.live[base + lane];
+        const bool f1 = lane + 32 < M && !H.live[base + lane + 32];
+        uint64_t freem = (uint64_t)__ballot_sync(0xffffffffu, f0) | ((uint64_t)__ballot_sync(0xffffffffu, f1) << 32);
+        while (freem) {
+            const int i = __ffsll((long long)freem) - 1;
+            freem &= freem - 1;
             ++count;
             double pn[3];
 #pragma unroll
@@ -356,17 +458,86 @@ __global__ void __launch_bounds__(kThreads)
                                                  (uint32_t)d);
                 pn[d] = qc[d] + dq[d] * fma(0.95, r, 0.05);  // new_particle, injection.jl:411-417
             }
+            const int64_t ai = c + nc * i;
+            if (lane == 0) {
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) X.c[d][a] = pn[d];
-            index[a] = 1;
-            int64_t src = 0;
-            if (nearest_particle<DIM>(g, X, index, pn, i, idx, &src)) {
-                for (int k = 0; k < A.n; ++k) A.a[k][a] = A.a[k][src];
-            } else if (A.n > 0) {
-                errs |= kWarnNoNeighbour;
+                for (int d = 0; d < DIM; ++d) {
+                    X.c[d][ai] = pn[d];
+                    H.x[d][base + i] = pn[d];
+                }
+                index[ai] = 1;
+                H.live[base + i] = 1;
             }
+            __syncwarp();
+            // pass 1: squared distances of every candidate, lane-strided
+            double lmin = CUDART_INF;
+            for (int o = lane; o < ncand; o += 32) {
+                double ss = CUDART_INF;
+                if (H.live[o] && o != base + i) {
+                    double e[3];
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) e[d] = H.x[d][o] - pn[d];
+                    const double t = DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
+                    if (!isnan(t)) ss = t;
+                }
+                H.ss[o] = ss;
+                lmin = fmin(lmin, ss);
+            }
+            const double best = warp_min(lmin);
+            __syncwarp();
+            int64_t src = -1;
+            if (best < CUDART_INF) {
+                // pass 2: the first candidate (in order) whose rounded distance equals sqrt(best)
+                const double dmin = sqrt(best);
+                const double bound = best * (1.0 + 0x1.0p-48);
+                int lo = 0x7fffffff;
+                for (int o = lane; o < ncand; o += 32) {
+                    const double ss = H.ss[o];
+                    if (ss <= bound && sqrt(ss) == dmin) {
+                        lo = o;
+                        break;  // lane-strided order: the first hit is this lane's smallest
+                    }
+                }
+                const int win = __reduce_min_sync(0xffffffffu, lo);
+                const int nb = win / M, s = win - nb * M;
+                const int64_t J[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1, DIM == 3 ? I[2] + nb / 9 - 1 : 0};
+                src = cell_linear<DIM>(g, J) + nc * s;
+            }
+            if (src >= 0) {
+                for (int k = lane; k < A.n; k += 32) A.a[k][ai] = A.a[k][src];
+            } else if (A.n > 0) {
+                *errs |= kWarnNoNeighbour;
+            }
+            __syncwarp();
             if (count >= min_xq) break;
         }
+    }
+}
+
+// One colour pass: warps take the colour's listed cells in turn.
+template <int DIM>
+__global__ void inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, InjectLists Ls, int col,
+                            uint32_t call, int* d_err)
+{
+    extern __shared__ __align__(16) unsigned char smem_inject[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int M = g.max_xcell;
+    const int ncand = (DIM == 2 ? 9 : 27) * M;
+    unsigned char* base = smem_inject + (size_t)wib * hood_bytes<DIM>(M);
+    Hood<DIM> H;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) H.x[d] = (double*)base + (size_t)d * ncand;
+    H.ss = (double*)base + (size_t)DIM * ncand;
+    H.live = base + (size_t)(DIM + 1) * ncand * sizeof(double);
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int count = Ls.counts[col];
+    int errs = 0;
+    for (int k = gw; k < count; k += nwarps) {
+        const int64_t c = Ls.list[Ls.off[col] + k];
+        inject_cell_warp<DIM>(g, X, index, A, call, c, H, lane, &errs);
+        __syncwarp();
     }
     raise_err(d_err, errs);
 }
@@ -421,16 +592,18 @@ cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index
     MoveView S{m.L0, m.L, m.M, m.R, m.U, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell};
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(P->g.ncells);
+    const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const int ntw = 32 * kWarpsPerBlock;
     int64_t mc[3] = {1, 1, 1};
     for (int d = 0; d < N; ++d) mc[d] = (P->g.n[d] + 2) / 3;  // ceil(n/3)
     const unsigned nbp = grid_blocks(mc[0] * mc[1] * mc[2]);
     if (N == 2) {
-        move_classify<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        move_classify<2><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
         for (int pass = 0; pass < 9; ++pass)  // offsetᵢ outer, offsetⱼ inner (move_safe.jl:32)
             move_allocate<2><<<nbp, kThreads, 0, st>>>(P->g, S, pass / 3, pass % 3, 0, mc[0], mc[1], 1);
         move_apply<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     } else {
-        move_classify<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        move_classify<3><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
         for (int pass = 0; pass < 27; ++pass)  // i outer, k inner (move_safe.jl:39)
             move_allocate<3><<<nbp, kThreads, 0, st>>>(P->g, S, pass / 9, (pass / 3) % 3, pass % 3, mc[0], mc[1],
                                                        mc[2]);
@@ -443,31 +616,58 @@ cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* ind
                           int nargs, uint32_t call)
 {
     const int N = P->g.ndim;
-    if (!P->inject.flag) {
-        cudaError_t e = cudaMalloc(&P->inject.flag, P->g.ncells);
+    const int64_t nc = P->g.ncells;
+    if (!P->inject.counts) {
+        cudaError_t e = cudaMalloc(&P->inject.counts, (8 + nc) * sizeof(int));
         if (e != cudaSuccess) return e;
+        P->inject.list = P->inject.counts + 8;
     }
+    InjectLists Ls;
+    Ls.counts = P->inject.counts;
+    Ls.list = P->inject.list;
+    // colour regions: cells whose index parity along every axis is fixed
+    int64_t cnt[3][2];
+    for (int d = 0; d < 3; ++d)
+        for (int o = 0; o < 2; ++o) cnt[d][o] = d < N ? (P->g.n[d] - o + 1) / 2 : (o == 0 ? 1 : 0);
+    int64_t off = 0;
+    for (int col = 0; col < 8; ++col) {
+        Ls.off[col] = off;
+        off += cnt[0][col & 1] * cnt[1][(col >> 1) & 1] * cnt[2][(col >> 2) & 1];
+    }
+    cudaStream_t st = P->stream;
+    cudaError_t e = cudaMemsetAsync(P->inject.counts, 0, 8 * sizeof(int), st);
+    if (e != cudaSuccess) return e;
     Coords X{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};
     CCoords CX{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};
     Args A{};
     A.n = nargs;
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
-    cudaStream_t st = P->stream;
-    const unsigned nb = grid_blocks(P->g.ncells);
-    int64_t mc[3] = {1, 1, 1};
-    for (int d = 0; d < N; ++d) mc[d] = (P->g.n[d] + 1) / 2;  // ceil(n/2)
-    const unsigned nbp = grid_blocks(mc[0] * mc[1] * mc[2]);
-    uint8_t* flag = P->inject.flag;
+    const unsigned nb = grid_blocks(nc);
+    const int M = P->g.max_xcell;
+    const int wpb = N == 2 ? 4 : 1;  // warps per block of the pass kernels
+    const size_t smem = N == 2 ? wpb * hood_bytes<2>(M) : wpb * hood_bytes<3>(M);
+    // enough warps to keep every SM busy; each strides over its colour's list
+    const unsigned nbp = (unsigned)(152 * (N == 2 ? 8 : 16));
     if (N == 2) {
-        inject_flag<2><<<nb, kThreads, 0, st>>>(P->g, CX, index, flag);
-        for (int pass = 0; pass < 4; ++pass)
-            inject_pass<2><<<nbp, kThreads, 0, st>>>(P->g, X, index, A, flag, call, pass / 2, pass % 2, 0, mc[0],
-                                                     mc[1], 1, P->d_err);
+        if (smem > 48 * 1024) {
+            e = cudaFuncSetAttribute(inject_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        inject_flag<2><<<nb, kThreads, 0, st>>>(P->g, CX, index, Ls);
+        for (int pass = 0; pass < 4; ++pass) {  // offsetᵢ outer, offsetⱼ inner (injection.jl:31)
+            const int col = (pass / 2) + 2 * (pass % 2);
+            inject_pass<2><<<nbp, 32 * wpb, smem, st>>>(P->g, X, index, A, Ls, col, call, P->d_err);
+        }
     } else {
-        inject_flag<3><<<nb, kThreads, 0, st>>>(P->g, CX, index, flag);
-        for (int pass = 0; pass < 8; ++pass)
-            inject_pass<3><<<nbp, kThreads, 0, st>>>(P->g, X, index, A, flag, call, pass / 4, (pass / 2) % 2,
-                                                     pass % 2, mc[0], mc[1], mc[2], P->d_err);
+        if (smem > 48 * 1024) {
+            e = cudaFuncSetAttribute(inject_pass<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        inject_flag<3><<<nb, kThreads, 0, st>>>(P->g, CX, index, Ls);
+        for (int pass = 0; pass < 8; ++pass) {  // i outer, k inner (injection.jl:38)
+            const int col = (pass / 4) + 2 * ((pass / 2) % 2) + 4 * (pass % 2);
+            inject_pass<3><<<nbp, 32 * wpb, smem, st>>>(P->g, X, index, A, Ls, col, call, P->d_err);
+        }
     }
     return cudaGetLastError();
 }

@@ -7,6 +7,8 @@
 // (FP64) or 32-byte (index) transaction per warp.
 #include <math_constants.h>
 
+#include <cmath>
+
 #include "jp_internal.cuh"
 
 namespace jp {
@@ -55,25 +57,45 @@ __global__ void __launch_bounds__(kThreads) init_kernel(DevGrid g, Coords X, uin
 
 // ----------------------------------------------------------- advection
 // interp_velocity2particle for component `comp`
-// (src/Particles/Advection/advection.jl:93-148, src/Advection/advection.jl:3-47)
+// (src/Particles/Advection/advection.jl:93-148, src/Advection/advection.jl:3-47).
+// A point inside the seed interval [x[I], x[I+1]] is inside the grid's limits
+// too, so the limits test (check_local_limits) only runs when that first
+// bisection test fails; the result is the same for every input. The seed test
+// itself compares integer keys (exact, see okey) and falls back to the FP64
+// comparisons of the reference whenever it does not accept.
+struct AdvParams {
+    double adt;  // alpha * dt (first stage)
+    double dt;
+    double ca;   // RK2 with alpha != 1/2: 1 - 1/(2 alpha) and 1/(2 alpha)
+    double cb;
+    int half;    // alpha == 1/2
+};
+
 template <int DIM>
 __device__ __forceinline__ double interp_component(const DevGrid& g, int comp, const double* p,
-                                                   const int64_t* I, const double* __restrict__ V,
-                                                   int* errs)
+                                                   const long long* kp, bool pnan, const int* I,
+                                                   const double* __restrict__ V, int* errs)
 {
-#pragma unroll
-    for (int d = 0; d < DIM; ++d)
-        if (!(g.lim_lo[comp][d] <= p[d] && p[d] <= g.lim_hi[comp][d])) return CUDART_INF;
     int64_t idx[3];
-    double t[3];
+    double xc[3];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         const double* x = g.xvel[comp][d];
-        idx[d] = find_cell(p[d], x, g.nvel[comp][d], I[d], errs);
-        const double xc = ldg(x + idx[d]);
-        const double dx = ldg(g.dxvel[comp][d] + idx[d]);
-        t[d] = (p[d] - xc) * (1.0 / dx);
+        const double a = ldg(x + I[d]), b = ldg(x + I[d] + 1);
+        if (!pnan && okey(a) <= kp[d] && kp[d] <= okey(b)) {
+            idx[d] = I[d];
+            xc[d] = a;
+        } else {
+#pragma unroll
+            for (int e = 0; e < DIM; ++e)
+                if (!(g.lim_lo[comp][e] <= p[e] && p[e] <= g.lim_hi[comp][e])) return CUDART_INF;
+            idx[d] = find_cell(p[d], x, g.nvel[comp][d], I[d], errs);
+            xc[d] = ldg(x + idx[d]);
+        }
     }
+    double t[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) t[d] = (p[d] - xc[d]) * ldg(g.ixvel[comp][d] + idx[d]);
     const int64_t L0 = g.nvel[comp][0];
     double v[8];
     if (DIM == 2) {
@@ -99,77 +121,94 @@ __device__ __forceinline__ double interp_component(const DevGrid& g, int comp, c
 }
 
 template <int DIM>
-__device__ __forceinline__ void interp_velocity(const DevGrid& g, const CVel& V, const double* p,
-                                                const int64_t* I, double* v, int* errs)
+__device__ __forceinline__ void interp_velocity(const DevGrid& g, const CVel& V, const double* p, const int* I,
+                                                double* v, int* errs)
 {
+    long long kp[3];
+    bool pnan = false;
 #pragma unroll
-    for (int c = 0; c < DIM; ++c) v[c] = interp_component<DIM>(g, c, p, I, V.v[c], errs);
+    for (int d = 0; d < DIM; ++d) {
+        kp[d] = okey(p[d]);
+        pnan |= is_nan_bits(p[d]);
+    }
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) v[c] = interp_component<DIM>(g, c, p, kp, pnan, I, V.v[c], errs);
 }
 
 // advect_particle: RK2 src/Particles/Advection/advection.jl:154-179 with
-// first/second_stage of src/Advection/RK2.jl; RK4 :261-279; Euler :348-367.
+// first/second_stage of src/Advection/RK2.jl (muladd(1, (alpha*dt)*v, p) etc.);
+// RK4 :261-279; Euler :348-367.
 template <int DIM, int METHOD>
-__device__ __forceinline__ void advect_particle(const DevGrid& g, const CVel& V, double alpha, double dt,
-                                                const int64_t* I, const double* p0, double* p, int* errs)
+__device__ __forceinline__ void advect_particle(const DevGrid& g, const CVel& V, const AdvParams& P,
+                                                const int* I, const double* p0, double* p, int* errs)
 {
     if (METHOD == JP_RUNGE_KUTTA2) {
         double v0[3], v1[3], p1[3];
         interp_velocity<DIM>(g, V, p0, I, v0, errs);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) p1[d] = fma(1.0, (alpha * dt) * v0[d], p0[d]);
+        for (int d = 0; d < DIM; ++d) p1[d] = fma(1.0, P.adt * v0[d], p0[d]);
         interp_velocity<DIM>(g, V, p1, I, v1, errs);
-        if (alpha == 0.5) {
+        if (P.half) {
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, dt * v1[d], p0[d]);
+            for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, P.dt * v1[d], p0[d]);
         } else {
-            const double ia = 1.0 / alpha;
-            const double a = fma(-0.5, ia, 1.0);
-            const double b = 0.5 * ia;
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, dt * fma(a, v0[d], b * v1[d]), p0[d]);
+            for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, P.dt * fma(P.ca, v0[d], P.cb * v1[d]), p0[d]);
         }
     } else if (METHOD == JP_RUNGE_KUTTA4) {
         double k1[3], k2[3], k3[3], k4[3], q[3];
         interp_velocity<DIM>(g, V, p0, I, k1, errs);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) q[d] = p0[d] + (dt * k1[d]) / 2.0;
+        for (int d = 0; d < DIM; ++d) q[d] = p0[d] + (P.dt * k1[d]) * 0.5;  // x / 2 == x * 0.5 exactly
         interp_velocity<DIM>(g, V, q, I, k2, errs);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) q[d] = p0[d] + (dt * k2[d]) / 2.0;
+        for (int d = 0; d < DIM; ++d) q[d] = p0[d] + (P.dt * k2[d]) * 0.5;
         interp_velocity<DIM>(g, V, q, I, k3, errs);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) q[d] = p0[d] + dt * k3[d];
+        for (int d = 0; d < DIM; ++d) q[d] = p0[d] + P.dt * k3[d];
         interp_velocity<DIM>(g, V, q, I, k4, errs);
 #pragma unroll
         for (int d = 0; d < DIM; ++d)
-            p[d] = p0[d] + (dt * (((k1[d] + 2.0 * k2[d]) + 2.0 * k3[d]) + k4[d])) / 6.0;
+            p[d] = p0[d] + __ddiv_rn(P.dt * (((k1[d] + 2.0 * k2[d]) + 2.0 * k3[d]) + k4[d]), 6.0);
     } else {
         double v0[3];
         interp_velocity<DIM>(g, V, p0, I, v0, errs);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, dt * v0[d], p0[d]);
+        for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, P.dt * v0[d], p0[d]);
     }
 }
 
-// advection_kernel!: src/Particles/Advection/advection.jl:66-91
+// advection_kernel! (src/Particles/Advection/advection.jl:66-91): one warp per
+// 32 consecutive cells, work spread over the warp's live slots.
 template <int DIM, int METHOD>
-__global__ void __launch_bounds__(kThreads)
-    advect_kernel(DevGrid g, CVel V, double alpha, double dt, Coords X, const uint8_t* __restrict__ index,
-                  int* d_err)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    advect_kernel(DevGrid g, CVel V, AdvParams P, Coords X, const uint8_t* __restrict__ index, int* d_err)
 {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.ncells) return;
-    int64_t I[3];
-    cell_coords(g, c, I);
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ int cellI[kWarpsPerBlock][32][3];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
     const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
+    }
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
     int errs = 0;
-    for (int s = 0; s < g.max_xcell; ++s) {
-        const int64_t a = c + nc * s;
-        if (!index[a]) continue;
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
         double p0[3], p[3];
 #pragma unroll
         for (int d = 0; d < DIM; ++d) p0[d] = X.c[d][a];
-        advect_particle<DIM, METHOD>(g, V, alpha, dt, I, p0, p, &errs);
+        advect_particle<DIM, METHOD>(g, V, P, I, p0, p, &errs);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) X.c[d][a] = p[d];
     }
@@ -177,43 +216,55 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------- grid2particle!
-// _grid2particle_classic!: src/Interpolations/grid_to_particle.jl:64-82
+// _grid2particle_classic! (src/Interpolations/grid_to_particle.jl:64-82): the
+// corner values, lower-left vertex and inverse spacing of each of the warp's
+// cells are staged once, then the warp's live slots are interpolated.
 template <int DIM>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
     g2p_kernel(DevGrid g, double* __restrict__ Fp, const double* __restrict__ F, CCoords X,
                const uint8_t* __restrict__ index)
 {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.ncells) return;
-    int64_t I[3];
-    cell_coords(g, c, I);
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ double cellv[kWarpsPerBlock][32][(1 << DIM) + 2 * DIM];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
     const int64_t nc = g.ncells;
-    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
-    double x0[3], idx_[3], v[8];
+    const int M = g.max_xcell;
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+        const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
+        double* cv = cellv[w][lane];
+        const double* b = F + I[0] + V0 * (I[1] + (DIM == 3 ? V1 * I[2] : 0));
+        cv[0] = ldg(b);
+        cv[1] = ldg(b + 1);
+        cv[2] = ldg(b + V0);
+        cv[3] = ldg(b + V0 + 1);
+        if (DIM == 3) {
+            const int64_t sz = V0 * V1;
+            cv[4] = ldg(b + sz);
+            cv[5] = ldg(b + sz + 1);
+            cv[6] = ldg(b + sz + V0);
+            cv[7] = ldg(b + sz + V0 + 1);
+        }
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-        x0[d] = ldg(g.xv[d] + I[d]);
-        idx_[d] = 1.0 / ldg(g.dxv[d] + I[d]);
+        for (int d = 0; d < DIM; ++d) {
+            cv[(1 << DIM) + d] = ldg(g.xv[d] + I[d]);
+            cv[(1 << DIM) + DIM + d] = ldg(g.ixv[d] + I[d]);
+        }
     }
-    const double* b = F + I[0] + V0 * (I[1] + (DIM == 3 ? V1 * I[2] : 0));
-    v[0] = ldg(b);
-    v[1] = ldg(b + 1);
-    v[2] = ldg(b + V0);
-    v[3] = ldg(b + V0 + 1);
-    if (DIM == 3) {
-        const int64_t sz = V0 * V1;
-        v[4] = ldg(b + sz);
-        v[5] = ldg(b + sz + 1);
-        v[6] = ldg(b + sz + V0);
-        v[7] = ldg(b + sz + V0 + 1);
-    }
-    for (int s = 0; s < g.max_xcell; ++s) {
-        const int64_t a = c + nc * s;
-        if (!index[a]) continue;
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        const double* cv = cellv[w][l];
         double t[3];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) t[d] = (X.c[d][a] - x0[d]) * idx_[d];
-        Fp[a] = lerpN<DIM>(v, t);
+        for (int d = 0; d < DIM; ++d) t[d] = (X.c[d][a] - cv[(1 << DIM) + d]) * cv[(1 << DIM) + DIM + d];
+        Fp[a] = lerpN<DIM>(cv, t);
     }
 }
 
@@ -247,8 +298,8 @@ __device__ __forceinline__ void p2g_cell(const DevGrid& g, int64_t c, const doub
                 const double dz = q_cur[2] - p[2];
                 ss = (dx * dx + dy * dy) + dz * dz;
             }
-            const double dist = sqrt(ss);
-            const double wi = 1.0 / (dist * dist);
+            const double dist = __dsqrt_rn(ss);
+            const double wi = __drcp_rn(dist * dist);
             w_c += wi;
             wF_c = fma(wi, f, wF_c);
         }
@@ -261,8 +312,8 @@ __device__ __forceinline__ void p2g_cell(const DevGrid& g, int64_t c, const doub
                 const double dz = q_nxt[2] - p[2];
                 ss = (dx * dx + dy * dy) + dz * dz;
             }
-            const double dist = sqrt(ss);
-            const double wi = 1.0 / (dist * dist);
+            const double dist = __dsqrt_rn(ss);
+            const double wi = __drcp_rn(dist * dist);
             w_n += wi;
             wF_n = fma(wi, f, wF_n);
         }
@@ -334,7 +385,7 @@ __global__ void __launch_bounds__(kThreads)
                 p2g_cell<DIM>(g, cells[k], q_cur, q_nxt, has_next, Fp, X, index, w_c, wF_c, w_n, wF_n);
         }
         const int64_t v = DIM == 2 ? i + V0 * r : i + V0 * (j + V1 * r);
-        F[v] = DIM == 2 ? wF_c / w_c : wF_c * (1.0 / w_c);
+        F[v] = DIM == 2 ? wF_c / w_c : wF_c * __drcp_rn(w_c);
         w_c = w_n;
         wF_c = wF_n;
     }
@@ -358,9 +409,17 @@ cudaError_t launch_advection(jp_particles* P, int method, double alpha, const do
     const bool d3 = P->g.ndim == 3;
     Coords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
     CVel Vv{{V[0], V[1], d3 ? V[2] : nullptr}};
-    const unsigned nb = grid_blocks(P->g.ncells);
+    AdvParams ap;
+    ap.adt = alpha * dt;
+    ap.dt = dt;
+    const double ia = 1.0 / alpha;  // second_stage, src/Advection/RK2.jl:38-41
+    ap.ca = std::fma(-0.5, ia, 1.0);
+    ap.cb = 0.5 * ia;
+    ap.half = alpha == 0.5;
+    const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const int nt = 32 * kWarpsPerBlock;
     cudaStream_t s = P->stream;
-#define JP_ADV(D, M) advect_kernel<D, M><<<nb, kThreads, 0, s>>>(P->g, Vv, alpha, dt, X, index, P->d_err)
+#define JP_ADV(D, M) advect_kernel<D, M><<<nb, nt, 0, s>>>(P->g, Vv, ap, X, index, P->d_err)
     if (!d3) {
         if (method == JP_RUNGE_KUTTA2) JP_ADV(2, JP_RUNGE_KUTTA2);
         else if (method == JP_RUNGE_KUTTA4) JP_ADV(2, JP_RUNGE_KUTTA4);
@@ -379,11 +438,12 @@ cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const doubl
 {
     const bool d3 = P->g.ndim == 3;
     CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
-    const unsigned nb = grid_blocks(P->g.ncells);
+    const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const int nt = 32 * kWarpsPerBlock;
     if (!d3)
-        g2p_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, X, index);
+        g2p_kernel<2><<<nb, nt, 0, P->stream>>>(P->g, Fp, F, X, index);
     else
-        g2p_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, X, index);
+        g2p_kernel<3><<<nb, nt, 0, P->stream>>>(P->g, Fp, F, X, index);
     return cudaGetLastError();
 }
 

@@ -136,7 +136,8 @@ def TA(backend):
 
     def convert(a):
         a = np.asarray(a, dtype=np.float64)
-        return torch.from_numpy(np.ascontiguousarray(a.T)).to("cuda").T
+        rev = tuple(reversed(range(a.ndim)))
+        return torch.from_numpy(np.ascontiguousarray(a.transpose(rev))).to("cuda").permute(*rev)
 
     return convert
 

@@ -89,8 +89,10 @@ def linear_T(g, axis):
 
 
 def cfl_dt(g, V, factor=1.0):
-    """dt = min over axes of dx / max|V| (README.md:77), times ``factor``."""
-    return factor * min(g["dx"][d] / float(np.max(np.abs(V[d]))) for d in range(g["ndim"]))
+    """dt = min over axes of dx / max|V| (README.md:77), times ``factor``
+    (axes whose velocity is zero everywhere do not limit dt)."""
+    return factor * min(g["dx"][d] / float(np.max(np.abs(V[d]))) for d in range(g["ndim"])
+                        if np.max(np.abs(V[d])) > 0)
 
 
 # The five benchmark configurations (sizes, particle counts, steps).
@@ -109,9 +111,12 @@ CONFIGS = {
 }
 
 
-def setup(name: str):
-    """Grid, velocity, vertex temperature and dt of a configuration."""
+def setup(name: str, ni=None):
+    """Grid, velocity, vertex temperature and dt of a configuration
+    (``ni`` overrides the cell counts, e.g. for a small profiling case)."""
     cfg = dict(CONFIGS[name])
+    if ni is not None:
+        cfg["ni"] = tuple(ni)
     g = grid(cfg["ni"])
     if cfg["velocity"] == "stream":
         V = stream_velocity(g)
