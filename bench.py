@@ -1,11 +1,14 @@
 """Throughput of the JustPIC particle-in-cell hot path on one GB300.
 
-Workload (default): 2D temperature advection, FP64, 1024 x 1024 cells, 24
+Default workload (C2): 2D temperature advection, FP64, 1024 x 1024 cells, 24
 particles per cell (max 48, min 12, seeded uniform placement), rigid-body
 rotation velocity on the staggered ghost-node grids, vertex temperature
 exp(-((x-0.5)^2+(y-0.75)^2)/0.01) carried by the particles. One step is the
 reference miniapp cycle (test/test_2D.jl:516-524): particle2grid!,
 advection! (RK2), move_particles!, inject_particles!, grid2particle!.
+``--workload C1`` (256^2, stream function, advection! + move_particles!, no
+fields) and ``--workload C3`` (128^3, cellular flow + drift, particle2grid!,
+advection!, move_particles!, inject_particles!) use the same harness.
 
 Metric: particle-steps/s = live particles x steps / device time. ``value`` is
 measured with the particle data resident in HBM and asynchronous calls;
@@ -33,24 +36,47 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-WORKLOAD = "C2"
 METRIC = "particle-steps/s on 1 GB300, FP32-offset vs FP64 at stated error; HBM % of peak"
 UNIT = "particle-steps/s"
 
-# Algorithmic bytes per live particle of each call (2D FP64, one particle field):
-# every live particle's data once per call, the Bool index at 1 byte per slot
-# (2 bytes per live particle at 24 of 48 slots), grid arrays once per call
-# amortised over the particles; movers (fraction m) re-read and re-write their
-# coordinates and field.
-BYTES = {
-    "advection!": lambda m: 16 + 16 + 2 + 0.7,
-    "move_particles!": lambda m: 16 + 2 + m * (2 * (16 + 8) + 2),
-    "inject_particles!": lambda m: 16 + 2,
-    "grid2particle!": lambda m: 16 + 2 + 8 + 0.35,
-    "particle2grid!": lambda m: 16 + 2 + 8 + 0.35,
+STEPS = {
+    "C1": ["advection!", "move_particles!"],
+    "C2": ["particle2grid!", "advection!", "move_particles!", "inject_particles!", "grid2particle!"],
+    "C3": ["particle2grid!", "advection!", "move_particles!", "inject_particles!"],
 }
-LAUNCHES_PER_STEP = {"particle2grid!": 1, "advection!": 1, "move_particles!": 11, "inject_particles!": 5,
-                     "grid2particle!": 1}
+DESC = {
+    "C1": "C1: 2D RK2 advection FP64, 256x256 cells, 24/48/12 particles per cell, stream-function velocity, "
+          "step = advection!+move_particles!",
+    "C2": "C2: 2D temperature advection FP64, 1024x1024 cells, 24/48/12 particles per cell, rigid rotation, RK2, "
+          "step = particle2grid!+advection!+move_particles!+inject_particles!+grid2particle!",
+    "C3": "C3: 3D temperature advection FP64, 128^3 cells, 24/48/12 particles per cell, cellular flow + 0.1 z "
+          "drift, RK2, step = particle2grid!+advection!+move_particles!+inject_particles!",
+}
+
+
+def algorithmic_bytes(op, N, nf, m, slots_per_live, grid_bytes_per_live, field_bytes_per_live):
+    """Bytes per live particle of one call: every live particle's data once,
+    the Bool index at 1 byte per slot, grid arrays once per call amortised
+    over the particles; movers (fraction m) re-read and re-write their
+    coordinates and fields."""
+    coords = 8 * N
+    idx = slots_per_live
+    if op == "advection!":
+        return 2 * coords + idx + grid_bytes_per_live
+    if op == "move_particles!":
+        return coords + idx + m * (2 * (coords + 8 * nf) + 2)
+    if op == "inject_particles!":
+        return coords + idx
+    if op == "grid2particle!":
+        return coords + idx + 8 + field_bytes_per_live
+    if op == "particle2grid!":
+        return coords + idx + 8 + field_bytes_per_live
+    raise KeyError(op)
+
+
+def launches(op, N):
+    return {"advection!": 1, "move_particles!": 2 + 3 ** N, "inject_particles!": 1 + 2 ** N,
+            "grid2particle!": 1, "particle2grid!": 1}[op]
 
 
 def _peaks():
@@ -118,10 +144,10 @@ def _dist():
     return world, rank, local
 
 
-def movers_fraction(jp, p, torch):
+def movers_fraction(p, torch):
     """Fraction of live particles outside their cell (after an advection!)."""
     idx = p.index.data.bool()
-    m, live = 0, int(idx.sum())
+    live = int(idx.sum())
     ncells = p.index.data.shape[1]
     cells = torch.arange(ncells, device="cuda")
     out = torch.zeros_like(idx)
@@ -134,15 +160,19 @@ def movers_fraction(jp, p, torch):
         lo, hi = xv[I], xv[I + 1]
         x = p.coords[d].data
         out |= ~((x > lo) & (x < hi))
-    m = int((out & idx).sum())
-    return m / max(1, live)
+    return int((out & idx).sum()) / max(1, live)
+
+
+def _setup_cfg(workload, ni):
+    from justpic_gb300 import workloads as W
+    base = W.CONFIGS[workload]["ni"]
+    return W.setup(workload, None if ni is None else (ni,) * len(base))
 
 
 def run_ours(args):
     import torch
 
     import justpic_gb300 as jp
-    from justpic_gb300 import workloads as W
 
     world, rank, local = _dist()
     if world > 1:
@@ -153,43 +183,55 @@ def run_ours(args):
         torch.cuda.set_device(0)
     jp._native.load()
 
-    cfg = W.setup(WORKLOAD, args.ni and (args.ni, args.ni))
+    cfg = _setup_cfg(args.workload, args.ni)
     g = cfg["grid"]
-    Vx, Vy = cfg["V"]
+    N = g["ndim"]
+    nf = 1 if "particle2grid!" in STEPS[args.workload] else 0
     dt = cfg["dt"]
     p = jp.init_particles(jp.CUDABackend, cfg["nxcell"], cfg["max_xcell"], cfg["min_xcell"], *g["grid_v"],
                           seed=jp.DEFAULT_SEED + rank)
-    pT, = jp.init_cell_arrays(p, 1)
-    V = (jp.TA("CUDA")(Vx), jp.TA("CUDA")(Vy))
+    fields = jp.init_cell_arrays(p, nf)
+    pT = fields[0] if nf else None
+    V = tuple(jp.TA("CUDA")(v) for v in cfg["V"])
     T = jp.TA("CUDA")(cfg["T"])
     method = jp.RungeKutta2()
-    jp.grid2particle_(pT, T, p)
+    if nf:
+        jp.grid2particle_(pT, T, p)
 
     stream = torch.cuda.current_stream()
-    ops = ["particle2grid!", "advection!", "move_particles!", "inject_particles!", "grid2particle!"]
+    ops = STEPS[args.workload]
+    Vcur = [V]
+
+    def call(op):
+        if op == "particle2grid!":
+            jp.particle2grid_(T, pT, p)
+        elif op == "advection!":
+            jp.advection_(p, method, Vcur[0], dt)
+        elif op == "move_particles!":
+            jp.move_particles_(p, fields)
+        elif op == "inject_particles!":
+            jp.inject_particles_(p, fields)
+        elif op == "grid2particle!":
+            jp.grid2particle_(pT, T, p)
 
     def step(ev=None):
-        calls = [
-            lambda: jp.particle2grid_(T, pT, p),
-            lambda: jp.advection_(p, method, V, dt),
-            lambda: jp.move_particles_(p, (pT,)),
-            lambda: jp.inject_particles_(p, (pT,)),
-            lambda: jp.grid2particle_(pT, T, p),
-        ]
-        for k, call in enumerate(calls):
+        for k, op in enumerate(ops):
             if ev is not None:
                 ev[k][0].record(stream)
-            call()
+            call(op)
             if ev is not None:
                 ev[k][1].record(stream)
 
     # movers fraction of this workload (measured once, outside the timed region)
-    jp.particle2grid_(T, pT, p)
+    if nf:
+        jp.particle2grid_(T, pT, p)
     jp.advection_(p, method, V, dt)
-    m = movers_fraction(jp, p, torch)
-    jp.move_particles_(p, (pT,))
-    jp.inject_particles_(p, (pT,))
-    jp.grid2particle_(pT, T, p)
+    m = movers_fraction(p, torch)
+    jp.move_particles_(p, fields)
+    if "inject_particles!" in ops:
+        jp.inject_particles_(p, fields)
+    if "grid2particle!" in ops:
+        jp.grid2particle_(pT, T, p)
 
     # ---- device-resident throughput (asynchronous calls) ----
     jp.set_synchronous(p, False)
@@ -225,34 +267,36 @@ def run_ours(args):
 
     # ---- end to end through the public API (synchronous, host buffers) ----
     jp.set_synchronous(p, True)
-    hVx = torch.from_numpy(np.ascontiguousarray(Vx.T)).pin_memory()
-    hVy = torch.from_numpy(np.ascontiguousarray(Vy.T)).pin_memory()
-    hT = torch.empty(tuple(reversed(T.shape)), dtype=torch.float64).pin_memory()
-    dVx = torch.empty_like(hVx, device="cuda")
-    dVy = torch.empty_like(hVy, device="cuda")
+    hV = [torch.from_numpy(np.ascontiguousarray(v.transpose(tuple(reversed(range(v.ndim)))))).pin_memory()
+          for v in cfg["V"]]
+    dV = [torch.empty_like(h, device="cuda") for h in hV]
+    rev = tuple(reversed(range(N)))
+    hT = torch.empty(tuple(reversed(T.shape)), dtype=torch.float64).pin_memory() if nf else None
     e2e_steps = max(1, min(args.steps, 50))
     torch.cuda.synchronize()
     w0 = time.perf_counter()
     for _ in range(e2e_steps):
-        dVx.copy_(hVx, non_blocking=True)
-        dVy.copy_(hVy, non_blocking=True)
-        Vstep = (dVx.T, dVy.T)
-        jp.particle2grid_(T, pT, p)
-        jp.advection_(p, method, Vstep, dt)
-        jp.move_particles_(p, (pT,))
-        jp.inject_particles_(p, (pT,))
-        jp.grid2particle_(pT, T, p)
-        hT.copy_(T.T, non_blocking=False)
+        for h, d in zip(hV, dV):
+            d.copy_(h, non_blocking=True)
+        Vcur[0] = tuple(d.permute(*rev) for d in dV)
+        step()
+        if nf:
+            hT.copy_(T.permute(*rev), non_blocking=False)
     torch.cuda.synchronize()
     e2e_time = time.perf_counter() - w0
+    Vcur[0] = V
     e2e_value = live * e2e_steps * world / e2e_time
 
     # ---- roofline of the dominant call ----
     peak, peak_kind = _peaks()
+    nvel_bytes = sum(v.size * 8 for v in cfg["V"])
+    slots_per_live = p.max_xcell * int(np.prod(p.ni)) / live
+    gb = nvel_bytes / live
+    fb = T.numel() * 8 / live
+    bpp = {op: algorithmic_bytes(op, N, nf, m, slots_per_live, gb, fb) for op in ops}
     dom = max(op_ms, key=op_ms.get)
-    bytes_dom = BYTES[dom](m) * live
-    achieved = bytes_dom / (op_ms[dom] / 1e3) / 1e9
-    step_bytes = sum(BYTES[o](m) for o in ops) * live
+    achieved = bpp[dom] * live / (op_ms[dom] / 1e3) / 1e9
+    step_bytes = sum(bpp.values()) * live
     step_gbs = step_bytes / (elapsed / args.steps) / 1e9
 
     result = {
@@ -267,19 +311,19 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (seeded analytic rigid-rotation workload; no public dataset exists)",
+        "data": "synthetic (seeded analytic flow; the reference publishes no dataset)",
         "config": {
-            "workload": "C2: 2D temperature advection FP64, 1024x1024 cells, 24/48/12 particles per cell, "
-                        "rigid rotation, RK2, step = particle2grid!+advection!+move_particles!+"
-                        "inject_particles!+grid2particle!",
-            "cells": [1024, 1024],
+            "workload": DESC[args.workload] if args.ni is None else DESC[args.workload] + f" (resized to {args.ni} "
+                                                                                         "cells per axis)",
+            "cells": list(p.ni),
             "live_particles": live,
             "dt": dt,
             "movers_fraction": m,
-            "l2": "inputs larger than L2 (coordinates alone 805 MB)",
-            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "inputs larger than L2 (the coordinate arrays alone exceed 129 MB)",
+            "parallelism": "independent replicas" if world > 1 else "single GPU",
         },
         "per_call_ms": op_ms,
+        "algorithmic_bytes_per_particle": bpp,
         "step_algorithmic_gbs": step_gbs,
         "roofline": {
             "bound": "hbm",
@@ -288,75 +332,81 @@ def run_ours(args):
             "peak": peak,
             "unit": "GB/s",
             "frac": achieved / peak,
-            "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
+            "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
             else "fallback 6.8 TB/s",
-            "bytes_per_particle": BYTES[dom](m),
             "traffic": None,
         },
         "e2e": {
             "value": e2e_value,
             "unit": UNIT,
-            "h2d_bytes_per_step": int(hVx.numel() * 8 + hVy.numel() * 8),
-            "d2h_bytes_per_step": int(hT.numel() * 8),
+            "h2d_bytes_per_step": int(sum(h.numel() * 8 for h in hV)),
+            "d2h_bytes_per_step": int(hT.numel() * 8) if nf else 0,
             "steps": e2e_steps,
-            "mode": "public API, synchronous calls, velocity in / vertex temperature out each step",
+            "mode": "public API, synchronous calls; velocity grids in and (with fields) the vertex field out each step",
         },
-        "gpu_launches": sum(LAUNCHES_PER_STEP.values()) * args.steps,
+        "gpu_launches": sum(launches(op, N) for op in ops) * args.steps,
         "clocks": clocks.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+        result["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)
     if world > 1:
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(result))
 
 
-def _cpu_setup():
-    from justpic_gb300 import workloads as W
+def _cpu_setup(workload):
     from oracle import oracle as O
 
-    cfg = W.setup(WORKLOAD)
+    cfg = _setup_cfg(workload, None)
     g = cfg["grid"]
+    ops = STEPS[workload]
+    nf = 1 if "particle2grid!" in ops else 0
     grids = tuple(tuple(np.asarray(x) for x in comp) for comp in g["grid_v"])
     o = O.OracleParticles(grids, cfg["nxcell"], cfg["max_xcell"], cfg["min_xcell"], uniform=True)
     o.init_particles()
-    oT = o.cell_array()
+    fields = [o.cell_array() for _ in range(nf)]
     T = np.asfortranarray(cfg["T"].copy())
-    o.grid2particle(oT, T)
+    if nf:
+        o.grid2particle(fields[0], T)
     V = cfg["V"]
     dt = cfg["dt"]
 
     def step():
-        o.particle2grid(T, oT)
-        o.advection(O.RK2, 0.5, V, dt)
-        o.move_particles((oT,))
-        o.inject_particles((oT,))
-        o.grid2particle(oT, T)
+        for op in ops:
+            if op == "particle2grid!":
+                o.particle2grid(T, fields[0])
+            elif op == "advection!":
+                o.advection(O.RK2, 0.5, V, dt)
+            elif op == "move_particles!":
+                o.move_particles(fields)
+            elif op == "inject_particles!":
+                o.inject_particles(fields)
+            elif op == "grid2particle!":
+                o.grid2particle(fields[0], T)
 
     return o, step
 
 
-def cpu_baseline(seconds=20.0, max_steps=None):
+def cpu_baseline(workload="C2", seconds=20.0, max_steps=None):
     """The FP64 C restatement of the reference's CPU path, all host threads, on
     the same workload; times whole steps until ``seconds`` of CPU work."""
     from oracle import oracle as O
 
     cores = os.cpu_count() or 1
     O.set_threads(cores)
-    o, step = _cpu_setup()
+    o, step = _cpu_setup(workload)
     step()  # warm-up (page faults, thread pool)
-    n, t = 0, 0.0
+    n, t, live_sum = 0, 0.0, 0
     while t < seconds and (max_steps is None or n < max_steps):
-        live = int(o.index.sum())
+        live_sum += int(o.index.sum())
         w0 = time.perf_counter()
         step()
         t += time.perf_counter() - w0
         n += 1
-    value = live * n / t
-    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{n} full C2 steps (1024x1024 cells, ~25M particles) in {t:.1f} s with {cores} OpenMP "
-                      "threads; C restatement of the reference's FP64 CPU path (Julia is not available)"}
+    return {"value": live_sum / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} full {workload} steps in {t:.1f} s with {cores} OpenMP threads; FP64 C restatement of "
+                      "the reference's CPU path (Julia is not available)"}
 
 
 def run_reference(args):
@@ -367,12 +417,11 @@ def run_reference(args):
 
     cores = os.cpu_count() or 1
     O.set_threads(cores)
-    o, step = _cpu_setup()
+    o, step = _cpu_setup(args.workload)
     for _ in range(max(0, min(args.warmup, 1))):
         step()
     budget = 90.0
-    n, t = 0, 0.0
-    live_sum = 0
+    n, t, live_sum = 0, 0.0, 0
     while n < args.steps and (t < budget or n == 0):
         live_sum += int(o.index.sum())
         w0 = time.perf_counter()
@@ -393,12 +442,11 @@ def run_reference(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (seeded analytic rigid-rotation workload)",
-        "config": {"workload": "C2: 2D temperature advection FP64, 1024x1024 cells, 24/48/12 particles per "
-                               "cell, rigid rotation, RK2, five calls per step", "cells": [1024, 1024]},
+        "data": "synthetic (seeded analytic flow; the reference publishes no dataset)",
+        "config": {"workload": DESC[args.workload]},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{n} of {args.steps} requested full steps timed (capped at {budget:.0f} s); "
-                                   "FP64 C restatement of JustPIC.CPU (Julia is not installed)"},
+                                   "FP64 C restatement of JustPIC's CPU path (Julia is not installed)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -409,10 +457,11 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(STEPS), default="C2")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ni", type=int, default=None,
-                    help="cells per axis instead of 1024 (small cases for ncu captures; not a bench line)")
+                    help="cells per axis instead of the workload's (small cases for ncu captures; not a bench line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -24,6 +24,7 @@ constexpr int kThreads = 256;
 // re-examined as a mover when that cell is walked), 0x3F = leaves / dropped.
 constexpr uint8_t kCodeExit = 0x3F;
 constexpr uint8_t kCodeUnstable = 0x40;
+constexpr uint8_t kCodeStay = 0x80;  // live slot that did not move (never read as a destination)
 
 // Geometry of a container, passed to kernels by value.
 struct DevGrid {

@@ -31,6 +31,8 @@
 
 namespace jp {
 
+constexpr int kAllocThreads = 64;  // small blocks spread the sparse colour passes over all SMs
+
 struct MoveView {
     uint64_t* L0;
     uint64_t* L;
@@ -41,6 +43,7 @@ struct MoveView {
     uint16_t* orig;
     double* shadow;
     int64_t nslots;
+    int comps;  // values per shadow record: DIM coordinates, then the fields (records are interleaved)
 };
 
 // find_parent_cell_bisection with integer-key comparisons (px not NaN):
@@ -119,10 +122,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             kp[d] = okey(p[d]);
             pnan |= is_nan_bits(p[d]);
         }
+        // The shadow copy is written for every live slot, movers or not: whole
+        // 32-byte sectors reach memory instead of partial ones that L2 would
+        // first have to read back from DRAM.
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) S.shadow[a * S.comps + d] = p[d];
+        for (int j = 0; j < A.n; ++j) S.shadow[a * S.comps + DIM + j] = A.a[j][a];
         bool in = !pnan;  // isincell, strict (src/Particles/utils.jl:7-15)
 #pragma unroll
         for (int d = 0; d < DIM; ++d) in = in & (cellk[w][l][d] < kp[d]) & (kp[d] < cellk[w][l][DIM + d]);
-        if (in) continue;  // move_safe.jl:93
+        if (in) {  // move_safe.jl:93
+            S.code[a] = kCodeStay;
+            continue;
+        }
         atomicOr(&movers[w][l], 1ull << s);
         bool inside = !pnan;  // indomain, strict (move_safe.jl:199-206)
 #pragma unroll
@@ -145,9 +157,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             } else {
                 code = (uint8_t)nb_code<DIM>(off);
                 if (!inT) code |= kCodeUnstable;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) S.shadow[d * S.nslots + a] = p[d];
-                for (int j = 0; j < A.n; ++j) S.shadow[(DIM + j) * S.nslots + a] = A.a[j][a];
             }
         }
         S.code[a] = code;
@@ -166,11 +175,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 
 // -------------------------------------------------------------- allocate
 // One colour pass of move_particles!: sources 3*J + o, neighbourhoods
-// disjoint, so every mask touched here belongs to exactly one thread.
+// disjoint, so every mask touched here belongs to exactly one thread. The
+// destination codes and the masks of every neighbour the walk will touch are
+// loaded up front (independent loads), the walk then runs on thread-local
+// copies, and the touched masks are written back at the end.
 template <int DIM>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kAllocThreads)
     move_allocate(DevGrid g, MoveView S, int o0, int o1, int o2, int64_t m0, int64_t m1, int64_t m2)
 {
+    constexpr int NB = DIM == 2 ? 9 : 27;
+    constexpr int CENTER = DIM == 2 ? 4 : 13;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= m0 * m1 * m2) return;
     int64_t idx[3];
@@ -183,93 +197,118 @@ __global__ void __launch_bounds__(kThreads)
     const int64_t nc = g.ncells;
     const int64_t sc = cell_linear<DIM>(g, idx);
     const uint64_t Mv = S.M[sc];
-    uint64_t U = S.U[sc];
-    if (Mv == 0 && U == 0) return;
-    uint64_t L = S.L[sc], R = S.R[sc];
+    const uint64_t U0 = S.U[sc];
+    if (Mv == 0 && U0 == 0) return;
+    uint64_t nL[NB], nR[NB], nU[NB];
+    uint8_t codes[64];
+    nL[CENTER] = S.L[sc];
+    nR[CENTER] = S.R[sc];
+    nU[CENTER] = U0;
+    uint32_t touched = 1u << CENTER;
+    // codes of the original movers (slots not refilled by an earlier pass)
+    uint64_t orig_movers = Mv & ~nR[CENTER];
+    for (uint64_t m = orig_movers; m; m &= m - 1) {
+        const int s = __ffsll((long long)m) - 1;
+        const uint8_t cb = S.code[sc + nc * s];
+        codes[s] = cb;
+        if (cb != kCodeExit) touched |= 1u << (cb & 0x1F);
+    }
+    for (uint32_t m = touched & ~(1u << CENTER); m; m &= m - 1) {
+        const int nb = __ffs(m) - 1;
+        int off[3];
+        nb_offset<DIM>(nb, off);
+        const int64_t J[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
+        const int64_t jc = cell_linear<DIM>(g, J);
+        nL[nb] = S.L[jc];
+        nR[nb] = S.R[jc];
+        nU[nb] = S.U[jc];
+    }
     const int nslot = g.max_xcell;
     const uint64_t valid = nslot == 64 ? ~0ull : ((1ull << nslot) - 1);
     int sp = 0;  // starting_point (move_safe.jl:83)
     int cur = 0;
     while (cur < nslot) {
-        uint64_t cand = L & ((Mv & ~R) | (R & U)) & (~0ull << cur);
+        const uint64_t L = nL[CENTER], R = nR[CENTER], U = nU[CENTER];
+        const uint64_t cand = L & ((Mv & ~R) | (R & U)) & (~0ull << cur);
         if (!cand) break;
         const int s = __ffsll((long long)cand) - 1;
         cur = s + 1;
         const uint64_t bit = 1ull << s;
         int code;
         bool unstable;
-        bool from_refill = (R & bit) != 0;
+        const bool from_refill = (R & bit) != 0;
         uint16_t tag = 0;
         if (from_refill) {
-            code = self_code<DIM>();
+            code = CENTER;
             unstable = true;
             tag = S.orig[sc + nc * s];
         } else {
-            const uint8_t cb = S.code[sc + nc * s];
+            const uint8_t cb = codes[s];
             if (cb == kCodeExit) {  // left the domain (or moved too far): cleared
-                L &= ~bit;
+                nL[CENTER] = L & ~bit;
                 continue;
             }
             code = cb & 0x1F;
             unstable = (cb & kCodeUnstable) != 0;
-        }
-        // remove the particle from its slot (move_safe.jl:110-112)
-        L &= ~bit;
-        R &= ~bit;
-        U &= ~bit;
-        int off[3];
-        nb_offset<DIM>(code, off);
-        int64_t T[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
-        const int64_t tc = cell_linear<DIM>(g, T);
-        if (!from_refill) {
+            int off[3];
+            nb_offset<DIM>(code, off);
             const int back[3] = {-off[0], -off[1], -off[2]};
             tag = (uint16_t)(nb_code<DIM>(back) | (s << 5));
         }
-        const bool same = tc == sc;
-        uint64_t LT = same ? L : S.L[tc];
+        // remove the particle from its slot (move_safe.jl:110-112)
+        nL[CENTER] = L & ~bit;
+        nR[CENTER] = R & ~bit;
+        nU[CENTER] = U & ~bit;
         // find_free_memory(starting_point, ...) (move_safe.jl:192-197)
-        const uint64_t freem = ~LT & valid & (~0ull << sp);
+        const uint64_t freem = ~nL[code] & valid & (~0ull << sp);
         if (!freem) continue;  // dropped: no free slot at or after starting_point
         const int f = __ffsll((long long)freem) - 1;
         sp = f;
         const uint64_t fb = 1ull << f;
-        uint64_t RT = same ? R : S.R[tc];
-        uint64_t UT = same ? U : S.U[tc];
-        LT |= fb;
-        RT |= fb;
-        UT = unstable ? (UT | fb) : (UT & ~fb);
-        S.orig[tc + nc * f] = tag;
-        if (same) {
-            L = LT;
-            R = RT;
-            U = UT;
-        } else {
-            S.L[tc] = LT;
-            S.R[tc] = RT;
-            S.U[tc] = UT;
-        }
+        nL[code] |= fb;
+        nR[code] |= fb;
+        nU[code] = unstable ? (nU[code] | fb) : (nU[code] & ~fb);
+        int off[3];
+        nb_offset<DIM>(code, off);
+        const int64_t T[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
+        S.orig[cell_linear<DIM>(g, T) + nc * f] = tag;
     }
-    S.L[sc] = L;
-    S.R[sc] = R;
-    S.U[sc] = U;
+    for (uint32_t m = touched; m; m &= m - 1) {
+        const int nb = __ffs(m) - 1;
+        int off[3];
+        nb_offset<DIM>(nb, off);
+        const int64_t J[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
+        const int64_t jc = cell_linear<DIM>(g, J);
+        S.L[jc] = nL[nb];
+        S.R[jc] = nR[nb];
+        S.U[jc] = nU[nb];
+    }
 }
 
 // ----------------------------------------------------------------- apply
+// Slot-major over a warp's 32 cells: at each slot the lanes whose slot changed
+// store together, so every 32-byte sector is written in one go.
 template <int DIM>
 __global__ void __launch_bounds__(kThreads)
     move_apply(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, MoveView S)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.ncells) return;
-    const uint64_t L0 = S.L0[c], L = S.L[c], R = S.R[c];
-    uint64_t changed = (L0 & ~L) | R;
-    if (!changed) return;
-    int64_t I[3];
-    cell_coords(g, c, I);
     const int64_t nc = g.ncells;
-    while (changed) {
-        const int s = __ffsll((long long)changed) - 1;
-        changed &= changed - 1;
+    const bool valid = c < nc;
+    uint64_t L0 = 0, L = 0, R = 0;
+    if (valid) {
+        L0 = S.L0[c];
+        L = S.L[c];
+        R = S.R[c];
+    }
+    uint64_t changed = (L0 & ~L) | R;
+    // slots past the highest changed slot of any lane need no visit
+    const uint32_t hi_any = __reduce_max_sync(0xffffffffu, changed ? 64u - (uint32_t)__clzll((long long)changed) : 0u);
+    if (hi_any == 0) return;
+    int64_t I[3] = {0, 0, 0};
+    if (valid) cell_coords(g, c, I);
+    for (int s = 0; s < (int)hi_any; ++s) {
+        if (!((changed >> s) & 1)) continue;
         const int64_t a = c + nc * s;
         if ((R >> s) & 1) {
             const uint16_t tag = S.orig[a];
@@ -278,8 +317,8 @@ __global__ void __launch_bounds__(kThreads)
             const int64_t J[3] = {I[0] + off[0], I[1] + off[1], DIM == 3 ? I[2] + off[2] : 0};
             const int64_t b = cell_linear<DIM>(g, J) + nc * (tag >> 5);
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) X.c[d][a] = S.shadow[d * S.nslots + b];
-            for (int k = 0; k < A.n; ++k) A.a[k][a] = S.shadow[(DIM + k) * S.nslots + b];
+            for (int d = 0; d < DIM; ++d) X.c[d][a] = S.shadow[b * S.comps + d];
+            for (int k = 0; k < A.n; ++k) A.a[k][a] = S.shadow[b * S.comps + DIM + k];
             index[a] = 1;
         } else {
 #pragma unroll
@@ -360,30 +399,54 @@ __device__ __forceinline__ double warp_min(double v)
     return v;
 }
 
-// Per-warp shared-memory image of a cell's 3^N neighbourhood: coordinates
-// and occupancy of every candidate slot, plus the squared distances of the
-// current search.
+// Per-warp shared-memory image of a cell's 3^N neighbourhood: occupancy and
+// FP32 coordinates relative to the cell's lower-left vertex for every
+// candidate slot, the FP64 coordinates of the cell's own slots, and the FP32
+// squared distances of the current search.
 template <int DIM>
 struct Hood {
-    double* x[DIM];
-    double* ss;
-    uint8_t* live;
+    float* r[DIM];     // candidate coordinate minus the cell corner, rounded to FP32
+    float* ss32;       // FP32 squared distance of the current search (-1: evaluate in FP64)
+    double* own[DIM];  // FP64 coordinates of the cell's own slots
+    uint8_t* live;     // 0 empty, 1 live, 2 live but too far for the FP32 screen
 };
 
 template <int DIM>
 __host__ __device__ __forceinline__ size_t hood_bytes(int M)
 {
     const int n = (DIM == 2 ? 9 : 27) * M;
-    const size_t bytes = (size_t)n * (DIM * sizeof(double) + sizeof(double) + 1);
-    return (bytes + 15) & ~(size_t)15;  // keep every warp's doubles 16-byte aligned
+    const size_t bytes = (size_t)M * DIM * sizeof(double) + (size_t)n * ((DIM + 1) * sizeof(float) + 1);
+    return (bytes + 15) & ~(size_t)15;  // keep every warp's arrays 16-byte aligned
+}
+
+template <int DIM>
+__device__ __forceinline__ double candidate_ss(const DevGrid& g, const Coords& X, const Hood<DIM>& H,
+                                               const int64_t* I, int o, int M, const double* pn)
+{
+    constexpr int CENTER = DIM == 2 ? 4 : 13;
+    const int nb = o / M, s = o - nb * M;
+    double e[3];
+    if (nb == CENTER) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) e[d] = H.own[d][s] - pn[d];
+    } else {
+        const int64_t J[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1, DIM == 3 ? I[2] + nb / 9 - 1 : 0};
+        const int64_t a = cell_linear<DIM>(g, J) + g.ncells * s;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) e[d] = X.c[d][a] - pn[d];
+    }
+    return DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
 }
 
 // _inject_particles! (src/Particles/injection.jl:68-131) for one cell, by one warp.
 // The nearest-neighbour result of index_min_distance (injection.jl:330-393) is
 // the first candidate, in the reference's k -> j -> i -> slot order, whose
-// distance sqrt(ss) equals the minimum: the lanes find the minimum ss over
-// the staged candidates, then only candidates within rounding of it
-// evaluate sqrt.
+// FP64 distance sqrt(ss) equals the minimum. An FP32 screen finds it without
+// FP64 work on every candidate: with an absolute error bound E on the FP32
+// squared distances, only candidates whose FP32 value is within
+// (min + E)(1 + tol) + E can be at (or within rounding of) the FP64 minimum;
+// those, and any candidate too far from the cell for the bound to hold, are
+// evaluated exactly in FP64, then sqrt decides the tie-break as in the reference.
 template <int DIM>
 __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __restrict__ index, const Args& A,
                                  uint32_t call, int64_t c, const Hood<DIM>& H, int lane, int* errs)
@@ -395,6 +458,23 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
     const int ncand = NB * M;
     int64_t I[3];
     cell_coords(g, c, I);
+    double corner[3], dq[3];
+    float hmax[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        corner[d] = ldg(g.xv[d] + I[d]);
+        const double dx = ldg(g.dxv[d] + I[d]);
+        dq[d] = dx / 2.0;
+        double h = dx;
+        if (I[d] > 0) h = fmax(h, ldg(g.dxv[d] + I[d] - 1));
+        if (I[d] + 1 < g.n[d]) h = fmax(h, ldg(g.dxv[d] + I[d] + 1));
+        hmax[d] = (float)h;
+    }
+    // the FP32 screen needs spacings well inside FP32 range; otherwise every
+    // candidate is evaluated in FP64
+    bool screen_ok = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) screen_ok &= hmax[d] >= 1e-12f && hmax[d] <= 1e12f;
     // stage the neighbourhood
     for (int o = lane; o < ncand; o += 32) {
         const int nb = o / M, s = o - nb * M;
@@ -406,19 +486,26 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
             const int64_t a = cell_linear<DIM>(g, J) + nc * s;
             live = index[a];
             if (live) {
+                bool far = false;
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) H.x[d][o] = X.c[d][a];
+                for (int d = 0; d < DIM; ++d) {
+                    const double x = X.c[d][a];
+                    const float r = (float)(x - corner[d]);
+                    H.r[d][o] = r;
+                    far |= (!(fabsf(r) <= 4.0f * hmax[d]) && !isnan(r)) || !screen_ok;
+                    if (nb == CENTER) H.own[d][s] = x;
+                }
+                live = far ? 2 : 1;
             }
         }
         H.live[o] = live;
     }
     __syncwarp();
-    double corner[3], dq[3];
+    // E: bound on |ss32 - ss64| for screened candidates (|r| <= 4h, new point inside the cell)
+    float E = 0.0f;
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-        corner[d] = ldg(g.xv[d] + I[d]);
-        dq[d] = ldg(g.dxv[d] + I[d]) / 2.0;
-    }
+    for (int d = 0; d < DIM; ++d) E += 36.0f * hmax[d] * hmax[d];
+    E *= 0x1.0p-16f;
     const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
     const int base = CENTER * M;
     for (int q = 0; q < (1 << DIM); ++q) {
@@ -436,7 +523,7 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
             bool in = true;
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
-                const double x = H.x[d][base + s];
+                const double x = H.own[d][s];
                 const long long k = okey(x);
                 in = in & !is_nan_bits(x) & (klo[d] < k) & (k < khi[d]);
             }
@@ -452,50 +539,76 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
             freem &= freem - 1;
             ++count;
             double pn[3];
+            float pr[3];
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
                 const double r = jp_rand_uniform(g.seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)i,
                                                  (uint32_t)d);
                 pn[d] = qc[d] + dq[d] * fma(0.95, r, 0.05);  // new_particle, injection.jl:411-417
+                pr[d] = (float)(pn[d] - corner[d]);
             }
             const int64_t ai = c + nc * i;
             if (lane == 0) {
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) {
                     X.c[d][ai] = pn[d];
-                    H.x[d][base + i] = pn[d];
+                    H.own[d][i] = pn[d];
+                    H.r[d][base + i] = pr[d];
                 }
                 index[ai] = 1;
                 H.live[base + i] = 1;
             }
             __syncwarp();
-            // pass 1: squared distances of every candidate, lane-strided
-            double lmin = CUDART_INF;
+            // screen: FP32 squared distances
+            float lmin = CUDART_INF_F;
             for (int o = lane; o < ncand; o += 32) {
-                double ss = CUDART_INF;
-                if (H.live[o] && o != base + i) {
-                    double e[3];
+                float s32 = CUDART_NAN_F;  // not a candidate: fails every screen test
+                const uint8_t lv = H.live[o];
+                if (lv && o != base + i) {
+                    if (lv == 2) {
+                        s32 = -1.0f;
+                    } else {
+                        float t = 0.0f;
 #pragma unroll
-                    for (int d = 0; d < DIM; ++d) e[d] = H.x[d][o] - pn[d];
-                    const double t = DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
-                    if (!isnan(t)) ss = t;
+                        for (int d = 0; d < DIM; ++d) {
+                            const float e = H.r[d][o] - pr[d];
+                            t += e * e;
+                        }
+                        s32 = t;  // NaN coordinates give NaN and never pass the screen
+                        lmin = fminf(lmin, t);
+                    }
                 }
-                H.ss[o] = ss;
-                lmin = fmin(lmin, ss);
+                H.ss32[o] = s32;
             }
-            const double best = warp_min(lmin);
+            float m32 = lmin;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) m32 = fminf(m32, __shfl_xor_sync(0xffffffffu, m32, off));
+            const float thr = (m32 + E) * (1.0f + 0x1.0p-20f) + E;
             __syncwarp();
+            // exact FP64 distances of the screened candidates
+            double lbest = CUDART_INF;
+            for (int o = lane; o < ncand; o += 32) {
+                const float s32 = H.ss32[o];
+                if (s32 < 0.0f || s32 <= thr) {
+                    const double ss = candidate_ss<DIM>(g, X, H, I, o, M, pn);
+                    if (!isnan(ss)) lbest = fmin(lbest, ss);
+                }
+            }
+            const double best = warp_min(lbest);
             int64_t src = -1;
             if (best < CUDART_INF) {
-                // pass 2: the first candidate (in order) whose rounded distance equals sqrt(best)
+                // the first candidate (in order) whose rounded distance equals sqrt(best)
                 const double dmin = sqrt(best);
                 const double bound = best * (1.0 + 0x1.0p-48);
                 int lo = 0x7fffffff;
                 for (int o = lane; o < ncand; o += 32) {
-                    const double ss = H.ss[o];
-                    if (ss <= bound && sqrt(ss) == dmin) {
-                        lo = o;
-                        break;  // lane-strided order: the first hit is this lane's smallest
+                    const float s32 = H.ss32[o];
+                    if (s32 < 0.0f || s32 <= thr) {
+                        const double ss = candidate_ss<DIM>(g, X, H, I, o, M, pn);
+                        if (ss <= bound && sqrt(ss) == dmin) {
+                            lo = o;
+                            break;  // lane-strided order: the first hit is this lane's smallest
+                        }
                     }
                 }
                 const int win = __reduce_min_sync(0xffffffffu, lo);
@@ -527,9 +640,12 @@ __global__ void inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Ar
     unsigned char* base = smem_inject + (size_t)wib * hood_bytes<DIM>(M);
     Hood<DIM> H;
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) H.x[d] = (double*)base + (size_t)d * ncand;
-    H.ss = (double*)base + (size_t)DIM * ncand;
-    H.live = base + (size_t)(DIM + 1) * ncand * sizeof(double);
+    for (int d = 0; d < DIM; ++d) H.own[d] = (double*)base + (size_t)d * M;
+    float* fb = (float*)(base + (size_t)DIM * M * sizeof(double));
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) H.r[d] = fb + (size_t)d * ncand;
+    H.ss32 = fb + (size_t)DIM * ncand;
+    H.live = (uint8_t*)(fb + (size_t)(DIM + 1) * ncand);
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int count = Ls.counts[col];
@@ -589,24 +705,24 @@ cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index
     A.n = nargs;
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
     const MoveScratch& m = P->move;
-    MoveView S{m.L0, m.L, m.M, m.R, m.U, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell};
+    MoveView S{m.L0, m.L, m.M, m.R, m.U, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, N + nargs};
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(P->g.ncells);
     const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
     const int ntw = 32 * kWarpsPerBlock;
     int64_t mc[3] = {1, 1, 1};
     for (int d = 0; d < N; ++d) mc[d] = (P->g.n[d] + 2) / 3;  // ceil(n/3)
-    const unsigned nbp = grid_blocks(mc[0] * mc[1] * mc[2]);
+    const unsigned nbp = grid_blocks(mc[0] * mc[1] * mc[2], kAllocThreads);
     if (N == 2) {
         move_classify<2><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
         for (int pass = 0; pass < 9; ++pass)  // offsetᵢ outer, offsetⱼ inner (move_safe.jl:32)
-            move_allocate<2><<<nbp, kThreads, 0, st>>>(P->g, S, pass / 3, pass % 3, 0, mc[0], mc[1], 1);
+            move_allocate<2><<<nbp, kAllocThreads, 0, st>>>(P->g, S, pass / 3, pass % 3, 0, mc[0], mc[1], 1);
         move_apply<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     } else {
         move_classify<3><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
         for (int pass = 0; pass < 27; ++pass)  // i outer, k inner (move_safe.jl:39)
-            move_allocate<3><<<nbp, kThreads, 0, st>>>(P->g, S, pass / 9, (pass / 3) % 3, pass % 3, mc[0], mc[1],
-                                                       mc[2]);
+            move_allocate<3><<<nbp, kAllocThreads, 0, st>>>(P->g, S, pass / 9, (pass / 3) % 3, pass % 3, mc[0],
+                                                            mc[1], mc[2]);
         move_apply<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     }
     return cudaGetLastError();
@@ -644,7 +760,7 @@ cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* ind
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
     const unsigned nb = grid_blocks(nc);
     const int M = P->g.max_xcell;
-    const int wpb = N == 2 ? 4 : 1;  // warps per block of the pass kernels
+    const int wpb = N == 2 ? 4 : 2;  // warps per block of the pass kernels
     const size_t smem = N == 2 ? wpb * hood_bytes<2>(M) : wpb * hood_bytes<3>(M);
     // enough warps to keep every SM busy; each strides over its colour's list
     const unsigned nbp = (unsigned)(152 * (N == 2 ? 8 : 16));

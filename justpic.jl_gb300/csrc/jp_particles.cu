@@ -81,10 +81,19 @@ __device__ __forceinline__ double interp_component(const DevGrid& g, int comp, c
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         const double* x = g.xvel[comp][d];
-        const double a = ldg(x + I[d]), b = ldg(x + I[d] + 1);
-        if (!pnan && okey(a) <= kp[d] && kp[d] <= okey(b)) {
-            idx[d] = I[d];
+        const int J = I[d];
+        const double a = ldg(x + J), b = ldg(x + J + 1);
+        const long long ka = okey(a), kb = okey(b);
+        if (!pnan && ka <= kp[d] && kp[d] <= kb) {  // the reference's first test (closed interval)
+            idx[d] = J;
             xc[d] = a;
+        } else if (!pnan && kb < kp[d] && J + 2 < g.nvel[comp][d] && kp[d] < okey(ldg(x + J + 2))) {
+            // strictly inside the next interval: the only answer the bisection can give
+            idx[d] = J + 1;
+            xc[d] = b;
+        } else if (!pnan && kp[d] < ka && J >= 1 && okey(ldg(x + J - 1)) < kp[d]) {
+            idx[d] = J - 1;  // strictly inside the previous interval
+            xc[d] = ldg(x + J - 1);
         } else {
 #pragma unroll
             for (int e = 0; e < DIM; ++e)
@@ -272,24 +281,35 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 // src/Interpolations/particle_to_grid.jl:37-68 (2D), :113-151 (3D).
 // One thread per vertex column marching along the last axis over `chunk`
 // vertex rows: the cells of row r are read once and feed both vertex r (its
-// upper half of the stencil) and vertex r+1 (its lower half), so every
-// vertex accumulates its cells in the reference's order (offsets of the last
-// axis outermost, x innermost, slots in order) and the sums are bit-identical.
-template <int DIM>
-__device__ __forceinline__ void p2g_cell(const DevGrid& g, int64_t c, const double* q_cur, const double* q_nxt,
-                                         bool has_next, const double* __restrict__ Fp, const CCoords& X,
-                                         const uint8_t* __restrict__ index, double& w_c, double& wF_c,
-                                         double& w_n, double& wF_n)
+// upper half of the stencil) and vertex r+1 (its lower half), so every vertex
+// accumulates its cells in the reference's order (offsets of the last axis
+// outermost, x innermost, slots in order) and the sums are bit-identical. Each
+// cell is walked through its 64-bit live mask, so no lane spends FP64 issue
+// slots on empty slots; the mask of the left neighbour cell comes from the
+// neighbouring lane. The loop trip count is the same for every lane of a warp.
+__device__ __forceinline__ uint64_t live_mask(const uint8_t* __restrict__ index, int64_t c, int64_t nc, int M)
 {
-    const int64_t nc = g.ncells;
-    for (int s = 0; s < g.max_xcell; ++s) {
+    uint64_t m = 0;
+#pragma unroll 8
+    for (int s = 0; s < M; ++s) m |= (uint64_t)(index[c + nc * s] != 0) << s;
+    return m;
+}
+
+template <int DIM>
+__device__ __forceinline__ void p2g_cell(int64_t c, uint64_t mask, int64_t nc, const double* q_cur,
+                                         const double* q_nxt, bool do_cur, bool do_nxt,
+                                         const double* __restrict__ Fp, const CCoords& X, double& w_c,
+                                         double& wF_c, double& w_n, double& wF_n)
+{
+    while (mask) {
+        const int s = __ffsll((long long)mask) - 1;
+        mask &= mask - 1;
         const int64_t a = c + nc * s;
-        if (!index[a]) continue;
         double p[3];
 #pragma unroll
         for (int d = 0; d < DIM; ++d) p[d] = X.c[d][a];
         const double f = Fp[a];
-        {
+        if (do_cur) {
             double ss;
             const double dx = q_cur[0] - p[0], dy = q_cur[1] - p[1];
             if (DIM == 2) {
@@ -299,11 +319,11 @@ __device__ __forceinline__ void p2g_cell(const DevGrid& g, int64_t c, const doub
                 ss = (dx * dx + dy * dy) + dz * dz;
             }
             const double dist = __dsqrt_rn(ss);
-            const double wi = __drcp_rn(dist * dist);
+            const double wi = __drcp_rn(dist * dist);  // inv(distance^2), particle_to_grid.jl:203-205
             w_c += wi;
             wF_c = fma(wi, f, wF_c);
         }
-        if (has_next) {
+        if (do_nxt) {
             double ss;
             const double dx = q_nxt[0] - p[0], dy = q_nxt[1] - p[1];
             if (DIM == 2) {
@@ -323,69 +343,72 @@ __device__ __forceinline__ void p2g_cell(const DevGrid& g, int64_t c, const doub
 template <int DIM>
 __global__ void __launch_bounds__(kThreads)
     p2g_kernel(DevGrid g, double* __restrict__ F, const double* __restrict__ Fp, CCoords X,
-               const uint8_t* __restrict__ index, int chunk)
+               const uint8_t* __restrict__ index, int chunk, int64_t nthreads)
 {
     const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
     constexpr int LAST = DIM - 1;
     const int64_t nlast = g.n[LAST];  // cells along the marching axis
     const int64_t cols = DIM == 2 ? V0 : V0 * V1;
-    const int64_t col = t % cols;
-    const int64_t q = t / cols;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    const bool active = t < nthreads;
+    const int64_t col = active ? t % cols : 0;
+    const int64_t q = active ? t / cols : 0;
     const int64_t r0 = q * chunk;
-    if (r0 > nlast) return;  // vertex rows along the last axis: 0..nlast
-    const int64_t r1 = min(r0 + (int64_t)chunk, nlast + 1);
+    const int64_t r1 = active ? min(r0 + (int64_t)chunk, nlast + 1) : r0;
     const int64_t i = col % V0;
     const int64_t j = DIM == 3 ? col / V0 : 0;
-    double qv[3];
-    qv[0] = ldg(g.xv[0] + i);
-    if (DIM == 3) qv[1] = ldg(g.xv[1] + j);
+    const bool has_i0 = i >= 1, has_i1 = i < g.n[0];          // cells i-1 and i exist
+    const bool has_j0 = DIM == 2 || j >= 1, has_j1 = DIM == 2 || j < g.n[1];
+    double q_cur[3], q_nxt[3];
+    q_cur[0] = q_nxt[0] = ldg(g.xv[0] + i);
+    if (DIM == 3) q_cur[1] = q_nxt[1] = ldg(g.xv[1] + j);
 
-    // the (up to) 2^(DIM-1) cells of one row/layer, in reference order
-    int64_t cells[4];
-    int ncell_row = 0;
-    auto row_cells = [&](int64_t r) {
-        ncell_row = 0;
-        if (DIM == 2) {
-            for (int io = -1; io <= 0; ++io) {
-                const int64_t ic = i + io;
-                if (0 <= ic && ic < g.n[0]) cells[ncell_row++] = ic + g.n[0] * r;
-            }
-        } else {
-            for (int jo = -1; jo <= 0; ++jo) {
-                const int64_t jc = j + jo;
-                if (!(0 <= jc && jc < g.n[1])) continue;
-                for (int io = -1; io <= 0; ++io) {
-                    const int64_t ic = i + io;
-                    if (0 <= ic && ic < g.n[0]) cells[ncell_row++] = ic + g.n[0] * (jc + g.n[1] * r);
-                }
-            }
+    // cell index of (i + di, j + dj, r); valid only where the has_* flags say so
+    auto cell = [&](int di, int dj, int64_t r) -> int64_t {
+        return DIM == 2 ? (i + di) + g.n[0] * r : (i + di) + g.n[0] * ((j + dj) + g.n[1] * r);
+    };
+    // accumulate row r into (cur, nxt): cells in reference order
+    auto row = [&](int64_t r, bool do_cur, bool do_nxt, double& w_c, double& wF_c, double& w_n, double& wF_n) {
+        const bool rok = active && r >= 0 && r < nlast;
+        // own cell (i, j, r) and its left neighbour (i-1, j, r) from the lane to the left
+        const uint64_t m_own = (rok && has_i1 && has_j1) ? live_mask(index, cell(0, 0, r), nc, M) : 0;
+        uint64_t m_left = __shfl_up_sync(0xffffffffu, m_own, 1);
+        if (lane == 0 && rok && has_i0 && has_j1) m_left = live_mask(index, cell(-1, 0, r), nc, M);
+        if (!(rok && has_i0 && has_j1)) m_left = 0;
+        if (DIM == 3) {
+            // row j-1 first (joffset = -1), then row j
+            const uint64_t mb0 = (rok && has_i0 && has_j0) ? live_mask(index, cell(-1, -1, r), nc, M) : 0;
+            const uint64_t mb1 = (rok && has_i1 && has_j0) ? live_mask(index, cell(0, -1, r), nc, M) : 0;
+            if (mb0) p2g_cell<DIM>(cell(-1, -1, r), mb0, nc, q_cur, q_nxt, do_cur, do_nxt, Fp, X, w_c, wF_c, w_n, wF_n);
+            if (mb1) p2g_cell<DIM>(cell(0, -1, r), mb1, nc, q_cur, q_nxt, do_cur, do_nxt, Fp, X, w_c, wF_c, w_n, wF_n);
         }
+        if (m_left) p2g_cell<DIM>(cell(-1, 0, r), m_left, nc, q_cur, q_nxt, do_cur, do_nxt, Fp, X, w_c, wF_c, w_n, wF_n);
+        if (m_own) p2g_cell<DIM>(cell(0, 0, r), m_own, nc, q_cur, q_nxt, do_cur, do_nxt, Fp, X, w_c, wF_c, w_n, wF_n);
     };
 
-    double w_c = 0.0, wF_c = 0.0;
-    double q_cur[3], q_nxt[3];
-    q_cur[0] = q_nxt[0] = qv[0];
-    if (DIM == 3) q_cur[1] = q_nxt[1] = qv[1];
-    if (r0 >= 1) {  // prologue: row r0-1 is the lower half of vertex r0's stencil
-        q_nxt[LAST] = ldg(g.xv[LAST] + r0);
-        row_cells(r0 - 1);
-        double w_d = 0.0, wF_d = 0.0;
-        for (int k = 0; k < ncell_row; ++k)
-            p2g_cell<DIM>(g, cells[k], q_nxt, q_nxt, false, Fp, X, index, w_c, wF_c, w_d, wF_d);
+    double w_c = 0.0, wF_c = 0.0, w_n = 0.0, wF_n = 0.0;
+    // prologue: row r0-1 is the lower half of vertex r0's stencil
+    if (active && r0 >= 1) q_nxt[LAST] = ldg(g.xv[LAST] + r0);
+    {
+        double wd = 0.0, wFd = 0.0;
+        row(r0 - 1, false, true, wd, wFd, w_c, wF_c);
     }
-    for (int64_t r = r0; r < r1; ++r) {
+    for (int k = 0; k < chunk; ++k) {
+        const int64_t r = r0 + k;
+        const bool vok = r < r1;  // vertex row r belongs to this thread
         const bool has_next = r + 1 < r1;
-        q_cur[LAST] = ldg(g.xv[LAST] + r);
+        if (vok) q_cur[LAST] = ldg(g.xv[LAST] + r);
         if (has_next) q_nxt[LAST] = ldg(g.xv[LAST] + r + 1);
-        double w_n = 0.0, wF_n = 0.0;
-        if (r < nlast) {
-            row_cells(r);
-            for (int k = 0; k < ncell_row; ++k)
-                p2g_cell<DIM>(g, cells[k], q_cur, q_nxt, has_next, Fp, X, index, w_c, wF_c, w_n, wF_n);
+        w_n = 0.0;
+        wF_n = 0.0;
+        row(vok ? r : -1, vok, has_next, w_c, wF_c, w_n, wF_n);
+        if (vok) {
+            const int64_t v = DIM == 2 ? i + V0 * r : i + V0 * (j + V1 * r);
+            F[v] = DIM == 2 ? wF_c / w_c : wF_c * __drcp_rn(w_c);
         }
-        const int64_t v = DIM == 2 ? i + V0 * r : i + V0 * (j + V1 * r);
-        F[v] = DIM == 2 ? wF_c / w_c : wF_c * __drcp_rn(w_c);
         w_c = w_n;
         wF_c = wF_n;
     }
@@ -454,15 +477,18 @@ cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const doubl
     CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
     const int64_t V0 = P->g.n[0] + 1, V1 = P->g.n[1] + 1;
     const int64_t cols = d3 ? V0 * V1 : V0;
-    const int64_t nlast = P->g.n[d3 ? 2 : 1];
-    // about four threads' worth of work per SM lane: columns x row chunks
-    int chunk = 8;
-    const int64_t nchunks = (nlast + 1 + chunk - 1) / chunk;
-    const unsigned nb = grid_blocks(cols * nchunks);
+    const int64_t rows = P->g.n[d3 ? 2 : 1] + 1;
+    // rows per thread: long enough to amortise the prologue row, short enough
+    // to give every SM about 2048 threads
+    const int64_t want = 152LL * 2048;
+    int chunk = (int)((cols * rows) / want);
+    chunk = chunk < 2 ? 2 : (chunk > 16 ? 16 : chunk);
+    const int64_t nthreads = cols * ((rows + chunk - 1) / chunk);
+    const unsigned nb = grid_blocks(nthreads);
     if (!d3)
-        p2g_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk);
+        p2g_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk, nthreads);
     else
-        p2g_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk);
+        p2g_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk, nthreads);
     return cudaGetLastError();
 }
 
