@@ -120,6 +120,31 @@ int jp_move_particles(jp_particles* p, double* const coords[3], uint8_t* index,
                       double* const* args, int32_t nargs);
 
 /*
+ * move_particles! for callers that cannot allocate device memory. It has no
+ * counterpart in the reference; it exists for code that must not call
+ * cudaMalloc while it runs: a step recorded into a CUDA graph under stream
+ * capture (where allocation calls are refused), a time-stepping loop that
+ * cannot afford the device-wide synchronisation an allocation may cause, or an
+ * application whose device memory is all handed out by its own pool.
+ *
+ * Same arguments and results as jp_move_particles, but the scratch memory the
+ * relocation needs (64-bit occupancy masks per cell, a code, an origin tag and
+ * a shadow record per slot) comes from one fixed device array of
+ * JP_NOALLOC_SCRATCH_BYTES that is part of the library: every GPU on which the
+ * library is loaded holds it until the process exits. A container needing more
+ * (5*8 bytes per cell plus (8*(ndim+nargs)+3) bytes per slot) is rejected with
+ * JP_ERR_INVALID_ARGUMENT and a message naming the sizes; use
+ * jp_move_particles there. The first call on a device looks up the array's
+ * device address (and may load the library's device code), so make that first
+ * call before any stream capture. All calls share the array and leave their
+ * contents in it; nothing needs to start at zero. Calls whose kernels overlap
+ * on the GPU (e.g. on two streams) race on the array.
+ */
+#define JP_NOALLOC_SCRATCH_BYTES (32u << 20)
+int jp_move_particles_noalloc(jp_particles* p, double* const coords[3], uint8_t* index,
+                              double* const* args, int32_t nargs);
+
+/*
  * inject_particles! (src/Particles/injection.jl:19-131): reseed quadrants of
  * under-populated cells; new particles copy the fields of their nearest
  * neighbour.

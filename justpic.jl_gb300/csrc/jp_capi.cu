@@ -268,6 +268,24 @@ int jp_move_particles(jp_particles* P, double* const coords[3], uint8_t* index, 
     return finish(P, jp::launch_move(P, coords, index, args, nargs), "jp_move_particles");
 }
 
+int jp_move_particles_noalloc(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
+                              int32_t nargs)
+{
+    if (!P || !index || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles_noalloc: null pointer");
+    if (nargs < 0 || nargs > JP_MAX_ARGS || (nargs > 0 && !args))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles_noalloc: bad particle field list");
+    for (int k = 0; k < nargs; ++k)
+        if (!args[k]) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles_noalloc: null field");
+    const size_t need = jp::move_scratch_bytes(P->g, P->g.ndim + nargs);
+    if (need > jp::kNoAllocScratchBytes)
+        return fail(JP_ERR_INVALID_ARGUMENT,
+                    "jp_move_particles_noalloc: this container needs " + std::to_string(need) +
+                        " bytes of scratch but the fixed buffer holds " + std::to_string(jp::kNoAllocScratchBytes) +
+                        " (JP_NOALLOC_SCRATCH_BYTES); use jp_move_particles for larger grids");
+    return finish(P, jp::launch_move_noalloc(P, coords, index, args, nargs), "jp_move_particles_noalloc");
+}
+
 int jp_inject_particles(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
                         int32_t nargs)
 {

@@ -307,6 +307,12 @@ cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const doubl
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
                        const uint8_t* index);
 
+// move_particles! with its scratch in a fixed device array (no allocation)
+constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;
+size_t move_scratch_bytes(const DevGrid& g, int comps);
+cudaError_t launch_move_noalloc(jp_particles* P, double* const coords[3], uint8_t* index,
+                                double* const* args, int nargs);
+
 // argument blocks passed by value
 struct Coords {
     double* c[3];

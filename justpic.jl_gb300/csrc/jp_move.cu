@@ -788,4 +788,97 @@ cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* ind
     return cudaGetLastError();
 }
 
+// ------------------------------------------- move_particles! without allocating
+// jp_move_particles_noalloc runs the same three stages as launch_move, but its
+// scratch (occupancy masks, destination codes, origin tags, shadow records)
+// lives in this fixed device array instead of memory obtained from cudaMalloc.
+// The array is part of this library's device image: every GPU on which the
+// library's kernels are loaded holds these bytes until the process exits. All
+// calls share it and each call overwrites what the previous one left; nothing
+// in it has to start at zero, because every stage writes each entry it later
+// reads within the same call. Two calls whose kernels overlap on the GPU (for
+// example on two streams) race on the array.
+static_assert(kNoAllocScratchBytes == JP_NOALLOC_SCRATCH_BYTES, "fixed scratch size differs from the header");
+static __device__ __align__(256) unsigned char g_move_scratch[kNoAllocScratchBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+void* g_move_scratch_addr[kMaxDevices] = {};  // device address of g_move_scratch, per device
+}  // namespace
+
+size_t move_scratch_bytes(const DevGrid& g, int comps)
+{
+    const size_t nc = (size_t)g.ncells;
+    const size_t ns = nc * (size_t)g.max_xcell;
+    return 5 * nc * sizeof(uint64_t) + (size_t)comps * ns * sizeof(double) + ns * sizeof(uint16_t) + ns;
+}
+
+// Host code may not use g_move_scratch's name as a device address: it stands
+// for a host-side shadow. The first call on each device (with that device
+// current) asks the runtime for the real address and keeps it; this may load
+// the library's device image, so that first call should happen before any
+// stream capture.
+static cudaError_t move_scratch_address(void** out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    if (!g_move_scratch_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_move_scratch);
+        if (e != cudaSuccess) return e;
+        g_move_scratch_addr[dev] = p;
+    }
+    *out = g_move_scratch_addr[dev];
+    return cudaSuccess;
+}
+
+cudaError_t launch_move_noalloc(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
+                                int nargs)
+{
+    const int N = P->g.ndim;
+    void* scratch = nullptr;
+    cudaError_t e = move_scratch_address(&scratch);
+    if (e != cudaSuccess) return e;
+    const int64_t nc = P->g.ncells;
+    const int64_t ns = nc * P->g.max_xcell;
+    char* base = (char*)scratch;
+    MoveView S;
+    S.L0 = (uint64_t*)base;
+    S.L = S.L0 + nc;
+    S.M = S.L + nc;
+    S.R = S.M + nc;
+    S.U = S.R + nc;
+    S.shadow = (double*)(base + 5 * nc * sizeof(uint64_t));
+    S.orig = (uint16_t*)((char*)S.shadow + (size_t)(N + nargs) * ns * sizeof(double));
+    S.code = (uint8_t*)((char*)S.orig + ns * sizeof(uint16_t));
+    S.nslots = ns;
+    S.comps = N + nargs;
+    Coords X{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};
+    Args A{};
+    A.n = nargs;
+    for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
+    cudaStream_t st = P->stream;
+    const unsigned nb = grid_blocks(nc);
+    const unsigned nbw = grid_blocks(nc, 32 * kWarpsPerBlock);
+    const int ntw = 32 * kWarpsPerBlock;
+    int64_t mc[3] = {1, 1, 1};
+    for (int d = 0; d < N; ++d) mc[d] = (P->g.n[d] + 2) / 3;
+    const unsigned nbp = grid_blocks(mc[0] * mc[1] * mc[2], kAllocThreads);
+    if (N == 2) {
+        move_classify<2><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        for (int pass = 0; pass < 9; ++pass)
+            move_allocate<2><<<nbp, kAllocThreads, 0, st>>>(P->g, S, pass / 3, pass % 3, 0, mc[0], mc[1], 1);
+        move_apply<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
+    } else {
+        move_classify<3><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        for (int pass = 0; pass < 27; ++pass)
+            move_allocate<3><<<nbp, kAllocThreads, 0, st>>>(P->g, S, pass / 9, (pass / 3) % 3, pass % 3, mc[0],
+                                                            mc[1], mc[2]);
+        move_apply<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace jp
