@@ -43,6 +43,7 @@ STEPS = {
     "C1": ["advection!", "move_particles!"],
     "C2": ["particle2grid!", "advection!", "move_particles!", "inject_particles!", "grid2particle!"],
     "C3": ["particle2grid!", "advection!", "move_particles!", "inject_particles!"],
+    "C4": ["particle2grid!", "advection!", "move_particles!", "inject_particles!", "grid2particle!"],
 }
 DESC = {
     "C1": "C1: 2D RK2 advection FP64, 256x256 cells, 24/48/12 particles per cell, stream-function velocity, "
@@ -51,27 +52,43 @@ DESC = {
           "step = particle2grid!+advection!+move_particles!+inject_particles!+grid2particle!",
     "C3": "C3: 3D temperature advection FP64, 128^3 cells, 24/48/12 particles per cell, cellular flow + 0.1 z "
           "drift, RK2, step = particle2grid!+advection!+move_particles!+inject_particles!",
+    "C4": "C4: 2D, 2048x2048 cells, 24/48/12 particles per cell, stream-function velocity, RK4, "
+          "step = particle2grid!+advection!+move_particles!+inject_particles!+grid2particle!",
 }
 
 
-def algorithmic_bytes(op, N, nf, m, slots_per_live, grid_bytes_per_live, field_bytes_per_live):
+def algorithmic_bytes(op, N, nf, m, slots_per_live, grid_bytes_per_live, field_bytes_per_live, vb=8):
     """Bytes per live particle of one call: every live particle's data once,
     the Bool index at 1 byte per slot, grid arrays once per call amortised
     over the particles; movers (fraction m) re-read and re-write their
     coordinates and fields."""
-    coords = 8 * N
+    coords = vb * N
     idx = slots_per_live
     if op == "advection!":
         return 2 * coords + idx + grid_bytes_per_live
     if op == "move_particles!":
-        return coords + idx + m * (2 * (coords + 8 * nf) + 2)
+        return coords + idx + m * (2 * (coords + vb * nf) + 2)
     if op == "inject_particles!":
         return coords + idx
     if op == "grid2particle!":
-        return coords + idx + 8 + field_bytes_per_live
+        return coords + idx + vb + field_bytes_per_live
     if op == "particle2grid!":
-        return coords + idx + 8 + field_bytes_per_live
+        return coords + idx + vb + field_bytes_per_live
     raise KeyError(op)
+
+
+# DRAM bytes per live particle of each call, FP64 form, 2D, one particle field:
+# dram__bytes_read.sum + dram__bytes_write.sum of the call's kernels in one ncu
+# capture of a 512x512-cell C2 case (5.79M particles; profiles/c2_fp64_kernels_512.md),
+# divided by its particle count. Traffic grows with the particle count, so the
+# bench scales it by the live particles of its own run.
+DRAM_BYTES_PER_PARTICLE_2D_F64 = {
+    "particle2grid!": 623.9e6 / 5.790e6,
+    "advection!": 304.0e6 / 5.790e6,
+    "grid2particle!": 309.1e6 / 5.790e6,
+    "move_particles!": 1535.5e6 / 5.790e6,
+    "inject_particles!": 510.7e6 / 5.790e6,
+}
 
 
 def launches(op, N):
@@ -188,21 +205,39 @@ def run_ours(args):
     N = g["ndim"]
     nf = 1 if "particle2grid!" in STEPS[args.workload] else 0
     dt = cfg["dt"]
+    f32 = args.form == "f32"
     p = jp.init_particles(jp.CUDABackend, cfg["nxcell"], cfg["max_xcell"], cfg["min_xcell"], *g["grid_v"],
                           seed=jp.DEFAULT_SEED + rank)
-    fields = jp.init_cell_arrays(p, nf)
-    pT = fields[0] if nf else None
     V = tuple(jp.TA("CUDA")(v) for v in cfg["V"])
     T = jp.TA("CUDA")(cfg["T"])
-    method = jp.RungeKutta2()
-    if nf:
-        jp.grid2particle_(pT, T, p)
+    if f32:
+        xi = jp.init_offsets(p)
+        fields = jp.init_cell_arrays_f32(p, nf)
+        V = tuple(v.float() for v in V)
+        T = T.float()
+    else:
+        fields = jp.init_cell_arrays(p, nf)
+    pT = fields[0] if nf else None
+    rk4 = args.method == "rk4" or (args.method is None and cfg["method"] == "RK4")
+    method = jp.RungeKutta4() if rk4 else jp.RungeKutta2()
 
     stream = torch.cuda.current_stream()
     ops = STEPS[args.workload]
     Vcur = [V]
 
     def call(op):
+        if f32:
+            if op == "particle2grid!":
+                jp.particle2grid_f32_(T, pT, p, xi)
+            elif op == "advection!":
+                jp.advection_f32_(p, xi, method, Vcur[0], dt)
+            elif op == "move_particles!":
+                jp.move_particles_f32_(p, xi, fields)
+            elif op == "inject_particles!":
+                jp.inject_particles_f32_(p, xi, fields)
+            elif op == "grid2particle!":
+                jp.grid2particle_f32_(pT, T, p, xi)
+            return
         if op == "particle2grid!":
             jp.particle2grid_(T, pT, p)
         elif op == "advection!":
@@ -222,16 +257,26 @@ def run_ours(args):
             if ev is not None:
                 ev[k][1].record(stream)
 
+    if nf:
+        call("grid2particle!")
     # movers fraction of this workload (measured once, outside the timed region)
     if nf:
-        jp.particle2grid_(T, pT, p)
-    jp.advection_(p, method, V, dt)
-    m = movers_fraction(p, torch)
-    jp.move_particles_(p, fields)
+        call("particle2grid!")
+    call("advection!")
+    if f32:
+        live_mask = p.index.data.bool()
+        out = torch.zeros_like(live_mask)
+        for d in range(N):
+            x = xi[d].data
+            out |= ~((x >= 0) & (x < 1))
+        m = int((out & live_mask).sum()) / max(1, int(live_mask.sum()))
+    else:
+        m = movers_fraction(p, torch)
+    call("move_particles!")
     if "inject_particles!" in ops:
-        jp.inject_particles_(p, fields)
+        call("inject_particles!")
     if "grid2particle!" in ops:
-        jp.grid2particle_(pT, T, p)
+        call("grid2particle!")
 
     # ---- device-resident throughput (asynchronous calls) ----
     jp.set_synchronous(p, False)
@@ -267,11 +312,12 @@ def run_ours(args):
 
     # ---- end to end through the public API (synchronous, host buffers) ----
     jp.set_synchronous(p, True)
-    hV = [torch.from_numpy(np.ascontiguousarray(v.transpose(tuple(reversed(range(v.ndim)))))).pin_memory()
+    hdt = np.float32 if f32 else np.float64
+    hV = [torch.from_numpy(np.ascontiguousarray(v.transpose(tuple(reversed(range(v.ndim)))), dtype=hdt)).pin_memory()
           for v in cfg["V"]]
     dV = [torch.empty_like(h, device="cuda") for h in hV]
     rev = tuple(reversed(range(N)))
-    hT = torch.empty(tuple(reversed(T.shape)), dtype=torch.float64).pin_memory() if nf else None
+    hT = torch.empty(tuple(reversed(T.shape)), dtype=T.dtype).pin_memory() if nf else None
     e2e_steps = max(1, min(args.steps, 50))
     torch.cuda.synchronize()
     w0 = time.perf_counter()
@@ -293,7 +339,8 @@ def run_ours(args):
     slots_per_live = p.max_xcell * int(np.prod(p.ni)) / live
     gb = nvel_bytes / live
     fb = T.numel() * 8 / live
-    bpp = {op: algorithmic_bytes(op, N, nf, m, slots_per_live, gb, fb) for op in ops}
+    vb = 4 if f32 else 8  # bytes per value of coordinates/offsets and fields
+    bpp = {op: algorithmic_bytes(op, N, nf, m, slots_per_live, gb * vb / 8, fb * vb / 8, vb) for op in ops}
     dom = max(op_ms, key=op_ms.get)
     achieved = bpp[dom] * live / (op_ms[dom] / 1e3) / 1e9
     step_bytes = sum(bpp.values()) * live
@@ -310,9 +357,11 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "f32 offsets + int32 cell (FP64 renormalisation and p2g sums)" if f32 else "f64",
         "data": "synthetic (seeded analytic flow; the reference publishes no dataset)",
         "config": {
+            "form": "split precision (FP32 cell offset)" if f32 else "FP64",
+            "integrator": type(method).__name__,
             "workload": DESC[args.workload] if args.ni is None else DESC[args.workload] + f" (resized to {args.ni} "
                                                                                          "cells per axis)",
             "cells": list(p.ni),
@@ -334,13 +383,15 @@ def run_ours(args):
             "frac": achieved / peak,
             "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
             else "fallback 6.8 TB/s",
-            "traffic": None,
+            "traffic": (DRAM_BYTES_PER_PARTICLE_2D_F64[dom] * live / 1e9
+                        if (N == 2 and not f32 and nf == 1) else None),
+            "traffic_unit": "GB per launch, from ncu dram bytes of a 512^2 capture scaled by particle count",
         },
         "e2e": {
             "value": e2e_value,
             "unit": UNIT,
-            "h2d_bytes_per_step": int(sum(h.numel() * 8 for h in hV)),
-            "d2h_bytes_per_step": int(hT.numel() * 8) if nf else 0,
+            "h2d_bytes_per_step": int(sum(h.numel() * h.element_size() for h in hV)),
+            "d2h_bytes_per_step": int(hT.numel() * hT.element_size()) if nf else 0,
             "steps": e2e_steps,
             "mode": "public API, synchronous calls; velocity grids in and (with fields) the vertex field out each step",
         },
@@ -353,6 +404,94 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(result))
+
+
+def run_compare(args):
+    """The same seeded run in both forms for ``--steps`` steps (no timing):
+    position error of the split-precision form in cell widths, by particle id,
+    for every particle present once in both runs, and L-inf / L2 error of the
+    gridded field, both against the FP64 form."""
+    import torch
+
+    import justpic_gb300 as jp
+
+    torch.cuda.set_device(0)
+    cfg = _setup_cfg(args.workload, args.ni)
+    g = cfg["grid"]
+    N = g["ndim"]
+    dt = cfg["dt"]
+    rk4 = args.method == "rk4" or (args.method is None and cfg["method"] == "RK4")
+    method = jp.RungeKutta4() if rk4 else jp.RungeKutta2()
+    a = jp.init_particles(jp.CUDABackend, cfg["nxcell"], cfg["max_xcell"], cfg["min_xcell"], *g["grid_v"])
+    b = jp.init_particles(jp.CUDABackend, cfg["nxcell"], cfg["max_xcell"], cfg["min_xcell"], *g["grid_v"])
+    live = a.index.data.bool()
+    ids = torch.full(a.index.data.shape, float("nan"), dtype=torch.float64, device="cuda")
+    ids[live] = torch.arange(int(live.sum()), device="cuda", dtype=torch.float64)
+    hi = torch.floor(ids / 4096.0)
+    lo = ids - hi * 4096.0
+    Ta = jp.TA("CUDA")(cfg["T"])
+    Tb = Ta.float()
+    Va = tuple(jp.TA("CUDA")(v) for v in cfg["V"])
+    Vb = tuple(v.float() for v in Va)
+    pTa, = jp.init_cell_arrays(a, 1)
+    pTb, = jp.init_cell_arrays_f32(b, 1)
+    fa = (pTa, jp.CellArray(ids, a.ni))
+    fb = (pTb, jp.CellArray(hi.float().contiguous(), b.ni), jp.CellArray(lo.float().contiguous(), b.ni))
+    xi = jp.init_offsets(b)
+    jp.set_synchronous(a, False)
+    jp.set_synchronous(b, False)
+    jp.grid2particle_(pTa, Ta, a)
+    jp.grid2particle_f32_(pTb, Tb, b, xi)
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        jp.particle2grid_(Ta, pTa, a)
+        jp.advection_(a, method, Va, dt)
+        jp.move_particles_(a, fa)
+        jp.inject_particles_(a, fa)
+        jp.grid2particle_(pTa, Ta, a)
+        jp.particle2grid_f32_(Tb, pTb, b, xi)
+        jp.advection_f32_(b, xi, method, Vb, dt)
+        jp.move_particles_f32_(b, xi, fb)
+        jp.inject_particles_f32_(b, xi, fb)
+        jp.grid2particle_f32_(pTb, Tb, b, xi)
+    jp.synchronize(a)
+    jp.synchronize(b)
+    wall = time.perf_counter() - w0
+    la = a.index.data.bool()
+    lb = b.index.data.bool()
+    ida = fa[1].data[la].long()
+    idb = (fb[1].data[lb].double() * 4096 + fb[2].data[lb].double()).long()
+    pa = torch.stack([c.data[la] for c in a.coords], 1)
+    back = jp.coords_from_offsets(b, xi)
+    pb = torch.stack([c.data[lb] for c in back], 1)
+    n_ids = int(ida.max()) + 2
+
+    def unique_pos(idv, pos):
+        cnt = torch.bincount(idv, minlength=n_ids)
+        keep = cnt[idv] == 1
+        table = torch.full((n_ids, N), float("nan"), dtype=torch.float64, device="cuda")
+        table[idv[keep]] = pos[keep]
+        return table
+
+    ta, tb = unique_pos(ida, pa), unique_pos(idb, pb)
+    both = ~torch.isnan(ta[:, 0]) & ~torch.isnan(tb[:, 0])
+    dxs = torch.tensor(g["dx"], dtype=torch.float64, device="cuda")
+    err = ((ta[both] - tb[both]).abs() / dxs).max(dim=1).values
+    Ferr = (Ta.double() - Tb.double())
+    out = {
+        "workload": DESC[args.workload] if args.ni is None else DESC[args.workload] + f" (resized to {args.ni})",
+        "integrator": type(method).__name__,
+        "steps": args.steps,
+        "particles_compared": int(both.sum()),
+        "live_fp64": int(la.sum()), "live_split": int(lb.sum()),
+        "position_error_cells": {"max": float(err.max()), "p99": float(torch.quantile(err[:1 << 24], 0.99)),
+                                 "mean": float(err.mean())},
+        "gridded_field_error": {"linf": float(Ferr.abs().max()),
+                                "l2_rel": float(Ferr.norm() / Ta.norm()),
+                                "field_range": float(Ta.max() - Ta.min())},
+        "wall_s_both_forms": wall,
+    }
+    print(json.dumps(out))
 
 
 def _cpu_setup(workload):
@@ -377,7 +516,7 @@ def _cpu_setup(workload):
             if op == "particle2grid!":
                 o.particle2grid(T, fields[0])
             elif op == "advection!":
-                o.advection(O.RK2, 0.5, V, dt)
+                o.advection(O.RK4 if cfg["method"] == "RK4" else O.RK2, 0.5, V, dt)
             elif op == "move_particles!":
                 o.move_particles(fields)
             elif op == "inject_particles!":
@@ -458,6 +597,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(STEPS), default="C2")
+    ap.add_argument("--form", choices=["f64", "f32"], default="f64",
+                    help="f64: the reference's FP64 form; f32: int32 cell + FP32 offset form")
+    ap.add_argument("--method", choices=["rk2", "rk4"], default=None,
+                    help="integrator (default: the workload's, RK2 except C4)")
+    ap.add_argument("--compare-forms", action="store_true",
+                    help="run the same seeded workload in both forms for --steps steps and print the errors")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ni", type=int, default=None,
@@ -467,6 +612,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.compare_forms:
+        run_compare(args)
     else:
         run_ours(args)
 

@@ -162,6 +162,35 @@ int jp_grid2particle(jp_particles* p, double* Fp, const double* F, const double*
 int jp_particle2grid(jp_particles* p, double* F, const double* Fp, const double* const coords[3],
                      const uint8_t* index);
 
+/*
+ * Split-precision form (no reference counterpart; the scope of this library
+ * asks for it beside the plain FP64 form). Each particle is the cell of its
+ * slot (an implicit int32 index) plus an FP32 offset xi in [0, 1)^N in units
+ * of the cell spacing, stored in the same blocklength-0 layout as the
+ * coordinates (4 bytes per value). Velocity fields, particle fields and vertex
+ * fields are FP32; FP64 is used only to re-normalise (cell, offset) when a
+ * particle changes cell and for the weight sums of particle2grid. Uniform
+ * (range) grids only. Semantics in cell units: a particle belongs to its cell
+ * when 0 <= xi < 1; move_particles sends it to cell + floor(xi) with the same
+ * colour-pass slot allocation as the FP64 form; the other rules follow the
+ * FP64 form (see jp_f32.cu). Error against the FP64 form is measured by the
+ * tests and the bench.
+ */
+int jp_offsets_from_coords(jp_particles* p, const double* const coords[3], const uint8_t* index,
+                           float* const xi[3]);
+int jp_coords_from_offsets(jp_particles* p, const float* const xi[3], const uint8_t* index,
+                           double* const coords[3]);
+int jp_advection_f32(jp_particles* p, int32_t method, double alpha, const float* const V[3], double dt,
+                     float* const xi[3], const uint8_t* index);
+int jp_move_particles_f32(jp_particles* p, float* const xi[3], uint8_t* index, float* const* args,
+                          int32_t nargs);
+int jp_inject_particles_f32(jp_particles* p, float* const xi[3], uint8_t* index, float* const* args,
+                            int32_t nargs);
+int jp_grid2particle_f32(jp_particles* p, float* Fp, const float* F, const float* const xi[3],
+                         const uint8_t* index);
+int jp_particle2grid_f32(jp_particles* p, float* F, const float* Fp, const float* const xi[3],
+                         const uint8_t* index);
+
 #ifdef __cplusplus
 }
 #endif

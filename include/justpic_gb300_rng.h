@@ -86,4 +86,19 @@ JP_RNG_QUAL double jp_rand_uniform(uint64_t seed, uint32_t stream, uint32_t call
     return (double)(u >> 11) * 0x1.0p-53;
 }
 
+/* The same draw as a float on [0, 1): the top 24 bits of that 64-bit integer. */
+JP_RNG_QUAL float jp_rand_uniform_f32(uint64_t seed, uint32_t stream, uint32_t call,
+                                      uint64_t cell, uint32_t slot, uint32_t dim)
+{
+    uint32_t ctr[4], key[2], out[4];
+    ctr[0] = (uint32_t)cell;
+    ctr[1] = (uint32_t)(cell >> 32);
+    ctr[2] = (slot & 0xFFFFu) | ((dim & 0xFFu) << 16) | ((stream & 0xFFu) << 24);
+    ctr[3] = call;
+    key[0] = (uint32_t)seed;
+    key[1] = (uint32_t)(seed >> 32);
+    jp_philox4x32_10(ctr, key, out);
+    return (float)(out[0] >> 8) * 0x1.0p-24f;
+}
+
 #endif /* JUSTPIC_GB300_RNG_H */

@@ -42,3 +42,16 @@ def build(force: bool = False) -> str:
     """Compile libjustpic_gb300.so for sm_103a (nvcc) and return its path."""
     from . import native_build as _b
     return _b.build(force=force)
+
+from .split import (  # noqa: F401,E402
+    advection_f32_,
+    cell_array_f32,
+    coords_from_offsets,
+    grid2particle_f32_,
+    grid_field_f32,
+    init_cell_arrays_f32,
+    init_offsets,
+    inject_particles_f32_,
+    move_particles_f32_,
+    particle2grid_f32_,
+)

@@ -77,6 +77,17 @@ SIGNATURES = [
     ("jp_inject_particles", ctypes.c_int, [ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     ("jp_grid2particle", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
     ("jp_particle2grid", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
+    # split-precision (FP32 cell offset) form
+    ("jp_offsets_from_coords", ctypes.c_int, [ctypes.c_void_p, P3, ctypes.c_void_p, P3]),
+    ("jp_coords_from_offsets", ctypes.c_int, [ctypes.c_void_p, P3, ctypes.c_void_p, P3]),
+    ("jp_advection_f32", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, P3, ctypes.c_double, P3, ctypes.c_void_p]),
+    ("jp_move_particles_f32", ctypes.c_int,
+     [ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    ("jp_inject_particles_f32", ctypes.c_int,
+     [ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    ("jp_grid2particle_f32", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
+    ("jp_particle2grid_f32", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
 ]
 
 _lib = None

@@ -75,11 +75,11 @@ def _coords(p: Particles) -> P3:
     return P3(*[c.data_ptr() for c in p.coords], *([None] * (3 - p.ndim)))
 
 
-def _check_cellarray(p: Particles, A: CellArray, what: str) -> None:
+def _check_cellarray(p: Particles, A: CellArray, what: str, dtype=torch.float64) -> None:
     if not isinstance(A, CellArray):
         raise ArgumentError(f"{what} must be a CellArray")
-    if A.data.dtype != torch.float64 or not A.data.is_cuda:
-        raise ArgumentError(f"{what} must hold float64 CUDA data")
+    if A.data.dtype != dtype or not A.data.is_cuda:
+        raise ArgumentError(f"{what} must hold {dtype} CUDA data")
     if A.ni != p.ni or A.ncap != p.max_xcell:
         raise ArgumentError(f"{what} does not have the particle layout {p.max_xcell} x {p.ni}")
 

@@ -120,6 +120,7 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
         }
         g.dom_lo[d] = lo;
         g.dom_hi[d] = hi;
+        P->dx_host[d] = x[1] - x[0];
     }
     for (int c = 0; c < N; ++c)
         for (int d = 0; d < N; ++d) {
@@ -131,6 +132,26 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
             g.nvel[c][d] = n;
             g.lim_lo[c][d] = x[0];  // inner_limits: first/last (src/Advection/advection.jl:73-81)
             g.lim_hi[c][d] = x[n - 1];
+        }
+    // The split-precision form samples velocities in cell units and assumes the
+    // standard staggering: component c on the vertices along axis c and on the
+    // ghost-expanded cell centres (vertex origin - dx/2 + k*dx) along the others.
+    P->staggered_std = grid->uniform ? 1 : 0;
+    for (int c = 0; c < N && P->staggered_std; ++c)
+        for (int d = 0; d < N && P->staggered_std; ++d) {
+            const double* x = grid->xi_vel[c][d];
+            const int64_t n = grid->n_vel[c][d];
+            const double x0 = grid->xi_vel[d][d][0], dx = P->dx_host[d];
+            const double shift = c == d ? 0.0 : -0.5;
+            if (n != (c == d ? g.n[d] + 1 : g.n[d] + 2)) {
+                P->staggered_std = 0;
+                break;
+            }
+            for (int64_t k = 0; k < n; ++k)
+                if (std::fabs(x[k] - (x0 + ((double)k + shift) * dx)) > 1e-9 * dx * (double)(n + 1)) {
+                    P->staggered_std = 0;
+                    break;
+                }
         }
     cudaError_t e = cudaMalloc(&P->dev_block, host.size() * sizeof(double));
     if (e == cudaSuccess)
@@ -298,6 +319,88 @@ int jp_inject_particles(jp_particles* P, double* const coords[3], uint8_t* index
     const uint32_t call = (uint32_t)P->inject_calls;
     P->inject_calls += 1;
     return finish(P, jp::launch_inject(P, coords, index, args, nargs, call), "jp_inject_particles");
+}
+
+// ---- split-precision form ----------------------------------------------
+static int check_f32(const jp_particles* P, const void* const* xi, const void* index, const char* what)
+{
+    if (!P || !index || !check_coords(P, xi)) return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": null pointer");
+    if (!P->g.uniform || !P->staggered_std)
+        return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) +
+                                                 ": the FP32 cell-offset form needs uniform (range) grids with the "
+                                                 "standard ghost-node staggering of the velocity components");
+    return JP_OK;
+}
+
+int jp_offsets_from_coords(jp_particles* P, const double* const coords[3], const uint8_t* index, float* const xi[3])
+{
+    int rc = check_f32(P, (const void* const*)xi, index, "jp_offsets_from_coords");
+    if (rc) return rc;
+    if (!check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_offsets_from_coords: null pointer");
+    return finish(P, jp::launch_to_offsets(P, coords, index, xi), "jp_offsets_from_coords");
+}
+
+int jp_coords_from_offsets(jp_particles* P, const float* const xi[3], const uint8_t* index, double* const coords[3])
+{
+    int rc = check_f32(P, (const void* const*)xi, index, "jp_coords_from_offsets");
+    if (rc) return rc;
+    if (!check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_coords_from_offsets: null pointer");
+    return finish(P, jp::launch_to_coords(P, xi, index, coords), "jp_coords_from_offsets");
+}
+
+int jp_advection_f32(jp_particles* P, int32_t method, double alpha, const float* const V[3], double dt,
+                     float* const xi[3], const uint8_t* index)
+{
+    int rc = check_f32(P, (const void* const*)xi, index, "jp_advection_f32");
+    if (rc) return rc;
+    if (!check_coords(P, (const void* const*)V)) return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_f32: null velocity");
+    if (method != JP_EULER && method != JP_RUNGE_KUTTA2 && method != JP_RUNGE_KUTTA4)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_f32: unknown integrator");
+    if (method == JP_RUNGE_KUTTA2 && !(0.0 < alpha && alpha < 1.0))
+        return fail(JP_ERR_INVALID_ARGUMENT, "Only 0 < α < 1 is supported");
+    return finish(P, jp::launch_advection_f32(P, method, alpha, V, dt, xi, index), "jp_advection_f32");
+}
+
+int jp_move_particles_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int32_t nargs)
+{
+    int rc = check_f32(P, (const void* const*)xi, index, "jp_move_particles_f32");
+    if (rc) return rc;
+    if (nargs < 0 || nargs > JP_MAX_ARGS || (nargs > 0 && !args))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles_f32: bad particle field list");
+    for (int k = 0; k < nargs; ++k)
+        if (!args[k]) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles_f32: null field");
+    return finish(P, jp::launch_move_f32(P, xi, index, args, nargs), "jp_move_particles_f32");
+}
+
+int jp_inject_particles_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int32_t nargs)
+{
+    int rc = check_f32(P, (const void* const*)xi, index, "jp_inject_particles_f32");
+    if (rc) return rc;
+    if (nargs < 0 || nargs > JP_MAX_ARGS || (nargs > 0 && !args))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_particles_f32: bad particle field list");
+    for (int k = 0; k < nargs; ++k)
+        if (!args[k]) return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_particles_f32: null field");
+    const uint32_t call = (uint32_t)P->inject_calls;
+    P->inject_calls += 1;
+    return finish(P, jp::launch_inject_f32(P, xi, index, args, nargs, call), "jp_inject_particles_f32");
+}
+
+int jp_grid2particle_f32(jp_particles* P, float* Fp, const float* F, const float* const xi[3], const uint8_t* index)
+{
+    int rc = check_f32(P, (const void* const*)xi, index, "jp_grid2particle_f32");
+    if (rc) return rc;
+    if (!Fp || !F) return fail(JP_ERR_INVALID_ARGUMENT, "jp_grid2particle_f32: null field");
+    return finish(P, jp::launch_g2p_f32(P, Fp, F, xi, index), "jp_grid2particle_f32");
+}
+
+int jp_particle2grid_f32(jp_particles* P, float* F, const float* Fp, const float* const xi[3], const uint8_t* index)
+{
+    int rc = check_f32(P, (const void* const*)xi, index, "jp_particle2grid_f32");
+    if (rc) return rc;
+    if (!Fp || !F) return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_f32: null field");
+    return finish(P, jp::launch_p2g_f32(P, F, Fp, xi, index), "jp_particle2grid_f32");
 }
 
 int jp_grid2particle(jp_particles* P, double* Fp, const double* F, const double* const coords[3],

@@ -1,0 +1,918 @@
+// jp_f32.cu -- the split-precision form of the hot path.
+//
+// Each particle is its slot's cell (an implicit int32 cell index: the
+// CellArray slot belongs to one cell) plus an FP32 offset xi in [0, 1)^N in
+// units of that cell's spacing, so round-off scales with the cell width and not
+// with the domain. Velocities, interpolation weights and Runge-Kutta stages
+// are FP32; FP64 is kept for the re-normalisation of (cell, offset) when a
+// particle changes cell and for the weight sums of particle2grid!. Uniform
+// grids only (every spacing is one number per axis). The form has no reference
+// counterpart: its error is stated against the FP64 form on the same seeded run.
+//
+// Semantics in cell units (FP64 form: the reference's rules):
+//   * a particle belongs to its cell when 0 <= xi < 1 on every axis;
+//   * velocity component c is sampled on its staggered grid: along its own
+//     axis the nodes are the cell vertices (node k at k), along the others the
+//     ghost-expanded centres (node k at k - 1/2); outside a grid's limits the
+//     sample is Inf, as in the reference;
+//   * move_particles! sends a particle to cell + floor(xi) with
+//     xi - floor(xi) (computed in FP64, kept below 1), with the reference's
+//     colour-pass slot allocation (shared allocate stage);
+//   * inject_particles! follows the reference's quadrant walk; new offsets are
+//     quadrant corner + 1/2 * (0.05 + 0.95 r) and the nearest neighbour is the
+//     first minimum of the FP32 squared physical distance in k -> j -> i ->
+//     slot order;
+//   * particle2grid! weights are 1 / |vertex - particle|^2 in FP32, summed in
+//     FP64 in the reference's order.
+#include <math_constants.h>
+
+#include <cmath>
+
+#include "jp_internal.cuh"
+#include "jp_move_core.cuh"
+
+namespace jp {
+
+struct XiF {
+    float* x[3];
+};
+struct CXiF {
+    const float* x[3];
+};
+struct ArgsF {
+    float* a[JP_MAX_ARGS];
+    int n;
+};
+struct CVelF {
+    const float* v[3];
+};
+
+// per-call constants of the FP32 form
+struct F32Params {
+    float dx[3];   // spacing per axis
+    float w[3];    // dt / dx per axis (time step in cell units per unit velocity)
+    float aw[3];   // alpha * dt / dx
+    float ca, cb;  // RK2 blend for alpha != 1/2
+    int half;
+};
+
+__device__ __forceinline__ float lerpf1(float t, float v0, float v1) { return fmaf(t, v1, fmaf(-t, v0, v0)); }
+
+template <int DIM>
+__device__ __forceinline__ float lerpNf(const float* v, const float* t)
+{
+    if (DIM == 2) return lerpf1(t[1], lerpf1(t[0], v[0], v[1]), lerpf1(t[0], v[2], v[3]));
+    return lerpf1(t[2], lerpf1(t[1], lerpf1(t[0], v[0], v[1]), lerpf1(t[0], v[2], v[3])),
+                  lerpf1(t[1], lerpf1(t[0], v[4], v[5]), lerpf1(t[0], v[6], v[7])));
+}
+
+// ------------------------------------------------------------ conversions
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    to_offsets(DevGrid g, CCoords X, const uint8_t* __restrict__ index, XiF Xi)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    const int64_t nc = g.ncells;
+    double x0[3], ix[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        x0[d] = ldg(g.xv[d] + I[d]);
+        ix[d] = ldg(g.ixv[d] + I[d]);
+    }
+    for (int s = 0; s < g.max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        const bool live = index[a] != 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) Xi.x[d][a] = live ? (float)((X.c[d][a] - x0[d]) * ix[d]) : CUDART_NAN_F;
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    to_coords(DevGrid g, CXiF Xi, const uint8_t* __restrict__ index, Coords X)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    const int64_t nc = g.ncells;
+    double x0[3], dx[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        x0[d] = ldg(g.xv[d] + I[d]);
+        dx[d] = ldg(g.dxv[d] + I[d]);
+    }
+    for (int s = 0; s < g.max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        const bool live = index[a] != 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) X.c[d][a] = live ? fma((double)Xi.x[d][a], dx[d], x0[d]) : CUDART_NAN;
+    }
+}
+
+// ------------------------------------------------------------- advection
+// Velocity component `comp` at cell I + offset xi.
+template <int DIM>
+__device__ __forceinline__ float velocity_f32(const DevGrid& g, int comp, const int* I, const float* xi,
+                                              const float* __restrict__ V)
+{
+    int k[3];
+    float t[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const float y = (d == comp) ? xi[d] : xi[d] + 0.5f;
+        if (!(fabsf(y) < 1e6f)) return CUDART_INF_F;  // NaN, Inf or far outside
+        const float fl = floorf(y);
+        int kk = I[d] + (int)fl;
+        float tt = y - fl;
+        const int L = (int)g.nvel[comp][d];
+        if (kk == L - 1 && tt == 0.0f) {  // exactly on the last node
+            kk = L - 2;
+            tt = 1.0f;
+        }
+        if (kk < 0 || kk > L - 2) return CUDART_INF_F;  // outside the grid's limits
+        k[d] = kk;
+        t[d] = tt;
+    }
+    const int64_t L0 = g.nvel[comp][0];
+    float v[8];
+    if (DIM == 2) {
+        const float* b = V + k[0] + L0 * k[1];
+        v[0] = __ldg(b);
+        v[1] = __ldg(b + 1);
+        v[2] = __ldg(b + L0);
+        v[3] = __ldg(b + L0 + 1);
+    } else {
+        const int64_t L1 = g.nvel[comp][1];
+        const int64_t sz = L0 * L1;
+        const float* b = V + k[0] + L0 * (k[1] + L1 * (int64_t)k[2]);
+        v[0] = __ldg(b);
+        v[1] = __ldg(b + 1);
+        v[2] = __ldg(b + L0);
+        v[3] = __ldg(b + L0 + 1);
+        v[4] = __ldg(b + sz);
+        v[5] = __ldg(b + sz + 1);
+        v[6] = __ldg(b + sz + L0);
+        v[7] = __ldg(b + sz + L0 + 1);
+    }
+    return lerpNf<DIM>(v, t);
+}
+
+template <int DIM, int METHOD>
+__device__ __forceinline__ void advect_f32(const DevGrid& g, const CVelF& V, const F32Params& P, const int* I,
+                                           const float* x0, float* x)
+{
+    float v0[3], v1[3], q[3];
+    if (METHOD == JP_RUNGE_KUTTA2) {
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) v0[c] = velocity_f32<DIM>(g, c, I, x0, V.v[c]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) q[d] = fmaf(P.aw[d], v0[d], x0[d]);
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) v1[c] = velocity_f32<DIM>(g, c, I, q, V.v[c]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            x[d] = P.half ? fmaf(P.w[d], v1[d], x0[d]) : fmaf(P.w[d], fmaf(P.ca, v0[d], P.cb * v1[d]), x0[d]);
+    } else if (METHOD == JP_RUNGE_KUTTA4) {
+        float k1[3], k2[3], k3[3], k4[3];
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) k1[c] = velocity_f32<DIM>(g, c, I, x0, V.v[c]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) q[d] = fmaf(0.5f * P.w[d], k1[d], x0[d]);
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) k2[c] = velocity_f32<DIM>(g, c, I, q, V.v[c]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) q[d] = fmaf(0.5f * P.w[d], k2[d], x0[d]);
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) k3[c] = velocity_f32<DIM>(g, c, I, q, V.v[c]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) q[d] = fmaf(P.w[d], k3[d], x0[d]);
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) k4[c] = velocity_f32<DIM>(g, c, I, q, V.v[c]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            x[d] = fmaf(P.w[d] * (1.0f / 6.0f), (k1[d] + 2.0f * k2[d]) + (2.0f * k3[d] + k4[d]), x0[d]);
+    } else {
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) v0[c] = velocity_f32<DIM>(g, c, I, x0, V.v[c]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) x[d] = fmaf(P.w[d], v0[d], x0[d]);
+    }
+}
+
+template <int DIM, int METHOD>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    advect_f32_kernel(DevGrid g, CVelF V, F32Params P, XiF Xi, const uint8_t* __restrict__ index)
+{
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ int cellI[kWarpsPerBlock][32][3];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
+    }
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        const int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
+        float x0[3], x[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) x0[d] = Xi.x[d][a];
+        advect_f32<DIM, METHOD>(g, V, P, I, x0, x);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) Xi.x[d][a] = x[d];
+    }
+}
+
+// ------------------------------------------------------------------- move
+struct MoveViewF {
+    MoveView m;
+    float* shadow;  // interleaved records: DIM offsets, then the fields
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    move_classify_f32(DevGrid g, XiF Xi, const uint8_t* __restrict__ index, ArgsF A, MoveViewF S, int* d_err)
+{
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ int cellI[kWarpsPerBlock][32][3];
+    __shared__ unsigned long long movers[kWarpsPerBlock][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
+        movers[w][lane] = 0;
+    }
+    uint64_t L;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &L);
+    const int comps = S.m.comps;
+    int errs = 0;
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        float xi[3];
+        bool out = false;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            xi[d] = Xi.x[d][a];
+            out |= !(xi[d] >= 0.0f && xi[d] < 1.0f);
+        }
+        float* rec = S.shadow + a * comps;
+        for (int j = 0; j < A.n; ++j) rec[DIM + j] = A.a[j][a];
+        if (!out) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) rec[d] = xi[d];
+            S.m.code[a] = kCodeStay;
+            continue;
+        }
+        atomicOr(&movers[w][l], 1ull << s);
+        uint8_t code = kCodeExit;
+        int off[3] = {0, 0, 0};
+        bool inside = true, far = false;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            if (!(fabsf(xi[d]) < 1e6f)) {  // NaN / Inf: left the domain
+                inside = false;
+                continue;
+            }
+            const float fl = floorf(xi[d]);
+            const int o = (int)fl;
+            const int T = cellI[w][l][d] + o;
+            inside &= T >= 0 && T < g.n[d];
+            far |= o > 1 || o < -1;
+            off[d] = o;
+            // re-normalised offset in the target cell, in FP64, kept below 1
+            float r = (float)((double)xi[d] - (double)fl);
+            rec[d] = r < 1.0f ? r : 0x1.fffffep-1f;
+        }
+        if (inside) {
+            if (far) {
+                errs |= kWarnFarMove;
+            } else {
+                code = (uint8_t)nb_code<DIM>(off);
+            }
+        }
+        S.m.code[a] = code;
+    }
+    __syncwarp();
+    const int64_t c = c0 + lane;
+    if (c < nc) {
+        S.m.L0[c] = L;
+        S.m.L[c] = L;
+        S.m.M[c] = movers[w][lane];
+        S.m.R[c] = 0;
+        S.m.U[c] = 0;
+    }
+    raise_err(d_err, errs);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    move_apply_f32(DevGrid g, XiF Xi, uint8_t* __restrict__ index, ArgsF A, MoveViewF S)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nc = g.ncells;
+    const bool valid = c < nc;
+    uint64_t L0 = 0, L = 0, R = 0;
+    if (valid) {
+        L0 = S.m.L0[c];
+        L = S.m.L[c];
+        R = S.m.R[c];
+    }
+    const uint64_t changed = (L0 & ~L) | R;
+    const uint32_t hi_any = __reduce_max_sync(0xffffffffu, changed ? 64u - (uint32_t)__clzll((long long)changed) : 0u);
+    if (hi_any == 0) return;
+    int64_t I[3] = {0, 0, 0};
+    if (valid) cell_coords(g, c, I);
+    const int comps = S.m.comps;
+    for (int s = 0; s < (int)hi_any; ++s) {
+        if (!((changed >> s) & 1)) continue;
+        const int64_t a = c + nc * s;
+        if ((R >> s) & 1) {
+            const uint16_t tag = S.m.orig[a];
+            int off[3];
+            nb_offset<DIM>(tag & 0x1F, off);
+            const int64_t J[3] = {I[0] + off[0], I[1] + off[1], DIM == 3 ? I[2] + off[2] : 0};
+            const float* rec = S.shadow + (cell_linear<DIM>(g, J) + nc * (tag >> 5)) * comps;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) Xi.x[d][a] = rec[d];
+            for (int k = 0; k < A.n; ++k) A.a[k][a] = rec[DIM + k];
+            index[a] = 1;
+        } else {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) Xi.x[d][a] = CUDART_NAN_F;
+            for (int k = 0; k < A.n; ++k) A.a[k][a] = CUDART_NAN_F;
+            index[a] = 0;
+        }
+    }
+}
+
+// ------------------------------------------------------------- injection
+struct InjectListsF {
+    int* counts;
+    int* list;
+    int64_t off[8];
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    inject_flag_f32(DevGrid g, CXiF Xi, const uint8_t* __restrict__ index, InjectListsF Ls)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool flag = false;
+    int col = 0;
+    if (c < g.ncells) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        col = (int)(I[0] & 1) + 2 * (int)(I[1] & 1) + (DIM == 3 ? 4 * (int)(I[2] & 1) : 0);
+        const int64_t nc = g.ncells;
+        const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
+        int count = 0;
+        for (int s = 0; s < g.max_xcell && count < min_xq; ++s) {
+            const int64_t a = c + nc * s;
+            if (!index[a]) continue;
+            bool in = true;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const float x = Xi.x[d][a];
+                in = in && x > 0.0f && x < 0.5f;
+            }
+            count += in ? 1 : 0;
+        }
+        flag = count < min_xq;
+    }
+    const unsigned active = __ballot_sync(0xffffffffu, flag);
+    if (flag) {
+        const unsigned grp = __match_any_sync(active, col);
+        const int leader = __ffs(grp) - 1;
+        const int rank = __popc(grp & ((1u << lane) - 1u));
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&Ls.counts[col], __popc(grp));
+        base = __shfl_sync(grp, base, leader);
+        Ls.list[Ls.off[col] + base + rank] = (int)c;
+    }
+}
+
+template <int DIM>
+__host__ __device__ __forceinline__ size_t hood_bytes_f32(int M)
+{
+    const int n = (DIM == 2 ? 9 : 27) * M;
+    const size_t bytes = (size_t)n * (DIM * sizeof(float) + 1);
+    return (bytes + 15) & ~(size_t)15;
+}
+
+template <int DIM>
+__device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const XiF& Xi,
+                                     uint8_t* __restrict__ index, const ArgsF& A, uint32_t call, int64_t c,
+                                     float* const* r, uint8_t* live, int lane, int* errs)
+{
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    constexpr int NB = DIM == 2 ? 9 : 27;
+    constexpr int CENTER = DIM == 2 ? 4 : 13;
+    const int ncand = NB * M;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    // stage: positions in cell units relative to this cell's lower-left vertex
+    for (int o = lane; o < ncand; o += 32) {
+        const int nb = o / M, s = o - nb * M;
+        const int off[3] = {nb % 3 - 1, (nb / 3) % 3 - 1, DIM == 3 ? nb / 9 - 1 : 0};
+        const int64_t J[3] = {I[0] + off[0], I[1] + off[1], I[2] + off[2]};
+        bool ok = J[0] >= 0 && J[1] >= 0 && J[0] < g.n[0] && J[1] < g.n[1] &&
+                  (DIM == 2 || (J[2] >= 0 && J[2] < g.n[2]));
+        uint8_t lv = 0;
+        if (ok) {
+            const int64_t a = cell_linear<DIM>(g, J) + nc * s;
+            lv = index[a];
+            if (lv) {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) r[d][o] = (float)off[d] + Xi.x[d][a];
+            }
+        }
+        live[o] = lv;
+    }
+    __syncwarp();
+    const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
+    const int base = CENTER * M;
+    for (int q = 0; q < (1 << DIM); ++q) {
+        float qc[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) qc[d] = 0.5f * (float)((q >> d) & 1);
+        int cnt = 0;
+        for (int s = lane; s < M; s += 32) {
+            if (!live[base + s]) continue;
+            bool in = true;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) in = in && r[d][base + s] > qc[d] && r[d][base + s] < qc[d] + 0.5f;
+            cnt += in ? 1 : 0;
+        }
+        int count = __reduce_add_sync(0xffffffffu, cnt);
+        if (count >= min_xq) break;
+        const bool f0 = lane < M && !live[base + lane];
+        const bool f1 = lane + 32 < M && !live[base + lane + 32];
+        uint64_t freem = (uint64_t)__ballot_sync(0xffffffffu, f0) | ((uint64_t)__ballot_sync(0xffffffffu, f1) << 32);
+        while (freem) {
+            const int i = __ffsll((long long)freem) - 1;
+            freem &= freem - 1;
+            ++count;
+            float pn[3];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const float u = jp_rand_uniform_f32(g.seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)i,
+                                                    (uint32_t)d);
+                pn[d] = qc[d] + 0.5f * fmaf(0.95f, u, 0.05f);
+            }
+            const int64_t ai = c + nc * i;
+            if (lane == 0) {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    Xi.x[d][ai] = pn[d];
+                    r[d][base + i] = pn[d];
+                }
+                index[ai] = 1;
+                live[base + i] = 1;
+            }
+            __syncwarp();
+            // nearest: first minimum of the FP32 squared physical distance in candidate order
+            float best = CUDART_INF_F;
+            int bo = 0x7fffffff;
+            for (int o = lane; o < ncand; o += 32) {
+                if (!live[o] || o == base + i) continue;
+                float ss = 0.0f;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const float e = (r[d][o] - pn[d]) * P.dx[d];
+                    ss = fmaf(e, e, ss);
+                }
+                if (ss < best) {  // NaN never wins
+                    best = ss;
+                    bo = o;
+                }
+            }
+#pragma unroll
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                const float ob = __shfl_xor_sync(0xffffffffu, best, sh);
+                const int oo = __shfl_xor_sync(0xffffffffu, bo, sh);
+                if (ob < best || (ob == best && oo < bo)) {
+                    best = ob;
+                    bo = oo;
+                }
+            }
+            if (bo != 0x7fffffff) {
+                const int nb = bo / M, s = bo - nb * M;
+                const int64_t J[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1, DIM == 3 ? I[2] + nb / 9 - 1 : 0};
+                const int64_t src = cell_linear<DIM>(g, J) + nc * s;
+                for (int k = lane; k < A.n; k += 32) A.a[k][ai] = A.a[k][src];
+            } else if (A.n > 0) {
+                *errs |= kWarnNoNeighbour;
+            }
+            __syncwarp();
+            if (count >= min_xq) break;
+        }
+    }
+}
+
+template <int DIM>
+__global__ void inject_pass_f32(DevGrid g, F32Params P, XiF Xi, uint8_t* __restrict__ index, ArgsF A,
+                                InjectListsF Ls, int col, uint32_t call, int* d_err)
+{
+    extern __shared__ __align__(16) unsigned char smem_f32[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int M = g.max_xcell;
+    const int ncand = (DIM == 2 ? 9 : 27) * M;
+    unsigned char* base = smem_f32 + (size_t)wib * hood_bytes_f32<DIM>(M);
+    float* r[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) r[d] = (float*)base + (size_t)d * ncand;
+    uint8_t* live = base + (size_t)DIM * ncand * sizeof(float);
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int count = Ls.counts[col];
+    int errs = 0;
+    for (int k = gw; k < count; k += nwarps) {
+        const int64_t c = Ls.list[Ls.off[col] + k];
+        inject_cell_warp_f32<DIM>(g, P, Xi, index, A, call, c, r, live, lane, &errs);
+        __syncwarp();
+    }
+    raise_err(d_err, errs);
+}
+
+// ------------------------------------------------------- grid2particle!
+template <int DIM>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    g2p_f32_kernel(DevGrid g, float* __restrict__ Fp, const float* __restrict__ F, CXiF Xi,
+                   const uint8_t* __restrict__ index)
+{
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ float cellv[kWarpsPerBlock][32][1 << DIM];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+        const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
+        float* cv = cellv[w][lane];
+        const float* b = F + I[0] + V0 * (I[1] + (DIM == 3 ? V1 * I[2] : 0));
+        cv[0] = __ldg(b);
+        cv[1] = __ldg(b + 1);
+        cv[2] = __ldg(b + V0);
+        cv[3] = __ldg(b + V0 + 1);
+        if (DIM == 3) {
+            const int64_t sz = V0 * V1;
+            cv[4] = __ldg(b + sz);
+            cv[5] = __ldg(b + sz + 1);
+            cv[6] = __ldg(b + sz + V0);
+            cv[7] = __ldg(b + sz + V0 + 1);
+        }
+    }
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        float t[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) t[d] = Xi.x[d][a];
+        Fp[a] = lerpNf<DIM>(cellv[w][l], t);
+    }
+}
+
+// ------------------------------------------------------- particle2grid!
+// Same marching scheme and accumulation order as the FP64 kernel; weights in
+// FP32, their sums (and the weighted field sums) in FP64.
+template <int DIM>
+__device__ __forceinline__ void p2g_cell_f32(int64_t c, uint64_t mask, int64_t nc, const float* kc, const float* kn,
+                                             bool do_cur, bool do_nxt, const float* dx,
+                                             const float* __restrict__ Fp, const CXiF& Xi, double& w_c, double& wF_c,
+                                             double& w_n, double& wF_n)
+{
+    while (mask) {
+        const int s = __ffsll((long long)mask) - 1;
+        mask &= mask - 1;
+        const int64_t a = c + nc * s;
+        float xi[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xi[d] = Xi.x[d][a];
+        const double f = (double)Fp[a];
+        if (do_cur) {
+            float ss = 0.0f;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const float e = (kc[d] - xi[d]) * dx[d];
+                ss = fmaf(e, e, ss);
+            }
+            const double wi = (double)__frcp_rn(ss);
+            w_c += wi;
+            wF_c = fma(wi, f, wF_c);
+        }
+        if (do_nxt) {
+            float ss = 0.0f;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const float e = (kn[d] - xi[d]) * dx[d];
+                ss = fmaf(e, e, ss);
+            }
+            const double wi = (double)__frcp_rn(ss);
+            w_n += wi;
+            wF_n = fma(wi, f, wF_n);
+        }
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    p2g_f32_kernel(DevGrid g, F32Params P, float* __restrict__ F, const float* __restrict__ Fp, CXiF Xi,
+                   const uint8_t* __restrict__ index, int chunk, int64_t nthreads)
+{
+    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    constexpr int LAST = DIM - 1;
+    const int64_t nlast = g.n[LAST];
+    const int64_t cols = DIM == 2 ? V0 : V0 * V1;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    const bool active = t < nthreads;
+    const int64_t col = active ? t % cols : 0;
+    const int64_t q = active ? t / cols : 0;
+    const int64_t r0 = q * chunk;
+    const int64_t r1 = active ? min(r0 + (int64_t)chunk, nlast + 1) : r0;
+    const int64_t i = col % V0;
+    const int64_t j = DIM == 3 ? col / V0 : 0;
+    const bool has_i0 = i >= 1, has_i1 = i < g.n[0];
+    const bool has_j0 = DIM == 2 || j >= 1, has_j1 = DIM == 2 || j < g.n[1];
+    auto cell = [&](int di, int dj, int64_t r) -> int64_t {
+        return DIM == 2 ? (i + di) + g.n[0] * r : (i + di) + g.n[0] * ((j + dj) + g.n[1] * r);
+    };
+    // vertex position relative to a cell's lower-left corner, in cell units:
+    // the own cell (i, j) sees the vertex at 0, the cell to the left at 1, ...
+    auto row = [&](int64_t r, bool do_cur, bool do_nxt, double& w_c, double& wF_c, double& w_n, double& wF_n) {
+        const bool rok = active && r >= 0 && r < nlast;
+        const uint64_t m_own = (rok && has_i1 && has_j1) ? live_mask(index, cell(0, 0, r), nc, M) : 0;
+        uint64_t m_left = __shfl_up_sync(0xffffffffu, m_own, 1);
+        if (lane == 0 && rok && has_i0 && has_j1) m_left = live_mask(index, cell(-1, 0, r), nc, M);
+        if (!(rok && has_i0 && has_j1)) m_left = 0;
+        // the current vertex row is the cell row's lower side (0), the next one its upper side (1)
+        float kc[3], kn[3];
+        if (DIM == 3) {
+            const uint64_t mb0 = (rok && has_i0 && has_j0) ? live_mask(index, cell(-1, -1, r), nc, M) : 0;
+            const uint64_t mb1 = (rok && has_i1 && has_j0) ? live_mask(index, cell(0, -1, r), nc, M) : 0;
+            kc[1] = kn[1] = 1.0f;
+            kc[2] = 0.0f;
+            kn[2] = 1.0f;
+            kc[0] = kn[0] = 1.0f;
+            if (mb0) p2g_cell_f32<DIM>(cell(-1, -1, r), mb0, nc, kc, kn, do_cur, do_nxt, P.dx, Fp, Xi, w_c, wF_c, w_n, wF_n);
+            kc[0] = kn[0] = 0.0f;
+            if (mb1) p2g_cell_f32<DIM>(cell(0, -1, r), mb1, nc, kc, kn, do_cur, do_nxt, P.dx, Fp, Xi, w_c, wF_c, w_n, wF_n);
+            kc[1] = kn[1] = 0.0f;
+        } else {
+            kc[1] = 0.0f;
+            kn[1] = 1.0f;
+        }
+        kc[0] = kn[0] = 1.0f;
+        if (m_left) p2g_cell_f32<DIM>(cell(-1, 0, r), m_left, nc, kc, kn, do_cur, do_nxt, P.dx, Fp, Xi, w_c, wF_c, w_n, wF_n);
+        kc[0] = kn[0] = 0.0f;
+        if (m_own) p2g_cell_f32<DIM>(cell(0, 0, r), m_own, nc, kc, kn, do_cur, do_nxt, P.dx, Fp, Xi, w_c, wF_c, w_n, wF_n);
+    };
+    double w_c = 0.0, wF_c = 0.0, w_n = 0.0, wF_n = 0.0;
+    {
+        double wd = 0.0, wFd = 0.0;
+        row(r0 - 1, false, true, wd, wFd, w_c, wF_c);
+    }
+    for (int k = 0; k < chunk; ++k) {
+        const int64_t r = r0 + k;
+        const bool vok = r < r1;
+        const bool has_next = r + 1 < r1;
+        w_n = 0.0;
+        wF_n = 0.0;
+        row(vok ? r : -1, vok, has_next, w_c, wF_c, w_n, wF_n);
+        if (vok) {
+            const int64_t v = DIM == 2 ? i + V0 * r : i + V0 * (j + V1 * r);
+            F[v] = (float)(wF_c / w_c);
+        }
+        w_c = w_n;
+        wF_c = wF_n;
+    }
+}
+
+// ------------------------------------------------------------ launchers
+static F32Params make_params(const jp_particles* P, double alpha, double dt)
+{
+    F32Params p{};
+    for (int d = 0; d < 3; ++d) {
+        const double dx = P->dx_host[d];
+        p.dx[d] = (float)dx;
+        p.w[d] = (float)(dt / dx);
+        p.aw[d] = (float)(alpha * dt / dx);
+    }
+    const double ia = 1.0 / alpha;
+    p.ca = (float)std::fma(-0.5, ia, 1.0);
+    p.cb = (float)(0.5 * ia);
+    p.half = alpha == 0.5;
+    return p;
+}
+
+cudaError_t launch_to_offsets(jp_particles* P, const double* const coords[3], const uint8_t* index,
+                              float* const xi[3])
+{
+    const bool d3 = P->g.ndim == 3;
+    CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
+    XiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
+    const unsigned nb = grid_blocks(P->g.ncells);
+    if (!d3)
+        to_offsets<2><<<nb, kThreads, 0, P->stream>>>(P->g, X, index, Xi);
+    else
+        to_offsets<3><<<nb, kThreads, 0, P->stream>>>(P->g, X, index, Xi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_coords(jp_particles* P, const float* const xi[3], const uint8_t* index,
+                             double* const coords[3])
+{
+    const bool d3 = P->g.ndim == 3;
+    Coords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
+    CXiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
+    const unsigned nb = grid_blocks(P->g.ncells);
+    if (!d3)
+        to_coords<2><<<nb, kThreads, 0, P->stream>>>(P->g, Xi, index, X);
+    else
+        to_coords<3><<<nb, kThreads, 0, P->stream>>>(P->g, Xi, index, X);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advection_f32(jp_particles* P, int method, double alpha, const float* const V[3], double dt,
+                                 float* const xi[3], const uint8_t* index)
+{
+    const bool d3 = P->g.ndim == 3;
+    XiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
+    CVelF Vv{{V[0], V[1], d3 ? V[2] : nullptr}};
+    const F32Params prm = make_params(P, alpha, dt);
+    const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const int nt = 32 * kWarpsPerBlock;
+    cudaStream_t s = P->stream;
+#define JP_ADVF(D, M) advect_f32_kernel<D, M><<<nb, nt, 0, s>>>(P->g, Vv, prm, Xi, index)
+    if (!d3) {
+        if (method == JP_RUNGE_KUTTA2) JP_ADVF(2, JP_RUNGE_KUTTA2);
+        else if (method == JP_RUNGE_KUTTA4) JP_ADVF(2, JP_RUNGE_KUTTA4);
+        else JP_ADVF(2, JP_EULER);
+    } else {
+        if (method == JP_RUNGE_KUTTA2) JP_ADVF(3, JP_RUNGE_KUTTA2);
+        else if (method == JP_RUNGE_KUTTA4) JP_ADVF(3, JP_RUNGE_KUTTA4);
+        else JP_ADVF(3, JP_EULER);
+    }
+#undef JP_ADVF
+    return cudaGetLastError();
+}
+
+cudaError_t launch_move_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int nargs)
+{
+    const int N = P->g.ndim;
+    // FP32 records (4 bytes per value) fit in the scratch sized for FP64 records
+    cudaError_t e = ensure_move_scratch(P, N + nargs);
+    if (e != cudaSuccess) return e;
+    XiF Xi{{xi[0], xi[1], N == 3 ? xi[2] : nullptr}};
+    ArgsF A{};
+    A.n = nargs;
+    for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
+    const MoveScratch& m = P->move;
+    MoveViewF S;
+    S.m = MoveView{m.L0, m.L, m.M, m.R, m.U, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, N + nargs};
+    S.shadow = (float*)m.shadow;
+    cudaStream_t st = P->stream;
+    const unsigned nb = grid_blocks(P->g.ncells);
+    const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const int ntw = 32 * kWarpsPerBlock;
+    int64_t mc[3] = {1, 1, 1};
+    for (int d = 0; d < N; ++d) mc[d] = (P->g.n[d] + 2) / 3;
+    const unsigned nbp = grid_blocks(mc[0] * mc[1] * mc[2], kAllocThreads);
+    if (N == 2) {
+        move_classify_f32<2><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, P->d_err);
+        for (int pass = 0; pass < 9; ++pass)
+            move_allocate<2><<<nbp, kAllocThreads, 0, st>>>(P->g, S.m, pass / 3, pass % 3, 0, mc[0], mc[1], 1);
+        move_apply_f32<2><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S);
+    } else {
+        move_classify_f32<3><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, P->d_err);
+        for (int pass = 0; pass < 27; ++pass)
+            move_allocate<3><<<nbp, kAllocThreads, 0, st>>>(P->g, S.m, pass / 9, (pass / 3) % 3, pass % 3, mc[0],
+                                                            mc[1], mc[2]);
+        move_apply_f32<3><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_inject_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int nargs,
+                              uint32_t call)
+{
+    const int N = P->g.ndim;
+    const int64_t nc = P->g.ncells;
+    if (!P->inject.counts) {
+        cudaError_t e = cudaMalloc(&P->inject.counts, (8 + nc) * sizeof(int));
+        if (e != cudaSuccess) return e;
+        P->inject.list = P->inject.counts + 8;
+    }
+    InjectListsF Ls;
+    Ls.counts = P->inject.counts;
+    Ls.list = P->inject.list;
+    int64_t cnt[3][2];
+    for (int d = 0; d < 3; ++d)
+        for (int o = 0; o < 2; ++o) cnt[d][o] = d < N ? (P->g.n[d] - o + 1) / 2 : (o == 0 ? 1 : 0);
+    int64_t off = 0;
+    for (int col = 0; col < 8; ++col) {
+        Ls.off[col] = off;
+        off += cnt[0][col & 1] * cnt[1][(col >> 1) & 1] * cnt[2][(col >> 2) & 1];
+    }
+    cudaStream_t st = P->stream;
+    cudaError_t e = cudaMemsetAsync(P->inject.counts, 0, 8 * sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    XiF Xi{{xi[0], xi[1], N == 3 ? xi[2] : nullptr}};
+    CXiF CX{{xi[0], xi[1], N == 3 ? xi[2] : nullptr}};
+    ArgsF A{};
+    A.n = nargs;
+    for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
+    const F32Params prm = make_params(P, 0.5, 0.0);
+    const unsigned nb = grid_blocks(nc);
+    const int M = P->g.max_xcell;
+    const int wpb = 4;
+    const size_t smem = N == 2 ? wpb * hood_bytes_f32<2>(M) : wpb * hood_bytes_f32<3>(M);
+    const unsigned nbp = (unsigned)(152 * 8);
+    if (N == 2) {
+        inject_flag_f32<2><<<nb, kThreads, 0, st>>>(P->g, CX, index, Ls);
+        for (int pass = 0; pass < 4; ++pass) {
+            const int col = (pass / 2) + 2 * (pass % 2);
+            inject_pass_f32<2><<<nbp, 32 * wpb, smem, st>>>(P->g, prm, Xi, index, A, Ls, col, call, P->d_err);
+        }
+    } else {
+        if (smem > 48 * 1024) {
+            e = cudaFuncSetAttribute(inject_pass_f32<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        inject_flag_f32<3><<<nb, kThreads, 0, st>>>(P->g, CX, index, Ls);
+        for (int pass = 0; pass < 8; ++pass) {
+            const int col = (pass / 4) + 2 * ((pass / 2) % 2) + 4 * (pass % 2);
+            inject_pass_f32<3><<<nbp, 32 * wpb, smem, st>>>(P->g, prm, Xi, index, A, Ls, col, call, P->d_err);
+        }
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_g2p_f32(jp_particles* P, float* Fp, const float* F, const float* const xi[3],
+                           const uint8_t* index)
+{
+    const bool d3 = P->g.ndim == 3;
+    CXiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
+    const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const int nt = 32 * kWarpsPerBlock;
+    if (!d3)
+        g2p_f32_kernel<2><<<nb, nt, 0, P->stream>>>(P->g, Fp, F, Xi, index);
+    else
+        g2p_f32_kernel<3><<<nb, nt, 0, P->stream>>>(P->g, Fp, F, Xi, index);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_p2g_f32(jp_particles* P, float* F, const float* Fp, const float* const xi[3],
+                           const uint8_t* index)
+{
+    const bool d3 = P->g.ndim == 3;
+    CXiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
+    const F32Params prm = make_params(P, 0.5, 0.0);
+    const int64_t V0 = P->g.n[0] + 1, V1 = P->g.n[1] + 1;
+    const int64_t cols = d3 ? V0 * V1 : V0;
+    const int64_t rows = P->g.n[d3 ? 2 : 1] + 1;
+    const int64_t want = 152LL * 2048;
+    int chunk = (int)((cols * rows) / want);
+    chunk = chunk < 2 ? 2 : (chunk > 16 ? 16 : chunk);
+    const int64_t nthreads = cols * ((rows + chunk - 1) / chunk);
+    const unsigned nb = grid_blocks(nthreads);
+    if (!d3)
+        p2g_f32_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, chunk, nthreads);
+    else
+        p2g_f32_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, chunk, nthreads);
+    return cudaGetLastError();
+}
+
+}  // namespace jp

@@ -78,6 +78,8 @@ struct jp_particles {
     int synchronous = 1;
     uint32_t warnings = 0;
     uint64_t inject_calls = 0;
+    double dx_host[3] = {1.0, 1.0, 1.0};  // spacing per axis (uniform grids) for the split-precision form
+    int staggered_std = 0;                // velocity grids have the standard ghost-node staggering
     jp::MoveScratch move;
     jp::InjectScratch inject;
 };
@@ -289,6 +291,15 @@ __device__ __forceinline__ void slot_item(const SlotList& Lst, int M, int k, int
 
 constexpr int kWarpsPerBlock = 8;
 
+// 64-bit occupancy mask of cell c (bit s = slot s is live)
+__device__ __forceinline__ uint64_t live_mask(const uint8_t* __restrict__ index, int64_t c, int64_t nc, int M)
+{
+    uint64_t m = 0;
+#pragma unroll 8
+    for (int s = 0; s < M; ++s) m |= (uint64_t)(index[c + nc * s] != 0) << s;
+    return m;
+}
+
 inline unsigned grid_blocks(int64_t n, int threads = kThreads)
 {
     return (unsigned)((n + threads - 1) / threads);
@@ -306,6 +317,24 @@ cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const doubl
                        const uint8_t* index);
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
                        const uint8_t* index);
+
+// scratch of move_particles! owned by the container (allocated on first use)
+cudaError_t ensure_move_scratch(jp_particles* P, int comps);
+
+// split-precision form (jp_f32.cu)
+cudaError_t launch_to_offsets(jp_particles* P, const double* const coords[3], const uint8_t* index,
+                              float* const xi[3]);
+cudaError_t launch_to_coords(jp_particles* P, const float* const xi[3], const uint8_t* index,
+                             double* const coords[3]);
+cudaError_t launch_advection_f32(jp_particles* P, int method, double alpha, const float* const V[3], double dt,
+                                 float* const xi[3], const uint8_t* index);
+cudaError_t launch_move_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int nargs);
+cudaError_t launch_inject_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int nargs,
+                              uint32_t call);
+cudaError_t launch_g2p_f32(jp_particles* P, float* Fp, const float* F, const float* const xi[3],
+                           const uint8_t* index);
+cudaError_t launch_p2g_f32(jp_particles* P, float* F, const float* Fp, const float* const xi[3],
+                           const uint8_t* index);
 
 // move_particles! with its scratch in a fixed device array (no allocation)
 constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;

@@ -287,14 +287,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 // cell is walked through its 64-bit live mask, so no lane spends FP64 issue
 // slots on empty slots; the mask of the left neighbour cell comes from the
 // neighbouring lane. The loop trip count is the same for every lane of a warp.
-__device__ __forceinline__ uint64_t live_mask(const uint8_t* __restrict__ index, int64_t c, int64_t nc, int M)
-{
-    uint64_t m = 0;
-#pragma unroll 8
-    for (int s = 0; s < M; ++s) m |= (uint64_t)(index[c + nc * s] != 0) << s;
-    return m;
-}
-
 template <int DIM>
 __device__ __forceinline__ void p2g_cell(int64_t c, uint64_t mask, int64_t nc, const double* q_cur,
                                          const double* q_nxt, bool do_cur, bool do_nxt,

@@ -104,6 +104,9 @@ CONFIGS = {
                velocity="rotation", fields=1,
                desc="2D temperature advection, FP64, 1024x1024 cells, rigid rotation, advection!+move_particles!"
                     "+inject_particles!+grid2particle!+particle2grid!"),
+    "C4": dict(ni=(2048, 2048), nxcell=24, max_xcell=48, min_xcell=12, method="RK4", steps=750,
+               velocity="stream", fields=1,
+               desc="2D split-precision comparison, 2048x2048 cells, stream-function velocity, RK4, C2 step"),
     "C3": dict(ni=(128, 128, 128), nxcell=24, max_xcell=48, min_xcell=12, method="RK2", steps=300,
                velocity="cellular3d", fields=1,
                desc="3D temperature advection, FP64, 128^3 cells, cellular flow + 0.1 z drift, advection!"
