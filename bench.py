@@ -44,6 +44,7 @@ STEPS = {
     "C2": ["particle2grid!", "advection!", "move_particles!", "inject_particles!", "grid2particle!"],
     "C3": ["particle2grid!", "advection!", "move_particles!", "inject_particles!"],
     "C4": ["particle2grid!", "advection!", "move_particles!", "inject_particles!", "grid2particle!"],
+    "C5": ["advection!", "move_particles!", "inject_particles!"],
 }
 DESC = {
     "C1": "C1: 2D RK2 advection FP64, 256x256 cells, 24/48/12 particles per cell, stream-function velocity, "
@@ -54,6 +55,9 @@ DESC = {
           "drift, RK2, step = particle2grid!+advection!+move_particles!+inject_particles!",
     "C4": "C4: 2D, 2048x2048 cells, 24/48/12 particles per cell, stream-function velocity, RK4, "
           "step = particle2grid!+advection!+move_particles!+inject_particles!+grid2particle!",
+    "C5": "C5: 2D adjoint, FP64, 512x512 cells, 16/32/8 particles per cell, stream-function velocity plus "
+          "N(0, 25^2) node noise, RK2, 100 steps, loss 0.5||particle2grid(T) - T_target||^2, checkpoints every "
+          "10 steps, gradients w.r.t. Vx, Vy, T0",
 }
 
 
@@ -409,8 +413,9 @@ def run_ours(args):
 def run_compare(args):
     """The same seeded run in both forms for ``--steps`` steps (no timing):
     position error of the split-precision form in cell widths, by particle id,
-    for every particle present once in both runs, and L-inf / L2 error of the
-    gridded field, both against the FP64 form."""
+    for every initial particle still present in both runs (injected particles
+    copy a neighbour's fields, so their ids are cleared), and L-inf / L2 error
+    of the gridded field, both against the FP64 form."""
     import torch
 
     import justpic_gb300 as jp
@@ -447,24 +452,31 @@ def run_compare(args):
         jp.particle2grid_(Ta, pTa, a)
         jp.advection_(a, method, Va, dt)
         jp.move_particles_(a, fa)
+        before = a.index.data.clone()
         jp.inject_particles_(a, fa)
+        fa[1].data[a.index.data.bool() & ~before.bool()] = float("nan")  # injected copies carry no id
         jp.grid2particle_(pTa, Ta, a)
         jp.particle2grid_f32_(Tb, pTb, b, xi)
         jp.advection_f32_(b, xi, method, Vb, dt)
         jp.move_particles_f32_(b, xi, fb)
+        before = b.index.data.clone()
         jp.inject_particles_f32_(b, xi, fb)
+        new = b.index.data.bool() & ~before.bool()
+        fb[1].data[new] = float("nan")
+        fb[2].data[new] = float("nan")
         jp.grid2particle_f32_(pTb, Tb, b, xi)
     jp.synchronize(a)
     jp.synchronize(b)
     wall = time.perf_counter() - w0
-    la = a.index.data.bool()
-    lb = b.index.data.bool()
+    # original particles only: every injected particle (and its copies' ids) was marked NaN
+    la = a.index.data.bool() & ~torch.isnan(fa[1].data)
+    lb = b.index.data.bool() & ~torch.isnan(fb[1].data)
     ida = fa[1].data[la].long()
     idb = (fb[1].data[lb].double() * 4096 + fb[2].data[lb].double()).long()
     pa = torch.stack([c.data[la] for c in a.coords], 1)
     back = jp.coords_from_offsets(b, xi)
     pb = torch.stack([c.data[lb] for c in back], 1)
-    n_ids = int(ida.max()) + 2
+    n_ids = int(max(int(ida.max()), int(idb.max()))) + 2
 
     def unique_pos(idv, pos):
         cnt = torch.bincount(idv, minlength=n_ids)
@@ -483,7 +495,7 @@ def run_compare(args):
         "integrator": type(method).__name__,
         "steps": args.steps,
         "particles_compared": int(both.sum()),
-        "live_fp64": int(la.sum()), "live_split": int(lb.sum()),
+        "live_fp64": int(a.index.data.sum()), "live_split": int(b.index.data.sum()),
         "position_error_cells": {"max": float(err.max()), "p99": float(torch.quantile(err[:1 << 24], 0.99)),
                                  "mean": float(err.mean())},
         "gridded_field_error": {"linf": float(Ferr.abs().max()),
@@ -492,6 +504,81 @@ def run_compare(args):
         "wall_s_both_forms": wall,
     }
     print(json.dumps(out))
+
+
+def run_adjoint(args):
+    """C5: cost of the checkpointed gradient against the forward run alone,
+    and central finite differences (h = 1e-6) on --fd-nodes random velocity
+    nodes, each formed vertex by vertex."""
+    import torch
+
+    import justpic_gb300 as jp
+    from justpic_gb300 import adjoint as A
+
+    torch.cuda.set_device(0)
+    cfg = _setup_cfg("C5", args.ni)
+    g = cfg["grid"]
+    nsteps = cfg["steps"]
+    k = cfg["checkpoint_every"]
+    p = jp.init_particles(jp.CUDABackend, cfg["nxcell"], cfg["max_xcell"], cfg["min_xcell"], *g["grid_v"])
+    V = tuple(jp.TA("CUDA")(v) for v in cfg["V"])
+    dt = cfg["dt"]
+    (T0,) = jp.init_cell_arrays(p, 1)
+    jp.grid2particle_(T0, jp.TA("CUDA")(cfg["T"]), p)
+    target = jp.TA("CUDA")(cfg["T_target"])
+    method = jp.RungeKutta2()
+    live = int(p.index.data.sum())
+
+    def timed(fn, reps):
+        ts = []
+        out = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        return float(np.median(ts)), out
+
+    fwd = lambda: A.forward_field(p, method, V, dt, nsteps, T0)  # noqa: E731
+    grad = lambda: A.misfit_gradient(p, method, V, dt, nsteps, T0, target, checkpoint_every=k)  # noqa: E731
+    for _ in range(max(1, min(args.warmup, 3))):
+        fwd()
+        grad()
+    reps = max(1, min(args.steps, 5))
+    t_fwd, _ = timed(fwd, reps)
+    t_grad, (loss, gV, gT0) = timed(grad, reps)
+    rng = np.random.default_rng(17)
+    worst, checked = 0.0, []
+    h = 1e-6
+    Vh = cfg["V"]
+    for n in range(args.fd_nodes):
+        c = n % 2
+        gc = gV[c].cpu().numpy()
+        node = np.unravel_index(rng.integers(gc.size), gc.shape, order="F")
+        Vp = [v.copy(order="F") for v in Vh]
+        Vm = [v.copy(order="F") for v in Vh]
+        Vp[c][node] += h
+        Vm[c][node] -= h
+        Fp, Wp = A.forward_field(p, method, tuple(jp.TA("CUDA")(v) for v in Vp), dt, nsteps, T0)
+        Fm, Wm = A.forward_field(p, method, tuple(jp.TA("CUDA")(v) for v in Vm), dt, nsteps, T0)
+        fd = A.misfit_difference(Fp, Wp, Fm, Wm, target) / (2 * h)
+        checked.append((float(gc[node]), fd))
+    if checked:
+        adj = np.array([a for a, _ in checked])
+        fd = np.array([f for _, f in checked])
+        scale = np.max(np.abs(fd))
+        worst = float(np.max(np.abs(adj - fd) / np.maximum(np.abs(fd), 1e-6 * scale)))
+    print(json.dumps({
+        "workload": DESC["C5"] if args.ni is None else DESC["C5"] + f" (resized to {args.ni})",
+        "live_particles": live, "steps": nsteps, "checkpoint_every": k, "loss": loss,
+        "forward_s": t_fwd, "forward_plus_gradient_s": t_grad, "gradient_cost_vs_forward": t_grad / t_fwd,
+        "forward_particle_steps_per_s": live * nsteps / t_fwd,
+        "fd_check": {"nodes": len(checked), "h": h, "max_rel_err": worst,
+                     "floor": "1e-6 of the largest |fd| among the checked nodes"},
+    }))
 
 
 def _cpu_setup(workload):
@@ -605,12 +692,16 @@ def main():
                     help="run the same seeded workload in both forms for --steps steps and print the errors")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fd-nodes", type=int, default=0,
+                    help="C5: number of random velocity nodes checked by central finite differences")
     ap.add_argument("--ni", type=int, default=None,
                     help="cells per axis instead of the workload's (small cases for ncu captures; not a bench line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
-    if args.impl == "reference":
+    if args.workload == "C5" and args.impl == "ours":
+        run_adjoint(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.compare_forms:
         run_compare(args)

@@ -38,6 +38,7 @@ extern "C" {
 #define JP_ERR_OUT_OF_MEMORY (-3)
 #define JP_ERR_BISECTION_LIMIT (-4)  /* a cell search hit its iteration cap */
 #define JP_ERR_NOT_BUILT (-5)
+#define JP_ERR_ADJOINT_WINDOW (-6)   /* an adjoint gather met a particle outside its fixed window */
 
 #define JP_MAX_ARGS 16
 
@@ -161,6 +162,54 @@ int jp_grid2particle(jp_particles* p, double* Fp, const double* F, const double*
    squared distance average of Fp onto the vertex field F. */
 int jp_particle2grid(jp_particles* p, double* F, const double* Fp, const double* const coords[3],
                      const uint8_t* index);
+
+/*
+ * Adjoint (vector-Jacobian products) of the FP64 path, 2D only. No
+ * counterpart in the reference: it is what a ChainRulesCore rrule of the
+ * Julia API calls. Gradient arrays share the layout of the values they
+ * belong to. Transposes are gathers with a fixed summation order: results are
+ * reproducible run to run. Particle relocation is replayed as integer data
+ * from the forward sweep and is not differentiated.
+ *
+ * jp_particle2grid_with_weights: particle2grid!, also writing the weight sum
+ *   W of every vertex (needed by jp_particle2grid_vjp).
+ * jp_move_permutation: right after jp_move_particles, dest[a] = slot that
+ *   now holds the particle that sat in slot a before the move, or -1
+ *   (empty slot, dropped particle). int32; needs < 2^31 slots.
+ * jp_permute_vjp: pre[k][a] = post[k][dest[a]] (0 where dest is -1), k < n <= 8.
+ * jp_slot_ids: ids[a] = a (as a double) for live slots, -1 elsewhere. Pass ids
+ *   as an extra particle field to jp_inject_particles: afterwards an injected
+ *   slot holds the id of the particle its fields were copied from.
+ * jp_inject_vjp: with those ids, pre[k][a] = post[k][a] for slots that existed
+ *   before the injection and 0 for injected ones; with copies != 0 each
+ *   existing slot also receives post[k] of the slots injected from it (use
+ *   copies = 0 for positions, 1 for particle fields).
+ * jp_advection_vjp: one advection! step (same method, alpha, V, dt) taken
+ *   from coords (the positions BEFORE the step): lam holds dL/dX after the step
+ *   on entry and dL/dX before it on return; dL/dV is ADDED to gV. Fails with
+ *   JP_ERR_ADJOINT_WINDOW if a stage point lies more than one cell from its
+ *   particle's cell (dt above the CFL limit).
+ * jp_particle2grid_vjp: from gF = dL/dF, ADDS dL/dFp to gFp and, when gX is
+ *   not NULL, dL/dX to gX. F and W are the forward's outputs.
+ * jp_grid2particle_vjp: from gFp = dL/dFp, ADDS dL/dF to gF (when not NULL)
+ *   and dL/dX to gX (when not NULL; needs F).
+ */
+int jp_particle2grid_with_weights(jp_particles* p, double* F, double* W, const double* Fp,
+                                  const double* const coords[3], const uint8_t* index);
+int jp_move_permutation(jp_particles* p, int32_t* dest);
+int jp_permute_vjp(jp_particles* p, const int32_t* dest, const double* const* post, double* const* pre,
+                   int32_t n);
+int jp_slot_ids(jp_particles* p, const uint8_t* index, double* ids);
+int jp_inject_vjp(jp_particles* p, const double* ids, const double* const* post, double* const* pre, int32_t n,
+                  int32_t copies);
+int jp_advection_vjp(jp_particles* p, int32_t method, double alpha, const double* const V[3], double dt,
+                     const double* const coords[3], const uint8_t* index, double* const lam[3],
+                     double* const gV[3]);
+int jp_particle2grid_vjp(jp_particles* p, const double* F, const double* W, const double* Fp,
+                         const double* const coords[3], const uint8_t* index, const double* gF, double* gFp,
+                         double* const gX[3]);
+int jp_grid2particle_vjp(jp_particles* p, const double* F, const double* gFp, const double* const coords[3],
+                         const uint8_t* index, double* gF, double* const gX[3]);
 
 /*
  * Split-precision form (no reference counterpart; the scope of this library

@@ -17,6 +17,7 @@ JP_ERR_CUDA = -2
 JP_ERR_OUT_OF_MEMORY = -3
 JP_ERR_BISECTION_LIMIT = -4
 JP_ERR_NOT_BUILT = -5
+JP_ERR_ADJOINT_WINDOW = -6
 
 JP_WARN_FAR_MOVE = 0x2
 JP_WARN_NO_NEIGHBOUR = 0x4
@@ -88,6 +89,22 @@ SIGNATURES = [
      [ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     ("jp_grid2particle_f32", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
     ("jp_particle2grid_f32", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
+    # adjoint (2D, FP64)
+    ("jp_particle2grid_with_weights", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
+    ("jp_move_permutation", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    ("jp_permute_vjp", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_int32]),
+    ("jp_slot_ids", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("jp_inject_vjp", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_int32, ctypes.c_int32]),
+    ("jp_advection_vjp", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, P3, ctypes.c_double, P3, ctypes.c_void_p, P3, P3]),
+    ("jp_particle2grid_vjp", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_void_p]),
+    ("jp_grid2particle_vjp", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
 ]
 
 _lib = None

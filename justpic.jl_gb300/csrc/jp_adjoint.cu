@@ -1,0 +1,605 @@
+// jp_adjoint.cu -- hand-written adjoint (vector-Jacobian products) of the
+// FP64 hot path in 2D: one advection! step (Euler, RK2, RK4), particle2grid!,
+// grid2particle!, and the replay of move_particles!'s and
+// inject_particles!'s slot maps.
+//
+// None of this has a counterpart in the reference. Conventions:
+//   * lam holds dL/d(position) per slot; gV dL/d(velocity node) per
+//     component; gF dL/d(vertex field); gFp dL/d(particle field);
+//   * relocation is integer data recorded in the forward sweep (the move's
+//     destination map, the injection's source ids) and replayed by gathers;
+//     it is not differentiated: dropped particles pass no gradient back, and
+//     the positions of injected particles depend on nothing;
+//   * every transpose is a gather with a fixed summation order, so results do
+//     not depend on scheduling (no floating-point atomics).
+//
+// Transpose of the velocity sampling: a particle owned by cell I whose stage
+// points stay within one cell of I deposits only on velocity nodes in a fixed
+// window around I (4 x 5 nodes for Vx, 5 x 4 for Vy on the ghost-node grids).
+// One thread per owning cell accumulates its particles' deposits, in slot
+// order, into 40 partial sums; one thread per velocity node then adds the
+// partial sums of the 20 owning cells whose windows contain it. A stage point
+// outside the window is reported as JP_ERR_ADJOINT_WINDOW.
+#include <cmath>
+
+#include <math_constants.h>
+
+#include "jp_internal.cuh"
+#include "jp_move_core.cuh"
+
+namespace jp {
+
+constexpr int kAdjThreads = 128;
+constexpr int kWinParts = 40;    // 4*5 + 5*4 partial sums per owning cell
+constexpr int kInjectReach = 4;  // 2D: four colour passes, each copy reaches one cell further
+
+// node window of Vx (comp 0) / Vy (comp 1) around the owning cell
+__host__ __device__ constexpr int win_nx(int comp) { return comp == 0 ? 4 : 5; }
+__host__ __device__ constexpr int win_ny(int comp) { return comp == 0 ? 5 : 4; }
+
+// ------------------------------------------------------- move permutation
+// dest[a] = slot holding, after the last move, the particle that sat in slot a
+// before it; -1 for empty slots and dropped particles.
+__global__ void __launch_bounds__(kThreads)
+    perm_init(DevGrid g, const uint64_t* __restrict__ L0, const uint64_t* __restrict__ L,
+              const uint64_t* __restrict__ R, int32_t* __restrict__ dest)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const uint64_t stay = L0[c] & L[c] & ~R[c];
+    for (int s = 0; s < g.max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        dest[a] = ((stay >> s) & 1) ? (int32_t)a : -1;
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) perm_scatter(DevGrid g, MoveView S, int32_t* __restrict__ dest)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    uint64_t R = S.R[c];
+    if (!R) return;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    while (R) {
+        const int s = __ffsll((long long)R) - 1;
+        R &= R - 1;
+        const int64_t a = c + nc * s;
+        const uint16_t tag = S.orig[a];
+        int off[3];
+        nb_offset<DIM>(tag & 0x1F, off);
+        const int64_t J[3] = {I[0] + off[0], I[1] + off[1], DIM == 3 ? I[2] + off[2] : 0};
+        dest[cell_linear<DIM>(g, J) + nc * (tag >> 5)] = (int32_t)a;  // each origin has one destination
+    }
+}
+
+struct PermArrays {
+    const double* post[8];
+    double* pre[8];
+    int n;
+};
+
+__global__ void __launch_bounds__(kThreads)
+    permute_vjp_kernel(int64_t nslots, const int32_t* __restrict__ dest, PermArrays P)
+{
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nslots) return;
+    const int32_t d = dest[a];
+    const bool ok = d >= 0 && d < nslots;
+    for (int k = 0; k < P.n; ++k) P.pre[k][a] = ok ? P.post[k][d] : 0.0;
+}
+
+// ------------------------------------------------------------ injection
+__global__ void __launch_bounds__(kThreads)
+    slot_ids_kernel(int64_t nslots, const uint8_t* __restrict__ index, double* __restrict__ ids)
+{
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nslots) return;
+    ids[a] = index[a] ? (double)a : -1.0;
+}
+
+// Per cell: the slots whose id names another slot (particles injected by the
+// traced call), after checking that each source lies within reach.
+__global__ void __launch_bounds__(kThreads)
+    inject_mask_kernel(DevGrid g, const double* __restrict__ ids, uint64_t* __restrict__ inj, int* d_err)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int64_t ns = nc * g.max_xcell;
+    const int64_t cx = c % g.n[0], cy = c / g.n[0];
+    uint64_t m = 0;
+    int errs = 0;
+    for (int s = 0; s < g.max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        const double id = ids[a];
+        if (id >= 0.0 && id != (double)a) {
+            const int64_t src = id < (double)ns ? (int64_t)id : ns;
+            const int64_t sc = src % nc;
+            const int64_t sx = sc % g.n[0], sy = sc / g.n[0];
+            if (src >= ns || sx < cx - kInjectReach || sx > cx + kInjectReach || sy < cy - kInjectReach ||
+                sy > cy + kInjectReach)
+                errs |= kErrAdjointWindow;
+            else
+                m |= 1ull << s;
+        }
+    }
+    inj[c] = m;
+    raise_err(d_err, errs);
+}
+
+// pre[k][a] = post[k][a] for slots that existed before the injection (id ==
+// own slot), 0 otherwise; with `copies`, a pre-existing slot also collects
+// post[k][b] of every slot b injected from it, cells of the window in order
+// (y outer, x inner), slots ascending.
+__global__ void __launch_bounds__(kThreads)
+    inject_vjp_kernel(DevGrid g, const double* __restrict__ ids, const uint64_t* __restrict__ inj, PermArrays P,
+                      int copies)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    for (int s = 0; s < g.max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        const bool kept = ids[a] == (double)a;
+        for (int k = 0; k < P.n; ++k) P.pre[k][a] = kept ? P.post[k][a] : 0.0;
+    }
+    if (!copies) return;
+    const int64_t cx = c % g.n[0], cy = c / g.n[0];
+    for (int64_t y = max(cy - kInjectReach, (int64_t)0); y <= min(cy + kInjectReach, g.n[1] - 1); ++y)
+        for (int64_t x = max(cx - kInjectReach, (int64_t)0); x <= min(cx + kInjectReach, g.n[0] - 1); ++x) {
+            const int64_t w = x + g.n[0] * y;
+            uint64_t m = inj[w];
+            while (m) {
+                const int s = __ffsll((long long)m) - 1;
+                m &= m - 1;
+                const int64_t b = w + nc * s;
+                const int64_t src = (int64_t)ids[b];  // in range: inject_mask_kernel checked it
+                if (src % nc != c) continue;
+                for (int k = 0; k < P.n; ++k) P.pre[k][src] += P.post[k][b];
+            }
+        }
+}
+
+// --------------------------------------------------------- advection step
+// Value, gradient, grid cell and local coordinates of one velocity component
+// at p, with the forward's cell selection (seed = the particle's cell; the
+// limits test only when the seed interval does not hold p).
+struct Samp {
+    double v;
+    double dv[2];
+    int idx[2];
+    double t[2];
+    bool ok;
+};
+
+__device__ __forceinline__ Samp sample2(const DevGrid& g, int comp, const double* p, const int* I,
+                                        const double* __restrict__ V, int* errs)
+{
+    Samp r;
+    r.ok = true;
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+        const double* x = g.xvel[comp][d];
+        const int J = I[d];
+        const double a = ldg(x + J), b = ldg(x + J + 1);
+        int64_t k;
+        if (a <= p[d] && p[d] <= b) {
+            k = J;
+        } else {
+            if (!(g.lim_lo[comp][0] <= p[0] && p[0] <= g.lim_hi[comp][0] && g.lim_lo[comp][1] <= p[1] &&
+                  p[1] <= g.lim_hi[comp][1])) {
+                r.ok = false;
+                return r;
+            }
+            k = find_cell(p[d], x, g.nvel[comp][d], J, errs);
+        }
+        r.idx[d] = (int)k;
+        r.t[d] = (p[d] - ldg(x + k)) * ldg(g.ixvel[comp][d] + k);
+    }
+    const int64_t L0 = g.nvel[comp][0];
+    const double* b = V + r.idx[0] + L0 * r.idx[1];
+    const double v00 = ldg(b), v10 = ldg(b + 1), v01 = ldg(b + L0), v11 = ldg(b + L0 + 1);
+    const double tx = r.t[0], ty = r.t[1];
+    r.v = lerp1(ty, lerp1(tx, v00, v10), lerp1(tx, v01, v11));
+    r.dv[0] = ((1.0 - ty) * (v10 - v00) + ty * (v11 - v01)) * ldg(g.ixvel[comp][0] + r.idx[0]);
+    r.dv[1] = ((1.0 - tx) * (v01 - v00) + tx * (v11 - v10)) * ldg(g.ixvel[comp][1] + r.idx[1]);
+    return r;
+}
+
+struct AdjParams {
+    double dt, adt;
+    double ca, cb;  // RK2: X' = X + dt (ca V(X) + cb V(X + alpha dt V(X)))
+    int method;
+};
+
+// deposit w * (bilinear weights) of one stage sample on the owning cell's window
+__device__ __forceinline__ bool deposit(double (*part)[kAdjThreads], int comp, const Samp& s, const int* I,
+                                        double w)
+{
+    const int NX = win_nx(comp), NY = win_ny(comp);
+    const int ox = s.idx[0] - I[0] + 1, oy = s.idx[1] - I[1] + 1;
+    if (ox < 0 || ox > NX - 2 || oy < 0 || oy > NY - 2) return false;
+    const int base = (comp == 0 ? 0 : 20) + ox + NX * oy;
+    const double tx = s.t[0], ty = s.t[1];
+    const int t = threadIdx.x;
+    part[base][t] = fma(w, (1.0 - tx) * (1.0 - ty), part[base][t]);
+    part[base + 1][t] = fma(w, tx * (1.0 - ty), part[base + 1][t]);
+    part[base + NX][t] = fma(w, (1.0 - tx) * ty, part[base + NX][t]);
+    part[base + NX + 1][t] = fma(w, tx * ty, part[base + NX + 1][t]);
+    return true;
+}
+
+// J^T g for the two components sampled at one point
+__device__ __forceinline__ void jt(const Samp* s, const double* g, double* out)
+{
+    out[0] = s[0].dv[0] * g[0] + s[1].dv[0] * g[1];
+    out[1] = s[0].dv[1] * g[0] + s[1].dv[1] * g[1];
+}
+
+// One thread per owning cell: replays the step's stages for each live slot (in
+// slot order), maps lam (dL/dX after the step) to dL/dX before it, and
+// accumulates the velocity deposits into the cell's 40 partial sums.
+template <int METHOD>
+__global__ void __launch_bounds__(kAdjThreads)
+    advect_vjp_kernel(DevGrid g, const double* __restrict__ V0, const double* __restrict__ V1, AdjParams P,
+                      CCoords X, const uint8_t* __restrict__ index, Coords Lam, double* __restrict__ parts,
+                      int* d_err)
+{
+    constexpr int NS = METHOD == JP_RUNGE_KUTTA4 ? 4 : (METHOD == JP_RUNGE_KUTTA2 ? 2 : 1);
+    __shared__ double part[kWinParts][kAdjThreads];
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    for (int k = 0; k < kWinParts; ++k) part[k][threadIdx.x] = 0.0;
+    const int I[2] = {(int)(c % g.n[0]), (int)(c / g.n[0])};
+    const double* Vc[2] = {V0, V1};
+    int errs = 0;
+    uint64_t m = live_mask(index, c, nc, g.max_xcell);
+    while (m) {
+        const int s = __ffsll((long long)m) - 1;
+        m &= m - 1;
+        const int64_t a = c + nc * s;
+        const double p0[2] = {X.c[0][a], X.c[1][a]};
+        const double lam[2] = {Lam.c[0][a], Lam.c[1][a]};
+        // forward stages with the forward's arithmetic, keeping every sample
+        Samp S[NS][2];
+        bool ok = true;
+#pragma unroll
+        for (int st = 0; st < NS; ++st) {
+            double q[2];
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                if (st == 0)
+                    q[d] = p0[d];
+                else if (METHOD == JP_RUNGE_KUTTA2)
+                    q[d] = fma(1.0, P.adt * S[0][d].v, p0[d]);
+                else if (st < 3)
+                    q[d] = p0[d] + (P.dt * S[st - 1][d].v) * 0.5;
+                else
+                    q[d] = p0[d] + P.dt * S[2][d].v;
+            }
+#pragma unroll
+            for (int cc = 0; cc < 2; ++cc) {
+                S[st][cc] = sample2(g, cc, q, I, Vc[cc], &errs);
+                ok &= S[st][cc].ok;
+            }
+            if (!ok) break;
+        }
+        if (!ok) {  // the forward sent this particle to Inf; move_particles! dropped it
+            Lam.c[0][a] = 0.0;
+            Lam.c[1][a] = 0.0;
+            continue;
+        }
+        // reverse sweep over the stages: gk[st] = dL/d(velocity sample of stage st)
+        double gk[NS][2], l0[2] = {lam[0], lam[1]}, qb[2];
+        if (METHOD == JP_RUNGE_KUTTA2) {
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                gk[NS - 1][d] = P.dt * P.cb * lam[d];
+                gk[0][d] = P.dt * P.ca * lam[d];
+            }
+            jt(S[NS - 1], gk[NS - 1], qb);  // q2 = p0 + alpha dt k1
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                l0[d] += qb[d];
+                gk[0][d] += P.adt * qb[d];
+            }
+        } else if (METHOD == JP_RUNGE_KUTTA4) {
+            const double w6 = P.dt / 6.0;
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                gk[0][d] = w6 * lam[d];
+                gk[1][d] = 2.0 * w6 * lam[d];
+                gk[2][d] = 2.0 * w6 * lam[d];
+                gk[NS - 1][d] = w6 * lam[d];
+            }
+#pragma unroll
+            for (int st = NS - 1; st >= 1; --st) {  // q4 = p0 + dt k3, q3 = p0 + dt/2 k2, q2 = p0 + dt/2 k1
+                jt(S[st], gk[st], qb);
+                const double h = st == 3 ? P.dt : 0.5 * P.dt;
+#pragma unroll
+                for (int d = 0; d < 2; ++d) {
+                    l0[d] += qb[d];
+                    gk[st - 1][d] += h * qb[d];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int d = 0; d < 2; ++d) gk[0][d] = P.dt * lam[d];
+        }
+        jt(S[0], gk[0], qb);  // the first stage samples at p0 itself
+#pragma unroll
+        for (int d = 0; d < 2; ++d) l0[d] += qb[d];
+        Lam.c[0][a] = l0[0];
+        Lam.c[1][a] = l0[1];
+#pragma unroll
+        for (int st = 0; st < NS; ++st)
+#pragma unroll
+            for (int cc = 0; cc < 2; ++cc)
+                if (!deposit(part, cc, S[st][cc], I, gk[st][cc])) errs |= kErrAdjointWindow;
+    }
+    for (int k = 0; k < kWinParts; ++k) parts[k * nc + c] = part[k][threadIdx.x];
+    raise_err(d_err, errs);
+}
+
+// dL/dV at every node of component `comp`: the partial sums of the owning
+// cells whose window holds the node (cells y outer, x inner).
+__global__ void __launch_bounds__(kThreads)
+    vel_gather_kernel(DevGrid g, int comp, const double* __restrict__ parts, double* __restrict__ gV)
+{
+    const int64_t L0 = g.nvel[comp][0], L1 = g.nvel[comp][1];
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L0 * L1) return;
+    const int64_t i = t % L0, j = t / L0;
+    const int NX = win_nx(comp), NY = win_ny(comp);
+    const int64_t nc = g.ncells;
+    double acc = 0.0;
+    // owning cell (cx, cy) holds node (i, j) at window position (i - cx + 1, j - cy + 1)
+    for (int64_t cy = max(j + 2 - NY, (int64_t)0); cy <= min(j + 1, g.n[1] - 1); ++cy)
+        for (int64_t cx = max(i + 2 - NX, (int64_t)0); cx <= min(i + 1, g.n[0] - 1); ++cx) {
+            const int k = (comp == 0 ? 0 : 20) + (int)(i - cx + 1) + NX * (int)(j - cy + 1);
+            acc += parts[k * nc + cx + g.n[0] * cy];
+        }
+    gV[t] += acc;
+}
+
+// --------------------------------------------------------- particle2grid!
+// per particle: F_v = sum_i w_vi Fp_i / W_v with w = 1 / |x_v - x_i|^2, so
+//   dL/dFp_i += sum_v gF_v w_vi / W_v
+//   dL/dx_i  += sum_v gF_v (Fp_i - F_v) / W_v * 2 (x_v - x_i) w_vi^2
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    p2g_vjp_kernel(DevGrid g, const double* __restrict__ F, const double* __restrict__ W,
+                   const double* __restrict__ Fp, CCoords X, const uint8_t* __restrict__ index,
+                   const double* __restrict__ gF, double* __restrict__ gFp, Coords gX)
+{
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ int cellI[kWarpsPerBlock][32][2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+        cellI[w][lane][0] = (int)I[0];
+        cellI[w][lane][1] = (int)I[1];
+    }
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
+    const int64_t V0 = g.n[0] + 1;
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        const int I[2] = {cellI[w][l][0], cellI[w][l][1]};
+        const double px = X.c[0][a], py = X.c[1][a], f = Fp[a];
+        double gf = 0.0, gx = 0.0, gy = 0.0;
+        for (int kb = 0; kb < 2; ++kb)
+            for (int ka = 0; ka < 2; ++ka) {
+                const int64_t v = (I[0] + ka) + V0 * (I[1] + kb);
+                const double ex = ldg(g.xv[0] + I[0] + ka) - px, ey = ldg(g.xv[1] + I[1] + kb) - py;
+                const double dist = __dsqrt_rn(ex * ex + ey * ey);
+                const double wi = __drcp_rn(dist * dist);
+                const double r = ldg(gF + v) / ldg(W + v);
+                gf = fma(r, wi, gf);
+                const double q = r * (f - ldg(F + v)) * 2.0 * wi * wi;
+                gx = fma(q, ex, gx);
+                gy = fma(q, ey, gy);
+            }
+        gFp[a] += gf;
+        if (gX.c[0]) {
+            gX.c[0][a] += gx;
+            gX.c[1][a] += gy;
+        }
+    }
+}
+
+// --------------------------------------------------------- grid2particle!
+// dL/dF_v += sum over the particles of the (up to) four cells around v of
+// gFp_i * (bilinear weight of v at x_i), cells y outer, x inner, slots ascending.
+__global__ void __launch_bounds__(kThreads)
+    g2p_vjp_kernel(DevGrid g, const double* __restrict__ gFp, CCoords X, const uint8_t* __restrict__ index,
+                   double* __restrict__ gF)
+{
+    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= V0 * V1) return;
+    const int64_t i = t % V0, j = t / V0;
+    const int64_t nc = g.ncells;
+    double acc = 0.0;
+    for (int64_t cy = j - 1; cy <= j; ++cy) {
+        if (cy < 0 || cy >= g.n[1]) continue;
+        for (int64_t cx = i - 1; cx <= i; ++cx) {
+            if (cx < 0 || cx >= g.n[0]) continue;
+            const int64_t c = cx + g.n[0] * cy;
+            const double x0 = ldg(g.xv[0] + cx), y0 = ldg(g.xv[1] + cy);
+            const double ixx = ldg(g.ixv[0] + cx), iyy = ldg(g.ixv[1] + cy);
+            uint64_t m = live_mask(index, c, nc, g.max_xcell);
+            while (m) {
+                const int s = __ffsll((long long)m) - 1;
+                m &= m - 1;
+                const int64_t a = c + nc * s;
+                const double tx = (X.c[0][a] - x0) * ixx, ty = (X.c[1][a] - y0) * iyy;
+                const double fx = cx == i ? 1.0 - tx : tx;
+                const double fy = cy == j ? 1.0 - ty : ty;
+                acc = fma(gFp[a], fx * fy, acc);
+            }
+        }
+    }
+    gF[t] += acc;
+}
+
+// dL/dx_i += gFp_i * grad(bilinear F)(x_i)
+__global__ void __launch_bounds__(kThreads)
+    g2p_vjp_pos_kernel(DevGrid g, const double* __restrict__ F, const double* __restrict__ gFp, CCoords X,
+                       const uint8_t* __restrict__ index, Coords gX)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int64_t cx = c % g.n[0], cy = c / g.n[0];
+    const int64_t V0 = g.n[0] + 1;
+    const double* b = F + cx + V0 * cy;
+    const double f00 = ldg(b), f10 = ldg(b + 1), f01 = ldg(b + V0), f11 = ldg(b + V0 + 1);
+    const double x0 = ldg(g.xv[0] + cx), y0 = ldg(g.xv[1] + cy);
+    const double ixx = ldg(g.ixv[0] + cx), iyy = ldg(g.ixv[1] + cy);
+    uint64_t m = live_mask(index, c, nc, g.max_xcell);
+    while (m) {
+        const int s = __ffsll((long long)m) - 1;
+        m &= m - 1;
+        const int64_t a = c + nc * s;
+        const double tx = (X.c[0][a] - x0) * ixx, ty = (X.c[1][a] - y0) * iyy;
+        const double gp = gFp[a];
+        gX.c[0][a] += gp * ((1.0 - ty) * (f10 - f00) + ty * (f11 - f01)) * ixx;
+        gX.c[1][a] += gp * ((1.0 - tx) * (f01 - f00) + tx * (f11 - f10)) * iyy;
+    }
+}
+
+// ------------------------------------------------------------ launchers
+static cudaError_t ensure_adjoint_scratch(jp_particles* P)
+{
+    if (P->adj_rec) return cudaSuccess;
+    const size_t bytes = (size_t)P->g.ncells * (kWinParts * sizeof(double) + sizeof(uint64_t));
+    return cudaMalloc(&P->adj_rec, bytes);
+}
+
+static double* adj_parts(jp_particles* P) { return (double*)P->adj_rec; }
+static uint64_t* adj_inj(jp_particles* P) { return (uint64_t*)((double*)P->adj_rec + kWinParts * P->g.ncells); }
+
+cudaError_t launch_move_permutation(jp_particles* P, int32_t* dest)
+{
+    const MoveScratch& m = P->move;
+    if (!m.L0) return cudaErrorInvalidValue;
+    const unsigned nb = grid_blocks(P->g.ncells);
+    MoveView S{m.L0, m.L, m.M, m.R, m.U, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, 0};
+    perm_init<<<nb, kThreads, 0, P->stream>>>(P->g, m.L0, m.L, m.R, dest);
+    if (P->g.ndim == 2)
+        perm_scatter<2><<<nb, kThreads, 0, P->stream>>>(P->g, S, dest);
+    else
+        perm_scatter<3><<<nb, kThreads, 0, P->stream>>>(P->g, S, dest);
+    return cudaGetLastError();
+}
+
+static PermArrays perm_arrays(const double* const* post, double* const* pre, int n)
+{
+    PermArrays A{};
+    A.n = n;
+    for (int k = 0; k < n; ++k) {
+        A.post[k] = post[k];
+        A.pre[k] = pre[k];
+    }
+    return A;
+}
+
+cudaError_t launch_permute_vjp(jp_particles* P, const int32_t* dest, const double* const* post, double* const* pre,
+                               int n)
+{
+    const int64_t ns = P->g.ncells * P->g.max_xcell;
+    permute_vjp_kernel<<<grid_blocks(ns), kThreads, 0, P->stream>>>(ns, dest, perm_arrays(post, pre, n));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_slot_ids(jp_particles* P, const uint8_t* index, double* ids)
+{
+    const int64_t ns = P->g.ncells * P->g.max_xcell;
+    slot_ids_kernel<<<grid_blocks(ns), kThreads, 0, P->stream>>>(ns, index, ids);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_inject_vjp(jp_particles* P, const double* ids, const double* const* post, double* const* pre,
+                              int n, int copies)
+{
+    cudaError_t e = ensure_adjoint_scratch(P);
+    if (e != cudaSuccess) return e;
+    const unsigned nb = grid_blocks(P->g.ncells);
+    if (copies) inject_mask_kernel<<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), P->d_err);
+    inject_vjp_kernel<<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), perm_arrays(post, pre, n), copies);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advection_vjp(jp_particles* P, int method, double alpha, const double* const V[3], double dt,
+                                 const double* const coords[3], const uint8_t* index, double* const lam[3],
+                                 double* const gV[3])
+{
+    cudaError_t e = ensure_adjoint_scratch(P);
+    if (e != cudaSuccess) return e;
+    AdjParams prm;
+    prm.method = method;
+    prm.dt = dt;
+    prm.adt = alpha * dt;
+    // the forward's coefficients (alpha == 1/2 takes the dt * V(X1) form)
+    const double ia = 1.0 / alpha;
+    prm.ca = alpha == 0.5 ? 0.0 : std::fma(-0.5, ia, 1.0);
+    prm.cb = alpha == 0.5 ? 1.0 : 0.5 * ia;
+    CCoords X{{coords[0], coords[1], nullptr}};
+    Coords L{{lam[0], lam[1], nullptr}};
+    const unsigned nb = grid_blocks(P->g.ncells, kAdjThreads);
+    cudaStream_t st = P->stream;
+    if (method == JP_RUNGE_KUTTA2)
+        advect_vjp_kernel<JP_RUNGE_KUTTA2><<<nb, kAdjThreads, 0, st>>>(P->g, V[0], V[1], prm, X, index, L,
+                                                                       adj_parts(P), P->d_err);
+    else if (method == JP_RUNGE_KUTTA4)
+        advect_vjp_kernel<JP_RUNGE_KUTTA4><<<nb, kAdjThreads, 0, st>>>(P->g, V[0], V[1], prm, X, index, L,
+                                                                       adj_parts(P), P->d_err);
+    else
+        advect_vjp_kernel<JP_EULER><<<nb, kAdjThreads, 0, st>>>(P->g, V[0], V[1], prm, X, index, L, adj_parts(P),
+                                                                P->d_err);
+    for (int c = 0; c < 2; ++c) {
+        const int64_t nn = P->g.nvel[c][0] * P->g.nvel[c][1];
+        vel_gather_kernel<<<grid_blocks(nn), kThreads, 0, st>>>(P->g, c, adj_parts(P), gV[c]);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_p2g_vjp(jp_particles* P, const double* F, const double* W, const double* Fp,
+                           const double* const coords[3], const uint8_t* index, const double* gF, double* gFp,
+                           double* const gX[3])
+{
+    CCoords X{{coords[0], coords[1], nullptr}};
+    Coords G{{gX ? gX[0] : nullptr, gX ? gX[1] : nullptr, nullptr}};
+    p2g_vjp_kernel<<<grid_blocks(P->g.ncells, 32 * kWarpsPerBlock), 32 * kWarpsPerBlock, 0, P->stream>>>(
+        P->g, F, W, Fp, X, index, gF, gFp, G);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_g2p_vjp(jp_particles* P, const double* F, const double* gFp, const double* const coords[3],
+                           const uint8_t* index, double* gF, double* const gX[3])
+{
+    CCoords X{{coords[0], coords[1], nullptr}};
+    if (gF) {
+        const int64_t nv = (P->g.n[0] + 1) * (P->g.n[1] + 1);
+        g2p_vjp_kernel<<<grid_blocks(nv), kThreads, 0, P->stream>>>(P->g, gFp, X, index, gF);
+    }
+    if (gX) {
+        Coords G{{gX[0], gX[1], nullptr}};
+        g2p_vjp_pos_kernel<<<grid_blocks(P->g.ncells), kThreads, 0, P->stream>>>(P->g, F, gFp, X, index, G);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace jp

@@ -186,6 +186,7 @@ int jp_particles_destroy(jp_particles* P)
     if (P->h_err) cudaFreeHost(P->h_err);
     cudaFree(P->move.L0);  // one allocation holds all move scratch
     cudaFree(P->inject.counts);  // counters and lists share one allocation
+    cudaFree(P->adj_rec);
     delete P;
     return JP_OK;
 }
@@ -232,6 +233,10 @@ int jp_synchronize(jp_particles* P)
     P->warnings |= (uint32_t)(bits & (jp::kWarnFarMove | jp::kWarnNoNeighbour));
     if (bits & jp::kErrBisection)
         return fail(JP_ERR_BISECTION_LIMIT, "cell search exceeded its iteration cap (NaN or out-of-grid position)");
+    if (bits & jp::kErrAdjointWindow)
+        return fail(JP_ERR_ADJOINT_WINDOW,
+                    "adjoint: a stage point or an injection source lies outside the window the gather covers "
+                    "(a step moved a particle more than one cell)");
     return JP_OK;
 }
 
@@ -401,6 +406,100 @@ int jp_particle2grid_f32(jp_particles* P, float* F, const float* Fp, const float
     if (rc) return rc;
     if (!Fp || !F) return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_f32: null field");
     return finish(P, jp::launch_p2g_f32(P, F, Fp, xi, index), "jp_particle2grid_f32");
+}
+
+// ---- adjoint (2D, FP64) -----------------------------------------------
+static int check_adj(const jp_particles* P, const void* const* coords, const void* index, const char* what)
+{
+    if (!P || !index || !check_coords(P, coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": null pointer");
+    if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": the adjoint is built for 2D");
+    return JP_OK;
+}
+
+static bool slots_fit_int32(const jp_particles* P)
+{
+    return (double)P->g.ncells * P->g.max_xcell < 2147483647.0;
+}
+
+int jp_move_permutation(jp_particles* P, int32_t* dest)
+{
+    if (!P || !dest) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: null pointer");
+    if (!P->move.L0) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: no move_particles call to replay");
+    if (!slots_fit_int32(P)) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: more than 2^31 slots");
+    return finish(P, jp::launch_move_permutation(P, dest), "jp_move_permutation");
+}
+
+int jp_permute_vjp(jp_particles* P, const int32_t* dest, const double* const* post, double* const* pre, int32_t n)
+{
+    if (!P || !dest || !post || !pre || n < 0 || n > 8)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_permute_vjp: bad arguments");
+    for (int k = 0; k < n; ++k)
+        if (!post[k] || !pre[k] || post[k] == pre[k])
+            return fail(JP_ERR_INVALID_ARGUMENT, "jp_permute_vjp: null or aliased array");
+    return finish(P, jp::launch_permute_vjp(P, dest, post, pre, n), "jp_permute_vjp");
+}
+
+int jp_slot_ids(jp_particles* P, const uint8_t* index, double* ids)
+{
+    if (!P || !index || !ids) return fail(JP_ERR_INVALID_ARGUMENT, "jp_slot_ids: null pointer");
+    return finish(P, jp::launch_slot_ids(P, index, ids), "jp_slot_ids");
+}
+
+int jp_inject_vjp(jp_particles* P, const double* ids, const double* const* post, double* const* pre, int32_t n,
+                  int32_t copies)
+{
+    if (!P || !ids || !post || !pre || n < 0 || n > 8)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp: bad arguments");
+    if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp: the adjoint is built for 2D");
+    for (int k = 0; k < n; ++k)
+        if (!post[k] || !pre[k] || post[k] == pre[k])
+            return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp: null or aliased array");
+    return finish(P, jp::launch_inject_vjp(P, ids, post, pre, n, copies ? 1 : 0), "jp_inject_vjp");
+}
+
+int jp_advection_vjp(jp_particles* P, int32_t method, double alpha, const double* const V[3], double dt,
+                     const double* const coords[3], const uint8_t* index, double* const lam[3], double* const gV[3])
+{
+    int rc = check_adj(P, (const void* const*)coords, index, "jp_advection_vjp");
+    if (rc) return rc;
+    if (!check_coords(P, (const void* const*)V) || !check_coords(P, (const void* const*)lam) ||
+        !check_coords(P, (const void* const*)gV))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_vjp: null pointer");
+    if (method != JP_EULER && method != JP_RUNGE_KUTTA2 && method != JP_RUNGE_KUTTA4)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_vjp: unknown integrator");
+    if (method == JP_RUNGE_KUTTA2 && !(0.0 < alpha && alpha < 1.0))
+        return fail(JP_ERR_INVALID_ARGUMENT, "Only 0 < α < 1 is supported");
+    return finish(P, jp::launch_advection_vjp(P, method, alpha, V, dt, coords, index, lam, gV), "jp_advection_vjp");
+}
+
+int jp_particle2grid_with_weights(jp_particles* P, double* F, double* W, const double* Fp,
+                                  const double* const coords[3], const uint8_t* index)
+{
+    if (!P || !Fp || !F || !W || !index || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_with_weights: null pointer");
+    return finish(P, jp::launch_p2g(P, F, Fp, coords, index, W), "jp_particle2grid_with_weights");
+}
+
+int jp_particle2grid_vjp(jp_particles* P, const double* F, const double* W, const double* Fp,
+                         const double* const coords[3], const uint8_t* index, const double* gF, double* gFp,
+                         double* const gX[3])
+{
+    int rc = check_adj(P, (const void* const*)coords, index, "jp_particle2grid_vjp");
+    if (rc) return rc;
+    if (!F || !W || !Fp || !gF || !gFp || (gX && !check_coords(P, (const void* const*)gX)))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_vjp: null pointer");
+    return finish(P, jp::launch_p2g_vjp(P, F, W, Fp, coords, index, gF, gFp, gX), "jp_particle2grid_vjp");
+}
+
+int jp_grid2particle_vjp(jp_particles* P, const double* F, const double* gFp, const double* const coords[3],
+                         const uint8_t* index, double* gF, double* const gX[3])
+{
+    int rc = check_adj(P, (const void* const*)coords, index, "jp_grid2particle_vjp");
+    if (rc) return rc;
+    if (!gFp || (gX && (!F || !check_coords(P, (const void* const*)gX))))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_grid2particle_vjp: null pointer");
+    return finish(P, jp::launch_g2p_vjp(P, F, gFp, coords, index, gF, gX), "jp_grid2particle_vjp");
 }
 
 int jp_grid2particle(jp_particles* P, double* Fp, const double* F, const double* const coords[3],

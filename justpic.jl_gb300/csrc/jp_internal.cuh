@@ -15,6 +15,7 @@ namespace jp {
 constexpr int kErrBisection = 0x1;
 constexpr int kWarnFarMove = 0x2;
 constexpr int kWarnNoNeighbour = 0x4;
+constexpr int kErrAdjointWindow = 0x8;  // adjoint gather window exceeded
 
 constexpr int kBisectCap = 256;
 constexpr int kThreads = 256;
@@ -82,6 +83,7 @@ struct jp_particles {
     int staggered_std = 0;                // velocity grids have the standard ghost-node staggering
     jp::MoveScratch move;
     jp::InjectScratch inject;
+    void* adj_rec = nullptr;  // adjoint records of the last advection VJP
 };
 
 namespace jp {
@@ -316,7 +318,23 @@ cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* ind
 cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const double* const coords[3],
                        const uint8_t* index);
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
-                       const uint8_t* index);
+                       const uint8_t* index, double* W = nullptr);
+
+// adjoint (jp_adjoint.cu), 2D
+cudaError_t launch_move_permutation(jp_particles* P, int32_t* dest);
+cudaError_t launch_permute_vjp(jp_particles* P, const int32_t* dest, const double* const* post, double* const* pre,
+                               int n);
+cudaError_t launch_slot_ids(jp_particles* P, const uint8_t* index, double* ids);
+cudaError_t launch_inject_vjp(jp_particles* P, const double* ids, const double* const* post, double* const* pre,
+                              int n, int copies);
+cudaError_t launch_advection_vjp(jp_particles* P, int method, double alpha, const double* const V[3], double dt,
+                                 const double* const coords[3], const uint8_t* index, double* const lam[3],
+                                 double* const gV[3]);
+cudaError_t launch_p2g_vjp(jp_particles* P, const double* F, const double* W, const double* Fp,
+                           const double* const coords[3], const uint8_t* index, const double* gF, double* gFp,
+                           double* const gX[3]);
+cudaError_t launch_g2p_vjp(jp_particles* P, const double* F, const double* gFp, const double* const coords[3],
+                           const uint8_t* index, double* gF, double* const gX[3]);
 
 // scratch of move_particles! owned by the container (allocated on first use)
 cudaError_t ensure_move_scratch(jp_particles* P, int comps);

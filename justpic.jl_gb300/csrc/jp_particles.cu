@@ -335,7 +335,7 @@ __device__ __forceinline__ void p2g_cell(int64_t c, uint64_t mask, int64_t nc, c
 template <int DIM>
 __global__ void __launch_bounds__(kThreads)
     p2g_kernel(DevGrid g, double* __restrict__ F, const double* __restrict__ Fp, CCoords X,
-               const uint8_t* __restrict__ index, int chunk, int64_t nthreads)
+               const uint8_t* __restrict__ index, int chunk, int64_t nthreads, double* __restrict__ Wout)
 {
     const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -400,6 +400,7 @@ __global__ void __launch_bounds__(kThreads)
         if (vok) {
             const int64_t v = DIM == 2 ? i + V0 * r : i + V0 * (j + V1 * r);
             F[v] = DIM == 2 ? wF_c / w_c : wF_c * __drcp_rn(w_c);
+            if (Wout) Wout[v] = w_c;  // weight sums, kept for the adjoint
         }
         w_c = w_n;
         wF_c = wF_n;
@@ -463,7 +464,7 @@ cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const doubl
 }
 
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
-                       const uint8_t* index)
+                       const uint8_t* index, double* W)
 {
     const bool d3 = P->g.ndim == 3;
     CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
@@ -478,9 +479,9 @@ cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const doubl
     const int64_t nthreads = cols * ((rows + chunk - 1) / chunk);
     const unsigned nb = grid_blocks(nthreads);
     if (!d3)
-        p2g_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk, nthreads);
+        p2g_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk, nthreads, W);
     else
-        p2g_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk, nthreads);
+        p2g_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk, nthreads, W);
     return cudaGetLastError();
 }
 

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libjustpic_gb300.so")
 
-SOURCES = ["jp_capi.cu", "jp_particles.cu", "jp_move.cu", "jp_f32.cu"]
+SOURCES = ["jp_capi.cu", "jp_particles.cu", "jp_move.cu", "jp_f32.cu", "jp_adjoint.cu"]
 HEADERS = ["jp_internal.cuh", "jp_move_core.cuh"]
 PUBLIC_HEADERS = ["justpic_gb300.h", "justpic_gb300_rng.h"]
 

@@ -95,7 +95,7 @@ def cfl_dt(g, V, factor=1.0):
                         if np.max(np.abs(V[d])) > 0)
 
 
-# The five benchmark configurations (sizes, particle counts, steps).
+# The benchmark configurations (sizes, particle counts, steps).
 CONFIGS = {
     "C1": dict(ni=(256, 256), nxcell=24, max_xcell=48, min_xcell=12, method="RK2", steps=750,
                velocity="stream", fields=0,
@@ -107,11 +107,41 @@ CONFIGS = {
     "C4": dict(ni=(2048, 2048), nxcell=24, max_xcell=48, min_xcell=12, method="RK4", steps=750,
                velocity="stream", fields=1,
                desc="2D split-precision comparison, 2048x2048 cells, stream-function velocity, RK4, C2 step"),
+    "C5": dict(ni=(512, 512), nxcell=16, max_xcell=32, min_xcell=8, method="RK2", steps=100,
+               velocity="stream+noise", fields=1, checkpoint_every=10,
+               desc="2D adjoint run, FP64, 512x512 cells, stream-function velocity plus N(0, (0.1*250)^2) node "
+                    "noise, misfit 0.5||particle2grid(T) - T_target||^2, gradients w.r.t. Vx, Vy, T0"),
     "C3": dict(ni=(128, 128, 128), nxcell=24, max_xcell=48, min_xcell=12, method="RK2", steps=300,
                velocity="cellular3d", fields=1,
                desc="3D temperature advection, FP64, 128^3 cells, cellular flow + 0.1 z drift, advection!"
                     "+move_particles!+inject_particles!+particle2grid!"),
 }
+
+
+def perturbed_stream_velocity(g, sigma=0.1 * 250.0, seed=5):
+    """The stream-function velocity plus i.i.d. N(0, sigma^2) noise on every
+    staggered node (fixed over time)."""
+    rng = np.random.default_rng(seed)
+    return tuple(np.asfortranarray(v + sigma * rng.standard_normal(v.shape)) for v in stream_velocity(g))
+
+
+def fourier_target(g, nmodes=16, kmax=4, seed=11):
+    """A smooth random vertex field: the sum of ``nmodes`` Fourier modes with
+    integer wavenumbers 0 <= kx, ky <= kmax, random phases and N(0, 1/4)
+    amplitudes."""
+    rng = np.random.default_rng(seed)
+    kx = rng.integers(0, kmax + 1, nmodes)
+    ky = rng.integers(0, kmax + 1, nmodes)
+    ph = rng.uniform(0.0, 2.0 * np.pi, nmodes)
+    amp = 0.5 * rng.standard_normal(nmodes)
+
+    def f(x, y):
+        out = np.zeros_like(x)
+        for m in range(nmodes):
+            out += amp[m] * np.cos(2.0 * np.pi * (kx[m] * x + ky[m] * y) + ph[m])
+        return out
+
+    return on_grid(f, g["xv"])
 
 
 def setup(name: str, ni=None):
@@ -123,6 +153,9 @@ def setup(name: str, ni=None):
     g = grid(cfg["ni"])
     if cfg["velocity"] == "stream":
         V = stream_velocity(g)
+    elif cfg["velocity"] == "stream+noise":
+        V = perturbed_stream_velocity(g)
+        cfg["T_target"] = fourier_target(g)
     elif cfg["velocity"] == "rotation":
         V = rotation_velocity(g)
     else:
@@ -134,4 +167,5 @@ def setup(name: str, ni=None):
 
 
 __all__ = ["expand_range", "grid", "on_grid", "stream_velocity", "rotation_velocity", "cellular_velocity_3d",
-           "stream_velocity_3d", "gaussian_T", "linear_T", "cfl_dt", "CONFIGS", "setup"]
+           "stream_velocity_3d", "perturbed_stream_velocity", "fourier_target", "gaussian_T", "linear_T", "cfl_dt",
+           "CONFIGS", "setup"]
