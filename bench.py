@@ -190,17 +190,20 @@ def _setup_cfg(workload, ni):
     return W.setup(workload, None if ni is None else (ni,) * len(base))
 
 
-def run_ours(args):
+def run_ours(args, form=None, minimal=False):
+    """The bench line. With ``minimal`` (used for the split-precision figures
+    added to the FP64 line) only the device-resident timing is done and the
+    result is returned instead of printed."""
     import torch
 
     import justpic_gb300 as jp
 
     world, rank, local = _dist()
-    if world > 1:
+    if world > 1 and not minimal:
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    else:
+    elif world == 1:
         torch.cuda.set_device(0)
     jp._native.load()
 
@@ -209,7 +212,7 @@ def run_ours(args):
     N = g["ndim"]
     nf = 1 if "particle2grid!" in STEPS[args.workload] else 0
     dt = cfg["dt"]
-    f32 = args.form == "f32"
+    f32 = (form or args.form) == "f32"
     p = jp.init_particles(jp.CUDABackend, cfg["nxcell"], cfg["max_xcell"], cfg["min_xcell"], *g["grid_v"],
                           seed=jp.DEFAULT_SEED + rank)
     V = tuple(jp.TA("CUDA")(v) for v in cfg["V"])
@@ -313,6 +316,9 @@ def run_ours(args):
     value = live * args.steps * world / elapsed
     op_ms = {op: float(np.mean([events[k][i][0].elapsed_time(events[k][i][1]) for k in range(args.steps)]))
              for i, op in enumerate(ops)}
+    if minimal:
+        return {"value": live * args.steps / elapsed, "ms_per_step": 1e3 * elapsed / args.steps,
+                "per_call_ms": op_ms, "clocks": clocks.summary()}
 
     # ---- end to end through the public API (synchronous, host buffers) ----
     jp.set_synchronous(p, True)
@@ -402,6 +408,17 @@ def run_ours(args):
         "gpu_launches": sum(launches(op, N) for op in ops) * args.steps,
         "clocks": clocks.summary(),
     }
+    if not f32 and N == 2 and not args.no_split:
+        # the split-precision form on the same workload, and its error against this form
+        del p, fields, pT
+        sp = run_ours(args, "f32", True)
+        sp["speedup_vs_fp64"] = sp["value"] / value
+        sp["form"] = "split precision: int32 cell + FP32 offset, FP32 velocities/fields, FP64 renormalisation " \
+                     "and particle2grid! sums"
+        if rank == 0:
+            cmp_steps = 100
+            sp["error_vs_fp64"] = run_compare(args, steps=cmp_steps, quiet=True)
+        result["split_precision"] = sp
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)
     if world > 1:
@@ -410,7 +427,7 @@ def run_ours(args):
         print(json.dumps(result))
 
 
-def run_compare(args):
+def run_compare(args, steps=None, quiet=False):
     """The same seeded run in both forms for ``--steps`` steps (no timing):
     position error of the split-precision form in cell widths, by particle id,
     for every initial particle still present in both runs (injected particles
@@ -420,7 +437,9 @@ def run_compare(args):
 
     import justpic_gb300 as jp
 
-    torch.cuda.set_device(0)
+    if not quiet:
+        torch.cuda.set_device(0)
+    nsteps = steps or args.steps
     cfg = _setup_cfg(args.workload, args.ni)
     g = cfg["grid"]
     N = g["ndim"]
@@ -448,7 +467,7 @@ def run_compare(args):
     jp.grid2particle_(pTa, Ta, a)
     jp.grid2particle_f32_(pTb, Tb, b, xi)
     w0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(nsteps):
         jp.particle2grid_(Ta, pTa, a)
         jp.advection_(a, method, Va, dt)
         jp.move_particles_(a, fa)
@@ -493,7 +512,7 @@ def run_compare(args):
     out = {
         "workload": DESC[args.workload] if args.ni is None else DESC[args.workload] + f" (resized to {args.ni})",
         "integrator": type(method).__name__,
-        "steps": args.steps,
+        "steps": nsteps,
         "particles_compared": int(both.sum()),
         "live_fp64": int(a.index.data.sum()), "live_split": int(b.index.data.sum()),
         "position_error_cells": {"max": float(err.max()), "p99": float(torch.quantile(err[:1 << 24], 0.99)),
@@ -503,6 +522,8 @@ def run_compare(args):
                                 "field_range": float(Ta.max() - Ta.min())},
         "wall_s_both_forms": wall,
     }
+    if quiet:
+        return out
     print(json.dumps(out))
 
 
@@ -518,7 +539,7 @@ def run_adjoint(args):
     torch.cuda.set_device(0)
     cfg = _setup_cfg("C5", args.ni)
     g = cfg["grid"]
-    nsteps = cfg["steps"]
+    nsteps = args.adjoint_steps or cfg["steps"]
     k = cfg["checkpoint_every"]
     p = jp.init_particles(jp.CUDABackend, cfg["nxcell"], cfg["max_xcell"], cfg["min_xcell"], *g["grid_v"])
     V = tuple(jp.TA("CUDA")(v) for v in cfg["V"])
@@ -551,13 +572,17 @@ def run_adjoint(args):
     t_fwd, _ = timed(fwd, reps)
     t_grad, (loss, gV, gT0) = timed(grad, reps)
     rng = np.random.default_rng(17)
-    worst, checked = 0.0, []
+    checked = []
     h = 1e-6
     Vh = cfg["V"]
+    gmax = max(float(gv.abs().max()) for gv in gV)
     for n in range(args.fd_nodes):
-        c = n % 2
+        # even n: any node; odd n: a node where |dL/dV| is at least 1e-3 of its maximum
+        c = (n // 2) % 2
         gc = gV[c].cpu().numpy()
-        node = np.unravel_index(rng.integers(gc.size), gc.shape, order="F")
+        flat = gc.reshape(-1, order="F")
+        pool = np.flatnonzero(np.abs(flat) >= 1e-3 * gmax) if n % 2 else np.arange(flat.size)
+        node = np.unravel_index(int(rng.choice(pool)), gc.shape, order="F")
         Vp = [v.copy(order="F") for v in Vh]
         Vm = [v.copy(order="F") for v in Vh]
         Vp[c][node] += h
@@ -566,18 +591,26 @@ def run_adjoint(args):
         Fm, Wm = A.forward_field(p, method, tuple(jp.TA("CUDA")(v) for v in Vm), dt, nsteps, T0)
         fd = A.misfit_difference(Fp, Wp, Fm, Wm, target) / (2 * h)
         checked.append((float(gc[node]), fd))
+    fd_out = {"nodes": len(checked), "h": h}
     if checked:
         adj = np.array([a for a, _ in checked])
         fd = np.array([f for _, f in checked])
-        scale = np.max(np.abs(fd))
-        worst = float(np.max(np.abs(adj - fd) / np.maximum(np.abs(fd), 1e-6 * scale)))
+        err = np.abs(adj - fd)
+        active = np.abs(fd) >= 1e-3 * gmax
+        fd_out.update({
+            "max_err_over_max_gradient": float(np.max(err) / gmax),
+            "max_rel_err_active_nodes": float(np.max(err[active] / np.abs(fd[active]))) if active.any() else None,
+            "active_nodes": int(active.sum()),
+            "active": "|fd| >= 1e-3 of max |dL/dV|",
+            "pairs_adjoint_fd": [[float(a), float(f)] for a, f in checked[:8]],
+        })
     print(json.dumps({
         "workload": DESC["C5"] if args.ni is None else DESC["C5"] + f" (resized to {args.ni})",
         "live_particles": live, "steps": nsteps, "checkpoint_every": k, "loss": loss,
         "forward_s": t_fwd, "forward_plus_gradient_s": t_grad, "gradient_cost_vs_forward": t_grad / t_fwd,
         "forward_particle_steps_per_s": live * nsteps / t_fwd,
-        "fd_check": {"nodes": len(checked), "h": h, "max_rel_err": worst,
-                     "floor": "1e-6 of the largest |fd| among the checked nodes"},
+        "max_abs_gradient": gmax,
+        "fd_check": fd_out,
     }))
 
 
@@ -692,6 +725,10 @@ def main():
                     help="run the same seeded workload in both forms for --steps steps and print the errors")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-split", action="store_true",
+                    help="FP64 line without the split-precision timing and error added to it")
+    ap.add_argument("--adjoint-steps", type=int, default=0,
+                    help="C5: steps of the run (default: the workload's 100)")
     ap.add_argument("--fd-nodes", type=int, default=0,
                     help="C5: number of random velocity nodes checked by central finite differences")
     ap.add_argument("--ni", type=int, default=None,

@@ -133,7 +133,7 @@ int jp_move_particles(jp_particles* p, double* const coords[3], uint8_t* index,
  * a shadow record per slot) comes from one fixed device array of
  * JP_NOALLOC_SCRATCH_BYTES that is part of the library: every GPU on which the
  * library is loaded holds it until the process exits. A container needing more
- * (5*8 bytes per cell plus (8*(ndim+nargs)+3) bytes per slot) is rejected with
+ * (120 bytes per cell in 2D, 40 in 3D, plus (8*(ndim+nargs)+3) bytes per slot) is rejected with
  * JP_ERR_INVALID_ARGUMENT and a message naming the sizes; use
  * jp_move_particles there. The first call on a device looks up the array's
  * device address (and may load the library's device code), so make that first
@@ -164,6 +164,26 @@ int jp_particle2grid(jp_particles* p, double* F, const double* Fp, const double*
                      const uint8_t* index);
 
 /*
+ * Transfers beside the hot path, on the same layout (FP64, 2D and 3D):
+ * grid2particle_flip!(Fp, xvi, F, F0, particles; α)
+ *   (src/Interpolations/grid_to_particle.jl:125-170) with xvi = the container's
+ *   vertex grid: Fp = muladd(F_pic, α, (Fp + F_pic - F0_pic) (1 - α)) for every
+ *   live slot, F and F0 vertex fields;
+ * centroid2particle!(Fp, F, particles) (src/Interpolations/centroid_to_particle.jl:13-46):
+ *   N-linear interpolation of the cell-centred field F (n0 x n1 (x n2)) to every
+ *   slot with non-NaN coordinates;
+ * particle2centroid!(F, Fp, particles) (src/Interpolations/particle_to_grid_centroid.jl:10-110):
+ *   bilinear-weight average of each cell's particles at its centre.
+ * The centroid transfers use the container's centre grids (Particles.xci,
+ * di.center) and need the ghost-expanded centre grids of init_particles with
+ * at least 2 cells per axis (JP_ERR_INVALID_ARGUMENT otherwise).
+ */
+int jp_grid2particle_flip(jp_particles* p, double* Fp, const double* F, const double* F0, double alpha,
+                          const double* const coords[3], const uint8_t* index);
+int jp_centroid2particle(jp_particles* p, double* Fp, const double* F, const double* const coords[3]);
+int jp_particle2centroid(jp_particles* p, double* F, const double* Fp, const double* const coords[3]);
+
+/*
  * Adjoint (vector-Jacobian products) of the FP64 path, 2D only. No
  * counterpart in the reference: it is what a ChainRulesCore rrule of the
  * Julia API calls. Gradient arrays share the layout of the values they
@@ -181,9 +201,9 @@ int jp_particle2grid(jp_particles* p, double* F, const double* Fp, const double*
  *   as an extra particle field to jp_inject_particles: afterwards an injected
  *   slot holds the id of the particle its fields were copied from.
  * jp_inject_vjp: with those ids, pre[k][a] = post[k][a] for slots that existed
- *   before the injection and 0 for injected ones; with copies != 0 each
- *   existing slot also receives post[k] of the slots injected from it (use
- *   copies = 0 for positions, 1 for particle fields).
+ *   before the injection and 0 for injected ones; for the arrays k whose bit is
+ *   set in `copies`, each existing slot also receives post[k] of the slots
+ *   injected from it (set the bits of particle fields, not of positions).
  * jp_advection_vjp: one advection! step (same method, alpha, V, dt) taken
  *   from coords (the positions BEFORE the step): lam holds dL/dX after the step
  *   on entry and dL/dX before it on return; dL/dV is ADDED to gV. Fails with

@@ -16,7 +16,10 @@ All compute runs in hand-written sm_103a CUDA kernels; there is no CPU path.
 from ._native import ArgumentError, JustPICError, NativeLibraryMissing  # noqa: F401
 from .api import (  # noqa: F401
     advection_,
+    centroid2particle_,
     grid2particle_,
+    grid2particle_flip_,
+    particle2centroid_,
     inject_particles_,
     move_particles_,
     particle2grid_,

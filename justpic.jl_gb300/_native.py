@@ -89,6 +89,11 @@ SIGNATURES = [
      [ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     ("jp_grid2particle_f32", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
     ("jp_particle2grid_f32", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
+    # transfers beside the hot path
+    ("jp_grid2particle_flip", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, P3, ctypes.c_void_p]),
+    ("jp_centroid2particle", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3]),
+    ("jp_particle2centroid", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3]),
     # adjoint (2D, FP64)
     ("jp_particle2grid_with_weights", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),

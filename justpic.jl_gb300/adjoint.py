@@ -134,13 +134,16 @@ def slot_ids(particles: Particles, index=None) -> CellArray:
     return ids
 
 
-def inject_vjp_(particles: Particles, ids: CellArray, post, pre, copies: bool) -> None:
-    """Replay of an inject_particles! call traced with ``ids``."""
+def inject_vjp_(particles: Particles, ids: CellArray, post, pre, copies) -> None:
+    """Replay of an inject_particles! call traced with ``ids``. ``copies``:
+    True/False for every array, or one flag per array (True for particle
+    fields, whose values injected particles copied; False for positions)."""
     _require_2d(particles)
     post, pre = list(post), list(pre)
+    flags = [bool(copies)] * len(post) if isinstance(copies, bool) else [bool(c) for c in copies]
+    mask = sum(1 << k for k, f in enumerate(flags) if f)
     _bind_stream(particles)
-    rc = _native.load().jp_inject_vjp(particles.handle, ids.data_ptr(), _ptrs(post), _ptrs(pre), len(post),
-                                      1 if copies else 0)
+    rc = _native.load().jp_inject_vjp(particles.handle, ids.data_ptr(), _ptrs(post), _ptrs(pre), len(post), mask)
     _finish(particles, rc, "inject_particles! adjoint")
 
 
@@ -197,24 +200,46 @@ def misfit(F: torch.Tensor, W: torch.Tensor, target: torch.Tensor):
     return 0.5 * float((r * r).sum()), r
 
 
+def _recorded_step(p: Particles, method, V, dt, fields, inject: bool):
+    """One step that also records what the reverse sweep needs: positions and
+    occupancy before it, the move's slot map and the injection's source ids."""
+    X = tuple(c.data.clone() for c in p.coords)
+    idx = p.index.data.clone()
+    advection_(p, method, V, dt)
+    move_particles_(p, fields)
+    dest = move_permutation(p)
+    ids = None
+    if inject:
+        ids = slot_ids(p)
+        inject_particles_(p, tuple(fields) + (ids,))
+    return X, idx, dest, ids
+
+
 def run_forward(particles: Particles, method, V, dt, nsteps: int, T: CellArray, inject: bool = True,
-                checkpoint_every: int = 0):
+                checkpoint_every: int = 0, record_last_segment: bool = False):
     """Run nsteps of advection!/move_particles!(/inject_particles!) carrying
     the particle field T, in place; returns the checkpoints taken every
-    ``checkpoint_every`` steps (the state before steps 0, k, 2k, ...)."""
-    cps = []
+    ``checkpoint_every`` steps (the state before steps 0, k, 2k, ...) and,
+    with ``record_last_segment``, the records of the steps after the last
+    checkpoint (so the reverse sweep need not run them again)."""
+    cps, recs = [], []
+    last = ((nsteps - 1) // checkpoint_every) * checkpoint_every if checkpoint_every and nsteps else nsteps
     for n in range(nsteps):
         if checkpoint_every and n % checkpoint_every == 0:
             cps.append(_save(particles))
-        _step(particles, method, V, dt, (T,), inject)
-    return cps
+        if record_last_segment and n >= last:
+            recs.append(_recorded_step(particles, method, V, dt, (T,), inject))
+        else:
+            _step(particles, method, V, dt, (T,), inject)
+    return (cps, recs) if record_last_segment else cps
 
 
 def reverse_sweep(particles: Particles, method, V, dt, nsteps: int, checkpoints, k: int, gX, gT: CellArray,
-                  inject: bool = True):
+                  inject: bool = True, last_records=None):
     """Back-propagate dL/dX (gX) and dL/dT (gT) of the state after nsteps to
-    the state before step 0, accumulating dL/dV. The particles are left in
-    the state before step 0. Returns (gV, gX0, gT0)."""
+    the state before step 0, accumulating dL/dV (``last_records``: the last
+    segment's records from run_forward, if it kept them). The particles are
+    left in the state before step 0. Returns (gV, gX0, gT0)."""
     _require_2d(particles)
     gV = tuple(grid_field(tuple(v.shape), 0.0) for v in V)
     lam = [c.data.clone() for c in gX]
@@ -225,29 +250,19 @@ def reverse_sweep(particles: Particles, method, V, dt, nsteps: int, checkpoints,
     for seg in reversed(range(nseg)):
         n0 = seg * k
         n1 = min(n0 + k, nsteps)
-        _restore(particles, checkpoints[seg])
-        recs = []
-        for n in range(n0, n1):  # recompute the segment, recording positions and slot maps
-            X = tuple(c.data.clone() for c in particles.coords)
-            idx = particles.index.data.clone()
-            advection_(particles, method, V, dt)
-            move_particles_(particles, ())
-            dest = move_permutation(particles)
-            ids = None
-            if inject:
-                ids = slot_ids(particles)
-                inject_particles_(particles, (ids,))
-            recs.append((X, idx, dest, ids))
+        if seg == nseg - 1 and last_records:
+            recs = last_records
+        else:  # recompute the segment, recording positions and slot maps
+            _restore(particles, checkpoints[seg])
+            recs = [_recorded_step(particles, method, V, dt, (), inject) for _ in range(n0, n1)]
         for X, idx, dest, ids in reversed(recs):
             if ids is not None:
-                inject_vjp_(particles, ids, lam, tmp_x, copies=False)
-                inject_vjp_(particles, ids, (gT,), (tmp_t,), copies=True)
+                inject_vjp_(particles, ids, lam + [gT], tmp_x + [tmp_t], copies=(False, False, True))
                 permute_vjp_(particles, dest, tmp_x + [tmp_t], lam + [gT])
             else:
-                for a, b in zip(lam, tmp_x):
-                    b.copy_(a)
-                tmp_t.copy_(gT)
-                permute_vjp_(particles, dest, tmp_x + [tmp_t], lam + [gT])
+                permute_vjp_(particles, dest, lam + [gT], tmp_x + [tmp_t])
+                lam, tmp_x = tmp_x, lam
+                gT, tmp_t = tmp_t, gT
             advection_vjp_(particles, method, V, dt, X, _Idx(idx), lam, gV)
     _restore(particles, checkpoints[0])
     ni = particles.ni
@@ -279,7 +294,8 @@ def misfit_gradient(particles: Particles, method, V, dt, nsteps: int, T0: CellAr
     T = CellArray(T0.data.clone(), T0.ni)
     try:
         with _deferred(particles):
-            cps = run_forward(particles, method, V, dt, nsteps, T, inject, checkpoint_every=k)
+            cps, last = run_forward(particles, method, V, dt, nsteps, T, inject, checkpoint_every=k,
+                                    record_last_segment=True)
             if not cps:
                 cps = [start]
             F = grid_field(_vertex_shape(particles), 0.0)
@@ -289,7 +305,8 @@ def misfit_gradient(particles: Particles, method, V, dt, nsteps: int, T0: CellAr
             gT = _like(particles)
             gX = tuple(_like(particles) for _ in range(particles.ndim))
             particle2grid_vjp_(gT, gX, _colmajor(gF), F, W, T, particles)
-            gV, _, gT0 = reverse_sweep(particles, method, V, dt, nsteps, cps, k, gX, gT, inject)
+            gV, _, gT0 = reverse_sweep(particles, method, V, dt, nsteps, cps, k, gX, gT, inject,
+                                       last_records=last)
     finally:
         _restore(particles, start)
     return loss, gV, gT0

@@ -162,3 +162,48 @@ def particle2grid_(F: torch.Tensor, Fp: CellArray, particles: Particles) -> None
     rc = _native.load().jp_particle2grid(particles.handle, F.data_ptr(), Fp.data_ptr(), _coords(particles),
                                          particles.index.data_ptr())
     _finish(particles, rc, "particle2grid!")
+
+
+# ---- transfers beside the hot path ------------------------------------------
+def _centre_shape(p: Particles):
+    return tuple(p.ni)
+
+
+def grid2particle_flip_(Fp: CellArray, xvi, F: torch.Tensor, F0: torch.Tensor, particles: Particles,
+                        alpha: float = 0.0) -> None:
+    """``grid2particle_flip!(Fp, xvi, F, F0, particles; α)``
+    (src/Interpolations/grid_to_particle.jl:125): PIC/FLIP blend of the vertex
+    fields F (new) and F0 (old) into Fp. ``xvi`` must be the particles'
+    vertex grid (or None for it)."""
+    _check_cellarray(particles, Fp, "Fp")
+    _check_grid(F, _vertex_shape(particles), "F")
+    _check_grid(F0, _vertex_shape(particles), "F0")
+    if xvi is not None:
+        for d in range(particles.ndim):
+            if not np.array_equal(np.asarray(xvi[d], dtype=np.float64), np.asarray(particles.xvi[d])):
+                raise ArgumentError("grid2particle_flip!: xvi must be the particles' vertex grid")
+    _bind_stream(particles)
+    rc = _native.load().jp_grid2particle_flip(particles.handle, Fp.data_ptr(), F.data_ptr(), F0.data_ptr(),
+                                              float(alpha), _coords(particles), particles.index.data_ptr())
+    _finish(particles, rc, "grid2particle_flip!")
+
+
+def centroid2particle_(Fp: CellArray, F: torch.Tensor, particles: Particles) -> None:
+    """``centroid2particle!(Fp, F, particles)`` (src/Interpolations/centroid_to_particle.jl:13):
+    cell-centred field F (one value per cell) to the particles."""
+    _check_cellarray(particles, Fp, "Fp")
+    _check_grid(F, _centre_shape(particles), "F")
+    _bind_stream(particles)
+    rc = _native.load().jp_centroid2particle(particles.handle, Fp.data_ptr(), F.data_ptr(), _coords(particles))
+    _finish(particles, rc, "centroid2particle!")
+
+
+def particle2centroid_(F: torch.Tensor, Fp: CellArray, particles: Particles) -> None:
+    """``particle2centroid!(F, Fp, particles)`` (src/Interpolations/particle_to_grid_centroid.jl:10):
+    particles to the cell centres."""
+    _check_cellarray(particles, Fp, "Fp")
+    _check_grid(F, _centre_shape(particles), "F")
+    _bind_stream(particles)
+    rc = _native.load().jp_particle2centroid(particles.handle, F.data_ptr(), Fp.data_ptr(), _coords(particles))
+    _finish(particles, rc, "particle2centroid!")
+

@@ -16,10 +16,11 @@
 // Transpose of the velocity sampling: a particle owned by cell I whose stage
 // points stay within one cell of I deposits only on velocity nodes in a fixed
 // window around I (4 x 5 nodes for Vx, 5 x 4 for Vy on the ghost-node grids).
-// One thread per owning cell accumulates its particles' deposits, in slot
-// order, into 40 partial sums; one thread per velocity node then adds the
-// partial sums of the 20 owning cells whose windows contain it. A stage point
-// outside the window is reported as JP_ERR_ADJOINT_WINDOW.
+// The deposits of a cell's particles are accumulated, in slot order, into 40
+// partial sums per cell by the lane that owns the cell; one thread per
+// velocity node then adds the partial sums of the 20 owning cells whose
+// windows contain it. A stage point outside the window is reported as
+// JP_ERR_ADJOINT_WINDOW.
 #include <cmath>
 
 #include <math_constants.h>
@@ -29,7 +30,6 @@
 
 namespace jp {
 
-constexpr int kAdjThreads = 128;
 constexpr int kWinParts = 40;    // 4*5 + 5*4 partial sums per owning cell
 constexpr int kInjectReach = 4;  // 2D: four colour passes, each copy reaches one cell further
 
@@ -40,14 +40,12 @@ __host__ __device__ constexpr int win_ny(int comp) { return comp == 0 ? 5 : 4; }
 // ------------------------------------------------------- move permutation
 // dest[a] = slot holding, after the last move, the particle that sat in slot a
 // before it; -1 for empty slots and dropped particles.
-__global__ void __launch_bounds__(kThreads)
-    perm_init(DevGrid g, const uint64_t* __restrict__ L0, const uint64_t* __restrict__ L,
-              const uint64_t* __restrict__ R, int32_t* __restrict__ dest)
+__global__ void __launch_bounds__(kThreads) perm_init(DevGrid g, MoveView S, int32_t* __restrict__ dest)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncells) return;
     const int64_t nc = g.ncells;
-    const uint64_t stay = L0[c] & L[c] & ~R[c];
+    const uint64_t stay = S.L0(c) & S.L(c) & ~S.R(c);
     for (int s = 0; s < g.max_xcell; ++s) {
         const int64_t a = c + nc * s;
         dest[a] = ((stay >> s) & 1) ? (int32_t)a : -1;
@@ -60,7 +58,7 @@ __global__ void __launch_bounds__(kThreads) perm_scatter(DevGrid g, MoveView S, 
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncells) return;
     const int64_t nc = g.ncells;
-    uint64_t R = S.R[c];
+    uint64_t R = S.R(c);
     if (!R) return;
     int64_t I[3];
     cell_coords(g, c, I);
@@ -132,12 +130,12 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // pre[k][a] = post[k][a] for slots that existed before the injection (id ==
-// own slot), 0 otherwise; with `copies`, a pre-existing slot also collects
-// post[k][b] of every slot b injected from it, cells of the window in order
-// (y outer, x inner), slots ascending.
+// own slot), 0 otherwise; for the arrays k in the `copies` bit mask, a
+// pre-existing slot also collects post[k][b] of every slot b injected from it,
+// cells of the window in order (y outer, x inner), slots ascending.
 __global__ void __launch_bounds__(kThreads)
     inject_vjp_kernel(DevGrid g, const double* __restrict__ ids, const uint64_t* __restrict__ inj, PermArrays P,
-                      int copies)
+                      unsigned copies)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncells) return;
@@ -159,7 +157,8 @@ __global__ void __launch_bounds__(kThreads)
                 const int64_t b = w + nc * s;
                 const int64_t src = (int64_t)ids[b];  // in range: inject_mask_kernel checked it
                 if (src % nc != c) continue;
-                for (int k = 0; k < P.n; ++k) P.pre[k][src] += P.post[k][b];
+                for (int k = 0; k < P.n; ++k)
+                    if ((copies >> k) & 1u) P.pre[k][src] += P.post[k][b];
             }
         }
 }
@@ -186,8 +185,10 @@ __device__ __forceinline__ Samp sample2(const DevGrid& g, int comp, const double
         const double* x = g.xvel[comp][d];
         const int J = I[d];
         const double a = ldg(x + J), b = ldg(x + J + 1);
+        const long long kp = okey(p[d]);
         int64_t k;
-        if (a <= p[d] && p[d] <= b) {
+        // the seed test on integer keys (exact for non-NaN values, off the FP64 pipe)
+        if (!is_nan_bits(p[d]) && okey(a) <= kp && kp <= okey(b)) {
             k = J;
         } else {
             if (!(g.lim_lo[comp][0] <= p[0] && p[0] <= g.lim_hi[comp][0] && g.lim_lo[comp][1] <= p[1] &&
@@ -204,9 +205,12 @@ __device__ __forceinline__ Samp sample2(const DevGrid& g, int comp, const double
     const double* b = V + r.idx[0] + L0 * r.idx[1];
     const double v00 = ldg(b), v10 = ldg(b + 1), v01 = ldg(b + L0), v11 = ldg(b + L0 + 1);
     const double tx = r.t[0], ty = r.t[1];
-    r.v = lerp1(ty, lerp1(tx, v00, v10), lerp1(tx, v01, v11));
-    r.dv[0] = ((1.0 - ty) * (v10 - v00) + ty * (v11 - v01)) * ldg(g.ixvel[comp][0] + r.idx[0]);
-    r.dv[1] = ((1.0 - tx) * (v01 - v00) + tx * (v11 - v10)) * ldg(g.ixvel[comp][1] + r.idx[1]);
+    const double a0 = lerp1(tx, v00, v10), a1 = lerp1(tx, v01, v11);
+    r.v = lerp1(ty, a0, a1);
+    // gradient of the bilinear form: d/dtx = (1-ty)(v10-v00) + ty(v11-v01), d/dty = a1 - a0
+    const double ax = v10 - v00, bx = v11 - v01;
+    r.dv[0] = fma(ty, bx - ax, ax) * ldg(g.ixvel[comp][0] + r.idx[0]);
+    r.dv[1] = (a1 - a0) * ldg(g.ixvel[comp][1] + r.idx[1]);
     return r;
 }
 
@@ -216,23 +220,6 @@ struct AdjParams {
     int method;
 };
 
-// deposit w * (bilinear weights) of one stage sample on the owning cell's window
-__device__ __forceinline__ bool deposit(double (*part)[kAdjThreads], int comp, const Samp& s, const int* I,
-                                        double w)
-{
-    const int NX = win_nx(comp), NY = win_ny(comp);
-    const int ox = s.idx[0] - I[0] + 1, oy = s.idx[1] - I[1] + 1;
-    if (ox < 0 || ox > NX - 2 || oy < 0 || oy > NY - 2) return false;
-    const int base = (comp == 0 ? 0 : 20) + ox + NX * oy;
-    const double tx = s.t[0], ty = s.t[1];
-    const int t = threadIdx.x;
-    part[base][t] = fma(w, (1.0 - tx) * (1.0 - ty), part[base][t]);
-    part[base + 1][t] = fma(w, tx * (1.0 - ty), part[base + 1][t]);
-    part[base + NX][t] = fma(w, (1.0 - tx) * ty, part[base + NX][t]);
-    part[base + NX + 1][t] = fma(w, tx * ty, part[base + NX + 1][t]);
-    return true;
-}
-
 // J^T g for the two components sampled at one point
 __device__ __forceinline__ void jt(const Samp* s, const double* g, double* out)
 {
@@ -240,109 +227,195 @@ __device__ __forceinline__ void jt(const Samp* s, const double* g, double* out)
     out[1] = s[0].dv[1] * g[0] + s[1].dv[1] * g[1];
 }
 
-// One thread per owning cell: replays the step's stages for each live slot (in
-// slot order), maps lam (dL/dX after the step) to dL/dX before it, and
-// accumulates the velocity deposits into the cell's 40 partial sums.
+constexpr int kAdjWarps = 4;
+
+// One staged particle: per velocity sample q (stage q/2, component q%2) its
+// local coordinates, its cotangent and its window position.
+template <int NSAMP>
+struct Staged {
+    double tx[NSAMP], ty[NSAMP], gk[NSAMP];
+    int8_t ox[NSAMP], oy[NSAMP];
+    int cell;  // owning lane, -1: nothing to deposit
+};
+
 template <int METHOD>
-__global__ void __launch_bounds__(kAdjThreads)
+constexpr int adj_stages()
+{
+    return METHOD == JP_RUNGE_KUTTA4 ? 4 : (METHOD == JP_RUNGE_KUTTA2 ? 2 : 1);
+}
+
+template <int METHOD>
+constexpr size_t advect_vjp_smem()
+{
+    return (size_t)kAdjWarps * (kWinParts * 32 * sizeof(double) + 32 * sizeof(Staged<2 * adj_stages<METHOD>()>));
+}
+
+// Each warp covers 32 consecutive cells. Its lanes take the warp's live
+// particles in slot-major order (full lanes whatever the cell occupancy),
+// replay each particle's stages with the forward's cell selection, map lam
+// (dL/dX after the step) to dL/dX before it, and stage the velocity
+// cotangents; then the lane owning each cell adds its staged particles to the
+// cell's 40 window partial sums. A round of 32 slot-major items holds each
+// cell at most a few times, so the owners' work is balanced too, and each cell
+// accumulates its particles in slot order (deterministic).
+template <int METHOD>
+__global__ void __launch_bounds__(32 * kAdjWarps)
     advect_vjp_kernel(DevGrid g, const double* __restrict__ V0, const double* __restrict__ V1, AdjParams P,
                       CCoords X, const uint8_t* __restrict__ index, Coords Lam, double* __restrict__ parts,
                       int* d_err)
 {
-    constexpr int NS = METHOD == JP_RUNGE_KUTTA4 ? 4 : (METHOD == JP_RUNGE_KUTTA2 ? 2 : 1);
-    __shared__ double part[kWinParts][kAdjThreads];
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.ncells) return;
+    constexpr int NS = adj_stages<METHOD>();
+    constexpr int NQ = 2 * NS;
+    extern __shared__ __align__(16) unsigned char smem_adj[];
+    __shared__ SlotList lists[kAdjWarps];
+    __shared__ int cellI[kAdjWarps][32][2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* part = (double*)smem_adj + (size_t)w * kWinParts * 32;  // [k][lane]
+    Staged<NQ>* st = (Staged<NQ>*)(smem_adj + (size_t)kAdjWarps * kWinParts * 32 * sizeof(double)) + w * 32;
+    const int64_t c0 = ((int64_t)blockIdx.x * kAdjWarps + w) * 32;
+    if (c0 >= g.ncells) return;
     const int64_t nc = g.ncells;
-    for (int k = 0; k < kWinParts; ++k) part[k][threadIdx.x] = 0.0;
-    const int I[2] = {(int)(c % g.n[0]), (int)(c / g.n[0])};
+    const int M = g.max_xcell;
+    {
+        const int64_t c = min(c0 + lane, nc - 1);
+        cellI[w][lane][0] = (int)(c % g.n[0]);
+        cellI[w][lane][1] = (int)(c / g.n[0]);
+    }
+    for (int k = 0; k < kWinParts; ++k) part[k * 32 + lane] = 0.0;
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
     const double* Vc[2] = {V0, V1};
     int errs = 0;
-    uint64_t m = live_mask(index, c, nc, g.max_xcell);
-    while (m) {
-        const int s = __ffsll((long long)m) - 1;
-        m &= m - 1;
-        const int64_t a = c + nc * s;
-        const double p0[2] = {X.c[0][a], X.c[1][a]};
-        const double lam[2] = {Lam.c[0][a], Lam.c[1][a]};
-        // forward stages with the forward's arithmetic, keeping every sample
-        Samp S[NS][2];
-        bool ok = true;
+    for (int base = 0; base < K; base += 32) {
+        const int k = base + lane;
+        int owner = -1;
+        if (k < K) {
+            int s, l;
+            slot_item(lists[w], M, k, &s, &l);
+            const int64_t a = c0 + l + nc * s;
+            const int I[2] = {cellI[w][l][0], cellI[w][l][1]};
+            const double p0[2] = {X.c[0][a], X.c[1][a]};
+            const double lam[2] = {Lam.c[0][a], Lam.c[1][a]};
+            // forward stages with the forward's arithmetic, keeping every sample
+            Samp S[NS][2];
+            bool ok = true;
 #pragma unroll
-        for (int st = 0; st < NS; ++st) {
-            double q[2];
-#pragma unroll
-            for (int d = 0; d < 2; ++d) {
-                if (st == 0)
-                    q[d] = p0[d];
-                else if (METHOD == JP_RUNGE_KUTTA2)
-                    q[d] = fma(1.0, P.adt * S[0][d].v, p0[d]);
-                else if (st < 3)
-                    q[d] = p0[d] + (P.dt * S[st - 1][d].v) * 0.5;
-                else
-                    q[d] = p0[d] + P.dt * S[2][d].v;
-            }
-#pragma unroll
-            for (int cc = 0; cc < 2; ++cc) {
-                S[st][cc] = sample2(g, cc, q, I, Vc[cc], &errs);
-                ok &= S[st][cc].ok;
-            }
-            if (!ok) break;
-        }
-        if (!ok) {  // the forward sent this particle to Inf; move_particles! dropped it
-            Lam.c[0][a] = 0.0;
-            Lam.c[1][a] = 0.0;
-            continue;
-        }
-        // reverse sweep over the stages: gk[st] = dL/d(velocity sample of stage st)
-        double gk[NS][2], l0[2] = {lam[0], lam[1]}, qb[2];
-        if (METHOD == JP_RUNGE_KUTTA2) {
-#pragma unroll
-            for (int d = 0; d < 2; ++d) {
-                gk[NS - 1][d] = P.dt * P.cb * lam[d];
-                gk[0][d] = P.dt * P.ca * lam[d];
-            }
-            jt(S[NS - 1], gk[NS - 1], qb);  // q2 = p0 + alpha dt k1
-#pragma unroll
-            for (int d = 0; d < 2; ++d) {
-                l0[d] += qb[d];
-                gk[0][d] += P.adt * qb[d];
-            }
-        } else if (METHOD == JP_RUNGE_KUTTA4) {
-            const double w6 = P.dt / 6.0;
-#pragma unroll
-            for (int d = 0; d < 2; ++d) {
-                gk[0][d] = w6 * lam[d];
-                gk[1][d] = 2.0 * w6 * lam[d];
-                gk[2][d] = 2.0 * w6 * lam[d];
-                gk[NS - 1][d] = w6 * lam[d];
-            }
-#pragma unroll
-            for (int st = NS - 1; st >= 1; --st) {  // q4 = p0 + dt k3, q3 = p0 + dt/2 k2, q2 = p0 + dt/2 k1
-                jt(S[st], gk[st], qb);
-                const double h = st == 3 ? P.dt : 0.5 * P.dt;
+            for (int q = 0; q < NS; ++q) {
+                double x[2];
 #pragma unroll
                 for (int d = 0; d < 2; ++d) {
-                    l0[d] += qb[d];
-                    gk[st - 1][d] += h * qb[d];
+                    if (q == 0)
+                        x[d] = p0[d];
+                    else if (METHOD == JP_RUNGE_KUTTA2)
+                        x[d] = fma(1.0, P.adt * S[0][d].v, p0[d]);
+                    else if (q < 3)
+                        x[d] = p0[d] + (P.dt * S[q - 1][d].v) * 0.5;
+                    else
+                        x[d] = p0[d] + P.dt * S[2][d].v;
                 }
+#pragma unroll
+                for (int cc = 0; cc < 2; ++cc) {
+                    S[q][cc] = sample2(g, cc, x, I, Vc[cc], &errs);
+                    ok &= S[q][cc].ok;
+                }
+                if (!ok) break;
             }
-        } else {
+            if (!ok) {  // the forward sent this particle to Inf; move_particles! dropped it
+                Lam.c[0][a] = 0.0;
+                Lam.c[1][a] = 0.0;
+            } else {
+                // reverse sweep over the stages: gk[q] = dL/d(velocity sample of stage q)
+                double gk[NS][2], l0[2] = {lam[0], lam[1]}, qb[2];
+                if (METHOD == JP_RUNGE_KUTTA2) {
 #pragma unroll
-            for (int d = 0; d < 2; ++d) gk[0][d] = P.dt * lam[d];
+                    for (int d = 0; d < 2; ++d) {
+                        gk[NS - 1][d] = P.dt * P.cb * lam[d];
+                        gk[0][d] = P.dt * P.ca * lam[d];
+                    }
+                    jt(S[NS - 1], gk[NS - 1], qb);  // x1 = p0 + alpha dt k0
+#pragma unroll
+                    for (int d = 0; d < 2; ++d) {
+                        l0[d] += qb[d];
+                        gk[0][d] += P.adt * qb[d];
+                    }
+                } else if (METHOD == JP_RUNGE_KUTTA4) {
+                    const double w6 = P.dt / 6.0;
+#pragma unroll
+                    for (int d = 0; d < 2; ++d) {
+                        gk[0][d] = w6 * lam[d];
+                        gk[1][d] = 2.0 * w6 * lam[d];
+                        gk[2][d] = 2.0 * w6 * lam[d];
+                        gk[NS - 1][d] = w6 * lam[d];
+                    }
+#pragma unroll
+                    for (int q = NS - 1; q >= 1; --q) {  // x3 = p0 + dt k2, x2 = p0 + dt/2 k1, x1 = p0 + dt/2 k0
+                        jt(S[q], gk[q], qb);
+                        const double h = q == 3 ? P.dt : 0.5 * P.dt;
+#pragma unroll
+                        for (int d = 0; d < 2; ++d) {
+                            l0[d] += qb[d];
+                            gk[q - 1][d] += h * qb[d];
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int d = 0; d < 2; ++d) gk[0][d] = P.dt * lam[d];
+                }
+                jt(S[0], gk[0], qb);  // the first stage samples at p0 itself
+#pragma unroll
+                for (int d = 0; d < 2; ++d) l0[d] += qb[d];
+                Lam.c[0][a] = l0[0];
+                Lam.c[1][a] = l0[1];
+                Staged<NQ>& r = st[lane];
+#pragma unroll
+                for (int q = 0; q < NS; ++q)
+#pragma unroll
+                    for (int cc = 0; cc < 2; ++cc) {
+                        const int j = 2 * q + cc;
+                        const int ox = S[q][cc].idx[0] - I[0] + 1, oy = S[q][cc].idx[1] - I[1] + 1;
+                        const bool in = ox >= 0 && ox <= win_nx(cc) - 2 && oy >= 0 && oy <= win_ny(cc) - 2;
+                        if (!in) errs |= kErrAdjointWindow;
+                        r.ox[j] = (int8_t)(in ? ox : -1);
+                        r.oy[j] = (int8_t)oy;
+                        r.tx[j] = S[q][cc].t[0];
+                        r.ty[j] = S[q][cc].t[1];
+                        r.gk[j] = gk[q][cc];
+                    }
+                owner = l;
+            }
         }
-        jt(S[0], gk[0], qb);  // the first stage samples at p0 itself
+        st[lane].cell = owner;
+        __syncwarp();
+        // Each lane adds the staged particles of its own cell, in slot order:
+        // the round's items span slots s_lo..s_hi, and cell `lane` holds item
+        // pre[s] + (live cells below it in slot s) of each slot where it is live.
+        int s_lo, s_hi, l_unused;
+        slot_item(lists[w], M, base, &s_lo, &l_unused);
+        slot_item(lists[w], M, min(base + 31, K - 1), &s_hi, &l_unused);
+        for (int s = s_lo; s <= s_hi; ++s) {
+            const uint32_t m = lists[w].mask[s];
+            if (!((m >> lane) & 1u)) continue;
+            const int j = lists[w].pre[s] + __popc(m & ((1u << lane) - 1u)) - base;
+            if (j < 0 || j >= 32 || st[j].cell != lane) continue;
+            const Staged<NQ>& r = st[j];
 #pragma unroll
-        for (int d = 0; d < 2; ++d) l0[d] += qb[d];
-        Lam.c[0][a] = l0[0];
-        Lam.c[1][a] = l0[1];
-#pragma unroll
-        for (int st = 0; st < NS; ++st)
-#pragma unroll
-            for (int cc = 0; cc < 2; ++cc)
-                if (!deposit(part, cc, S[st][cc], I, gk[st][cc])) errs |= kErrAdjointWindow;
+            for (int q = 0; q < NQ; ++q) {
+                if (r.ox[q] < 0) continue;
+                const int cc = q & 1;
+                const int NX = win_nx(cc);
+                const int b = (cc == 0 ? 0 : 20) + r.ox[q] + NX * r.oy[q];
+                const double tx = r.tx[q], ty = r.ty[q];
+                const double g0 = r.gk[q] * (1.0 - ty), g1 = r.gk[q] * ty;
+                part[b * 32 + lane] = fma(g0, 1.0 - tx, part[b * 32 + lane]);
+                part[(b + 1) * 32 + lane] = fma(g0, tx, part[(b + 1) * 32 + lane]);
+                part[(b + NX) * 32 + lane] = fma(g1, 1.0 - tx, part[(b + NX) * 32 + lane]);
+                part[(b + NX + 1) * 32 + lane] = fma(g1, tx, part[(b + NX + 1) * 32 + lane]);
+            }
+        }
+        __syncwarp();
     }
-    for (int k = 0; k < kWinParts; ++k) parts[k * nc + c] = part[k][threadIdx.x];
+    if (c0 + lane < nc)
+        for (int k = 0; k < kWinParts; ++k) parts[k * nc + c0 + lane] = part[k * 32 + lane];
     raise_err(d_err, errs);
 }
 
@@ -494,10 +567,10 @@ static uint64_t* adj_inj(jp_particles* P) { return (uint64_t*)((double*)P->adj_r
 cudaError_t launch_move_permutation(jp_particles* P, int32_t* dest)
 {
     const MoveScratch& m = P->move;
-    if (!m.L0) return cudaErrorInvalidValue;
+    if (!m.rec) return cudaErrorInvalidValue;
     const unsigned nb = grid_blocks(P->g.ncells);
-    MoveView S{m.L0, m.L, m.M, m.R, m.U, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, 0};
-    perm_init<<<nb, kThreads, 0, P->stream>>>(P->g, m.L0, m.L, m.R, dest);
+    MoveView S{m.rec, P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, 0};
+    perm_init<<<nb, kThreads, 0, P->stream>>>(P->g, S, dest);
     if (P->g.ndim == 2)
         perm_scatter<2><<<nb, kThreads, 0, P->stream>>>(P->g, S, dest);
     else
@@ -532,13 +605,28 @@ cudaError_t launch_slot_ids(jp_particles* P, const uint8_t* index, double* ids)
 }
 
 cudaError_t launch_inject_vjp(jp_particles* P, const double* ids, const double* const* post, double* const* pre,
-                              int n, int copies)
+                              int n, unsigned copies)
 {
     cudaError_t e = ensure_adjoint_scratch(P);
     if (e != cudaSuccess) return e;
     const unsigned nb = grid_blocks(P->g.ncells);
     if (copies) inject_mask_kernel<<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), P->d_err);
     inject_vjp_kernel<<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), perm_arrays(post, pre, n), copies);
+    return cudaGetLastError();
+}
+
+template <int METHOD>
+static cudaError_t launch_advect_vjp(jp_particles* P, unsigned nb, cudaStream_t st, const double* const V[3],
+                                     const AdjParams& prm, const CCoords& X, const uint8_t* index, const Coords& L)
+{
+    constexpr size_t smem = advect_vjp_smem<METHOD>();
+    static_assert(smem <= 200 * 1024, "advect_vjp_kernel shared memory");
+    // static shared memory comes on top of the dynamic part: always raise the cap
+    cudaError_t e = cudaFuncSetAttribute(advect_vjp_kernel<METHOD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    advect_vjp_kernel<METHOD><<<nb, 32 * kAdjWarps, smem, st>>>(P->g, V[0], V[1], prm, X, index, L, adj_parts(P),
+                                                                 P->d_err);
     return cudaGetLastError();
 }
 
@@ -558,17 +646,15 @@ cudaError_t launch_advection_vjp(jp_particles* P, int method, double alpha, cons
     prm.cb = alpha == 0.5 ? 1.0 : 0.5 * ia;
     CCoords X{{coords[0], coords[1], nullptr}};
     Coords L{{lam[0], lam[1], nullptr}};
-    const unsigned nb = grid_blocks(P->g.ncells, kAdjThreads);
+    const unsigned nb = grid_blocks(P->g.ncells, 32 * kAdjWarps);
     cudaStream_t st = P->stream;
     if (method == JP_RUNGE_KUTTA2)
-        advect_vjp_kernel<JP_RUNGE_KUTTA2><<<nb, kAdjThreads, 0, st>>>(P->g, V[0], V[1], prm, X, index, L,
-                                                                       adj_parts(P), P->d_err);
+        e = launch_advect_vjp<JP_RUNGE_KUTTA2>(P, nb, st, V, prm, X, index, L);
     else if (method == JP_RUNGE_KUTTA4)
-        advect_vjp_kernel<JP_RUNGE_KUTTA4><<<nb, kAdjThreads, 0, st>>>(P->g, V[0], V[1], prm, X, index, L,
-                                                                       adj_parts(P), P->d_err);
+        e = launch_advect_vjp<JP_RUNGE_KUTTA4>(P, nb, st, V, prm, X, index, L);
     else
-        advect_vjp_kernel<JP_EULER><<<nb, kAdjThreads, 0, st>>>(P->g, V[0], V[1], prm, X, index, L, adj_parts(P),
-                                                                P->d_err);
+        e = launch_advect_vjp<JP_EULER>(P, nb, st, V, prm, X, index, L);
+    if (e != cudaSuccess) return e;
     for (int c = 0; c < 2; ++c) {
         const int64_t nn = P->g.nvel[c][0] * P->g.nvel[c][1];
         vel_gather_kernel<<<grid_blocks(nn), kThreads, 0, st>>>(P->g, c, adj_parts(P), gV[c]);

@@ -133,6 +133,41 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
             g.lim_lo[c][d] = x[0];  // inner_limits: first/last (src/Advection/advection.jl:73-81)
             g.lim_hi[c][d] = x[n - 1];
         }
+    // Cell centres (Particles.xci) and their spacing (di.center): the interior
+    // of the ghost-expanded centre grids (src/Particles/particles_utils.jl:56-79,
+    // :108-140). A range stays a range: Julia's LinRange[2:end-1] is
+    // LinRange(r[2], r[end-1], n - 2), whose elements are recomputed from those
+    // end points ((1 - t) a + t b, t = k / (n - 1)); its spacing is element 2
+    // minus element 1. Vector grids are sliced, spacing = diff.
+    size_t off_xc[3], off_dxc[3], off_ixc[3];
+    P->centres_ok = 1;
+    for (int d = 0; d < N; ++d) {
+        const double* v = d == 0 ? grid->xi_vel[1][0] : grid->xi_vel[0][d];
+        const int64_t n = (d == 0 ? grid->n_vel[1][0] : grid->n_vel[0][d]) - 2;
+        if (n != g.n[d] || n < 2) P->centres_ok = 0;
+        const int64_t m = n < 1 ? 1 : n;
+        std::vector<double> xc((size_t)m, 0.0), dxc((size_t)(m > 1 ? m - 1 : 1), 1.0), ixc(dxc.size(), 1.0);
+        for (int64_t k = 0; k < n; ++k) {
+            if (grid->uniform && n > 1) {
+                const double tk = (double)k / (double)(n - 1);
+                xc[k] = (1.0 - tk) * v[1] + tk * v[n];
+            } else {
+                xc[k] = v[k + 1];
+            }
+        }
+        for (int64_t k = 0; k + 1 < n; ++k) {
+            dxc[k] = grid->uniform ? xc[1] - xc[0] : xc[k + 1] - xc[k];
+            ixc[k] = 1.0 / dxc[k];
+        }
+        off_xc[d] = push(xc.data(), (int64_t)xc.size());
+        off_dxc[d] = push(dxc.data(), (int64_t)dxc.size());
+        off_ixc[d] = push(ixc.data(), (int64_t)ixc.size());
+        // grid_size(xvi) of grid2particle_flip!: the smallest vertex spacing (src/Interpolations/utils.jl:61-63)
+        const double* x = grid->xi_vel[d][d];
+        double dm = x[1] - x[0];
+        for (int64_t i = 1; i < g.n[d]; ++i) dm = (x[i + 1] - x[i]) < dm ? (x[i + 1] - x[i]) : dm;
+        g.idmin[d] = 1.0 / std::fabs(dm);
+    }
     // The split-precision form samples velocities in cell units and assumes the
     // standard staggering: component c on the vertices along axis c and on the
     // ghost-expanded cell centres (vertex origin - dx/2 + k*dx) along the others.
@@ -165,6 +200,9 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
         return rc;
     }
     for (int d = 0; d < N; ++d) {
+        g.xc[d] = P->dev_block + off_xc[d];
+        g.dxc[d] = P->dev_block + off_dxc[d];
+        g.ixc[d] = P->dev_block + off_ixc[d];
         g.xv[d] = P->dev_block + off_xv[d];
         g.dxv[d] = P->dev_block + off_dxv[d];
         g.ixv[d] = P->dev_block + off_ixv[d];
@@ -184,7 +222,7 @@ int jp_particles_destroy(jp_particles* P)
     cudaFree(P->dev_block);
     cudaFree(P->d_err);
     if (P->h_err) cudaFreeHost(P->h_err);
-    cudaFree(P->move.L0);  // one allocation holds all move scratch
+    cudaFree(P->move.rec);  // one allocation holds all move scratch
     cudaFree(P->inject.counts);  // counters and lists share one allocation
     cudaFree(P->adj_rec);
     delete P;
@@ -425,7 +463,7 @@ static bool slots_fit_int32(const jp_particles* P)
 int jp_move_permutation(jp_particles* P, int32_t* dest)
 {
     if (!P || !dest) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: null pointer");
-    if (!P->move.L0) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: no move_particles call to replay");
+    if (!P->move.rec) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: no move_particles call to replay");
     if (!slots_fit_int32(P)) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: more than 2^31 slots");
     return finish(P, jp::launch_move_permutation(P, dest), "jp_move_permutation");
 }
@@ -455,7 +493,8 @@ int jp_inject_vjp(jp_particles* P, const double* ids, const double* const* post,
     for (int k = 0; k < n; ++k)
         if (!post[k] || !pre[k] || post[k] == pre[k])
             return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp: null or aliased array");
-    return finish(P, jp::launch_inject_vjp(P, ids, post, pre, n, copies ? 1 : 0), "jp_inject_vjp");
+    return finish(P, jp::launch_inject_vjp(P, ids, post, pre, n, (unsigned)copies & ((1u << n) - 1u)),
+                  "jp_inject_vjp");
 }
 
 int jp_advection_vjp(jp_particles* P, int32_t method, double alpha, const double* const V[3], double dt,
@@ -508,6 +547,34 @@ int jp_grid2particle(jp_particles* P, double* Fp, const double* F, const double*
     if (!P || !Fp || !F || !index || !check_coords(P, (const void* const*)coords))
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_grid2particle: null pointer");
     return finish(P, jp::launch_g2p(P, Fp, F, coords, index), "jp_grid2particle");
+}
+
+int jp_grid2particle_flip(jp_particles* P, double* Fp, const double* F, const double* F0, double alpha,
+                          const double* const coords[3], const uint8_t* index)
+{
+    if (!P || !Fp || !F || !F0 || !index || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "grid2particle_flip!: null pointer");
+    return finish(P, jp::launch_g2p_flip(P, Fp, F, F0, alpha, coords, index), "grid2particle_flip!");
+}
+
+int jp_centroid2particle(jp_particles* P, double* Fp, const double* F, const double* const coords[3])
+{
+    if (!P || !Fp || !F || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "centroid2particle!: null pointer");
+    if (!P->centres_ok)
+        return fail(JP_ERR_INVALID_ARGUMENT,
+                    "centroid2particle!: needs ghost-expanded centre grids with at least 2 cells per axis");
+    return finish(P, jp::launch_c2p(P, Fp, F, coords), "centroid2particle!");
+}
+
+int jp_particle2centroid(jp_particles* P, double* F, const double* Fp, const double* const coords[3])
+{
+    if (!P || !Fp || !F || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "particle2centroid!: null pointer");
+    if (!P->centres_ok)
+        return fail(JP_ERR_INVALID_ARGUMENT,
+                    "particle2centroid!: needs ghost-expanded centre grids with at least 2 cells per axis");
+    return finish(P, jp::launch_p2c(P, F, Fp, coords), "particle2centroid!");
 }
 
 int jp_particle2grid(jp_particles* P, double* F, const double* Fp, const double* const coords[3],

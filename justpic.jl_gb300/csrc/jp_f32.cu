@@ -249,6 +249,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     __shared__ SlotList lists[kWarpsPerBlock];
     __shared__ int cellI[kWarpsPerBlock][32][3];
     __shared__ unsigned long long movers[kWarpsPerBlock][32];
+    constexpr int NT = DIM == 2 ? kTargetMasks2D : 1;
+    __shared__ unsigned long long tmask[kWarpsPerBlock][32][NT];  // 2D: movers per target
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
     if (c0 >= g.ncells) return;
@@ -260,6 +262,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 #pragma unroll
         for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
         movers[w][lane] = 0;
+#pragma unroll
+        for (int k = 0; k < NT; ++k) tmask[w][lane][k] = 0;
     }
     uint64_t L;
     const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &L);
@@ -281,7 +285,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         if (!out) {
 #pragma unroll
             for (int d = 0; d < DIM; ++d) rec[d] = xi[d];
-            S.m.code[a] = kCodeStay;
+            if (DIM == 3) S.m.code[a] = kCodeStay;
             continue;
         }
         atomicOr(&movers[w][l], 1ull << s);
@@ -311,16 +315,23 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
                 code = (uint8_t)nb_code<DIM>(off);
             }
         }
-        S.m.code[a] = code;
+        if (DIM == 2) {
+            if (code != kCodeExit) atomicOr(&tmask[w][l][code], 1ull << s);
+        } else {
+            S.m.code[a] = code;
+        }
     }
     __syncwarp();
     const int64_t c = c0 + lane;
     if (c < nc) {
-        S.m.L0[c] = L;
-        S.m.L[c] = L;
-        S.m.M[c] = movers[w][lane];
-        S.m.R[c] = 0;
-        S.m.U[c] = 0;
+        S.m.L(c) = L;
+        S.m.R(c) = 0;
+        S.m.U(c) = 0;
+        S.m.L0(c) = L;
+        S.m.M(c) = movers[w][lane];
+        if (DIM == 2)
+#pragma unroll
+            for (int k = 0; k < NT; ++k) S.m.T(c, k) = tmask[w][lane][k];
     }
     raise_err(d_err, errs);
 }
@@ -334,9 +345,9 @@ __global__ void __launch_bounds__(kThreads)
     const bool valid = c < nc;
     uint64_t L0 = 0, L = 0, R = 0;
     if (valid) {
-        L0 = S.m.L0[c];
-        L = S.m.L[c];
-        R = S.m.R[c];
+        L0 = S.m.L0(c);
+        L = S.m.L(c);
+        R = S.m.R(c);
     }
     const uint64_t changed = (L0 & ~L) | R;
     const uint32_t hi_any = __reduce_max_sync(0xffffffffu, changed ? 64u - (uint32_t)__clzll((long long)changed) : 0u);
@@ -801,25 +812,19 @@ cudaError_t launch_move_f32(jp_particles* P, float* const xi[3], uint8_t* index,
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
     const MoveScratch& m = P->move;
     MoveViewF S;
-    S.m = MoveView{m.L0, m.L, m.M, m.R, m.U, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, N + nargs};
+    S.m = MoveView{m.rec, P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, N + nargs};
     S.shadow = (float*)m.shadow;
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(P->g.ncells);
     const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
     const int ntw = 32 * kWarpsPerBlock;
-    int64_t mc[3] = {1, 1, 1};
-    for (int d = 0; d < N; ++d) mc[d] = (P->g.n[d] + 2) / 3;
-    const unsigned nbp = grid_blocks(mc[0] * mc[1] * mc[2], kAllocThreads);
     if (N == 2) {
         move_classify_f32<2><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, P->d_err);
-        for (int pass = 0; pass < 9; ++pass)
-            move_allocate<2><<<nbp, kAllocThreads, 0, st>>>(P->g, S.m, pass / 3, pass % 3, 0, mc[0], mc[1], 1);
+        launch_allocate_passes(P->g, S.m, st);
         move_apply_f32<2><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S);
     } else {
         move_classify_f32<3><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, P->d_err);
-        for (int pass = 0; pass < 27; ++pass)
-            move_allocate<3><<<nbp, kAllocThreads, 0, st>>>(P->g, S.m, pass / 9, (pass / 3) % 3, pass % 3, mc[0],
-                                                            mc[1], mc[2]);
+        launch_allocate_passes(P->g, S.m, st);
         move_apply_f32<3><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S);
     }
     return cudaGetLastError();

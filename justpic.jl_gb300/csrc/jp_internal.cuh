@@ -47,16 +47,16 @@ struct DevGrid {
     int64_t nvel[3][3];
     double dom_lo[3], dom_hi[3];  // extrema of the vertex grid
     double lim_lo[3][3], lim_hi[3][3];  // first/last of every velocity grid
+    const double* xc[3];   // cell centres (Particles.xci), n[d]
+    const double* dxc[3];  // their spacing (di.center) per interval, n[d] - 1
+    const double* ixc[3];  // 1/spacing
+    double idmin[3];       // 1 / smallest vertex spacing per axis (grid_size, the FLIP transfer's di)
 };
 
 // Scratch owned by a container for move_particles! (allocated on first use).
 struct MoveScratch {
-    uint64_t* L0 = nullptr;   // occupancy before the move
-    uint64_t* L = nullptr;    // occupancy, updated by the colour passes
-    uint64_t* M = nullptr;    // movers found by the classify pass
-    uint64_t* R = nullptr;    // slots refilled during this move
-    uint64_t* U = nullptr;    // refilled slots whose particle is not strictly inside
-    uint8_t* code = nullptr;  // destination code per mover slot
+    uint64_t* rec = nullptr;  // the per-cell 64-bit slot mask arrays (layout: MoveView)
+    uint8_t* code = nullptr;  // destination code per mover slot (3D)
     uint16_t* orig = nullptr; // origin tag per refilled slot
     double* shadow = nullptr; // movers' coordinates and fields, per component
     int shadow_comps = 0;
@@ -81,6 +81,7 @@ struct jp_particles {
     uint64_t inject_calls = 0;
     double dx_host[3] = {1.0, 1.0, 1.0};  // spacing per axis (uniform grids) for the split-precision form
     int staggered_std = 0;                // velocity grids have the standard ghost-node staggering
+    int centres_ok = 0;                   // the centre grids have one node per cell and >= 2 nodes per axis
     jp::MoveScratch move;
     jp::InjectScratch inject;
     void* adj_rec = nullptr;  // adjoint records of the last advection VJP
@@ -317,6 +318,11 @@ cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* ind
                           double* const* args, int nargs, uint32_t call);
 cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const double* const coords[3],
                        const uint8_t* index);
+// transfers beside the hot path (jp_transfer.cu)
+cudaError_t launch_g2p_flip(jp_particles* P, double* Fp, const double* F, const double* F0, double alpha,
+                            const double* const coords[3], const uint8_t* index);
+cudaError_t launch_c2p(jp_particles* P, double* Fp, const double* F, const double* const coords[3]);
+cudaError_t launch_p2c(jp_particles* P, double* F, const double* Fp, const double* const coords[3]);
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
                        const uint8_t* index, double* W = nullptr);
 
@@ -326,7 +332,7 @@ cudaError_t launch_permute_vjp(jp_particles* P, const int32_t* dest, const doubl
                                int n);
 cudaError_t launch_slot_ids(jp_particles* P, const uint8_t* index, double* ids);
 cudaError_t launch_inject_vjp(jp_particles* P, const double* ids, const double* const* post, double* const* pre,
-                              int n, int copies);
+                              int n, unsigned copies);
 cudaError_t launch_advection_vjp(jp_particles* P, int method, double alpha, const double* const V[3], double dt,
                                  const double* const coords[3], const uint8_t* index, double* const lam[3],
                                  double* const gV[3]);
@@ -338,6 +344,8 @@ cudaError_t launch_g2p_vjp(jp_particles* P, const double* F, const double* gFp, 
 
 // scratch of move_particles! owned by the container (allocated on first use)
 cudaError_t ensure_move_scratch(jp_particles* P, int comps);
+struct MoveView;
+void launch_allocate_passes(const DevGrid& g, const MoveView& S, cudaStream_t st);
 
 // split-precision form (jp_f32.cu)
 cudaError_t launch_to_offsets(jp_particles* P, const double* const coords[3], const uint8_t* index,

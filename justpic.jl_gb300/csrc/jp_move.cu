@@ -69,6 +69,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     __shared__ long long cellk[kWarpsPerBlock][32][2 * DIM];  // keys of corner and corner + dx
     __shared__ int cellI[kWarpsPerBlock][32][3];
     __shared__ unsigned long long movers[kWarpsPerBlock][32];
+    constexpr int NT = DIM == 2 ? kTargetMasks2D : 1;
+    __shared__ unsigned long long tmask[kWarpsPerBlock][32][NT];  // 2D: movers per target, unstable ones
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
     if (c0 >= g.ncells) return;
@@ -85,6 +87,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             cellI[w][lane][d] = (int)I[d];
         }
         movers[w][lane] = 0;
+#pragma unroll
+        for (int k = 0; k < NT; ++k) tmask[w][lane][k] = 0;
     }
     long long kdlo[3], kdhi[3];
 #pragma unroll
@@ -118,7 +122,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 #pragma unroll
         for (int d = 0; d < DIM; ++d) in = in & (cellk[w][l][d] < kp[d]) & (kp[d] < cellk[w][l][DIM + d]);
         if (in) {  // move_safe.jl:93
-            S.code[a] = kCodeStay;
+            if (DIM == 3) S.code[a] = kCodeStay;
             continue;
         }
         atomicOr(&movers[w][l], 1ull << s);
@@ -145,16 +149,26 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
                 if (!inT) code |= kCodeUnstable;
             }
         }
-        S.code[a] = code;
+        if (DIM == 2) {
+            if (code != kCodeExit) {
+                atomicOr(&tmask[w][l][code & 0x1F], 1ull << s);
+                if (code & kCodeUnstable) atomicOr(&tmask[w][l][NT - 1], 1ull << s);
+            }
+        } else {
+            S.code[a] = code;
+        }
     }
     __syncwarp();
     const int64_t c = c0 + lane;
     if (c < nc) {
-        S.L0[c] = L;
-        S.L[c] = L;
-        S.M[c] = movers[w][lane];
-        S.R[c] = 0;
-        S.U[c] = 0;
+        S.L(c) = L;
+        S.R(c) = 0;
+        S.U(c) = 0;
+        S.L0(c) = L;
+        S.M(c) = movers[w][lane];
+        if (DIM == 2)
+#pragma unroll
+            for (int k = 0; k < NT; ++k) S.T(c, k) = tmask[w][lane][k];
     }
     raise_err(d_err, errs);
 }
@@ -171,9 +185,9 @@ __global__ void __launch_bounds__(kThreads)
     const bool valid = c < nc;
     uint64_t L0 = 0, L = 0, R = 0;
     if (valid) {
-        L0 = S.L0[c];
-        L = S.L[c];
-        R = S.R[c];
+        L0 = S.L0(c);
+        L = S.L(c);
+        R = S.R(c);
     }
     uint64_t changed = (L0 & ~L) | R;
     // slots past the highest changed slot of any lane need no visit
@@ -536,16 +550,17 @@ __global__ void inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Ar
 cudaError_t ensure_move_scratch(jp_particles* P, int comps)
 {
     MoveScratch& m = P->move;
-    if (m.L0 && m.shadow_comps >= comps) return cudaSuccess;
-    if (m.L0) {
+    if (m.rec && m.shadow_comps >= comps) return cudaSuccess;
+    if (m.rec) {
         cudaError_t e = cudaStreamSynchronize(P->stream);
         if (e != cudaSuccess) return e;
-        cudaFree(m.L0);
+        cudaFree(m.rec);
         m = MoveScratch();
     }
     const int64_t nc = P->g.ncells;
     const int64_t ns = nc * P->g.max_xcell;
-    size_t bytes = 5 * nc * sizeof(uint64_t);  // masks first (8-byte aligned)
+    const int rs = P->g.ndim == 2 ? kRecWords2D : kRecWords3D;
+    size_t bytes = (size_t)rs * nc * sizeof(uint64_t);  // mask arrays first (8-byte aligned)
     const size_t off_shadow = bytes;
     bytes += (size_t)comps * ns * sizeof(double);
     const size_t off_orig = bytes;
@@ -555,11 +570,7 @@ cudaError_t ensure_move_scratch(jp_particles* P, int comps)
     char* base = nullptr;
     cudaError_t e = cudaMalloc(&base, bytes);
     if (e != cudaSuccess) return e;
-    m.L0 = (uint64_t*)base;
-    m.L = m.L0 + nc;
-    m.M = m.L + nc;
-    m.R = m.M + nc;
-    m.U = m.R + nc;
+    m.rec = (uint64_t*)base;
     m.shadow = (double*)(base + off_shadow);
     m.orig = (uint16_t*)(base + off_orig);
     m.code = (uint8_t*)(base + off_code);
@@ -579,27 +590,37 @@ cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index
     A.n = nargs;
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
     const MoveScratch& m = P->move;
-    MoveView S{m.L0, m.L, m.M, m.R, m.U, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, N + nargs};
+    MoveView S{m.rec, P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, N + nargs};
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(P->g.ncells);
     const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
     const int ntw = 32 * kWarpsPerBlock;
-    int64_t mc[3] = {1, 1, 1};
-    for (int d = 0; d < N; ++d) mc[d] = (P->g.n[d] + 2) / 3;  // ceil(n/3)
-    const unsigned nbp = grid_blocks(mc[0] * mc[1] * mc[2], kAllocThreads);
     if (N == 2) {
         move_classify<2><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
-        for (int pass = 0; pass < 9; ++pass)  // offsetᵢ outer, offsetⱼ inner (move_safe.jl:32)
-            move_allocate<2><<<nbp, kAllocThreads, 0, st>>>(P->g, S, pass / 3, pass % 3, 0, mc[0], mc[1], 1);
+        launch_allocate_passes(P->g, S, st);
         move_apply<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     } else {
         move_classify<3><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
-        for (int pass = 0; pass < 27; ++pass)  // i outer, k inner (move_safe.jl:39)
-            move_allocate<3><<<nbp, kAllocThreads, 0, st>>>(P->g, S, pass / 9, (pass / 3) % 3, pass % 3, mc[0],
-                                                            mc[1], mc[2]);
+        launch_allocate_passes(P->g, S, st);
         move_apply<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     }
     return cudaGetLastError();
+}
+
+// the 3^N colour passes of the allocate stage, in the reference's order
+void launch_allocate_passes(const DevGrid& g, const MoveView& S, cudaStream_t st)
+{
+    int64_t mc[3] = {1, 1, 1};
+    for (int d = 0; d < g.ndim; ++d) mc[d] = (g.n[d] + 2) / 3;  // ceil(n/3)
+    const unsigned nbp = grid_blocks(mc[0] * mc[1] * mc[2], kAllocThreads);
+    if (g.ndim == 2) {
+        for (int pass = 0; pass < 9; ++pass)  // offsetᵢ outer, offsetⱼ inner (move_safe.jl:32)
+            move_allocate_2d<<<nbp, kAllocThreads, 0, st>>>(g, S, pass / 3, pass % 3, mc[0], mc[1]);
+    } else {
+        for (int pass = 0; pass < 27; ++pass)  // i outer, k inner (move_safe.jl:39)
+            move_allocate<3><<<nbp, kAllocThreads, 0, st>>>(g, S, pass / 9, (pass / 3) % 3, pass % 3, mc[0],
+                                                            mc[1], mc[2]);
+    }
 }
 
 cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
@@ -684,7 +705,8 @@ size_t move_scratch_bytes(const DevGrid& g, int comps)
 {
     const size_t nc = (size_t)g.ncells;
     const size_t ns = nc * (size_t)g.max_xcell;
-    return 5 * nc * sizeof(uint64_t) + (size_t)comps * ns * sizeof(double) + ns * sizeof(uint16_t) + ns;
+    const size_t rs = g.ndim == 2 ? kRecWords2D : kRecWords3D;
+    return rs * nc * sizeof(uint64_t) + (size_t)comps * ns * sizeof(double) + ns * sizeof(uint16_t) + ns;
 }
 
 // Host code may not use g_move_scratch's name as a device address: it stands
@@ -719,12 +741,9 @@ cudaError_t launch_move_noalloc(jp_particles* P, double* const coords[3], uint8_
     const int64_t ns = nc * P->g.max_xcell;
     char* base = (char*)scratch;
     MoveView S;
-    S.L0 = (uint64_t*)base;
-    S.L = S.L0 + nc;
-    S.M = S.L + nc;
-    S.R = S.M + nc;
-    S.U = S.R + nc;
-    S.shadow = (double*)(base + 5 * nc * sizeof(uint64_t));
+    S.rec = (uint64_t*)base;
+    S.nc = nc;
+    S.shadow = (double*)(base + (size_t)(N == 2 ? kRecWords2D : kRecWords3D) * nc * sizeof(uint64_t));
     S.orig = (uint16_t*)((char*)S.shadow + (size_t)(N + nargs) * ns * sizeof(double));
     S.code = (uint8_t*)((char*)S.orig + ns * sizeof(uint16_t));
     S.nslots = ns;
@@ -737,19 +756,13 @@ cudaError_t launch_move_noalloc(jp_particles* P, double* const coords[3], uint8_
     const unsigned nb = grid_blocks(nc);
     const unsigned nbw = grid_blocks(nc, 32 * kWarpsPerBlock);
     const int ntw = 32 * kWarpsPerBlock;
-    int64_t mc[3] = {1, 1, 1};
-    for (int d = 0; d < N; ++d) mc[d] = (P->g.n[d] + 2) / 3;
-    const unsigned nbp = grid_blocks(mc[0] * mc[1] * mc[2], kAllocThreads);
     if (N == 2) {
         move_classify<2><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
-        for (int pass = 0; pass < 9; ++pass)
-            move_allocate<2><<<nbp, kAllocThreads, 0, st>>>(P->g, S, pass / 3, pass % 3, 0, mc[0], mc[1], 1);
+        launch_allocate_passes(P->g, S, st);
         move_apply<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     } else {
         move_classify<3><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
-        for (int pass = 0; pass < 27; ++pass)
-            move_allocate<3><<<nbp, kAllocThreads, 0, st>>>(P->g, S, pass / 9, (pass / 3) % 3, pass % 3, mc[0],
-                                                            mc[1], mc[2]);
+        launch_allocate_passes(P->g, S, st);
         move_apply<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     }
     return cudaGetLastError();

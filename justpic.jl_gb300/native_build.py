@@ -19,12 +19,12 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libjustpic_gb300.so")
 
-SOURCES = ["jp_capi.cu", "jp_particles.cu", "jp_move.cu", "jp_f32.cu", "jp_adjoint.cu"]
+SOURCES = ["jp_capi.cu", "jp_particles.cu", "jp_move.cu", "jp_f32.cu", "jp_adjoint.cu", "jp_transfer.cu"]
 HEADERS = ["jp_internal.cuh", "jp_move_core.cuh"]
 PUBLIC_HEADERS = ["justpic_gb300.h", "justpic_gb300_rng.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 

@@ -202,11 +202,20 @@ class Particles:
         check(_native.load().jp_set_rng_counter(self._handle, int(value)))
 
 
-def _center_coordinates(xi_vel):
-    """center_coordinates (src/Particles/particles_utils.jl:55-69)."""
-    if len(xi_vel) == 2:
-        return (xi_vel[1][0][1:-1], xi_vel[0][1][1:-1])
-    return (xi_vel[1][0][1:-1], xi_vel[0][1][1:-1], xi_vel[0][2][1:-1])
+def _center_coordinates(xi_vel, uniform=False):
+    """center_coordinates (src/Particles/particles_utils.jl:55-69): the
+    interior of the ghost-expanded centre grids. A range stays a range
+    (Julia's LinRange[2:end-1] = LinRange(r[2], r[end-1], n - 2), elements
+    recomputed from those end points); vectors are sliced."""
+    src = [xi_vel[1][0], xi_vel[0][1]] + ([xi_vel[0][2]] if len(xi_vel) == 3 else [])
+    out = []
+    for v in src:
+        v = np.asarray(v, dtype=np.float64)
+        if uniform and len(v) > 3:
+            out.append(LinRange(v[1], v[len(v) - 2], len(v) - 2).values)
+        else:
+            out.append(v[1:-1])
+    return tuple(out)
 
 
 def init_particles(backend, nxcell, max_xcell, min_xcell, *xi_vel, seed: int = DEFAULT_SEED) -> Particles:
@@ -251,7 +260,7 @@ def init_particles(backend, nxcell, max_xcell, min_xcell, *xi_vel, seed: int = D
     ni = tuple(int(nc[d]) for d in range(N))
 
     xvi = tuple(host[d][d] for d in range(N))
-    xci = _center_coordinates(host)
+    xci = _center_coordinates(host, uniform)
     if uniform:
         dvert = tuple(x[1] - x[0] for x in xvi)
         dcent = tuple(x[1] - x[0] for x in xci)

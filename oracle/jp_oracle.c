@@ -573,6 +573,149 @@ void jpo_grid2particle(const jpo_grid* g, double* Fp, const double* F,
     }
 }
 
+/* ---------------------------------------------------- grid2particle_flip! */
+
+/*
+ * grid2particle_flip!(Fp, xvi, F, F0, particles; α) with xvi = the vertex grid
+ * (src/Interpolations/grid_to_particle.jl:125-170): per live particle the PIC
+ * values of F and F0 at its position, then the blend
+ * muladd(F_pic, α, (Fp + (F_pic - F0_pic)) * (1 - α)). The spacing is
+ * grid_size(xvi) (src/Interpolations/utils.jl:61-63): the smallest vertex
+ * spacing of each axis, used for every cell.
+ */
+void jpo_grid2particle_flip(const jpo_grid* g, double* Fp, const double* F, const double* F0, double alpha,
+                            const double* const coords[3], const uint8_t* index)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int64_t V0 = g->n[0] + 1, V1 = g->n[1] + 1;
+    double di[3];
+    for (int d = 0; d < N; ++d) {
+        double m = g->xv[d][1] - g->xv[d][0];
+        for (int64_t i = 1; i < g->n[d]; ++i) {
+            const double s = g->xv[d][i + 1] - g->xv[d][i];
+            m = s < m ? s : m;
+        }
+        di[d] = fabs(m);
+    }
+    const double beta = 1.0 - alpha;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t c = 0; c < nc; ++c) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        double x0[3], v[8], v0[8];
+        for (int d = 0; d < N; ++d) x0[d] = g->xv[d][I[d]];
+        const int64_t b = I[0] + V0 * (I[1] + (N == 3 ? V1 * I[2] : 0));
+        const int64_t sz = V0 * V1;
+        const int64_t off[8] = {b, b + 1, b + V0, b + V0 + 1, b + sz, b + sz + 1, b + sz + V0, b + sz + V0 + 1};
+        for (int k = 0; k < (1 << N); ++k) {
+            v[k] = F[off[k]];
+            v0[k] = F0[off[k]];
+        }
+        for (int s = 0; s < M; ++s) {
+            const int64_t a = c + nc * s;
+            if (!index[a]) continue;
+            double t[3];
+            for (int d = 0; d < N; ++d) t[d] = (coords[d][a] - x0[d]) * (1.0 / di[d]);
+            const double fpic = lerpN(N, v, t), f0pic = lerpN(N, v0, t);
+            const double flip = Fp[a] + (fpic - f0pic);
+            Fp[a] = fma(fpic, alpha, flip * beta);
+        }
+    }
+}
+
+/* ------------------------------------------------------- centroid2particle! */
+
+/*
+ * centroid2particle!(Fp, F, particles) (src/Interpolations/centroid_to_particle.jl:13-46):
+ * every slot with non-NaN coordinates (the reference tests the coordinates,
+ * not the index) takes the N-linear interpolation of the cell-centred field F
+ * from the centre cell below it along each axis (its own cell's centre, or the
+ * previous one if the particle lies below that centre), clamped to the
+ * centre grid, with the centre spacing of Particles.di.center.
+ */
+void jpo_centroid2particle(const jpo_grid* g, double* Fp, const double* F, const double* const coords[3])
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int64_t C0 = g->n[0], C1 = g->n[1];
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t c = 0; c < nc; ++c) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        for (int s = 0; s < M; ++s) {
+            const int64_t a = c + nc * s;
+            double p[3];
+            int nan = 0;
+            for (int d = 0; d < N; ++d) {
+                p[d] = coords[d][a];
+                nan |= isnan(p[d]);
+            }
+            if (nan) continue;
+            int64_t J[3] = {0, 0, 0};
+            double t[3];
+            for (int d = 0; d < N; ++d) {
+                int64_t j = p[d] < g->xc[d][I[d]] ? I[d] - 1 : I[d];  /* shifted_index */
+                const int64_t hi = g->n[d] - 2;                        /* clamp to 1..size(F)-1 (1-based) */
+                j = j < 0 ? 0 : (j > hi ? hi : j);
+                J[d] = j;
+                t[d] = (p[d] - g->xc[d][j]) * (1.0 / g->dxc[d][j]);
+            }
+            const int64_t b = J[0] + C0 * (J[1] + (N == 3 ? C1 * J[2] : 0));
+            const int64_t sz = C0 * C1;
+            double v[8];
+            const int64_t off[8] = {b, b + 1, b + C0, b + C0 + 1, b + sz, b + sz + 1, b + sz + C0, b + sz + C0 + 1};
+            for (int k = 0; k < (1 << N); ++k) v[k] = F[off[k]];
+            Fp[a] = lerpN(N, v, t);
+        }
+    }
+}
+
+/* ------------------------------------------------------- particle2centroid! */
+
+/*
+ * particle2centroid!(F, Fp, particles) (src/Interpolations/particle_to_grid_centroid.jl:10-45 2D,
+ * :88-110 3D): per cell, the bilinear-weight average of its own particles'
+ * values at the cell centre, weight prod_d muladd(-|xc_d - p_d|, inv(dx_d), 1)
+ * (bilinear_weight, src/Interpolations/particle_to_grid.jl:210-222) with the
+ * cell's vertex spacing. 2D skips slots with any NaN coordinate, 3D those
+ * whose first coordinate is NaN; 2D divides, 3D multiplies by the inverse.
+ */
+void jpo_particle2centroid(const jpo_grid* g, double* F, const double* Fp, const double* const coords[3])
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t c = 0; c < nc; ++c) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        double xcen[3], dx[3];
+        for (int d = 0; d < N; ++d) {
+            xcen[d] = g->xc[d][I[d]];
+            dx[d] = g->dxv[d][I[d]];
+        }
+        double w = 0.0, wF = 0.0;
+        for (int s = 0; s < M; ++s) {
+            const int64_t a = c + nc * s;
+            double p[3];
+            int skip = 0;
+            for (int d = 0; d < N; ++d) {
+                p[d] = coords[d][a];
+                if (N == 2 || d == 0) skip |= isnan(p[d]);
+            }
+            if (skip) continue;
+            double wi = 1.0;
+            for (int d = 0; d < N; ++d) wi *= fma(-fabs(xcen[d] - p[d]), 1.0 / dx[d], 1.0);
+            w += wi;
+            wF = fma(wi, Fp[a], wF);
+        }
+        F[c] = N == 2 ? wF / w : wF * (1.0 / w);
+    }
+}
+
 /* ---------------------------------------------------------- particle2grid! */
 
 void jpo_particle2grid(const jpo_grid* g, double* F, const double* Fp,

@@ -38,6 +38,8 @@ typedef struct jpo_grid {
     const double* xvel[3][3];  /* velocity grid of component c along dim d */
     const double* dxvel[3][3]; /* its spacing per interval, length nvel - 1 */
     int64_t nvel[3][3];
+    const double* xc[3];     /* cell centres (Particles.xci), length n[d] */
+    const double* dxc[3];    /* their spacing (Particles.di.center) per interval, length n[d] - 1 */
 } jpo_grid;
 
 /* error bits returned by the mutating calls (0 = clean) */
@@ -73,6 +75,25 @@ void jpo_grid2particle(const jpo_grid* g, double* Fp, const double* F,
 /* particle2grid!: src/Interpolations/particle_to_grid.jl:23-151 */
 void jpo_particle2grid(const jpo_grid* g, double* F, const double* Fp,
                        const double* const coords[3], const uint8_t* index);
+
+/* grid2particle_flip!: src/Interpolations/grid_to_particle.jl:125-170 */
+void jpo_grid2particle_flip(const jpo_grid* g, double* Fp, const double* F, const double* F0, double alpha,
+                            const double* const coords[3], const uint8_t* index);
+
+/* centroid2particle!: src/Interpolations/centroid_to_particle.jl:13-46; F is a cell-centred field
+   (n[0] x n[1] (x n[2])) */
+void jpo_centroid2particle(const jpo_grid* g, double* Fp, const double* F, const double* const coords[3]);
+
+/* particle2centroid!: src/Interpolations/particle_to_grid_centroid.jl:10-45, :88-110 */
+void jpo_particle2centroid(const jpo_grid* g, double* F, const double* Fp, const double* const coords[3]);
+
+/* forward-mode derivatives (jp_oracle_jvp.c): the same calls on (value,
+   tangent) pairs; dV / dFp may be NULL (zero tangent) */
+int jpo_advection_jvp(const jpo_grid* g, int method, double alpha, const double* const V[3],
+                      const double* const dV[3], double dt, double* const coords[3], double* const dcoords[3],
+                      const uint8_t* index);
+void jpo_particle2grid_jvp(const jpo_grid* g, double* F, double* dF, const double* Fp, const double* dFp,
+                           const double* const coords[3], const double* const dcoords[3], const uint8_t* index);
 
 /* known-answer helpers (test/test_integrators.jl, test_interpolation_kernels.jl) */
 void jpo_first_stage(int method, double alpha, double dt, int n, const double* v,

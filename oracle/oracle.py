@@ -43,13 +43,16 @@ class _Grid(ctypes.Structure):
         ("xvel", (_dp * 3) * 3),
         ("dxvel", (_dp * 3) * 3),
         ("nvel", (ctypes.c_int64 * 3) * 3),
+        ("xc", _dp * 3),
+        ("dxc", _dp * 3),
     ]
 
 
 def build(force: bool = False) -> str:
     """Compile the oracle shared library with its Makefile (gcc, OpenMP)."""
-    src = os.path.join(_HERE, "jp_oracle.c")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("jp_oracle.c", "jp_oracle_jvp.c", "jp_oracle.h")]
+    if force or not os.path.exists(_LIB_PATH) or \
+            os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(s) for s in srcs):
         subprocess.run(["make", "-s", "-C", _HERE, "-B" if force else "all"], check=True)
     return _LIB_PATH
 
@@ -74,6 +77,15 @@ def lib():
         L.jpo_inject_particles.restype = ctypes.c_int
         L.jpo_grid2particle.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]
         L.jpo_particle2grid.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]
+        L.jpo_grid2particle_flip.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                                             P3, ctypes.c_void_p]
+        L.jpo_centroid2particle.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3]
+        L.jpo_particle2centroid.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3]
+        L.jpo_advection_jvp.argtypes = [G, ctypes.c_int, ctypes.c_double, P3, P3, ctypes.c_double, P3, P3,
+                                        ctypes.c_void_p]
+        L.jpo_advection_jvp.restype = ctypes.c_int
+        L.jpo_particle2grid_jvp.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            P3, P3, ctypes.c_void_p]
         L.jpo_first_stage.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                       _dp, _dp, _dp]
         L.jpo_second_stage.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp, _dp]
@@ -100,6 +112,32 @@ def _ptr(a: np.ndarray):
 
 def _dptr(a: np.ndarray):
     return a.ctypes.data_as(_dp)
+
+
+def _centres(xi_vel, uniform: bool):
+    """Particles.xci and di.center (src/Particles/particles_utils.jl:56-79,
+    :108-140): the interior of the ghost-expanded centre grids
+    xi_vel[1][0], xi_vel[0][1] (, xi_vel[0][2]). A range keeps being a range:
+    Julia's LinRange[2:end-1] is LinRange(r[2], r[end-1], n - 2), whose
+    elements are recomputed from those end points; its spacing is one number,
+    element 2 minus element 1. Vectors are sliced; spacing = diff."""
+    N = len(xi_vel)
+    src = [xi_vel[1][0], xi_vel[0][1]] + ([xi_vel[0][2]] if N == 3 else [])
+    xc, dxc = [], []
+    for v in src:
+        v = np.asarray(v, dtype=np.float64)
+        n = len(v) - 2
+        if uniform:
+            j = np.arange(n, dtype=np.float64)
+            t = j / float(n - 1) if n > 1 else np.zeros(1)
+            x = (1.0 - t) * v[1] + t * v[n]
+            d = np.full(max(n - 1, 1), x[1] - x[0] if n > 1 else 0.0)
+        else:
+            x = np.ascontiguousarray(v[1:-1])
+            d = np.ascontiguousarray(np.diff(x)) if n > 1 else np.zeros(1)
+        xc.append(np.ascontiguousarray(x))
+        dxc.append(np.ascontiguousarray(d))
+    return tuple(xc), tuple(dxc)
 
 
 def _spacing(x: np.ndarray, uniform: bool) -> np.ndarray:
@@ -131,6 +169,7 @@ class OracleParticles:
         self.uniform = bool(uniform)
         self.dxv = tuple(_spacing(x, uniform) for x in self.xvi)
         self.dxvel = tuple(tuple(_spacing(x, uniform) for x in comp) for comp in self.xi_vel)
+        self.xc, self.dxc = _centres(self.xi_vel, uniform)
         g = _Grid()
         g.ndim = ndim
         for d in range(3):
@@ -146,6 +185,8 @@ class OracleParticles:
                 g.xvel[c][d] = _dptr(self.xi_vel[c][d])
                 g.dxvel[c][d] = _dptr(self.dxvel[c][d])
                 g.nvel[c][d] = len(self.xi_vel[c][d])
+            g.xc[d] = _dptr(self.xc[d])
+            g.dxc[d] = _dptr(self.dxc[d])
         self._g = g
         shape = (self.max_xcell, self.ncells)
         self.coords = tuple(np.full(shape, np.nan) for _ in range(ndim))
@@ -197,6 +238,39 @@ class OracleParticles:
     def particle2grid(self, F, Fp):
         assert F.flags.f_contiguous and F.dtype == np.float64
         lib().jpo_particle2grid(ctypes.byref(self._g), _ptr(F), _ptr(Fp), self._p3(self.coords), _ptr(self.index))
+
+    # -- the adjacent transfers -------------------------------------------
+    def grid2particle_flip(self, Fp, F, F0, alpha=0.0):
+        F = np.asfortranarray(F, dtype=np.float64)
+        F0 = np.asfortranarray(F0, dtype=np.float64)
+        lib().jpo_grid2particle_flip(ctypes.byref(self._g), _ptr(Fp), _ptr(F), _ptr(F0), float(alpha),
+                                     self._p3(self.coords), _ptr(self.index))
+
+    def centroid2particle(self, Fp, F):
+        F = np.asfortranarray(F, dtype=np.float64)
+        lib().jpo_centroid2particle(ctypes.byref(self._g), _ptr(Fp), _ptr(F), self._p3(self.coords))
+
+    def particle2centroid(self, F, Fp):
+        assert F.flags.f_contiguous and F.dtype == np.float64
+        lib().jpo_particle2centroid(ctypes.byref(self._g), _ptr(F), _ptr(Fp), self._p3(self.coords))
+
+    # -- forward-mode derivatives (dual numbers through the same code) ----
+    def advection_jvp(self, method, alpha, V, dV, dt, dcoords):
+        """advection! on (value, tangent) pairs: coords advance exactly as in
+        ``advection``; ``dcoords`` (per-slot arrays) carry the tangent for a
+        velocity tangent ``dV`` (grid fields like V, or None)."""
+        V = [np.asfortranarray(v, dtype=np.float64) for v in V]
+        dV = [np.asfortranarray(v, dtype=np.float64) for v in dV] if dV is not None else None
+        self._keep = (V, dV)
+        return lib().jpo_advection_jvp(ctypes.byref(self._g), int(method), float(alpha), self._p3(V),
+                                       self._p3(dV if dV is not None else []), float(dt),
+                                       self._p3(self.coords), self._p3(dcoords), _ptr(self.index))
+
+    def particle2grid_jvp(self, F, dF, Fp, dFp, dcoords):
+        """particle2grid! and its tangent dF for tangents dFp (or None) and dcoords."""
+        assert F.flags.f_contiguous and dF.flags.f_contiguous
+        lib().jpo_particle2grid_jvp(ctypes.byref(self._g), _ptr(F), _ptr(dF), _ptr(Fp), _ptr(dFp),
+                                    self._p3(self.coords), self._p3(dcoords), _ptr(self.index))
 
 
 # -- known-answer helpers (test/test_integrators.jl, test_interpolation_kernels.jl)

@@ -1,14 +1,17 @@
 """Adjoint of the FP64 path (2D) against central finite differences of the
-forward path, on small seeded cases.
+forward path and against forward-mode derivatives (dual numbers) through
+the CPU oracle.
 
 The forward path is bit-identical to the CPU oracle (test_gpu_parity.py), and
 test_fd_is_oracle_fd checks that on the perturbed runs too, so every finite
 difference below is also a finite difference through the oracle.
 
-Tolerance: relative 1e-6 of the finite difference, with a floor of 1e-6 of
-the largest checked gradient (nodes no particle reaches have a zero
-gradient on both sides). Finite differences are formed per particle / per
-vertex before any reduction, so their round-off stays far below it.
+Tolerances: finite differences, relative 1e-6 of the difference with a floor
+of 1e-6 of the largest checked gradient (nodes no particle reaches have a
+zero gradient on both sides); differences are formed per particle / per
+vertex before any reduction, so their round-off stays below it. Dual numbers
+through the oracle carry no truncation or cancellation error, so the adjoint
+must match them to 1e-9 relative (floor: 1e-9 of the largest gradient).
 """
 import numpy as np
 import pytest
@@ -274,6 +277,9 @@ def test_inject_ids_name_the_sources():
     pre_x, pre_t = torch.empty_like(post), torch.empty_like(post)
     A.inject_vjp_(p, ids, [post], [pre_x], copies=False)
     A.inject_vjp_(p, ids, [post], [pre_t], copies=True)
+    both = [torch.empty_like(post), torch.empty_like(post)]
+    A.inject_vjp_(p, ids, [post, post], both, copies=(False, True))  # one call, per-array flags
+    assert torch.equal(both[0], pre_x) and torch.equal(both[1], pre_t)
     pn = post.cpu().numpy()
     ref_x = np.where(live0, pn, 0.0)
     assert np.array_equal(pre_x.cpu().numpy(), ref_x)
@@ -397,3 +403,91 @@ def test_fd_is_oracle_fd():
     pair.assert_same("perturbed run")
     Fo, Fg = pair.p2g(0)
     assert np.array_equal(np.nan_to_num(Fo, nan=-7.0), np.nan_to_num(Fg, nan=-7.0))
+
+
+# --------------------------------------------- forward mode through the oracle
+def oracle_jvp_run(g, Vh, dV, dt, nsteps, T0_grid, target, dT0=None, method=O.RK2, alpha=0.5,
+                   nxcell=16, max_xcell=32, min_xcell=8, seed=0x4A50):
+    """dL along (dV, dT0) by dual numbers through the oracle: the tangents of
+    positions and of T ride along as particle fields through move and inject
+    (an injected particle copies T and its tangent; its position tangent is 0)."""
+    o = O.OracleParticles(tuple(tuple(np.asarray(x, dtype=np.float64) for x in c) for c in g["grid_v"]),
+                          nxcell, max_xcell, min_xcell, seed=seed)
+    o.init_particles()
+    T = o.cell_array()
+    o.grid2particle(T, T0_grid)
+    dT = o.cell_array() if dT0 is None else dT0.copy()
+    dX = [o.cell_array() for _ in range(2)]
+    for _ in range(nsteps):
+        o.advection_jvp(method, alpha, Vh, dV, dt, dX)
+        o.move_particles([T, dT, dX[0], dX[1]])
+        before = o.index.copy()
+        o.inject_particles([T, dT, dX[0], dX[1]])
+        new = o.index.astype(bool) & ~before.astype(bool)
+        for d in range(2):
+            dX[d][new] = 0.0
+    shape = tuple(n + 1 for n in o.n)
+    F = np.asfortranarray(np.zeros(shape))
+    dF = np.asfortranarray(np.zeros(shape))
+    o.particle2grid_jvp(F, dF, T, dT, dX)
+    ok = np.isfinite(F)
+    return float(np.sum(np.where(ok, (F - target) * dF, 0.0))), o
+
+
+@pytest.mark.parametrize("method,nsteps", [("rk2", 20), ("rk4", 10), ("euler", 10)])
+def test_misfit_gradient_matches_oracle_jvp(method, nsteps):
+    g, p, Vh, V, dt, T0, target, _ = _run_case(ni=(32, 32), nsteps=nsteps)
+    om, pm, alpha = METHODS[method]
+    loss, gV, gT0 = A.misfit_gradient(p, pm, V, dt, nsteps, T0, target, checkpoint_every=4)
+    Tg = W.gaussian_T(g)
+    tgt = target.cpu().numpy()
+    rng = np.random.default_rng(6)
+    gmax = max(float(v.abs().max()) for v in gV)
+    adj, jvp = [], []
+    for c in range(2):
+        gc = gV[c].cpu().numpy()
+        big = np.argsort(-np.abs(gc.reshape(-1, order="F")))[:32]
+        nodes = [np.unravel_index(f, gc.shape, order="F") for f in rng.choice(big, 3, replace=False)]
+        nodes += _pick_nodes(gc.shape, 2, rng)
+        for node in nodes:
+            dV = [np.zeros_like(v) for v in Vh]
+            dV[c][node] = 1.0
+            d, _ = oracle_jvp_run(g, Vh, dV, dt, nsteps, Tg, tgt, method=om, alpha=alpha)
+            jvp.append(d)
+            adj.append(gc[node])
+    adj, jvp = np.array(adj), np.array(jvp)
+    err = np.abs(adj - jvp)
+    assert np.all(err <= 1e-9 * np.maximum(np.abs(jvp), gmax)), f"dL/dV vs oracle JVP: {adj} {jvp}"
+    # initial particle field: dL/dT0 along single slots
+    live = p.index.numpy().astype(bool)
+    slots = np.argwhere(live)
+    g0 = gT0.numpy()
+    for s, cc in slots[rng.choice(len(slots), 4, replace=False)]:
+        dT0 = np.zeros(live.shape)
+        dT0[s, cc] = 1.0
+        d, _ = oracle_jvp_run(g, Vh, None, dt, nsteps, Tg, tgt, dT0=dT0, method=om, alpha=alpha)
+        assert abs(g0[s, cc] - d) <= 1e-10 * max(abs(d), float(np.max(np.abs(g0)))), (s, cc, g0[s, cc], d)
+
+
+def test_c5_gradient_matches_oracle_jvp():
+    """The C5 adjoint run at full size (512^2 cells, 16 particles per cell,
+    RK2, 100 steps, checkpoints every 10) against dual numbers through the
+    oracle on the velocity nodes of largest gradient (about a minute of host
+    time per node)."""
+    cfg = W.setup("C5")
+    g, Vh, dt = cfg["grid"], cfg["V"], cfg["dt"]
+    p = jp.init_particles(jp.CUDABackend, cfg["nxcell"], cfg["max_xcell"], cfg["min_xcell"], *g["grid_v"])
+    (T0,) = jp.init_cell_arrays(p, 1)
+    jp.grid2particle_(T0, jp.TA("CUDA")(cfg["T"]), p)
+    target = jp.TA("CUDA")(cfg["T_target"])
+    loss, gV, gT0 = A.misfit_gradient(p, jp.RungeKutta2(), _dev(Vh), dt, cfg["steps"], T0, target,
+                                      checkpoint_every=cfg["checkpoint_every"])
+    gmax = max(float(v.abs().max()) for v in gV)
+    for c in range(2):
+        gc = gV[c].cpu().numpy()
+        node = np.unravel_index(int(np.argmax(np.abs(gc))), gc.shape)
+        dV = [np.zeros_like(v) for v in Vh]
+        dV[c][node] = 1.0
+        d, _ = oracle_jvp_run(g, Vh, dV, dt, cfg["steps"], cfg["T"], cfg["T_target"], nxcell=cfg["nxcell"],
+                              max_xcell=cfg["max_xcell"], min_xcell=cfg["min_xcell"])
+        assert abs(gc[node] - d) <= 1e-9 * max(abs(d), gmax), (c, node, gc[node], d)

@@ -114,6 +114,47 @@ def test_g2p_linear_field_and_p2g_error(ndim):
     assert np.linalg.norm(T2 - T) / T.size < 0.1
 
 
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_flip_and_centroid_transfers_linear_fields(ndim):
+    """test_interpolation_kernels.jl:96-115 (2D), :163-180 (3D): FLIP with
+    T0 = T keeps the PIC values; a linear centroid field interpolates exactly
+    (2D: checked on cell (2, 2), 3D: everywhere); particle2centroid! error
+    below 0.1."""
+    g = W.grid((4,) * ndim)
+    P = _oracle_particles(g, 5 if ndim == 2 else 12, 5 if ndim == 2 else 12, 1)
+    axis = ndim - 1
+    T = W.linear_T(g, axis)
+    pT = P.cell_array()
+    P.grid2particle(pT, T)
+    live = P.index.astype(bool)
+    assert live.all()  # nxcell rounds up to max_xcell: every slot holds a particle
+    P.grid2particle_flip(pT, T, T.copy(order="F"))
+    np.testing.assert_allclose(pT, P.coords[axis], rtol=1e-12)
+    Tc = W.on_grid(lambda *x: x[axis] + 0.0 * x[0], g["xc"])
+    P.centroid2particle(pT, Tc)
+    if ndim == 2:
+        c = 1 + 4 * 1  # cell (2, 2) of the 1-based reference test
+        np.testing.assert_allclose(pT[:, c], P.coords[axis][:, c], rtol=1e-12)
+    else:
+        np.testing.assert_allclose(pT, P.coords[axis], rtol=1e-12)
+    Tc2 = np.asfortranarray(np.zeros_like(Tc))
+    P.particle2centroid(Tc2, pT)
+    assert np.linalg.norm(Tc2 - Tc) / Tc.size < 0.1
+
+
+def test_flip_blend_arithmetic():
+    """grid_to_particle.jl:163-168: Fp = muladd(F_pic, a, (Fp + F_pic - F0_pic) (1 - a))."""
+    g = W.grid((3, 3))
+    P = _oracle_particles(g, 4, 4, 1)
+    T = W.linear_T(g, 0)
+    T0 = np.asfortranarray(0.5 * T)
+    pT = P.cell_array(0.25)
+    P.grid2particle_flip(pT, T, T0, alpha=0.3)
+    x = P.coords[0]
+    pic, pic0 = x, 0.5 * x  # linear fields interpolate exactly (to rounding)
+    np.testing.assert_allclose(pT, 0.3 * pic + (0.25 + pic - pic0) * 0.7, rtol=1e-12)
+
+
 def test_init_particles_layout():
     g = W.grid((6, 5))
     P = _oracle_particles(g, 24, 48, 12)
