@@ -565,6 +565,27 @@ def run_adjoint(args):
 
     fwd = lambda: A.forward_field(p, method, V, dt, nsteps, T0)  # noqa: E731
     grad = lambda: A.misfit_gradient(p, method, V, dt, nsteps, T0, target, checkpoint_every=k)  # noqa: E731
+    if args.form == "f32":  # the split-precision variant on the same run
+        xi = jp.init_offsets(p)
+        V32 = tuple(v.float() for v in V)
+        T0f = jp.CellArray(T0.data.float().contiguous(), p.ni)
+        tgt32 = target.float()
+
+        def fwd():
+            st = A._save_f32(p, xi)
+            T = jp.CellArray(T0f.data.clone(), p.ni)
+            try:
+                for _ in range(nsteps):
+                    jp.advection_f32_(p, xi, method, V32, dt)
+                    jp.move_particles_f32_(p, xi, (T,))
+                    jp.inject_particles_f32_(p, xi, (T,))
+                F = jp.grid_field_f32(tuple(n + 1 for n in p.ni))
+                jp.particle2grid_f32_(F, T, p, xi)
+            finally:
+                A._restore_f32(p, xi, st)
+
+        grad = lambda: A.misfit_gradient_f32(p, xi, method, V32, dt, nsteps, T0f, tgt32,  # noqa: E731
+                                             checkpoint_every=k)
     for _ in range(max(1, min(args.warmup, 3))):
         fwd()
         grad()
@@ -576,7 +597,7 @@ def run_adjoint(args):
     h = 1e-6
     Vh = cfg["V"]
     gmax = max(float(gv.abs().max()) for gv in gV)
-    for n in range(args.fd_nodes):
+    for n in range(args.fd_nodes if args.form == "f64" else 0):
         # even n: any node; odd n: a node where |dL/dV| is at least 1e-3 of its maximum
         c = (n // 2) % 2
         gc = gV[c].cpu().numpy()
@@ -605,6 +626,7 @@ def run_adjoint(args):
             "pairs_adjoint_fd": [[float(a), float(f)] for a, f in checked[:8]],
         })
     print(json.dumps({
+        "form": "split precision (FP32 offsets, FP64 cotangents)" if args.form == "f32" else "FP64",
         "workload": DESC["C5"] if args.ni is None else DESC["C5"] + f" (resized to {args.ni})",
         "live_particles": live, "steps": nsteps, "checkpoint_every": k, "loss": loss,
         "forward_s": t_fwd, "forward_plus_gradient_s": t_grad, "gradient_cost_vs_forward": t_grad / t_fwd,

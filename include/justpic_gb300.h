@@ -180,6 +180,18 @@ int jp_particle2grid(jp_particles* p, double* F, const double* Fp, const double*
  */
 int jp_grid2particle_flip(jp_particles* p, double* Fp, const double* F, const double* F0, double alpha,
                           const double* const coords[3], const uint8_t* index);
+
+/*
+ * update_phase_ratios!(phase_ratios, particles, phases) (src/PhaseRatios/utils.jl:3-40)
+ * without the 3D edge midpoints: for phase ids 1..nphases (<= 16) in the
+ * per-slot field `phases`, the phase fractions at the cell centres (center,
+ * n0 x n1 (x n2) nodes), the vertices (vertex, (n0+1) x ...) and the faces
+ * (faces[d], n + e_d nodes: the reference's Vx, Vy, Vz), each laid out
+ * out[k * nodes + node] like a CellArray of nphases-vectors. NULL skips a
+ * location. Kernels: centers.jl:3-30, vertices.jl:4-107, midpoints.jl:3-94.
+ */
+int jp_phase_ratios(jp_particles* p, int32_t nphases, const double* phases, const double* const coords[3],
+                    double* center, double* vertex, double* const faces[3]);
 int jp_centroid2particle(jp_particles* p, double* Fp, const double* F, const double* const coords[3]);
 int jp_particle2centroid(jp_particles* p, double* F, const double* Fp, const double* const coords[3]);
 
@@ -230,6 +242,29 @@ int jp_particle2grid_vjp(jp_particles* p, const double* F, const double* W, cons
                          double* const gX[3]);
 int jp_grid2particle_vjp(jp_particles* p, const double* F, const double* gFp, const double* const coords[3],
                          const uint8_t* index, double* gF, double* const gX[3]);
+
+/*
+ * Adjoint of the split-precision form (2D; uniform grids with the standard
+ * staggering). Offsets, velocities and fields are the form's FP32 arrays;
+ * cotangents are FP64: lam = dL/d(offset, cell units), gV and gF as above.
+ * jp_advection_vjp_f32 replays jp_advection_f32's stages in FP32 and sweeps
+ * back in FP64, with the FP64 entry's window rule and accumulation order.
+ * jp_particle2grid_f32_with_weights writes the FP64 weight sum of each vertex.
+ * Injection is traced with int32 ids (jp_slot_ids_i32) passed through
+ * jp_inject_particles_f32 as an FP32 field (copied bit for bit) and replayed
+ * by jp_inject_vjp_i32; the move's slot map is jp_move_permutation.
+ */
+int jp_slot_ids_i32(jp_particles* p, const uint8_t* index, int32_t* ids);
+int jp_inject_vjp_i32(jp_particles* p, const int32_t* ids, const double* const* post, double* const* pre,
+                      int32_t n, int32_t copies);
+int jp_advection_vjp_f32(jp_particles* p, int32_t method, double alpha, const float* const V[3], double dt,
+                         const float* const xi[3], const uint8_t* index, double* const lam[3],
+                         double* const gV[3]);
+int jp_particle2grid_f32_with_weights(jp_particles* p, float* F, double* W, const float* Fp,
+                                      const float* const xi[3], const uint8_t* index);
+int jp_particle2grid_vjp_f32(jp_particles* p, const float* F, const double* W, const float* Fp,
+                             const float* const xi[3], const uint8_t* index, const double* gF, double* gFp,
+                             double* const gxi[3]);
 
 /*
  * Split-precision form (no reference counterpart; the scope of this library

@@ -20,6 +20,8 @@ from .api import (  # noqa: F401
     grid2particle_,
     grid2particle_flip_,
     particle2centroid_,
+    PhaseRatios,
+    update_phase_ratios_,
     inject_particles_,
     move_particles_,
     particle2grid_,

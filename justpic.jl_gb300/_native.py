@@ -93,6 +93,8 @@ SIGNATURES = [
     ("jp_grid2particle_flip", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, P3, ctypes.c_void_p]),
     ("jp_centroid2particle", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3]),
+    ("jp_phase_ratios", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("jp_particle2centroid", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3]),
     # adjoint (2D, FP64)
     ("jp_particle2grid_with_weights", ctypes.c_int,
@@ -110,6 +112,17 @@ SIGNATURES = [
       ctypes.c_void_p, ctypes.c_void_p]),
     ("jp_grid2particle_vjp", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    # adjoint of the split-precision form
+    ("jp_slot_ids_i32", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("jp_inject_vjp_i32", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_int32, ctypes.c_int32]),
+    ("jp_advection_vjp_f32", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, P3, ctypes.c_double, P3, ctypes.c_void_p, P3, P3]),
+    ("jp_particle2grid_f32_with_weights", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
+    ("jp_particle2grid_vjp_f32", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_void_p]),
 ]
 
 _lib = None

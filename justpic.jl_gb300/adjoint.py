@@ -465,7 +465,162 @@ class AdvectionStep(torch.autograd.Function):
         return gV[0], gV[1], lam[0], lam[1], None, None, None
 
 
+# ---------------------------------------------- split-precision (FP32) form
+def particle2grid_f32_with_weights_(F: torch.Tensor, W: torch.Tensor, Fp: CellArray, particles: Particles,
+                                    xi) -> None:
+    """particle2grid! of the FP32 form that also writes the FP64 weight sums W."""
+    from .split import _check_xi, _p3 as _p3n
+    xi = _check_xi(particles, xi)
+    _bind_stream(particles)
+    rc = _native.load().jp_particle2grid_f32_with_weights(particles.handle, F.data_ptr(), W.data_ptr(),
+                                                          Fp.data_ptr(), _p3n(xi, particles.ndim),
+                                                          particles.index.data_ptr())
+    _finish(particles, rc, "particle2grid_f32!")
+
+
+def particle2grid_vjp_f32_(gFp: CellArray, gxi, gF: torch.Tensor, F: torch.Tensor, W: torch.Tensor, Fp: CellArray,
+                           particles: Particles, xi, index=None) -> None:
+    """FP32 form: adds dL/dFp to gFp and (if gxi is not None) dL/d(offset) to gxi."""
+    _require_2d(particles)
+    index = index if index is not None else particles.index
+    _bind_stream(particles)
+    rc = _native.load().jp_particle2grid_vjp_f32(particles.handle, F.data_ptr(), W.data_ptr(), Fp.data_ptr(),
+                                                 _p3(xi), index.data_ptr(), gF.data_ptr(), gFp.data_ptr(),
+                                                 _p3(gxi) if gxi is not None else None)
+    _finish(particles, rc, "particle2grid_f32! adjoint")
+
+
+def advection_vjp_f32_(particles: Particles, method: AbstractAdvectionIntegrator, V, dt, xi, index, lam,
+                       gV) -> None:
+    """FP32 form: one advection_f32! step taken from offsets ``xi``; ``lam``
+    (dL/d(offset) after, FP64) becomes dL/d(offset) before; dL/dV is added
+    to ``gV`` (FP64)."""
+    _require_2d(particles)
+    _bind_stream(particles)
+    rc = _native.load().jp_advection_vjp_f32(particles.handle, method.code, float(method.alpha), _p3(V), float(dt),
+                                             _p3(xi), index.data_ptr(), _p3(lam), _p3(gV))
+    _finish(particles, rc, "advection_f32! adjoint")
+
+
+def slot_ids_i32(particles: Particles) -> torch.Tensor:
+    """int32 ids (slot index or -1) to carry through inject_particles_f32! as
+    an FP32 field (``ids.view(torch.float32)``; copied bit for bit)."""
+    ids = torch.empty(tuple(particles.index.data.shape), dtype=torch.int32, device="cuda")
+    _bind_stream(particles)
+    _finish(particles, _native.load().jp_slot_ids_i32(particles.handle, particles.index.data_ptr(),
+                                                      ids.data_ptr()), "slot_ids_i32")
+    return ids
+
+
+def inject_vjp_i32_(particles: Particles, ids: torch.Tensor, post, pre, copies) -> None:
+    _require_2d(particles)
+    post, pre = list(post), list(pre)
+    flags = [bool(copies)] * len(post) if isinstance(copies, bool) else [bool(c) for c in copies]
+    mask = sum(1 << k for k, f in enumerate(flags) if f)
+    _bind_stream(particles)
+    rc = _native.load().jp_inject_vjp_i32(particles.handle, ids.data_ptr(), _ptrs(post), _ptrs(pre), len(post),
+                                          mask)
+    _finish(particles, rc, "inject_particles_f32! adjoint")
+
+
+@dataclass
+class _StateF32:
+    xi: tuple
+    index: torch.Tensor
+    rng: int
+
+
+def _save_f32(p: Particles, xi) -> _StateF32:
+    return _StateF32(tuple(x.data.clone() for x in xi), p.index.data.clone(), p.rng_counter)
+
+
+def _restore_f32(p: Particles, xi, s: _StateF32) -> None:
+    for x, d in zip(xi, s.xi):
+        x.data.copy_(d)
+    p.index.data.copy_(s.index)
+    p.rng_counter = s.rng
+
+
+def _recorded_step_f32(p: Particles, xi, method, V, dt, fields, inject: bool):
+    from .split import advection_f32_, inject_particles_f32_, move_particles_f32_
+    X = tuple(x.data.clone() for x in xi)
+    idx = p.index.data.clone()
+    advection_f32_(p, xi, method, V, dt)
+    move_particles_f32_(p, xi, fields)
+    dest = move_permutation(p)
+    ids = None
+    if inject:
+        ids = slot_ids_i32(p)
+        inject_particles_f32_(p, xi, tuple(fields) + (CellArray(ids.view(torch.float32), p.ni),))
+    return X, idx, dest, ids
+
+
+def misfit_gradient_f32(particles: Particles, xi, method, V, dt, nsteps: int, T0: CellArray, target: torch.Tensor,
+                        checkpoint_every: int = 10, inject: bool = True):
+    """The FP32 (split-precision) variant of misfit_gradient: the run uses the
+    FP32 forward path (offsets ``xi``, FP32 velocities V and particle field
+    T0, FP32 target); cotangents and the returned gradients are FP64. The
+    particles, xi and T0 are not modified. Returns (loss, gV, gT0)."""
+    from .split import advection_f32_, grid_field_f32, inject_particles_f32_, move_particles_f32_
+    _require_2d(particles)
+    k = max(1, int(checkpoint_every))
+    start = _save_f32(particles, xi)
+    T = CellArray(T0.data.clone(), T0.ni)
+    shape = _vertex_shape(particles)
+    try:
+        with _deferred(particles):
+            cps, last = [], []
+            last_seg = ((nsteps - 1) // k) * k if nsteps else 0
+            for n in range(nsteps):
+                if n % k == 0:
+                    cps.append(_save_f32(particles, xi))
+                if n >= last_seg:
+                    last.append(_recorded_step_f32(particles, xi, method, V, dt, (T,), inject))
+                else:
+                    advection_f32_(particles, xi, method, V, dt)
+                    move_particles_f32_(particles, xi, (T,))
+                    if inject:
+                        inject_particles_f32_(particles, xi, (T,))
+            if not cps:
+                cps = [start]
+            F = grid_field_f32(shape)
+            W = grid_field(shape, 0.0)
+            particle2grid_f32_with_weights_(F, W, T, particles, xi)
+            F64 = F.double()
+            loss, gF = misfit(F64, W, target.double())
+            gT = _like(particles)
+            gX = [_like(particles) for _ in range(2)]
+            particle2grid_vjp_f32_(gT, gX, _colmajor(gF), F, W, T, particles, xi)
+            gV = tuple(grid_field(tuple(v.shape), 0.0) for v in V)
+            lam = [c.data.clone() for c in gX]
+            gTd = gT.data.clone()
+            tmp_x = [torch.empty_like(lam[0]) for _ in range(2)]
+            tmp_t = torch.empty_like(gTd)
+            nseg = len(cps)
+            for seg in reversed(range(nseg)):
+                n0 = seg * k
+                n1 = min(n0 + k, nsteps)
+                if seg == nseg - 1 and last:
+                    recs = last
+                else:
+                    _restore_f32(particles, xi, cps[seg])
+                    recs = [_recorded_step_f32(particles, xi, method, V, dt, (), inject) for _ in range(n0, n1)]
+                for X, idx, dest, ids in reversed(recs):
+                    if ids is not None:
+                        inject_vjp_i32_(particles, ids, lam + [gTd], tmp_x + [tmp_t], copies=(False, False, True))
+                        permute_vjp_(particles, dest, tmp_x + [tmp_t], lam + [gTd])
+                    else:
+                        permute_vjp_(particles, dest, lam + [gTd], tmp_x + [tmp_t])
+                        lam, tmp_x = tmp_x, lam
+                        gTd, tmp_t = tmp_t, gTd
+                    advection_vjp_f32_(particles, method, V, dt, X, _Idx(idx), lam, gV)
+    finally:
+        _restore_f32(particles, xi, start)
+    return loss, gV, CellArray(gTd, particles.ni)
+
+
 __all__ = ["particle2grid_with_weights_", "particle2grid_vjp_", "grid2particle_vjp_", "advection_vjp_",
            "move_permutation", "permute_vjp_", "slot_ids", "inject_vjp_", "run_forward", "reverse_sweep",
            "misfit", "misfit_gradient", "misfit_value", "forward_field", "misfit_difference", "PICMisfit", "Grid2Particle", "Particle2Grid",
-           "AdvectionStep"]
+           "AdvectionStep", "particle2grid_f32_with_weights_", "particle2grid_vjp_f32_", "advection_vjp_f32_",
+           "slot_ids_i32", "inject_vjp_i32_", "misfit_gradient_f32"]

@@ -207,3 +207,41 @@ def particle2centroid_(F: torch.Tensor, Fp: CellArray, particles: Particles) -> 
     rc = _native.load().jp_particle2centroid(particles.handle, F.data_ptr(), Fp.data_ptr(), _coords(particles))
     _finish(particles, rc, "particle2centroid!")
 
+
+# ---- phase ratios -------------------------------------------------------------
+class PhaseRatios:
+    """``PhaseRatios`` (src/PhaseRatios/PhaseRatios.jl:12-33, constructors.jl:20-57)
+    for 2D/3D without the 3D edge midpoints: ``center``, ``vertex``, ``Vx``,
+    ``Vy`` (, ``Vz``) are CUDA float64 tensors of shape (nphases, nodes) in the
+    CellArray layout (phase k of node n at n + nodes * k), node index
+    column-major over the location's grid."""
+
+    def __init__(self, nphases: int, ni):
+        ni = tuple(int(n) for n in ni)
+        self.nphases = int(nphases)
+        self.ni = ni
+
+        def alloc(shape):
+            return torch.zeros((self.nphases, int(np.prod(shape))), dtype=torch.float64, device="cuda")
+
+        self.center = alloc(ni)
+        self.vertex = alloc(tuple(n + 1 for n in ni))
+        self.faces = tuple(alloc(tuple(n + (1 if e == d else 0) for e, n in enumerate(ni))) for d in range(len(ni)))
+        self.Vx, self.Vy = self.faces[0], self.faces[1]
+        self.Vz = self.faces[2] if len(ni) == 3 else None
+
+
+def update_phase_ratios_(phase_ratios: PhaseRatios, particles: Particles, phases: CellArray) -> None:
+    """``update_phase_ratios!(phase_ratios, particles, phases)`` (src/PhaseRatios/utils.jl:3-40)
+    without the 3D edge midpoints: the fraction of each phase (ids 1..nphases in
+    the per-slot field ``phases``) at cell centres, vertices and faces."""
+    _check_cellarray(particles, phases, "phases")
+    if phase_ratios.ni != particles.ni:
+        raise ArgumentError("phase_ratios does not match the particles' grid")
+    _bind_stream(particles)
+    faces = P3(*[f.data_ptr() for f in phase_ratios.faces], *([None] * (3 - particles.ndim)))
+    rc = _native.load().jp_phase_ratios(particles.handle, phase_ratios.nphases, phases.data_ptr(),
+                                        _coords(particles), phase_ratios.center.data_ptr(),
+                                        phase_ratios.vertex.data_ptr(), faces)
+    _finish(particles, rc, "update_phase_ratios!")
+

@@ -16,15 +16,16 @@
 // Transpose of the velocity sampling: a particle owned by cell I whose stage
 // points stay within one cell of I deposits only on velocity nodes in a fixed
 // window around I (4 x 5 nodes for Vx, 5 x 4 for Vy on the ghost-node grids).
-// The deposits of a cell's particles are accumulated, in slot order, into 40
-// partial sums per cell by the lane that owns the cell; one thread per
-// velocity node then adds the partial sums of the 20 owning cells whose
-// windows contain it. A stage point outside the window is reported as
-// JP_ERR_ADJOINT_WINDOW.
+// A replay kernel stages each particle's samples per slot; one thread per
+// cell then accumulates its particles' deposits, in slot order, into the
+// cell's 40 partial sums; one thread per velocity node adds the partial sums
+// of the 20 owning cells whose windows contain it. A stage point outside the
+// window is reported as JP_ERR_ADJOINT_WINDOW.
 #include <cmath>
 
 #include <math_constants.h>
 
+#include "jp_f32_core.cuh"
 #include "jp_internal.cuh"
 #include "jp_move_core.cuh"
 
@@ -91,18 +92,34 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------ injection
+template <typename IdT>
 __global__ void __launch_bounds__(kThreads)
-    slot_ids_kernel(int64_t nslots, const uint8_t* __restrict__ index, double* __restrict__ ids)
+    slot_ids_kernel(int64_t nslots, const uint8_t* __restrict__ index, IdT* __restrict__ ids)
 {
     const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= nslots) return;
-    ids[a] = index[a] ? (double)a : -1.0;
+    ids[a] = index[a] ? (IdT)a : (IdT)-1;
 }
 
 // Per cell: the slots whose id names another slot (particles injected by the
-// traced call), after checking that each source lies within reach.
+// traced call), after checking that each source lies within reach; and a flag
+// on every cell holding a source (an order-free atomicOr), so the gather
+// below only scans its window from those cells.
+// ids: a slot's own index when it held a particle before the traced call, the
+// index of the particle its fields were copied from when it was injected, a
+// negative value otherwise; as doubles (FP64 fields) or as int32 (carried bit
+// for bit through an FP32 field).
+__device__ __forceinline__ bool id_other(double id, int64_t a) { return id >= 0.0 && id != (double)a; }
+__device__ __forceinline__ bool id_other(int32_t id, int64_t a) { return id >= 0 && (int64_t)id != a; }
+__device__ __forceinline__ bool id_self(double id, int64_t a) { return id == (double)a; }
+__device__ __forceinline__ bool id_self(int32_t id, int64_t a) { return (int64_t)id == a; }
+__device__ __forceinline__ int64_t id_slot(double id, int64_t ns) { return id < (double)ns ? (int64_t)id : ns; }
+__device__ __forceinline__ int64_t id_slot(int32_t id, int64_t ns) { return (int64_t)id < ns ? (int64_t)id : ns; }
+
+template <typename IdT>
 __global__ void __launch_bounds__(kThreads)
-    inject_mask_kernel(DevGrid g, const double* __restrict__ ids, uint64_t* __restrict__ inj, int* d_err)
+    inject_mask_kernel(DevGrid g, const IdT* __restrict__ ids, uint64_t* __restrict__ inj,
+                       unsigned* __restrict__ srcflag, int* d_err)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncells) return;
@@ -113,16 +130,18 @@ __global__ void __launch_bounds__(kThreads)
     int errs = 0;
     for (int s = 0; s < g.max_xcell; ++s) {
         const int64_t a = c + nc * s;
-        const double id = ids[a];
-        if (id >= 0.0 && id != (double)a) {
-            const int64_t src = id < (double)ns ? (int64_t)id : ns;
+        const IdT id = ids[a];
+        if (id_other(id, a)) {
+            const int64_t src = id_slot(id, ns);
             const int64_t sc = src % nc;
             const int64_t sx = sc % g.n[0], sy = sc / g.n[0];
             if (src >= ns || sx < cx - kInjectReach || sx > cx + kInjectReach || sy < cy - kInjectReach ||
-                sy > cy + kInjectReach)
+                sy > cy + kInjectReach) {
                 errs |= kErrAdjointWindow;
-            else
+            } else {
                 m |= 1ull << s;
+                atomicOr(srcflag + sc, 1u);
+            }
         }
     }
     inj[c] = m;
@@ -133,19 +152,20 @@ __global__ void __launch_bounds__(kThreads)
 // own slot), 0 otherwise; for the arrays k in the `copies` bit mask, a
 // pre-existing slot also collects post[k][b] of every slot b injected from it,
 // cells of the window in order (y outer, x inner), slots ascending.
+template <typename IdT>
 __global__ void __launch_bounds__(kThreads)
-    inject_vjp_kernel(DevGrid g, const double* __restrict__ ids, const uint64_t* __restrict__ inj, PermArrays P,
-                      unsigned copies)
+    inject_vjp_kernel(DevGrid g, const IdT* __restrict__ ids, const uint64_t* __restrict__ inj,
+                      const unsigned* __restrict__ srcflag, PermArrays P, unsigned copies)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncells) return;
     const int64_t nc = g.ncells;
     for (int s = 0; s < g.max_xcell; ++s) {
         const int64_t a = c + nc * s;
-        const bool kept = ids[a] == (double)a;
+        const bool kept = id_self(ids[a], a);
         for (int k = 0; k < P.n; ++k) P.pre[k][a] = kept ? P.post[k][a] : 0.0;
     }
-    if (!copies) return;
+    if (!copies || !srcflag[c]) return;
     const int64_t cx = c % g.n[0], cy = c / g.n[0];
     for (int64_t y = max(cy - kInjectReach, (int64_t)0); y <= min(cy + kInjectReach, g.n[1] - 1); ++y)
         for (int64_t x = max(cx - kInjectReach, (int64_t)0); x <= min(cx + kInjectReach, g.n[0] - 1); ++x) {
@@ -155,7 +175,7 @@ __global__ void __launch_bounds__(kThreads)
                 const int s = __ffsll((long long)m) - 1;
                 m &= m - 1;
                 const int64_t b = w + nc * s;
-                const int64_t src = (int64_t)ids[b];  // in range: inject_mask_kernel checked it
+                const int64_t src = (int64_t)ids[b];  // a slot index: inject_mask_kernel checked it
                 if (src % nc != c) continue;
                 for (int k = 0; k < P.n; ++k)
                     if ((copies >> k) & 1u) P.pre[k][src] += P.post[k][b];
@@ -227,52 +247,39 @@ __device__ __forceinline__ void jt(const Samp* s, const double* g, double* out)
     out[1] = s[0].dv[1] * g[0] + s[1].dv[1] * g[1];
 }
 
-constexpr int kAdjWarps = 4;
-
-// One staged particle: per velocity sample q (stage q/2, component q%2) its
-// local coordinates, its cotangent and its window position.
-template <int NSAMP>
-struct Staged {
-    double tx[NSAMP], ty[NSAMP], gk[NSAMP];
-    int8_t ox[NSAMP], oy[NSAMP];
-    int cell;  // owning lane, -1: nothing to deposit
-};
-
 template <int METHOD>
 constexpr int adj_stages()
 {
     return METHOD == JP_RUNGE_KUTTA4 ? 4 : (METHOD == JP_RUNGE_KUTTA2 ? 2 : 1);
 }
 
-template <int METHOD>
-constexpr size_t advect_vjp_smem()
-{
-    return (size_t)kAdjWarps * (kWinParts * 32 * sizeof(double) + 32 * sizeof(Staged<2 * adj_stages<METHOD>()>));
-}
+// Per-slot record of one velocity sample q (stage q/2, component q%2) of a
+// particle, written by the replay kernel and read by the deposit kernel:
+// local coordinates, cotangent and window position (one byte: ox | oy << 4,
+// 0xFF when the sample deposits nothing).
+struct Staging {
+    double* t;     // [(q * 2 + d) * nslots + a]
+    double* gk;    // [q * nslots + a]
+    uint8_t* win;  // [q * nslots + a]
+    int64_t nslots;
+};
 
-// Each warp covers 32 consecutive cells. Its lanes take the warp's live
-// particles in slot-major order (full lanes whatever the cell occupancy),
-// replay each particle's stages with the forward's cell selection, map lam
-// (dL/dX after the step) to dL/dX before it, and stage the velocity
-// cotangents; then the lane owning each cell adds its staged particles to the
-// cell's 40 window partial sums. A round of 32 slot-major items holds each
-// cell at most a few times, so the owners' work is balanced too, and each cell
-// accumulates its particles in slot order (deterministic).
+// Replay: a warp covers 32 consecutive cells and its lanes take their live
+// particles in slot-major order (full lanes whatever the occupancy, and no
+// shared memory beyond the slot list, so many warps hide the latency of the
+// dependent velocity loads). Each particle's stages are replayed with the
+// forward's cell selection, lam (dL/dX after the step) becomes dL/dX before
+// it, and every velocity sample's deposit data is staged per slot.
 template <int METHOD>
-__global__ void __launch_bounds__(32 * kAdjWarps)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, METHOD == JP_RUNGE_KUTTA4 ? 2 : 3)
     advect_vjp_kernel(DevGrid g, const double* __restrict__ V0, const double* __restrict__ V1, AdjParams P,
-                      CCoords X, const uint8_t* __restrict__ index, Coords Lam, double* __restrict__ parts,
-                      int* d_err)
+                      CCoords X, const uint8_t* __restrict__ index, Coords Lam, Staging stg, int* d_err)
 {
     constexpr int NS = adj_stages<METHOD>();
-    constexpr int NQ = 2 * NS;
-    extern __shared__ __align__(16) unsigned char smem_adj[];
-    __shared__ SlotList lists[kAdjWarps];
-    __shared__ int cellI[kAdjWarps][32][2];
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ int cellI[kWarpsPerBlock][32][2];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double* part = (double*)smem_adj + (size_t)w * kWinParts * 32;  // [k][lane]
-    Staged<NQ>* st = (Staged<NQ>*)(smem_adj + (size_t)kAdjWarps * kWinParts * 32 * sizeof(double)) + w * 32;
-    const int64_t c0 = ((int64_t)blockIdx.x * kAdjWarps + w) * 32;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
     if (c0 >= g.ncells) return;
     const int64_t nc = g.ncells;
     const int M = g.max_xcell;
@@ -281,142 +288,383 @@ __global__ void __launch_bounds__(32 * kAdjWarps)
         cellI[w][lane][0] = (int)(c % g.n[0]);
         cellI[w][lane][1] = (int)(c / g.n[0]);
     }
-    for (int k = 0; k < kWinParts; ++k) part[k * 32 + lane] = 0.0;
     uint64_t mine;
     const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
     const double* Vc[2] = {V0, V1};
+    const int64_t ns = stg.nslots;
     int errs = 0;
-    for (int base = 0; base < K; base += 32) {
-        const int k = base + lane;
-        int owner = -1;
-        if (k < K) {
-            int s, l;
-            slot_item(lists[w], M, k, &s, &l);
-            const int64_t a = c0 + l + nc * s;
-            const int I[2] = {cellI[w][l][0], cellI[w][l][1]};
-            const double p0[2] = {X.c[0][a], X.c[1][a]};
-            const double lam[2] = {Lam.c[0][a], Lam.c[1][a]};
-            // forward stages with the forward's arithmetic, keeping every sample
-            Samp S[NS][2];
-            bool ok = true;
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        const int I[2] = {cellI[w][l][0], cellI[w][l][1]};
+        const double p0[2] = {X.c[0][a], X.c[1][a]};
+        const double lam[2] = {Lam.c[0][a], Lam.c[1][a]};
+        // forward stages with the forward's arithmetic, keeping every sample
+        Samp S[NS][2];
+        bool ok = true;
 #pragma unroll
-            for (int q = 0; q < NS; ++q) {
-                double x[2];
+        for (int q = 0; q < NS; ++q) {
+            double x[2];
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                if (q == 0)
+                    x[d] = p0[d];
+                else if (METHOD == JP_RUNGE_KUTTA2)
+                    x[d] = fma(1.0, P.adt * S[0][d].v, p0[d]);
+                else if (q < 3)
+                    x[d] = p0[d] + (P.dt * S[q - 1][d].v) * 0.5;
+                else
+                    x[d] = p0[d] + P.dt * S[2][d].v;
+            }
+#pragma unroll
+            for (int cc = 0; cc < 2; ++cc) {
+                S[q][cc] = sample2(g, cc, x, I, Vc[cc], &errs);
+                ok &= S[q][cc].ok;
+            }
+            if (!ok) break;
+        }
+        if (!ok) {  // the forward sent this particle to Inf; move_particles! dropped it
+            Lam.c[0][a] = 0.0;
+            Lam.c[1][a] = 0.0;
+#pragma unroll
+            for (int q = 0; q < 2 * NS; ++q) stg.win[q * ns + a] = 0xFF;
+            continue;
+        }
+        // reverse sweep over the stages: gk[q] = dL/d(velocity sample of stage q)
+        double gk[NS][2], l0[2] = {lam[0], lam[1]}, qb[2];
+        if (METHOD == JP_RUNGE_KUTTA2) {
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                gk[NS - 1][d] = P.dt * P.cb * lam[d];
+                gk[0][d] = P.dt * P.ca * lam[d];
+            }
+            jt(S[NS - 1], gk[NS - 1], qb);  // x1 = p0 + alpha dt k0
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                l0[d] += qb[d];
+                gk[0][d] += P.adt * qb[d];
+            }
+        } else if (METHOD == JP_RUNGE_KUTTA4) {
+            const double w6 = P.dt / 6.0;
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                gk[0][d] = w6 * lam[d];
+                gk[1][d] = 2.0 * w6 * lam[d];
+                gk[2][d] = 2.0 * w6 * lam[d];
+                gk[NS - 1][d] = w6 * lam[d];
+            }
+#pragma unroll
+            for (int q = NS - 1; q >= 1; --q) {  // x3 = p0 + dt k2, x2 = p0 + dt/2 k1, x1 = p0 + dt/2 k0
+                jt(S[q], gk[q], qb);
+                const double h = q == 3 ? P.dt : 0.5 * P.dt;
 #pragma unroll
                 for (int d = 0; d < 2; ++d) {
-                    if (q == 0)
-                        x[d] = p0[d];
-                    else if (METHOD == JP_RUNGE_KUTTA2)
-                        x[d] = fma(1.0, P.adt * S[0][d].v, p0[d]);
-                    else if (q < 3)
-                        x[d] = p0[d] + (P.dt * S[q - 1][d].v) * 0.5;
-                    else
-                        x[d] = p0[d] + P.dt * S[2][d].v;
+                    l0[d] += qb[d];
+                    gk[q - 1][d] += h * qb[d];
                 }
-#pragma unroll
-                for (int cc = 0; cc < 2; ++cc) {
-                    S[q][cc] = sample2(g, cc, x, I, Vc[cc], &errs);
-                    ok &= S[q][cc].ok;
-                }
-                if (!ok) break;
             }
-            if (!ok) {  // the forward sent this particle to Inf; move_particles! dropped it
-                Lam.c[0][a] = 0.0;
-                Lam.c[1][a] = 0.0;
-            } else {
-                // reverse sweep over the stages: gk[q] = dL/d(velocity sample of stage q)
-                double gk[NS][2], l0[2] = {lam[0], lam[1]}, qb[2];
-                if (METHOD == JP_RUNGE_KUTTA2) {
+        } else {
 #pragma unroll
-                    for (int d = 0; d < 2; ++d) {
-                        gk[NS - 1][d] = P.dt * P.cb * lam[d];
-                        gk[0][d] = P.dt * P.ca * lam[d];
-                    }
-                    jt(S[NS - 1], gk[NS - 1], qb);  // x1 = p0 + alpha dt k0
-#pragma unroll
-                    for (int d = 0; d < 2; ++d) {
-                        l0[d] += qb[d];
-                        gk[0][d] += P.adt * qb[d];
-                    }
-                } else if (METHOD == JP_RUNGE_KUTTA4) {
-                    const double w6 = P.dt / 6.0;
-#pragma unroll
-                    for (int d = 0; d < 2; ++d) {
-                        gk[0][d] = w6 * lam[d];
-                        gk[1][d] = 2.0 * w6 * lam[d];
-                        gk[2][d] = 2.0 * w6 * lam[d];
-                        gk[NS - 1][d] = w6 * lam[d];
-                    }
-#pragma unroll
-                    for (int q = NS - 1; q >= 1; --q) {  // x3 = p0 + dt k2, x2 = p0 + dt/2 k1, x1 = p0 + dt/2 k0
-                        jt(S[q], gk[q], qb);
-                        const double h = q == 3 ? P.dt : 0.5 * P.dt;
-#pragma unroll
-                        for (int d = 0; d < 2; ++d) {
-                            l0[d] += qb[d];
-                            gk[q - 1][d] += h * qb[d];
-                        }
-                    }
-                } else {
-#pragma unroll
-                    for (int d = 0; d < 2; ++d) gk[0][d] = P.dt * lam[d];
-                }
-                jt(S[0], gk[0], qb);  // the first stage samples at p0 itself
-#pragma unroll
-                for (int d = 0; d < 2; ++d) l0[d] += qb[d];
-                Lam.c[0][a] = l0[0];
-                Lam.c[1][a] = l0[1];
-                Staged<NQ>& r = st[lane];
-#pragma unroll
-                for (int q = 0; q < NS; ++q)
-#pragma unroll
-                    for (int cc = 0; cc < 2; ++cc) {
-                        const int j = 2 * q + cc;
-                        const int ox = S[q][cc].idx[0] - I[0] + 1, oy = S[q][cc].idx[1] - I[1] + 1;
-                        const bool in = ox >= 0 && ox <= win_nx(cc) - 2 && oy >= 0 && oy <= win_ny(cc) - 2;
-                        if (!in) errs |= kErrAdjointWindow;
-                        r.ox[j] = (int8_t)(in ? ox : -1);
-                        r.oy[j] = (int8_t)oy;
-                        r.tx[j] = S[q][cc].t[0];
-                        r.ty[j] = S[q][cc].t[1];
-                        r.gk[j] = gk[q][cc];
-                    }
-                owner = l;
-            }
+            for (int d = 0; d < 2; ++d) gk[0][d] = P.dt * lam[d];
         }
-        st[lane].cell = owner;
-        __syncwarp();
-        // Each lane adds the staged particles of its own cell, in slot order:
-        // the round's items span slots s_lo..s_hi, and cell `lane` holds item
-        // pre[s] + (live cells below it in slot s) of each slot where it is live.
-        int s_lo, s_hi, l_unused;
-        slot_item(lists[w], M, base, &s_lo, &l_unused);
-        slot_item(lists[w], M, min(base + 31, K - 1), &s_hi, &l_unused);
-        for (int s = s_lo; s <= s_hi; ++s) {
-            const uint32_t m = lists[w].mask[s];
-            if (!((m >> lane) & 1u)) continue;
-            const int j = lists[w].pre[s] + __popc(m & ((1u << lane) - 1u)) - base;
-            if (j < 0 || j >= 32 || st[j].cell != lane) continue;
-            const Staged<NQ>& r = st[j];
+        jt(S[0], gk[0], qb);  // the first stage samples at p0 itself
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) {
-                if (r.ox[q] < 0) continue;
-                const int cc = q & 1;
-                const int NX = win_nx(cc);
-                const int b = (cc == 0 ? 0 : 20) + r.ox[q] + NX * r.oy[q];
-                const double tx = r.tx[q], ty = r.ty[q];
-                const double g0 = r.gk[q] * (1.0 - ty), g1 = r.gk[q] * ty;
-                part[b * 32 + lane] = fma(g0, 1.0 - tx, part[b * 32 + lane]);
-                part[(b + 1) * 32 + lane] = fma(g0, tx, part[(b + 1) * 32 + lane]);
-                part[(b + NX) * 32 + lane] = fma(g1, 1.0 - tx, part[(b + NX) * 32 + lane]);
-                part[(b + NX + 1) * 32 + lane] = fma(g1, tx, part[(b + NX + 1) * 32 + lane]);
+        for (int d = 0; d < 2; ++d) l0[d] += qb[d];
+        Lam.c[0][a] = l0[0];
+        Lam.c[1][a] = l0[1];
+#pragma unroll
+        for (int q = 0; q < NS; ++q)
+#pragma unroll
+            for (int cc = 0; cc < 2; ++cc) {
+                const int j = 2 * q + cc;
+                const int ox = S[q][cc].idx[0] - I[0] + 1, oy = S[q][cc].idx[1] - I[1] + 1;
+                const bool in = ox >= 0 && ox <= win_nx(cc) - 2 && oy >= 0 && oy <= win_ny(cc) - 2;
+                if (!in) errs |= kErrAdjointWindow;
+                stg.win[j * ns + a] = in ? (uint8_t)(ox | (oy << 4)) : (uint8_t)0xFF;
+                stg.t[(2 * j) * ns + a] = S[q][cc].t[0];
+                stg.t[(2 * j + 1) * ns + a] = S[q][cc].t[1];
+                stg.gk[j * ns + a] = gk[q][cc];
             }
-        }
-        __syncwarp();
     }
-    if (c0 + lane < nc)
-        for (int k = 0; k < kWinParts; ++k) parts[k * nc + c0 + lane] = part[k * 32 + lane];
     raise_err(d_err, errs);
+}
+
+constexpr int kDepThreads = 128;
+
+// Deposit: one thread per owning cell adds its particles' staged samples, in
+// slot order, to the cell's 40 window partial sums (shared memory), then
+// writes them out for the node gather. The lanes of a warp walk the slots
+// together (up to the highest live slot of the warp), so every load of the
+// staged arrays is coalesced across the warp's 32 cells.
+template <int NQ>
+__global__ void __launch_bounds__(kDepThreads)
+    deposit_kernel(DevGrid g, const uint8_t* __restrict__ index, Staging stg, double* __restrict__ parts)
+{
+    __shared__ double part[kWinParts][kDepThreads];
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nc = g.ncells;
+    const bool valid = c < nc;
+    const int64_t ns = stg.nslots;
+    const int t = threadIdx.x;
+    for (int k = 0; k < kWinParts; ++k) part[k][t] = 0.0;
+    const uint64_t m = valid ? live_mask(index, c, nc, g.max_xcell) : 0;
+    const uint32_t hi = __reduce_max_sync(0xffffffffu, m ? 64u - (uint32_t)__clzll((long long)m) : 0u);
+    for (int s = 0; s < (int)hi; ++s) {
+        if (!((m >> s) & 1)) continue;
+        const int64_t a = c + nc * s;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const uint8_t wv = stg.win[q * ns + a];
+            if (wv == 0xFF) continue;
+            const int cc = q & 1;
+            const int NX = win_nx(cc);
+            const int b = (cc == 0 ? 0 : 20) + (wv & 0xF) + NX * (wv >> 4);
+            const double tx = stg.t[(2 * q) * ns + a], ty = stg.t[(2 * q + 1) * ns + a];
+            const double gq = stg.gk[q * ns + a];
+            const double g0 = gq * (1.0 - ty), g1 = gq * ty;
+            part[b][t] = fma(g0, 1.0 - tx, part[b][t]);
+            part[b + 1][t] = fma(g0, tx, part[b + 1][t]);
+            part[b + NX][t] = fma(g1, 1.0 - tx, part[b + NX][t]);
+            part[b + NX + 1][t] = fma(g1, tx, part[b + NX + 1][t]);
+        }
+    }
+    if (valid)
+        for (int k = 0; k < kWinParts; ++k) parts[k * nc + c] = part[k][t];
+}
+
+// ------------------------------------------- split-precision form (FP32)
+// Velocity sample of the FP32 form (velocity_f32's cell and local
+// coordinates, in cell units) with its gradient with respect to the offset.
+struct SampF {
+    float v;
+    float dv[2];
+    int idx[2];
+    float t[2];
+    bool ok;
+};
+
+__device__ __forceinline__ SampF sample2_f32(const DevGrid& g, int comp, const int* I, const float* xi,
+                                             const float* __restrict__ V)
+{
+    SampF r;
+    r.ok = true;
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+        const float y = (d == comp) ? xi[d] : xi[d] + 0.5f;
+        if (!(fabsf(y) < 1e6f)) {
+            r.ok = false;
+            return r;
+        }
+        const float fl = floorf(y);
+        int kk = I[d] + (int)fl;
+        float tt = y - fl;
+        const int L = (int)g.nvel[comp][d];
+        if (kk == L - 1 && tt == 0.0f) {
+            kk = L - 2;
+            tt = 1.0f;
+        }
+        if (kk < 0 || kk > L - 2) {
+            r.ok = false;
+            return r;
+        }
+        r.idx[d] = kk;
+        r.t[d] = tt;
+    }
+    const int64_t L0 = g.nvel[comp][0];
+    const float* b = V + r.idx[0] + L0 * r.idx[1];
+    const float v00 = __ldg(b), v10 = __ldg(b + 1), v01 = __ldg(b + L0), v11 = __ldg(b + L0 + 1);
+    const float tx = r.t[0], ty = r.t[1];
+    const float a0 = lerpf1(tx, v00, v10), a1 = lerpf1(tx, v01, v11);
+    r.v = lerpf1(ty, a0, a1);
+    const float ax = v10 - v00, bx = v11 - v01;
+    r.dv[0] = fmaf(ty, bx - ax, ax);
+    r.dv[1] = a1 - a0;
+    return r;
+}
+
+__device__ __forceinline__ void jt_f(const SampF* s, const double* g, double* out)
+{
+    out[0] = (double)s[0].dv[0] * g[0] + (double)s[1].dv[0] * g[1];
+    out[1] = (double)s[0].dv[1] * g[0] + (double)s[1].dv[1] * g[1];
+}
+
+// Replay kernel of the FP32 form: the stages of advect_f32 (offsets in cell
+// units, FP32, the same operations), then the same reverse sweep as the FP64
+// kernel with the per-axis step w = dt/dx, carried out in FP64; lam is
+// dL/d(offset). The staged samples feed the same deposit and node gather.
+template <int METHOD>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, METHOD == JP_RUNGE_KUTTA4 ? 2 : 3)
+    advect_vjp_f32_kernel(DevGrid g, const float* __restrict__ V0, const float* __restrict__ V1, F32Params P,
+                          CXiF Xi, const uint8_t* __restrict__ index, Coords Lam, Staging stg, int* d_err)
+{
+    constexpr int NS = adj_stages<METHOD>();
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ int cellI[kWarpsPerBlock][32][2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    {
+        const int64_t c = min(c0 + lane, nc - 1);
+        cellI[w][lane][0] = (int)(c % g.n[0]);
+        cellI[w][lane][1] = (int)(c / g.n[0]);
+    }
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
+    const float* Vc[2] = {V0, V1};
+    const int64_t ns = stg.nslots;
+    const double wd[2] = {(double)P.w[0], (double)P.w[1]}, awd[2] = {(double)P.aw[0], (double)P.aw[1]};
+    int errs = 0;
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        const int I[2] = {cellI[w][l][0], cellI[w][l][1]};
+        const float x0[2] = {Xi.x[0][a], Xi.x[1][a]};
+        const double lam[2] = {Lam.c[0][a], Lam.c[1][a]};
+        SampF S[NS][2];
+        bool ok = true;
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            float x[2];
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                if (q == 0)
+                    x[d] = x0[d];
+                else if (METHOD == JP_RUNGE_KUTTA2)
+                    x[d] = fmaf(P.aw[d], S[0][d].v, x0[d]);
+                else if (q < 3)
+                    x[d] = fmaf(0.5f * P.w[d], S[q - 1][d].v, x0[d]);
+                else
+                    x[d] = fmaf(P.w[d], S[2][d].v, x0[d]);
+            }
+#pragma unroll
+            for (int cc = 0; cc < 2; ++cc) {
+                S[q][cc] = sample2_f32(g, cc, I, x, Vc[cc]);
+                ok &= S[q][cc].ok;
+            }
+            if (!ok) break;
+        }
+        if (!ok) {  // the forward sent this particle to Inf; move_particles! dropped it
+            Lam.c[0][a] = 0.0;
+            Lam.c[1][a] = 0.0;
+#pragma unroll
+            for (int q = 0; q < 2 * NS; ++q) stg.win[q * ns + a] = 0xFF;
+            continue;
+        }
+        double gk[NS][2], l0[2] = {lam[0], lam[1]}, qb[2];
+        if (METHOD == JP_RUNGE_KUTTA2) {
+            const double A = P.half ? 0.0 : (double)P.ca, B = P.half ? 1.0 : (double)P.cb;
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                gk[NS - 1][d] = wd[d] * B * lam[d];
+                gk[0][d] = wd[d] * A * lam[d];
+            }
+            jt_f(S[NS - 1], gk[NS - 1], qb);  // x1 = x0 + aw v0
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                l0[d] += qb[d];
+                gk[0][d] += awd[d] * qb[d];
+            }
+        } else if (METHOD == JP_RUNGE_KUTTA4) {
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                const double w6 = wd[d] / 6.0;
+                gk[0][d] = w6 * lam[d];
+                gk[1][d] = 2.0 * w6 * lam[d];
+                gk[2][d] = 2.0 * w6 * lam[d];
+                gk[NS - 1][d] = w6 * lam[d];
+            }
+#pragma unroll
+            for (int q = NS - 1; q >= 1; --q) {
+                jt_f(S[q], gk[q], qb);
+#pragma unroll
+                for (int d = 0; d < 2; ++d) {
+                    l0[d] += qb[d];
+                    gk[q - 1][d] += (q == 3 ? wd[d] : 0.5 * wd[d]) * qb[d];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int d = 0; d < 2; ++d) gk[0][d] = wd[d] * lam[d];
+        }
+        jt_f(S[0], gk[0], qb);
+#pragma unroll
+        for (int d = 0; d < 2; ++d) l0[d] += qb[d];
+        Lam.c[0][a] = l0[0];
+        Lam.c[1][a] = l0[1];
+#pragma unroll
+        for (int q = 0; q < NS; ++q)
+#pragma unroll
+            for (int cc = 0; cc < 2; ++cc) {
+                const int j = 2 * q + cc;
+                const int ox = S[q][cc].idx[0] - I[0] + 1, oy = S[q][cc].idx[1] - I[1] + 1;
+                const bool in = ox >= 0 && ox <= win_nx(cc) - 2 && oy >= 0 && oy <= win_ny(cc) - 2;
+                if (!in) errs |= kErrAdjointWindow;
+                stg.win[j * ns + a] = in ? (uint8_t)(ox | (oy << 4)) : (uint8_t)0xFF;
+                stg.t[(2 * j) * ns + a] = (double)S[q][cc].t[0];
+                stg.t[(2 * j + 1) * ns + a] = (double)S[q][cc].t[1];
+                stg.gk[j * ns + a] = gk[q][cc];
+            }
+    }
+    raise_err(d_err, errs);
+}
+
+// particle2grid! of the FP32 form, per particle: F_v = sum_i w_i f_i / W_v with
+// w = 1 / ss, ss = sum_d ((k_d - xi_d) dx_d)^2 in FP32 (the forward's
+// weights), so
+//   dL/dFp_i  += sum_v gF_v w_i / W_v
+//   dL/dxi_d  += sum_v gF_v (f_i - F_v) / W_v * 2 w_i^2 (k_d - xi_d) dx_d^2
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    p2g_vjp_f32_kernel(DevGrid g, F32Params P, const float* __restrict__ F, const double* __restrict__ W,
+                       const float* __restrict__ Fp, CXiF Xi, const uint8_t* __restrict__ index,
+                       const double* __restrict__ gF, double* __restrict__ gFp, Coords gX)
+{
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ int cellI[kWarpsPerBlock][32][2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    {
+        const int64_t c = min(c0 + lane, nc - 1);
+        cellI[w][lane][0] = (int)(c % g.n[0]);
+        cellI[w][lane][1] = (int)(c / g.n[0]);
+    }
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
+    const int64_t V0 = g.n[0] + 1;
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        const int I[2] = {cellI[w][l][0], cellI[w][l][1]};
+        const float xi[2] = {Xi.x[0][a], Xi.x[1][a]};
+        const double f = (double)Fp[a];
+        double gf = 0.0, gx = 0.0, gy = 0.0;
+        for (int kb = 0; kb < 2; ++kb)
+            for (int ka = 0; ka < 2; ++ka) {
+                const int64_t v = (I[0] + ka) + V0 * (I[1] + kb);
+                const float ex = ((float)ka - xi[0]) * P.dx[0], ey = ((float)kb - xi[1]) * P.dx[1];
+                float ss = 0.0f;
+                ss = fmaf(ex, ex, ss);
+                ss = fmaf(ey, ey, ss);
+                const double wi = (double)__frcp_rn(ss);
+                const double r = ldg(gF + v) / ldg(W + v);
+                gf = fma(r, wi, gf);
+                const double q = r * (f - (double)__ldg(F + v)) * 2.0 * wi * wi;
+                gx = fma(q, (double)ex * (double)P.dx[0], gx);
+                gy = fma(q, (double)ey * (double)P.dx[1], gy);
+            }
+        gFp[a] += gf;
+        if (gX.c[0]) {
+            gX.c[0][a] += gx;
+            gX.c[1][a] += gy;
+        }
+    }
 }
 
 // dL/dV at every node of component `comp`: the partial sums of the owning
@@ -554,15 +802,42 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------ launchers
+// Adjoint scratch: the 40 window partial sums and the injected-slot mask per
+// cell, then the per-slot staging of up to 8 velocity samples (RK4).
+constexpr int kMaxSamples = 8;
+
+static size_t adjoint_scratch_bytes(const DevGrid& g)
+{
+    const size_t nc = (size_t)g.ncells, ns = nc * (size_t)g.max_xcell;
+    return nc * (kWinParts * sizeof(double) + sizeof(uint64_t)) +
+           ns * kMaxSamples * (3 * sizeof(double) + sizeof(uint8_t)) + nc * sizeof(unsigned);
+}
+
 static cudaError_t ensure_adjoint_scratch(jp_particles* P)
 {
     if (P->adj_rec) return cudaSuccess;
-    const size_t bytes = (size_t)P->g.ncells * (kWinParts * sizeof(double) + sizeof(uint64_t));
-    return cudaMalloc(&P->adj_rec, bytes);
+    return cudaMalloc(&P->adj_rec, adjoint_scratch_bytes(P->g));
 }
 
 static double* adj_parts(jp_particles* P) { return (double*)P->adj_rec; }
 static uint64_t* adj_inj(jp_particles* P) { return (uint64_t*)((double*)P->adj_rec + kWinParts * P->g.ncells); }
+
+static Staging adj_staging(jp_particles* P)
+{
+    const int64_t nc = P->g.ncells, ns = nc * P->g.max_xcell;
+    Staging s;
+    s.t = (double*)(adj_inj(P) + nc);
+    s.gk = s.t + 2 * kMaxSamples * ns;
+    s.win = (uint8_t*)(s.gk + kMaxSamples * ns);
+    s.nslots = ns;
+    return s;
+}
+
+static unsigned* adj_srcflag(jp_particles* P)
+{
+    const Staging s = adj_staging(P);
+    return (unsigned*)(s.win + kMaxSamples * s.nslots);
+}
 
 cudaError_t launch_move_permutation(jp_particles* P, int32_t* dest)
 {
@@ -597,36 +872,57 @@ cudaError_t launch_permute_vjp(jp_particles* P, const int32_t* dest, const doubl
     return cudaGetLastError();
 }
 
-cudaError_t launch_slot_ids(jp_particles* P, const uint8_t* index, double* ids)
+template <typename IdT>
+static cudaError_t slot_ids(jp_particles* P, const uint8_t* index, IdT* ids)
 {
     const int64_t ns = P->g.ncells * P->g.max_xcell;
-    slot_ids_kernel<<<grid_blocks(ns), kThreads, 0, P->stream>>>(ns, index, ids);
+    slot_ids_kernel<IdT><<<grid_blocks(ns), kThreads, 0, P->stream>>>(ns, index, ids);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_slot_ids(jp_particles* P, const uint8_t* index, double* ids) { return slot_ids(P, index, ids); }
+cudaError_t launch_slot_ids_i32(jp_particles* P, const uint8_t* index, int32_t* ids)
+{
+    return slot_ids(P, index, ids);
+}
+
+template <typename IdT>
+static cudaError_t inject_vjp(jp_particles* P, const IdT* ids, const double* const* post, double* const* pre, int n,
+                              unsigned copies)
+{
+    cudaError_t e = ensure_adjoint_scratch(P);
+    if (e != cudaSuccess) return e;
+    const unsigned nb = grid_blocks(P->g.ncells);
+    if (copies) {
+        e = cudaMemsetAsync(adj_srcflag(P), 0, (size_t)P->g.ncells * sizeof(unsigned), P->stream);
+        if (e != cudaSuccess) return e;
+        inject_mask_kernel<IdT><<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), adj_srcflag(P), P->d_err);
+    }
+    inject_vjp_kernel<IdT><<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), adj_srcflag(P),
+                                                           perm_arrays(post, pre, n), copies);
     return cudaGetLastError();
 }
 
 cudaError_t launch_inject_vjp(jp_particles* P, const double* ids, const double* const* post, double* const* pre,
                               int n, unsigned copies)
 {
-    cudaError_t e = ensure_adjoint_scratch(P);
-    if (e != cudaSuccess) return e;
-    const unsigned nb = grid_blocks(P->g.ncells);
-    if (copies) inject_mask_kernel<<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), P->d_err);
-    inject_vjp_kernel<<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), perm_arrays(post, pre, n), copies);
-    return cudaGetLastError();
+    return inject_vjp(P, ids, post, pre, n, copies);
+}
+cudaError_t launch_inject_vjp_i32(jp_particles* P, const int32_t* ids, const double* const* post,
+                                  double* const* pre, int n, unsigned copies)
+{
+    return inject_vjp(P, ids, post, pre, n, copies);
 }
 
 template <int METHOD>
-static cudaError_t launch_advect_vjp(jp_particles* P, unsigned nb, cudaStream_t st, const double* const V[3],
+static cudaError_t launch_advect_vjp(jp_particles* P, cudaStream_t st, const double* const V[3],
                                      const AdjParams& prm, const CCoords& X, const uint8_t* index, const Coords& L)
 {
-    constexpr size_t smem = advect_vjp_smem<METHOD>();
-    static_assert(smem <= 200 * 1024, "advect_vjp_kernel shared memory");
-    // static shared memory comes on top of the dynamic part: always raise the cap
-    cudaError_t e = cudaFuncSetAttribute(advect_vjp_kernel<METHOD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    advect_vjp_kernel<METHOD><<<nb, 32 * kAdjWarps, smem, st>>>(P->g, V[0], V[1], prm, X, index, L, adj_parts(P),
-                                                                 P->d_err);
+    const Staging stg = adj_staging(P);
+    advect_vjp_kernel<METHOD><<<grid_blocks(P->g.ncells, 32 * kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(
+        P->g, V[0], V[1], prm, X, index, L, stg, P->d_err);
+    deposit_kernel<2 * adj_stages<METHOD>()><<<grid_blocks(P->g.ncells, kDepThreads), kDepThreads, 0, st>>>(
+        P->g, index, stg, adj_parts(P));
     return cudaGetLastError();
 }
 
@@ -646,19 +942,61 @@ cudaError_t launch_advection_vjp(jp_particles* P, int method, double alpha, cons
     prm.cb = alpha == 0.5 ? 1.0 : 0.5 * ia;
     CCoords X{{coords[0], coords[1], nullptr}};
     Coords L{{lam[0], lam[1], nullptr}};
-    const unsigned nb = grid_blocks(P->g.ncells, 32 * kAdjWarps);
     cudaStream_t st = P->stream;
     if (method == JP_RUNGE_KUTTA2)
-        e = launch_advect_vjp<JP_RUNGE_KUTTA2>(P, nb, st, V, prm, X, index, L);
+        e = launch_advect_vjp<JP_RUNGE_KUTTA2>(P, st, V, prm, X, index, L);
     else if (method == JP_RUNGE_KUTTA4)
-        e = launch_advect_vjp<JP_RUNGE_KUTTA4>(P, nb, st, V, prm, X, index, L);
+        e = launch_advect_vjp<JP_RUNGE_KUTTA4>(P, st, V, prm, X, index, L);
     else
-        e = launch_advect_vjp<JP_EULER>(P, nb, st, V, prm, X, index, L);
+        e = launch_advect_vjp<JP_EULER>(P, st, V, prm, X, index, L);
     if (e != cudaSuccess) return e;
     for (int c = 0; c < 2; ++c) {
         const int64_t nn = P->g.nvel[c][0] * P->g.nvel[c][1];
         vel_gather_kernel<<<grid_blocks(nn), kThreads, 0, st>>>(P->g, c, adj_parts(P), gV[c]);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advection_vjp_f32(jp_particles* P, int method, double alpha, const float* const V[3], double dt,
+                                     const float* const xi[3], const uint8_t* index, double* const lam[3],
+                                     double* const gV[3])
+{
+    cudaError_t e = ensure_adjoint_scratch(P);
+    if (e != cudaSuccess) return e;
+    const F32Params prm = make_params(P, alpha, dt);
+    CXiF X{{xi[0], xi[1], nullptr}};
+    Coords L{{lam[0], lam[1], nullptr}};
+    const Staging stg = adj_staging(P);
+    cudaStream_t st = P->stream;
+    const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const unsigned nd = grid_blocks(P->g.ncells, kDepThreads);
+    const int nt = 32 * kWarpsPerBlock;
+    if (method == JP_RUNGE_KUTTA2) {
+        advect_vjp_f32_kernel<JP_RUNGE_KUTTA2><<<nb, nt, 0, st>>>(P->g, V[0], V[1], prm, X, index, L, stg, P->d_err);
+        deposit_kernel<4><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
+    } else if (method == JP_RUNGE_KUTTA4) {
+        advect_vjp_f32_kernel<JP_RUNGE_KUTTA4><<<nb, nt, 0, st>>>(P->g, V[0], V[1], prm, X, index, L, stg, P->d_err);
+        deposit_kernel<8><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
+    } else {
+        advect_vjp_f32_kernel<JP_EULER><<<nb, nt, 0, st>>>(P->g, V[0], V[1], prm, X, index, L, stg, P->d_err);
+        deposit_kernel<2><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
+    }
+    for (int c = 0; c < 2; ++c) {
+        const int64_t nn = P->g.nvel[c][0] * P->g.nvel[c][1];
+        vel_gather_kernel<<<grid_blocks(nn), kThreads, 0, st>>>(P->g, c, adj_parts(P), gV[c]);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_p2g_vjp_f32(jp_particles* P, const float* F, const double* W, const float* Fp,
+                               const float* const xi[3], const uint8_t* index, const double* gF, double* gFp,
+                               double* const gxi[3])
+{
+    const F32Params prm = make_params(P, 0.5, 0.0);
+    CXiF X{{xi[0], xi[1], nullptr}};
+    Coords G{{gxi ? gxi[0] : nullptr, gxi ? gxi[1] : nullptr, nullptr}};
+    p2g_vjp_f32_kernel<<<grid_blocks(P->g.ncells, 32 * kWarpsPerBlock), 32 * kWarpsPerBlock, 0, P->stream>>>(
+        P->g, prm, F, W, Fp, X, index, gF, gFp, G);
     return cudaGetLastError();
 }
 

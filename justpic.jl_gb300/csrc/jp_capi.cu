@@ -549,6 +549,89 @@ int jp_grid2particle(jp_particles* P, double* Fp, const double* F, const double*
     return finish(P, jp::launch_g2p(P, Fp, F, coords, index), "jp_grid2particle");
 }
 
+// ---- adjoint of the split-precision form (2D) ---------------------------
+static int check_f32_adj(const jp_particles* P, const char* what)
+{
+    if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": the adjoint is built for 2D");
+    if (!P->g.uniform || !P->staggered_std)
+        return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": the split-precision form needs uniform "
+                                                                 "grids with the standard ghost-node staggering");
+    return JP_OK;
+}
+
+int jp_slot_ids_i32(jp_particles* P, const uint8_t* index, int32_t* ids)
+{
+    if (!P || !index || !ids) return fail(JP_ERR_INVALID_ARGUMENT, "jp_slot_ids_i32: null pointer");
+    if (!slots_fit_int32(P)) return fail(JP_ERR_INVALID_ARGUMENT, "jp_slot_ids_i32: more than 2^31 slots");
+    return finish(P, jp::launch_slot_ids_i32(P, index, ids), "jp_slot_ids_i32");
+}
+
+int jp_inject_vjp_i32(jp_particles* P, const int32_t* ids, const double* const* post, double* const* pre,
+                      int32_t n, int32_t copies)
+{
+    if (!P || !ids || !post || !pre || n < 0 || n > 8)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp_i32: bad arguments");
+    if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp_i32: the adjoint is built for 2D");
+    for (int k = 0; k < n; ++k)
+        if (!post[k] || !pre[k] || post[k] == pre[k])
+            return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp_i32: null or aliased array");
+    return finish(P, jp::launch_inject_vjp_i32(P, ids, post, pre, n, (unsigned)copies & ((1u << n) - 1u)),
+                  "jp_inject_vjp_i32");
+}
+
+int jp_advection_vjp_f32(jp_particles* P, int32_t method, double alpha, const float* const V[3], double dt,
+                         const float* const xi[3], const uint8_t* index, double* const lam[3], double* const gV[3])
+{
+    if (!P || !index || !check_coords(P, (const void* const*)xi) || !check_coords(P, (const void* const*)V) ||
+        !check_coords(P, (const void* const*)lam) || !check_coords(P, (const void* const*)gV))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_vjp_f32: null pointer");
+    int rc = check_f32_adj(P, "jp_advection_vjp_f32");
+    if (rc) return rc;
+    if (method != JP_EULER && method != JP_RUNGE_KUTTA2 && method != JP_RUNGE_KUTTA4)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_vjp_f32: unknown integrator");
+    if (method == JP_RUNGE_KUTTA2 && !(0.0 < alpha && alpha < 1.0))
+        return fail(JP_ERR_INVALID_ARGUMENT, "Only 0 < α < 1 is supported");
+    return finish(P, jp::launch_advection_vjp_f32(P, method, alpha, V, dt, xi, index, lam, gV),
+                  "jp_advection_vjp_f32");
+}
+
+int jp_particle2grid_f32_with_weights(jp_particles* P, float* F, double* W, const float* Fp, const float* const xi[3],
+                                      const uint8_t* index)
+{
+    if (!P || !F || !W || !Fp || !index || !check_coords(P, (const void* const*)xi))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_f32_with_weights: null pointer");
+    if (!P->g.uniform || !P->staggered_std)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_f32_with_weights: the split-precision form needs "
+                                             "uniform grids with the standard ghost-node staggering");
+    return finish(P, jp::launch_p2g_f32(P, F, Fp, xi, index, W), "jp_particle2grid_f32_with_weights");
+}
+
+int jp_particle2grid_vjp_f32(jp_particles* P, const float* F, const double* W, const float* Fp,
+                             const float* const xi[3], const uint8_t* index, const double* gF, double* gFp,
+                             double* const gxi[3])
+{
+    if (!P || !F || !W || !Fp || !gF || !gFp || !index || !check_coords(P, (const void* const*)xi) ||
+        (gxi && !check_coords(P, (const void* const*)gxi)))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_vjp_f32: null pointer");
+    int rc = check_f32_adj(P, "jp_particle2grid_vjp_f32");
+    if (rc) return rc;
+    return finish(P, jp::launch_p2g_vjp_f32(P, F, W, Fp, xi, index, gF, gFp, gxi), "jp_particle2grid_vjp_f32");
+}
+
+int jp_phase_ratios(jp_particles* P, int32_t nphases, const double* phases, const double* const coords[3],
+                    double* center, double* vertex, double* const faces[3])
+{
+    if (!P || !phases || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "update_phase_ratios!: null pointer");
+    if (nphases < 1 || nphases > 16)
+        return fail(JP_ERR_INVALID_ARGUMENT, "update_phase_ratios!: 1 to 16 phases are supported");
+    if (!P->centres_ok)
+        return fail(JP_ERR_INVALID_ARGUMENT,
+                    "update_phase_ratios!: needs ghost-expanded centre grids with at least 2 cells per axis");
+    return finish(P, jp::launch_phase_ratios(P, nphases, phases, coords, center, vertex, faces),
+                  "update_phase_ratios!");
+}
+
 int jp_grid2particle_flip(jp_particles* P, double* Fp, const double* F, const double* F0, double alpha,
                           const double* const coords[3], const uint8_t* index)
 {

@@ -22,49 +22,18 @@
 //     quadrant corner + 1/2 * (0.05 + 0.95 r) and the nearest neighbour is the
 //     first minimum of the FP32 squared physical distance in k -> j -> i ->
 //     slot order;
-//   * particle2grid! weights are 1 / |vertex - particle|^2 in FP32, summed in
-//     FP64 in the reference's order.
+//   * particle2grid! weights are 1 / |vertex - particle|^2 in FP32, summed at
+//     FP64 accuracy in the reference's order (compensated FP32 pairs within a
+//     cell, FP64 across cells).
 #include <math_constants.h>
 
 #include <cmath>
 
+#include "jp_f32_core.cuh"
 #include "jp_internal.cuh"
 #include "jp_move_core.cuh"
 
 namespace jp {
-
-struct XiF {
-    float* x[3];
-};
-struct CXiF {
-    const float* x[3];
-};
-struct ArgsF {
-    float* a[JP_MAX_ARGS];
-    int n;
-};
-struct CVelF {
-    const float* v[3];
-};
-
-// per-call constants of the FP32 form
-struct F32Params {
-    float dx[3];   // spacing per axis
-    float w[3];    // dt / dx per axis (time step in cell units per unit velocity)
-    float aw[3];   // alpha * dt / dx
-    float ca, cb;  // RK2 blend for alpha != 1/2
-    int half;
-};
-
-__device__ __forceinline__ float lerpf1(float t, float v0, float v1) { return fmaf(t, v1, fmaf(-t, v0, v0)); }
-
-template <int DIM>
-__device__ __forceinline__ float lerpNf(const float* v, const float* t)
-{
-    if (DIM == 2) return lerpf1(t[1], lerpf1(t[0], v[0], v[1]), lerpf1(t[0], v[2], v[3]));
-    return lerpf1(t[2], lerpf1(t[1], lerpf1(t[0], v[0], v[1]), lerpf1(t[0], v[2], v[3])),
-                  lerpf1(t[1], lerpf1(t[0], v[4], v[5]), lerpf1(t[0], v[6], v[7])));
-}
 
 // ------------------------------------------------------------ conversions
 template <int DIM>
@@ -114,53 +83,6 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------- advection
-// Velocity component `comp` at cell I + offset xi.
-template <int DIM>
-__device__ __forceinline__ float velocity_f32(const DevGrid& g, int comp, const int* I, const float* xi,
-                                              const float* __restrict__ V)
-{
-    int k[3];
-    float t[3];
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-        const float y = (d == comp) ? xi[d] : xi[d] + 0.5f;
-        if (!(fabsf(y) < 1e6f)) return CUDART_INF_F;  // NaN, Inf or far outside
-        const float fl = floorf(y);
-        int kk = I[d] + (int)fl;
-        float tt = y - fl;
-        const int L = (int)g.nvel[comp][d];
-        if (kk == L - 1 && tt == 0.0f) {  // exactly on the last node
-            kk = L - 2;
-            tt = 1.0f;
-        }
-        if (kk < 0 || kk > L - 2) return CUDART_INF_F;  // outside the grid's limits
-        k[d] = kk;
-        t[d] = tt;
-    }
-    const int64_t L0 = g.nvel[comp][0];
-    float v[8];
-    if (DIM == 2) {
-        const float* b = V + k[0] + L0 * k[1];
-        v[0] = __ldg(b);
-        v[1] = __ldg(b + 1);
-        v[2] = __ldg(b + L0);
-        v[3] = __ldg(b + L0 + 1);
-    } else {
-        const int64_t L1 = g.nvel[comp][1];
-        const int64_t sz = L0 * L1;
-        const float* b = V + k[0] + L0 * (k[1] + L1 * (int64_t)k[2]);
-        v[0] = __ldg(b);
-        v[1] = __ldg(b + 1);
-        v[2] = __ldg(b + L0);
-        v[3] = __ldg(b + L0 + 1);
-        v[4] = __ldg(b + sz);
-        v[5] = __ldg(b + sz + 1);
-        v[6] = __ldg(b + sz + L0);
-        v[7] = __ldg(b + sz + L0 + 1);
-    }
-    return lerpNf<DIM>(v, t);
-}
-
 template <int DIM, int METHOD>
 __device__ __forceinline__ void advect_f32(const DevGrid& g, const CVelF& V, const F32Params& P, const int* I,
                                            const float* x0, float* x)
@@ -381,6 +303,7 @@ __global__ void __launch_bounds__(kThreads)
 struct InjectListsF {
     int* counts;
     int* list;
+    uint64_t* lm;  // occupancy mask per cell
     int64_t off[8];
 };
 
@@ -398,10 +321,12 @@ __global__ void __launch_bounds__(kThreads)
         col = (int)(I[0] & 1) + 2 * (int)(I[1] & 1) + (DIM == 3 ? 4 * (int)(I[2] & 1) : 0);
         const int64_t nc = g.ncells;
         const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
+        // the cell's occupancy mask, kept for the passes' neighbourhood staging
+        const uint64_t live = live_mask(index, c, nc, g.max_xcell);
+        Ls.lm[c] = live;
         int count = 0;
-        for (int s = 0; s < g.max_xcell && count < min_xq; ++s) {
-            const int64_t a = c + nc * s;
-            if (!index[a]) continue;
+        for (uint64_t m = live; m && count < min_xq; m &= m - 1) {
+            const int64_t a = c + nc * (__ffsll((long long)m) - 1);
             bool in = true;
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
@@ -434,8 +359,8 @@ __host__ __device__ __forceinline__ size_t hood_bytes_f32(int M)
 
 template <int DIM>
 __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const XiF& Xi,
-                                     uint8_t* __restrict__ index, const ArgsF& A, uint32_t call, int64_t c,
-                                     float* const* r, uint8_t* live, int lane, int* errs)
+                                     uint8_t* __restrict__ index, uint64_t* lm, const ArgsF& A, uint32_t call,
+                                     int64_t c, float* const* r, uint8_t* live, int lane, int* errs)
 {
     const int64_t nc = g.ncells;
     const int M = g.max_xcell;
@@ -444,23 +369,49 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
     const int ncand = NB * M;
     int64_t I[3];
     cell_coords(g, c, I);
-    // stage: positions in cell units relative to this cell's lower-left vertex
-    for (int o = lane; o < ncand; o += 32) {
-        const int nb = o / M, s = o - nb * M;
-        const int off[3] = {nb % 3 - 1, (nb / 3) % 3 - 1, DIM == 3 ? nb / 9 - 1 : 0};
-        const int64_t J[3] = {I[0] + off[0], I[1] + off[1], I[2] + off[2]};
-        bool ok = J[0] >= 0 && J[1] >= 0 && J[0] < g.n[0] && J[1] < g.n[1] &&
-                  (DIM == 2 || (J[2] >= 0 && J[2] < g.n[2]));
-        uint8_t lv = 0;
+    // Stage positions in cell units relative to this cell's lower-left vertex.
+    // Occupancy from the flag pass's per-cell masks (one load per neighbour
+    // cell); the offsets of the live candidates are loaded in batches with all
+    // loads of a batch in flight together.
+    int64_t nbc = 0;
+    uint64_t nbm = 0;
+    if (lane < NB) {
+        const int64_t J[3] = {I[0] + lane % 3 - 1, I[1] + (lane / 3) % 3 - 1, DIM == 3 ? I[2] + lane / 9 - 1 : 0};
+        const bool ok = J[0] >= 0 && J[1] >= 0 && J[0] < g.n[0] && J[1] < g.n[1] &&
+                        (DIM == 2 || (J[2] >= 0 && J[2] < g.n[2]));
         if (ok) {
-            const int64_t a = cell_linear<DIM>(g, J) + nc * s;
-            lv = index[a];
-            if (lv) {
+            nbc = cell_linear<DIM>(g, J);
+            nbm = lm[nbc];
+        }
+    }
+    constexpr int B = 8;
+    for (int bo = 0; bo < ncand; bo += 32 * B) {
+        float xs[B][DIM];
+        bool lv[B];
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) r[d][o] = (float)off[d] + Xi.x[d][a];
+        for (int u = 0; u < B; ++u) {
+            const int o = bo + 32 * u + lane;
+            const int nb = o / M, s = o - nb * M;
+            const uint64_t m = __shfl_sync(0xffffffffu, nbm, nb < NB ? nb : 0);
+            const int64_t cc = __shfl_sync(0xffffffffu, nbc, nb < NB ? nb : 0);
+            lv[u] = o < ncand && ((m >> s) & 1ull);
+            if (lv[u]) {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) xs[u][d] = Xi.x[d][cc + nc * s];
             }
         }
-        live[o] = lv;
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int o = bo + 32 * u + lane;
+            if (o >= ncand) continue;
+            const int nb = o / M;
+            const int off[3] = {nb % 3 - 1, (nb / 3) % 3 - 1, DIM == 3 ? nb / 9 - 1 : 0};
+            if (lv[u]) {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) r[d][o] = (float)off[d] + xs[u][d];
+            }
+            live[o] = lv[u] ? 1 : 0;
+        }
     }
     __syncwarp();
     const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
@@ -541,6 +492,12 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
             if (count >= min_xq) break;
         }
     }
+    // the cell's occupancy after its injections, for the later passes' staging
+    __syncwarp();
+    const bool o0 = lane < M && live[base + lane];
+    const bool o1 = lane + 32 < M && live[base + lane + 32];
+    const uint64_t own = (uint64_t)__ballot_sync(0xffffffffu, o0) | ((uint64_t)__ballot_sync(0xffffffffu, o1) << 32);
+    if (lane == 0) lm[c] = own;
 }
 
 template <int DIM>
@@ -563,7 +520,7 @@ __global__ void inject_pass_f32(DevGrid g, F32Params P, XiF Xi, uint8_t* __restr
     int errs = 0;
     for (int k = gw; k < count; k += nwarps) {
         const int64_t c = Ls.list[Ls.off[col] + k];
-        inject_cell_warp_f32<DIM>(g, P, Xi, index, A, call, c, r, live, lane, &errs);
+        inject_cell_warp_f32<DIM>(g, P, Xi, index, Ls.lm, A, call, c, r, live, lane, &errs);
         __syncwarp();
     }
     raise_err(d_err, errs);
@@ -615,13 +572,45 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 
 // ------------------------------------------------------- particle2grid!
 // Same marching scheme and accumulation order as the FP64 kernel; weights in
-// FP32, their sums (and the weighted field sums) in FP64.
+// FP32, their sums (and the weighted field sums) at FP64 accuracy: within one
+// cell the terms are summed as compensated FP32 pairs (error-free TwoSum and
+// TwoProduct, Knuth / Dekker), and each cell's pair is added to the vertex's
+// FP64 accumulators. For the <= 64 terms of a cell the pair keeps the sum to
+// about 2^-42 relative, so the result matches FP64 summation to far below the
+// FP32 weights' own rounding, at a few FP64 operations per cell instead of two
+// per particle (GB300 issues FP64 at 1/64 of its FP32 rate).
+struct CSum {
+    float h = 0.0f, l = 0.0f;
+};
+
+// s += x with the rounding error kept in s.l (TwoSum; needs -fmad=false)
+__device__ __forceinline__ void csum_add(CSum& s, float x)
+{
+    const float t = s.h + x;
+    const float bp = t - s.h;
+    const float err = (s.h - (t - bp)) + (x - bp);
+    s.h = t;
+    s.l += err;
+}
+
+// s += a * b, the product's rounding error (exact by fmaf) added to s.l
+__device__ __forceinline__ void csum_add_prod(CSum& s, float a, float b)
+{
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    csum_add(s, p);
+    s.l += e;
+}
+
+__device__ __forceinline__ double csum_value(const CSum& s) { return (double)s.h + (double)s.l; }
+
 template <int DIM>
 __device__ __forceinline__ void p2g_cell_f32(int64_t c, uint64_t mask, int64_t nc, const float* kc, const float* kn,
                                              bool do_cur, bool do_nxt, const float* dx,
                                              const float* __restrict__ Fp, const CXiF& Xi, double& w_c, double& wF_c,
                                              double& w_n, double& wF_n)
 {
+    CSum sw_c, sF_c, sw_n, sF_n;
     while (mask) {
         const int s = __ffsll((long long)mask) - 1;
         mask &= mask - 1;
@@ -629,7 +618,7 @@ __device__ __forceinline__ void p2g_cell_f32(int64_t c, uint64_t mask, int64_t n
         float xi[3];
 #pragma unroll
         for (int d = 0; d < DIM; ++d) xi[d] = Xi.x[d][a];
-        const double f = (double)Fp[a];
+        const float f = Fp[a];
         if (do_cur) {
             float ss = 0.0f;
 #pragma unroll
@@ -637,9 +626,9 @@ __device__ __forceinline__ void p2g_cell_f32(int64_t c, uint64_t mask, int64_t n
                 const float e = (kc[d] - xi[d]) * dx[d];
                 ss = fmaf(e, e, ss);
             }
-            const double wi = (double)__frcp_rn(ss);
-            w_c += wi;
-            wF_c = fma(wi, f, wF_c);
+            const float wi = __frcp_rn(ss);
+            csum_add(sw_c, wi);
+            csum_add_prod(sF_c, wi, f);
         }
         if (do_nxt) {
             float ss = 0.0f;
@@ -648,17 +637,25 @@ __device__ __forceinline__ void p2g_cell_f32(int64_t c, uint64_t mask, int64_t n
                 const float e = (kn[d] - xi[d]) * dx[d];
                 ss = fmaf(e, e, ss);
             }
-            const double wi = (double)__frcp_rn(ss);
-            w_n += wi;
-            wF_n = fma(wi, f, wF_n);
+            const float wi = __frcp_rn(ss);
+            csum_add(sw_n, wi);
+            csum_add_prod(sF_n, wi, f);
         }
+    }
+    if (do_cur) {
+        w_c += csum_value(sw_c);
+        wF_c += csum_value(sF_c);
+    }
+    if (do_nxt) {
+        w_n += csum_value(sw_n);
+        wF_n += csum_value(sF_n);
     }
 }
 
 template <int DIM>
 __global__ void __launch_bounds__(kThreads)
     p2g_f32_kernel(DevGrid g, F32Params P, float* __restrict__ F, const float* __restrict__ Fp, CXiF Xi,
-                   const uint8_t* __restrict__ index, int chunk, int64_t nthreads)
+                   const uint8_t* __restrict__ index, int chunk, int64_t nthreads, double* __restrict__ Wout)
 {
     const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -725,6 +722,7 @@ __global__ void __launch_bounds__(kThreads)
         if (vok) {
             const int64_t v = DIM == 2 ? i + V0 * r : i + V0 * (j + V1 * r);
             F[v] = (float)(wF_c / w_c);
+            if (Wout) Wout[v] = w_c;
         }
         w_c = w_n;
         wF_c = wF_n;
@@ -732,22 +730,6 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------ launchers
-static F32Params make_params(const jp_particles* P, double alpha, double dt)
-{
-    F32Params p{};
-    for (int d = 0; d < 3; ++d) {
-        const double dx = P->dx_host[d];
-        p.dx[d] = (float)dx;
-        p.w[d] = (float)(dt / dx);
-        p.aw[d] = (float)(alpha * dt / dx);
-    }
-    const double ia = 1.0 / alpha;
-    p.ca = (float)std::fma(-0.5, ia, 1.0);
-    p.cb = (float)(0.5 * ia);
-    p.half = alpha == 0.5;
-    return p;
-}
-
 cudaError_t launch_to_offsets(jp_particles* P, const double* const coords[3], const uint8_t* index,
                               float* const xi[3])
 {
@@ -835,14 +817,14 @@ cudaError_t launch_inject_f32(jp_particles* P, float* const xi[3], uint8_t* inde
 {
     const int N = P->g.ndim;
     const int64_t nc = P->g.ncells;
-    if (!P->inject.counts) {
-        cudaError_t e = cudaMalloc(&P->inject.counts, (8 + nc) * sizeof(int));
+    {
+        cudaError_t e = ensure_inject_scratch(P);
         if (e != cudaSuccess) return e;
-        P->inject.list = P->inject.counts + 8;
     }
     InjectListsF Ls;
     Ls.counts = P->inject.counts;
     Ls.list = P->inject.list;
+    Ls.lm = P->inject.lm;
     int64_t cnt[3][2];
     for (int d = 0; d < 3; ++d)
         for (int o = 0; o < 2; ++o) cnt[d][o] = d < N ? (P->g.n[d] - o + 1) / 2 : (o == 0 ? 1 : 0);
@@ -900,7 +882,7 @@ cudaError_t launch_g2p_f32(jp_particles* P, float* Fp, const float* F, const flo
 }
 
 cudaError_t launch_p2g_f32(jp_particles* P, float* F, const float* Fp, const float* const xi[3],
-                           const uint8_t* index)
+                           const uint8_t* index, double* W)
 {
     const bool d3 = P->g.ndim == 3;
     CXiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
@@ -914,9 +896,9 @@ cudaError_t launch_p2g_f32(jp_particles* P, float* F, const float* Fp, const flo
     const int64_t nthreads = cols * ((rows + chunk - 1) / chunk);
     const unsigned nb = grid_blocks(nthreads);
     if (!d3)
-        p2g_f32_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, chunk, nthreads);
+        p2g_f32_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, chunk, nthreads, W);
     else
-        p2g_f32_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, chunk, nthreads);
+        p2g_f32_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, chunk, nthreads, W);
     return cudaGetLastError();
 }
 

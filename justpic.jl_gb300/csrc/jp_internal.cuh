@@ -64,9 +64,13 @@ struct MoveScratch {
 };
 
 struct InjectScratch {
-    int* counts = nullptr;  // flagged cells per colour (8 counters), then the lists
-    int* list = nullptr;    // flagged cells, one region per colour
+    int* counts = nullptr;     // flagged cells per colour (8 counters), then the lists
+    int* list = nullptr;       // flagged cells, one region per colour
+    uint64_t* lm = nullptr;    // occupancy mask per cell (written by the flag pass)
 };
+
+// counters, lists and masks of inject_particles! in one allocation
+cudaError_t ensure_inject_scratch(jp_particles* P);
 
 }  // namespace jp
 
@@ -323,6 +327,8 @@ cudaError_t launch_g2p_flip(jp_particles* P, double* Fp, const double* F, const 
                             const double* const coords[3], const uint8_t* index);
 cudaError_t launch_c2p(jp_particles* P, double* Fp, const double* F, const double* const coords[3]);
 cudaError_t launch_p2c(jp_particles* P, double* F, const double* Fp, const double* const coords[3]);
+cudaError_t launch_phase_ratios(jp_particles* P, int nph, const double* phases, const double* const coords[3],
+                                double* center, double* vertex, double* const faces[3]);
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
                        const uint8_t* index, double* W = nullptr);
 
@@ -360,7 +366,17 @@ cudaError_t launch_inject_f32(jp_particles* P, float* const xi[3], uint8_t* inde
 cudaError_t launch_g2p_f32(jp_particles* P, float* Fp, const float* F, const float* const xi[3],
                            const uint8_t* index);
 cudaError_t launch_p2g_f32(jp_particles* P, float* F, const float* Fp, const float* const xi[3],
-                           const uint8_t* index);
+                           const uint8_t* index, double* W = nullptr);
+// adjoint of the split-precision form (jp_adjoint.cu), 2D
+cudaError_t launch_slot_ids_i32(jp_particles* P, const uint8_t* index, int32_t* ids);
+cudaError_t launch_inject_vjp_i32(jp_particles* P, const int32_t* ids, const double* const* post,
+                                  double* const* pre, int n, unsigned copies);
+cudaError_t launch_advection_vjp_f32(jp_particles* P, int method, double alpha, const float* const V[3], double dt,
+                                     const float* const xi[3], const uint8_t* index, double* const lam[3],
+                                     double* const gV[3]);
+cudaError_t launch_p2g_vjp_f32(jp_particles* P, const float* F, const double* W, const float* Fp,
+                               const float* const xi[3], const uint8_t* index, const double* gF, double* gFp,
+                               double* const gxi[3]);
 
 // move_particles! with its scratch in a fixed device array (no allocation)
 constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;

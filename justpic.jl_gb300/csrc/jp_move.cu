@@ -221,6 +221,7 @@ __global__ void __launch_bounds__(kThreads)
 struct InjectLists {
     int* counts;     // [8]
     int* list;       // ncells entries
+    uint64_t* lm;    // occupancy mask per cell
     int64_t off[8];  // start of each colour's region in `list`
 };
 
@@ -253,10 +254,12 @@ __global__ void __launch_bounds__(kThreads)
             khi[d] = okey(lo + ldg(g.dxv[d] + I[d]) / 2.0);  // quadrant corner + dx/2
         }
         const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
+        // the cell's occupancy mask, kept for the passes' neighbourhood staging
+        const uint64_t live = live_mask(index, c, nc, g.max_xcell);
+        Ls.lm[c] = live;
         int count = 0;
-        for (int s = 0; s < g.max_xcell && count < min_xq; ++s) {
-            const int64_t a = c + nc * s;
-            if (!index[a]) continue;
+        for (uint64_t m = live; m && count < min_xq; m &= m - 1) {
+            const int64_t a = c + nc * (__ffsll((long long)m) - 1);
             bool in = true;
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
@@ -336,8 +339,8 @@ __device__ __forceinline__ double candidate_ss(const DevGrid& g, const Coords& X
 // those, and any candidate too far from the cell for the bound to hold, are
 // evaluated exactly in FP64, then sqrt decides the tie-break as in the reference.
 template <int DIM>
-__device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __restrict__ index, const Args& A,
-                                 uint32_t call, int64_t c, const Hood<DIM>& H, int lane, int* errs)
+__device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __restrict__ index, uint64_t* lm,
+                                 const Args& A, uint32_t call, int64_t c, const Hood<DIM>& H, int lane, int* errs)
 {
     const int64_t nc = g.ncells;
     const int M = g.max_xcell;
@@ -363,21 +366,50 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
     bool screen_ok = true;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) screen_ok &= hmax[d] >= 1e-12f && hmax[d] <= 1e12f;
-    // stage the neighbourhood
-    for (int o = lane; o < ncand; o += 32) {
-        const int nb = o / M, s = o - nb * M;
-        const int64_t J[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1, DIM == 3 ? I[2] + nb / 9 - 1 : 0};
-        bool ok = J[0] >= 0 && J[1] >= 0 && J[0] < g.n[0] && J[1] < g.n[1] &&
-                  (DIM == 2 || (J[2] >= 0 && J[2] < g.n[2]));
-        uint8_t live = 0;
+    // Stage the neighbourhood. The occupancy comes from the flag pass's
+    // per-cell masks (one load per neighbour cell); the coordinates of the
+    // live candidates are loaded in batches, all loads of a batch in flight
+    // together, then converted and stored.
+    int64_t nbc = 0;
+    uint64_t nbm = 0;
+    if (lane < NB) {
+        const int64_t J[3] = {I[0] + lane % 3 - 1, I[1] + (lane / 3) % 3 - 1, DIM == 3 ? I[2] + lane / 9 - 1 : 0};
+        const bool ok = J[0] >= 0 && J[1] >= 0 && J[0] < g.n[0] && J[1] < g.n[1] &&
+                        (DIM == 2 || (J[2] >= 0 && J[2] < g.n[2]));
         if (ok) {
-            const int64_t a = cell_linear<DIM>(g, J) + nc * s;
-            live = index[a];
-            if (live) {
+            nbc = cell_linear<DIM>(g, J);
+            nbm = lm[nbc];
+        }
+    }
+    constexpr int B = 6;
+    for (int base = 0; base < ncand; base += 32 * B) {
+        double xs[B][DIM];
+        bool lv[B];
+        int64_t av[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int o = base + 32 * u + lane;
+            const int nb = o / M, s = o - nb * M;
+            const uint64_t m = __shfl_sync(0xffffffffu, nbm, nb < NB ? nb : 0);
+            const int64_t cc = __shfl_sync(0xffffffffu, nbc, nb < NB ? nb : 0);
+            lv[u] = o < ncand && ((m >> s) & 1ull);
+            av[u] = cc + nc * s;
+            if (lv[u]) {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) xs[u][d] = X.c[d][av[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int o = base + 32 * u + lane;
+            if (o >= ncand) continue;
+            const int nb = o / M, s = o - nb * M;
+            uint8_t live = 0;
+            if (lv[u]) {
                 bool far = false;
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) {
-                    const double x = X.c[d][a];
+                    const double x = xs[u][d];
                     const float r = (float)(x - corner[d]);
                     H.r[d][o] = r;
                     far |= (!(fabsf(r) <= 4.0f * hmax[d]) && !isnan(r)) || !screen_ok;
@@ -385,8 +417,8 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
                 }
                 live = far ? 2 : 1;
             }
+            H.live[o] = live;
         }
-        H.live[o] = live;
     }
     __syncwarp();
     // E: bound on |ss32 - ss64| for screened candidates (|r| <= 4h, new point inside the cell)
@@ -513,6 +545,12 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
             if (count >= min_xq) break;
         }
     }
+    // the cell's occupancy after its injections, for the later passes' staging
+    __syncwarp();
+    const bool o0 = lane < M && H.live[base + lane];
+    const bool o1 = lane + 32 < M && H.live[base + lane + 32];
+    const uint64_t own = (uint64_t)__ballot_sync(0xffffffffu, o0) | ((uint64_t)__ballot_sync(0xffffffffu, o1) << 32);
+    if (lane == 0) lm[c] = own;
 }
 
 // One colour pass: warps take the colour's listed cells in turn.
@@ -540,13 +578,27 @@ __global__ void inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Ar
     int errs = 0;
     for (int k = gw; k < count; k += nwarps) {
         const int64_t c = Ls.list[Ls.off[col] + k];
-        inject_cell_warp<DIM>(g, X, index, A, call, c, H, lane, &errs);
+        inject_cell_warp<DIM>(g, X, index, Ls.lm, A, call, c, H, lane, &errs);
         __syncwarp();
     }
     raise_err(d_err, errs);
 }
 
 // ------------------------------------------------------------ launchers
+cudaError_t ensure_inject_scratch(jp_particles* P)
+{
+    if (P->inject.counts) return cudaSuccess;
+    const int64_t nc = P->g.ncells;
+    const size_t list_bytes = ((8 + (size_t)nc) * sizeof(int) + 7) & ~(size_t)7;
+    char* base = nullptr;
+    cudaError_t e = cudaMalloc(&base, list_bytes + (size_t)nc * sizeof(uint64_t));
+    if (e != cudaSuccess) return e;
+    P->inject.counts = (int*)base;
+    P->inject.list = P->inject.counts + 8;
+    P->inject.lm = (uint64_t*)(base + list_bytes);
+    return cudaSuccess;
+}
+
 cudaError_t ensure_move_scratch(jp_particles* P, int comps)
 {
     MoveScratch& m = P->move;
@@ -628,14 +680,12 @@ cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* ind
 {
     const int N = P->g.ndim;
     const int64_t nc = P->g.ncells;
-    if (!P->inject.counts) {
-        cudaError_t e = cudaMalloc(&P->inject.counts, (8 + nc) * sizeof(int));
-        if (e != cudaSuccess) return e;
-        P->inject.list = P->inject.counts + 8;
-    }
+    cudaError_t e = ensure_inject_scratch(P);
+    if (e != cudaSuccess) return e;
     InjectLists Ls;
     Ls.counts = P->inject.counts;
     Ls.list = P->inject.list;
+    Ls.lm = P->inject.lm;
     // colour regions: cells whose index parity along every axis is fixed
     int64_t cnt[3][2];
     for (int d = 0; d < 3; ++d)
@@ -646,7 +696,7 @@ cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* ind
         off += cnt[0][col & 1] * cnt[1][(col >> 1) & 1] * cnt[2][(col >> 2) & 1];
     }
     cudaStream_t st = P->stream;
-    cudaError_t e = cudaMemsetAsync(P->inject.counts, 0, 8 * sizeof(int), st);
+    e = cudaMemsetAsync(P->inject.counts, 0, 8 * sizeof(int), st);
     if (e != cudaSuccess) return e;
     Coords X{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};
     CCoords CX{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};

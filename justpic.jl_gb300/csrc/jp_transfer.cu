@@ -1,6 +1,7 @@
 // jp_transfer.cu -- the transfers beside the hot path that work on the same
 // layout: grid2particle_flip! (PIC/FLIP blend), centroid2particle! and
-// particle2centroid! (cell-centred fields), FP64, 2D and 3D.
+// particle2centroid! (cell-centred fields), and the phase ratios of
+// update_phase_ratios!, FP64, 2D and 3D.
 //
 // Each follows the reference's operation order (fma at its muladd sites), so
 // the results are bit-identical to the CPU oracle; see the kernel comments for
@@ -187,6 +188,188 @@ __global__ void __launch_bounds__(kThreads)
     F[c] = DIM == 2 ? wF / w : wF * (1.0 / w);
 }
 
+// ---------------------------------------------------------- phase ratios
+// update_phase_ratios! (src/PhaseRatios/): the fraction of each phase (ids
+// 1..nph in a per-slot field) around cell centres, vertices and faces, as a
+// bilinear-weight average of the nearby particles. One thread per output
+// node, particles and phases in the reference's order, so the sums are
+// bit-identical to the CPU oracle. Output: out[k * nodes + node].
+constexpr int kMaxPhases = 16;
+
+template <int DIM>
+__device__ __forceinline__ double bilinear_weight(const double* a, const double* b, const double* idi)
+{
+    double val = 1.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) val *= fma(-fabs(a[d] - b[d]), idi[d], 1.0);
+    return val;
+}
+
+__device__ __forceinline__ void accumulate_phase(double* w, int nph, double x, double ph)
+{
+    for (int k = 0; k < nph; ++k)
+        if (ph == (double)(k + 1)) w[k] = w[k] + x;
+}
+
+__device__ __forceinline__ void store_normalised(double* w, int nph, double* out, int64_t node, int64_t nodes,
+                                                 bool nan_to_zero)
+{
+    double s = w[0];
+    for (int k = 1; k < nph; ++k) s = s + w[k];
+    const double is = 1.0 / s;
+    for (int k = 0; k < nph; ++k) {
+        const double v = w[k] * is;
+        out[node + nodes * k] = (nan_to_zero && isnan(v)) ? 0.0 : v;
+    }
+}
+
+// src/PhaseRatios/centers.jl:3-30 with phase_ratio_weights (utils.jl:44-61):
+// the cell's own slots whose first coordinate is not NaN.
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    phase_center_kernel(DevGrid g, int nph, const double* __restrict__ phases, CCoords X, double* __restrict__ out)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    double xc[3], idi[3], w[kMaxPhases];
+    for (int k = 0; k < kMaxPhases; ++k) w[k] = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        xc[d] = ldg(g.xc[d] + I[d]);
+        idi[d] = ldg(g.ixv[d] + I[d]);
+    }
+    for (int s = 0; s < g.max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        double p[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) p[d] = X.c[d][a];
+        if (is_nan_bits(p[0])) continue;
+        accumulate_phase(w, nph, bilinear_weight<DIM>(xc, p, idi), phases[a]);
+    }
+    store_normalised(w, nph, out, c, nc, false);
+}
+
+// src/PhaseRatios/vertices.jl:14-107: the 2^N cells around the vertex (offsets
+// -1..0, first axis outermost), particles within half a cell of it.
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    phase_vertex_kernel(DevGrid g, int nph, const double* __restrict__ phases, CCoords X, double* __restrict__ out)
+{
+    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1, V2 = DIM == 3 ? g.n[2] + 1 : 1;
+    const int64_t nv = V0 * V1 * V2;
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const int64_t nc = g.ncells;
+    const int64_t I[3] = {v % V0, (v / V0) % V1, v / (V0 * V1)};
+    double xv[3], w[kMaxPhases];
+    for (int k = 0; k < kMaxPhases; ++k) w[k] = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) xv[d] = ldg(g.xv[d] + I[d]);
+    for (int oi = -1; oi <= 0; ++oi)
+        for (int oj = -1; oj <= 0; ++oj)
+            for (int ok = (DIM == 3 ? -1 : 0); ok <= 0; ++ok) {
+                const int64_t J[3] = {I[0] + oi, I[1] + oj, DIM == 3 ? I[2] + ok : 0};
+                if (J[0] < 0 || J[0] >= g.n[0] || J[1] < 0 || J[1] >= g.n[1]) continue;
+                if (DIM == 3 && (J[2] < 0 || J[2] >= g.n[2])) continue;
+                const int64_t c = cell_linear<DIM>(g, J);
+                double di[3], idi[3];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    di[d] = ldg(g.dxv[d] + J[d]);
+                    idi[d] = ldg(g.ixv[d] + J[d]);
+                }
+                for (int s = 0; s < g.max_xcell; ++s) {
+                    const int64_t a = c + nc * s;
+                    double p[3];
+                    bool nan = false, far = false;
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) {
+                        p[d] = X.c[d][a];
+                        nan |= is_nan_bits(p[d]);
+                    }
+                    if (nan) continue;
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) far |= fabs(p[d] - xv[d]) >= di[d] / 2.0;
+                    if (far) continue;
+                    accumulate_phase(w, nph, bilinear_weight<DIM>(xv, p, idi), phases[a]);
+                }
+            }
+    store_normalised(w, nph, out, v, nv, false);
+}
+
+template <int DIM>
+__device__ __forceinline__ void face_cell(const DevGrid& g, int nph, const double* __restrict__ phases,
+                                          const CCoords& X, int64_t c, const double* xf, const double* di,
+                                          const double* idi, double* w)
+{
+    const int64_t nc = g.ncells;
+    for (int s = 0; s < g.max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        double p[3];
+        bool nan = false, in = true;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            p[d] = X.c[d][a];
+            nan |= is_nan_bits(p[d]);
+        }
+        if (nan) continue;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) in &= fabs(p[d] - xf[d]) <= di[d] / 2.0;  // isinhalfcell, utils.jl:79
+        if (!in) continue;
+        accumulate_phase(w, nph, bilinear_weight<DIM>(xf, p, idi), phases[a]);
+    }
+}
+
+// src/PhaseRatios/midpoints.jl:19-94 along axis `dim`, one thread per cell I:
+// face I + e gathers cells I and min(I + e, n) (the last cell twice at the far
+// boundary, as the reference does); the first cell also writes face I, with
+// the spacing the loop left behind. Faces without particles get 0.
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    phase_face_kernel(DevGrid g, int nph, const double* __restrict__ phases, CCoords X, int dim,
+                      double* __restrict__ out)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    int64_t F[3] = {g.n[0], g.n[1], DIM == 3 ? g.n[2] : 1};
+    F[dim] += 1;
+    const int64_t nf = F[0] * F[1] * F[2];
+    double xcen[3], xf[3], di[3], idi[3], w[kMaxPhases];
+    for (int k = 0; k < kMaxPhases; ++k) w[k] = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        xcen[d] = ldg(g.xc[d] + I[d]);
+        di[d] = ldg(g.dxv[d] + I[d]);
+        xf[d] = xcen[d] + (d == dim ? (di[d] * 1.0) / 2.0 : (di[d] * 0.0) / 2.0);
+    }
+    for (int it = 0; it < 2; ++it) {
+        int64_t J[3] = {I[0], I[1], I[2]};
+        if (it == 1) J[dim] = J[dim] + 1 < g.n[dim] ? J[dim] + 1 : g.n[dim] - 1;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            di[d] = ldg(g.dxv[d] + J[d]);
+            idi[d] = ldg(g.ixv[d] + J[d]);
+        }
+        face_cell<DIM>(g, nph, phases, X, cell_linear<DIM>(g, J), xf, di, idi, w);
+    }
+    int64_t Fi[3] = {I[0], I[1], I[2]};
+    Fi[dim] += 1;
+    store_normalised(w, nph, out, Fi[0] + F[0] * (Fi[1] + F[1] * Fi[2]), nf, true);
+    if (I[dim] == 0) {
+        double xb[3], wb[kMaxPhases];
+        for (int k = 0; k < kMaxPhases; ++k) wb[k] = 0.0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xb[d] = xcen[d] - (d == dim ? (di[d] * 1.0) / 2.0 : (di[d] * 0.0) / 2.0);
+        face_cell<DIM>(g, nph, phases, X, c, xb, di, idi, wb);
+        store_normalised(wb, nph, out, I[0] + F[0] * (I[1] + F[1] * I[2]), nf, true);
+    }
+}
+
 // ------------------------------------------------------------ launchers
 cudaError_t launch_g2p_flip(jp_particles* P, double* Fp, const double* F, const double* F0, double alpha,
                             const double* const coords[3], const uint8_t* index)
@@ -224,6 +407,28 @@ cudaError_t launch_p2c(jp_particles* P, double* F, const double* Fp, const doubl
         p2c_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X);
     else
         p2c_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phase_ratios(jp_particles* P, int nph, const double* phases, const double* const coords[3],
+                                double* center, double* vertex, double* const faces[3])
+{
+    const bool d3 = P->g.ndim == 3;
+    CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
+    cudaStream_t st = P->stream;
+    const unsigned nb = grid_blocks(P->g.ncells);
+    const int64_t nv = (P->g.n[0] + 1) * (P->g.n[1] + 1) * (d3 ? P->g.n[2] + 1 : 1);
+    if (d3) {
+        if (center) phase_center_kernel<3><<<nb, kThreads, 0, st>>>(P->g, nph, phases, X, center);
+        if (vertex) phase_vertex_kernel<3><<<grid_blocks(nv), kThreads, 0, st>>>(P->g, nph, phases, X, vertex);
+        for (int d = 0; d < 3; ++d)
+            if (faces && faces[d]) phase_face_kernel<3><<<nb, kThreads, 0, st>>>(P->g, nph, phases, X, d, faces[d]);
+    } else {
+        if (center) phase_center_kernel<2><<<nb, kThreads, 0, st>>>(P->g, nph, phases, X, center);
+        if (vertex) phase_vertex_kernel<2><<<grid_blocks(nv), kThreads, 0, st>>>(P->g, nph, phases, X, vertex);
+        for (int d = 0; d < 2; ++d)
+            if (faces && faces[d]) phase_face_kernel<2><<<nb, kThreads, 0, st>>>(P->g, nph, phases, X, d, faces[d]);
+    }
     return cudaGetLastError();
 }
 

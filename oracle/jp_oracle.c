@@ -716,6 +716,183 @@ void jpo_particle2centroid(const jpo_grid* g, double* F, const double* Fp, const
     }
 }
 
+/* ---------------------------------------------------------- phase ratios */
+
+#define JPO_MAX_PHASES 16
+
+/* bilinear_weight (src/PhaseRatios/utils.jl:64-74): prod_d muladd(-|a_d - b_d|, inv(di_d), 1) */
+static inline double bilinear_weight(int N, const double* a, const double* b, const double* di)
+{
+    double val = 1.0;
+    for (int d = 0; d < N; ++d) val *= fma(-fabs(a[d] - b[d]), 1.0 / di[d], 1.0);
+    return val;
+}
+
+/* w .* inv(sum(w)) with sum a left fold over the phases */
+static inline void normalise(int nph, double* w)
+{
+    double s = w[0];
+    for (int k = 1; k < nph; ++k) s = s + w[k];
+    const double is = 1.0 / s;
+    for (int k = 0; k < nph; ++k) w[k] = w[k] * is;
+}
+
+/* w .+ x .* ntuple(j -> ph == j) (src/PhaseRatios/utils.jl:55-58): only the
+   matching phase moves (the others add a signed zero) */
+static inline void accumulate_weight(int nph, double* w, double x, double ph)
+{
+    for (int k = 0; k < nph; ++k)
+        if (ph == (double)(k + 1)) w[k] = w[k] + x;
+}
+
+static inline void cell_spacing(const jpo_grid* g, const int64_t* J, double* di)
+{
+    for (int d = 0; d < g->ndim; ++d) di[d] = g->dxv[d][J[d]];
+}
+
+/* phase_ratios_center! (src/PhaseRatios/centers.jl:3-30, phase_ratio_weights
+   utils.jl:44-61): the cell's own particles, weight at the cell centre with
+   the cell's vertex spacing; slots skipped when their first coordinate is NaN. */
+void jpo_phase_ratios_center(const jpo_grid* g, int nph, const double* phases, const double* const coords[3],
+                             double* out)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t c = 0; c < nc; ++c) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        double xc[3], di[3], w[JPO_MAX_PHASES] = {0};
+        for (int d = 0; d < N; ++d) xc[d] = g->xc[d][I[d]];
+        cell_spacing(g, I, di);
+        for (int s = 0; s < M; ++s) {
+            const int64_t a = c + nc * s;
+            double p[3] = {0.0, 0.0, 0.0};
+            for (int d = 0; d < N; ++d) p[d] = coords[d][a];
+            if (isnan(p[0])) continue;
+            accumulate_weight(nph, w, bilinear_weight(N, xc, p, di), phases[a]);
+        }
+        normalise(nph, w);
+        for (int k = 0; k < nph; ++k) out[c + nc * k] = w[k];
+    }
+}
+
+/* phase_ratios_vertex! (src/PhaseRatios/vertices.jl:4-107): particles of the
+   2^N cells around the vertex (offsets -1..0, the first axis outermost), those
+   within half a cell of it on every axis, weight with each cell's spacing. */
+void jpo_phase_ratios_vertex(const jpo_grid* g, int nph, const double* phases, const double* const coords[3],
+                             double* out)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int64_t V0 = g->n[0] + 1, V1 = g->n[1] + 1, V2 = N == 3 ? g->n[2] + 1 : 1;
+    const int64_t nv = V0 * V1 * V2;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t v = 0; v < nv; ++v) {
+        const int64_t I[3] = {v % V0, (v / V0) % V1, v / (V0 * V1)};
+        double xv[3], w[JPO_MAX_PHASES] = {0};
+        for (int d = 0; d < N; ++d) xv[d] = g->xv[d][I[d]];
+        for (int oi = -1; oi <= 0; ++oi)
+            for (int oj = -1; oj <= 0; ++oj)
+                for (int ok = (N == 3 ? -1 : 0); ok <= 0; ++ok) {
+                    const int64_t J[3] = {I[0] + oi, I[1] + oj, N == 3 ? I[2] + ok : 0};
+                    if (J[0] < 0 || J[0] >= g->n[0] || J[1] < 0 || J[1] >= g->n[1]) continue;
+                    if (N == 3 && (J[2] < 0 || J[2] >= g->n[2])) continue;
+                    const int64_t c = J[0] + g->n[0] * (J[1] + g->n[1] * J[2]);
+                    double di[3];
+                    cell_spacing(g, J, di);
+                    for (int s = 0; s < M; ++s) {
+                        const int64_t a = c + nc * s;
+                        double p[3];
+                        int nan = 0, far = 0;
+                        for (int d = 0; d < N; ++d) {
+                            p[d] = coords[d][a];
+                            nan |= isnan(p[d]);
+                        }
+                        if (nan) continue;
+                        for (int d = 0; d < N && !far; ++d) far = fabs(p[d] - xv[d]) >= di[d] / 2.0;
+                        if (far) continue;
+                        accumulate_weight(nph, w, bilinear_weight(N, xv, p, di), phases[a]);
+                    }
+                }
+        normalise(nph, w);
+        for (int k = 0; k < nph; ++k) out[v + nv * k] = w[k];
+    }
+}
+
+/* isinhalfcell (src/PhaseRatios/utils.jl:79): |p_d - x_d| <= di_d / 2 on every axis */
+static inline int in_half_cell(int N, const double* p, const double* x, const double* di)
+{
+    int in = 1;
+    for (int d = 0; d < N; ++d) in &= fabs(p[d] - x[d]) <= di[d] / 2.0;
+    return in;
+}
+
+static void face_cell_particles(const jpo_grid* g, int nph, const double* phases, const double* const coords[3],
+                                int64_t c, const double* x, const double* di, double* w)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    for (int s = 0; s < g->max_xcell; ++s) {
+        const int64_t a = c + nc * s;
+        double p[3];
+        int nan = 0;
+        for (int d = 0; d < N; ++d) {
+            p[d] = coords[d][a];
+            nan |= isnan(p[d]);
+        }
+        if (nan || !in_half_cell(N, p, x, di)) continue;
+        accumulate_weight(nph, w, bilinear_weight(N, x, p, di), phases[a]);
+    }
+}
+
+/* phase_ratios_face! (src/PhaseRatios/midpoints.jl:3-94) along axis `dim`: per
+   cell I, the face I + e_dim gathers the particles of cells I and
+   min(I + e_dim, n) (the last cell twice at the far boundary, as the reference
+   does) within half a cell of the face; the first cell also writes face I
+   (the near boundary), with the spacing the loop left behind. Faces without
+   particles get 0. The output grid is n + e_dim. */
+void jpo_phase_ratios_face(const jpo_grid* g, int nph, const double* phases, const double* const coords[3],
+                           int dim, double* out)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    int64_t F[3] = {g->n[0], g->n[1], N == 3 ? g->n[2] : 1};
+    F[dim] += 1;
+    const int64_t nf = F[0] * F[1] * F[2];
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t c = 0; c < nc; ++c) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        double di[3], xf[3], w[JPO_MAX_PHASES] = {0};
+        cell_spacing(g, I, di);
+        for (int d = 0; d < N; ++d) xf[d] = g->xc[d][I[d]] + (d == dim ? (di[d] * 1.0) / 2.0 : (di[d] * 0.0) / 2.0);
+        double xcen[3];
+        for (int d = 0; d < N; ++d) xcen[d] = g->xc[d][I[d]];
+        for (int it = 0; it < 2; ++it) {
+            int64_t J[3] = {I[0], I[1], I[2]};
+            if (it == 1) J[dim] = J[dim] + 1 < g->n[dim] ? J[dim] + 1 : g->n[dim] - 1;
+            cell_spacing(g, J, di);
+            face_cell_particles(g, nph, phases, coords, J[0] + g->n[0] * (J[1] + g->n[1] * J[2]), xf, di, w);
+        }
+        normalise(nph, w);
+        int64_t Fi[3] = {I[0], I[1], I[2]};
+        Fi[dim] += 1;
+        const int64_t fo = Fi[0] + F[0] * (Fi[1] + F[1] * Fi[2]);
+        for (int k = 0; k < nph; ++k) out[fo + nf * k] = isnan(w[k]) ? 0.0 : w[k];
+        if (I[dim] == 0) {
+            double xb[3], wb[JPO_MAX_PHASES] = {0};
+            for (int d = 0; d < N; ++d) xb[d] = xcen[d] - (d == dim ? (di[d] * 1.0) / 2.0 : (di[d] * 0.0) / 2.0);
+            face_cell_particles(g, nph, phases, coords, c, xb, di, wb);
+            normalise(nph, wb);
+            const int64_t fb = I[0] + F[0] * (I[1] + F[1] * I[2]);
+            for (int k = 0; k < nph; ++k) out[fb + nf * k] = isnan(wb[k]) ? 0.0 : wb[k];
+        }
+    }
+}
+
 /* ---------------------------------------------------------- particle2grid! */
 
 void jpo_particle2grid(const jpo_grid* g, double* F, const double* Fp,

@@ -87,6 +87,15 @@ void jpo_centroid2particle(const jpo_grid* g, double* Fp, const double* F, const
 /* particle2centroid!: src/Interpolations/particle_to_grid_centroid.jl:10-45, :88-110 */
 void jpo_particle2centroid(const jpo_grid* g, double* F, const double* Fp, const double* const coords[3]);
 
+/* update_phase_ratios! pieces (src/PhaseRatios/): out[k * nodes + node] for
+   phases 1..nph (at most 16); phases are the per-slot phase ids */
+void jpo_phase_ratios_center(const jpo_grid* g, int nph, const double* phases, const double* const coords[3],
+                             double* out);
+void jpo_phase_ratios_vertex(const jpo_grid* g, int nph, const double* phases, const double* const coords[3],
+                             double* out);
+void jpo_phase_ratios_face(const jpo_grid* g, int nph, const double* phases, const double* const coords[3],
+                           int dim, double* out);
+
 /* forward-mode derivatives (jp_oracle_jvp.c): the same calls on (value,
    tangent) pairs; dV / dFp may be NULL (zero tangent) */
 int jpo_advection_jvp(const jpo_grid* g, int method, double alpha, const double* const V[3],

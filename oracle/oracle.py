@@ -81,6 +81,9 @@ def lib():
                                              P3, ctypes.c_void_p]
         L.jpo_centroid2particle.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3]
         L.jpo_particle2centroid.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3]
+        L.jpo_phase_ratios_center.argtypes = [G, ctypes.c_int, ctypes.c_void_p, P3, ctypes.c_void_p]
+        L.jpo_phase_ratios_vertex.argtypes = [G, ctypes.c_int, ctypes.c_void_p, P3, ctypes.c_void_p]
+        L.jpo_phase_ratios_face.argtypes = [G, ctypes.c_int, ctypes.c_void_p, P3, ctypes.c_int, ctypes.c_void_p]
         L.jpo_advection_jvp.argtypes = [G, ctypes.c_int, ctypes.c_double, P3, P3, ctypes.c_double, P3, P3,
                                         ctypes.c_void_p]
         L.jpo_advection_jvp.restype = ctypes.c_int
@@ -253,6 +256,25 @@ class OracleParticles:
     def particle2centroid(self, F, Fp):
         assert F.flags.f_contiguous and F.dtype == np.float64
         lib().jpo_particle2centroid(ctypes.byref(self._g), _ptr(F), _ptr(Fp), self._p3(self.coords))
+
+    # -- phase ratios (src/PhaseRatios/) ---------------------------------
+    def phase_ratios(self, phases, nphases):
+        """update_phase_ratios! without the 3D edge midpoints: dict of arrays
+        (nphases, nodes) for 'center', 'vertex' and the faces 'Vx', 'Vy' (, 'Vz');
+        node index column-major over the location's grid."""
+        N = self.ndim
+        G = ctypes.byref(self._g)
+        c3 = self._p3(self.coords)
+        out = {"center": np.zeros((nphases, self.ncells))}
+        lib().jpo_phase_ratios_center(G, int(nphases), _ptr(phases), c3, _ptr(out["center"]))
+        nv = int(np.prod([n + 1 for n in self.n]))
+        out["vertex"] = np.zeros((nphases, nv))
+        lib().jpo_phase_ratios_vertex(G, int(nphases), _ptr(phases), c3, _ptr(out["vertex"]))
+        for d, name in enumerate(["Vx", "Vy", "Vz"][:N]):
+            nf = int(np.prod([n + (1 if e == d else 0) for e, n in enumerate(self.n)]))
+            out[name] = np.zeros((nphases, nf))
+            lib().jpo_phase_ratios_face(G, int(nphases), _ptr(phases), c3, d, _ptr(out[name]))
+        return out
 
     # -- forward-mode derivatives (dual numbers through the same code) ----
     def advection_jvp(self, method, alpha, V, dV, dt, dcoords):

@@ -491,3 +491,39 @@ def test_c5_gradient_matches_oracle_jvp():
         d, _ = oracle_jvp_run(g, Vh, dV, dt, cfg["steps"], cfg["T"], cfg["T_target"], nxcell=cfg["nxcell"],
                               max_xcell=cfg["max_xcell"], min_xcell=cfg["min_xcell"])
         assert abs(gc[node] - d) <= 1e-9 * max(abs(d), gmax), (c, node, gc[node], d)
+
+
+# ------------------------------------------- split-precision (FP32) variant
+def _f32_case(ni=(32, 32), nsteps=20):
+    g, p, Vh, V, dt, T0, target, _ = _run_case(ni=ni, nsteps=nsteps)
+    xi = jp.init_offsets(p)
+    V32 = tuple(v.float() for v in V)
+    T0f = jp.CellArray(T0.data.float().contiguous(), p.ni)
+    return g, p, V, V32, dt, T0, T0f, target, xi, nsteps
+
+
+@pytest.mark.parametrize("method", ["rk2", "rk4"])
+def test_f32_adjoint_agrees_with_fp64_adjoint(method):
+    """The split-precision run follows the FP64 run to FP32 rounding (a few
+    particles make other discrete choices), so its gradients must agree with
+    the FP64 adjoint's to FP32-form accuracy."""
+    g, p, V, V32, dt, T0, T0f, target, xi, nsteps = _f32_case()
+    _, pm, _ = METHODS[method]
+    l64, gV64, gT64 = A.misfit_gradient(p, pm, V, dt, nsteps, T0, target, checkpoint_every=5)
+    l32, gV32, gT32 = A.misfit_gradient_f32(p, xi, pm, V32, dt, nsteps, T0f, target.float(), checkpoint_every=5)
+    assert abs(l32 - l64) <= 2e-3 * l64
+    for a, b in zip(gV32 + (gT32.data,), gV64 + (gT64.data,)):
+        a, b = a.double().flatten(), b.double().flatten()
+        rel = float((a - b).norm() / b.norm())
+        cos = float((a @ b) / (a.norm() * b.norm()))
+        assert rel < 2e-2 and cos > 0.999, (rel, cos)
+
+
+def test_f32_adjoint_is_reproducible():
+    g, p, V, V32, dt, T0, T0f, target, xi, nsteps = _f32_case(ni=(24, 24), nsteps=8)
+    m = jp.RungeKutta2()
+    r1 = A.misfit_gradient_f32(p, xi, m, V32, dt, nsteps, T0f, target.float(), checkpoint_every=3)
+    r2 = A.misfit_gradient_f32(p, xi, m, V32, dt, nsteps, T0f, target.float(), checkpoint_every=4)
+    assert r1[0] == r2[0]
+    for a, b in zip(r1[1] + (r1[2].data,), r2[1] + (r2[2].data,)):
+        assert torch.equal(a, b)

@@ -3,6 +3,7 @@ centroid2particle!, particle2centroid!) against the CPU oracle, bit for bit,
 on particles that have been advected, moved and re-injected."""
 import numpy as np
 import pytest
+import torch
 
 from _harness import Pair, W, assert_bits_equal, jp, refined_grid
 
@@ -55,8 +56,35 @@ def test_centroid_transfers_bit_exact(ni, refined):
 
 
 def test_centroid_transfers_reject_single_cell_axes():
-    g = W.grid((1, 4))
-    p = jp.init_particles(jp.CUDABackend, 4, 4, 1, *g["grid_v"])
+    # one cell along x: the centre grid has a single node, nothing to interpolate between
+    xv, yv = np.array([0.0, 1.0]), np.linspace(0.0, 1.0, 5)
+    xc, yc = np.array([0.5]), 0.5 * (yv[1:] + yv[:-1])
+
+    def expand(x, d):
+        return np.concatenate([[x[0] - d], x, [x[-1] + d]])
+
+    grids = ((xv, expand(yc, 0.25)), (expand(xc, 1.0), yv))
+    p = jp.init_particles(jp.CUDABackend, 4, 4, 1, *grids)
     (pT,) = jp.init_cell_arrays(p, 1)
     with pytest.raises(jp.ArgumentError):
         jp.centroid2particle_(pT, jp.grid_field((1, 4)), p)
+    with pytest.raises(jp.ArgumentError):
+        jp.particle2centroid_(jp.grid_field((1, 4)), pT, p)
+
+
+@pytest.mark.parametrize("ni,refined", CASES)
+@pytest.mark.parametrize("nphases", [2, 3])
+def test_phase_ratios_bit_exact(ni, refined, nphases):
+    pair, g = _moved_pair(ni, refined)
+    live = pair.o.index.astype(bool)
+    # phase ids from the particles' position: bands along the last axis, ids 1..nphases
+    ph = np.floor(pair.o.coords[len(ni) - 1] * nphases) + 1.0
+    ph = np.where(live, np.clip(ph, 1, nphases), np.nan)
+    ref = pair.o.phase_ratios(ph, nphases)
+    phases = jp.CellArray(torch.from_numpy(np.ascontiguousarray(ph)).cuda(), pair.p.ni)
+    pr = jp.PhaseRatios(nphases, ni)
+    jp.update_phase_ratios_(pr, pair.p, phases)
+    assert_bits_equal(ref["center"], pr.center.cpu().numpy(), "center")
+    assert_bits_equal(ref["vertex"], pr.vertex.cpu().numpy(), "vertex")
+    for d, name in enumerate(["Vx", "Vy", "Vz"][:len(ni)]):
+        assert_bits_equal(ref[name], pr.faces[d].cpu().numpy(), name)
