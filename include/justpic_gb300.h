@@ -153,6 +153,19 @@ int jp_move_particles_noalloc(jp_particles* p, double* const coords[3], uint8_t*
 int jp_inject_particles(jp_particles* p, double* const coords[3], uint8_t* index,
                         double* const* args, int32_t nargs);
 
+/*
+ * inject_particles_phase! (src/Particles/injection.jl:133-325): as
+ * jp_inject_particles, but every quadrant of a cell is checked, a new
+ * particle takes the phase id (per-slot FP64 field `phases`) of its nearest
+ * neighbour, and particle field args[k] takes the clamped N-linear
+ * interpolation of grid field fields[k] at the new particle: cell-centred
+ * (shape ni, column-major) when centred[k] != 0, else on the vertices (shape
+ * ni + 1). Shares the injection call counter with jp_inject_particles.
+ */
+int jp_inject_particles_phase(jp_particles* p, double* const coords[3], uint8_t* index, double* phases,
+                              double* const* args, const double* const* fields, const int32_t* centred,
+                              int32_t nargs);
+
 /* grid2particle! (src/Interpolations/grid_to_particle.jl:26-45): vertex field F
    (n0+1 x n1+1 (x n2+1)) to the live slots of Fp. */
 int jp_grid2particle(jp_particles* p, double* Fp, const double* F, const double* const coords[3],

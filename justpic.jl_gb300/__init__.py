@@ -23,6 +23,7 @@ from .api import (  # noqa: F401
     PhaseRatios,
     update_phase_ratios_,
     inject_particles_,
+    inject_particles_phase_,
     move_particles_,
     particle2grid_,
     set_synchronous,

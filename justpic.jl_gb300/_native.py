@@ -76,6 +76,9 @@ SIGNATURES = [
     ("jp_move_particles_noalloc", ctypes.c_int,
      [ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     ("jp_inject_particles", ctypes.c_int, [ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    ("jp_inject_particles_phase", ctypes.c_int,
+     [ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+      ctypes.c_int32]),
     ("jp_grid2particle", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
     ("jp_particle2grid", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),
     # split-precision (FP32 cell offset) form

@@ -2,15 +2,16 @@
 
 Julia's in-place ``f!`` becomes ``f_`` here (PyTorch's in-place convention):
 
-=====================  ===============================================
-Python                 reference
-=====================  ===============================================
-``advection_``         ``advection!`` (src/Particles/Advection/advection.jl:21)
-``move_particles_``    ``move_particles!`` (src/Particles/move_safe.jl:21)
-``inject_particles_``  ``inject_particles!`` (src/Particles/injection.jl:19)
-``grid2particle_``     ``grid2particle!`` (src/Interpolations/grid_to_particle.jl:26)
-``particle2grid_``     ``particle2grid!`` (src/Interpolations/particle_to_grid.jl:23)
-=====================  ===============================================
+===========================  ==============================================================
+Python                       reference
+===========================  ==============================================================
+``advection_``               ``advection!`` (src/Particles/Advection/advection.jl:21)
+``move_particles_``          ``move_particles!`` (src/Particles/move_safe.jl:21)
+``inject_particles_``        ``inject_particles!`` (src/Particles/injection.jl:19)
+``inject_particles_phase_``  ``inject_particles_phase!`` (src/Particles/injection.jl:133)
+``grid2particle_``           ``grid2particle!`` (src/Interpolations/grid_to_particle.jl:26)
+``particle2grid_``           ``particle2grid!`` (src/Interpolations/particle_to_grid.jl:23)
+===========================  ==============================================================
 
 Calls are synchronous (like the reference's ``launch!``) unless
 ``set_synchronous(particles, False)`` was called; kernels run on PyTorch's
@@ -138,6 +139,33 @@ def inject_particles_(particles: Particles, args=()) -> None:
     rc = _native.load().jp_inject_particles(particles.handle, _coords(particles), particles.index.data_ptr(),
                                             arr, n)
     _finish(particles, rc, "inject_particles!")
+
+
+def inject_particles_phase_(particles: Particles, particles_phases: CellArray, args=(), fields=()) -> None:
+    """``inject_particles_phase!(particles, particles_phases, args, fields, grid)``
+    (src/Particles/injection.jl:133): reseed every under-populated quadrant;
+    a new particle takes the phase of its nearest neighbour and ``args[k]``
+    the clamped interpolation of grid field ``fields[k]`` (cell-centred when
+    its shape is the cells', else on the vertices). The grid is the one the
+    particles were made on."""
+    _check_cellarray(particles, particles_phases, "particles_phases")
+    arr, n = _args(particles, args)
+    fields = tuple(fields) if fields is not None else ()
+    if len(fields) != n:
+        raise ArgumentError("args and fields must have the same length")
+    centred = []
+    for k, f in enumerate(fields):
+        c = isinstance(f, torch.Tensor) and tuple(f.shape) == tuple(particles.ni)
+        _check_grid(f, tuple(particles.ni) if c else _vertex_shape(particles), f"fields[{k}]")
+        if c and min(particles.ni) < 2:
+            raise ArgumentError(f"fields[{k}]: a cell-centred field needs at least 2 cells per axis")
+        centred.append(1 if c else 0)
+    fp = (ctypes.c_void_p * max(1, n))(*[f.data_ptr() for f in fields])
+    cf = (ctypes.c_int32 * max(1, n))(*centred)
+    _bind_stream(particles)
+    rc = _native.load().jp_inject_particles_phase(particles.handle, _coords(particles), particles.index.data_ptr(),
+                                                  particles_phases.data_ptr(), arr, fp, cf, n)
+    _finish(particles, rc, "inject_particles_phase!")
 
 
 def _vertex_shape(p: Particles):

@@ -364,6 +364,29 @@ int jp_inject_particles(jp_particles* P, double* const coords[3], uint8_t* index
     return finish(P, jp::launch_inject(P, coords, index, args, nargs, call), "jp_inject_particles");
 }
 
+int jp_inject_particles_phase(jp_particles* P, double* const coords[3], uint8_t* index, double* phases,
+                              double* const* args, const double* const* fields, const int32_t* centred,
+                              int32_t nargs)
+{
+    if (!P || !index || !phases || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_particles_phase: null pointer");
+    if (nargs < 0 || nargs > JP_MAX_ARGS || (nargs > 0 && (!args || !fields || !centred)))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_particles_phase: bad field list");
+    int cflags[JP_MAX_ARGS] = {0};
+    for (int k = 0; k < nargs; ++k) {
+        if (!args[k] || !fields[k]) return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_particles_phase: null field");
+        cflags[k] = centred[k] != 0;
+        // a centred field needs two centres per axis to interpolate between
+        for (int d = 0; d < P->g.ndim && cflags[k]; ++d)
+            if (P->g.n[d] < 2)
+                return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_particles_phase: centred field on a 1-cell axis");
+    }
+    const uint32_t call = (uint32_t)P->inject_calls;
+    P->inject_calls += 1;
+    return finish(P, jp::launch_inject_phase(P, coords, index, phases, args, fields, cflags, nargs, call),
+                  "jp_inject_particles_phase");
+}
+
 // ---- split-precision form ----------------------------------------------
 static int check_f32(const jp_particles* P, const void* const* xi, const void* index, const char* what)
 {

@@ -320,6 +320,9 @@ cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index
                         double* const* args, int nargs);
 cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* index,
                           double* const* args, int nargs, uint32_t call);
+cudaError_t launch_inject_phase(jp_particles* P, double* const coords[3], uint8_t* index, double* phases,
+                                double* const* args, const double* const* fields, const int* centred, int nargs,
+                                uint32_t call);
 cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const double* const coords[3],
                        const uint8_t* index);
 // transfers beside the hot path (jp_transfer.cu)

@@ -231,9 +231,13 @@ __device__ __forceinline__ int colour_of(const int64_t* I)
     return (int)(I[0] & 1) + 2 * (int)(I[1] & 1) + (DIM == 3 ? 4 * (int)(I[2] & 1) : 0);
 }
 
-// first-quadrant occupancy test (injection.jl:81-100 for the first vertex);
-// flagged cells are appended to their colour's list.
-template <int DIM>
+// Occupancy test of a cell before its pass: inject_particles! only works on a
+// cell whose first quadrant is short (injection.jl:81-100 stops at the first
+// quadrant that is not), inject_particles_phase! (PHASE) on a cell with any
+// short quadrant (injection.jl:262-280). A cell's own slots change only in its
+// own pass, so the test on the state before the colour passes is exact.
+// Flagged cells are appended to their colour's list.
+template <int DIM, bool PHASE>
 __global__ void __launch_bounds__(kThreads)
     inject_flag(DevGrid g, CCoords X, const uint8_t* __restrict__ index, InjectLists Ls)
 {
@@ -257,8 +261,39 @@ __global__ void __launch_bounds__(kThreads)
         // the cell's occupancy mask, kept for the passes' neighbourhood staging
         const uint64_t live = live_mask(index, c, nc, g.max_xcell);
         Ls.lm[c] = live;
-        int count = 0;
-        for (uint64_t m = live; m && count < min_xq; m &= m - 1) {
+        if (PHASE) {
+            // upper halves: corner + dx/2 .. corner + dx/2 + dx/2 (quadrant_corners, injection.jl:442-466)
+            long long klo1[3], khi1[3];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const double lo = ldg(g.xv[d] + I[d]) + ldg(g.dxv[d] + I[d]) / 2.0;
+                klo1[d] = okey(lo);
+                khi1[d] = okey(lo + ldg(g.dxv[d] + I[d]) / 2.0);
+            }
+            int cq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (uint64_t m = live; m; m &= m - 1) {
+                const int64_t a = c + nc * (__ffsll((long long)m) - 1);
+                unsigned in0 = 0, in1 = 0;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const double x = X.c[d][a];
+                    const long long k = okey(x);
+                    const bool ok = !is_nan_bits(x);
+                    in0 |= (unsigned)(ok & (klo[d] < k) & (k < khi[d])) << d;
+                    in1 |= (unsigned)(ok & (klo1[d] < k) & (k < khi1[d])) << d;
+                }
+#pragma unroll
+                for (int q = 0; q < (1 << DIM); ++q) {
+                    // quadrant q takes the upper half along axis d when bit d of q is set
+                    const unsigned need = (unsigned)q, full = (1u << DIM) - 1u;
+                    cq[q] += (((in1 & need) | (in0 & ~need & full)) == full) ? 1 : 0;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < (1 << DIM); ++q) flag |= cq[q] < min_xq;
+        } else {
+            int count = 0;
+            for (uint64_t m = live; m && count < min_xq; m &= m - 1) {
             const int64_t a = c + nc * (__ffsll((long long)m) - 1);
             bool in = true;
 #pragma unroll
@@ -268,8 +303,9 @@ __global__ void __launch_bounds__(kThreads)
                 in = in & !is_nan_bits(x) & (klo[d] < k) & (k < khi[d]);
             }
             count += in ? 1 : 0;
+            }
+            flag = count < min_xq;
         }
-        flag = count < min_xq;
     }
     const unsigned active = __ballot_sync(0xffffffffu, flag);
     if (flag) {
@@ -338,9 +374,75 @@ __device__ __forceinline__ double candidate_ss(const DevGrid& g, const Coords& X
 // (min + E)(1 + tol) + E can be at (or within rounding of) the FP64 minimum;
 // those, and any candidate too far from the cell for the bound to hold, are
 // evaluated exactly in FP64, then sqrt decides the tie-break as in the reference.
+// Grid fields that inject_particles_phase! interpolates onto new particles
+// (one per particle field of Args), each cell-centred or on the vertices.
+struct PhaseFields {
+    const double* f[JP_MAX_ARGS];
+    int centred[JP_MAX_ARGS];
+    double* phases;  // per-slot phase ids, copied from the nearest neighbour
+};
+
+// Julia's min / max on floats: NaN wins, -0.0 is below +0.0
+__device__ __forceinline__ double jl_min(double x, double y)
+{
+    return ((y < x) || (signbit(y) && !signbit(x))) ? (isnan(x) ? x : y) : (isnan(y) ? y : x);
+}
+__device__ __forceinline__ double jl_max(double x, double y)
+{
+    return ((y > x) || (!signbit(y) && signbit(x))) ? (isnan(x) ? x : y) : (isnan(y) ? y : x);
+}
+
+// src/Particles/injection.jl:300-318: the clamped N-linear interpolation of a
+// cell-centred (centre cell below p, clamped; centre spacing) or vertex field
+// (the particle's own cell) at the new particle.
 template <int DIM>
+__device__ double phase_field_value(const DevGrid& g, const double* __restrict__ F, bool centred, const double* pn,
+                                    const int64_t* I, const double* corner, const double* dq)
+{
+    int64_t J[3] = {0, 0, 0};
+    double t[3];
+    int64_t L0, L1;
+    if (centred) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            const double xcen = corner[d] + dq[d];
+            int64_t j = pn[d] < xcen ? I[d] - 1 : I[d];
+            const int64_t hi = g.n[d] - 2;
+            j = j < 0 ? 0 : (j > hi ? hi : j);
+            J[d] = j;
+            t[d] = (pn[d] - ldg(g.xc[d] + j)) * ldg(g.ixc[d] + j);
+        }
+        L0 = g.n[0];
+        L1 = g.n[1];
+    } else {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            J[d] = I[d];
+            t[d] = (pn[d] - ldg(g.xv[d] + I[d])) * ldg(g.ixv[d] + I[d]);
+        }
+        L0 = g.n[0] + 1;
+        L1 = g.n[1] + 1;
+    }
+    const int64_t b = J[0] + L0 * (J[1] + (DIM == 3 ? L1 * J[2] : 0));
+    const int64_t sz = L0 * L1;
+    const int64_t off[8] = {b, b + 1, b + L0, b + L0 + 1, b + sz, b + sz + 1, b + sz + L0, b + sz + L0 + 1};
+    double v[8];
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); ++k) v[k] = ldg(F + off[k]);
+    const double tmp = lerpN<DIM>(v, t);
+    double lo = v[0], hi = v[0];
+#pragma unroll
+    for (int k = 1; k < (1 << DIM); ++k) {
+        hi = jl_max(v[k], hi);
+        lo = jl_min(v[k], lo);
+    }
+    return tmp > hi ? hi : (tmp < lo ? lo : tmp);
+}
+
+template <int DIM, bool PHASE>
 __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __restrict__ index, uint64_t* lm,
-                                 const Args& A, uint32_t call, int64_t c, const Hood<DIM>& H, int lane, int* errs)
+                                 const Args& A, const PhaseFields& PF, uint32_t call, int64_t c, const Hood<DIM>& H,
+                                 int lane, int* errs)
 {
     const int64_t nc = g.ncells;
     const int M = g.max_xcell;
@@ -450,7 +552,10 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
             cnt += in ? 1 : 0;
         }
         int count = __reduce_add_sync(0xffffffffu, cnt);
-        if (count >= min_xq) break;  // injection.jl:100
+        if (count >= min_xq) {
+            if (PHASE) continue;  // inject_particles_phase! checks every quadrant (injection.jl:273)
+            break;                // injection.jl:100
+        }
         const bool f0 = lane < M && !H.live[base + lane];
         const bool f1 = lane + 32 < M && !H.live[base + lane + 32];
         uint64_t freem = (uint64_t)__ballot_sync(0xffffffffu, f0) | ((uint64_t)__ballot_sync(0xffffffffu, f1) << 32);
@@ -536,7 +641,15 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
                 const int64_t J[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1, DIM == 3 ? I[2] + nb / 9 - 1 : 0};
                 src = cell_linear<DIM>(g, J) + nc * s;
             }
-            if (src >= 0) {
+            if (PHASE) {
+                if (src >= 0) {
+                    if (lane == 0) PF.phases[ai] = PF.phases[src];
+                } else {
+                    *errs |= kWarnNoNeighbour;
+                }
+                for (int k = lane; k < A.n; k += 32)
+                    A.a[k][ai] = phase_field_value<DIM>(g, PF.f[k], PF.centred[k] != 0, pn, I, corner, dq);
+            } else if (src >= 0) {
                 for (int k = lane; k < A.n; k += 32) A.a[k][ai] = A.a[k][src];
             } else if (A.n > 0) {
                 *errs |= kWarnNoNeighbour;
@@ -554,9 +667,9 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
 }
 
 // One colour pass: warps take the colour's listed cells in turn.
-template <int DIM>
-__global__ void inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, InjectLists Ls, int col,
-                            uint32_t call, int* d_err)
+template <int DIM, bool PHASE>
+__global__ void inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, PhaseFields PF, InjectLists Ls,
+                            int col, uint32_t call, int* d_err)
 {
     extern __shared__ __align__(16) unsigned char smem_inject[];
     const int lane = threadIdx.x & 31;
@@ -578,7 +691,7 @@ __global__ void inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Ar
     int errs = 0;
     for (int k = gw; k < count; k += nwarps) {
         const int64_t c = Ls.list[Ls.off[col] + k];
-        inject_cell_warp<DIM>(g, X, index, Ls.lm, A, call, c, H, lane, &errs);
+        inject_cell_warp<DIM, PHASE>(g, X, index, Ls.lm, A, PF, call, c, H, lane, &errs);
         __syncwarp();
     }
     raise_err(d_err, errs);
@@ -675,8 +788,32 @@ void launch_allocate_passes(const DevGrid& g, const MoveView& S, cudaStream_t st
     }
 }
 
+template <bool PHASE>
+static cudaError_t inject_launch(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
+                                 int nargs, const PhaseFields& PF, uint32_t call);
+
 cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
                           int nargs, uint32_t call)
+{
+    return inject_launch<false>(P, coords, index, args, nargs, PhaseFields{}, call);
+}
+
+cudaError_t launch_inject_phase(jp_particles* P, double* const coords[3], uint8_t* index, double* phases,
+                                double* const* args, const double* const* fields, const int* centred, int nargs,
+                                uint32_t call)
+{
+    PhaseFields PF{};
+    PF.phases = phases;
+    for (int k = 0; k < nargs; ++k) {
+        PF.f[k] = fields[k];
+        PF.centred[k] = centred[k];
+    }
+    return inject_launch<true>(P, coords, index, args, nargs, PF, call);
+}
+
+template <bool PHASE>
+static cudaError_t inject_launch(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
+                                 int nargs, const PhaseFields& PF, uint32_t call)
 {
     const int N = P->g.ndim;
     const int64_t nc = P->g.ncells;
@@ -711,23 +848,23 @@ cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* ind
     const unsigned nbp = (unsigned)(152 * (N == 2 ? 8 : 16));
     if (N == 2) {
         if (smem > 48 * 1024) {
-            e = cudaFuncSetAttribute(inject_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            e = cudaFuncSetAttribute(inject_pass<2, PHASE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
         }
-        inject_flag<2><<<nb, kThreads, 0, st>>>(P->g, CX, index, Ls);
+        inject_flag<2, PHASE><<<nb, kThreads, 0, st>>>(P->g, CX, index, Ls);
         for (int pass = 0; pass < 4; ++pass) {  // offsetᵢ outer, offsetⱼ inner (injection.jl:31)
             const int col = (pass / 2) + 2 * (pass % 2);
-            inject_pass<2><<<nbp, 32 * wpb, smem, st>>>(P->g, X, index, A, Ls, col, call, P->d_err);
+            inject_pass<2, PHASE><<<nbp, 32 * wpb, smem, st>>>(P->g, X, index, A, PF, Ls, col, call, P->d_err);
         }
     } else {
         if (smem > 48 * 1024) {
-            e = cudaFuncSetAttribute(inject_pass<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            e = cudaFuncSetAttribute(inject_pass<3, PHASE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
         }
-        inject_flag<3><<<nb, kThreads, 0, st>>>(P->g, CX, index, Ls);
+        inject_flag<3, PHASE><<<nb, kThreads, 0, st>>>(P->g, CX, index, Ls);
         for (int pass = 0; pass < 8; ++pass) {  // i outer, k inner (injection.jl:38)
             const int col = (pass / 4) + 2 * ((pass / 2) % 2) + 4 * (pass % 2);
-            inject_pass<3><<<nbp, 32 * wpb, smem, st>>>(P->g, X, index, A, Ls, col, call, P->d_err);
+            inject_pass<3, PHASE><<<nbp, 32 * wpb, smem, st>>>(P->g, X, index, A, PF, Ls, col, call, P->d_err);
         }
     }
     return cudaGetLastError();

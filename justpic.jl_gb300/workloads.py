@@ -118,6 +118,33 @@ CONFIGS = {
 }
 
 
+def pure_shear(ni=(128, 128), rate=-1.0):
+    """The phase miniapp's pure-shear setup (test/test_2D.jl:385-433): unit
+    square centred on the origin, ghost-node velocity grids
+    LinRange(-L/2 - dx/2, L/2 + dx/2, n + 2), vx = x * rate, vy = -y * rate.
+    Returns (grid, (Vx, Vy), dt) with dt = 0.25 * min(dx) / max|V|."""
+    nx, ny = ni
+    xv = (LinRange(-0.5, 0.5, nx + 1), LinRange(-0.5, 0.5, ny + 1))
+    dx = (1.0 / nx, 1.0 / ny)
+    xc = tuple(LinRange(-0.5 + dx[d] / 2, 0.5 - dx[d] / 2, ni[d]) for d in range(2))
+    ext = tuple(LinRange(-0.5 - dx[d] / 2, 0.5 + dx[d] / 2, ni[d] + 2) for d in range(2))
+    grid_v = ((xv[0], ext[1]), (ext[0], xv[1]))
+    g = {"ndim": 2, "ni": tuple(ni), "xv": xv, "xc": xc, "dx": dx, "grid_v": grid_v}
+    x = np.asarray(xv[0])
+    y = np.asarray(xv[1])
+    Vx = np.asfortranarray(np.repeat((x * rate)[:, None], ny + 2, axis=1))
+    Vy = np.asfortranarray(np.repeat((-y * rate)[None, :], nx + 2, axis=0))
+    dt = 0.25 * min(dx) / max(float(np.max(np.abs(Vx))), float(np.max(np.abs(Vy))))
+    return g, (Vx, Vy), dt
+
+
+def shear_phases(coords, index):
+    """Phase 1 where x < y, else 2, on live slots (test/test_2D.jl:387-401);
+    dead slots hold NaN."""
+    x, y = (np.asarray(c) for c in coords[:2])
+    return np.where(np.asarray(index).astype(bool), np.where(x < y, 1.0, 2.0), np.nan)
+
+
 def perturbed_stream_velocity(g, sigma=0.1 * 250.0, seed=5):
     """The stream-function velocity plus i.i.d. N(0, sigma^2) noise on every
     staggered node (fixed over time)."""

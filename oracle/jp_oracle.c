@@ -496,6 +496,153 @@ static void inject_cell(const jpo_grid* g, const int64_t* idx, double* const coo
     }
 }
 
+/* Julia's min / max on floats: NaN wins, -0.0 is below +0.0 */
+static inline double jl_min(double x, double y)
+{
+    return ((y < x) || (!!signbit(y) > !!signbit(x))) ? (isnan(x) ? x : y) : (isnan(y) ? y : x);
+}
+
+static inline double jl_max(double x, double y)
+{
+    return ((y > x) || (!!signbit(y) < !!signbit(x))) ? (isnan(x) ? x : y) : (isnan(y) ? y : x);
+}
+
+/* the field value given to an injected particle by inject_particles_phase!
+   (src/Particles/injection.jl:300-318): the N-linear interpolation at p of a
+   cell-centred field (the centre cell below p, clamped, centre spacing) or a
+   vertex field (the particle's own cell), clamped to the extrema of the
+   interpolation's corner values */
+static double phase_field_value(const jpo_grid* g, const double* F, int centred, const double* pn, const int64_t* I,
+                                const double* corner, const double* dq)
+{
+    const int N = g->ndim;
+    int64_t J[3] = {0, 0, 0};
+    double t[3];
+    int64_t L0, L1;
+    if (centred) {
+        for (int d = 0; d < N; ++d) {
+            const double xcen = corner[d] + dq[d];
+            int64_t j = pn[d] < xcen ? I[d] - 1 : I[d];
+            const int64_t hi = g->n[d] - 2;
+            j = j < 0 ? 0 : (j > hi ? hi : j);
+            J[d] = j;
+            t[d] = (pn[d] - g->xc[d][j]) * (1.0 / g->dxc[d][j]);
+        }
+        L0 = g->n[0];
+        L1 = g->n[1];
+    } else {
+        for (int d = 0; d < N; ++d) {
+            J[d] = I[d];
+            t[d] = (pn[d] - g->xv[d][I[d]]) * (1.0 / g->dxv[d][I[d]]);
+        }
+        L0 = g->n[0] + 1;
+        L1 = g->n[1] + 1;
+    }
+    const int64_t b = J[0] + L0 * (J[1] + (N == 3 ? L1 * J[2] : 0));
+    const int64_t sz = L0 * L1;
+    const int64_t off[8] = {b, b + 1, b + L0, b + L0 + 1, b + sz, b + sz + 1, b + sz + L0, b + sz + L0 + 1};
+    double v[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = 0; k < (1 << N); ++k) v[k] = F[off[k]];
+    const double tmp = lerpN(N, v, t);
+    double lo = v[0], hi = v[0];
+    for (int k = 1; k < (1 << N); ++k) {
+        hi = jl_max(v[k], hi);
+        lo = jl_min(v[k], lo);
+    }
+    return tmp > hi ? hi : (tmp < lo ? lo : tmp);  /* clamp */
+}
+
+/* _inject_particles_phase! (src/Particles/injection.jl:232-325): as
+   _inject_particles! but every quadrant is checked (`continue`, not `break`),
+   the new particle copies the phase of its nearest neighbour, and each field
+   in args takes the clamped interpolation of the matching grid field. */
+static void inject_cell_phase(const jpo_grid* g, const int64_t* idx, double* const coords[3], uint8_t* index,
+                              double* phases, double* const* args, const double* const* fields,
+                              const int* centred, int nargs, uint32_t call, int* err)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int NQ = 1 << N;
+    const int64_t c = cell_linear(g, idx);
+    double corner[3], dq[3];
+    for (int d = 0; d < N; ++d) {
+        corner[d] = g->xv[d][idx[d]];
+        dq[d] = g->dxv[d][idx[d]] / 2.0;
+    }
+    const int min_xq = (g->min_xcell + NQ - 1) / NQ;
+    for (int q = 0; q < NQ; ++q) {
+        double qc[3];
+        for (int d = 0; d < N; ++d) qc[d] = corner[d] + dq[d] * (double)((q >> d) & 1);
+        int count = 0;
+        for (int i = 0; i < M; ++i) {
+            const int64_t a = c + nc * i;
+            if (!index[a]) continue;
+            double p[3];
+            for (int d = 0; d < N; ++d) p[d] = coords[d][a];
+            if (isincell(N, p, qc, dq)) ++count;
+        }
+        if (count >= min_xq) continue;
+        for (int i = 0; i < M; ++i) {
+            const int64_t a = c + nc * i;
+            if (index[a]) continue;
+            ++count;
+            double pn[3];
+            for (int d = 0; d < N; ++d) {
+                const double r = jp_rand_uniform(g->seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)i,
+                                                 (uint32_t)d);
+                pn[d] = qc[d] + dq[d] * fma(0.95, r, 0.05);
+            }
+            int64_t src = 0;
+            if (nearest_particle(g, coords, index, pn, i, idx, &src))
+                phases[a] = phases[src];
+            else
+                *err |= JPO_ERR_NO_NEIGHBOUR;
+            for (int d = 0; d < N; ++d) coords[d][a] = pn[d];
+            index[a] = 1;
+            for (int k = 0; k < nargs; ++k)
+                args[k][a] = phase_field_value(g, fields[k], centred[k], pn, idx, corner, dq);
+            if (count >= min_xq) break;
+        }
+    }
+}
+
+int jpo_inject_particles_phase(const jpo_grid* g, double* const coords[3], uint8_t* index, double* phases,
+                               double* const* args, const double* const* fields, const int* centred, int nargs,
+                               uint32_t call)
+{
+    const int N = g->ndim;
+    int err = 0;
+    int64_t ncol[3] = {1, 1, 1};
+    for (int d = 0; d < N; ++d) ncol[d] = (g->n[d] + 1) / 2;
+    const int npass = 1 << N;
+    const int64_t ntot = ncol[0] * ncol[1] * ncol[2];
+    for (int pass = 0; pass < npass; ++pass) {
+        int64_t off[3];
+        if (N == 2) {
+            off[0] = pass / 2;
+            off[1] = pass % 2;
+            off[2] = 0;
+        } else {
+            off[0] = pass / 4;
+            off[1] = (pass / 2) % 2;
+            off[2] = pass % 2;
+        }
+#pragma omp parallel for schedule(static) num_threads(nthreads()) reduction(| : err)
+        for (int64_t w = 0; w < ntot; ++w) {
+            int64_t J[3] = {w % ncol[0], (w / ncol[0]) % ncol[1], w / (ncol[0] * ncol[1])};
+            int64_t idx[3] = {0, 0, 0};
+            int ok = 1;
+            for (int d = 0; d < N; ++d) {
+                idx[d] = 2 * J[d] + off[d];
+                if (idx[d] >= g->n[d]) ok = 0;
+            }
+            if (ok) inject_cell_phase(g, idx, coords, index, phases, args, fields, centred, nargs, call, &err);
+        }
+    }
+    return err;
+}
+
 int jpo_inject_particles(const jpo_grid* g, double* const coords[3], uint8_t* index,
                          double* const* args, int nargs, uint32_t call)
 {

@@ -68,6 +68,12 @@ int jpo_move_particles(const jpo_grid* g, double* const coords[3], uint8_t* inde
 int jpo_inject_particles(const jpo_grid* g, double* const coords[3], uint8_t* index,
                          double* const* args, int nargs, uint32_t call);
 
+/* inject_particles_phase!: src/Particles/injection.jl:137-325; fields[k] is
+   cell-centred (n cells) when centred[k], a vertex field otherwise */
+int jpo_inject_particles_phase(const jpo_grid* g, double* const coords[3], uint8_t* index, double* phases,
+                               double* const* args, const double* const* fields, const int* centred, int nargs,
+                               uint32_t call);
+
 /* grid2particle!: src/Interpolations/grid_to_particle.jl:26-82 */
 void jpo_grid2particle(const jpo_grid* g, double* Fp, const double* F,
                        const double* const coords[3], const uint8_t* index);

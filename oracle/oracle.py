@@ -75,6 +75,9 @@ def lib():
         L.jpo_move_particles.restype = ctypes.c_int
         L.jpo_inject_particles.argtypes = [G, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32]
         L.jpo_inject_particles.restype = ctypes.c_int
+        L.jpo_inject_particles_phase.argtypes = [G, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32]
+        L.jpo_inject_particles_phase.restype = ctypes.c_int
         L.jpo_grid2particle.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]
         L.jpo_particle2grid.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]
         L.jpo_grid2particle_flip.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
@@ -231,6 +234,21 @@ class OracleParticles:
         a, n = self._args(args)
         err = lib().jpo_inject_particles(ctypes.byref(self._g), self._p3(self.coords), _ptr(self.index), a, n,
                                          self.inject_calls)
+        self.inject_calls += 1
+        return err
+
+    def inject_particles_phase(self, phases, args=(), fields=()):
+        """inject_particles_phase!(particles, phases, args, fields): a field of
+        the cells' shape is cell-centred, one of the vertices' shape a vertex
+        field. Shares the injection call counter with inject_particles."""
+        args, fields = tuple(args), tuple(np.asfortranarray(f, dtype=np.float64) for f in fields)
+        assert len(args) == len(fields)
+        centred = (ctypes.c_int * max(1, len(args)))(*[int(tuple(f.shape) == tuple(self.n)) for f in fields])
+        a, n = self._args(args)
+        fp = (ctypes.c_void_p * max(1, len(fields)))(*[f.ctypes.data for f in fields])
+        self._keep = fields
+        err = lib().jpo_inject_particles_phase(ctypes.byref(self._g), self._p3(self.coords), _ptr(self.index),
+                                               _ptr(phases), a, fp, centred, n, self.inject_calls)
         self.inject_calls += 1
         return err
 

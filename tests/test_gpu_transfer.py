@@ -88,3 +88,85 @@ def test_phase_ratios_bit_exact(ni, refined, nphases):
     assert_bits_equal(ref["vertex"], pr.vertex.cpu().numpy(), "vertex")
     for d, name in enumerate(["Vx", "Vy", "Vz"][:len(ni)]):
         assert_bits_equal(ref[name], pr.faces[d].cpu().numpy(), name)
+
+
+def _set_field(pair, k, values):
+    pair.of[k][...] = values
+    pair.pf[k].data.copy_(torch.from_numpy(np.ascontiguousarray(values)))
+
+
+def _inject_phase(pair, fields):
+    err = pair.o.inject_particles_phase(pair.of[0], pair.of[1:], fields)
+    jp.inject_particles_phase_(pair.p, pair.pf[0], tuple(pair.pf[1:]), tuple(jp.TA("CUDA")(f) for f in fields))
+    return err
+
+
+@pytest.mark.parametrize("ni,refined", CASES)
+def test_inject_particles_phase_bit_exact(ni, refined):
+    """inject_particles_phase! against the oracle: phases copied from the
+    nearest particle, one vertex and one cell-centred field interpolated,
+    every quadrant refilled; after advection and move_particles! carrying
+    the phases."""
+    g = refined_grid(ni) if refined else W.grid(ni)
+    pair = Pair(g, 24, 48, 20, nfields=3)  # phases, vertex-interpolated, centre-interpolated
+    _set_field(pair, 0, W.shear_phases(pair.o.coords, pair.o.index))
+    V = W.stream_velocity(g) if len(ni) == 2 else W.stream_velocity_3d(g)
+    rng = np.random.default_rng(6)
+    Fv = np.asfortranarray(rng.standard_normal(tuple(n + 1 for n in ni)))
+    Fc = np.asfortranarray(rng.standard_normal(tuple(ni)))
+    dt = W.cfl_dt(g, V)
+    injected = 0
+    for step in range(3):
+        pair.advection("rk2", V, dt)
+        pair.move()
+        before = int(pair.o.index.sum())
+        _inject_phase(pair, (Fv, Fc))
+        injected += int(pair.o.index.sum()) - before
+        pair.assert_same(f"inject_particles_phase! step {step}")
+    assert injected > 0
+
+
+def test_pure_shear_phase_miniapp_bit_exact():
+    """The phase miniapp (test/test_2D.jl:385-481) on 32^2 cells, 60/64/50
+    particles per cell (the miniapp's 80-slot capacity is above this
+    library's 64), 10 steps of RK2 + move + inject_particles_phase! +
+    update_phase_ratios!, against the oracle; the ratios sum to one."""
+    g, V, dt = W.pure_shear((32, 32))
+    pair = Pair(g, 60, 64, 50, nfields=1, uniform=True)
+    _set_field(pair, 0, W.shear_phases(pair.o.coords, pair.o.index))
+    pr = jp.PhaseRatios(2, g["ni"])
+    for step in range(10):
+        pair.advection("rk2", V, dt)
+        pair.move()
+        _inject_phase(pair, ())
+        pair.assert_same(f"pure shear step {step}")
+        ref = pair.o.phase_ratios(pair.of[0], 2)
+        jp.update_phase_ratios_(pr, pair.p, pair.pf[0])
+        assert_bits_equal(ref["center"], pr.center.cpu().numpy(), "center")
+        assert_bits_equal(ref["vertex"], pr.vertex.cpu().numpy(), "vertex")
+    for name, a in (("center", pr.center), ("vertex", pr.vertex), ("Vx", pr.Vx), ("Vy", pr.Vy)):
+        s = a.sum(dim=0).cpu().numpy()
+        np.testing.assert_allclose(s, 1.0, rtol=1e-12, err_msg=name)  # test_2D.jl:476-479
+
+
+def test_pure_shear_phase_miniapp_full_size():
+    """The same miniapp at its own size (128^2 cells, 20 steps) on the GPU
+    alone: every location keeps ratios summing to one."""
+    g, V, dt = W.pure_shear((128, 128))
+    p = jp.init_particles(jp.CUDABackend, 60, 64, 50, *g["grid_v"])
+    (phases,) = jp.init_cell_arrays(p, 1)
+    ph = W.shear_phases([c.numpy() for c in p.coords], p.index.numpy())
+    phases.data.copy_(torch.from_numpy(np.ascontiguousarray(ph)))
+    pr = jp.PhaseRatios(2, g["ni"])
+    jp.update_phase_ratios_(pr, p, phases)
+    Vd = tuple(jp.TA("CUDA")(v) for v in V)
+    for _ in range(20):
+        jp.advection_(p, jp.RungeKutta2(), Vd, dt)
+        jp.move_particles_(p, (phases,))
+        jp.inject_particles_phase_(p, phases, (), ())
+        jp.update_phase_ratios_(pr, p, phases)
+    for name, a in (("center", pr.center), ("vertex", pr.vertex), ("Vx", pr.Vx), ("Vy", pr.Vy)):
+        s = a.sum(dim=0).cpu().numpy()
+        np.testing.assert_allclose(s, 1.0, rtol=1e-12, err_msg=name)
+    ph_now = phases.numpy()[p.index.numpy().astype(bool)]
+    assert set(np.unique(ph_now)) <= {1.0, 2.0}

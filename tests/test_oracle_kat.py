@@ -229,3 +229,76 @@ def test_rotating_circle_miniapp():
     nsteps = int(tmax // 200) + 1
     err = _miniapp(g, (Vx, Vy), T, 200.0, nsteps, 0.5)
     assert err < 1e-1
+
+
+# --- inject_particles_phase! (src/Particles/injection.jl:133-325) -------------
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_inject_phase_checks_every_quadrant(ndim):
+    """A cell whose last quadrant is empty: inject_particles! stops at the
+    first (full) quadrant and leaves it, inject_particles_phase! refills it
+    with new particles that take the nearest particle's phase and the
+    interpolated grid fields."""
+    ni = (4,) * ndim
+    g = W.grid(ni)
+    nxcell, mx, mn = (24, 48, 12) if ndim == 2 else (24, 48, 16)
+    P1 = _oracle_particles(g, nxcell, mx, mn)
+    P2 = _oracle_particles(g, nxcell, mx, mn)
+    npq = P1.np_quadrant
+    cell = (1,) * ndim
+    c = sum(cell[d] * 4 ** d for d in range(ndim))
+    last = (1 << ndim) - 1
+    for P in (P1, P2):
+        for l in range(last * npq, (last + 1) * npq):
+            P.index[l, c] = 0
+            for d in range(ndim):
+                P.coords[d][l, c] = np.nan
+    before = P1.index.copy()
+    assert P1.inject_particles(()) == 0
+    assert np.array_equal(P1.index, before)  # first quadrant full: nothing injected
+
+    ids = P2.cell_array(np.nan)
+    live0 = P2.index.astype(bool)
+    ids[live0] = np.arange(live0.sum(), dtype=np.float64)  # unique phase id per particle
+    pT, pS = P2.cell_array(), P2.cell_array()
+    lin = lambda *x: sum((d + 1.0) * x[d] for d in range(ndim))  # noqa: E731
+    Fv = W.on_grid(lin, g["xv"])
+    Fc = W.on_grid(lin, g["xc"])
+    assert P2.inject_particles_phase(ids, (pT, pS), (Fv, Fc)) == 0
+    new = P2.index.astype(bool) & ~live0
+    min_xq = -(-mn // (1 << ndim))
+    assert new.sum() == min_xq and new[:, c].sum() == min_xq
+    xv = [np.asarray(a) for a in g["xv"]]
+    pts = np.stack([P2.coords[d] for d in range(ndim)], axis=-1)
+    orig = pts[live0]
+    for l in np.nonzero(new[:, c])[0]:
+        p = pts[l, c]
+        for d in range(ndim):  # inside the refilled (upper) quadrant
+            mid = 0.5 * (xv[d][cell[d]] + xv[d][cell[d] + 1])
+            assert mid < p[d] < xv[d][cell[d] + 1]
+        src = np.argwhere(ids == ids[l, c])
+        assert len(src) >= 1 and not np.isnan(ids[l, c])
+        dsrc = min(np.sum((pts[i, j] - p) ** 2) for i, j in src if (i, j) != (l, c))
+        assert dsrc <= np.min(np.sum((orig - p) ** 2, axis=-1))  # no original particle is nearer
+        np.testing.assert_allclose(pT[l, c], lin(*p), rtol=1e-12)
+        np.testing.assert_allclose(pS[l, c], lin(*p), rtol=1e-12)
+
+
+def test_inject_phase_clamps_to_corner_extrema():
+    """Interpolated values never leave the range of the cell's grid values
+    (injection.jl:300-316): a centred field whose bracketing centres are
+    clamped at the domain edge gives the extrapolation clipped to the corners."""
+    g = W.grid((4, 4))
+    P = _oracle_particles(g, 24, 48, 12)
+    for l in range(24):  # empty cell (0, 0) entirely
+        P.index[l, 0] = 0
+        P.coords[0][l, 0] = P.coords[1][l, 0] = np.nan
+    ids = P.cell_array(1.0)
+    pS = P.cell_array()
+    Fc = W.on_grid(lambda x, y: np.exp(3 * x) + y, g["xc"])
+    assert P.inject_particles_phase(ids, (pS,), (Fc,)) == 0
+    live = P.index.astype(bool)
+    vals = pS[:, 0][live[:, 0]]
+    corners = Fc[0:2, 0:2]
+    assert len(vals) > 0
+    assert vals.min() >= corners.min() and vals.max() <= corners.max()
+    assert np.all(ids[:, 0][live[:, 0]] == 1.0)
