@@ -113,6 +113,19 @@ int jp_advection(jp_particles* p, int32_t method, double alpha, const double* co
                  double dt, double* const coords[3], const uint8_t* index);
 
 /*
+ * advection_LinP! (src/Particles/Advection/advection_LinP.jl:27-62) and
+ * advection_MQS! (src/Particles/Advection/advection_MQS.jl:30-66): as
+ * jp_advection, with the LinP (2/3 N-linear + 1/3 pressure-point) or MQS
+ * (quadratic-spline corrected) velocity interpolation wherever the parent
+ * interval is at least one interval away from the component grid's edges
+ * (N-linear elsewhere), as the reference does.
+ */
+int jp_advection_linp(jp_particles* p, int32_t method, double alpha, const double* const V[3],
+                      double dt, double* const coords[3], const uint8_t* index);
+int jp_advection_mqs(jp_particles* p, int32_t method, double alpha, const double* const V[3],
+                     double dt, double* const coords[3], const uint8_t* index);
+
+/*
  * move_particles! (src/Particles/move_safe.jl:21-125): relocate particles that
  * left their cell, carrying the nargs particle fields args[0..nargs-1]. Slot
  * allocation reproduces the reference's colour passes exactly.
@@ -195,16 +208,22 @@ int jp_grid2particle_flip(jp_particles* p, double* Fp, const double* F, const do
                           const double* const coords[3], const uint8_t* index);
 
 /*
- * update_phase_ratios!(phase_ratios, particles, phases) (src/PhaseRatios/utils.jl:3-40)
- * without the 3D edge midpoints: for phase ids 1..nphases (<= 16) in the
- * per-slot field `phases`, the phase fractions at the cell centres (center,
- * n0 x n1 (x n2) nodes), the vertices (vertex, (n0+1) x ...) and the faces
- * (faces[d], n + e_d nodes: the reference's Vx, Vy, Vz), each laid out
- * out[k * nodes + node] like a CellArray of nphases-vectors. NULL skips a
- * location. Kernels: centers.jl:3-30, vertices.jl:4-107, midpoints.jl:3-94.
+ * update_phase_ratios!(phase_ratios, particles, phases) (src/PhaseRatios/utils.jl:3-40):
+ * for phase ids 1..nphases (<= 16) in the per-slot field `phases`, the phase
+ * fractions at the cell centres (center, n0 x n1 (x n2) nodes), the vertices
+ * (vertex, (n0+1) x ...) and the faces (faces[d], n + e_d nodes: the
+ * reference's Vx, Vy, Vz), each laid out out[k * nodes + node] like a
+ * CellArray of nphases-vectors. NULL skips a location. Kernels:
+ * centers.jl:3-30, vertices.jl:4-107, midpoints.jl:3-94.
+ *
+ * jp_phase_ratios_midpoints: the 3D edge midpoints (midpoints.jl:108-242),
+ * mids[0] = xy (n + (1,1,0) nodes), mids[1] = yz (n + (0,1,1)), mids[2] = xz
+ * (n + (1,0,1)); needs at least 2 cells per axis.
  */
 int jp_phase_ratios(jp_particles* p, int32_t nphases, const double* phases, const double* const coords[3],
                     double* center, double* vertex, double* const faces[3]);
+int jp_phase_ratios_midpoints(jp_particles* p, int32_t nphases, const double* phases,
+                              const double* const coords[3], double* const mids[3]);
 int jp_centroid2particle(jp_particles* p, double* Fp, const double* F, const double* const coords[3]);
 int jp_particle2centroid(jp_particles* p, double* F, const double* Fp, const double* const coords[3]);
 

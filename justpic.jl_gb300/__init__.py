@@ -16,6 +16,8 @@ All compute runs in hand-written sm_103a CUDA kernels; there is no CPU path.
 from ._native import ArgumentError, JustPICError, NativeLibraryMissing  # noqa: F401
 from .api import (  # noqa: F401
     advection_,
+    advection_LinP_,
+    advection_MQS_,
     centroid2particle_,
     grid2particle_,
     grid2particle_flip_,

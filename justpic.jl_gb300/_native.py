@@ -72,6 +72,10 @@ SIGNATURES = [
     ("jp_init_particles", ctypes.c_int, [ctypes.c_void_p, P3, ctypes.c_void_p]),
     ("jp_advection", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, P3, ctypes.c_double, P3, ctypes.c_void_p]),
+    ("jp_advection_linp", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, P3, ctypes.c_double, P3, ctypes.c_void_p]),
+    ("jp_advection_mqs", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, P3, ctypes.c_double, P3, ctypes.c_void_p]),
     ("jp_move_particles", ctypes.c_int, [ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     ("jp_move_particles_noalloc", ctypes.c_int,
      [ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
@@ -98,6 +102,7 @@ SIGNATURES = [
     ("jp_centroid2particle", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3]),
     ("jp_phase_ratios", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("jp_phase_ratios_midpoints", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, P3, P3]),
     ("jp_particle2centroid", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3]),
     # adjoint (2D, FP64)
     ("jp_particle2grid_with_weights", ctypes.c_int,

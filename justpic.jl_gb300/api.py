@@ -6,6 +6,8 @@ Julia's in-place ``f!`` becomes ``f_`` here (PyTorch's in-place convention):
 Python                       reference
 ===========================  ==============================================================
 ``advection_``               ``advection!`` (src/Particles/Advection/advection.jl:21)
+``advection_LinP_``          ``advection_LinP!`` (src/Particles/Advection/advection_LinP.jl:13)
+``advection_MQS_``           ``advection_MQS!`` (src/Particles/Advection/advection_MQS.jl:16)
 ``move_particles_``          ``move_particles!`` (src/Particles/move_safe.jl:21)
 ``inject_particles_``        ``inject_particles!`` (src/Particles/injection.jl:19)
 ``inject_particles_phase_``  ``inject_particles_phase!`` (src/Particles/injection.jl:133)
@@ -105,9 +107,7 @@ def _args(p: Particles, args):
     return arr, len(args)
 
 
-def advection_(particles: Particles, method: AbstractAdvectionIntegrator, V, dt) -> None:
-    """``advection!(particles, method, V, dt)``: advect every live particle
-    through the staggered velocity components ``V`` (one per axis)."""
+def _advect(particles: Particles, method, V, dt, entry: str, what: str) -> None:
     if not isinstance(method, AbstractAdvectionIntegrator):
         raise ArgumentError("method must be Euler(), RungeKutta2(α) or RungeKutta4()")
     N = particles.ndim
@@ -118,9 +118,29 @@ def advection_(particles: Particles, method: AbstractAdvectionIntegrator, V, dt)
         _check_grid(V[c], tuple(len(x) for x in particles.xi_vel[c]), f"V[{c}]")
     _bind_stream(particles)
     vp = P3(*[v.data_ptr() for v in V], *([None] * (3 - N)))
-    rc = _native.load().jp_advection(particles.handle, method.code, float(method.alpha), vp, float(dt),
-                                     _coords(particles), particles.index.data_ptr())
-    _finish(particles, rc, "advection!")
+    rc = getattr(_native.load(), entry)(particles.handle, method.code, float(method.alpha), vp, float(dt),
+                                        _coords(particles), particles.index.data_ptr())
+    _finish(particles, rc, what)
+
+
+def advection_(particles: Particles, method: AbstractAdvectionIntegrator, V, dt) -> None:
+    """``advection!(particles, method, V, dt)``: advect every live particle
+    through the staggered velocity components ``V`` (one per axis)."""
+    _advect(particles, method, V, dt, "jp_advection", "advection!")
+
+
+def advection_LinP_(particles: Particles, method: AbstractAdvectionIntegrator, V, dt) -> None:
+    """``advection_LinP!(particles, method, V, dt)``
+    (src/Particles/Advection/advection_LinP.jl:13): as ``advection_`` with
+    the LinP velocity interpolation."""
+    _advect(particles, method, V, dt, "jp_advection_linp", "advection_LinP!")
+
+
+def advection_MQS_(particles: Particles, method: AbstractAdvectionIntegrator, V, dt) -> None:
+    """``advection_MQS!(particles, method, V, dt)``
+    (src/Particles/Advection/advection_MQS.jl:16): as ``advection_`` with the
+    MQS velocity interpolation."""
+    _advect(particles, method, V, dt, "jp_advection_mqs", "advection_MQS!")
 
 
 def move_particles_(particles: Particles, args=()) -> None:
@@ -238,11 +258,13 @@ def particle2centroid_(F: torch.Tensor, Fp: CellArray, particles: Particles) -> 
 
 # ---- phase ratios -------------------------------------------------------------
 class PhaseRatios:
-    """``PhaseRatios`` (src/PhaseRatios/PhaseRatios.jl:12-33, constructors.jl:20-57)
-    for 2D/3D without the 3D edge midpoints: ``center``, ``vertex``, ``Vx``,
-    ``Vy`` (, ``Vz``) are CUDA float64 tensors of shape (nphases, nodes) in the
-    CellArray layout (phase k of node n at n + nodes * k), node index
-    column-major over the location's grid."""
+    """``PhaseRatios`` (src/PhaseRatios/PhaseRatios.jl:12-33, constructors.jl:18-57):
+    ``center``, ``vertex``, ``Vx``, ``Vy`` (, ``Vz`` and the 3D edge
+    midpoints ``yz``, ``xz``, ``xy``) are CUDA float64 tensors of shape
+    (nphases, nodes) in the CellArray layout (phase k of node n at
+    n + nodes * k), node index column-major over the location's grid."""
+
+    MIDPOINTS = (("xy", (1, 1, 0)), ("yz", (0, 1, 1)), ("xz", (1, 0, 1)))
 
     def __init__(self, nphases: int, ni):
         ni = tuple(int(n) for n in ni)
@@ -257,12 +279,16 @@ class PhaseRatios:
         self.faces = tuple(alloc(tuple(n + (1 if e == d else 0) for e, n in enumerate(ni))) for d in range(len(ni)))
         self.Vx, self.Vy = self.faces[0], self.faces[1]
         self.Vz = self.faces[2] if len(ni) == 3 else None
+        self.midpoints = None
+        if len(ni) == 3:
+            self.midpoints = tuple(alloc(tuple(n + o for n, o in zip(ni, off))) for _, off in self.MIDPOINTS)
+            self.xy, self.yz, self.xz = self.midpoints
 
 
 def update_phase_ratios_(phase_ratios: PhaseRatios, particles: Particles, phases: CellArray) -> None:
-    """``update_phase_ratios!(phase_ratios, particles, phases)`` (src/PhaseRatios/utils.jl:3-40)
-    without the 3D edge midpoints: the fraction of each phase (ids 1..nphases in
-    the per-slot field ``phases``) at cell centres, vertices and faces."""
+    """``update_phase_ratios!(phase_ratios, particles, phases)`` (src/PhaseRatios/utils.jl:3-40):
+    the fraction of each phase (ids 1..nphases in the per-slot field
+    ``phases``) at cell centres, vertices, faces and, in 3D, edge midpoints."""
     _check_cellarray(particles, phases, "phases")
     if phase_ratios.ni != particles.ni:
         raise ArgumentError("phase_ratios does not match the particles' grid")
@@ -271,5 +297,9 @@ def update_phase_ratios_(phase_ratios: PhaseRatios, particles: Particles, phases
     rc = _native.load().jp_phase_ratios(particles.handle, phase_ratios.nphases, phases.data_ptr(),
                                         _coords(particles), phase_ratios.center.data_ptr(),
                                         phase_ratios.vertex.data_ptr(), faces)
+    if rc == 0 and particles.ndim == 3:
+        mids = P3(*[m.data_ptr() for m in phase_ratios.midpoints])
+        rc = _native.load().jp_phase_ratios_midpoints(particles.handle, phase_ratios.nphases, phases.data_ptr(),
+                                                      _coords(particles), mids)
     _finish(particles, rc, "update_phase_ratios!")
 

@@ -307,17 +307,35 @@ int jp_init_particles(jp_particles* P, double* const coords[3], uint8_t* index)
     return finish(P, jp::launch_init(P, coords, index), "jp_init_particles");
 }
 
-int jp_advection(jp_particles* P, int32_t method, double alpha, const double* const V[3], double dt,
-                 double* const coords[3], const uint8_t* index)
+static int advection_common(jp_particles* P, int32_t method, int interp, double alpha, const double* const V[3],
+                            double dt, double* const coords[3], const uint8_t* index, const char* what)
 {
     if (!P || !index || !check_coords(P, (const void* const*)coords) ||
         !check_coords(P, (const void* const*)V))
-        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection: null pointer");
+        return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": null pointer");
     if (method != JP_EULER && method != JP_RUNGE_KUTTA2 && method != JP_RUNGE_KUTTA4)
-        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection: unknown integrator");
+        return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": unknown integrator");
     if (method == JP_RUNGE_KUTTA2 && !(0.0 < alpha && alpha < 1.0))
         return fail(JP_ERR_INVALID_ARGUMENT, "Only 0 < α < 1 is supported");
-    return finish(P, jp::launch_advection(P, method, alpha, V, dt, coords, index), "jp_advection");
+    return finish(P, jp::launch_advection_interp(P, method, interp, alpha, V, dt, coords, index), what);
+}
+
+int jp_advection(jp_particles* P, int32_t method, double alpha, const double* const V[3], double dt,
+                 double* const coords[3], const uint8_t* index)
+{
+    return advection_common(P, method, 0, alpha, V, dt, coords, index, "jp_advection");
+}
+
+int jp_advection_linp(jp_particles* P, int32_t method, double alpha, const double* const V[3], double dt,
+                      double* const coords[3], const uint8_t* index)
+{
+    return advection_common(P, method, 1, alpha, V, dt, coords, index, "jp_advection_linp");
+}
+
+int jp_advection_mqs(jp_particles* P, int32_t method, double alpha, const double* const V[3], double dt,
+                     double* const coords[3], const uint8_t* index)
+{
+    return advection_common(P, method, 2, alpha, V, dt, coords, index, "jp_advection_mqs");
 }
 
 int jp_move_particles(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
@@ -653,6 +671,20 @@ int jp_phase_ratios(jp_particles* P, int32_t nphases, const double* phases, cons
                     "update_phase_ratios!: needs ghost-expanded centre grids with at least 2 cells per axis");
     return finish(P, jp::launch_phase_ratios(P, nphases, phases, coords, center, vertex, faces),
                   "update_phase_ratios!");
+}
+
+int jp_phase_ratios_midpoints(jp_particles* P, int32_t nphases, const double* phases,
+                              const double* const coords[3], double* const mids[3])
+{
+    if (!P || !phases || !mids || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "update_phase_ratios!: null pointer");
+    if (P->g.ndim != 3) return fail(JP_ERR_INVALID_ARGUMENT, "update_phase_ratios!: edge midpoints are 3D only");
+    if (nphases < 1 || nphases > 16)
+        return fail(JP_ERR_INVALID_ARGUMENT, "update_phase_ratios!: 1 to 16 phases are supported");
+    if (!P->centres_ok)
+        return fail(JP_ERR_INVALID_ARGUMENT,
+                    "update_phase_ratios!: needs ghost-expanded centre grids with at least 2 cells per axis");
+    return finish(P, jp::launch_phase_midpoints(P, nphases, phases, coords, mids), "update_phase_ratios!");
 }
 
 int jp_grid2particle_flip(jp_particles* P, double* Fp, const double* F, const double* F0, double alpha,

@@ -316,6 +316,9 @@ inline unsigned grid_blocks(int64_t n, int threads = kThreads)
 cudaError_t launch_init(jp_particles* P, double* const coords[3], uint8_t* index);
 cudaError_t launch_advection(jp_particles* P, int method, double alpha, const double* const V[3],
                              double dt, double* const coords[3], const uint8_t* index);
+// interp: 0 N-linear (advection!), 1 LinP (advection_LinP!), 2 MQS (advection_MQS!)
+cudaError_t launch_advection_interp(jp_particles* P, int method, int interp, double alpha, const double* const V[3],
+                                    double dt, double* const coords[3], const uint8_t* index);
 cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index,
                         double* const* args, int nargs);
 cudaError_t launch_inject(jp_particles* P, double* const coords[3], uint8_t* index,
@@ -332,6 +335,8 @@ cudaError_t launch_c2p(jp_particles* P, double* Fp, const double* F, const doubl
 cudaError_t launch_p2c(jp_particles* P, double* F, const double* Fp, const double* const coords[3]);
 cudaError_t launch_phase_ratios(jp_particles* P, int nph, const double* phases, const double* const coords[3],
                                 double* center, double* vertex, double* const faces[3]);
+cudaError_t launch_phase_midpoints(jp_particles* P, int nph, const double* phases, const double* const coords[3],
+                                   double* const mids[3]);
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
                        const uint8_t* index, double* W = nullptr);
 

@@ -71,7 +71,141 @@ struct AdvParams {
     int half;    // alpha == 1/2
 };
 
+// Velocity interpolation of the advection call: N-linear (advection!), LinP
+// (advection_LinP!) or MQS (advection_MQS!).
+constexpr int kInterpLinear = 0;
+constexpr int kInterpLinP = 1;
+constexpr int kInterpMQS = 2;
+
+// F(i, j[, k]) of a component grid, indices clamped to the grid
 template <int DIM>
+__device__ __forceinline__ double vel_at(const DevGrid& g, int comp, const double* __restrict__ V, int64_t i,
+                                         int64_t j, int64_t k)
+{
+    const int64_t L0 = g.nvel[comp][0], L1 = g.nvel[comp][1], L2 = DIM == 3 ? g.nvel[comp][2] : 1;
+    i = i < 0 ? 0 : (i > L0 - 1 ? L0 - 1 : i);
+    j = j < 0 ? 0 : (j > L1 - 1 ? L1 - 1 : j);
+    k = k < 0 ? 0 : (k > L2 - 1 ? L2 - 1 : k);
+    return ldg(V + i + L0 * (j + L1 * k));
+}
+
+// LinP (src/Particles/Advection/advection_LinP.jl:112-391) away from the
+// grid's edges: 2/3 of the N-linear value VL plus 1/3 of the N-linear
+// interpolation of the velocities averaged to the pressure points
+// (interpolate_V_to_P, its augment_offset rows and swap_F order included),
+// each product and sum rounded on its own as the reference writes it.
+template <int DIM>
+__device__ double linp_value(const DevGrid& g, int comp, const double* __restrict__ V, const double* p,
+                             const int64_t* idx, const double* xc, const double* dx, double VL)
+{
+    int64_t b[3] = {idx[0], idx[1], DIM == 3 ? idx[2] : 0};
+    b[comp] += p[comp] > xc[comp] + dx[comp] / 2.0 ? 1 : 0;  // offset_LinP
+    const int r2 = comp == 1 ? 0 : 1;  // row 2 shifts x (y-component) or y
+    const int r3 = comp == 2 ? 0 : 2;  // row 3 shifts x (z-component) or z
+    constexpr int NR = DIM == 3 ? 4 : 2;
+    double av[8];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+        int64_t q[3] = {b[0], b[1], b[2]};
+        if (r == 1 || r == 3) q[r2] += 1;
+        if (r >= 2) q[r3] += 1;
+        double f[3];
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+            int64_t e[3] = {q[0], q[1], q[2]};
+            e[comp] += s - 1;
+            f[s] = vel_at<DIM>(g, comp, V, e[0], e[1], e[2]);
+        }
+        av[2 * r] = (f[0] + f[1]) / 2.0;
+        av[2 * r + 1] = (f[2] + f[1]) / 2.0;
+    }
+    double FP[8];
+    if (comp == 0) {
+#pragma unroll
+        for (int k = 0; k < 2 * NR; ++k) FP[k] = av[k];
+    } else {  // swap_F: (1, 3, 2, 4, 5, 7, 6, 8)
+#pragma unroll
+        for (int k = 0; k < 2 * NR; ++k) FP[k] = av[(k & 4) | ((k & 1) << 1) | ((k & 2) >> 1)];
+    }
+    // correct_xci_to_pressure_point (advection_LinP.jl:151-189)
+    double tP[3];
+    const int off = 1 - 2 * (p[comp] < xc[comp] + dx[comp] / 2.0 ? 1 : 0);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const double xP = d == comp ? xc[d] + ((double)off * dx[d]) / 2.0 : xc[d];
+        tP[d] = (p[d] - xP) * ldg(g.ixvel[comp][d] + idx[d]);
+    }
+    const double VP = lerpN<DIM>(FP, tP);
+    constexpr double A = 2.0 / 3.0;
+    constexpr double B = 1.0 - A;
+    return __dadd_rn(__dmul_rn(A, VL), __dmul_rn(B, VP));
+}
+
+// lerp of (a, b) at t plus half * (t - half)^2 * (muladd(-2, v1, v0) + v2)
+// with the stencil extended below (lo) or above (hi): one edge of MQS
+// (src/Interpolations/MQS.jl), each operation rounded on its own.
+__device__ __forceinline__ double mqs_edge(double t, double a, double b, double lo, double hi)
+{
+    const bool below = t < 0.5;
+    const double v0 = below ? lo : a, v1 = below ? a : b, v2 = below ? b : hi;
+    const double d = __dadd_rn(t, -0.5);
+    const double corr = __dmul_rn(__dmul_rn(0.5, __dmul_rn(d, d)), __dadd_rn(fma(-2.0, v1, v0), v2));
+    return __dadd_rn(lerp1(t, a, b), corr);
+}
+
+// MQS (src/Interpolations/MQS.jl:1-158) away from the grid's edges, v the
+// corner values and t the normalised position. In 3D the layer k + 1 (x, y)
+// and row j + 1 (z) corrections use the stencil of layer k / row j, as the
+// reference does.
+template <int DIM>
+__device__ double mqs_value(const DevGrid& g, int comp, const double* __restrict__ V, const int64_t* idx,
+                            const double* v, const double* t)
+{
+    const int64_t i = idx[0], j = idx[1], k = DIM == 3 ? idx[2] : 0;
+    if (DIM == 2) {
+        if (comp == 0) {
+            const double r0 = mqs_edge(t[0], v[0], v[1], vel_at<2>(g, 0, V, i - 1, j, 0), vel_at<2>(g, 0, V, i + 2, j, 0));
+            const double r1 =
+                mqs_edge(t[0], v[2], v[3], vel_at<2>(g, 0, V, i - 1, j + 1, 0), vel_at<2>(g, 0, V, i + 2, j + 1, 0));
+            return lerp1(t[1], r0, r1);
+        }
+        const double r0 = mqs_edge(t[1], v[0], v[2], vel_at<2>(g, 1, V, i, j - 1, 0), vel_at<2>(g, 1, V, i, j + 2, 0));
+        const double r1 =
+            mqs_edge(t[1], v[1], v[3], vel_at<2>(g, 1, V, i + 1, j - 1, 0), vel_at<2>(g, 1, V, i + 1, j + 2, 0));
+        return lerp1(t[0], r0, r1);
+    }
+    double r[2];
+    if (comp == 0) {
+        const double lo0 = vel_at<3>(g, 0, V, i - 1, j, k), hi0 = vel_at<3>(g, 0, V, i + 2, j, k);
+        const double lo1 = vel_at<3>(g, 0, V, i - 1, j + 1, k), hi1 = vel_at<3>(g, 0, V, i + 2, j + 1, k);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const double* w = v + 4 * h;
+            r[h] = lerp1(t[1], mqs_edge(t[0], w[0], w[1], lo0, hi0), mqs_edge(t[0], w[2], w[3], lo1, hi1));
+        }
+        return lerp1(t[2], r[0], r[1]);
+    }
+    if (comp == 1) {
+        const double lo0 = vel_at<3>(g, 1, V, i, j - 1, k), hi0 = vel_at<3>(g, 1, V, i, j + 2, k);
+        const double lo1 = vel_at<3>(g, 1, V, i + 1, j - 1, k), hi1 = vel_at<3>(g, 1, V, i + 1, j + 2, k);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const double* w = v + 4 * h;
+            r[h] = lerp1(t[0], mqs_edge(t[1], w[0], w[2], lo0, hi0), mqs_edge(t[1], w[1], w[3], lo1, hi1));
+        }
+        return lerp1(t[2], r[0], r[1]);
+    }
+    // MQS-z: front (v1, v2, v5, v6) and back (v3, v4, v7, v8), corrections along x
+    const double lo0 = vel_at<3>(g, 2, V, i - 1, j, k), hi0 = vel_at<3>(g, 2, V, i + 2, j, k);
+    const double lo1 = vel_at<3>(g, 2, V, i - 1, j, k + 1), hi1 = vel_at<3>(g, 2, V, i + 2, j, k + 1);
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        r[h] = lerp1(t[2], mqs_edge(t[0], v[2 * h], v[2 * h + 1], lo0, hi0),
+                     mqs_edge(t[0], v[2 * h + 4], v[2 * h + 5], lo1, hi1));
+    return lerp1(t[1], r[0], r[1]);
+}
+
+template <int DIM, int INTERP = kInterpLinear>
 __device__ __forceinline__ double interp_component(const DevGrid& g, int comp, const double* p,
                                                    const long long* kp, bool pnan, const int* I,
                                                    const double* __restrict__ V, int* errs)
@@ -126,10 +260,23 @@ __device__ __forceinline__ double interp_component(const DevGrid& g, int comp, c
         v[6] = ldg(b + sz + L0);
         v[7] = ldg(b + sz + L0 + 1);
     }
-    return lerpN<DIM>(v, t);
+    const double VL = lerpN<DIM>(v, t);
+    if (INTERP == kInterpLinear) return VL;
+    // away from the edges only: 1 < index < size - 1 (1-based) on every axis
+    bool inner = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) inner &= idx[d] >= 1 && idx[d] <= g.nvel[comp][d] - 3;
+    if (!inner) return VL;
+    if (INTERP == kInterpLinP) {
+        double dx[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) dx[d] = ldg(g.dxvel[comp][d] + idx[d]);
+        return linp_value<DIM>(g, comp, V, p, idx, xc, dx, VL);
+    }
+    return mqs_value<DIM>(g, comp, V, idx, v, t);
 }
 
-template <int DIM>
+template <int DIM, int INTERP = kInterpLinear>
 __device__ __forceinline__ void interp_velocity(const DevGrid& g, const CVel& V, const double* p, const int* I,
                                                 double* v, int* errs)
 {
@@ -141,22 +288,22 @@ __device__ __forceinline__ void interp_velocity(const DevGrid& g, const CVel& V,
         pnan |= is_nan_bits(p[d]);
     }
 #pragma unroll
-    for (int c = 0; c < DIM; ++c) v[c] = interp_component<DIM>(g, c, p, kp, pnan, I, V.v[c], errs);
+    for (int c = 0; c < DIM; ++c) v[c] = interp_component<DIM, INTERP>(g, c, p, kp, pnan, I, V.v[c], errs);
 }
 
 // advect_particle: RK2 src/Particles/Advection/advection.jl:154-179 with
 // first/second_stage of src/Advection/RK2.jl (muladd(1, (alpha*dt)*v, p) etc.);
 // RK4 :261-279; Euler :348-367.
-template <int DIM, int METHOD>
+template <int DIM, int METHOD, int INTERP = kInterpLinear>
 __device__ __forceinline__ void advect_particle(const DevGrid& g, const CVel& V, const AdvParams& P,
                                                 const int* I, const double* p0, double* p, int* errs)
 {
     if (METHOD == JP_RUNGE_KUTTA2) {
         double v0[3], v1[3], p1[3];
-        interp_velocity<DIM>(g, V, p0, I, v0, errs);
+        interp_velocity<DIM, INTERP>(g, V, p0, I, v0, errs);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) p1[d] = fma(1.0, P.adt * v0[d], p0[d]);
-        interp_velocity<DIM>(g, V, p1, I, v1, errs);
+        interp_velocity<DIM, INTERP>(g, V, p1, I, v1, errs);
         if (P.half) {
 #pragma unroll
             for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, P.dt * v1[d], p0[d]);
@@ -166,22 +313,22 @@ __device__ __forceinline__ void advect_particle(const DevGrid& g, const CVel& V,
         }
     } else if (METHOD == JP_RUNGE_KUTTA4) {
         double k1[3], k2[3], k3[3], k4[3], q[3];
-        interp_velocity<DIM>(g, V, p0, I, k1, errs);
+        interp_velocity<DIM, INTERP>(g, V, p0, I, k1, errs);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) q[d] = p0[d] + (P.dt * k1[d]) * 0.5;  // x / 2 == x * 0.5 exactly
-        interp_velocity<DIM>(g, V, q, I, k2, errs);
+        interp_velocity<DIM, INTERP>(g, V, q, I, k2, errs);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) q[d] = p0[d] + (P.dt * k2[d]) * 0.5;
-        interp_velocity<DIM>(g, V, q, I, k3, errs);
+        interp_velocity<DIM, INTERP>(g, V, q, I, k3, errs);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) q[d] = p0[d] + P.dt * k3[d];
-        interp_velocity<DIM>(g, V, q, I, k4, errs);
+        interp_velocity<DIM, INTERP>(g, V, q, I, k4, errs);
 #pragma unroll
         for (int d = 0; d < DIM; ++d)
             p[d] = p0[d] + __ddiv_rn(P.dt * (((k1[d] + 2.0 * k2[d]) + 2.0 * k3[d]) + k4[d]), 6.0);
     } else {
         double v0[3];
-        interp_velocity<DIM>(g, V, p0, I, v0, errs);
+        interp_velocity<DIM, INTERP>(g, V, p0, I, v0, errs);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) p[d] = fma(1.0, P.dt * v0[d], p0[d]);
     }
@@ -189,7 +336,7 @@ __device__ __forceinline__ void advect_particle(const DevGrid& g, const CVel& V,
 
 // advection_kernel! (src/Particles/Advection/advection.jl:66-91): one warp per
 // 32 consecutive cells, work spread over the warp's live slots.
-template <int DIM, int METHOD>
+template <int DIM, int METHOD, int INTERP>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     advect_kernel(DevGrid g, CVel V, AdvParams P, Coords X, const uint8_t* __restrict__ index, int* d_err)
 {
@@ -217,7 +364,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         double p0[3], p[3];
 #pragma unroll
         for (int d = 0; d < DIM; ++d) p0[d] = X.c[d][a];
-        advect_particle<DIM, METHOD>(g, V, P, I, p0, p, &errs);
+        advect_particle<DIM, METHOD, INTERP>(g, V, P, I, p0, p, &errs);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) X.c[d][a] = p[d];
     }
@@ -422,6 +569,12 @@ cudaError_t launch_init(jp_particles* P, double* const coords[3], uint8_t* index
 cudaError_t launch_advection(jp_particles* P, int method, double alpha, const double* const V[3], double dt,
                              double* const coords[3], const uint8_t* index)
 {
+    return launch_advection_interp(P, method, kInterpLinear, alpha, V, dt, coords, index);
+}
+
+cudaError_t launch_advection_interp(jp_particles* P, int method, int interp, double alpha, const double* const V[3],
+                                    double dt, double* const coords[3], const uint8_t* index)
+{
     const bool d3 = P->g.ndim == 3;
     Coords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
     CVel Vv{{V[0], V[1], d3 ? V[2] : nullptr}};
@@ -435,16 +588,25 @@ cudaError_t launch_advection(jp_particles* P, int method, double alpha, const do
     const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
     const int nt = 32 * kWarpsPerBlock;
     cudaStream_t s = P->stream;
-#define JP_ADV(D, M) advect_kernel<D, M><<<nb, nt, 0, s>>>(P->g, Vv, ap, X, index, P->d_err)
-    if (!d3) {
-        if (method == JP_RUNGE_KUTTA2) JP_ADV(2, JP_RUNGE_KUTTA2);
-        else if (method == JP_RUNGE_KUTTA4) JP_ADV(2, JP_RUNGE_KUTTA4);
-        else JP_ADV(2, JP_EULER);
-    } else {
-        if (method == JP_RUNGE_KUTTA2) JP_ADV(3, JP_RUNGE_KUTTA2);
-        else if (method == JP_RUNGE_KUTTA4) JP_ADV(3, JP_RUNGE_KUTTA4);
-        else JP_ADV(3, JP_EULER);
-    }
+#define JP_ADV(D, M, IP) advect_kernel<D, M, IP><<<nb, nt, 0, s>>>(P->g, Vv, ap, X, index, P->d_err)
+#define JP_ADV_M(D, IP)                                  \
+    do {                                                 \
+        if (method == JP_RUNGE_KUTTA2) JP_ADV(D, JP_RUNGE_KUTTA2, IP); \
+        else if (method == JP_RUNGE_KUTTA4) JP_ADV(D, JP_RUNGE_KUTTA4, IP); \
+        else JP_ADV(D, JP_EULER, IP);                    \
+    } while (0)
+#define JP_ADV_I(D)                                                  \
+    do {                                                             \
+        if (interp == kInterpLinP) JP_ADV_M(D, kInterpLinP);         \
+        else if (interp == kInterpMQS) JP_ADV_M(D, kInterpMQS);      \
+        else JP_ADV_M(D, kInterpLinear);                             \
+    } while (0)
+    if (!d3)
+        JP_ADV_I(2);
+    else
+        JP_ADV_I(3);
+#undef JP_ADV_I
+#undef JP_ADV_M
 #undef JP_ADV
     return cudaGetLastError();
 }

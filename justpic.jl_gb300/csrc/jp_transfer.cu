@@ -370,6 +370,76 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// src/PhaseRatios/midpoints.jl:108-242 (3D edge midpoints), one thread per
+// cell I, offsets e = (1,1,0) xy, (0,1,1) yz, (1,0,1) xz: midpoint I + e at
+// the cell centre plus half the cell's spacing along e gathers the cells
+// min(I + e .* mask, n) for mask (1,0,0), (0,1,0), (0,0,1), (1,1,1) (a clamped
+// cell counts again). A cell first along an offset axis also writes midpoint
+// I and I + b (b: the offset axes where I is the last cell) from the
+// particles around the centre moved by half a spacing along b. Writes never
+// overlap when every axis has two cells or more.
+__constant__ int kMidOff[3][3] = {{1, 1, 0}, {0, 1, 1}, {1, 0, 1}};
+__constant__ int kMidMask[4][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 1}};
+
+__device__ __forceinline__ void midpoint_gather(const DevGrid& g, int nph, const double* __restrict__ phases,
+                                                const CCoords& X, const int64_t* I, const int* off,
+                                                const double* xm, double* w)
+{
+    for (int m = 0; m < 4; ++m) {
+        int64_t J[3];
+        double di[3], idi[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int64_t j = I[d] + off[d] * kMidMask[m][d];
+            J[d] = j < g.n[d] - 1 ? j : g.n[d] - 1;
+            di[d] = ldg(g.dxv[d] + J[d]);
+            idi[d] = ldg(g.ixv[d] + J[d]);
+        }
+        face_cell<3>(g, nph, phases, X, cell_linear<3>(g, J), xm, di, idi, w);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    phase_midpoint_kernel(DevGrid g, int nph, const double* __restrict__ phases, CCoords X, int which,
+                          double* __restrict__ out)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    int off[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) off[d] = kMidOff[which][d];
+    int64_t I[3];
+    cell_coords(g, c, I);
+    const int64_t Mn[3] = {g.n[0] + off[0], g.n[1] + off[1], g.n[2] + off[2]};
+    const int64_t nm = Mn[0] * Mn[1] * Mn[2];
+    double xcen[3], di[3], xm[3], w[kMaxPhases];
+    for (int k = 0; k < kMaxPhases; ++k) w[k] = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        xcen[d] = ldg(g.xc[d] + I[d]);
+        di[d] = ldg(g.dxv[d] + I[d]);
+        xm[d] = xcen[d] + (di[d] * (double)off[d]) / 2.0;
+    }
+    midpoint_gather(g, nph, phases, X, I, off, xm, w);
+    store_normalised(w, nph, out, (I[0] + off[0]) + Mn[0] * ((I[1] + off[1]) + Mn[1] * (I[2] + off[2])), nm, true);
+    bool first = false;
+    int b[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        first |= off[d] && I[d] == 0;
+        b[d] = (off[d] && I[d] == g.n[d] - 1) ? 1 : 0;
+    }
+    if (!first) return;
+    double xb[3];
+    for (int k = 0; k < kMaxPhases; ++k) w[k] = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xb[d] = xcen[d] - ((di[d] * (double)off[d]) * (double)(0 - b[d])) / 2.0;
+    midpoint_gather(g, nph, phases, X, I, off, xb, w);
+    store_normalised(w, nph, out, I[0] + Mn[0] * (I[1] + Mn[1] * I[2]), nm, true);
+    if (b[0] | b[1] | b[2])
+        store_normalised(w, nph, out, (I[0] + b[0]) + Mn[0] * ((I[1] + b[1]) + Mn[1] * (I[2] + b[2])), nm, true);
+}
+
 // ------------------------------------------------------------ launchers
 cudaError_t launch_g2p_flip(jp_particles* P, double* Fp, const double* F, const double* F0, double alpha,
                             const double* const coords[3], const uint8_t* index)
@@ -429,6 +499,16 @@ cudaError_t launch_phase_ratios(jp_particles* P, int nph, const double* phases, 
         for (int d = 0; d < 2; ++d)
             if (faces && faces[d]) phase_face_kernel<2><<<nb, kThreads, 0, st>>>(P->g, nph, phases, X, d, faces[d]);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phase_midpoints(jp_particles* P, int nph, const double* phases, const double* const coords[3],
+                                   double* const mids[3])
+{
+    CCoords X{{coords[0], coords[1], coords[2]}};
+    const unsigned nb = grid_blocks(P->g.ncells);
+    for (int w = 0; w < 3; ++w)
+        if (mids[w]) phase_midpoint_kernel<<<nb, kThreads, 0, P->stream>>>(P->g, nph, phases, X, w, mids[w]);
     return cudaGetLastError();
 }
 

@@ -154,8 +154,16 @@ void jpo_init_particles(const jpo_grid* g, double* const coords[3], uint8_t* ind
  * src/Advection/advection.jl:3-47): Inf outside the component grid's limits,
  * else bisection seeded by the cell index, corner values and N-linear lerp.
  */
+static double linp_value(const jpo_grid* g, int comp, const double* V, const double* p, const int64_t* idx,
+                         const double* xc, const double* dx, double VL);
+static double mqs_value(const jpo_grid* g, int comp, const double* V, const int64_t* idx, const double* v,
+                        const double* t);
+
+/* `interp`: the velocity interpolation of the advection call, 0 N-linear
+   (advection!), JPO_INTERP_LINP (advection_LinP!) or JPO_INTERP_MQS
+   (advection_MQS!) */
 static double interp_component(const jpo_grid* g, int comp, const double* p, const int64_t* I,
-                               const double* V, int* err)
+                               const double* V, int* err, int interp)
 {
     const int N = g->ndim;
     for (int d = 0; d < N; ++d) {
@@ -164,12 +172,14 @@ static double interp_component(const jpo_grid* g, int comp, const double* p, con
         if (!(x[0] <= p[d] && p[d] <= x[L - 1])) return INFINITY;
     }
     int64_t idx[3] = {0, 0, 0};
-    double t[3];
+    double t[3], xcs[3], dxs[3];
     for (int d = 0; d < N; ++d) {
         const double* x = g->xvel[comp][d];
         idx[d] = jpo_bisection(p[d], x, g->nvel[comp][d], I[d], err);
         const double xc = x[idx[d]];
         const double dx = g->dxvel[comp][d][idx[d]];
+        xcs[d] = xc;
+        dxs[d] = dx;
         t[d] = (p[d] - xc) * (1.0 / dx);
     }
     const int64_t L0 = g->nvel[comp][0], L1 = g->nvel[comp][1];
@@ -192,13 +202,159 @@ static double interp_component(const jpo_grid* g, int comp, const double* p, con
         v[6] = V[b + sz + L0];
         v[7] = V[b + sz + L0 + 1];
     }
-    return lerpN(N, v, t);
+    const double VL = lerpN(N, v, t);
+    if (interp == 0) return VL;
+    /* away from the edges only: 1 < index < size - 1 (1-based) on every axis */
+    for (int d = 0; d < N; ++d)
+        if (!(idx[d] >= 1 && idx[d] <= g->nvel[comp][d] - 3)) return VL;
+    if (interp == JPO_INTERP_LINP) return linp_value(g, comp, V, p, idx, xcs, dxs, VL);
+    return mqs_value(g, comp, V, idx, v, t);
+}
+
+/* F(i, j[, k]) of a component grid, indices clamped to the grid */
+static inline double vel_at(const jpo_grid* g, int comp, const double* V, int64_t i, int64_t j, int64_t k)
+{
+    const int64_t L0 = g->nvel[comp][0], L1 = g->nvel[comp][1], L2 = g->ndim == 3 ? g->nvel[comp][2] : 1;
+    i = i < 0 ? 0 : (i > L0 - 1 ? L0 - 1 : i);
+    j = j < 0 ? 0 : (j > L1 - 1 ? L1 - 1 : j);
+    k = k < 0 ? 0 : (k > L2 - 1 ? L2 - 1 : k);
+    return V[i + L0 * (j + L1 * k)];
+}
+
+/* LinP (src/Particles/Advection/advection_LinP.jl:92-391) for component
+   `comp` at a cell away from the grid's edges: VL (the N-linear value) blended
+   with the N-linear interpolation of velocities averaged to the pressure
+   points, 2/3 VL + (1 - 2/3) VP, without fused operations. */
+static double linp_value(const jpo_grid* g, int comp, const double* V, const double* p, const int64_t* idx,
+                         const double* xc, const double* dx, double VL)
+{
+    const int N = g->ndim;
+    int64_t b[3] = {idx[0], idx[1], N == 3 ? idx[2] : 0};
+    /* offset_LinP: +1 past the middle of the interval along the component axis */
+    b[comp] += p[comp] > xc[comp] + dx[comp] / 2.0 ? 1 : 0;
+    /* rows of augment_offset (:352-391): the shifts of rows 2..4 */
+    int64_t row[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    const int r2 = comp == 1 ? 0 : 1; /* row 2 shifts x (y-component) or y */
+    const int r3 = comp == 2 ? 0 : 2; /* row 3 shifts x (z-component) or z */
+    row[1][r2] = 1;
+    if (N == 3) { /* row 4 = the shifts of rows 2 and 3 together */
+        row[2][r3] = 1;
+        row[3][r2] = 1;
+        row[3][r3] = 1;
+    }
+    const int nrows = N == 3 ? 4 : 2;
+    double av[8];
+    for (int r = 0; r < nrows; ++r) {
+        double f[3];
+        for (int s = -1; s <= 1; ++s) {
+            int64_t q[3] = {b[0] + row[r][0], b[1] + row[r][1], b[2] + row[r][2]};
+            q[comp] += s;
+            f[s + 1] = vel_at(g, comp, V, q[0], q[1], q[2]);
+        }
+        av[2 * r] = (f[0] + f[1]) / 2.0;
+        av[2 * r + 1] = (f[2] + f[1]) / 2.0;
+    }
+    double FP[8];
+    if (comp == 0) {
+        for (int k = 0; k < 2 * nrows; ++k) FP[k] = av[k];
+    } else { /* swap_F: (1, 3, 2, 4, 5, 7, 6, 8) */
+        static const int SW[8] = {0, 2, 1, 3, 4, 6, 5, 7};
+        for (int k = 0; k < 2 * nrows; ++k) FP[k] = av[SW[k]];
+    }
+    /* correct_xci_to_pressure_point (:151-189) */
+    double xP[3] = {xc[0], xc[1], N == 3 ? xc[2] : 0.0};
+    const int off = 1 - 2 * (p[comp] < xc[comp] + dx[comp] / 2.0);
+    xP[comp] = xc[comp] + ((double)off * dx[comp]) / 2.0;
+    double tP[3];
+    for (int d = 0; d < N; ++d) tP[d] = (p[d] - xP[d]) * (1.0 / dx[d]);
+    const double VP = lerpN(N, FP, tP);
+    const double A = 2.0 / 3.0;
+    const double a = A * VL;
+    const double bb = (1.0 - A) * VP;
+    return a + bb;
+}
+
+/* half * (t - half)^2 * (muladd(-2, v1, v0) + v2) (src/Interpolations/MQS.jl) */
+static inline double mqs_correction(double t, double v0, double v1, double v2)
+{
+    const double d = t - 0.5;
+    const double q = 0.5 * (d * d);
+    const double s = fma(-2.0, v1, v0) + v2;
+    return q * s;
+}
+
+/* one MQS pair: lerp of (a, b) at t plus the curvature correction, with the
+   stencil extended below (lo) or above (hi) */
+static inline double mqs_edge(double t, double a, double b, double lo, double hi)
+{
+    const double l = lerp1(t, a, b);
+    const double c = t < 0.5 ? mqs_correction(t, lo, a, b) : mqs_correction(t, a, b, hi);
+    return l + c;
+}
+
+/* MQS (src/Interpolations/MQS.jl:1-131) for component `comp` at a cell away
+   from the grid's edges; v are the corner values, t the normalised position. */
+static double mqs_value(const jpo_grid* g, int comp, const double* V, const int64_t* idx, const double* v,
+                        const double* t)
+{
+    const int64_t i = idx[0], j = idx[1];
+    if (g->ndim == 2) {
+        if (comp == 0) { /* MQS-x: corrections along x, then lerp along y */
+            const double r0 = mqs_edge(t[0], v[0], v[1], vel_at(g, 0, V, i - 1, j, 0), vel_at(g, 0, V, i + 2, j, 0));
+            const double r1 =
+                mqs_edge(t[0], v[2], v[3], vel_at(g, 0, V, i - 1, j + 1, 0), vel_at(g, 0, V, i + 2, j + 1, 0));
+            return lerp1(t[1], r0, r1);
+        }
+        const double r0 = mqs_edge(t[1], v[0], v[2], vel_at(g, 1, V, i, j - 1, 0), vel_at(g, 1, V, i, j + 2, 0));
+        const double r1 =
+            mqs_edge(t[1], v[1], v[3], vel_at(g, 1, V, i + 1, j - 1, 0), vel_at(g, 1, V, i + 1, j + 2, 0));
+        return lerp1(t[0], r0, r1);
+    }
+    const int64_t k = idx[2];
+    if (comp == 0 || comp == 1) { /* the 2D pair at layers k and k + 1, both with the stencil of layer k */
+        double r[2];
+        for (int h = 0; h < 2; ++h) {
+            const double* w = v + 4 * h;
+            double e0, e1;
+            if (comp == 0) {
+                e0 = mqs_edge(t[0], w[0], w[1], vel_at(g, 0, V, i - 1, j, k), vel_at(g, 0, V, i + 2, j, k));
+                e1 = mqs_edge(t[0], w[2], w[3], vel_at(g, 0, V, i - 1, j + 1, k), vel_at(g, 0, V, i + 2, j + 1, k));
+                r[h] = lerp1(t[1], e0, e1);
+            } else {
+                e0 = mqs_edge(t[1], w[0], w[2], vel_at(g, 1, V, i, j - 1, k), vel_at(g, 1, V, i, j + 2, k));
+                e1 = mqs_edge(t[1], w[1], w[3], vel_at(g, 1, V, i + 1, j - 1, k), vel_at(g, 1, V, i + 1, j + 2, k));
+                r[h] = lerp1(t[0], e0, e1);
+            }
+        }
+        return lerp1(t[2], r[0], r[1]);
+    }
+    /* MQS-z: front (v1, v2, v5, v6) and back (v3, v4, v7, v8) with the stencil
+       of row j, corrections along x, lerp along z, then along y */
+    double r[2];
+    for (int h = 0; h < 2; ++h) {
+        const double w[4] = {v[2 * h], v[2 * h + 1], v[2 * h + 4], v[2 * h + 5]};
+        const double e0 = mqs_edge(t[0], w[0], w[1], vel_at(g, 2, V, i - 1, j, k), vel_at(g, 2, V, i + 2, j, k));
+        const double e1 =
+            mqs_edge(t[0], w[2], w[3], vel_at(g, 2, V, i - 1, j, k + 1), vel_at(g, 2, V, i + 2, j, k + 1));
+        r[h] = lerp1(t[2], e0, e1);
+    }
+    return lerp1(t[1], r[0], r[1]);
 }
 
 static void interp_velocity(const jpo_grid* g, const double* p, const int64_t* I,
-                            const double* const V[3], double* v, int* err)
+                            const double* const V[3], double* v, int* err, int interp)
 {
-    for (int c = 0; c < g->ndim; ++c) v[c] = interp_component(g, c, p, I, V[c], err);
+    for (int c = 0; c < g->ndim; ++c) v[c] = interp_component(g, c, p, I, V[c], err, interp);
+}
+
+/* one velocity sample (interp_velocity2particle[_LinP|_MQS]) at p, bisection
+   seeded by the 0-based cell I */
+int jpo_interp_velocity(const jpo_grid* g, int interp, const double* const V[3], const double* p,
+                        const int64_t* I, double* v)
+{
+    int err = 0;
+    interp_velocity(g, p, I, V, v, &err, interp);
+    return err;
 }
 
 void jpo_first_stage(int method, double alpha, double dt, int n, const double* v,
@@ -232,38 +388,48 @@ void jpo_second_stage(double alpha, double dt, int n, const double* v0, const do
 }
 
 static void advect_particle(const jpo_grid* g, int method, double alpha, const double* const V[3],
-                            double dt, const int64_t* I, const double* p0, double* pout, int* err)
+                            double dt, const int64_t* I, const double* p0, double* pout, int* err, int interp)
 {
     const int N = g->ndim;
     if (method == JPO_RK2) {
         /* src/Particles/Advection/advection.jl:154-179 */
         double v0[3], v1[3], p1[3];
-        interp_velocity(g, p0, I, V, v0, err);
+        interp_velocity(g, p0, I, V, v0, err, interp);
         jpo_first_stage(JPO_RK2, alpha, dt, N, v0, p0, p1);
-        interp_velocity(g, p1, I, V, v1, err);
+        interp_velocity(g, p1, I, V, v1, err, interp);
         jpo_second_stage(alpha, dt, N, v0, v1, p0, pout);
     } else if (method == JPO_RK4) {
         /* src/Particles/Advection/advection.jl:261-279 (no muladd) */
         double k1[3], k2[3], k3[3], k4[3], q[3];
-        interp_velocity(g, p0, I, V, k1, err);
+        interp_velocity(g, p0, I, V, k1, err, interp);
         for (int d = 0; d < N; ++d) q[d] = p0[d] + (dt * k1[d]) / 2.0;
-        interp_velocity(g, q, I, V, k2, err);
+        interp_velocity(g, q, I, V, k2, err, interp);
         for (int d = 0; d < N; ++d) q[d] = p0[d] + (dt * k2[d]) / 2.0;
-        interp_velocity(g, q, I, V, k3, err);
+        interp_velocity(g, q, I, V, k3, err, interp);
         for (int d = 0; d < N; ++d) q[d] = p0[d] + dt * k3[d];
-        interp_velocity(g, q, I, V, k4, err);
+        interp_velocity(g, q, I, V, k4, err, interp);
         for (int d = 0; d < N; ++d)
             pout[d] = p0[d] + (dt * (((k1[d] + 2.0 * k2[d]) + 2.0 * k3[d]) + k4[d])) / 6.0;
     } else {
         /* src/Particles/Advection/advection.jl:348-367 */
         double v0[3];
-        interp_velocity(g, p0, I, V, v0, err);
+        interp_velocity(g, p0, I, V, v0, err, interp);
         jpo_first_stage(JPO_EULER, alpha, dt, N, v0, p0, pout);
     }
 }
 
 int jpo_advection(const jpo_grid* g, int method, double alpha, const double* const V[3],
                   double dt, double* const coords[3], const uint8_t* index)
+{
+    return jpo_advection_interp(g, method, 0, alpha, V, dt, coords, index);
+}
+
+/* advection! / advection_LinP! / advection_MQS!
+   (src/Particles/Advection/advection.jl:21-91, advection_LinP.jl:27-90,
+   advection_MQS.jl:30-94): the same integrators, with the velocity
+   interpolation `interp` */
+int jpo_advection_interp(const jpo_grid* g, int method, int interp, double alpha, const double* const V[3],
+                         double dt, double* const coords[3], const uint8_t* index)
 {
     const int N = g->ndim;
     const int64_t nc = g->ncells;
@@ -278,7 +444,7 @@ int jpo_advection(const jpo_grid* g, int method, double alpha, const double* con
             if (!index[c + nc * s]) continue;
             double p0[3], p[3];
             for (int d = 0; d < N; ++d) p0[d] = coords[d][c + nc * s];
-            advect_particle(g, method, alpha, V, dt, I, p0, p, &err);
+            advect_particle(g, method, alpha, V, dt, I, p0, p, &err, interp);
             for (int d = 0; d < N; ++d) coords[d][c + nc * s] = p[d];
         }
     }
@@ -1036,6 +1202,76 @@ void jpo_phase_ratios_face(const jpo_grid* g, int nph, const double* phases, con
             normalise(nph, wb);
             const int64_t fb = I[0] + F[0] * (I[1] + F[1] * I[2]);
             for (int k = 0; k < nph; ++k) out[fb + nf * k] = isnan(wb[k]) ? 0.0 : wb[k];
+        }
+    }
+}
+
+/* phase_ratios_midpoint! (src/PhaseRatios/midpoints.jl:108-242), 3D: the
+   edge midpoints `which` = 0 (xy, offsets (1,1,0)), 1 (yz, (0,1,1)), 2 (xz,
+   (1,0,1)). Per cell I the midpoint I + offsets sits at the cell centre plus
+   half the cell's spacing along the offset axes and gathers the cells
+   min(I + offsets .* mask, n) for mask (1,0,0), (0,1,0), (0,0,1), (1,1,1) in
+   that order (a clamped cell is visited again). A cell on a first boundary
+   of an offset axis also writes midpoint I, and midpoint I + b where b marks
+   the offset axes on which I is the last cell, both from the particles
+   around the cell centre moved by half a spacing along b. Midpoints without
+   particles get 0. Output shape: n + offsets. */
+void jpo_phase_ratios_midpoint(const jpo_grid* g, int nph, const double* phases, const double* const coords[3],
+                               int which, double* out)
+{
+    static const int OFF[3][3] = {{1, 1, 0}, {0, 1, 1}, {1, 0, 1}};
+    static const int MASK[4][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 1}};
+    const int* off = OFF[which];
+    const int64_t nc = g->ncells;
+    const int64_t Mn[3] = {g->n[0] + off[0], g->n[1] + off[1], g->n[2] + off[2]};
+    const int64_t nm = Mn[0] * Mn[1] * Mn[2];
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t c = 0; c < nc; ++c) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        double xcen[3], di[3], xm[3], w[JPO_MAX_PHASES] = {0};
+        cell_spacing(g, I, di);
+        for (int d = 0; d < 3; ++d) {
+            xcen[d] = g->xc[d][I[d]];
+            xm[d] = xcen[d] + (di[d] * (double)off[d]) / 2.0;
+        }
+        for (int m = 0; m < 4; ++m) {
+            int64_t J[3];
+            for (int d = 0; d < 3; ++d) {
+                const int64_t j = I[d] + off[d] * MASK[m][d];
+                J[d] = j < g->n[d] - 1 ? j : g->n[d] - 1;
+            }
+            double dj[3];
+            cell_spacing(g, J, dj);
+            face_cell_particles(g, nph, phases, coords, J[0] + g->n[0] * (J[1] + g->n[1] * J[2]), xm, dj, w);
+        }
+        normalise(nph, w);
+        const int64_t mo = (I[0] + off[0]) + Mn[0] * ((I[1] + off[1]) + Mn[1] * (I[2] + off[2]));
+        for (int k = 0; k < nph; ++k) out[mo + nm * k] = isnan(w[k]) ? 0.0 : w[k];
+        /* isboundary (utils.jl:86-91): the first cell along an offset axis */
+        int first = 0, b[3];
+        for (int d = 0; d < 3; ++d) {
+            first |= off[d] && I[d] == 0;
+            b[d] = off[d] && I[d] == g->n[d] - 1; /* lastboundary_offset, midpoints.jl:226-229 */
+        }
+        if (!first) continue;
+        double xb[3], wb[JPO_MAX_PHASES] = {0};
+        for (int d = 0; d < 3; ++d) xb[d] = xcen[d] - ((di[d] * (double)off[d]) * (double)(0 - b[d])) / 2.0;
+        for (int m = 0; m < 4; ++m) {
+            int64_t J[3];
+            for (int d = 0; d < 3; ++d) {
+                const int64_t j = I[d] + off[d] * MASK[m][d];
+                J[d] = j < g->n[d] - 1 ? j : g->n[d] - 1;
+            }
+            double dj[3];
+            cell_spacing(g, J, dj);
+            face_cell_particles(g, nph, phases, coords, J[0] + g->n[0] * (J[1] + g->n[1] * J[2]), xb, dj, wb);
+        }
+        normalise(nph, wb);
+        for (int r = 0; r < 2; ++r) {
+            const int64_t K[3] = {I[0] + r * b[0], I[1] + r * b[1], I[2] + r * b[2]};
+            const int64_t ko = K[0] + Mn[0] * (K[1] + Mn[1] * K[2]);
+            for (int k = 0; k < nph; ++k) out[ko + nm * k] = isnan(wb[k]) ? 0.0 : wb[k];
         }
     }
 }

@@ -50,6 +50,8 @@ typedef struct jpo_grid {
 #define JPO_EULER 0
 #define JPO_RK2 1
 #define JPO_RK4 2
+#define JPO_INTERP_LINP 1
+#define JPO_INTERP_MQS 2
 
 void jpo_set_threads(int nthreads);
 
@@ -59,6 +61,10 @@ void jpo_init_particles(const jpo_grid* g, double* const coords[3], uint8_t* ind
 /* advection!: src/Particles/Advection/advection.jl:35-91 */
 int jpo_advection(const jpo_grid* g, int method, double alpha, const double* const V[3],
                   double dt, double* const coords[3], const uint8_t* index);
+int jpo_advection_interp(const jpo_grid* g, int method, int interp, double alpha, const double* const V[3],
+                         double dt, double* const coords[3], const uint8_t* index);
+int jpo_interp_velocity(const jpo_grid* g, int interp, const double* const V[3], const double* p,
+                        const int64_t* I, double* v);
 
 /* move_particles!: src/Particles/move_safe.jl:21-125 */
 int jpo_move_particles(const jpo_grid* g, double* const coords[3], uint8_t* index,
@@ -101,6 +107,8 @@ void jpo_phase_ratios_vertex(const jpo_grid* g, int nph, const double* phases, c
                              double* out);
 void jpo_phase_ratios_face(const jpo_grid* g, int nph, const double* phases, const double* const coords[3],
                            int dim, double* out);
+void jpo_phase_ratios_midpoint(const jpo_grid* g, int nph, const double* phases, const double* const coords[3],
+                               int which, double* out);
 
 /* forward-mode derivatives (jp_oracle_jvp.c): the same calls on (value,
    tangent) pairs; dV / dFp may be NULL (zero tangent) */

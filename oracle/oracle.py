@@ -23,6 +23,9 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libjp_oracle.so")
 
 EULER, RK2, RK4 = 0, 1, 2
+LINEAR, LINP, MQS = 0, 1, 2  # velocity interpolation of advection!, advection_LinP!, advection_MQS!
+# 3D edge midpoints of update_phase_ratios! (src/PhaseRatios/midpoints.jl:214-224)
+MIDPOINTS = (("xy", (1, 1, 0)), ("yz", (0, 1, 1)), ("xz", (1, 0, 1)))
 ERR_BISECTION_LIMIT, ERR_FAR_MOVE, ERR_NO_NEIGHBOUR = 0x1, 0x2, 0x4
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -71,6 +74,11 @@ def lib():
         L.jpo_init_particles.argtypes = [G, P3, ctypes.c_void_p]
         L.jpo_advection.argtypes = [G, ctypes.c_int, ctypes.c_double, P3, ctypes.c_double, P3, ctypes.c_void_p]
         L.jpo_advection.restype = ctypes.c_int
+        L.jpo_advection_interp.argtypes = [G, ctypes.c_int, ctypes.c_int, ctypes.c_double, P3, ctypes.c_double, P3,
+                                           ctypes.c_void_p]
+        L.jpo_advection_interp.restype = ctypes.c_int
+        L.jpo_interp_velocity.argtypes = [G, ctypes.c_int, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.jpo_interp_velocity.restype = ctypes.c_int
         L.jpo_move_particles.argtypes = [G, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.jpo_move_particles.restype = ctypes.c_int
         L.jpo_inject_particles.argtypes = [G, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32]
@@ -87,6 +95,7 @@ def lib():
         L.jpo_phase_ratios_center.argtypes = [G, ctypes.c_int, ctypes.c_void_p, P3, ctypes.c_void_p]
         L.jpo_phase_ratios_vertex.argtypes = [G, ctypes.c_int, ctypes.c_void_p, P3, ctypes.c_void_p]
         L.jpo_phase_ratios_face.argtypes = [G, ctypes.c_int, ctypes.c_void_p, P3, ctypes.c_int, ctypes.c_void_p]
+        L.jpo_phase_ratios_midpoint.argtypes = [G, ctypes.c_int, ctypes.c_void_p, P3, ctypes.c_int, ctypes.c_void_p]
         L.jpo_advection_jvp.argtypes = [G, ctypes.c_int, ctypes.c_double, P3, P3, ctypes.c_double, P3, P3,
                                         ctypes.c_void_p]
         L.jpo_advection_jvp.restype = ctypes.c_int
@@ -220,11 +229,21 @@ class OracleParticles:
     def init_particles(self):
         lib().jpo_init_particles(ctypes.byref(self._g), self._p3(self.coords), _ptr(self.index))
 
-    def advection(self, method, alpha, V, dt):
+    def advection(self, method, alpha, V, dt, interp=LINEAR):
+        """advection! (interp LINEAR), advection_LinP! (LINP) or advection_MQS! (MQS)."""
         V = [np.asfortranarray(v, dtype=np.float64) for v in V]
         self._keep = V
-        return lib().jpo_advection(ctypes.byref(self._g), int(method), float(alpha), self._p3(V), float(dt),
-                                   self._p3(self.coords), _ptr(self.index))
+        return lib().jpo_advection_interp(ctypes.byref(self._g), int(method), int(interp), float(alpha),
+                                          self._p3(V), float(dt), self._p3(self.coords), _ptr(self.index))
+
+    def interp_velocity(self, V, p, I, interp=LINEAR):
+        """One velocity sample at point p, the bisection seeded by 0-based cell I."""
+        V = [np.asfortranarray(v, dtype=np.float64) for v in V]
+        pa = np.ascontiguousarray(p, dtype=np.float64)
+        Ia = np.ascontiguousarray(I, dtype=np.int64)
+        out = np.zeros(self.ndim)
+        lib().jpo_interp_velocity(ctypes.byref(self._g), int(interp), self._p3(V), _ptr(pa), _ptr(Ia), _ptr(out))
+        return out
 
     def move_particles(self, args=()):
         a, n = self._args(args)
@@ -277,9 +296,9 @@ class OracleParticles:
 
     # -- phase ratios (src/PhaseRatios/) ---------------------------------
     def phase_ratios(self, phases, nphases):
-        """update_phase_ratios! without the 3D edge midpoints: dict of arrays
-        (nphases, nodes) for 'center', 'vertex' and the faces 'Vx', 'Vy' (, 'Vz');
-        node index column-major over the location's grid."""
+        """update_phase_ratios!: dict of arrays (nphases, nodes) for 'center',
+        'vertex', the faces 'Vx', 'Vy' (, 'Vz') and in 3D the edge midpoints
+        'xy', 'yz', 'xz'; node index column-major over the location's grid."""
         N = self.ndim
         G = ctypes.byref(self._g)
         c3 = self._p3(self.coords)
@@ -292,6 +311,11 @@ class OracleParticles:
             nf = int(np.prod([n + (1 if e == d else 0) for e, n in enumerate(self.n)]))
             out[name] = np.zeros((nphases, nf))
             lib().jpo_phase_ratios_face(G, int(nphases), _ptr(phases), c3, d, _ptr(out[name]))
+        if N == 3:
+            for which, (name, off) in enumerate(MIDPOINTS):
+                nm = int(np.prod([n + o for n, o in zip(self.n, off)]))
+                out[name] = np.zeros((nphases, nm))
+                lib().jpo_phase_ratios_midpoint(G, int(nphases), _ptr(phases), c3, which, _ptr(out[name]))
         return out
 
     # -- forward-mode derivatives (dual numbers through the same code) ----

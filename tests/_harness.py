@@ -11,6 +11,11 @@ import justpic_gb300 as jp
 from justpic_gb300 import workloads as W
 from oracle import oracle as O
 
+INTERPS = {  # advection!, advection_LinP!, advection_MQS!
+    "linear": (O.LINEAR, jp.advection_),
+    "linp": (O.LINP, jp.advection_LinP_),
+    "mqs": (O.MQS, jp.advection_MQS_),
+}
 METHODS = {
     "euler": (O.EULER, jp.Euler(), 0.5),
     "rk2": (O.RK2, jp.RungeKutta2(), 0.5),
@@ -56,10 +61,11 @@ class Pair:
         self.pf = list(jp.init_cell_arrays(self.p, nfields))
 
     # -- mirrored operations -------------------------------------------
-    def advection(self, method, V, dt):
+    def advection(self, method, V, dt, interp="linear"):
         om, pm, alpha = METHODS[method]
-        err = self.o.advection(om, alpha, V, dt)
-        jp.advection_(self.p, pm, tuple(jp.TA("CUDA")(v) for v in V), dt)
+        oi, fn = INTERPS[interp]
+        err = self.o.advection(om, alpha, V, dt, oi)
+        fn(self.p, pm, tuple(jp.TA("CUDA")(v) for v in V), dt)
         return err
 
     def move(self):

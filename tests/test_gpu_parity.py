@@ -34,6 +34,27 @@ def test_advection_bit_exact(method, ni):
     pair.assert_same(f"advection {method}")
 
 
+@pytest.mark.parametrize("interp", ["linp", "mqs"])
+@pytest.mark.parametrize("method", ["euler", "rk2_23", "rk4"])
+@pytest.mark.parametrize("ni,refined", [((16, 16), False), ((11, 9), True), ((6, 5, 7), False),
+                                         ((5, 6, 4), True)])
+def test_advection_linp_mqs_bit_exact(interp, method, ni, refined):
+    """advection_LinP! / advection_MQS! against the oracle, then a full step
+    (move_particles! + inject_particles!) so the next advection starts from
+    relocated particles."""
+    pair, g = _setup(ni, refined=refined)
+    rng = np.random.default_rng(8)
+    V = W.stream_velocity(g) if len(ni) == 2 else W.stream_velocity_3d(g)
+    V = tuple(np.asfortranarray(v * (1.0 + 0.2 * rng.standard_normal(v.shape))) for v in V)
+    dt = W.cfl_dt(g, V, 0.5)
+    for step in range(2):
+        assert pair.advection(method, V, dt, interp) == 0
+        pair.assert_same(f"advection {interp} {method} step {step}")
+        pair.move()
+        pair.inject()
+        pair.assert_same(f"move+inject after {interp} step {step}")
+
+
 def test_advection_outside_limits_gives_inf():
     # a step far beyond the velocity grid sends particles to Inf (advection.jl:104-108)
     pair, g = _setup((8, 8))

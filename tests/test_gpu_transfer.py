@@ -88,6 +88,11 @@ def test_phase_ratios_bit_exact(ni, refined, nphases):
     assert_bits_equal(ref["vertex"], pr.vertex.cpu().numpy(), "vertex")
     for d, name in enumerate(["Vx", "Vy", "Vz"][:len(ni)]):
         assert_bits_equal(ref[name], pr.faces[d].cpu().numpy(), name)
+    if len(ni) == 3:
+        for name in ("xy", "yz", "xz"):
+            assert_bits_equal(ref[name], getattr(pr, name).cpu().numpy(), name)
+            s = getattr(pr, name).sum(dim=0).cpu().numpy()
+            assert np.all((np.abs(s - 1.0) < 1e-12) | (s == 0.0)), name
 
 
 def _set_field(pair, k, values):

@@ -302,3 +302,58 @@ def test_inject_phase_clamps_to_corner_extrema():
     assert len(vals) > 0
     assert vals.min() >= corners.min() and vals.max() <= corners.max()
     assert np.all(ids[:, 0][live[:, 0]] == 1.0)
+
+
+def _midpoint_ratios_loops(P, phases, nph, off):
+    """Plain-loop restatement of phase_ratios_midpoint! (src/PhaseRatios/midpoints.jl:128-212)
+    in 1-based indices, for a cross-check of the oracle on a small grid."""
+    n = P.n
+    xc = [np.asarray(P.xc[d]) for d in range(3)]
+    dx = [np.asarray(P.dxv[d]) for d in range(3)]
+    Mn = tuple(n[d] + off[d] for d in range(3))
+    out = np.zeros((nph,) + Mn)
+    masks = ((1, 0, 0), (0, 1, 0), (0, 0, 1), (1, 1, 1))
+
+    def gather(I, xm):
+        w = np.zeros(nph)
+        for mask in masks:
+            J = tuple(min(I[d] + off[d] * mask[d], n[d]) for d in range(3))
+            di = [dx[d][J[d] - 1] for d in range(3)]
+            c = (J[0] - 1) + n[0] * ((J[1] - 1) + n[1] * (J[2] - 1))
+            for s in range(P.max_xcell):
+                p = [P.coords[d][s, c] for d in range(3)]
+                if any(np.isnan(p)) or not all(abs(p[d] - xm[d]) <= di[d] / 2 for d in range(3)):
+                    continue
+                x = np.prod([1.0 - abs(xm[d] - p[d]) / di[d] for d in range(3)])
+                if not np.isnan(phases[s, c]):
+                    w[int(phases[s, c]) - 1] += x
+        w = w / w.sum() if w.sum() != 0 else w * np.nan
+        return np.where(np.isnan(w), 0.0, w)
+
+    for k in range(1, n[2] + 1):
+        for j in range(1, n[1] + 1):
+            for i in range(1, n[0] + 1):
+                I = (i, j, k)
+                cc = [xc[d][I[d] - 1] for d in range(3)]
+                di = [dx[d][I[d] - 1] for d in range(3)]
+                out[(slice(None),) + tuple(I[d] + off[d] - 1 for d in range(3))] = \
+                    gather(I, [cc[d] + di[d] * off[d] / 2 for d in range(3)])
+                if any(off[d] * I[d] == 1 for d in range(3)):
+                    b = [int(n[d] == off[d] * I[d]) for d in range(3)]
+                    w = gather(I, [cc[d] + di[d] * off[d] * b[d] / 2 for d in range(3)])
+                    for r in (0, 1):
+                        out[(slice(None),) + tuple(I[d] - 1 + r * b[d] for d in range(3))] = w
+    return out.reshape(nph, -1, order="F")
+
+
+def test_phase_ratios_midpoints_against_loops():
+    g = W.grid((3, 4, 3))
+    P = _oracle_particles(g, 8, 16, 4)
+    rng = np.random.default_rng(9)
+    ph = np.where(P.index.astype(bool), rng.integers(1, 4, P.index.shape).astype(np.float64), np.nan)
+    ref = P.phase_ratios(ph, 3)
+    for name, off in O.MIDPOINTS:
+        np.testing.assert_allclose(ref[name], _midpoint_ratios_loops(P, ph, 3, off), rtol=1e-13, atol=1e-15,
+                                   err_msg=name)
+        s = ref[name].sum(axis=0)
+        assert np.all((np.abs(s - 1) < 1e-12) | (s == 0))
