@@ -225,6 +225,19 @@ int jp_phase_ratios(jp_particles* p, int32_t nphases, const double* phases, cons
 int jp_phase_ratios_midpoints(jp_particles* p, int32_t nphases, const double* phases,
                               const double* const coords[3], double* const mids[3]);
 int jp_centroid2particle(jp_particles* p, double* Fp, const double* F, const double* const coords[3]);
+
+/*
+ * CellArray layout conversion (src/CellArrays/conversion.jl:36-41,
+ * ext/JustPICCUDAExt.jl:178-191, the permutedims(data, (3, 2, 1)) between
+ * the GPU and CPU CellArrays): component k of node c sits at c + nnodes * k
+ * in the GPU form (blocklength 0) and at k + ncomp * c in the CPU form
+ * (blocklength 1). to_cpu != 0 converts GPU form -> CPU form, else back.
+ * src and dst are distinct device buffers of nnodes * ncomp elements of
+ * elem_bytes (1, 2, 4 or 8) bytes; runs on the container's stream. Used for
+ * Array(particles) / TA(backend)(Float64, data) and checkpoints.
+ */
+int jp_cellarray_permute(jp_particles* p, const void* src, void* dst, int64_t nnodes, int32_t ncomp,
+                         int32_t elem_bytes, int32_t to_cpu);
 int jp_particle2centroid(jp_particles* p, double* F, const double* Fp, const double* const coords[3]);
 
 /*

@@ -63,3 +63,12 @@ from .split import (  # noqa: F401,E402
     move_particles_f32_,
     particle2grid_f32_,
 )
+from .conversion import (  # noqa: F401,E402
+    Array,
+    HostCellArray,
+    HostParticles,
+    HostPhaseRatios,
+    checkpoint_name,
+    checkpointing_particles,
+    load_checkpoint,
+)

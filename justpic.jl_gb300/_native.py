@@ -104,6 +104,9 @@ SIGNATURES = [
      [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("jp_phase_ratios_midpoints", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, P3, P3]),
     ("jp_particle2centroid", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3]),
+    ("jp_cellarray_permute", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+      ctypes.c_int32]),
     # adjoint (2D, FP64)
     ("jp_particle2grid_with_weights", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]),

@@ -687,6 +687,22 @@ int jp_phase_ratios_midpoints(jp_particles* P, int32_t nphases, const double* ph
     return finish(P, jp::launch_phase_midpoints(P, nphases, phases, coords, mids), "update_phase_ratios!");
 }
 
+int jp_cellarray_permute(jp_particles* P, const void* src, void* dst, int64_t nnodes, int32_t ncomp,
+                         int32_t elem_bytes, int32_t to_cpu)
+{
+    if (!P || !src || !dst) return fail(JP_ERR_INVALID_ARGUMENT, "jp_cellarray_permute: null pointer");
+    if (nnodes < 0 || ncomp < 0) return fail(JP_ERR_INVALID_ARGUMENT, "jp_cellarray_permute: negative size");
+    if (elem_bytes != 1 && elem_bytes != 2 && elem_bytes != 4 && elem_bytes != 8)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_cellarray_permute: elem_bytes must be 1, 2, 4 or 8");
+    const uintptr_t a = (uintptr_t)src, b = (uintptr_t)dst;
+    const uintptr_t n = (uintptr_t)nnodes * (uintptr_t)ncomp * (uintptr_t)elem_bytes;
+    if (a % elem_bytes || b % elem_bytes)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_cellarray_permute: misaligned buffer");
+    if (n && a < b + n && b < a + n) return fail(JP_ERR_INVALID_ARGUMENT, "jp_cellarray_permute: buffers overlap");
+    return finish(P, jp::launch_cell_permute(P, src, dst, nnodes, ncomp, elem_bytes, to_cpu != 0),
+                  "jp_cellarray_permute");
+}
+
 int jp_grid2particle_flip(jp_particles* P, double* Fp, const double* F, const double* F0, double alpha,
                           const double* const coords[3], const uint8_t* index)
 {

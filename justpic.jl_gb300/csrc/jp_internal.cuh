@@ -337,6 +337,9 @@ cudaError_t launch_phase_ratios(jp_particles* P, int nph, const double* phases, 
                                 double* center, double* vertex, double* const faces[3]);
 cudaError_t launch_phase_midpoints(jp_particles* P, int nph, const double* phases, const double* const coords[3],
                                    double* const mids[3]);
+// CellArray layout conversion, GPU form (node + nnodes * k) <-> CPU form (k + ncomp * node)
+cudaError_t launch_cell_permute(jp_particles* P, const void* src, void* dst, int64_t nnodes, int ncomp,
+                                int elem_bytes, bool to_cpu);
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
                        const uint8_t* index, double* W = nullptr);
 

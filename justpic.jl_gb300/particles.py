@@ -131,11 +131,20 @@ def cell_array(backend, x, ncells, ni) -> CellArray:
 def TA(backend):
     """Array constructor of a backend (JustPIC ``TA``): host array (Julia shape,
     any order) -> CUDA float64 tensor with the same shape and column-major
-    strides."""
+    strides. ``TA(backend)(T, x[, particles])`` also takes the host containers
+    of ``Array`` (particles, cell arrays, phase ratios; ext/JustPICCUDAExt.jl:51-191)."""
     _check_backend(backend)
 
-    def convert(a):
-        a = np.asarray(a, dtype=np.float64)
+    def convert(*args):
+        if len(args) >= 2:
+            T, x, rest = args[0], args[1], args[2:]
+            from . import conversion
+            if isinstance(x, (conversion.HostParticles, conversion.HostCellArray, conversion.HostPhaseRatios,
+                              tuple, list)):
+                return conversion.to_device(T, x, *rest)
+            a = np.asarray(x, dtype=conversion._np_dtype(T))
+        else:
+            a = np.asarray(args[0], dtype=np.float64)
         rev = tuple(reversed(range(a.ndim)))
         return torch.from_numpy(np.ascontiguousarray(a.transpose(rev))).to("cuda").permute(*rev)
 
@@ -226,6 +235,17 @@ def init_particles(backend, nxcell, max_xcell, min_xcell, *xi_vel, seed: int = D
     velocity component. If every vector is a ``LinRange`` the range rules
     apply (a single spacing per axis), otherwise the vector rules.
     """
+    p = init_particles_empty(backend, nxcell, max_xcell, min_xcell, *xi_vel, seed=seed)
+    from .api import _bind_stream, _finish
+    _bind_stream(p)
+    ptrs = _native.P3(*[c.data_ptr() for c in p.coords], *([None] * (3 - p.ndim)))
+    _finish(p, _native.load().jp_init_particles(p.handle, ptrs, p.index.data_ptr()), "init_particles")
+    return p
+
+
+def init_particles_empty(backend, nxcell, max_xcell, min_xcell, *xi_vel, seed: int = DEFAULT_SEED) -> Particles:
+    """The container of ``init_particles`` with every slot empty (NaN
+    coordinates, index false): the target of a restart."""
     _check_backend(backend)
     if len(xi_vel) == 1 and isinstance(xi_vel[0], tuple) and len(xi_vel[0]) in (2, 3) and \
             isinstance(xi_vel[0][0], tuple):
@@ -277,13 +297,8 @@ def init_particles(backend, nxcell, max_xcell, min_xcell, *xi_vel, seed: int = D
 
     coords = tuple(cell_array(backend, float("nan"), (mx_r.value,), ni) for _ in range(N))
     index = cell_array(backend, False, (mx_r.value,), ni)
-    p = Particles(handle, coords, index, nx_r.value, mx_r.value, mn_r.value, np_.value, di, _di, xci, xvi, host,
-                  uniform, seed)
-    from .api import _bind_stream, _finish
-    _bind_stream(p)
-    ptrs = _native.P3(*[c.data_ptr() for c in coords], *([None] * (3 - N)))
-    _finish(p, lib.jp_init_particles(handle, ptrs, index.data_ptr()), "init_particles")
-    return p
+    return Particles(handle, coords, index, nx_r.value, mx_r.value, mn_r.value, np_.value, di, _di, xci, xvi, host,
+                     uniform, seed)
 
 
 def init_cell_arrays(particles: Particles, n) -> tuple:
