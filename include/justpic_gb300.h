@@ -19,8 +19,11 @@
  * Kernels run on the stream given to jp_set_stream (default: the legacy
  * default stream). The handle is not thread-safe.
  *
- * Limits: ndim 2 or 3; 1 <= max_xcell <= 64; at most JP_MAX_ARGS particle
- * fields per call; grids strictly increasing.
+ * Limits: ndim 2 or 3; 1 <= max_xcell <= JP_MAX_XCELL (cells above 64 slots
+ * run the reference's own per-cell schedule for move_particles! and
+ * inject_particles!, and the split-precision form and the adjoint need
+ * max_xcell <= 64); at most JP_MAX_ARGS particle fields per call; grids
+ * strictly increasing.
  */
 #ifndef JUSTPIC_GB300_H
 #define JUSTPIC_GB300_H
@@ -41,6 +44,7 @@ extern "C" {
 #define JP_ERR_ADJOINT_WINDOW (-6)   /* an adjoint gather met a particle outside its fixed window */
 
 #define JP_MAX_ARGS 16
+#define JP_MAX_XCELL 1024
 
 /* warning bits (jp_get_warnings): conditions the reference does not report */
 #define JP_WARN_FAR_MOVE 0x2     /* a particle moved more than one cell; it was dropped */

@@ -18,6 +18,13 @@ int fail(int code, const std::string& msg)
     return code;
 }
 
+// the split-precision form and the adjoint keep 64-bit slot masks: cells of at most 64 slots
+#define JP_REQUIRE_NARROW(P, what)                                                                        \
+    do {                                                                                                  \
+        if ((P) && (P)->g.max_xcell > 64)                                                                 \
+            return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": needs max_xcell <= 64");         \
+    } while (0)
+
 int cuda_fail(cudaError_t e, const char* where)
 {
     return fail(e == cudaErrorMemoryAllocation ? JP_ERR_OUT_OF_MEMORY : JP_ERR_CUDA,
@@ -73,7 +80,7 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
     const int npq = (nxcell + NQ - 1) / NQ;
     const int nx_r = npq * NQ;
     const int mx = max_xcell > nx_r ? max_xcell : nx_r;
-    if (mx > 64) return fail(JP_ERR_INVALID_ARGUMENT, "max_xcell above 64 is not supported");
+    if (mx > JP_MAX_XCELL) return fail(JP_ERR_INVALID_ARGUMENT, "max_xcell above JP_MAX_XCELL is not supported");
 
     auto* P = new jp_particles();
     jp::DevGrid& g = P->g;
@@ -418,6 +425,7 @@ static int check_f32(const jp_particles* P, const void* const* xi, const void* i
 
 int jp_offsets_from_coords(jp_particles* P, const double* const coords[3], const uint8_t* index, float* const xi[3])
 {
+    JP_REQUIRE_NARROW(P, "jp_offsets_from_coords");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_offsets_from_coords");
     if (rc) return rc;
     if (!check_coords(P, (const void* const*)coords))
@@ -427,6 +435,7 @@ int jp_offsets_from_coords(jp_particles* P, const double* const coords[3], const
 
 int jp_coords_from_offsets(jp_particles* P, const float* const xi[3], const uint8_t* index, double* const coords[3])
 {
+    JP_REQUIRE_NARROW(P, "jp_coords_from_offsets");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_coords_from_offsets");
     if (rc) return rc;
     if (!check_coords(P, (const void* const*)coords))
@@ -437,6 +446,7 @@ int jp_coords_from_offsets(jp_particles* P, const float* const xi[3], const uint
 int jp_advection_f32(jp_particles* P, int32_t method, double alpha, const float* const V[3], double dt,
                      float* const xi[3], const uint8_t* index)
 {
+    JP_REQUIRE_NARROW(P, "jp_advection_f32");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_advection_f32");
     if (rc) return rc;
     if (!check_coords(P, (const void* const*)V)) return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_f32: null velocity");
@@ -449,6 +459,7 @@ int jp_advection_f32(jp_particles* P, int32_t method, double alpha, const float*
 
 int jp_move_particles_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int32_t nargs)
 {
+    JP_REQUIRE_NARROW(P, "jp_move_particles_f32");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_move_particles_f32");
     if (rc) return rc;
     if (nargs < 0 || nargs > JP_MAX_ARGS || (nargs > 0 && !args))
@@ -460,6 +471,7 @@ int jp_move_particles_f32(jp_particles* P, float* const xi[3], uint8_t* index, f
 
 int jp_inject_particles_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int32_t nargs)
 {
+    JP_REQUIRE_NARROW(P, "jp_inject_particles_f32");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_inject_particles_f32");
     if (rc) return rc;
     if (nargs < 0 || nargs > JP_MAX_ARGS || (nargs > 0 && !args))
@@ -473,6 +485,7 @@ int jp_inject_particles_f32(jp_particles* P, float* const xi[3], uint8_t* index,
 
 int jp_grid2particle_f32(jp_particles* P, float* Fp, const float* F, const float* const xi[3], const uint8_t* index)
 {
+    JP_REQUIRE_NARROW(P, "jp_grid2particle_f32");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_grid2particle_f32");
     if (rc) return rc;
     if (!Fp || !F) return fail(JP_ERR_INVALID_ARGUMENT, "jp_grid2particle_f32: null field");
@@ -481,6 +494,7 @@ int jp_grid2particle_f32(jp_particles* P, float* Fp, const float* F, const float
 
 int jp_particle2grid_f32(jp_particles* P, float* F, const float* Fp, const float* const xi[3], const uint8_t* index)
 {
+    JP_REQUIRE_NARROW(P, "jp_particle2grid_f32");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_particle2grid_f32");
     if (rc) return rc;
     if (!Fp || !F) return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_f32: null field");
@@ -503,6 +517,7 @@ static bool slots_fit_int32(const jp_particles* P)
 
 int jp_move_permutation(jp_particles* P, int32_t* dest)
 {
+    JP_REQUIRE_NARROW(P, "jp_move_permutation");
     if (!P || !dest) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: null pointer");
     if (!P->move.rec) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: no move_particles call to replay");
     if (!slots_fit_int32(P)) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: more than 2^31 slots");
@@ -511,6 +526,7 @@ int jp_move_permutation(jp_particles* P, int32_t* dest)
 
 int jp_permute_vjp(jp_particles* P, const int32_t* dest, const double* const* post, double* const* pre, int32_t n)
 {
+    JP_REQUIRE_NARROW(P, "jp_permute_vjp");
     if (!P || !dest || !post || !pre || n < 0 || n > 8)
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_permute_vjp: bad arguments");
     for (int k = 0; k < n; ++k)
@@ -521,6 +537,7 @@ int jp_permute_vjp(jp_particles* P, const int32_t* dest, const double* const* po
 
 int jp_slot_ids(jp_particles* P, const uint8_t* index, double* ids)
 {
+    JP_REQUIRE_NARROW(P, "jp_slot_ids");
     if (!P || !index || !ids) return fail(JP_ERR_INVALID_ARGUMENT, "jp_slot_ids: null pointer");
     return finish(P, jp::launch_slot_ids(P, index, ids), "jp_slot_ids");
 }
@@ -528,6 +545,7 @@ int jp_slot_ids(jp_particles* P, const uint8_t* index, double* ids)
 int jp_inject_vjp(jp_particles* P, const double* ids, const double* const* post, double* const* pre, int32_t n,
                   int32_t copies)
 {
+    JP_REQUIRE_NARROW(P, "jp_inject_vjp");
     if (!P || !ids || !post || !pre || n < 0 || n > 8)
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp: bad arguments");
     if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp: the adjoint is built for 2D");
@@ -541,6 +559,7 @@ int jp_inject_vjp(jp_particles* P, const double* ids, const double* const* post,
 int jp_advection_vjp(jp_particles* P, int32_t method, double alpha, const double* const V[3], double dt,
                      const double* const coords[3], const uint8_t* index, double* const lam[3], double* const gV[3])
 {
+    JP_REQUIRE_NARROW(P, "jp_advection_vjp");
     int rc = check_adj(P, (const void* const*)coords, index, "jp_advection_vjp");
     if (rc) return rc;
     if (!check_coords(P, (const void* const*)V) || !check_coords(P, (const void* const*)lam) ||
@@ -565,6 +584,7 @@ int jp_particle2grid_vjp(jp_particles* P, const double* F, const double* W, cons
                          const double* const coords[3], const uint8_t* index, const double* gF, double* gFp,
                          double* const gX[3])
 {
+    JP_REQUIRE_NARROW(P, "jp_particle2grid_vjp");
     int rc = check_adj(P, (const void* const*)coords, index, "jp_particle2grid_vjp");
     if (rc) return rc;
     if (!F || !W || !Fp || !gF || !gFp || (gX && !check_coords(P, (const void* const*)gX)))
@@ -575,6 +595,7 @@ int jp_particle2grid_vjp(jp_particles* P, const double* F, const double* W, cons
 int jp_grid2particle_vjp(jp_particles* P, const double* F, const double* gFp, const double* const coords[3],
                          const uint8_t* index, double* gF, double* const gX[3])
 {
+    JP_REQUIRE_NARROW(P, "jp_grid2particle_vjp");
     int rc = check_adj(P, (const void* const*)coords, index, "jp_grid2particle_vjp");
     if (rc) return rc;
     if (!gFp || (gX && (!F || !check_coords(P, (const void* const*)gX))))
@@ -602,6 +623,7 @@ static int check_f32_adj(const jp_particles* P, const char* what)
 
 int jp_slot_ids_i32(jp_particles* P, const uint8_t* index, int32_t* ids)
 {
+    JP_REQUIRE_NARROW(P, "jp_slot_ids_i32");
     if (!P || !index || !ids) return fail(JP_ERR_INVALID_ARGUMENT, "jp_slot_ids_i32: null pointer");
     if (!slots_fit_int32(P)) return fail(JP_ERR_INVALID_ARGUMENT, "jp_slot_ids_i32: more than 2^31 slots");
     return finish(P, jp::launch_slot_ids_i32(P, index, ids), "jp_slot_ids_i32");
@@ -610,6 +632,7 @@ int jp_slot_ids_i32(jp_particles* P, const uint8_t* index, int32_t* ids)
 int jp_inject_vjp_i32(jp_particles* P, const int32_t* ids, const double* const* post, double* const* pre,
                       int32_t n, int32_t copies)
 {
+    JP_REQUIRE_NARROW(P, "jp_inject_vjp_i32");
     if (!P || !ids || !post || !pre || n < 0 || n > 8)
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp_i32: bad arguments");
     if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp_i32: the adjoint is built for 2D");
@@ -623,6 +646,7 @@ int jp_inject_vjp_i32(jp_particles* P, const int32_t* ids, const double* const* 
 int jp_advection_vjp_f32(jp_particles* P, int32_t method, double alpha, const float* const V[3], double dt,
                          const float* const xi[3], const uint8_t* index, double* const lam[3], double* const gV[3])
 {
+    JP_REQUIRE_NARROW(P, "jp_advection_vjp_f32");
     if (!P || !index || !check_coords(P, (const void* const*)xi) || !check_coords(P, (const void* const*)V) ||
         !check_coords(P, (const void* const*)lam) || !check_coords(P, (const void* const*)gV))
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_vjp_f32: null pointer");
@@ -639,6 +663,7 @@ int jp_advection_vjp_f32(jp_particles* P, int32_t method, double alpha, const fl
 int jp_particle2grid_f32_with_weights(jp_particles* P, float* F, double* W, const float* Fp, const float* const xi[3],
                                       const uint8_t* index)
 {
+    JP_REQUIRE_NARROW(P, "jp_particle2grid_f32_with_weights");
     if (!P || !F || !W || !Fp || !index || !check_coords(P, (const void* const*)xi))
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_f32_with_weights: null pointer");
     if (!P->g.uniform || !P->staggered_std)
@@ -651,6 +676,7 @@ int jp_particle2grid_vjp_f32(jp_particles* P, const float* F, const double* W, c
                              const float* const xi[3], const uint8_t* index, const double* gF, double* gFp,
                              double* const gxi[3])
 {
+    JP_REQUIRE_NARROW(P, "jp_particle2grid_vjp_f32");
     if (!P || !F || !W || !Fp || !gF || !gFp || !index || !check_coords(P, (const void* const*)xi) ||
         (gxi && !check_coords(P, (const void* const*)gxi)))
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_vjp_f32: null pointer");

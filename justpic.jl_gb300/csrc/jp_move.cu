@@ -697,6 +697,237 @@ __global__ void inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Ar
     raise_err(d_err, errs);
 }
 
+// ------------------------------------------------- cells above 64 slots
+// Containers with max_xcell > 64 do not fit the 64-bit slot masks of the
+// kernels above. They run the reference's own schedule instead: the colour
+// passes of move_particles! with one thread per cell walking its slots in
+// order (move_safe.jl:64-125), and the colour passes of inject_particles! with
+// one warp per cell (injection.jl:68-131, 232-325), the warp sharing the
+// quadrant counts and the nearest-neighbour search. Same results, bit for bit.
+
+// one cell of move_kernel! (src/Particles/move_safe.jl:72-125)
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    move_wide_kernel(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, int pass, int* d_err)
+{
+    int64_t ncol[3] = {1, 1, 1}, off[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ncol[d] = (g.n[d] + 2) / 3;
+    if (DIM == 2) {  // offsets: i outermost, last axis innermost (move_safe.jl:32,39)
+        off[0] = pass / 3;
+        off[1] = pass % 3;
+    } else {
+        off[0] = pass / 9;
+        off[1] = (pass / 3) % 3;
+        off[2] = pass % 3;
+    }
+    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= ncol[0] * ncol[1] * ncol[2]) return;
+    const int64_t J[3] = {w % ncol[0], (w / ncol[0]) % ncol[1], w / (ncol[0] * ncol[1])};
+    int64_t I[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        I[d] = 3 * J[d] + off[d];
+        if (I[d] >= g.n[d]) return;
+    }
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    const int64_t c = cell_linear<DIM>(g, I);
+    double corner[3], dx[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        corner[d] = ldg(g.xv[d] + I[d]);
+        dx[d] = ldg(g.dxv[d] + I[d]);
+    }
+    int errs = 0;
+    int sp = 0;  // starting_point
+    for (int ip = 0; ip < M; ++ip) {
+        const int64_t a = c + nc * ip;
+        if (!index[a]) continue;
+        double p[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) p[d] = X.c[d][a];
+        if (isincell<DIM>(p, corner, dx)) continue;
+        bool inside = true;  // indomain, strict (move_safe.jl:199-206)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) inside &= (g.dom_lo[d] < p[d]) & (p[d] < g.dom_hi[d]);
+        if (!inside) {
+            index[a] = 0;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) X.c[d][a] = CUDART_NAN;
+            for (int k = 0; k < A.n; ++k) A.a[k][a] = CUDART_NAN;
+            continue;
+        }
+        int64_t T[3] = {0, 0, 0};
+        bool far = false;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            T[d] = find_cell(p[d], g.xv[d], g.n[d] + 1, I[d], &errs);
+            far |= T[d] - I[d] > 1 || I[d] - T[d] > 1;
+        }
+        double cached[JP_MAX_ARGS];
+        for (int k = 0; k < A.n; ++k) cached[k] = A.a[k][a];
+        index[a] = 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) X.c[d][a] = CUDART_NAN;
+        for (int k = 0; k < A.n; ++k) A.a[k][a] = CUDART_NAN;
+        if (far) {  // the reference's colour passes race here; the particle is dropped
+            errs |= kWarnFarMove;
+            continue;
+        }
+        const int64_t tc = cell_linear<DIM>(g, T);
+        int fr = -1;
+        for (int i = sp; i < M; ++i)  // find_free_memory (move_safe.jl:192-197)
+            if (!index[tc + nc * i]) {
+                fr = i;
+                break;
+            }
+        if (fr < 0) continue;  // target cell full: dropped
+        sp = fr;
+        const int64_t b = tc + nc * fr;
+        index[b] = 1;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) X.c[d][b] = p[d];
+        for (int k = 0; k < A.n; ++k) A.a[k][b] = cached[k];
+    }
+    raise_err(d_err, errs);
+}
+
+// one cell of _inject_particles! / _inject_particles_phase! per warp
+template <int DIM, bool PHASE>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    inject_wide_kernel(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, PhaseFields PF, int pass,
+                       uint32_t call, int* d_err)
+{
+    int64_t ncol[3] = {1, 1, 1}, off[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ncol[d] = (g.n[d] + 1) / 2;
+    if (DIM == 2) {  // offsets: i outermost, last axis innermost (injection.jl:31,38)
+        off[0] = pass / 2;
+        off[1] = pass % 2;
+    } else {
+        off[0] = pass / 4;
+        off[1] = (pass / 2) % 2;
+        off[2] = pass % 2;
+    }
+    const int lane = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= ncol[0] * ncol[1] * ncol[2]) return;
+    const int64_t J[3] = {w % ncol[0], (w / ncol[0]) % ncol[1], w / (ncol[0] * ncol[1])};
+    int64_t I[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        I[d] = 2 * J[d] + off[d];
+        if (I[d] >= g.n[d]) return;  // the same for the whole warp
+    }
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    constexpr int NB = DIM == 2 ? 9 : 27;
+    constexpr int CENTER = DIM == 2 ? 4 : 13;
+    const int64_t c = cell_linear<DIM>(g, I);
+    double corner[3], dq[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        corner[d] = ldg(g.xv[d] + I[d]);
+        dq[d] = ldg(g.dxv[d] + I[d]) / 2.0;
+    }
+    const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
+    int errs = 0;
+    for (int q = 0; q < (1 << DIM); ++q) {
+        double qc[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) qc[d] = corner[d] + dq[d] * (double)((q >> d) & 1);
+        int cnt = 0;
+        for (int s = lane; s < M; s += 32) {
+            const int64_t a = c + nc * s;
+            if (!index[a]) continue;
+            double p[3];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) p[d] = X.c[d][a];
+            cnt += isincell<DIM>(p, qc, dq) ? 1 : 0;
+        }
+        int count = __reduce_add_sync(0xffffffffu, cnt);
+        if (count >= min_xq) {
+            if (PHASE) continue;  // every quadrant is checked (injection.jl:273)
+            break;                // injection.jl:100
+        }
+        bool done = false;
+        for (int base = 0; base < M && !done; base += 32) {
+            const int s = base + lane;
+            uint32_t freem = __ballot_sync(0xffffffffu, s < M && !index[c + nc * s]);
+            while (freem) {
+                const int i = base + __ffs(freem) - 1;
+                freem &= freem - 1;
+                ++count;
+                double pn[3];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const double r = jp_rand_uniform(g.seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)i,
+                                                     (uint32_t)d);
+                    pn[d] = qc[d] + dq[d] * fma(0.95, r, 0.05);  // new_particle, injection.jl:411-417
+                }
+                const int64_t ai = c + nc * i;
+                if (lane == 0) {
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) X.c[d][ai] = pn[d];
+                    index[ai] = 1;
+                }
+                __syncwarp();
+                // index_min_distance: neighbour cells k, j, i (x fastest), slots in order, strict <
+                double lbest = CUDART_INF;
+                int lo = 0x7fffffff;
+                for (int o = lane; o < NB * M; o += 32) {
+                    const int nb = o / M, sl = o - nb * M;
+                    if (nb == CENTER && sl == i) continue;
+                    const int64_t K[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1,
+                                          DIM == 3 ? I[2] + nb / 9 - 1 : 0};
+                    if (K[0] < 0 || K[1] < 0 || K[0] >= g.n[0] || K[1] >= g.n[1]) continue;
+                    if (DIM == 3 && (K[2] < 0 || K[2] >= g.n[2])) continue;
+                    const int64_t b = cell_linear<DIM>(g, K) + nc * sl;
+                    if (!index[b]) continue;
+                    double e[3];
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) e[d] = X.c[d][b] - pn[d];
+                    const double ss = DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
+                    const double dist = __dsqrt_rn(ss);
+                    if (dist < lbest) {  // lane-strided order: the first of equal distances stays
+                        lbest = dist;
+                        lo = o;
+                    }
+                }
+                const double best = warp_min(lbest);
+                const int win = __reduce_min_sync(0xffffffffu, lbest == best && best < CUDART_INF ? lo : 0x7fffffff);
+                int64_t src = -1;
+                if (win != 0x7fffffff) {
+                    const int nb = win / M, sl = win - nb * M;
+                    const int64_t K[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1,
+                                          DIM == 3 ? I[2] + nb / 9 - 1 : 0};
+                    src = cell_linear<DIM>(g, K) + nc * sl;
+                }
+                if (PHASE) {
+                    if (src >= 0) {
+                        if (lane == 0) PF.phases[ai] = PF.phases[src];
+                    } else {
+                        errs |= kWarnNoNeighbour;
+                    }
+                    for (int k = lane; k < A.n; k += 32)
+                        A.a[k][ai] = phase_field_value<DIM>(g, PF.f[k], PF.centred[k] != 0, pn, I, corner, dq);
+                } else if (src >= 0) {
+                    for (int k = lane; k < A.n; k += 32) A.a[k][ai] = A.a[k][src];
+                } else if (A.n > 0) {
+                    errs |= kWarnNoNeighbour;
+                }
+                __syncwarp();
+                if (count >= min_xq) {
+                    done = true;
+                    break;
+                }
+            }
+        }
+    }
+    raise_err(d_err, errs);
+}
+
 // ------------------------------------------------------------ launchers
 cudaError_t ensure_inject_scratch(jp_particles* P)
 {
@@ -744,9 +975,30 @@ cudaError_t ensure_move_scratch(jp_particles* P, int comps)
     return cudaSuccess;
 }
 
+static cudaError_t launch_move_wide(jp_particles* P, double* const coords[3], uint8_t* index,
+                                    double* const* args, int nargs)
+{
+    const int N = P->g.ndim;
+    Coords X{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};
+    Args A{};
+    A.n = nargs;
+    for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
+    int64_t per = 1;
+    for (int d = 0; d < N; ++d) per *= (P->g.n[d] + 2) / 3;
+    const unsigned nb = grid_blocks(per);
+    for (int pass = 0; pass < (N == 2 ? 9 : 27); ++pass) {
+        if (N == 2)
+            move_wide_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, X, index, A, pass, P->d_err);
+        else
+            move_wide_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, X, index, A, pass, P->d_err);
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
                         int nargs)
 {
+    if (P->g.max_xcell > 64) return launch_move_wide(P, coords, index, args, nargs);
     const int N = P->g.ndim;
     cudaError_t e = ensure_move_scratch(P, N + nargs);
     if (e != cudaSuccess) return e;
@@ -815,6 +1067,25 @@ template <bool PHASE>
 static cudaError_t inject_launch(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
                                  int nargs, const PhaseFields& PF, uint32_t call)
 {
+    if (P->g.max_xcell > 64) {
+        const int N = P->g.ndim;
+        Coords X{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};
+        Args A{};
+        A.n = nargs;
+        for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
+        int64_t per = 1;
+        for (int d = 0; d < N; ++d) per *= (P->g.n[d] + 1) / 2;
+        const unsigned nb = grid_blocks(per * 32, 32 * kWarpsPerBlock);
+        for (int pass = 0; pass < (1 << N); ++pass) {
+            if (N == 2)
+                inject_wide_kernel<2, PHASE><<<nb, 32 * kWarpsPerBlock, 0, P->stream>>>(P->g, X, index, A, PF, pass,
+                                                                                         call, P->d_err);
+            else
+                inject_wide_kernel<3, PHASE><<<nb, 32 * kWarpsPerBlock, 0, P->stream>>>(P->g, X, index, A, PF, pass,
+                                                                                         call, P->d_err);
+        }
+        return cudaGetLastError();
+    }
     const int N = P->g.ndim;
     const int64_t nc = P->g.ncells;
     cudaError_t e = ensure_inject_scratch(P);
@@ -920,6 +1191,7 @@ static cudaError_t move_scratch_address(void** out)
 cudaError_t launch_move_noalloc(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
                                 int nargs)
 {
+    if (P->g.max_xcell > 64) return launch_move_wide(P, coords, index, args, nargs);  // needs no scratch
     const int N = P->g.ndim;
     void* scratch = nullptr;
     cudaError_t e = move_scratch_address(&scratch);

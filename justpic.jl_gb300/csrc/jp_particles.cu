@@ -353,20 +353,25 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 #pragma unroll
         for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
     }
-    uint64_t mine;
-    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
     int errs = 0;
-    for (int k = lane; k < K; k += 32) {
-        int s, l;
-        slot_item(lists[w], M, k, &s, &l);
-        const int64_t a = c0 + l + nc * s;
-        int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
-        double p0[3], p[3];
+    // slots in chunks of 64 (one chunk unless max_xcell > 64)
+    for (int s0 = 0; s0 < M; s0 += 64) {
+        const int Mc = min(64, M - s0);
+        uint64_t mine;
+        const int K = build_slot_list(lists[w], index + nc * s0, c0, nc, Mc, lane, &mine);
+        for (int k = lane; k < K; k += 32) {
+            int s, l;
+            slot_item(lists[w], Mc, k, &s, &l);
+            const int64_t a = c0 + l + nc * (s0 + s);
+            int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
+            double p0[3], p[3];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) p0[d] = X.c[d][a];
-        advect_particle<DIM, METHOD, INTERP>(g, V, P, I, p0, p, &errs);
+            for (int d = 0; d < DIM; ++d) p0[d] = X.c[d][a];
+            advect_particle<DIM, METHOD, INTERP>(g, V, P, I, p0, p, &errs);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) X.c[d][a] = p[d];
+            for (int d = 0; d < DIM; ++d) X.c[d][a] = p[d];
+        }
+        __syncwarp();
     }
     raise_err(d_err, errs);
 }
@@ -410,17 +415,21 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             cv[(1 << DIM) + DIM + d] = ldg(g.ixv[d] + I[d]);
         }
     }
-    uint64_t mine;
-    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
-    for (int k = lane; k < K; k += 32) {
-        int s, l;
-        slot_item(lists[w], M, k, &s, &l);
-        const int64_t a = c0 + l + nc * s;
-        const double* cv = cellv[w][l];
-        double t[3];
+    for (int s0 = 0; s0 < M; s0 += 64) {  // slots in chunks of 64
+        const int Mc = min(64, M - s0);
+        uint64_t mine;
+        const int K = build_slot_list(lists[w], index + nc * s0, c0, nc, Mc, lane, &mine);
+        for (int k = lane; k < K; k += 32) {
+            int s, l;
+            slot_item(lists[w], Mc, k, &s, &l);
+            const int64_t a = c0 + l + nc * (s0 + s);
+            const double* cv = cellv[w][l];
+            double t[3];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) t[d] = (X.c[d][a] - cv[(1 << DIM) + d]) * cv[(1 << DIM) + DIM + d];
-        Fp[a] = lerpN<DIM>(cv, t);
+            for (int d = 0; d < DIM; ++d) t[d] = (X.c[d][a] - cv[(1 << DIM) + d]) * cv[(1 << DIM) + DIM + d];
+            Fp[a] = lerpN<DIM>(cv, t);
+        }
+        __syncwarp();
     }
 }
 
@@ -554,6 +563,57 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// particle2grid! for cells of more than 64 slots: one thread per vertex, the
+// cells of its stencil and their slots in the reference's order (the same sums
+// as p2g_kernel, without the per-cell bit masks).
+template <int DIM>
+__global__ void __launch_bounds__(kThreads)
+    p2g_wide_kernel(DevGrid g, double* __restrict__ F, const double* __restrict__ Fp, CCoords X,
+                    const uint8_t* __restrict__ index, double* __restrict__ Wout)
+{
+    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1, V2 = DIM == 3 ? g.n[2] + 1 : 1;
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V0 * V1 * V2) return;
+    const int64_t nc = g.ncells;
+    const int64_t i = v % V0, j = (v / V0) % V1, k = v / (V0 * V1);
+    double q[3];
+    q[0] = ldg(g.xv[0] + i);
+    q[1] = ldg(g.xv[1] + j);
+    q[2] = DIM == 3 ? ldg(g.xv[2] + k) : 0.0;
+    double w = 0.0, wF = 0.0;
+    for (int ko = (DIM == 3 ? -1 : 0); ko <= 0; ++ko) {
+        const int64_t kc = k + ko;
+        if (DIM == 3 && !(0 <= kc && kc < g.n[2])) continue;
+        for (int jo = -1; jo <= 0; ++jo) {
+            const int64_t jc = j + jo;
+            if (!(0 <= jc && jc < g.n[1])) continue;
+            for (int io = -1; io <= 0; ++io) {
+                const int64_t ic = i + io;
+                if (!(0 <= ic && ic < g.n[0])) continue;
+                const int64_t c = ic + g.n[0] * (jc + g.n[1] * (DIM == 3 ? kc : 0));
+                for (int s = 0; s < g.max_xcell; ++s) {
+                    const int64_t a = c + nc * s;
+                    if (!index[a]) continue;
+                    const double dx = q[0] - X.c[0][a], dy = q[1] - X.c[1][a];
+                    double ss;
+                    if (DIM == 2) {
+                        ss = dx * dx + dy * dy;
+                    } else {
+                        const double dz = q[2] - X.c[2][a];
+                        ss = (dx * dx + dy * dy) + dz * dz;
+                    }
+                    const double dist = __dsqrt_rn(ss);
+                    const double wi = __drcp_rn(dist * dist);
+                    w += wi;
+                    wF = fma(wi, Fp[a], wF);
+                }
+            }
+        }
+    }
+    F[v] = DIM == 2 ? wF / w : wF * __drcp_rn(w);
+    if (Wout) Wout[v] = w;
+}
+
 // ------------------------------------------------------------ launchers
 cudaError_t launch_init(jp_particles* P, double* const coords[3], uint8_t* index)
 {
@@ -631,6 +691,14 @@ cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const doubl
     const bool d3 = P->g.ndim == 3;
     CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
     const int64_t V0 = P->g.n[0] + 1, V1 = P->g.n[1] + 1;
+    if (P->g.max_xcell > 64) {
+        const unsigned nbw = grid_blocks(V0 * V1 * (d3 ? P->g.n[2] + 1 : 1));
+        if (!d3)
+            p2g_wide_kernel<2><<<nbw, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, W);
+        else
+            p2g_wide_kernel<3><<<nbw, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, W);
+        return cudaGetLastError();
+    }
     const int64_t cols = d3 ? V0 * V1 : V0;
     const int64_t rows = P->g.n[d3 ? 2 : 1] + 1;
     // rows per thread: long enough to amortise the prologue row, short enough

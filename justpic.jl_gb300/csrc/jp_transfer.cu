@@ -45,20 +45,24 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 #pragma unroll
         for (int d = 0; d < DIM; ++d) cv[2 * NV + d] = ldg(g.xv[d] + I[d]);
     }
-    uint64_t mine;
-    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
     const double beta = 1.0 - alpha;
-    for (int k = lane; k < K; k += 32) {
-        int s, l;
-        slot_item(lists[w], M, k, &s, &l);
-        const int64_t a = c0 + l + nc * s;
-        const double* cv = cellv[w][l];
-        double t[3];
+    for (int s0 = 0; s0 < M; s0 += 64) {  // slots in chunks of 64
+        const int Mc = min(64, M - s0);
+        uint64_t mine;
+        const int K = build_slot_list(lists[w], index + nc * s0, c0, nc, Mc, lane, &mine);
+        for (int k = lane; k < K; k += 32) {
+            int s, l;
+            slot_item(lists[w], Mc, k, &s, &l);
+            const int64_t a = c0 + l + nc * (s0 + s);
+            const double* cv = cellv[w][l];
+            double t[3];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) t[d] = (X.c[d][a] - cv[2 * NV + d]) * g.idmin[d];
-        const double fpic = lerpN<DIM>(cv, t), f0pic = lerpN<DIM>(cv + NV, t);
-        const double flip = Fp[a] + (fpic - f0pic);
-        Fp[a] = fma(fpic, alpha, flip * beta);
+            for (int d = 0; d < DIM; ++d) t[d] = (X.c[d][a] - cv[2 * NV + d]) * g.idmin[d];
+            const double fpic = lerpN<DIM>(cv, t), f0pic = lerpN<DIM>(cv + NV, t);
+            const double flip = Fp[a] + (fpic - f0pic);
+            Fp[a] = fma(fpic, alpha, flip * beta);
+        }
+        __syncwarp();
     }
 }
 
@@ -67,8 +71,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 // centroid kernels take every slot whose coordinates are not NaN, whatever
 // the index says.
 template <int DIM>
-__device__ __forceinline__ int build_coord_list(SlotList& Lst, const CCoords& X, int64_t c0, int64_t nc, int M,
-                                                int lane)
+__device__ __forceinline__ int build_coord_list(SlotList& Lst, const CCoords& X, int64_t c0, int64_t nc, int s0,
+                                                int M, int lane)
 {
     const bool valid = c0 + lane < nc;
     int K = 0;
@@ -77,7 +81,7 @@ __device__ __forceinline__ int build_coord_list(SlotList& Lst, const CCoords& X,
         bool live = valid;
         if (valid) {
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) live = live & !is_nan_bits(X.c[d][c0 + lane + nc * s]);
+            for (int d = 0; d < DIM; ++d) live = live & !is_nan_bits(X.c[d][c0 + lane + nc * (s0 + s)]);
         }
         const uint32_t m = __ballot_sync(0xffffffffu, live);
         if (lane == 0) {
@@ -112,12 +116,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 #pragma unroll
         for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
     }
-    const int K = build_coord_list<DIM>(lists[w], X, c0, nc, M, lane);
     const int64_t C0 = g.n[0], C1 = g.n[1], sz = C0 * C1;
+    for (int s0 = 0; s0 < M; s0 += 64) {  // slots in chunks of 64
+    const int Mc = min(64, M - s0);
+    const int K = build_coord_list<DIM>(lists[w], X, c0, nc, s0, Mc, lane);
     for (int k = lane; k < K; k += 32) {
         int s, l;
-        slot_item(lists[w], M, k, &s, &l);
-        const int64_t a = c0 + l + nc * s;
+        slot_item(lists[w], Mc, k, &s, &l);
+        const int64_t a = c0 + l + nc * (s0 + s);
         int64_t J[3] = {0, 0, 0};
         double t[3];
 #pragma unroll
@@ -143,6 +149,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             v[7] = ldg(F + b + sz + C0 + 1);
         }
         Fp[a] = lerpN<DIM>(v, t);
+    }
+    __syncwarp();
     }
 }
 

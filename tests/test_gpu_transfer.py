@@ -132,10 +132,11 @@ def test_inject_particles_phase_bit_exact(ni, refined):
 
 
 def test_pure_shear_phase_miniapp_bit_exact():
-    """The phase miniapp (test/test_2D.jl:385-481) on 32^2 cells, 60/64/50
-    particles per cell (the miniapp's 80-slot capacity is above this
-    library's 64), 10 steps of RK2 + move + inject_particles_phase! +
-    update_phase_ratios!, against the oracle; the ratios sum to one."""
+    """The phase miniapp (test/test_2D.jl:385-481) on 32^2 cells with 64
+    slots per cell (the bit-mask kernels; the miniapp's own 80 slots are
+    covered by the wide-cell tests), 10 steps of RK2 + move +
+    inject_particles_phase! + update_phase_ratios!, against the oracle; the
+    ratios sum to one."""
     g, V, dt = W.pure_shear((32, 32))
     pair = Pair(g, 60, 64, 50, nfields=1, uniform=True)
     _set_field(pair, 0, W.shear_phases(pair.o.coords, pair.o.index))
@@ -155,10 +156,11 @@ def test_pure_shear_phase_miniapp_bit_exact():
 
 
 def test_pure_shear_phase_miniapp_full_size():
-    """The same miniapp at its own size (128^2 cells, 20 steps) on the GPU
-    alone: every location keeps ratios summing to one."""
+    """The same miniapp at its own size (128^2 cells, 60/80/50 particles per
+    cell, 20 steps) on the GPU alone: every location keeps ratios summing to
+    one."""
     g, V, dt = W.pure_shear((128, 128))
-    p = jp.init_particles(jp.CUDABackend, 60, 64, 50, *g["grid_v"])
+    p = jp.init_particles(jp.CUDABackend, 60, 80, 50, *g["grid_v"])
     (phases,) = jp.init_cell_arrays(p, 1)
     ph = W.shear_phases([c.numpy() for c in p.coords], p.index.numpy())
     phases.data.copy_(torch.from_numpy(np.ascontiguousarray(ph)))
