@@ -240,6 +240,16 @@ int jp_centroid2particle(jp_particles* p, double* Fp, const double* F, const dou
  * elem_bytes (1, 2, 4 or 8) bytes; runs on the container's stream. Used for
  * Array(particles) / TA(backend)(Float64, data) and checkpoints.
  */
+/*
+ * Diagnostic (no reference counterpart): checks the integer-pipe evaluation of
+ * particle2grid!'s weight inv(sqrt(ss)^2) against CUDA's correctly rounded
+ * double sqrt, multiply and reciprocal, bit for bit, on n seeded inputs drawn
+ * from the whole double range (plus the edge families listed in
+ * csrc/jp_particles.cu). Writes the number of mismatches and the bits of the
+ * first mismatching input (0 if none). Synchronous; needs no container.
+ */
+int jp_selftest_weight(uint64_t seed, int64_t n, int64_t* mismatches, uint64_t* first_bad_input);
+
 int jp_cellarray_permute(jp_particles* p, const void* src, void* dst, int64_t nnodes, int32_t ncomp,
                          int32_t elem_bytes, int32_t to_cpu);
 int jp_particle2centroid(jp_particles* p, double* F, const double* Fp, const double* const coords[3]);

@@ -729,6 +729,23 @@ int jp_cellarray_permute(jp_particles* P, const void* src, void* dst, int64_t nn
                   "jp_cellarray_permute");
 }
 
+int jp_selftest_weight(uint64_t seed, int64_t n, int64_t* mismatches, uint64_t* first_bad_input)
+{
+    if (!mismatches || n < 0) return fail(JP_ERR_INVALID_ARGUMENT, "jp_selftest_weight: bad arguments");
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 2 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_fail(e, "jp_selftest_weight");
+    unsigned long long h[2] = {0, 0};
+    e = cudaMemset(d, 0, sizeof(h));
+    if (e == cudaSuccess) e = jp::launch_weight_selftest(seed, n, d, d + 1, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "jp_selftest_weight");
+    *mismatches = (int64_t)h[0];
+    if (first_bad_input) *first_bad_input = h[1];
+    return JP_OK;
+}
+
 int jp_grid2particle_flip(jp_particles* P, double* Fp, const double* F, const double* F0, double alpha,
                           const double* const coords[3], const uint8_t* index)
 {

@@ -340,6 +340,9 @@ cudaError_t launch_phase_midpoints(jp_particles* P, int nph, const double* phase
 // CellArray layout conversion, GPU form (node + nnodes * k) <-> CPU form (k + ncomp * node)
 cudaError_t launch_cell_permute(jp_particles* P, const void* src, void* dst, int64_t nnodes, int ncomp,
                                 int elem_bytes, bool to_cpu);
+// inv_dist2 (particle2grid! weights) against CUDA's chain: mismatch count and first bad input
+cudaError_t launch_weight_selftest(uint64_t seed, int64_t n, unsigned long long* d_bad, unsigned long long* d_first,
+                                   cudaStream_t st);
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
                        const uint8_t* index, double* W = nullptr);
 

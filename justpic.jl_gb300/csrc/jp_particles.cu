@@ -10,6 +10,7 @@
 #include <cmath>
 
 #include "jp_internal.cuh"
+#include "jp_weight.cuh"
 
 namespace jp {
 
@@ -466,8 +467,7 @@ __device__ __forceinline__ void p2g_cell(int64_t c, uint64_t mask, int64_t nc, c
                 const double dz = q_cur[2] - p[2];
                 ss = (dx * dx + dy * dy) + dz * dz;
             }
-            const double dist = __dsqrt_rn(ss);
-            const double wi = __drcp_rn(dist * dist);  // inv(distance^2), particle_to_grid.jl:203-205
+            const double wi = inv_dist2(ss);  // inv(distance^2), particle_to_grid.jl:203-205
             w_c += wi;
             wF_c = fma(wi, f, wF_c);
         }
@@ -480,8 +480,7 @@ __device__ __forceinline__ void p2g_cell(int64_t c, uint64_t mask, int64_t nc, c
                 const double dz = q_nxt[2] - p[2];
                 ss = (dx * dx + dy * dy) + dz * dz;
             }
-            const double dist = __dsqrt_rn(ss);
-            const double wi = __drcp_rn(dist * dist);
+            const double wi = inv_dist2(ss);
             w_n += wi;
             wF_n = fma(wi, f, wF_n);
         }
@@ -602,8 +601,7 @@ __global__ void __launch_bounds__(kThreads)
                         const double dz = q[2] - X.c[2][a];
                         ss = (dx * dx + dy * dy) + dz * dz;
                     }
-                    const double dist = __dsqrt_rn(ss);
-                    const double wi = __drcp_rn(dist * dist);
+                    const double wi = inv_dist2(ss);
                     w += wi;
                     wF = fma(wi, Fp[a], wF);
                 }
@@ -612,6 +610,75 @@ __global__ void __launch_bounds__(kThreads)
     }
     F[v] = DIM == 2 ? wF / w : wF * __drcp_rn(w);
     if (Wout) Wout[v] = w;
+}
+
+// ------------------------------------------------ weight self-test
+// inv_dist2 against CUDA's sqrt / multiply / reciprocal chain, bit for bit, on
+// seeded inputs: the whole normal range, the edges where d^2 or its inverse
+// leave it, squares of short doubles and their neighbours, sums of squares of
+// cell-sized distances (the inputs particle2grid! sees), and special values.
+__device__ __forceinline__ uint64_t mix64(uint64_t x)  // SplitMix64 finaliser
+{
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+__global__ void weight_selftest_kernel(uint64_t seed, int64_t n, unsigned long long* bad,
+                                       unsigned long long* first)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t h = mix64(seed ^ mix64((uint64_t)i)), h2 = mix64(h);
+        const uint64_t frac = h & ((1ull << 52) - 1);
+        double ss;
+        switch ((int)(h2 % 6)) {
+            case 0:  // any positive normal
+                ss = __longlong_as_double((long long)((((h2 >> 8) % 2046 + 1) << 52) | frac));
+                break;
+            case 1: {  // exponents where d^2 or 1/d^2 approach the ends of the normal range
+                const uint64_t e = (h2 >> 8) & 1 ? 1 + (h2 >> 9) % 560 : 1486 + (h2 >> 9) % 561;
+                ss = __longlong_as_double((long long)((e << 52) | frac));
+                break;
+            }
+            case 2: {  // squares of short doubles and their neighbours (exact and near-exact roots)
+                const double k = (double)((h >> 30) | 1) * __longlong_as_double((long long)(((h2 >> 8) % 1200 + 420) << 52));
+                const long long b = __double_as_longlong(__dmul_rn(k, k)) + (long long)((h2 >> 20) % 5) - 2;
+                ss = __longlong_as_double(b);
+                break;
+            }
+            case 3: {  // cell-sized distances
+                const double x = (double)(h >> 11) * 0x1p-53 * 1e-3, y = (double)(h2 >> 11) * 0x1p-53 * 1e-3;
+                ss = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+                break;
+            }
+            case 4: {  // significands near 1 and 2 (reciprocal and rounding boundaries)
+                const uint64_t f2 = (h2 >> 8) & 1 ? (h & 0xFFFF) : ((1ull << 52) - 1 - (h & 0xFFFF));
+                ss = __longlong_as_double((long long)((((h2 >> 9) % 2046 + 1) << 52) | f2));
+                break;
+            }
+            default: {  // zeros, subnormals, infinities, NaN, negatives, powers of two
+                const int k = (int)((h2 >> 8) % 7);
+                const double sp[7] = {0.0, -0.0, CUDART_INF, CUDART_NAN, -1.5, 0.0, 0.0};
+                ss = k < 5 ? sp[k]
+                           : (k == 5 ? __longlong_as_double((long long)frac)
+                                     : __longlong_as_double((long long)(((h2 >> 9) % 2046 + 1) << 52)));
+            }
+        }
+        const double a = inv_dist2(ss), b = weight_intrinsic(ss);
+        const bool same = __double_as_longlong(a) == __double_as_longlong(b) || (isnan(a) && isnan(b));
+        if (!same) {
+            atomicAdd(bad, 1ull);
+            atomicCAS(first, 0ull, (unsigned long long)__double_as_longlong(ss));
+        }
+    }
+}
+
+cudaError_t launch_weight_selftest(uint64_t seed, int64_t n, unsigned long long* d_bad, unsigned long long* d_first,
+                                   cudaStream_t st)
+{
+    weight_selftest_kernel<<<152 * 8, 256, 0, st>>>(seed, n, d_bad, d_first);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------ launchers

@@ -21,7 +21,7 @@ LIB = os.path.join(BUILD, "libjustpic_gb300.so")
 
 SOURCES = ["jp_capi.cu", "jp_particles.cu", "jp_move.cu", "jp_f32.cu", "jp_adjoint.cu", "jp_transfer.cu",
            "jp_layout.cu"]
-HEADERS = ["jp_internal.cuh", "jp_move_core.cuh", "jp_f32_core.cuh"]
+HEADERS = ["jp_internal.cuh", "jp_move_core.cuh", "jp_f32_core.cuh", "jp_weight.cuh"]
 PUBLIC_HEADERS = ["justpic_gb300.h", "justpic_gb300_rng.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
