@@ -28,6 +28,7 @@
 #include "jp_f32_core.cuh"
 #include "jp_internal.cuh"
 #include "jp_move_core.cuh"
+#include "jp_weight.cuh"
 
 namespace jp {
 
@@ -724,8 +725,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             for (int ka = 0; ka < 2; ++ka) {
                 const int64_t v = (I[0] + ka) + V0 * (I[1] + kb);
                 const double ex = ldg(g.xv[0] + I[0] + ka) - px, ey = ldg(g.xv[1] + I[1] + kb) - py;
-                const double dist = __dsqrt_rn(ex * ex + ey * ey);
-                const double wi = __drcp_rn(dist * dist);
+                const double wi = inv_dist2(ex * ex + ey * ey);  // the forward weight, bit for bit
                 const double r = ldg(gF + v) / ldg(W + v);
                 gf = fma(r, wi, gf);
                 const double q = r * (f - ldg(F + v)) * 2.0 * wi * wi;

@@ -67,6 +67,7 @@ struct InjectScratch {
     int* counts = nullptr;     // flagged cells per colour (8 counters), then the lists
     int* list = nullptr;       // flagged cells, one region per colour
     uint64_t* lm = nullptr;    // occupancy mask per cell (written by the flag pass)
+    float* box = nullptr;      // bounding box of each cell's live particles (flag pass)
 };
 
 // counters, lists and masks of inject_particles! in one allocation

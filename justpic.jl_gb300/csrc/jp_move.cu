@@ -222,6 +222,7 @@ struct InjectLists {
     int* counts;     // [8]
     int* list;       // ncells entries
     uint64_t* lm;    // occupancy mask per cell
+    float* box;      // bounding box of each cell's live particles: lo[0..2], hi[0..2], rounded outwards
     int64_t off[8];  // start of each colour's region in `list`
 };
 
@@ -261,6 +262,23 @@ __global__ void __launch_bounds__(kThreads)
         // the cell's occupancy mask, kept for the passes' neighbourhood staging
         const uint64_t live = live_mask(index, c, nc, g.max_xcell);
         Ls.lm[c] = live;
+        {  // bounding box of the live particles (NaN coordinates never win a search and are left out)
+            double lo[3] = {CUDART_INF, CUDART_INF, CUDART_INF}, hi[3] = {-CUDART_INF, -CUDART_INF, -CUDART_INF};
+            for (uint64_t m = live; m; m &= m - 1) {
+                const int64_t a = c + nc * (__ffsll((long long)m) - 1);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const double x = X.c[d][a];
+                    lo[d] = fmin(lo[d], x);
+                    hi[d] = fmax(hi[d], x);
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                Ls.box[6 * c + d] = __double2float_rd(lo[d]);
+                Ls.box[6 * c + 3 + d] = __double2float_ru(hi[d]);
+            }
+        }
         if (PHASE) {
             // upper halves: corner + dx/2 .. corner + dx/2 + dx/2 (quadrant_corners, injection.jl:442-466)
             long long klo1[3], khi1[3];
@@ -437,6 +455,202 @@ __device__ double phase_field_value(const DevGrid& g, const double* __restrict__
         lo = jl_min(v[k], lo);
     }
     return tmp > hi ? hi : (tmp < lo ? lo : tmp);
+}
+
+// One cell of _inject_particles! / _inject_particles_phase! per warp, with a
+// pruned exact nearest-neighbour search. The cell's own particles sit in shared
+// memory; for each new particle the warp first finds the nearest of them, then
+// examines only the neighbour cells whose bounding box (from the flag pass,
+// rounded outwards, widened by the new particles of earlier passes) can hold a
+// particle at most that far: a skipped cell's particles are all farther, by a
+// margin far above the rounding of the distances, so the minimum and its first
+// occurrence in the reference's order (cells k, j, i, x fastest; slots in
+// order; index_min_distance, injection.jl:330-393) are those of the full search.
+template <int DIM, bool PHASE>
+__device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* __restrict__ index,
+                                   const InjectLists& Ls, const Args& A, const PhaseFields& PF, uint32_t call,
+                                   int64_t c, double* __restrict__ own, int lane, int* errs)
+{
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    constexpr int NB = DIM == 2 ? 9 : 27;
+    constexpr int CENTER = DIM == 2 ? 4 : 13;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    double corner[3], dq[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        corner[d] = ldg(g.xv[d] + I[d]);
+        dq[d] = ldg(g.dxv[d] + I[d]) / 2.0;
+    }
+    uint64_t ownm = Ls.lm[c];
+    // the cell's own coordinates (own[d * M + s])
+    for (int s = lane; s < M; s += 32) {
+        const bool lv = (ownm >> s) & 1ull;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) own[d * M + s] = lv ? X.c[d][c + nc * s] : CUDART_NAN;
+    }
+    // lane nb < NB holds neighbour cell nb: its index, occupancy and box
+    int64_t nbc = -1;
+    uint64_t nbm = 0;
+    float blo[3] = {0.f, 0.f, 0.f}, bhi[3] = {0.f, 0.f, 0.f};
+    if (lane < NB && lane != CENTER) {
+        const int64_t J[3] = {I[0] + lane % 3 - 1, I[1] + (lane / 3) % 3 - 1, DIM == 3 ? I[2] + lane / 9 - 1 : 0};
+        const bool ok = J[0] >= 0 && J[1] >= 0 && J[0] < g.n[0] && J[1] < g.n[1] &&
+                        (DIM == 2 || (J[2] >= 0 && J[2] < g.n[2]));
+        if (ok) {
+            nbc = cell_linear<DIM>(g, J);
+            nbm = Ls.lm[nbc];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                blo[d] = Ls.box[6 * nbc + d];
+                bhi[d] = Ls.box[6 * nbc + 3 + d];
+            }
+        }
+    }
+    // the own cell's box grows with its new particles (read by later passes)
+    float olo = 0.f, ohi = 0.f;
+    if (lane < DIM) {
+        olo = Ls.box[6 * c + lane];
+        ohi = Ls.box[6 * c + 3 + lane];
+    }
+    __syncwarp();
+    const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
+    for (int q = 0; q < (1 << DIM); ++q) {
+        double qc[3];
+        long long klo[3], khi[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            qc[d] = corner[d] + dq[d] * (double)((q >> d) & 1);
+            klo[d] = okey(qc[d]);
+            khi[d] = okey(qc[d] + dq[d]);  // isincell(p, vertex, di_quadrant)
+        }
+        int cnt = 0;
+        for (int s = lane; s < M; s += 32) {
+            if (!((ownm >> s) & 1ull)) continue;
+            bool in = true;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const double x = own[d * M + s];
+                const long long k = okey(x);
+                in = in & !is_nan_bits(x) & (klo[d] < k) & (k < khi[d]);
+            }
+            cnt += in ? 1 : 0;
+        }
+        int count = __reduce_add_sync(0xffffffffu, cnt);
+        if (count >= min_xq) {
+            if (PHASE) continue;  // inject_particles_phase! checks every quadrant (injection.jl:273)
+            break;                // injection.jl:100
+        }
+        uint64_t freem = ~ownm & (M == 64 ? ~0ull : ((1ull << M) - 1));
+        while (freem) {
+            const int i = __ffsll((long long)freem) - 1;
+            freem &= freem - 1;
+            ++count;
+            double pn[3];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const double r = jp_rand_uniform(g.seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)i,
+                                                 (uint32_t)d);
+                pn[d] = qc[d] + dq[d] * fma(0.95, r, 0.05);  // new_particle, injection.jl:411-417
+            }
+            const int64_t ai = c + nc * i;
+            if (lane == 0) {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    X.c[d][ai] = pn[d];
+                    own[d * M + i] = pn[d];
+                }
+                index[ai] = 1;
+            }
+            if (lane < DIM) {
+                const double p = lane == 0 ? pn[0] : (lane == 1 ? pn[1] : pn[DIM - 1]);
+                olo = fminf(olo, __double2float_rd(p));
+                ohi = fmaxf(ohi, __double2float_ru(p));
+            }
+            ownm |= 1ull << i;
+            __syncwarp();
+            // (1) the own cell's particles
+            double bd = CUDART_INF;
+            int bo = 0x7fffffff;
+            for (int s = lane; s < M; s += 32) {
+                if (s == i || !((ownm >> s) & 1ull)) continue;
+                double e[3];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) e[d] = own[d * M + s] - pn[d];
+                const double ss = DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
+                const double dist = __dsqrt_rn(ss);
+                if (dist < bd) {  // slots in order within the lane: the first of equal distances stays
+                    bd = dist;
+                    bo = CENTER * M + s;
+                }
+            }
+            const double dmin_own = warp_min(bd);
+            // (2) neighbour cells whose box may hold a particle within dmin_own
+            bool look = false;
+            if (nbm != 0) {
+                double lb2 = 0.0;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const double gap = fmax(0.0, fmax((double)blo[d] - pn[d], pn[d] - (double)bhi[d]));
+                    lb2 += gap * gap;
+                }
+                // skip only when every particle of the box is farther by a relative 2^-40 (in the
+                // squared distance): far above the rounding of the box, the gaps and the distances
+                look = !(lb2 * (1.0 - 0x1p-40) > dmin_own * dmin_own * (1.0 + 0x1p-40));
+            }
+            uint32_t cells = __ballot_sync(0xffffffffu, look);
+            while (cells) {
+                const int nb = __ffs(cells) - 1;
+                cells &= cells - 1;
+                const uint64_t m = __shfl_sync(0xffffffffu, nbm, nb);
+                const int64_t cc = __shfl_sync(0xffffffffu, nbc, nb);
+                for (int s = lane; s < M; s += 32) {
+                    if (!((m >> s) & 1ull)) continue;
+                    const int64_t b = cc + nc * s;
+                    double e[3];
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) e[d] = X.c[d][b] - pn[d];
+                    const double ss =
+                        DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
+                    const double dist = __dsqrt_rn(ss);
+                    const int o = nb * M + s;
+                    if (dist < bd || (dist == bd && o < bo)) {
+                        bd = dist;
+                        bo = o;
+                    }
+                }
+            }
+            const double best = warp_min(bd);
+            const int win = __reduce_min_sync(0xffffffffu, (bd == best && best < CUDART_INF) ? bo : 0x7fffffff);
+            int64_t src = -1;
+            if (win != 0x7fffffff) {
+                const int nb = win / M, s = win - nb * M;
+                const int64_t J[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1, DIM == 3 ? I[2] + nb / 9 - 1 : 0};
+                src = cell_linear<DIM>(g, J) + nc * s;
+            }
+            if (PHASE) {
+                if (src >= 0) {
+                    if (lane == 0) PF.phases[ai] = PF.phases[src];
+                } else {
+                    *errs |= kWarnNoNeighbour;
+                }
+                for (int k = lane; k < A.n; k += 32)
+                    A.a[k][ai] = phase_field_value<DIM>(g, PF.f[k], PF.centred[k] != 0, pn, I, corner, dq);
+            } else if (src >= 0) {
+                for (int k = lane; k < A.n; k += 32) A.a[k][ai] = A.a[k][src];
+            } else if (A.n > 0) {
+                *errs |= kWarnNoNeighbour;
+            }
+            __syncwarp();
+            if (count >= min_xq) break;
+        }
+    }
+    if (lane == 0) Ls.lm[c] = ownm;
+    if (lane < DIM) {
+        Ls.box[6 * c + lane] = olo;
+        Ls.box[6 * c + 3 + lane] = ohi;
+    }
 }
 
 template <int DIM, bool PHASE>
@@ -675,23 +889,14 @@ __global__ void inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Ar
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int M = g.max_xcell;
-    const int ncand = (DIM == 2 ? 9 : 27) * M;
-    unsigned char* base = smem_inject + (size_t)wib * hood_bytes<DIM>(M);
-    Hood<DIM> H;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) H.own[d] = (double*)base + (size_t)d * M;
-    float* fb = (float*)(base + (size_t)DIM * M * sizeof(double));
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) H.r[d] = fb + (size_t)d * ncand;
-    H.ss32 = fb + (size_t)DIM * ncand;
-    H.live = (uint8_t*)(fb + (size_t)(DIM + 1) * ncand);
+    double* own = (double*)smem_inject + (size_t)wib * DIM * M;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int count = Ls.counts[col];
     int errs = 0;
     for (int k = gw; k < count; k += nwarps) {
         const int64_t c = Ls.list[Ls.off[col] + k];
-        inject_cell_warp<DIM, PHASE>(g, X, index, Ls.lm, A, PF, call, c, H, lane, &errs);
+        inject_cell_pruned<DIM, PHASE>(g, X, index, Ls, A, PF, call, c, own, lane, &errs);
         __syncwarp();
     }
     raise_err(d_err, errs);
@@ -934,12 +1139,14 @@ cudaError_t ensure_inject_scratch(jp_particles* P)
     if (P->inject.counts) return cudaSuccess;
     const int64_t nc = P->g.ncells;
     const size_t list_bytes = ((8 + (size_t)nc) * sizeof(int) + 7) & ~(size_t)7;
+    const size_t lm_bytes = (size_t)nc * sizeof(uint64_t);
     char* base = nullptr;
-    cudaError_t e = cudaMalloc(&base, list_bytes + (size_t)nc * sizeof(uint64_t));
+    cudaError_t e = cudaMalloc(&base, list_bytes + lm_bytes + (size_t)nc * 6 * sizeof(float));
     if (e != cudaSuccess) return e;
     P->inject.counts = (int*)base;
     P->inject.list = P->inject.counts + 8;
     P->inject.lm = (uint64_t*)(base + list_bytes);
+    P->inject.box = (float*)(base + list_bytes + lm_bytes);
     return cudaSuccess;
 }
 
@@ -1094,6 +1301,7 @@ static cudaError_t inject_launch(jp_particles* P, double* const coords[3], uint8
     Ls.counts = P->inject.counts;
     Ls.list = P->inject.list;
     Ls.lm = P->inject.lm;
+    Ls.box = P->inject.box;
     // colour regions: cells whose index parity along every axis is fixed
     int64_t cnt[3][2];
     for (int d = 0; d < 3; ++d)
@@ -1113,10 +1321,10 @@ static cudaError_t inject_launch(jp_particles* P, double* const coords[3], uint8
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
     const unsigned nb = grid_blocks(nc);
     const int M = P->g.max_xcell;
-    const int wpb = N == 2 ? 4 : 2;  // warps per block of the pass kernels
-    const size_t smem = N == 2 ? wpb * hood_bytes<2>(M) : wpb * hood_bytes<3>(M);
+    const int wpb = 8;  // warps per block of the pass kernels
+    const size_t smem = (size_t)wpb * N * M * sizeof(double);
     // enough warps to keep every SM busy; each strides over its colour's list
-    const unsigned nbp = (unsigned)(152 * (N == 2 ? 8 : 16));
+    const unsigned nbp = (unsigned)(152 * 8);
     if (N == 2) {
         if (smem > 48 * 1024) {
             e = cudaFuncSetAttribute(inject_pass<2, PHASE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
