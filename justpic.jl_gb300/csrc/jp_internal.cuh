@@ -228,6 +228,12 @@ __device__ __forceinline__ long long okey(double x)
     return b ^ ((b >> 63) & 0x7fffffffffffffffll);
 }
 
+// the double of an integer key (inverse of okey; -0.0 comes back as +0.0)
+__device__ __forceinline__ double okey_value(long long k)
+{
+    return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffll));
+}
+
 __device__ __forceinline__ bool is_nan_bits(double x)
 {
     return (__double_as_longlong(x) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;

@@ -27,6 +27,9 @@
 // change any result.
 #include <math_constants.h>
 
+#include <climits>
+#include <limits>
+
 #include "jp_internal.cuh"
 #include "jp_move_core.cuh"
 
@@ -262,21 +265,25 @@ __global__ void __launch_bounds__(kThreads)
         // the cell's occupancy mask, kept for the passes' neighbourhood staging
         const uint64_t live = live_mask(index, c, nc, g.max_xcell);
         Ls.lm[c] = live;
-        {  // bounding box of the live particles (NaN coordinates never win a search and are left out)
-            double lo[3] = {CUDART_INF, CUDART_INF, CUDART_INF}, hi[3] = {-CUDART_INF, -CUDART_INF, -CUDART_INF};
+        {  // bounding box of the live particles, on order-preserving integer keys (NaN
+           // coordinates never win a search and are left out)
+            long long lo[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, hi[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
             for (uint64_t m = live; m; m &= m - 1) {
                 const int64_t a = c + nc * (__ffsll((long long)m) - 1);
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) {
                     const double x = X.c[d][a];
-                    lo[d] = fmin(lo[d], x);
-                    hi[d] = fmax(hi[d], x);
+                    if (is_nan_bits(x)) continue;
+                    const long long k = okey(x);
+                    lo[d] = min(lo[d], k);
+                    hi[d] = max(hi[d], k);
                 }
             }
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
-                Ls.box[6 * c + d] = __double2float_rd(lo[d]);
-                Ls.box[6 * c + 3 + d] = __double2float_ru(hi[d]);
+                const bool any = lo[d] <= hi[d];
+                Ls.box[6 * c + d] = any ? __double2float_rd(okey_value(lo[d])) : CUDART_INF_F;
+                Ls.box[6 * c + 3 + d] = any ? __double2float_ru(okey_value(hi[d])) : -CUDART_INF_F;
             }
         }
         if (PHASE) {
@@ -457,6 +464,48 @@ __device__ double phase_field_value(const DevGrid& g, const double* __restrict__
     return tmp > hi ? hi : (tmp < lo ? lo : tmp);
 }
 
+// per-lane minimum of the squared distance: (ss1, the smallest order o with it)
+// and the smallest squared distance above ss1
+struct NearestTrack {
+    double ss1, ss2;
+    int o1;
+    __device__ __forceinline__ NearestTrack()
+        : ss1(std::numeric_limits<double>::infinity()), ss2(std::numeric_limits<double>::infinity()), o1(0x7fffffff)
+    {
+    }
+    __device__ __forceinline__ void add(double ss, int o)
+    {
+        if (ss < ss1) {  // NaN never enters
+            ss2 = ss1;
+            ss1 = ss;
+            o1 = o;
+        } else if (ss == ss1) {
+            o1 = min(o1, o);
+        } else if (ss < ss2) {
+            ss2 = ss;
+        }
+    }
+};
+
+// squared distance of the reference's distance() (sum of squares, x first)
+template <int DIM>
+__device__ __forceinline__ double own_ss(const double* own, int M, int s, const double* pn)
+{
+    double e[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) e[d] = own[d * M + s] - pn[d];
+    return DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
+}
+
+template <int DIM>
+__device__ __forceinline__ double glob_ss(const Coords& X, int64_t b, const double* pn)
+{
+    double e[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) e[d] = X.c[d][b] - pn[d];
+    return DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
+}
+
 // One cell of _inject_particles! / _inject_particles_phase! per warp, with a
 // pruned exact nearest-neighbour search. The cell's own particles sit in shared
 // memory; for each new particle the warp first finds the nearest of them, then
@@ -570,23 +619,21 @@ __device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* _
             }
             ownm |= 1ull << i;
             __syncwarp();
+            // The reference takes the first minimum of the rounded distance sqrt(ss) in its
+            // order. The search compares squared distances instead and keeps, per lane, the
+            // smallest (ss1, first o) and the smallest larger ss2: when no other candidate's
+            // squared distance lies within a relative 2^-50 of the minimum, no other
+            // candidate can round to the same distance (a larger root is ~2 ulps above) and
+            // the minimum's first occurrence is the answer; otherwise (in practice never)
+            // the rounded distances are compared again.
+            NearestTrack nt;
             // (1) the own cell's particles
-            double bd = CUDART_INF;
-            int bo = 0x7fffffff;
-            for (int s = lane; s < M; s += 32) {
-                if (s == i || !((ownm >> s) & 1ull)) continue;
-                double e[3];
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) e[d] = own[d * M + s] - pn[d];
-                const double ss = DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
-                const double dist = __dsqrt_rn(ss);
-                if (dist < bd) {  // slots in order within the lane: the first of equal distances stays
-                    bd = dist;
-                    bo = CENTER * M + s;
-                }
-            }
-            const double dmin_own = warp_min(bd);
-            // (2) neighbour cells whose box may hold a particle within dmin_own
+            for (int s = lane; s < M; s += 32)
+                if (s != i && ((ownm >> s) & 1ull)) nt.add(own_ss<DIM>(own, M, s, pn), CENTER * M + s);
+            const double ss_own = warp_min(nt.ss1);
+            // (2) neighbour cells whose box may hold a particle that close: skipped only when
+            // every particle of the box is farther by a relative 2^-40 in the squared distance,
+            // far above the rounding of the box, the gaps and the distances
             bool look = false;
             if (nbm != 0) {
                 double lb2 = 0.0;
@@ -595,34 +642,38 @@ __device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* _
                     const double gap = fmax(0.0, fmax((double)blo[d] - pn[d], pn[d] - (double)bhi[d]));
                     lb2 += gap * gap;
                 }
-                // skip only when every particle of the box is farther by a relative 2^-40 (in the
-                // squared distance): far above the rounding of the box, the gaps and the distances
-                look = !(lb2 * (1.0 - 0x1p-40) > dmin_own * dmin_own * (1.0 + 0x1p-40));
+                look = !(lb2 * (1.0 - 0x1p-40) > ss_own * (1.0 + 0x1p-40));
             }
-            uint32_t cells = __ballot_sync(0xffffffffu, look);
-            while (cells) {
-                const int nb = __ffs(cells) - 1;
-                cells &= cells - 1;
+            const uint32_t cells = __ballot_sync(0xffffffffu, look);
+            for (uint32_t cl = cells; cl;) {
+                const int nb = __ffs(cl) - 1;
+                cl &= cl - 1;
                 const uint64_t m = __shfl_sync(0xffffffffu, nbm, nb);
                 const int64_t cc = __shfl_sync(0xffffffffu, nbc, nb);
-                for (int s = lane; s < M; s += 32) {
-                    if (!((m >> s) & 1ull)) continue;
-                    const int64_t b = cc + nc * s;
-                    double e[3];
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d) e[d] = X.c[d][b] - pn[d];
-                    const double ss =
-                        DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
-                    const double dist = __dsqrt_rn(ss);
-                    const int o = nb * M + s;
-                    if (dist < bd || (dist == bd && o < bo)) {
-                        bd = dist;
-                        bo = o;
-                    }
-                }
+                for (int s = lane; s < M; s += 32)
+                    if ((m >> s) & 1ull) nt.add(glob_ss<DIM>(X, cc + nc * s, pn), nb * M + s);
             }
-            const double best = warp_min(bd);
-            const int win = __reduce_min_sync(0xffffffffu, (bd == best && best < CUDART_INF) ? bo : 0x7fffffff);
+            const double ss_min = warp_min(nt.ss1);
+            const double ss_next = warp_min(nt.ss1 > ss_min ? nt.ss1 : nt.ss2);
+            int win = __reduce_min_sync(0xffffffffu, (nt.ss1 == ss_min && ss_min < CUDART_INF) ? nt.o1 : 0x7fffffff);
+            if (ss_min < CUDART_INF && ss_next <= ss_min * (1.0 + 0x1p-50)) {
+                // near tie: first candidate in order whose rounded distance is the minimum
+                const double dmin = __dsqrt_rn(ss_min);
+                int lo = 0x7fffffff;
+                for (int s = lane; s < M; s += 32)
+                    if (s != i && ((ownm >> s) & 1ull) && __dsqrt_rn(own_ss<DIM>(own, M, s, pn)) == dmin)
+                        lo = min(lo, CENTER * M + s);
+                for (uint32_t cl = cells; cl;) {
+                    const int nb = __ffs(cl) - 1;
+                    cl &= cl - 1;
+                    const uint64_t m = __shfl_sync(0xffffffffu, nbm, nb);
+                    const int64_t cc = __shfl_sync(0xffffffffu, nbc, nb);
+                    for (int s = lane; s < M; s += 32)
+                        if (((m >> s) & 1ull) && __dsqrt_rn(glob_ss<DIM>(X, cc + nc * s, pn)) == dmin)
+                            lo = min(lo, nb * M + s);
+                }
+                win = __reduce_min_sync(0xffffffffu, lo);
+            }
             int64_t src = -1;
             if (win != 0x7fffffff) {
                 const int nb = win / M, s = win - nb * M;
@@ -882,7 +933,8 @@ __device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __r
 
 // One colour pass: warps take the colour's listed cells in turn.
 template <int DIM, bool PHASE>
-__global__ void inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, PhaseFields PF, InjectLists Ls,
+__global__ void __launch_bounds__(256, 3)
+    inject_pass(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, PhaseFields PF, InjectLists Ls,
                             int col, uint32_t call, int* d_err)
 {
     extern __shared__ __align__(16) unsigned char smem_inject[];
