@@ -247,90 +247,65 @@ __global__ void __launch_bounds__(kThreads)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    bool flag = false;
-    int col = 0;
-    if (c < g.ncells) {
-        int64_t I[3];
-        cell_coords(g, c, I);
-        col = colour_of<DIM>(I);
-        const int64_t nc = g.ncells;
-        long long klo[3], khi[3];
+    const bool valid = c < g.ncells;
+    const int64_t nc = g.ncells;
+    int64_t I[3] = {0, 0, 0};
+    cell_coords(g, valid ? c : 0, I);
+    const int col = colour_of<DIM>(I);
+    // quadrant bounds: lower half corner .. corner + dx/2, upper half corner + dx/2 .. + dx/2
+    // (quadrant_corners, injection.jl:442-466; isincell strict)
+    long long klo[2][3], khi[2][3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const double lo = ldg(g.xv[d] + I[d]), h = ldg(g.dxv[d] + I[d]) / 2.0;
+        klo[0][d] = okey(lo);
+        khi[0][d] = okey(lo + h);
+        klo[1][d] = okey(lo + h);
+        khi[1][d] = okey((lo + h) + h);
+    }
+    // the cell's occupancy mask, kept for the passes
+    const uint64_t live = valid ? live_mask(index, c, nc, g.max_xcell) : 0ull;
+    if (valid) Ls.lm[c] = live;
+    // one sweep over the slots, the same slot across the warp (coalesced): the bounding box
+    // of the live particles on order-preserving integer keys (NaN coordinates never win a
+    // search and are left out) and the quadrant counts
+    long long blo[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, bhi[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
+    int cq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int smax = __reduce_max_sync(0xffffffffu, live ? 64 - __clzll((long long)live) : 0);
+    for (int s = 0; s < smax; ++s) {
+        if (!((live >> s) & 1ull)) continue;
+        const int64_t a = c + nc * s;
+        unsigned in0 = 0, in1 = 0;
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
-            const double lo = ldg(g.xv[d] + I[d]);
-            klo[d] = okey(lo);
-            khi[d] = okey(lo + ldg(g.dxv[d] + I[d]) / 2.0);  // quadrant corner + dx/2
+            const double x = X.c[d][a];
+            const bool ok = !is_nan_bits(x);
+            const long long k = okey(x);
+            if (ok) {
+                blo[d] = min(blo[d], k);
+                bhi[d] = max(bhi[d], k);
+            }
+            in0 |= (unsigned)(ok & (klo[0][d] < k) & (k < khi[0][d])) << d;
+            in1 |= (unsigned)(ok & (klo[1][d] < k) & (k < khi[1][d])) << d;
+        }
+        constexpr unsigned full = (1u << DIM) - 1u;
+#pragma unroll
+        for (int q = 0; q < (PHASE ? (1 << DIM) : 1); ++q)  // quadrant q: upper half where bit d of q is set
+            cq[q] += (((in1 & (unsigned)q) | (in0 & ~(unsigned)q & full)) == full) ? 1 : 0;
+    }
+    bool flag = false;
+    if (valid) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            const bool any = blo[d] <= bhi[d];
+            Ls.box[6 * c + d] = any ? __double2float_rd(okey_value(blo[d])) : CUDART_INF_F;
+            Ls.box[6 * c + 3 + d] = any ? __double2float_ru(okey_value(bhi[d])) : -CUDART_INF_F;
         }
         const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
-        // the cell's occupancy mask, kept for the passes' neighbourhood staging
-        const uint64_t live = live_mask(index, c, nc, g.max_xcell);
-        Ls.lm[c] = live;
-        {  // bounding box of the live particles, on order-preserving integer keys (NaN
-           // coordinates never win a search and are left out)
-            long long lo[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, hi[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
-            for (uint64_t m = live; m; m &= m - 1) {
-                const int64_t a = c + nc * (__ffsll((long long)m) - 1);
+        // inject_particles! looks at a cell only while its first quadrant is short
+        // (injection.jl:81-100), inject_particles_phase! at any short quadrant (:262-280)
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) {
-                    const double x = X.c[d][a];
-                    if (is_nan_bits(x)) continue;
-                    const long long k = okey(x);
-                    lo[d] = min(lo[d], k);
-                    hi[d] = max(hi[d], k);
-                }
-            }
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const bool any = lo[d] <= hi[d];
-                Ls.box[6 * c + d] = any ? __double2float_rd(okey_value(lo[d])) : CUDART_INF_F;
-                Ls.box[6 * c + 3 + d] = any ? __double2float_ru(okey_value(hi[d])) : -CUDART_INF_F;
-            }
-        }
-        if (PHASE) {
-            // upper halves: corner + dx/2 .. corner + dx/2 + dx/2 (quadrant_corners, injection.jl:442-466)
-            long long klo1[3], khi1[3];
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const double lo = ldg(g.xv[d] + I[d]) + ldg(g.dxv[d] + I[d]) / 2.0;
-                klo1[d] = okey(lo);
-                khi1[d] = okey(lo + ldg(g.dxv[d] + I[d]) / 2.0);
-            }
-            int cq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            for (uint64_t m = live; m; m &= m - 1) {
-                const int64_t a = c + nc * (__ffsll((long long)m) - 1);
-                unsigned in0 = 0, in1 = 0;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) {
-                    const double x = X.c[d][a];
-                    const long long k = okey(x);
-                    const bool ok = !is_nan_bits(x);
-                    in0 |= (unsigned)(ok & (klo[d] < k) & (k < khi[d])) << d;
-                    in1 |= (unsigned)(ok & (klo1[d] < k) & (k < khi1[d])) << d;
-                }
-#pragma unroll
-                for (int q = 0; q < (1 << DIM); ++q) {
-                    // quadrant q takes the upper half along axis d when bit d of q is set
-                    const unsigned need = (unsigned)q, full = (1u << DIM) - 1u;
-                    cq[q] += (((in1 & need) | (in0 & ~need & full)) == full) ? 1 : 0;
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < (1 << DIM); ++q) flag |= cq[q] < min_xq;
-        } else {
-            int count = 0;
-            for (uint64_t m = live; m && count < min_xq; m &= m - 1) {
-            const int64_t a = c + nc * (__ffsll((long long)m) - 1);
-            bool in = true;
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const double x = X.c[d][a];
-                const long long k = okey(x);
-                in = in & !is_nan_bits(x) & (klo[d] < k) & (k < khi[d]);
-            }
-            count += in ? 1 : 0;
-            }
-            flag = count < min_xq;
-        }
+        for (int q = 0; q < (PHASE ? (1 << DIM) : 1); ++q) flag |= cq[q] < min_xq;
     }
     const unsigned active = __ballot_sync(0xffffffffu, flag);
     if (flag) {
