@@ -458,29 +458,27 @@ __device__ __forceinline__ void p2g_cell(int64_t c, uint64_t mask, int64_t nc, c
 #pragma unroll
         for (int d = 0; d < DIM; ++d) p[d] = X.c[d][a];
         const double f = Fp[a];
+        // the two vertices share the column (x in 2D, x and y in 3D): those terms of
+        // distance(xv, p)^2 = ((x - px)^2 + (y - py)^2) [+ (z - pz)^2] are formed once
+        const double dx = q_cur[0] - p[0];
+        double shared, ec, en;
+        if (DIM == 2) {
+            shared = dx * dx;
+            ec = q_cur[1] - p[1];
+            en = q_nxt[1] - p[1];
+        } else {
+            const double dy = q_cur[1] - p[1];
+            shared = dx * dx + dy * dy;
+            ec = q_cur[2] - p[2];
+            en = q_nxt[2] - p[2];
+        }
         if (do_cur) {
-            double ss;
-            const double dx = q_cur[0] - p[0], dy = q_cur[1] - p[1];
-            if (DIM == 2) {
-                ss = dx * dx + dy * dy;
-            } else {
-                const double dz = q_cur[2] - p[2];
-                ss = (dx * dx + dy * dy) + dz * dz;
-            }
-            const double wi = inv_dist2(ss);  // inv(distance^2), particle_to_grid.jl:203-205
+            const double wi = inv_dist2(shared + ec * ec);  // inv(distance^2), particle_to_grid.jl:203-205
             w_c += wi;
             wF_c = fma(wi, f, wF_c);
         }
         if (do_nxt) {
-            double ss;
-            const double dx = q_nxt[0] - p[0], dy = q_nxt[1] - p[1];
-            if (DIM == 2) {
-                ss = dx * dx + dy * dy;
-            } else {
-                const double dz = q_nxt[2] - p[2];
-                ss = (dx * dx + dy * dy) + dz * dz;
-            }
-            const double wi = inv_dist2(ss);
+            const double wi = inv_dist2(shared + en * en);
             w_n += wi;
             wF_n = fma(wi, f, wF_n);
         }
@@ -509,7 +507,7 @@ __global__ void __launch_bounds__(kThreads)
     const int64_t j = DIM == 3 ? col / V0 : 0;
     const bool has_i0 = i >= 1, has_i1 = i < g.n[0];          // cells i-1 and i exist
     const bool has_j0 = DIM == 2 || j >= 1, has_j1 = DIM == 2 || j < g.n[1];
-    double q_cur[3], q_nxt[3];
+    double q_cur[3] = {0.0, 0.0, 0.0}, q_nxt[3] = {0.0, 0.0, 0.0};
     q_cur[0] = q_nxt[0] = ldg(g.xv[0] + i);
     if (DIM == 3) q_cur[1] = q_nxt[1] = ldg(g.xv[1] + j);
 
