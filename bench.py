@@ -87,12 +87,37 @@ def algorithmic_bytes(op, N, nf, m, slots_per_live, grid_bytes_per_live, field_b
 # divided by its particle count. Traffic grows with the particle count, so the
 # bench scales it by the live particles of its own run.
 DRAM_BYTES_PER_PARTICLE_2D_F64 = {
-    "particle2grid!": 623.9e6 / 5.790e6,
-    "advection!": 304.0e6 / 5.790e6,
-    "grid2particle!": 309.1e6 / 5.790e6,
-    "move_particles!": 1535.5e6 / 5.790e6,
-    "inject_particles!": 510.7e6 / 5.790e6,
+    "particle2grid!": 673.6e6 / 5.790e6,
+    "advection!": 306.2e6 / 5.790e6,
+    "grid2particle!": 309.5e6 / 5.790e6,
+    "move_particles!": 1555.2e6 / 5.790e6,
+    "inject_particles!": 333.1e6 / 5.790e6,
 }
+
+
+def fp64_instructions(op, N, method):
+    """FP64 instructions per live particle of the interpolating calls, counted
+    from their kernels (every FP64 add, multiply and FMA; the bisection and
+    range tests run on integer keys, particle2grid!'s weights on the integer
+    pipe): advection samples 2 (Euler 1, RK4 4) velocities of N components,
+    each N normalisations (subtract, multiply) and 2^N - 1 lerps (2 FMA),
+    plus the stage updates; grid2particle! one N-linear sample;
+    particle2grid! 2^(N-1) column visits per particle, each forming the
+    column's shared squared terms once for its two vertices, then per vertex
+    one add and one FMA. None for the integer/memory calls."""
+    sample = N * (2 * N + 2 * ((1 << N) - 1))
+    if op == "advection!":
+        if method == "RungeKutta4":
+            return 4 * sample + N * (3 + 3 + 2) + N * 7
+        if method == "Euler":
+            return sample + 2 * N
+        return 2 * sample + 4 * N
+    if op == "grid2particle!":
+        return 2 * N + 2 * ((1 << N) - 1)
+    if op == "particle2grid!":
+        per_visit = (2 + 2 + 2 + 2) if N == 2 else (2 + 2 + 1 + 2 + 2 + 2)
+        return (1 << (N - 1)) * (per_visit + 2 * 2)
+    return None
 
 
 def launches(op, N):
@@ -355,6 +380,17 @@ def run_ours(args, form=None, minimal=False):
     achieved = bpp[dom] * live / (op_ms[dom] / 1e3) / 1e9
     step_bytes = sum(bpp.values()) * live
     step_gbs = step_bytes / (elapsed / args.steps) / 1e9
+    # the interpolating kernels are bound by GB300's FP64 issue rate (2 lanes per clock
+    # per SM), not by HBM: their FP64 instruction rate against that peak at the sampled clock
+    fp64_roof = None
+    fi = fp64_instructions(dom, N, type(method).__name__) if not f32 else None
+    if fi is not None:
+        mhz = clocks.summary().get("sm_mhz") or 2070.0
+        peak_i = 152 * 2 * mhz * 1e6
+        ach_i = fi * live / (op_ms[dom] / 1e3)
+        fp64_roof = {"kernel": dom, "fp64_instructions_per_particle": fi, "achieved_ginst_s": ach_i / 1e9,
+                     "peak_ginst_s": peak_i / 1e9, "frac": ach_i / peak_i,
+                     "peak_source": "152 SMs x 2 FP64 lanes per clock x sampled SM clock"}
 
     result = {
         "metric": METRIC,
@@ -384,6 +420,7 @@ def run_ours(args, form=None, minimal=False):
         "per_call_ms": op_ms,
         "algorithmic_bytes_per_particle": bpp,
         "step_algorithmic_gbs": step_gbs,
+        "fp64_roofline": fp64_roof,
         "roofline": {
             "bound": "hbm",
             "kernel": dom,
