@@ -241,6 +241,22 @@ int jp_centroid2particle(jp_particles* p, double* Fp, const double* F, const dou
  * Array(particles) / TA(backend)(Float64, data) and checkpoints.
  */
 /*
+ * Recorded adjoint steps (2D, FP64, max_xcell <= 64). jp_advection_record is
+ * jp_advection (same positions, bit for bit) that also writes, into a device
+ * buffer of jp_advection_record_bytes bytes, each live particle's velocity
+ * samples (local coordinates, bilinear gradients, deposit window);
+ * jp_advection_vjp_recorded is jp_advection_vjp for that step from the record
+ * instead of a replay of the stages (index = the occupancy before the step;
+ * gV is added to). A stage point more than one cell from its particle's cell
+ * raises JP_ERR_ADJOINT_WINDOW at recording.
+ */
+int jp_advection_record_bytes(jp_particles* p, int32_t method, uint64_t* bytes);
+int jp_advection_record(jp_particles* p, int32_t method, double alpha, const double* const V[3], double dt,
+                        double* const coords[3], const uint8_t* index, void* rec);
+int jp_advection_vjp_recorded(jp_particles* p, int32_t method, double alpha, double dt, const void* rec,
+                              const uint8_t* index, double* const lam[3], double* const gV[3]);
+
+/*
  * Diagnostic (no reference counterpart): checks the integer-pipe evaluation of
  * particle2grid!'s weight inv(sqrt(ss)^2) against CUDA's correctly rounded
  * double sqrt, multiply and reciprocal, bit for bit, on n seeded inputs drawn

@@ -104,6 +104,11 @@ SIGNATURES = [
      [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, P3, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("jp_phase_ratios_midpoints", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, P3, P3]),
     ("jp_particle2centroid", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P3]),
+    ("jp_advection_record_bytes", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)]),
+    ("jp_advection_record", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, P3, ctypes.c_double, P3, ctypes.c_void_p, ctypes.c_void_p]),
+    ("jp_advection_vjp_recorded", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, P3, P3]),
     ("jp_selftest_weight", ctypes.c_int,
      [ctypes.c_uint64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_uint64)]),
     ("jp_cellarray_permute", ctypes.c_int,

@@ -29,7 +29,7 @@ from dataclasses import dataclass
 import torch
 
 from . import _native
-from ._native import ArgumentError, P3
+from ._native import ArgumentError, P3, check
 from .api import _bind_stream, _check_cellarray, _check_grid, _coords, _finish, _vertex_shape
 from .api import advection_, inject_particles_, move_particles_
 from .integrators import AbstractAdvectionIntegrator
@@ -107,6 +107,34 @@ def advection_vjp_(particles: Particles, method: AbstractAdvectionIntegrator, V,
     _finish(particles, rc, "advection! adjoint")
 
 
+def record_buffer(particles: Particles, method: AbstractAdvectionIntegrator) -> torch.Tensor:
+    """Device buffer for one recorded advection step (jp_advection_record_bytes)."""
+    n = ctypes.c_uint64(0)
+    check(_native.load().jp_advection_record_bytes(particles.handle, method.code, ctypes.byref(n)))
+    return torch.empty(int(n.value), dtype=torch.uint8, device="cuda")
+
+
+def advection_record_(particles: Particles, method: AbstractAdvectionIntegrator, V, dt, rec: torch.Tensor) -> None:
+    """``advection!`` (the same positions, bit for bit) that also records each
+    live particle's velocity samples into ``rec`` for advection_vjp_recorded_."""
+    _require_2d(particles)
+    _bind_stream(particles)
+    rc = _native.load().jp_advection_record(particles.handle, method.code, float(method.alpha), _p3(V), float(dt),
+                                            _coords(particles), particles.index.data_ptr(), rec.data_ptr())
+    _finish(particles, rc, "advection! (recorded)")
+
+
+def advection_vjp_recorded_(particles: Particles, method: AbstractAdvectionIntegrator, dt, rec: torch.Tensor, index,
+                            lam, gV) -> None:
+    """advection_vjp_ of a recorded step: no replay of the stages. ``index``
+    is the occupancy before the step."""
+    _require_2d(particles)
+    _bind_stream(particles)
+    rc = _native.load().jp_advection_vjp_recorded(particles.handle, method.code, float(method.alpha), float(dt),
+                                                  rec.data_ptr(), index.data_ptr(), _p3(lam), _p3(gV))
+    _finish(particles, rc, "advection! adjoint (recorded)")
+
+
 def move_permutation(particles: Particles) -> torch.Tensor:
     """Slot map of the last move_particles! call: dest[s, c] = linear slot now
     holding the particle that sat in slot (s, c) before it, or -1."""
@@ -128,7 +156,8 @@ def slot_ids(particles: Particles, index=None) -> CellArray:
     """ids[s, c] = linear slot for live slots, -1 elsewhere (a particle field
     to pass through inject_particles!)."""
     index = index if index is not None else particles.index
-    ids = _like(particles, -1.0)
+    ids = CellArray(torch.empty(tuple(particles.index.data.shape), dtype=torch.float64, device="cuda"),
+                    particles.ni)  # every slot is written
     _bind_stream(particles)
     _finish(particles, _native.load().jp_slot_ids(particles.handle, index.data_ptr(), ids.data_ptr()), "slot_ids")
     return ids
@@ -201,11 +230,12 @@ def misfit(F: torch.Tensor, W: torch.Tensor, target: torch.Tensor):
 
 
 def _recorded_step(p: Particles, method, V, dt, fields, inject: bool):
-    """One step that also records what the reverse sweep needs: positions and
-    occupancy before it, the move's slot map and the injection's source ids."""
-    X = tuple(c.data.clone() for c in p.coords)
+    """One step that also records what the reverse sweep needs: the velocity
+    samples of its advection, the occupancy before it, the move's slot map and
+    the injection's source ids."""
     idx = p.index.data.clone()
-    advection_(p, method, V, dt)
+    X = record_buffer(p, method)
+    advection_record_(p, method, V, dt, X)
     move_particles_(p, fields)
     dest = move_permutation(p)
     ids = None
@@ -263,7 +293,7 @@ def reverse_sweep(particles: Particles, method, V, dt, nsteps: int, checkpoints,
                 permute_vjp_(particles, dest, lam + [gT], tmp_x + [tmp_t])
                 lam, tmp_x = tmp_x, lam
                 gT, tmp_t = tmp_t, gT
-            advection_vjp_(particles, method, V, dt, X, _Idx(idx), lam, gV)
+            advection_vjp_recorded_(particles, method, dt, X, _Idx(idx), lam, gV)
     _restore(particles, checkpoints[0])
     ni = particles.ni
     return gV, tuple(CellArray(l, ni) for l in lam), CellArray(gT, ni)

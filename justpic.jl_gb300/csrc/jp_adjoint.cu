@@ -93,14 +93,6 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------ injection
-template <typename IdT>
-__global__ void __launch_bounds__(kThreads)
-    slot_ids_kernel(int64_t nslots, const uint8_t* __restrict__ index, IdT* __restrict__ ids)
-{
-    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= nslots) return;
-    ids[a] = index[a] ? (IdT)a : (IdT)-1;
-}
 
 // Per cell: the slots whose id names another slot (particles injected by the
 // traced call), after checking that each source lies within reach; and a flag
@@ -110,12 +102,57 @@ __global__ void __launch_bounds__(kThreads)
 // index of the particle its fields were copied from when it was injected, a
 // negative value otherwise; as doubles (FP64 fields) or as int32 (carried bit
 // for bit through an FP32 field).
-__device__ __forceinline__ bool id_other(double id, int64_t a) { return id >= 0.0 && id != (double)a; }
+// Slot ids as doubles hold whole numbers below 2^53; they are built and read on
+// the integer pipe (GB300's FP64 conversions run at the FP64 rate): the double
+// of a >= 0 is exponent floor(log2 a) and the bits below the leading one.
+__device__ __forceinline__ uint64_t id_bits(int64_t a)
+{
+    if (a == 0) return 0ull;
+    const int e = 63 - __clzll(a);  // a < 2^53
+    return ((uint64_t)(1023 + e) << 52) | (((uint64_t)a << (52 - e)) & ((1ull << 52) - 1));
+}
+
+// the whole number a double id holds, or -1 for anything else (negative, NaN, >= 2^53)
+__device__ __forceinline__ int64_t id_value(double id)
+{
+    const uint64_t b = (uint64_t)__double_as_longlong(id);
+    if (b == 0) return 0;
+    const int E = (int)(b >> 52);  // sign bit included
+    if (E < 1023 || E > 1023 + 52) return -1;
+    const int e = E - 1023;
+    const uint64_t m = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    if (m & ((1ull << (52 - e)) - 1)) return -1;  // not a whole number
+    return (int64_t)(m >> (52 - e));
+}
+
+__device__ __forceinline__ bool id_other(double id, int64_t a)
+{
+    const int64_t v = id_value(id);
+    return v >= 0 && v != a;
+}
 __device__ __forceinline__ bool id_other(int32_t id, int64_t a) { return id >= 0 && (int64_t)id != a; }
-__device__ __forceinline__ bool id_self(double id, int64_t a) { return id == (double)a; }
+__device__ __forceinline__ bool id_self(double id, int64_t a) { return id_value(id) == a; }
 __device__ __forceinline__ bool id_self(int32_t id, int64_t a) { return (int64_t)id == a; }
-__device__ __forceinline__ int64_t id_slot(double id, int64_t ns) { return id < (double)ns ? (int64_t)id : ns; }
+__device__ __forceinline__ int64_t id_slot(double id, int64_t ns)
+{
+    const int64_t v = id_value(id);
+    return v >= 0 && v < ns ? v : ns;
+}
 __device__ __forceinline__ int64_t id_slot(int32_t id, int64_t ns) { return (int64_t)id < ns ? (int64_t)id : ns; }
+__device__ __forceinline__ double id_make(int64_t a, double) { return __longlong_as_double((long long)id_bits(a)); }
+__device__ __forceinline__ int32_t id_make(int64_t a, int32_t) { return (int32_t)a; }
+__device__ __forceinline__ double id_none(double) { return -1.0; }
+__device__ __forceinline__ int32_t id_none(int32_t) { return -1; }
+
+template <typename IdT>
+__global__ void __launch_bounds__(kThreads)
+    slot_ids_kernel(int64_t nslots, const uint8_t* __restrict__ index, IdT* __restrict__ ids)
+{
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nslots) return;
+    ids[a] = index[a] ? id_make(a, IdT()) : id_none(IdT());
+}
+
 
 template <typename IdT>
 __global__ void __launch_bounds__(kThreads)
@@ -167,6 +204,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int k = 0; k < P.n; ++k) P.pre[k][a] = kept ? P.post[k][a] : 0.0;
     }
     if (!copies || !srcflag[c]) return;
+    const int64_t ns = nc * g.max_xcell;
     const int64_t cx = c % g.n[0], cy = c / g.n[0];
     for (int64_t y = max(cy - kInjectReach, (int64_t)0); y <= min(cy + kInjectReach, g.n[1] - 1); ++y)
         for (int64_t x = max(cx - kInjectReach, (int64_t)0); x <= min(cx + kInjectReach, g.n[0] - 1); ++x) {
@@ -176,7 +214,7 @@ __global__ void __launch_bounds__(kThreads)
                 const int s = __ffsll((long long)m) - 1;
                 m &= m - 1;
                 const int64_t b = w + nc * s;
-                const int64_t src = (int64_t)ids[b];  // a slot index: inject_mask_kernel checked it
+                const int64_t src = id_slot(ids[b], ns);  // a slot index: inject_mask_kernel checked it
                 if (src % nc != c) continue;
                 for (int k = 0; k < P.n; ++k)
                     if ((copies >> k) & 1u) P.pre[k][src] += P.post[k][b];
@@ -206,11 +244,18 @@ __device__ __forceinline__ Samp sample2(const DevGrid& g, int comp, const double
         const double* x = g.xvel[comp][d];
         const int J = I[d];
         const double a = ldg(x + J), b = ldg(x + J + 1);
-        const long long kp = okey(p[d]);
+        const long long kp = okey(p[d]), ka = okey(a), kb = okey(b);
+        const bool pnan = is_nan_bits(p[d]);
         int64_t k;
-        // the seed test on integer keys (exact for non-NaN values, off the FP64 pipe)
-        if (!is_nan_bits(p[d]) && okey(a) <= kp && kp <= okey(b)) {
+        // the forward's cell selection (interp_component): the seed test, then the open
+        // neighbouring intervals (the only answers the bisection can give there), on
+        // integer keys (exact for non-NaN values, off the FP64 pipe)
+        if (!pnan && ka <= kp && kp <= kb) {
             k = J;
+        } else if (!pnan && kb < kp && J + 2 < g.nvel[comp][d] && kp < okey(ldg(x + J + 2))) {
+            k = J + 1;
+        } else if (!pnan && kp < ka && J >= 1 && okey(ldg(x + J - 1)) < kp) {
+            k = J - 1;
         } else {
             if (!(g.lim_lo[comp][0] <= p[0] && p[0] <= g.lim_hi[comp][0] && g.lim_lo[comp][1] <= p[1] &&
                   p[1] <= g.lim_hi[comp][1])) {
@@ -239,6 +284,7 @@ struct AdjParams {
     double dt, adt;
     double ca, cb;  // RK2: X' = X + dt (ca V(X) + cb V(X + alpha dt V(X)))
     int method;
+    int half;  // alpha == 1/2: the forward's X' = X + dt V(X1)
 };
 
 // J^T g for the two components sampled at one point
@@ -389,6 +435,220 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, METHOD == JP_RUNGE_KUTTA4
             }
     }
     raise_err(d_err, errs);
+}
+
+// ----------------------------------------- recorded stages (no replay)
+// A step's record, written by the recording advection and read by the
+// recorded VJP and the deposit: per slot and velocity sample j = 2 q + comp,
+// the local coordinates t and the gradient dv of the bilinear sample, and the
+// window byte (as in Staging; 0xFF: deposits nothing), then one byte per slot
+// that is 0 when the forward sent the particle to Inf. Layout (ns slots, NQ
+// samples): t[(2j + d) ns + a], dv[(2j + d) ns + a], win[j ns + a], okf[a].
+struct Record {
+    double* t;
+    double* dv;
+    uint8_t* win;
+    uint8_t* okf;
+    int64_t nslots;
+};
+
+template <int METHOD>
+__host__ __device__ constexpr int rec_samples()
+{
+    return 2 * adj_stages<METHOD>();
+}
+
+__host__ __device__ inline size_t record_bytes(int64_t ns, int nq)
+{
+    return (size_t)ns * nq * (4 * sizeof(double) + 1) + (size_t)ns;
+}
+
+__host__ __device__ inline Record record_view(void* base, int64_t ns, int nq)
+{
+    Record r;
+    r.t = (double*)base;
+    r.dv = r.t + 2 * (size_t)nq * ns;
+    r.win = (uint8_t*)(r.dv + 2 * (size_t)nq * ns);
+    r.okf = r.win + (size_t)nq * ns;
+    r.nslots = ns;
+    return r;
+}
+
+// advection! (RK2, RK4, Euler; 2D FP64) that also records every velocity
+// sample for the reverse sweep. The stages are the adjoint replay's (the
+// forward's arithmetic and cell selection), so positions are those of
+// advection!, bit for bit; a sample outside its grid's limits is Inf, as in the
+// forward. A stage point outside the deposit window raises JP_ERR_ADJOINT_WINDOW.
+template <int METHOD>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, METHOD == JP_RUNGE_KUTTA4 ? 2 : 4)
+    advect_record_kernel(DevGrid g, const double* __restrict__ V0, const double* __restrict__ V1, AdjParams P,
+                         Coords X, const uint8_t* __restrict__ index, Record rec, int* d_err)
+{
+    constexpr int NS = adj_stages<METHOD>();
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ int cellI[kWarpsPerBlock][32][2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    {
+        const int64_t c = min(c0 + lane, nc - 1);
+        cellI[w][lane][0] = (int)(c % g.n[0]);
+        cellI[w][lane][1] = (int)(c / g.n[0]);
+    }
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
+    const double* Vc[2] = {V0, V1};
+    const int64_t ns = rec.nslots;
+    int errs = 0;
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        const int I[2] = {cellI[w][l][0], cellI[w][l][1]};
+        const double p0[2] = {X.c[0][a], X.c[1][a]};
+        double v[NS][2];
+        bool ok = true;
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            double x[2];
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                if (q == 0)
+                    x[d] = p0[d];
+                else if (METHOD == JP_RUNGE_KUTTA2)
+                    x[d] = fma(1.0, P.adt * v[0][d], p0[d]);
+                else if (q < 3)
+                    x[d] = p0[d] + (P.dt * v[q - 1][d]) * 0.5;
+                else
+                    x[d] = p0[d] + P.dt * v[2][d];
+            }
+#pragma unroll
+            for (int cc = 0; cc < 2; ++cc) {
+                const Samp S = sample2(g, cc, x, I, Vc[cc], &errs);
+                v[q][cc] = S.ok ? S.v : CUDART_INF;  // interp_velocity2particle outside the limits
+                ok &= S.ok;
+                // written as soon as sampled (fewer live registers); a particle the forward
+                // sends to Inf gets its windows cleared below
+                const int j = 2 * q + cc;
+                uint8_t wv = 0xFF;
+                if (S.ok) {
+                    const int ox = S.idx[0] - I[0] + 1, oy = S.idx[1] - I[1] + 1;
+                    const bool in = ox >= 0 && ox <= win_nx(cc) - 2 && oy >= 0 && oy <= win_ny(cc) - 2;
+                    if (in) wv = (uint8_t)(ox | (oy << 4));
+                    else errs |= kErrAdjointWindow;
+                    rec.t[(2 * j) * ns + a] = S.t[0];
+                    rec.t[(2 * j + 1) * ns + a] = S.t[1];
+                    rec.dv[(2 * j) * ns + a] = S.dv[0];
+                    rec.dv[(2 * j + 1) * ns + a] = S.dv[1];
+                }
+                rec.win[j * ns + a] = wv;
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {  // the forward's update (advect_particle)
+            double pd;
+            if (METHOD == JP_RUNGE_KUTTA2)
+                pd = P.half ? fma(1.0, P.dt * v[1][d], p0[d])
+                            : fma(1.0, P.dt * fma(P.ca, v[0][d], P.cb * v[1][d]), p0[d]);
+            else if (METHOD == JP_RUNGE_KUTTA4)
+                pd = p0[d] + __ddiv_rn(P.dt * (((v[0][d] + 2.0 * v[1][d]) + 2.0 * v[2][d]) + v[3][d]), 6.0);
+            else
+                pd = fma(1.0, P.dt * v[0][d], p0[d]);
+            X.c[d][a] = pd;
+        }
+        rec.okf[a] = ok ? 1 : 0;
+        if (!ok)
+#pragma unroll
+            for (int j = 0; j < 2 * NS; ++j) rec.win[j * ns + a] = 0xFF;
+    }
+    raise_err(d_err, errs);
+}
+
+// The VJP of a recorded step: lam (dL/dX after the step) becomes dL/dX before
+// it, and each sample's cotangent gk goes to the staging for the deposit
+// (which reads t and the window byte from the record).
+template <int METHOD>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    advect_vjp_rec_kernel(DevGrid g, AdjParams P, const uint8_t* __restrict__ index, Record rec, Coords Lam,
+                          double* __restrict__ gk_out)
+{
+    constexpr int NS = adj_stages<METHOD>();
+    __shared__ SlotList lists[kWarpsPerBlock];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
+    const int64_t ns = rec.nslots;
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        if (!rec.okf[a]) {  // the forward sent this particle to Inf; move_particles! dropped it
+            Lam.c[0][a] = 0.0;
+            Lam.c[1][a] = 0.0;
+            continue;
+        }
+        const double lam[2] = {Lam.c[0][a], Lam.c[1][a]};
+        Samp S[NS][2];
+#pragma unroll
+        for (int q = 0; q < NS; ++q)
+#pragma unroll
+            for (int cc = 0; cc < 2; ++cc) {
+                const int j = 2 * q + cc;
+                S[q][cc].dv[0] = rec.dv[(2 * j) * ns + a];
+                S[q][cc].dv[1] = rec.dv[(2 * j + 1) * ns + a];
+            }
+        double gk[NS][2], l0[2] = {lam[0], lam[1]}, qb[2];
+        if (METHOD == JP_RUNGE_KUTTA2) {
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                gk[NS - 1][d] = P.dt * P.cb * lam[d];
+                gk[0][d] = P.dt * P.ca * lam[d];
+            }
+            jt(S[NS - 1], gk[NS - 1], qb);
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                l0[d] += qb[d];
+                gk[0][d] += P.adt * qb[d];
+            }
+        } else if (METHOD == JP_RUNGE_KUTTA4) {
+            const double w6 = P.dt / 6.0;
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                gk[0][d] = w6 * lam[d];
+                gk[1][d] = 2.0 * w6 * lam[d];
+                gk[2][d] = 2.0 * w6 * lam[d];
+                gk[NS - 1][d] = w6 * lam[d];
+            }
+#pragma unroll
+            for (int q = NS - 1; q >= 1; --q) {
+                jt(S[q], gk[q], qb);
+                const double h = q == 3 ? P.dt : 0.5 * P.dt;
+#pragma unroll
+                for (int d = 0; d < 2; ++d) {
+                    l0[d] += qb[d];
+                    gk[q - 1][d] += h * qb[d];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int d = 0; d < 2; ++d) gk[0][d] = P.dt * lam[d];
+        }
+        jt(S[0], gk[0], qb);
+#pragma unroll
+        for (int d = 0; d < 2; ++d) l0[d] += qb[d];
+        Lam.c[0][a] = l0[0];
+        Lam.c[1][a] = l0[1];
+#pragma unroll
+        for (int q = 0; q < NS; ++q)
+#pragma unroll
+            for (int cc = 0; cc < 2; ++cc) gk_out[(2 * q + cc) * ns + a] = gk[q][cc];
+    }
 }
 
 constexpr int kDepThreads = 128;
@@ -914,6 +1174,19 @@ cudaError_t launch_inject_vjp_i32(jp_particles* P, const int32_t* ids, const dou
     return inject_vjp(P, ids, post, pre, n, copies);
 }
 
+static AdjParams adj_params(int method, double alpha, double dt)
+{
+    AdjParams prm;
+    prm.method = method;
+    prm.dt = dt;
+    prm.adt = alpha * dt;
+    const double ia = 1.0 / alpha;  // the forward's coefficients (alpha == 1/2 takes the dt * V(X1) form)
+    prm.ca = alpha == 0.5 ? 0.0 : std::fma(-0.5, ia, 1.0);
+    prm.cb = alpha == 0.5 ? 1.0 : 0.5 * ia;
+    prm.half = alpha == 0.5;
+    return prm;
+}
+
 template <int METHOD>
 static cudaError_t launch_advect_vjp(jp_particles* P, cudaStream_t st, const double* const V[3],
                                      const AdjParams& prm, const CCoords& X, const uint8_t* index, const Coords& L)
@@ -932,14 +1205,7 @@ cudaError_t launch_advection_vjp(jp_particles* P, int method, double alpha, cons
 {
     cudaError_t e = ensure_adjoint_scratch(P);
     if (e != cudaSuccess) return e;
-    AdjParams prm;
-    prm.method = method;
-    prm.dt = dt;
-    prm.adt = alpha * dt;
-    // the forward's coefficients (alpha == 1/2 takes the dt * V(X1) form)
-    const double ia = 1.0 / alpha;
-    prm.ca = alpha == 0.5 ? 0.0 : std::fma(-0.5, ia, 1.0);
-    prm.cb = alpha == 0.5 ? 1.0 : 0.5 * ia;
+    const AdjParams prm = adj_params(method, alpha, dt);
     CCoords X{{coords[0], coords[1], nullptr}};
     Coords L{{lam[0], lam[1], nullptr}};
     cudaStream_t st = P->stream;
@@ -950,6 +1216,69 @@ cudaError_t launch_advection_vjp(jp_particles* P, int method, double alpha, cons
     else
         e = launch_advect_vjp<JP_EULER>(P, st, V, prm, X, index, L);
     if (e != cudaSuccess) return e;
+    for (int c = 0; c < 2; ++c) {
+        const int64_t nn = P->g.nvel[c][0] * P->g.nvel[c][1];
+        vel_gather_kernel<<<grid_blocks(nn), kThreads, 0, st>>>(P->g, c, adj_parts(P), gV[c]);
+    }
+    return cudaGetLastError();
+}
+
+static int method_samples(int method)
+{
+    return method == JP_RUNGE_KUTTA4 ? 8 : (method == JP_RUNGE_KUTTA2 ? 4 : 2);
+}
+
+size_t advection_record_bytes(const jp_particles* P, int method)
+{
+    return record_bytes(P->g.ncells * P->g.max_xcell, method_samples(method));
+}
+
+cudaError_t launch_advection_record(jp_particles* P, int method, double alpha, const double* const V[3], double dt,
+                                    double* const coords[3], const uint8_t* index, void* rec)
+{
+    const AdjParams prm = adj_params(method, alpha, dt);
+    Coords X{{coords[0], coords[1], nullptr}};
+    const int64_t ns = P->g.ncells * P->g.max_xcell;
+    const Record r = record_view(rec, ns, method_samples(method));
+    const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const int nt = 32 * kWarpsPerBlock;
+    cudaStream_t st = P->stream;
+    if (method == JP_RUNGE_KUTTA2)
+        advect_record_kernel<JP_RUNGE_KUTTA2><<<nb, nt, 0, st>>>(P->g, V[0], V[1], prm, X, index, r, P->d_err);
+    else if (method == JP_RUNGE_KUTTA4)
+        advect_record_kernel<JP_RUNGE_KUTTA4><<<nb, nt, 0, st>>>(P->g, V[0], V[1], prm, X, index, r, P->d_err);
+    else
+        advect_record_kernel<JP_EULER><<<nb, nt, 0, st>>>(P->g, V[0], V[1], prm, X, index, r, P->d_err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advection_vjp_recorded(jp_particles* P, int method, double alpha, double dt, const void* rec,
+                                          const uint8_t* index, double* const lam[3], double* const gV[3])
+{
+    cudaError_t e = ensure_adjoint_scratch(P);
+    if (e != cudaSuccess) return e;
+    const AdjParams prm = adj_params(method, alpha, dt);
+    Coords L{{lam[0], lam[1], nullptr}};
+    const int64_t ns = P->g.ncells * P->g.max_xcell;
+    const int nq = method_samples(method);
+    const Record r = record_view(const_cast<void*>(rec), ns, nq);
+    Staging stg = adj_staging(P);
+    stg.t = r.t;  // the deposit reads the recorded coordinates and windows
+    stg.win = r.win;
+    cudaStream_t st = P->stream;
+    const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const unsigned nd = grid_blocks(P->g.ncells, kDepThreads);
+    const int nt = 32 * kWarpsPerBlock;
+    if (method == JP_RUNGE_KUTTA2) {
+        advect_vjp_rec_kernel<JP_RUNGE_KUTTA2><<<nb, nt, 0, st>>>(P->g, prm, index, r, L, stg.gk);
+        deposit_kernel<4><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
+    } else if (method == JP_RUNGE_KUTTA4) {
+        advect_vjp_rec_kernel<JP_RUNGE_KUTTA4><<<nb, nt, 0, st>>>(P->g, prm, index, r, L, stg.gk);
+        deposit_kernel<8><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
+    } else {
+        advect_vjp_rec_kernel<JP_EULER><<<nb, nt, 0, st>>>(P->g, prm, index, r, L, stg.gk);
+        deposit_kernel<2><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
+    }
     for (int c = 0; c < 2; ++c) {
         const int64_t nn = P->g.nvel[c][0] * P->g.nvel[c][1];
         vel_gather_kernel<<<grid_blocks(nn), kThreads, 0, st>>>(P->g, c, adj_parts(P), gV[c]);

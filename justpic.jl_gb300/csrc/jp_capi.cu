@@ -729,6 +729,43 @@ int jp_cellarray_permute(jp_particles* P, const void* src, void* dst, int64_t nn
                   "jp_cellarray_permute");
 }
 
+int jp_advection_record_bytes(jp_particles* P, int32_t method, uint64_t* bytes)
+{
+    if (!P || !bytes) return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_record_bytes: null pointer");
+    JP_REQUIRE_NARROW(P, "jp_advection_record_bytes");
+    if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_record_bytes: the adjoint is 2D");
+    *bytes = (uint64_t)jp::advection_record_bytes(P, method);
+    return JP_OK;
+}
+
+int jp_advection_record(jp_particles* P, int32_t method, double alpha, const double* const V[3], double dt,
+                        double* const coords[3], const uint8_t* index, void* rec)
+{
+    JP_REQUIRE_NARROW(P, "jp_advection_record");
+    if (!P || !index || !rec || !check_coords(P, (const void* const*)coords) ||
+        !check_coords(P, (const void* const*)V))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_record: null pointer");
+    if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_record: the adjoint is 2D");
+    if (method != JP_EULER && method != JP_RUNGE_KUTTA2 && method != JP_RUNGE_KUTTA4)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_record: unknown integrator");
+    if (method == JP_RUNGE_KUTTA2 && !(0.0 < alpha && alpha < 1.0))
+        return fail(JP_ERR_INVALID_ARGUMENT, "Only 0 < α < 1 is supported");
+    return finish(P, jp::launch_advection_record(P, method, alpha, V, dt, coords, index, rec), "jp_advection_record");
+}
+
+int jp_advection_vjp_recorded(jp_particles* P, int32_t method, double alpha, double dt, const void* rec,
+                              const uint8_t* index, double* const lam[3], double* const gV[3])
+{
+    JP_REQUIRE_NARROW(P, "jp_advection_vjp_recorded");
+    if (!P || !rec || !index || !lam || !gV || !lam[0] || !lam[1] || !gV[0] || !gV[1])
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_vjp_recorded: null pointer");
+    if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_vjp_recorded: the adjoint is 2D");
+    if (method != JP_EULER && method != JP_RUNGE_KUTTA2 && method != JP_RUNGE_KUTTA4)
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_vjp_recorded: unknown integrator");
+    return finish(P, jp::launch_advection_vjp_recorded(P, method, alpha, dt, rec, index, lam, gV),
+                  "jp_advection_vjp_recorded");
+}
+
 int jp_selftest_weight(uint64_t seed, int64_t n, int64_t* mismatches, uint64_t* first_bad_input)
 {
     if (!mismatches || n < 0) return fail(JP_ERR_INVALID_ARGUMENT, "jp_selftest_weight: bad arguments");

@@ -350,6 +350,12 @@ cudaError_t launch_cell_permute(jp_particles* P, const void* src, void* dst, int
 // inv_dist2 (particle2grid! weights) against CUDA's chain: mismatch count and first bad input
 cudaError_t launch_weight_selftest(uint64_t seed, int64_t n, unsigned long long* d_bad, unsigned long long* d_first,
                                    cudaStream_t st);
+// advection! that records its velocity samples, and the VJP of a recorded step (2D FP64)
+size_t advection_record_bytes(const jp_particles* P, int method);
+cudaError_t launch_advection_record(jp_particles* P, int method, double alpha, const double* const V[3], double dt,
+                                    double* const coords[3], const uint8_t* index, void* rec);
+cudaError_t launch_advection_vjp_recorded(jp_particles* P, int method, double alpha, double dt, const void* rec,
+                                          const uint8_t* index, double* const lam[3], double* const gV[3]);
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
                        const uint8_t* index, double* W = nullptr);
 

@@ -118,6 +118,56 @@ def test_advection_vjp_window_error():
         A.advection_vjp_(p, jp.RungeKutta2(), V, dt, X0, A._Idx(p.index.data), lam, gV)
 
 
+@pytest.mark.parametrize("method", ["euler", "rk2", "rk2_23", "rk4"])
+@pytest.mark.parametrize("dt_factor", [0.5, 0.9])
+def test_recorded_advection_and_vjp_match(method, dt_factor):
+    """jp_advection_record moves particles exactly like advection! and its
+    recorded VJP returns exactly what the replaying VJP returns."""
+    _, pm, alpha = METHODS[method]
+    g, p, Vh = _setup((12, 10))
+    V = _dev(Vh)
+    dt = dt_factor * W.cfl_dt(g, Vh)
+    X0 = tuple(c.data.clone() for c in p.coords)
+    idx0 = p.index.data.clone()
+    jp.advection_(p, pm, V, dt)
+    X1 = tuple(c.data.clone() for c in p.coords)
+    _set_coords(p, X0)
+    rec = A.record_buffer(p, pm)
+    A.advection_record_(p, pm, V, dt, rec)
+    for d in range(2):
+        assert torch.equal(torch.nan_to_num(p.coords[d].data, nan=-7.0), torch.nan_to_num(X1[d], nan=-7.0))
+    rng = np.random.default_rng(3)
+    lam0 = [torch.from_numpy(rng.standard_normal(tuple(c.data.shape))).cuda() for c in p.coords]
+    la = [l.clone() for l in lam0]
+    lb = [l.clone() for l in lam0]
+    ga = tuple(jp.grid_field(v.shape) for v in Vh)
+    gb = tuple(jp.grid_field(v.shape) for v in Vh)
+    A.advection_vjp_(p, pm, V, dt, X0, A._Idx(idx0), la, ga)
+    A.advection_vjp_recorded_(p, pm, dt, rec, A._Idx(idx0), lb, gb)
+    live = idx0.bool()
+    for d in range(2):
+        assert torch.equal(la[d][live], lb[d][live])
+        assert torch.equal(ga[d], gb[d])
+
+
+def test_recorded_advection_sends_far_particles_to_inf_like_advection():
+    g, p, Vh = _setup((8, 8))
+    V = _dev(Vh)
+    X0 = tuple(c.data.clone() for c in p.coords)
+    dt = 0.02 * W.cfl_dt(g, Vh)
+    # particles placed outside the velocity grids get Inf velocities (advection.jl:104-108)
+    bad = tuple(x.clone() for x in X0)
+    bad[0][0, :8] = 5.0
+    _set_coords(p, bad)
+    jp.advection_(p, jp.RungeKutta2(), V, dt)
+    X1 = tuple(c.data.clone() for c in p.coords)
+    _set_coords(p, bad)
+    A.advection_record_(p, jp.RungeKutta2(), V, dt, A.record_buffer(p, jp.RungeKutta2()))
+    for d in range(2):
+        assert torch.equal(torch.nan_to_num(p.coords[d].data, nan=-7.0), torch.nan_to_num(X1[d], nan=-7.0))
+    assert torch.isinf(p.coords[0].data[0, :8]).all()
+
+
 # ------------------------------------------------------ interpolations
 def test_particle2grid_vjp_matches_fd():
     g, p, _ = _setup()
