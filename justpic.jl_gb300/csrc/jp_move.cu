@@ -19,12 +19,15 @@
 // inject_particles! (src/Particles/injection.jl:19-131) only changes a cell
 // whose first quadrant is under-populated (the `break` at injection.jl:100
 // ends the walk otherwise), and that test depends on the cell alone. A flag
-// pass over all cells appends those cells to one work list per colour; each of
-// the 2^N colour passes then gives every listed cell a warp that stages the
-// cell's 3^N neighbourhood in shared memory and runs the reference's
-// sequential walk with warp-wide counts and nearest-neighbour searches. Cells
-// of one colour are independent, so the list order (set by atomics) does not
-// change any result.
+// pass over all cells appends those cells to one work list per colour and
+// records each cell's occupancy mask and particle bounding box; each of the
+// 2^N colour passes then gives every listed cell a warp that keeps the cell's
+// own particles in shared memory and runs the reference's sequential walk with
+// warp-wide counts and an exact nearest-neighbour search that only visits the
+// neighbour cells whose box can hold a nearer particle. Cells of one colour
+// are independent, so the list order (set by atomics) does not change any
+// result. Containers of more than 64 slots per cell use the reference's own
+// per-cell schedule instead (bottom of this file).
 #include <math_constants.h>
 
 #include <climits>
@@ -326,54 +329,6 @@ __device__ __forceinline__ double warp_min(double v)
     return v;
 }
 
-// Per-warp shared-memory image of a cell's 3^N neighbourhood: occupancy and
-// FP32 coordinates relative to the cell's lower-left vertex for every
-// candidate slot, the FP64 coordinates of the cell's own slots, and the FP32
-// squared distances of the current search.
-template <int DIM>
-struct Hood {
-    float* r[DIM];     // candidate coordinate minus the cell corner, rounded to FP32
-    float* ss32;       // FP32 squared distance of the current search (-1: evaluate in FP64)
-    double* own[DIM];  // FP64 coordinates of the cell's own slots
-    uint8_t* live;     // 0 empty, 1 live, 2 live but too far for the FP32 screen
-};
-
-template <int DIM>
-__host__ __device__ __forceinline__ size_t hood_bytes(int M)
-{
-    const int n = (DIM == 2 ? 9 : 27) * M;
-    const size_t bytes = (size_t)M * DIM * sizeof(double) + (size_t)n * ((DIM + 1) * sizeof(float) + 1);
-    return (bytes + 15) & ~(size_t)15;  // keep every warp's arrays 16-byte aligned
-}
-
-template <int DIM>
-__device__ __forceinline__ double candidate_ss(const DevGrid& g, const Coords& X, const Hood<DIM>& H,
-                                               const int64_t* I, int o, int M, const double* pn)
-{
-    constexpr int CENTER = DIM == 2 ? 4 : 13;
-    const int nb = o / M, s = o - nb * M;
-    double e[3];
-    if (nb == CENTER) {
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) e[d] = H.own[d][s] - pn[d];
-    } else {
-        const int64_t J[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1, DIM == 3 ? I[2] + nb / 9 - 1 : 0};
-        const int64_t a = cell_linear<DIM>(g, J) + g.ncells * s;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) e[d] = X.c[d][a] - pn[d];
-    }
-    return DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
-}
-
-// _inject_particles! (src/Particles/injection.jl:68-131) for one cell, by one warp.
-// The nearest-neighbour result of index_min_distance (injection.jl:330-393) is
-// the first candidate, in the reference's k -> j -> i -> slot order, whose
-// FP64 distance sqrt(ss) equals the minimum. An FP32 screen finds it without
-// FP64 work on every candidate: with an absolute error bound E on the FP32
-// squared distances, only candidates whose FP32 value is within
-// (min + E)(1 + tol) + E can be at (or within rounding of) the FP64 minimum;
-// those, and any candidate too far from the cell for the bound to hold, are
-// evaluated exactly in FP64, then sqrt decides the tie-break as in the reference.
 // Grid fields that inject_particles_phase! interpolates onto new particles
 // (one per particle field of Args), each cell-centred or on the vertices.
 struct PhaseFields {
@@ -679,232 +634,6 @@ __device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* _
     }
 }
 
-template <int DIM, bool PHASE>
-__device__ void inject_cell_warp(const DevGrid& g, const Coords& X, uint8_t* __restrict__ index, uint64_t* lm,
-                                 const Args& A, const PhaseFields& PF, uint32_t call, int64_t c, const Hood<DIM>& H,
-                                 int lane, int* errs)
-{
-    const int64_t nc = g.ncells;
-    const int M = g.max_xcell;
-    constexpr int NB = DIM == 2 ? 9 : 27;
-    constexpr int CENTER = DIM == 2 ? 4 : 13;
-    const int ncand = NB * M;
-    int64_t I[3];
-    cell_coords(g, c, I);
-    double corner[3], dq[3];
-    float hmax[3];
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-        corner[d] = ldg(g.xv[d] + I[d]);
-        const double dx = ldg(g.dxv[d] + I[d]);
-        dq[d] = dx / 2.0;
-        double h = dx;
-        if (I[d] > 0) h = fmax(h, ldg(g.dxv[d] + I[d] - 1));
-        if (I[d] + 1 < g.n[d]) h = fmax(h, ldg(g.dxv[d] + I[d] + 1));
-        hmax[d] = (float)h;
-    }
-    // the FP32 screen needs spacings well inside FP32 range; otherwise every
-    // candidate is evaluated in FP64
-    bool screen_ok = true;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) screen_ok &= hmax[d] >= 1e-12f && hmax[d] <= 1e12f;
-    // Stage the neighbourhood. The occupancy comes from the flag pass's
-    // per-cell masks (one load per neighbour cell); the coordinates of the
-    // live candidates are loaded in batches, all loads of a batch in flight
-    // together, then converted and stored.
-    int64_t nbc = 0;
-    uint64_t nbm = 0;
-    if (lane < NB) {
-        const int64_t J[3] = {I[0] + lane % 3 - 1, I[1] + (lane / 3) % 3 - 1, DIM == 3 ? I[2] + lane / 9 - 1 : 0};
-        const bool ok = J[0] >= 0 && J[1] >= 0 && J[0] < g.n[0] && J[1] < g.n[1] &&
-                        (DIM == 2 || (J[2] >= 0 && J[2] < g.n[2]));
-        if (ok) {
-            nbc = cell_linear<DIM>(g, J);
-            nbm = lm[nbc];
-        }
-    }
-    constexpr int B = 6;
-    for (int base = 0; base < ncand; base += 32 * B) {
-        double xs[B][DIM];
-        bool lv[B];
-        int64_t av[B];
-#pragma unroll
-        for (int u = 0; u < B; ++u) {
-            const int o = base + 32 * u + lane;
-            const int nb = o / M, s = o - nb * M;
-            const uint64_t m = __shfl_sync(0xffffffffu, nbm, nb < NB ? nb : 0);
-            const int64_t cc = __shfl_sync(0xffffffffu, nbc, nb < NB ? nb : 0);
-            lv[u] = o < ncand && ((m >> s) & 1ull);
-            av[u] = cc + nc * s;
-            if (lv[u]) {
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) xs[u][d] = X.c[d][av[u]];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < B; ++u) {
-            const int o = base + 32 * u + lane;
-            if (o >= ncand) continue;
-            const int nb = o / M, s = o - nb * M;
-            uint8_t live = 0;
-            if (lv[u]) {
-                bool far = false;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) {
-                    const double x = xs[u][d];
-                    const float r = (float)(x - corner[d]);
-                    H.r[d][o] = r;
-                    far |= (!(fabsf(r) <= 4.0f * hmax[d]) && !isnan(r)) || !screen_ok;
-                    if (nb == CENTER) H.own[d][s] = x;
-                }
-                live = far ? 2 : 1;
-            }
-            H.live[o] = live;
-        }
-    }
-    __syncwarp();
-    // E: bound on |ss32 - ss64| for screened candidates (|r| <= 4h, new point inside the cell)
-    float E = 0.0f;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) E += 36.0f * hmax[d] * hmax[d];
-    E *= 0x1.0p-16f;
-    const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
-    const int base = CENTER * M;
-    for (int q = 0; q < (1 << DIM); ++q) {
-        double qc[3];
-        long long klo[3], khi[3];
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            qc[d] = corner[d] + dq[d] * (double)((q >> d) & 1);
-            klo[d] = okey(qc[d]);
-            khi[d] = okey(qc[d] + dq[d]);  // isincell(p, vertex, di_quadrant)
-        }
-        int cnt = 0;
-        for (int s = lane; s < M; s += 32) {
-            if (!H.live[base + s]) continue;
-            bool in = true;
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const double x = H.own[d][s];
-                const long long k = okey(x);
-                in = in & !is_nan_bits(x) & (klo[d] < k) & (k < khi[d]);
-            }
-            cnt += in ? 1 : 0;
-        }
-        int count = __reduce_add_sync(0xffffffffu, cnt);
-        if (count >= min_xq) {
-            if (PHASE) continue;  // inject_particles_phase! checks every quadrant (injection.jl:273)
-            break;                // injection.jl:100
-        }
-        const bool f0 = lane < M && !H.live[base + lane];
-        const bool f1 = lane + 32 < M && !H.live[base + lane + 32];
-        uint64_t freem = (uint64_t)__ballot_sync(0xffffffffu, f0) | ((uint64_t)__ballot_sync(0xffffffffu, f1) << 32);
-        while (freem) {
-            const int i = __ffsll((long long)freem) - 1;
-            freem &= freem - 1;
-            ++count;
-            double pn[3];
-            float pr[3];
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const double r = jp_rand_uniform(g.seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)i,
-                                                 (uint32_t)d);
-                pn[d] = qc[d] + dq[d] * fma(0.95, r, 0.05);  // new_particle, injection.jl:411-417
-                pr[d] = (float)(pn[d] - corner[d]);
-            }
-            const int64_t ai = c + nc * i;
-            if (lane == 0) {
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) {
-                    X.c[d][ai] = pn[d];
-                    H.own[d][i] = pn[d];
-                    H.r[d][base + i] = pr[d];
-                }
-                index[ai] = 1;
-                H.live[base + i] = 1;
-            }
-            __syncwarp();
-            // screen: FP32 squared distances
-            float lmin = CUDART_INF_F;
-            for (int o = lane; o < ncand; o += 32) {
-                float s32 = CUDART_NAN_F;  // not a candidate: fails every screen test
-                const uint8_t lv = H.live[o];
-                if (lv && o != base + i) {
-                    if (lv == 2) {
-                        s32 = -1.0f;
-                    } else {
-                        float t = 0.0f;
-#pragma unroll
-                        for (int d = 0; d < DIM; ++d) {
-                            const float e = H.r[d][o] - pr[d];
-                            t += e * e;
-                        }
-                        s32 = t;  // NaN coordinates give NaN and never pass the screen
-                        lmin = fminf(lmin, t);
-                    }
-                }
-                H.ss32[o] = s32;
-            }
-            float m32 = lmin;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) m32 = fminf(m32, __shfl_xor_sync(0xffffffffu, m32, off));
-            const float thr = (m32 + E) * (1.0f + 0x1.0p-20f) + E;
-            __syncwarp();
-            // exact FP64 distances of the screened candidates
-            double lbest = CUDART_INF;
-            for (int o = lane; o < ncand; o += 32) {
-                const float s32 = H.ss32[o];
-                if (s32 < 0.0f || s32 <= thr) {
-                    const double ss = candidate_ss<DIM>(g, X, H, I, o, M, pn);
-                    if (!isnan(ss)) lbest = fmin(lbest, ss);
-                }
-            }
-            const double best = warp_min(lbest);
-            int64_t src = -1;
-            if (best < CUDART_INF) {
-                // the first candidate (in order) whose rounded distance equals sqrt(best)
-                const double dmin = sqrt(best);
-                const double bound = best * (1.0 + 0x1.0p-48);
-                int lo = 0x7fffffff;
-                for (int o = lane; o < ncand; o += 32) {
-                    const float s32 = H.ss32[o];
-                    if (s32 < 0.0f || s32 <= thr) {
-                        const double ss = candidate_ss<DIM>(g, X, H, I, o, M, pn);
-                        if (ss <= bound && sqrt(ss) == dmin) {
-                            lo = o;
-                            break;  // lane-strided order: the first hit is this lane's smallest
-                        }
-                    }
-                }
-                const int win = __reduce_min_sync(0xffffffffu, lo);
-                const int nb = win / M, s = win - nb * M;
-                const int64_t J[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1, DIM == 3 ? I[2] + nb / 9 - 1 : 0};
-                src = cell_linear<DIM>(g, J) + nc * s;
-            }
-            if (PHASE) {
-                if (src >= 0) {
-                    if (lane == 0) PF.phases[ai] = PF.phases[src];
-                } else {
-                    *errs |= kWarnNoNeighbour;
-                }
-                for (int k = lane; k < A.n; k += 32)
-                    A.a[k][ai] = phase_field_value<DIM>(g, PF.f[k], PF.centred[k] != 0, pn, I, corner, dq);
-            } else if (src >= 0) {
-                for (int k = lane; k < A.n; k += 32) A.a[k][ai] = A.a[k][src];
-            } else if (A.n > 0) {
-                *errs |= kWarnNoNeighbour;
-            }
-            __syncwarp();
-            if (count >= min_xq) break;
-        }
-    }
-    // the cell's occupancy after its injections, for the later passes' staging
-    __syncwarp();
-    const bool o0 = lane < M && H.live[base + lane];
-    const bool o1 = lane + 32 < M && H.live[base + lane + 32];
-    const uint64_t own = (uint64_t)__ballot_sync(0xffffffffu, o0) | ((uint64_t)__ballot_sync(0xffffffffu, o1) << 32);
-    if (lane == 0) lm[c] = own;
-}
 
 // One colour pass: warps take the colour's listed cells in turn.
 template <int DIM, bool PHASE>
