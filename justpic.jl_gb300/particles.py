@@ -282,6 +282,10 @@ def init_particles_empty(backend, nxcell, max_xcell, min_xcell, *xi_vel, seed: i
     xvi = tuple(host[d][d] for d in range(N))
     xci = _center_coordinates(host, uniform)
     if uniform:
+        if any(len(x) < 2 for x in xci):
+            # the reference takes getindex(xci, 2) - first(xci) (particles_utils.jl:137), which
+            # has no second centre on a single-cell axis of a range grid
+            raise ArgumentError("range grids need at least 2 cells per axis (use vector grids for one cell)")
         dvert = tuple(x[1] - x[0] for x in xvi)
         dcent = tuple(x[1] - x[0] for x in xci)
         dvel = tuple(tuple(x[1] - x[0] for x in comp) for comp in host)
