@@ -366,7 +366,7 @@ int jp_move_particles_noalloc(jp_particles* P, double* const coords[3], uint8_t*
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles_noalloc: bad particle field list");
     for (int k = 0; k < nargs; ++k)
         if (!args[k]) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles_noalloc: null field");
-    const size_t need = jp::move_scratch_bytes(P->g, P->g.ndim + nargs);
+    const size_t need = jp::move_scratch_bytes(P->g, jp::shadow_stride(P->g.ndim + nargs));
     if (need > jp::kNoAllocScratchBytes)
         return fail(JP_ERR_INVALID_ARGUMENT,
                     "jp_move_particles_noalloc: this container needs " + std::to_string(need) +

@@ -786,7 +786,7 @@ cudaError_t launch_move_f32(jp_particles* P, float* const xi[3], uint8_t* index,
 {
     const int N = P->g.ndim;
     // FP32 records (4 bytes per value) fit in the scratch sized for FP64 records
-    cudaError_t e = ensure_move_scratch(P, N + nargs);
+    cudaError_t e = ensure_move_scratch(P, shadow_stride(N + nargs));
     if (e != cudaSuccess) return e;
     XiF Xi{{xi[0], xi[1], N == 3 ? xi[2] : nullptr}};
     ArgsF A{};
@@ -794,7 +794,8 @@ cudaError_t launch_move_f32(jp_particles* P, float* const xi[3], uint8_t* index,
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
     const MoveScratch& m = P->move;
     MoveViewF S;
-    S.m = MoveView{m.rec, P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, N + nargs};
+    S.m = MoveView{m.rec, P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell,
+                   shadow_stride(N + nargs)};  // 3 values padded to 4: 16-byte records
     S.shadow = (float*)m.shadow;
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(P->g.ncells);

@@ -377,6 +377,9 @@ cudaError_t launch_g2p_vjp(jp_particles* P, const double* F, const double* gFp, 
 
 // scratch of move_particles! owned by the container (allocated on first use)
 cudaError_t ensure_move_scratch(jp_particles* P, int comps);
+// stride of a shadow record of `comps` doubles: 3 (2D with one field) is padded
+// to 4, so that every record is one aligned 32-byte sector for apply's gathers
+inline int shadow_stride(int comps) { return comps == 3 ? 4 : comps; }
 struct MoveView;
 void launch_allocate_passes(const DevGrid& g, const MoveView& S, cudaStream_t st);
 

@@ -963,14 +963,14 @@ cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index
 {
     if (P->g.max_xcell > 64) return launch_move_wide(P, coords, index, args, nargs);
     const int N = P->g.ndim;
-    cudaError_t e = ensure_move_scratch(P, N + nargs);
+    cudaError_t e = ensure_move_scratch(P, shadow_stride(N + nargs));
     if (e != cudaSuccess) return e;
     Coords X{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};
     Args A{};
     A.n = nargs;
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
     const MoveScratch& m = P->move;
-    MoveView S{m.rec, P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, N + nargs};
+    MoveView S{m.rec, P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, shadow_stride(N + nargs)};
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(P->g.ncells);
     const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
@@ -1167,10 +1167,10 @@ cudaError_t launch_move_noalloc(jp_particles* P, double* const coords[3], uint8_
     S.rec = (uint64_t*)base;
     S.nc = nc;
     S.shadow = (double*)(base + (size_t)(N == 2 ? kRecWords2D : kRecWords3D) * nc * sizeof(uint64_t));
-    S.orig = (uint16_t*)((char*)S.shadow + (size_t)(N + nargs) * ns * sizeof(double));
+    S.orig = (uint16_t*)((char*)S.shadow + (size_t)shadow_stride(N + nargs) * ns * sizeof(double));
     S.code = (uint8_t*)((char*)S.orig + ns * sizeof(uint16_t));
     S.nslots = ns;
-    S.comps = N + nargs;
+    S.comps = shadow_stride(N + nargs);
     Coords X{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};
     Args A{};
     A.n = nargs;

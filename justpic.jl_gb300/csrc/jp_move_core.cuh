@@ -24,7 +24,7 @@ struct MoveView {
     uint16_t* orig;
     double* shadow;
     int64_t nslots;
-    int comps;  // values per shadow record: DIM coordinates, then the fields (records are interleaved)
+    int comps;  // stride of the shadow records: DIM coordinates, then the fields (records are interleaved)
     __device__ __forceinline__ uint64_t& L(int64_t c) const { return rec[c]; }
     __device__ __forceinline__ uint64_t& R(int64_t c) const { return rec[nc + c]; }
     __device__ __forceinline__ uint64_t& U(int64_t c) const { return rec[2 * nc + c]; }
