@@ -226,8 +226,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             inside &= T >= 0 && T < g.n[d];
             far |= o > 1 || o < -1;
             off[d] = o;
-            // re-normalised offset in the target cell, in FP64, kept below 1
-            float r = (float)((double)xi[d] - (double)fl);
+            // re-normalised offset in the target cell, kept below 1. xi - fl is one
+            // correctly rounded FP32 subtraction: for fl = 1 it is exact (Sterbenz), for
+            // fl = -1 the exact 1 + xi fits FP64 whenever it does not round to 1.0f in FP32
+            // either, so this equals the FP64 difference rounded to FP32 (the particles
+            // moving farther are dropped) without the FP64 pipe
+            const float r = xi[d] - fl;
             rec[d] = r < 1.0f ? r : 0x1.fffffep-1f;
         }
         if (inside) {
