@@ -190,6 +190,43 @@ def _dist():
     return world, rank, local
 
 
+def _init_ranks(local, backend="nccl"):
+    """One process per GPU (torchrun sets RANK/WORLD_SIZE/MASTER_*). The ranks
+    are independent replicas of the workload: the only collectives are the
+    barriers around the timed region and the reductions of its results."""
+    import torch
+    import torch.distributed as dist
+
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+
+
+def _reduce_over_ranks(x, op, world, device="cuda"):
+    """``x`` reduced over all ranks: op "max" (the elapsed times: the job ends
+    with its slowest rank) or "sum" (the particles every rank processed)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t)
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def job_throughput(units_per_rank, elapsed, world, device="cuda"):
+    """Whole-job units/s: the units of all ranks over the slowest rank's time."""
+    return (_reduce_over_ranks(units_per_rank, "sum", world, device)
+            / _reduce_over_ranks(elapsed, "max", world, device))
+
+
 def movers_fraction(p, torch):
     """Fraction of live particles outside their cell (after an advection!)."""
     idx = p.index.data.bool()
@@ -225,9 +262,7 @@ def run_ours(args, form=None, minimal=False):
 
     world, rank, local = _dist()
     if world > 1 and not minimal:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        _init_ranks(local)
     elif world == 1:
         torch.cuda.set_device(0)
     jp._native.load()
@@ -319,8 +354,7 @@ def run_ours(args, form=None, minimal=False):
     events = [[[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)] for _ in ops]
               for _ in range(args.steps)]
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if world > 1:
-        torch.distributed.barrier()
+    _barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         t0.record(stream)
@@ -329,20 +363,16 @@ def run_ours(args, form=None, minimal=False):
         t1.record(stream)
         torch.cuda.synchronize()
     jp.synchronize(p)
-    if world > 1:
-        torch.distributed.barrier()
+    _barrier(world)
     live1 = int(p.index.data.sum())
-    elapsed = t0.elapsed_time(t1) / 1e3
-    if world > 1:
-        tt = torch.tensor([elapsed], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(tt)
     live = 0.5 * (live0 + live1)
-    value = live * args.steps * world / elapsed
+    elapsed_rank = t0.elapsed_time(t1) / 1e3
+    elapsed = _reduce_over_ranks(elapsed_rank, "max", world)
+    value = job_throughput(live * args.steps, elapsed_rank, world)
     op_ms = {op: float(np.mean([events[k][i][0].elapsed_time(events[k][i][1]) for k in range(args.steps)]))
              for i, op in enumerate(ops)}
     if minimal:
-        return {"value": live * args.steps / elapsed, "ms_per_step": 1e3 * elapsed / args.steps,
+        return {"value": value, "ms_per_step": 1e3 * elapsed / args.steps,
                 "per_call_ms": op_ms, "clocks": clocks.summary()}
 
     # ---- end to end through the public API (synchronous, host buffers) ----
@@ -354,6 +384,7 @@ def run_ours(args, form=None, minimal=False):
     rev = tuple(reversed(range(N)))
     hT = torch.empty(tuple(reversed(T.shape)), dtype=T.dtype).pin_memory() if nf else None
     e2e_steps = max(1, min(args.steps, 50))
+    _barrier(world)
     torch.cuda.synchronize()
     w0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -366,7 +397,7 @@ def run_ours(args, form=None, minimal=False):
     torch.cuda.synchronize()
     e2e_time = time.perf_counter() - w0
     Vcur[0] = V
-    e2e_value = live * e2e_steps * world / e2e_time
+    e2e_value = job_throughput(live * e2e_steps, e2e_time, world)
 
     # ---- roofline of the dominant call ----
     peak, peak_kind = _peaks()
