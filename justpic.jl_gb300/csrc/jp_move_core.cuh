@@ -148,100 +148,144 @@ __global__ void __launch_bounds__(kAllocThreads)
     }
 }
 
-// The 2D colour pass with the whole walk in registers: the destinations come
-// as nine per-target masks written by the classify stage (plus the mask of
-// particles that are not strictly inside their new cell), the occupancy masks
-// of the 3x3 neighbourhood are loaded once, and every update selects its
-// target with unrolled predicated operations, so no thread-local array is
-// indexed at run time. Same walk, same result as move_allocate<2>.
+// The 2D colour pass. A pass has one thread per source cell and few cells
+// (n/3 x n/3 of them), so its time is the latency of one thread's walk, and
+// the walk is written for a short dependency chain per step:
+//  * the slots still to visit are a mask (the candidates of the reference's
+//    slot loop; a particle put back into the centre cell ahead of the walk
+//    is added to it), popped lowest bit first;
+//  * the destination of a slot comes from four bit planes of the nine
+//    per-target masks written by the classify stage (no per-slot table);
+//  * "first free slot at or after starting_point" is the lowest set bit of
+//    the free mask under a running mask of the slots >= starting_point;
+//  * the centre cell's masks stay in registers, the eight neighbours' sit in
+//    the thread's own column of shared memory (one indexed access, no select
+//    over the neighbours), all global loads are issued before the first
+//    shared-memory store.
+// Same walk, same result as move_allocate<2>.
 static __global__ void __launch_bounds__(kAllocThreads)
     move_allocate_2d(DevGrid g, MoveView S, int o0, int o1, int64_t m0, int64_t m1)
 {
     constexpr int CENTER = 4;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // [neighbour][thread]: a warp's 64-bit accesses are conflict-free whatever neighbour each lane picks
+    __shared__ uint64_t sL[9][kAllocThreads], sR[9][kAllocThreads], sU[9][kAllocThreads];
+    const int tid = threadIdx.x;
+    const int64_t t = (int64_t)blockIdx.x * kAllocThreads + tid;
     if (t >= m0 * m1) return;
-    const int64_t ix = 3 * (t % m0) + o0, iy = 3 * (t / m0) + o1;
-    if (ix >= g.n[0] || iy >= g.n[1]) return;
+    int64_t qx, qy;
+    if (m0 * m1 <= (int64_t)0xFFFFFFFF) {  // 32-bit division
+        const uint32_t t32 = (uint32_t)t, w = (uint32_t)m0;
+        const uint32_t y = t32 / w;
+        qy = y;
+        qx = t32 - y * w;
+    } else {
+        qy = t / m0;
+        qx = t - qy * m0;
+    }
+    const int64_t ix = 3 * qx + o0, iy = 3 * qy + o1;
+    const int64_t nx = g.n[0];
+    if (ix >= nx || iy >= g.n[1]) return;
     const int64_t nc = g.ncells;
-    const int64_t sc = ix + g.n[0] * iy;
+    const int64_t sc = ix + nx * iy;
     const uint64_t Mv = S.M(sc);
     const uint64_t U0 = S.U(sc);
     if (Mv == 0 && U0 == 0) return;
-    uint64_t nL[9], nR[9], nU[9], tm[9];
+    uint64_t Lc = S.L(sc), Rc = S.R(sc), Uc = U0;
+    uint64_t nl[9], nr[9], nu[9], tm[10];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
+        if (k == CENTER) continue;
         const int64_t jx = ix + k % 3 - 1, jy = iy + k / 3 - 1;
-        const bool in = jx >= 0 && jy >= 0 && jx < g.n[0] && jy < g.n[1];
-        const int64_t jc = jx + g.n[0] * jy;
-        nL[k] = in ? S.L(jc) : 0;
-        nR[k] = in ? S.R(jc) : 0;
-        nU[k] = in ? S.U(jc) : 0;
-        tm[k] = S.T(sc, k);
+        const bool in = jx >= 0 && jy >= 0 && jx < nx && jy < g.n[1];
+        const int64_t jc = jx + nx * jy;
+        nl[k] = in ? S.L(jc) : 0;
+        nr[k] = in ? S.R(jc) : 0;
+        nu[k] = in ? S.U(jc) : 0;
     }
-    const uint64_t unst = S.T(sc, 9);
+#pragma unroll
+    for (int k = 0; k < 10; ++k) tm[k] = S.T(sc, k);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        if (k == CENTER) continue;
+        sL[k][tid] = nl[k];
+        sR[k][tid] = nr[k];
+        sU[k][tid] = nu[k];
+    }
+    // bit j of a slot's destination code in plane j; movers with no destination leave the domain
+    uint64_t P0 = 0, P1 = 0, P2 = 0, P3 = 0, routed = 0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        routed |= tm[k];
+        if (k & 1) P0 |= tm[k];
+        if (k & 2) P1 |= tm[k];
+        if (k & 4) P2 |= tm[k];
+        if (k & 8) P3 |= tm[k];
+    }
+    const uint64_t exits = Mv & ~routed;
+    const uint64_t unst = tm[9];
     const int nslot = g.max_xcell;
     const uint64_t valid = nslot == 64 ? ~0ull : ((1ull << nslot) - 1);
-    uint32_t touched = 1u << CENTER;
-    int sp = 0;  // starting_point (move_safe.jl:83)
-    int cur = 0;
-    while (cur < nslot) {
-        const uint64_t L = nL[CENTER], R = nR[CENTER], U = nU[CENTER];
-        const uint64_t cand = L & ((Mv & ~R) | (R & U)) & (~0ull << cur);
-        if (!cand) break;
-        const int s = __ffsll((long long)cand) - 1;
-        cur = s + 1;
-        const uint64_t bit = 1ull << s;
-        int code = -1;
-        bool unstable;
-        uint16_t tag;
-        if (R & bit) {  // refilled by an earlier pass and not strictly inside: walked again
-            code = CENTER;
-            unstable = true;
-            tag = S.orig[sc + nc * s];
-        } else {
-#pragma unroll
-            for (int k = 0; k < 9; ++k)
-                if (tm[k] & bit) code = k;
-            if (code < 0) {  // left the domain (or moved too far): cleared
-                nL[CENTER] = L & ~bit;
-                continue;
-            }
-            unstable = (unst & bit) != 0;
-            const int back = (1 - (code % 3 - 1)) + 3 * (1 - (code / 3 - 1));
-            tag = (uint16_t)(back | (s << 5));
+    uint32_t touched = 0;  // neighbours (not the centre) whose masks changed
+    // the reference's candidates: live slots that are original movers, or
+    // refilled by an earlier pass and not strictly inside
+    uint64_t todo = Lc & ((Mv & ~Rc) | (Rc & Uc));
+    uint64_t from_sp = valid;  // slots at or after starting_point (move_safe.jl:83)
+    while (todo) {
+        const uint64_t bit = todo & (0ull - todo);
+        todo ^= bit;
+        const bool refill = (Rc & bit) != 0;  // refilled by an earlier pass: walked again, into the centre
+        if (!refill && (exits & bit)) {  // left the domain (or moved too far): cleared
+            Lc &= ~bit;
+            continue;
         }
+        const int code = refill ? CENTER
+                                : (((P0 & bit) ? 1 : 0) | ((P1 & bit) ? 2 : 0) | ((P2 & bit) ? 4 : 0) |
+                                   ((P3 & bit) ? 8 : 0));
+        const bool unstable = refill || (unst & bit) != 0;
         // remove the particle from its slot (move_safe.jl:110-112)
-        nL[CENTER] = L & ~bit;
-        nR[CENTER] = R & ~bit;
-        nU[CENTER] = U & ~bit;
+        Lc &= ~bit;
+        Rc &= ~bit;
+        Uc &= ~bit;
         // find_free_memory(starting_point, ...) (move_safe.jl:192-197)
-        uint64_t tL = 0;
-#pragma unroll
-        for (int k = 0; k < 9; ++k) tL = k == code ? nL[k] : tL;
-        const uint64_t freem = ~tL & valid & (~0ull << sp);
+        const uint64_t tL = code == CENTER ? Lc : sL[code][tid];
+        const uint64_t freem = ~tL & from_sp;
         if (!freem) continue;  // dropped: no free slot at or after starting_point
-        const int f = __ffsll((long long)freem) - 1;
-        sp = f;
-        const uint64_t fb = 1ull << f;
-#pragma unroll
-        for (int k = 0; k < 9; ++k)
-            if (k == code) {
-                nL[k] |= fb;
-                nR[k] |= fb;
-                nU[k] = unstable ? (nU[k] | fb) : (nU[k] & ~fb);
+        const uint64_t fb = freem & (0ull - freem);
+        from_sp = valid & ~(fb - 1);
+        if (code == CENTER) {
+            Lc |= fb;
+            Rc |= fb;
+            if (unstable) {
+                Uc |= fb;
+                if (fb > bit) todo |= fb;  // ahead of the walk: visited again
+            } else {
+                Uc &= ~fb;
             }
-        touched |= 1u << code;
-        const int64_t tx = ix + code % 3 - 1, ty = iy + code / 3 - 1;
-        S.orig[tx + g.n[0] * ty + nc * f] = tag;
-    }
-#pragma unroll
-    for (int k = 0; k < 9; ++k)
-        if ((touched >> k) & 1) {
-            const int64_t jc = (ix + k % 3 - 1) + g.n[0] * (iy + k / 3 - 1);
-            S.L(jc) = nL[k];
-            S.R(jc) = nR[k];
-            S.U(jc) = nU[k];
+        } else {
+            sL[code][tid] = tL | fb;
+            sR[code][tid] |= fb;
+            sU[code][tid] = unstable ? (sU[code][tid] | fb) : (sU[code][tid] & ~fb);
+            touched |= 1u << code;
         }
+        const int s = __ffsll((long long)bit) - 1, f = __ffsll((long long)fb) - 1;
+        uint16_t tag;
+        if (refill)
+            tag = S.orig[sc + nc * s];
+        else
+            tag = (uint16_t)((8 - code) | (s << 5));  // 8 - code: the neighbour code of the way back
+        const int dy = code / 3 - 1, dx = code - 3 * (dy + 1) - 1;
+        S.orig[sc + dx + nx * dy + nc * f] = tag;
+    }
+    S.L(sc) = Lc;
+    S.R(sc) = Rc;
+    S.U(sc) = Uc;
+    for (uint32_t m = touched; m; m &= m - 1) {
+        const int k = __ffs(m) - 1;
+        const int64_t jc = sc + (k % 3 - 1) + nx * (k / 3 - 1);
+        S.L(jc) = sL[k][tid];
+        S.R(jc) = sR[k][tid];
+        S.U(jc) = sU[k][tid];
+    }
 }
 
 }  // namespace jp
