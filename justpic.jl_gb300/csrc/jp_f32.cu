@@ -202,11 +202,28 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             xi[d] = Xi.x[d][a];
             out |= !(xi[d] >= 0.0f && xi[d] < 1.0f);
         }
+        // The record is built in registers and a record of 4 values is stored
+        // whole (padding included), so whole sectors reach memory instead of
+        // partial ones that L2 would first have to read back from DRAM.
         float* rec = S.shadow + a * comps;
-        for (int j = 0; j < A.n; ++j) rec[DIM + j] = A.a[j][a];
+        const bool whole = comps == 4;
+        float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (whole) {
+#pragma unroll
+            for (int j = 0; j < 4 - DIM; ++j)
+                if (j < A.n) v[DIM + j] = A.a[j][a];
+        } else {
+            for (int j = 0; j < A.n; ++j) rec[DIM + j] = A.a[j][a];
+        }
         if (!out) {
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) rec[d] = xi[d];
+            for (int d = 0; d < DIM; ++d) v[d] = xi[d];
+            if (whole) {
+                *reinterpret_cast<float4*>(rec) = make_float4(v[0], v[1], v[2], v[3]);
+            } else {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) rec[d] = v[d];
+            }
             if (DIM == 3) S.m.code[a] = kCodeStay;
             continue;
         }
@@ -232,7 +249,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             // either, so this equals the FP64 difference rounded to FP32 (the particles
             // moving farther are dropped) without the FP64 pipe
             const float r = xi[d] - fl;
-            rec[d] = r < 1.0f ? r : 0x1.fffffep-1f;
+            v[d] = r < 1.0f ? r : 0x1.fffffep-1f;
+        }
+        if (whole) {
+            *reinterpret_cast<float4*>(rec) = make_float4(v[0], v[1], v[2], v[3]);
+        } else {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) rec[d] = v[d];
         }
         if (inside) {
             if (far) {

@@ -118,12 +118,25 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             kp[d] = okey(p[d]);
             pnan |= is_nan_bits(p[d]);
         }
-        // The shadow copy is written for every live slot, movers or not: whole
-        // 32-byte sectors reach memory instead of partial ones that L2 would
-        // first have to read back from DRAM.
+        // The shadow copy is written for every live slot, movers or not, and a
+        // record of 4 values is written whole (padding included): whole 32-byte
+        // sectors reach memory instead of partial ones that L2 would first
+        // have to read back from DRAM.
+        if (S.comps == 4) {
+            double v[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) S.shadow[a * S.comps + d] = p[d];
-        for (int j = 0; j < A.n; ++j) S.shadow[a * S.comps + DIM + j] = A.a[j][a];
+            for (int d = 0; d < DIM; ++d) v[d] = p[d];
+#pragma unroll
+            for (int j = 0; j < 4 - DIM; ++j)
+                if (j < A.n) v[DIM + j] = A.a[j][a];
+            double2* rec = reinterpret_cast<double2*>(S.shadow + a * 4);
+            rec[0] = make_double2(v[0], v[1]);
+            rec[1] = make_double2(v[2], v[3]);
+        } else {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) S.shadow[a * S.comps + d] = p[d];
+            for (int j = 0; j < A.n; ++j) S.shadow[a * S.comps + DIM + j] = A.a[j][a];
+        }
         bool in = !pnan;  // isincell, strict (src/Particles/utils.jl:7-15)
 #pragma unroll
         for (int d = 0; d < DIM; ++d) in = in & (cellk[w][l][d] < kp[d]) & (kp[d] < cellk[w][l][DIM + d]);
@@ -918,8 +931,7 @@ cudaError_t ensure_move_scratch(jp_particles* P, int comps)
     }
     const int64_t nc = P->g.ncells;
     const int64_t ns = nc * P->g.max_xcell;
-    const int rs = P->g.ndim == 2 ? kRecWords2D : kRecWords3D;
-    size_t bytes = (size_t)rs * nc * sizeof(uint64_t);  // mask arrays first (8-byte aligned)
+    size_t bytes = move_shadow_offset(P->g);  // mask arrays first
     const size_t off_shadow = bytes;
     bytes += (size_t)comps * ns * sizeof(double);
     const size_t off_orig = bytes;
@@ -1127,8 +1139,7 @@ size_t move_scratch_bytes(const DevGrid& g, int comps)
 {
     const size_t nc = (size_t)g.ncells;
     const size_t ns = nc * (size_t)g.max_xcell;
-    const size_t rs = g.ndim == 2 ? kRecWords2D : kRecWords3D;
-    return rs * nc * sizeof(uint64_t) + (size_t)comps * ns * sizeof(double) + ns * sizeof(uint16_t) + ns;
+    return move_shadow_offset(g) + (size_t)comps * ns * sizeof(double) + ns * sizeof(uint16_t) + ns;
 }
 
 // Host code may not use g_move_scratch's name as a device address: it stands
@@ -1166,7 +1177,7 @@ cudaError_t launch_move_noalloc(jp_particles* P, double* const coords[3], uint8_
     MoveView S;
     S.rec = (uint64_t*)base;
     S.nc = nc;
-    S.shadow = (double*)(base + (size_t)(N == 2 ? kRecWords2D : kRecWords3D) * nc * sizeof(uint64_t));
+    S.shadow = (double*)(base + move_shadow_offset(P->g));
     S.orig = (uint16_t*)((char*)S.shadow + (size_t)shadow_stride(N + nargs) * ns * sizeof(double));
     S.code = (uint8_t*)((char*)S.orig + ns * sizeof(uint16_t));
     S.nslots = ns;

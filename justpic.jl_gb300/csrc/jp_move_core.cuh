@@ -36,6 +36,15 @@ struct MoveView {
 
 constexpr int kTargetMasks2D = 10;
 
+// Byte offset of the shadow records in a move scratch block: after the mask
+// arrays, rounded up to 256 bytes (records of 4 values are stored as 16- and
+// 32-byte vectors, so they need at least that alignment).
+inline size_t move_shadow_offset(const DevGrid& g)
+{
+    const size_t rs = g.ndim == 2 ? kRecWords2D : kRecWords3D;
+    return (rs * (size_t)g.ncells * sizeof(uint64_t) + 255) & ~(size_t)255;
+}
+
 // -------------------------------------------------------------- allocate
 // One colour pass of move_particles!: sources 3*J + o, neighbourhoods
 // disjoint, so every mask touched here belongs to exactly one thread. The
