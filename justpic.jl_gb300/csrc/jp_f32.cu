@@ -313,9 +313,19 @@ __global__ void __launch_bounds__(kThreads)
             nb_offset<DIM>(tag & 0x1F, off);
             const int64_t J[3] = {I[0] + off[0], I[1] + off[1], DIM == 3 ? I[2] + off[2] : 0};
             const float* rec = S.shadow + (cell_linear<DIM>(g, J) + nc * (tag >> 5)) * comps;
+            if (comps == 4) {  // the whole 16-byte record in one load
+                const float4 r4 = *reinterpret_cast<const float4*>(rec);
+                const float v[4] = {r4.x, r4.y, r4.z, r4.w};
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) Xi.x[d][a] = rec[d];
-            for (int k = 0; k < A.n; ++k) A.a[k][a] = rec[DIM + k];
+                for (int d = 0; d < DIM; ++d) Xi.x[d][a] = v[d];
+#pragma unroll
+                for (int k = 0; k < 4 - DIM; ++k)
+                    if (k < A.n) A.a[k][a] = v[DIM + k];
+            } else {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) Xi.x[d][a] = rec[d];
+                for (int k = 0; k < A.n; ++k) A.a[k][a] = rec[DIM + k];
+            }
             index[a] = 1;
         } else {
 #pragma unroll

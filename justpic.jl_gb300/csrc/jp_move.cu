@@ -118,28 +118,30 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             kp[d] = okey(p[d]);
             pnan |= is_nan_bits(p[d]);
         }
-        // The shadow copy is written for every live slot, movers or not, and a
-        // record of 4 values is written whole (padding included): whole 32-byte
-        // sectors reach memory instead of partial ones that L2 would first
-        // have to read back from DRAM.
+        bool in = !pnan;  // isincell, strict (src/Particles/utils.jl:7-15)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) in = in & (cellk[w][l][d] < kp[d]) & (kp[d] < cellk[w][l][DIM + d]);
+        // The shadow copy. A record of 4 values is exactly one 32-byte sector:
+        // it is written whole (padding included) in one access, and only for
+        // movers (the apply stage gathers nothing else). Smaller or larger
+        // records are written for every live slot, so that the records of
+        // neighbouring slots fill whole sectors instead of partial ones that L2
+        // would first have to read back from DRAM.
         if (S.comps == 4) {
-            double v[4] = {0.0, 0.0, 0.0, 0.0};
+            if (!in) {
+                double v[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) v[d] = p[d];
+                for (int d = 0; d < DIM; ++d) v[d] = p[d];
 #pragma unroll
-            for (int j = 0; j < 4 - DIM; ++j)
-                if (j < A.n) v[DIM + j] = A.a[j][a];
-            double2* rec = reinterpret_cast<double2*>(S.shadow + a * 4);
-            rec[0] = make_double2(v[0], v[1]);
-            rec[1] = make_double2(v[2], v[3]);
+                for (int j = 0; j < 4 - DIM; ++j)
+                    if (j < A.n) v[DIM + j] = A.a[j][a];
+                store_rec4(S.shadow + a * 4, v);
+            }
         } else {
 #pragma unroll
             for (int d = 0; d < DIM; ++d) S.shadow[a * S.comps + d] = p[d];
             for (int j = 0; j < A.n; ++j) S.shadow[a * S.comps + DIM + j] = A.a[j][a];
         }
-        bool in = !pnan;  // isincell, strict (src/Particles/utils.jl:7-15)
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) in = in & (cellk[w][l][d] < kp[d]) & (kp[d] < cellk[w][l][DIM + d]);
         if (in) {  // move_safe.jl:93
             if (DIM == 3) S.code[a] = kCodeStay;
             continue;
@@ -223,9 +225,19 @@ __global__ void __launch_bounds__(kThreads)
             nb_offset<DIM>(tag & 0x1F, off);
             const int64_t J[3] = {I[0] + off[0], I[1] + off[1], DIM == 3 ? I[2] + off[2] : 0};
             const int64_t b = cell_linear<DIM>(g, J) + nc * (tag >> 5);
+            if (S.comps == 4) {  // the whole record in one 32-byte load
+                double v[4];
+                load_rec4(S.shadow + b * 4, v);
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) X.c[d][a] = S.shadow[b * S.comps + d];
-            for (int k = 0; k < A.n; ++k) A.a[k][a] = S.shadow[b * S.comps + DIM + k];
+                for (int d = 0; d < DIM; ++d) X.c[d][a] = v[d];
+#pragma unroll
+                for (int k = 0; k < 4 - DIM; ++k)
+                    if (k < A.n) A.a[k][a] = v[DIM + k];
+            } else {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) X.c[d][a] = S.shadow[b * S.comps + d];
+                for (int k = 0; k < A.n; ++k) A.a[k][a] = S.shadow[b * S.comps + DIM + k];
+            }
             index[a] = 1;
         } else {
 #pragma unroll

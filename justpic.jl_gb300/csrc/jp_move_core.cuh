@@ -36,6 +36,23 @@ struct MoveView {
 
 constexpr int kTargetMasks2D = 10;
 
+// One 32-byte shadow record (4 doubles) in a single 256-bit access: a gather
+// of a record is one sector request instead of one per value. p must be
+// 32-byte aligned (records start at a multiple of 32 bytes of a 256-byte
+// aligned array).
+__device__ __forceinline__ void load_rec4(const double* p, double v[4])
+{
+    asm volatile("ld.global.v4.f64 {%0, %1, %2, %3}, [%4];"
+                 : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3])
+                 : "l"(p));
+}
+
+__device__ __forceinline__ void store_rec4(double* p, const double v[4])
+{
+    asm volatile("st.global.v4.f64 [%0], {%1, %2, %3, %4};" ::"l"(p), "d"(v[0]), "d"(v[1]), "d"(v[2]), "d"(v[3])
+                 : "memory");
+}
+
 // Byte offset of the shadow records in a move scratch block: after the mask
 // arrays, rounded up to 256 bytes (records of 4 values are stored as 16- and
 // 32-byte vectors, so they need at least that alignment).
