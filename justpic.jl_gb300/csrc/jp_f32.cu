@@ -190,28 +190,21 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     uint64_t L;
     const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &L);
     const int comps = S.m.comps;
+    const bool whole = comps == 4;
     int errs = 0;
-    for (int k = lane; k < K; k += 32) {
-        int s, l;
-        slot_item(lists[w], M, k, &s, &l);
-        const int64_t a = c0 + l + nc * s;
-        float xi[3];
+    // one live particle: xi its offsets, fv its fields (records of 4 values)
+    auto classify_one = [&](int s, int l, int64_t a, const float* xi, const float* fv) {
         bool out = false;
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            xi[d] = Xi.x[d][a];
-            out |= !(xi[d] >= 0.0f && xi[d] < 1.0f);
-        }
+        for (int d = 0; d < DIM; ++d) out |= !(xi[d] >= 0.0f && xi[d] < 1.0f);
         // The record is built in registers and a record of 4 values is stored
         // whole (padding included), so whole sectors reach memory instead of
         // partial ones that L2 would first have to read back from DRAM.
         float* rec = S.shadow + a * comps;
-        const bool whole = comps == 4;
         float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         if (whole) {
 #pragma unroll
-            for (int j = 0; j < 4 - DIM; ++j)
-                if (j < A.n) v[DIM + j] = A.a[j][a];
+            for (int j = 0; j < 4 - DIM; ++j) v[DIM + j] = fv[j];
         } else {
             for (int j = 0; j < A.n; ++j) rec[DIM + j] = A.a[j][a];
         }
@@ -225,7 +218,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
                 for (int d = 0; d < DIM; ++d) rec[d] = v[d];
             }
             if (DIM == 3) S.m.code[a] = kCodeStay;
-            continue;
+            return;
         }
         atomicOr(&movers[w][l], 1ull << s);
         uint8_t code = kCodeExit;
@@ -269,6 +262,31 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         } else {
             S.m.code[a] = code;
         }
+    };
+    // Two particles per lane at a time: the loads of both are in flight
+    // before either is classified (the kernel is bound by load latency).
+    constexpr int B = 2;
+    for (int k0 = lane; k0 < K; k0 += 32 * B) {
+        int sl[B], ll[B];
+        int64_t al[B];
+        float xl[B][3], fl[B][4 - DIM];
+        bool has[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int k = k0 + 32 * u;
+            has[u] = k < K;
+            sl[u] = 0;
+            ll[u] = 0;
+            if (has[u]) slot_item(lists[w], M, k, &sl[u], &ll[u]);
+            al[u] = c0 + ll[u] + nc * sl[u];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) xl[u][d] = has[u] ? Xi.x[d][al[u]] : 0.0f;
+#pragma unroll
+            for (int j = 0; j < 4 - DIM; ++j) fl[u][j] = (has[u] && whole && j < A.n) ? A.a[j][al[u]] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (has[u]) classify_one(sl[u], ll[u], al[u], xl[u], fl[u]);
     }
     __syncwarp();
     const int64_t c = c0 + lane;

@@ -105,16 +105,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     uint64_t L;
     const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &L);
     int errs = 0;
-    for (int k = lane; k < K; k += 32) {
-        int s, l;
-        slot_item(lists[w], M, k, &s, &l);
-        const int64_t a = c0 + l + nc * s;
-        double p[3];
+    const bool rec4 = S.comps == 4;
+    // one live particle: p its coordinates, fv its fields (records of 4 values)
+    auto classify_one = [&](int s, int l, int64_t a, const double* p, const double* fv) {
         long long kp[3];
         bool pnan = false;
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
-            p[d] = X.c[d][a];
             kp[d] = okey(p[d]);
             pnan |= is_nan_bits(p[d]);
         }
@@ -127,14 +124,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         // records are written for every live slot, so that the records of
         // neighbouring slots fill whole sectors instead of partial ones that L2
         // would first have to read back from DRAM.
-        if (S.comps == 4) {
+        if (rec4) {
             if (!in) {
                 double v[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) v[d] = p[d];
 #pragma unroll
-                for (int j = 0; j < 4 - DIM; ++j)
-                    if (j < A.n) v[DIM + j] = A.a[j][a];
+                for (int j = 0; j < 4 - DIM; ++j) v[DIM + j] = fv[j];
                 store_rec4(S.shadow + a * 4, v);
             }
         } else {
@@ -144,7 +140,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         }
         if (in) {  // move_safe.jl:93
             if (DIM == 3) S.code[a] = kCodeStay;
-            continue;
+            return;
         }
         atomicOr(&movers[w][l], 1ull << s);
         bool inside = !pnan;  // indomain, strict (move_safe.jl:199-206)
@@ -178,6 +174,31 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         } else {
             S.code[a] = code;
         }
+    };
+    // Two particles per lane at a time: the loads of both are in flight
+    // before either is classified (the kernel is bound by load latency).
+    constexpr int B = 2;
+    for (int k0 = lane; k0 < K; k0 += 32 * B) {
+        int sl[B], ll[B];
+        int64_t al[B];
+        double pl[B][3], fl[B][4 - DIM];
+        bool has[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int k = k0 + 32 * u;
+            has[u] = k < K;
+            sl[u] = 0;
+            ll[u] = 0;
+            if (has[u]) slot_item(lists[w], M, k, &sl[u], &ll[u]);
+            al[u] = c0 + ll[u] + nc * sl[u];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) pl[u][d] = has[u] ? X.c[d][al[u]] : 0.0;
+#pragma unroll
+            for (int j = 0; j < 4 - DIM; ++j) fl[u][j] = (has[u] && rec4 && j < A.n) ? A.a[j][al[u]] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (has[u]) classify_one(sl[u], ll[u], al[u], pl[u], fl[u]);
     }
     __syncwarp();
     const int64_t c = c0 + lane;
