@@ -482,6 +482,154 @@ __device__ __forceinline__ double glob_ss(const Coords& X, int64_t b, const doub
     return DIM == 2 ? e[0] * e[0] + e[1] * e[1] : (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
 }
 
+// ---- the integer screen of the nearest-neighbour search ----
+// Coordinates become signed fixed-point integers in units of 2^(emax - 1075),
+// emax one above the largest biased exponent of the domain bounds, by integer
+// operations on their bits (truncated toward zero: the real value lies within
+// one unit). Differences of two such integers are exact, so a squared distance
+// is known within bounds from per-axis differences known within 2 units; the
+// bounds are formed in FP32 with directed rounding. None of this touches the
+// FP64 pipe, which is the scarce resource of the exact search.
+constexpr long long kFixNone = LLONG_MIN;  // no fixed-point value (NaN, Inf, beyond the scale)
+
+template <int DIM>
+__device__ __forceinline__ int fix_emax(const DevGrid& g)
+{
+    int e = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        e = max(e, (int)((__double_as_longlong(g.dom_lo[d]) >> 52) & 0x7FF));
+        e = max(e, (int)((__double_as_longlong(g.dom_hi[d]) >> 52) & 0x7FF));
+    }
+    return min(e + 1, 2046);
+}
+
+__device__ __forceinline__ long long fix_double(double x, int emax)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0x7FF || e > emax) return kFixNone;
+    const unsigned long long m = (b & ((1ull << 52) - 1)) | (e ? (1ull << 52) : 0ull);
+    const int sh = emax - (e ? e : 1);  // x = m 2^(max(e,1) - 1075)
+    const unsigned long long v = sh >= 64 ? 0ull : (m >> sh);
+    return (b >> 63) ? -(long long)v : (long long)v;
+}
+
+__device__ __forceinline__ long long fix_float(float x, int emax)
+{
+    const uint32_t b = __float_as_uint(x);
+    const int e = (int)((b >> 23) & 0xFF);
+    if (e == 0xFF) return kFixNone;
+    const unsigned long long m = (b & 0x7FFFFFu) | (e ? 0x800000u : 0u);
+    const int sh = (e ? e : 1) + 925 - emax;  // x = m 2^(max(e,1) - 150), unit 2^(emax - 1075)
+    unsigned long long v;
+    if (sh >= 0) {
+        if (sh > 38) return kFixNone;  // |v| would reach 2^62
+        v = m << sh;
+    } else {
+        v = -sh >= 64 ? 0ull : (m >> -sh);
+    }
+    return (b >> 31) ? -(long long)v : (long long)v;
+}
+
+// lo <= squared distance / unit^2 <= hi, for per-axis differences dx known within 2 units
+template <int DIM>
+__device__ __forceinline__ void ss_bounds(const long long* dx, float* lo, float* hi)
+{
+    float l = 0.0f, h = 0.0f;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const long long a = dx[d] < 0 ? -dx[d] : dx[d];
+        const float al = __ll2float_rd(a > 2 ? a - 2 : 0);
+        const float ah = __ll2float_ru(a + 2);
+        l = __fmaf_rd(al, al, l);
+        h = __fmaf_ru(ah, ah, h);
+    }
+    *lo = l;
+    *hi = h;
+}
+
+// per lane: the smallest upper bound seen, and the candidate with the smallest
+// lower bound (lo1, o1) with the next lower bound lo2
+struct ScreenTrack {
+    float hmin, lo1, lo2;
+    int o1;
+    __device__ __forceinline__ ScreenTrack()
+        : hmin(std::numeric_limits<float>::infinity()), lo1(std::numeric_limits<float>::infinity()),
+          lo2(std::numeric_limits<float>::infinity()), o1(-1)
+    {
+    }
+    __device__ __forceinline__ void add(float lo, float hi, int o)
+    {
+        hmin = fminf(hmin, hi);
+        if (lo < lo1) {
+            lo2 = lo1;
+            lo1 = lo;
+            o1 = o;
+        } else if (lo < lo2) {
+            lo2 = lo;
+        }
+    }
+};
+
+// screen bounds of one candidate from its coordinates (a candidate without a
+// fixed-point value is kept: lo 0, hi infinite)
+template <int DIM>
+__device__ __forceinline__ void screen_double(const double* q, const long long* pnI, int emax, float* lo, float* hi)
+{
+    long long dx[3];
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const long long v = fix_double(q[d], emax);
+        ok &= v != kFixNone;
+        dx[d] = v - pnI[d];
+    }
+    if (ok) {
+        ss_bounds<DIM>(dx, lo, hi);
+    } else {
+        *lo = 0.0f;
+        *hi = CUDART_INF_F;
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ void screen_fixed(const long long* ownI, int M, int s, const long long* pnI, float* lo,
+                                             float* hi)
+{
+    long long dx[3];
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const long long v = ownI[d * M + s];
+        ok &= v != kFixNone;
+        dx[d] = v - pnI[d];
+    }
+    if (ok) {
+        ss_bounds<DIM>(dx, lo, hi);
+    } else {
+        *lo = 0.0f;
+        *hi = CUDART_INF_F;
+    }
+}
+
+// minimum over the warp of non-negative doubles (or +Inf), on their bit patterns
+__device__ __forceinline__ double warp_min_nonneg(double v)
+{
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, b, o);
+        b = w < b ? w : b;
+    }
+    return __longlong_as_double((long long)b);
+}
+
+__device__ __forceinline__ float warp_min_nonneg(float v)
+{
+    return __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(v)));
+}
+
 // One cell of _inject_particles! / _inject_particles_phase! per warp, with a
 // pruned exact nearest-neighbour search. The cell's own particles sit in shared
 // memory; for each new particle the warp first finds the nearest of them, then
@@ -494,7 +642,8 @@ __device__ __forceinline__ double glob_ss(const Coords& X, int64_t b, const doub
 template <int DIM, bool PHASE>
 __device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* __restrict__ index,
                                    const InjectLists& Ls, const Args& A, const PhaseFields& PF, uint32_t call,
-                                   int64_t c, double* __restrict__ own, int lane, int* errs)
+                                   int64_t c, double* __restrict__ own, long long* __restrict__ ownI, int lane,
+                                   int* errs)
 {
     const int64_t nc = g.ncells;
     const int M = g.max_xcell;
@@ -509,11 +658,16 @@ __device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* _
         dq[d] = ldg(g.dxv[d] + I[d]) / 2.0;
     }
     uint64_t ownm = Ls.lm[c];
-    // the cell's own coordinates (own[d * M + s])
+    const int emax = fix_emax<DIM>(g);
+    // the cell's own coordinates (own[d * M + s]) and their fixed-point values
     for (int s = lane; s < M; s += 32) {
         const bool lv = (ownm >> s) & 1ull;
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) own[d * M + s] = lv ? X.c[d][c + nc * s] : CUDART_NAN;
+        for (int d = 0; d < DIM; ++d) {
+            const double x = lv ? X.c[d][c + nc * s] : CUDART_NAN;
+            own[d * M + s] = x;
+            ownI[d * M + s] = fix_double(x, emax);
+        }
     }
     // lane nb < NB holds neighbour cell nb: its index, occupancy and box
     int64_t nbc = -1;
@@ -532,6 +686,15 @@ __device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* _
                 bhi[d] = Ls.box[6 * nbc + 3 + d];
             }
         }
+    }
+    // the box in fixed point, widened by one unit each way (kFixNone: always examined)
+    long long bloI[3] = {0, 0, 0}, bhiI[3] = {0, 0, 0};
+    bool box_fixed = nbm != 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        bloI[d] = fix_float(blo[d], emax);
+        bhiI[d] = fix_float(bhi[d], emax);
+        box_fixed &= bloI[d] != kFixNone && bhiI[d] != kFixNone;
     }
     // the own cell's box grows with its new particles (read by later passes)
     float olo = 0.f, ohi = 0.f;
@@ -580,11 +743,19 @@ __device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* _
                 pn[d] = qc[d] + dq[d] * fma(0.95, r, 0.05);  // new_particle, injection.jl:411-417
             }
             const int64_t ai = c + nc * i;
+            long long pnI[3] = {0, 0, 0};
+            bool pn_fixed = true;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                pnI[d] = fix_double(pn[d], emax);
+                pn_fixed &= pnI[d] != kFixNone;
+            }
             if (lane == 0) {
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) {
                     X.c[d][ai] = pn[d];
                     own[d * M + i] = pn[d];
+                    ownI[d * M + i] = pnI[d];
                 }
                 index[ai] = 1;
             }
@@ -596,29 +767,40 @@ __device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* _
             ownm |= 1ull << i;
             __syncwarp();
             // The reference takes the first minimum of the rounded distance sqrt(ss) in its
-            // order. The search compares squared distances instead and keeps, per lane, the
-            // smallest (ss1, first o) and the smallest larger ss2: when no other candidate's
-            // squared distance lies within a relative 2^-50 of the minimum, no other
-            // candidate can round to the same distance (a larger root is ~2 ulps above) and
-            // the minimum's first occurrence is the answer; otherwise (in practice never)
-            // the rounded distances are compared again.
-            NearestTrack nt;
-            // (1) the own cell's particles
+            // order. (a) Screen: every candidate's squared distance is bounded on the
+            // integer pipe; only candidates whose lower bound is within a relative 2^-20 of
+            // the smallest upper bound can be the nearest (any other is farther by far more
+            // than the rounding of the reference's distances), and those few are (b)
+            // evaluated exactly in FP64. The exact search compares squared distances and
+            // keeps, per lane, the smallest (ss1, first o) and the smallest larger ss2:
+            // when no other candidate's squared distance lies within a relative 2^-50 of
+            // the minimum, no other candidate can round to the same distance (a larger root
+            // is ~2 ulps above) and the minimum's first occurrence is the answer; otherwise
+            // (in practice never) the rounded distances are compared again. Without a
+            // fixed-point value for the new particle every candidate is evaluated exactly.
+            ScreenTrack st;
+            // (a1) the own cell's particles
             for (int s = lane; s < M; s += 32)
-                if (s != i && ((ownm >> s) & 1ull)) nt.add(own_ss<DIM>(own, M, s, pn), CENTER * M + s);
-            const double ss_own = warp_min(nt.ss1);
-            // (2) neighbour cells whose box may hold a particle that close: skipped only when
-            // every particle of the box is farther by a relative 2^-40 in the squared distance,
-            // far above the rounding of the box, the gaps and the distances
+                if (s != i && ((ownm >> s) & 1ull)) {
+                    float lo, hi;
+                    screen_fixed<DIM>(ownI, M, s, pnI, &lo, &hi);
+                    st.add(lo, hi, CENTER * M + s);
+                }
+            const float h_own = pn_fixed ? warp_min_nonneg(st.hmin) : CUDART_INF_F;
+            // (a2) neighbour cells whose box may hold a particle that close
             bool look = false;
             if (nbm != 0) {
-                double lb2 = 0.0;
+                look = true;
+                if (box_fixed && pn_fixed && h_own < CUDART_INF_F) {
+                    float lb2 = 0.0f;  // lower bound of the squared distance to the box
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) {
-                    const double gap = fmax(0.0, fmax((double)blo[d] - pn[d], pn[d] - (double)bhi[d]));
-                    lb2 += gap * gap;
+                    for (int d = 0; d < DIM; ++d) {
+                        const long long gap = max(0ll, max(bloI[d] - pnI[d] - 2, pnI[d] - bhiI[d] - 2));
+                        const float gf = __ll2float_rd(gap);
+                        lb2 = __fmaf_rd(gf, gf, lb2);
+                    }
+                    look = !(lb2 > __fmul_ru(h_own, 1.0f + 0x1p-20f));
                 }
-                look = !(lb2 * (1.0 - 0x1p-40) > ss_own * (1.0 + 0x1p-40));
             }
             const uint32_t cells = __ballot_sync(0xffffffffu, look);
             for (uint32_t cl = cells; cl;) {
@@ -627,10 +809,59 @@ __device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* _
                 const uint64_t m = __shfl_sync(0xffffffffu, nbm, nb);
                 const int64_t cc = __shfl_sync(0xffffffffu, nbc, nb);
                 for (int s = lane; s < M; s += 32)
-                    if ((m >> s) & 1ull) nt.add(glob_ss<DIM>(X, cc + nc * s, pn), nb * M + s);
+                    if ((m >> s) & 1ull) {
+                        double q[3];
+#pragma unroll
+                        for (int d = 0; d < DIM; ++d) q[d] = X.c[d][cc + nc * s];
+                        float lo, hi;
+                        screen_double<DIM>(q, pnI, emax, &lo, &hi);
+                        st.add(lo, hi, nb * M + s);
+                    }
             }
-            const double ss_min = warp_min(nt.ss1);
-            const double ss_next = warp_min(nt.ss1 > ss_min ? nt.ss1 : nt.ss2);
+            const float thr = pn_fixed ? __fmul_ru(warp_min_nonneg(st.hmin), 1.0f + 0x1p-20f) : CUDART_INF_F;
+            // (b) exact squared distances of the candidates that pass the screen: each lane's
+            // best one, and all of a lane's candidates when a second one passes too
+            NearestTrack nt;
+            {
+                const int o = st.o1 >= 0 ? st.o1 : CENTER * M;
+                const int nb1 = o / M, s1 = o - nb1 * M;
+                const int64_t cc1 = __shfl_sync(0xffffffffu, nbc, nb1);
+                if (st.o1 >= 0 && st.lo1 <= thr) {
+                    if (nb1 == CENTER) {
+                        nt.add(own_ss<DIM>(own, M, s1, pn), o);
+                    } else {
+                        nt.add(glob_ss<DIM>(X, cc1 + nc * s1, pn), o);
+                    }
+                }
+            }
+            const bool again = st.lo2 <= thr;
+            if (__any_sync(0xffffffffu, again)) {
+                NearestTrack nt2;
+                for (int s = lane; s < M; s += 32)
+                    if (again && s != i && ((ownm >> s) & 1ull)) {
+                        float lo, hi;
+                        screen_fixed<DIM>(ownI, M, s, pnI, &lo, &hi);
+                        if (!pn_fixed || lo <= thr) nt2.add(own_ss<DIM>(own, M, s, pn), CENTER * M + s);
+                    }
+                for (uint32_t cl = cells; cl;) {
+                    const int nb = __ffs(cl) - 1;
+                    cl &= cl - 1;
+                    const uint64_t m = __shfl_sync(0xffffffffu, nbm, nb);
+                    const int64_t cc = __shfl_sync(0xffffffffu, nbc, nb);
+                    for (int s = lane; s < M; s += 32)
+                        if (again && ((m >> s) & 1ull)) {
+                            double q[3];
+#pragma unroll
+                            for (int d = 0; d < DIM; ++d) q[d] = X.c[d][cc + nc * s];
+                            float lo, hi;
+                            screen_double<DIM>(q, pnI, emax, &lo, &hi);
+                            if (!pn_fixed || lo <= thr) nt2.add(glob_ss<DIM>(X, cc + nc * s, pn), nb * M + s);
+                        }
+                }
+                if (again) nt = nt2;
+            }
+            const double ss_min = warp_min_nonneg(nt.ss1);
+            const double ss_next = warp_min_nonneg(nt.ss1 > ss_min ? nt.ss1 : nt.ss2);
             int win = __reduce_min_sync(0xffffffffu, (nt.ss1 == ss_min && ss_min < CUDART_INF) ? nt.o1 : 0x7fffffff);
             if (ss_min < CUDART_INF && ss_next <= ss_min * (1.0 + 0x1p-50)) {
                 // near tie: first candidate in order whose rounded distance is the minimum
@@ -692,13 +923,14 @@ __global__ void __launch_bounds__(256, 3)
     const int wib = threadIdx.x >> 5;
     const int M = g.max_xcell;
     double* own = (double*)smem_inject + (size_t)wib * DIM * M;
+    long long* ownI = (long long*)((double*)smem_inject + (size_t)(blockDim.x >> 5) * DIM * M) + (size_t)wib * DIM * M;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int count = Ls.counts[col];
     int errs = 0;
     for (int k = gw; k < count; k += nwarps) {
         const int64_t c = Ls.list[Ls.off[col] + k];
-        inject_cell_pruned<DIM, PHASE>(g, X, index, Ls, A, PF, call, c, own, lane, &errs);
+        inject_cell_pruned<DIM, PHASE>(g, X, index, Ls, A, PF, call, c, own, ownI, lane, &errs);
         __syncwarp();
     }
     raise_err(d_err, errs);
@@ -1123,7 +1355,7 @@ static cudaError_t inject_launch(jp_particles* P, double* const coords[3], uint8
     const unsigned nb = grid_blocks(nc);
     const int M = P->g.max_xcell;
     const int wpb = 8;  // warps per block of the pass kernels
-    const size_t smem = (size_t)wpb * N * M * sizeof(double);
+    const size_t smem = (size_t)wpb * N * M * (sizeof(double) + sizeof(long long));  // coordinates + fixed point
     // enough warps to keep every SM busy; each strides over its colour's list
     const unsigned nbp = (unsigned)(152 * 8);
     if (N == 2) {

@@ -128,3 +128,36 @@ def test_nan_and_infinite_positions(ni):
     Fo, Fg = pair.p2g(0)
     assert_bits_equal(Fo, Fg, "particle2grid! with NaN/Inf positions")
     _step_all(pair, g, V, 0.5 * W.cfl_dt(g, V))
+
+
+@pytest.mark.parametrize("ni", [(8, 8), (4, 4, 3)])
+def test_inject_nearest_ties_take_the_first_in_order(ni):
+    """Exact distance ties in the nearest-neighbour search of inject_particles!
+    (index_min_distance, injection.jl:330-393): in every other cell all 40 live
+    particles share one position (so slots s and s + 32, which the search gives
+    to the same lane, tie too) and carry distinct field values; the other cells
+    are empty and inject. The field a new particle copies shows which of the
+    tied particles won: the first in the reference's order, on both sides."""
+    g = _grid(ni)
+    N = len(ni)
+    pair = Pair(g, 24, 48, 12, nfields=1)
+    M, nc = pair.o.index.shape
+    rng = np.random.default_rng(11)
+    X = [np.full((M, nc), np.nan) for _ in range(N)]
+    index = np.zeros((M, nc), dtype=np.uint8)
+    for c in range(nc):
+        I = np.unravel_index(c, ni, order="F")
+        if sum(I) % 2:
+            continue
+        index[:40, c] = 1
+        for d in range(N):
+            X[d][:40, c] = (I[d] + rng.uniform(0.05, 0.95)) / ni[d]
+    _set_state(pair, X, index)
+    F = np.where(index.astype(bool), rng.random((M, nc)), np.nan)
+    pair.of[0][...] = F
+    pair.pf[0].data.copy_(torch.from_numpy(np.ascontiguousarray(F)))
+    pair.assert_same("before inject")
+    for call in range(2):
+        pair.inject()
+        pair.assert_same(f"inject {call}")
+    assert pair.p.index.numpy().sum() > index.sum()  # the empty cells were reseeded
