@@ -632,7 +632,10 @@ def run_adjoint(args):
         return float(np.median(ts)), out
 
     fwd = lambda: A.forward_field(p, method, V, dt, nsteps, T0)  # noqa: E731
+    kept = A.kept_segments(p, method, nsteps, k)
     grad = lambda: A.misfit_gradient(p, method, V, dt, nsteps, T0, target, checkpoint_every=k)  # noqa: E731
+    grad1 = lambda: A.misfit_gradient(p, method, V, dt, nsteps, T0, target, checkpoint_every=k,  # noqa: E731
+                                      record_segments=1)
     if args.form == "f32":  # the split-precision variant on the same run
         xi = jp.init_offsets(p)
         V32 = tuple(v.float() for v in V)
@@ -654,12 +657,16 @@ def run_adjoint(args):
 
         grad = lambda: A.misfit_gradient_f32(p, xi, method, V32, dt, nsteps, T0f, tgt32,  # noqa: E731
                                              checkpoint_every=k)
+        grad1 = lambda: A.misfit_gradient_f32(p, xi, method, V32, dt, nsteps, T0f, tgt32,  # noqa: E731
+                                              checkpoint_every=k, record_segments=1)
     for _ in range(max(1, min(args.warmup, 3))):
         fwd()
         grad()
     reps = max(1, min(args.steps, 5))
     t_fwd, _ = timed(fwd, reps)
     t_grad, (loss, gV, gT0) = timed(grad, reps)
+    grad1()
+    t_grad1, _ = timed(grad1, reps)
     rng = np.random.default_rng(17)
     checked = []
     h = 1e-6
@@ -698,6 +705,10 @@ def run_adjoint(args):
         "workload": DESC["C5"] if args.ni is None else DESC["C5"] + f" (resized to {args.ni})",
         "live_particles": live, "steps": nsteps, "checkpoint_every": k, "loss": loss,
         "forward_s": t_fwd, "forward_plus_gradient_s": t_grad, "gradient_cost_vs_forward": t_grad / t_fwd,
+        "records_kept_segments": kept if args.form == "f64" else None,
+        "records": "checkpoints every checkpoint_every steps; the records of the last records_kept_segments "
+                   "segments stay in HBM (budget 64 GB), every other segment is run again from its checkpoint",
+        "gradient_cost_vs_forward_one_segment_kept": t_grad1 / t_fwd,
         "forward_particle_steps_per_s": live * nsteps / t_fwd,
         "max_abs_gradient": gmax,
         "fd_check": fd_out,

@@ -246,30 +246,59 @@ def _recorded_step(p: Particles, method, V, dt, fields, inject: bool):
 
 
 def run_forward(particles: Particles, method, V, dt, nsteps: int, T: CellArray, inject: bool = True,
-                checkpoint_every: int = 0, record_last_segment: bool = False):
+                checkpoint_every: int = 0, record_last_segment: bool = False, record_segments: int = None):
     """Run nsteps of advection!/move_particles!(/inject_particles!) carrying
     the particle field T, in place; returns the checkpoints taken every
     ``checkpoint_every`` steps (the state before steps 0, k, 2k, ...) and,
-    with ``record_last_segment``, the records of the steps after the last
-    checkpoint (so the reverse sweep need not run them again)."""
+    with ``record_segments`` > 0 (``record_last_segment``: 1), the records of
+    the steps of that many trailing segments, oldest first (the reverse sweep
+    need not run those again)."""
+    K = record_segments if record_segments is not None else (1 if record_last_segment else 0)
     cps, recs = [], []
-    last = ((nsteps - 1) // checkpoint_every) * checkpoint_every if checkpoint_every and nsteps else nsteps
+    k = checkpoint_every
+    if K <= 0:
+        first = nsteps
+    elif k and nsteps:
+        first = max(0, ((nsteps - 1) // k - (K - 1)) * k)  # start of the K-th segment from the end
+    else:
+        first = 0
     for n in range(nsteps):
-        if checkpoint_every and n % checkpoint_every == 0:
+        if k and n % k == 0:
             cps.append(_save(particles))
-        if record_last_segment and n >= last:
+        if n >= first:
             recs.append(_recorded_step(particles, method, V, dt, (T,), inject))
         else:
             _step(particles, method, V, dt, (T,), inject)
-    return (cps, recs) if record_last_segment else cps
+    return (cps, recs) if K > 0 else cps
+
+
+def record_step_bytes(particles: Particles, method) -> int:
+    """Device bytes the reverse sweep keeps for one recorded step: the velocity
+    samples, the occupancy before the step, the move's slot map and the
+    injection's source ids."""
+    n = ctypes.c_uint64(0)
+    check(_native.load().jp_advection_record_bytes(particles.handle, method.code, ctypes.byref(n)))
+    return int(n.value) + particles.index.data.numel() * (1 + 4 + 8)
+
+
+def kept_segments(particles: Particles, method, nsteps: int, checkpoint_every: int,
+                  budget_bytes: int = 64 << 30) -> int:
+    """How many trailing segments' records fit in ``budget_bytes`` (and in half
+    of the device memory free now): at least 1, at most all segments."""
+    k = max(1, int(checkpoint_every))
+    nseg = max(1, -(-nsteps // k))
+    free = torch.cuda.mem_get_info()[0]
+    cap = min(int(budget_bytes), free // 2)
+    return int(max(1, min(nseg, cap // max(1, k * record_step_bytes(particles, method)))))
 
 
 def reverse_sweep(particles: Particles, method, V, dt, nsteps: int, checkpoints, k: int, gX, gT: CellArray,
                   inject: bool = True, last_records=None):
     """Back-propagate dL/dX (gX) and dL/dT (gT) of the state after nsteps to
-    the state before step 0, accumulating dL/dV (``last_records``: the last
-    segment's records from run_forward, if it kept them). The particles are
-    left in the state before step 0. Returns (gV, gX0, gT0)."""
+    the state before step 0, accumulating dL/dV (``last_records``: the records
+    run_forward kept of the last steps, if any; the segments they cover are not
+    run again). The particles are left in the state before step 0. Returns
+    (gV, gX0, gT0)."""
     _require_2d(particles)
     gV = tuple(grid_field(tuple(v.shape), 0.0) for v in V)
     lam = [c.data.clone() for c in gX]
@@ -277,11 +306,12 @@ def reverse_sweep(particles: Particles, method, V, dt, nsteps: int, checkpoints,
     tmp_x = [torch.empty_like(lam[0]) for _ in range(2)]
     tmp_t = torch.empty_like(gT)
     nseg = len(checkpoints)
+    first = nsteps - len(last_records) if last_records else nsteps  # the first step with a kept record
     for seg in reversed(range(nseg)):
         n0 = seg * k
         n1 = min(n0 + k, nsteps)
-        if seg == nseg - 1 and last_records:
-            recs = last_records
+        if n0 >= first:
+            recs = last_records[n0 - first:n1 - first]
         else:  # recompute the segment, recording positions and slot maps
             _restore(particles, checkpoints[seg])
             recs = [_recorded_step(particles, method, V, dt, (), inject) for _ in range(n0, n1)]
@@ -310,22 +340,27 @@ class _Idx:
 
 
 def misfit_gradient(particles: Particles, method, V, dt, nsteps: int, T0: CellArray, target: torch.Tensor,
-                    checkpoint_every: int = 10, inject: bool = True):
+                    checkpoint_every: int = 10, inject: bool = True, record_segments: int = None):
     """Loss 0.5 ||particle2grid(T after nsteps) - target||^2 and its gradients
     with respect to the velocity grids V and the initial particle field T0.
 
+    The forward run checkpoints the state every ``checkpoint_every`` steps; the
+    records of the last ``record_segments`` segments (default: as many as
+    kept_segments fits in its memory budget) stay in device memory, and the
+    reverse sweep runs every other segment again from its checkpoint.
     The particles and T0 are not modified (the run works on copies). Returns
     (loss, gV, gT0)."""
     _require_2d(particles)
     if not isinstance(method, AbstractAdvectionIntegrator):
         raise ArgumentError("method must be Euler(), RungeKutta2(α) or RungeKutta4()")
     k = max(1, int(checkpoint_every))
+    K = kept_segments(particles, method, nsteps, k) if record_segments is None else max(1, int(record_segments))
     start = _save(particles)
     T = CellArray(T0.data.clone(), T0.ni)
     try:
         with _deferred(particles):
             cps, last = run_forward(particles, method, V, dt, nsteps, T, inject, checkpoint_every=k,
-                                    record_last_segment=True)
+                                    record_segments=K)
             if not cps:
                 cps = [start]
             F = grid_field(_vertex_shape(particles), 0.0)
@@ -586,25 +621,33 @@ def _recorded_step_f32(p: Particles, xi, method, V, dt, fields, inject: bool):
 
 
 def misfit_gradient_f32(particles: Particles, xi, method, V, dt, nsteps: int, T0: CellArray, target: torch.Tensor,
-                        checkpoint_every: int = 10, inject: bool = True):
+                        checkpoint_every: int = 10, inject: bool = True, record_segments: int = None):
     """The FP32 (split-precision) variant of misfit_gradient: the run uses the
     FP32 forward path (offsets ``xi``, FP32 velocities V and particle field
-    T0, FP32 target); cotangents and the returned gradients are FP64. The
-    particles, xi and T0 are not modified. Returns (loss, gV, gT0)."""
+    T0, FP32 target); cotangents and the returned gradients are FP64. Records
+    of the last ``record_segments`` segments are kept as in misfit_gradient.
+    The particles, xi and T0 are not modified. Returns (loss, gV, gT0)."""
     from .split import advection_f32_, grid_field_f32, inject_particles_f32_, move_particles_f32_
     _require_2d(particles)
     k = max(1, int(checkpoint_every))
+    if record_segments is None:
+        # per recorded step: the FP32 offsets, the occupancy, the slot map and the int32 source ids
+        per_step = particles.index.data.numel() * (2 * 4 + 1 + 4 + 4)
+        nseg = max(1, -(-nsteps // k))
+        cap = min(64 << 30, torch.cuda.mem_get_info()[0] // 2)
+        record_segments = max(1, min(nseg, cap // max(1, k * per_step)))
+    K = max(1, int(record_segments))
     start = _save_f32(particles, xi)
     T = CellArray(T0.data.clone(), T0.ni)
     shape = _vertex_shape(particles)
     try:
         with _deferred(particles):
             cps, last = [], []
-            last_seg = ((nsteps - 1) // k) * k if nsteps else 0
+            first = max(0, ((nsteps - 1) // k - (K - 1)) * k) if nsteps else 0  # first step recorded
             for n in range(nsteps):
                 if n % k == 0:
                     cps.append(_save_f32(particles, xi))
-                if n >= last_seg:
+                if n >= first:
                     last.append(_recorded_step_f32(particles, xi, method, V, dt, (T,), inject))
                 else:
                     advection_f32_(particles, xi, method, V, dt)
@@ -630,8 +673,8 @@ def misfit_gradient_f32(particles: Particles, xi, method, V, dt, nsteps: int, T0
             for seg in reversed(range(nseg)):
                 n0 = seg * k
                 n1 = min(n0 + k, nsteps)
-                if seg == nseg - 1 and last:
-                    recs = last
+                if last and n0 >= first:
+                    recs = last[n0 - first:n1 - first]
                 else:
                     _restore_f32(particles, xi, cps[seg])
                     recs = [_recorded_step_f32(particles, xi, method, V, dt, (), inject) for _ in range(n0, n1)]
@@ -651,6 +694,7 @@ def misfit_gradient_f32(particles: Particles, xi, method, V, dt, nsteps: int, T0
 
 __all__ = ["particle2grid_with_weights_", "particle2grid_vjp_", "grid2particle_vjp_", "advection_vjp_",
            "move_permutation", "permute_vjp_", "slot_ids", "inject_vjp_", "run_forward", "reverse_sweep",
+           "record_step_bytes", "kept_segments",
            "misfit", "misfit_gradient", "misfit_value", "forward_field", "misfit_difference", "PICMisfit", "Grid2Particle", "Particle2Grid",
            "AdvectionStep", "particle2grid_f32_with_weights_", "particle2grid_vjp_f32_", "advection_vjp_f32_",
            "slot_ids_i32", "inject_vjp_i32_", "misfit_gradient_f32"]

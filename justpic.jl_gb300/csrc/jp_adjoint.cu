@@ -166,19 +166,28 @@ __global__ void __launch_bounds__(kThreads)
     const int64_t cx = c % g.n[0], cy = c / g.n[0];
     uint64_t m = 0;
     int errs = 0;
-    for (int s = 0; s < g.max_xcell; ++s) {
-        const int64_t a = c + nc * s;
-        const IdT id = ids[a];
-        if (id_other(id, a)) {
-            const int64_t src = id_slot(id, ns);
-            const int64_t sc = src % nc;
-            const int64_t sx = sc % g.n[0], sy = sc / g.n[0];
-            if (src >= ns || sx < cx - kInjectReach || sx > cx + kInjectReach || sy < cy - kInjectReach ||
-                sy > cy + kInjectReach) {
-                errs |= kErrAdjointWindow;
-            } else {
-                m |= 1ull << s;
-                atomicOr(srcflag + sc, 1u);
+    constexpr int U = 4;  // slots whose ids are loaded together (the loop is bound by load latency)
+    for (int s0 = 0; s0 < g.max_xcell; s0 += U) {
+        IdT idl[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) idl[u] = s0 + u < g.max_xcell ? ids[c + nc * (s0 + u)] : ids[c];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int s = s0 + u;
+            if (s >= g.max_xcell) break;
+            const int64_t a = c + nc * s;
+            const IdT id = idl[u];
+            if (id_other(id, a)) {
+                const int64_t src = id_slot(id, ns);
+                const int64_t sc = src % nc;
+                const int64_t sx = sc % g.n[0], sy = sc / g.n[0];
+                if (src >= ns || sx < cx - kInjectReach || sx > cx + kInjectReach || sy < cy - kInjectReach ||
+                    sy > cy + kInjectReach) {
+                    errs |= kErrAdjointWindow;
+                } else {
+                    m |= 1ull << s;
+                    atomicOr(srcflag + sc, 1u);
+                }
             }
         }
     }
@@ -198,18 +207,43 @@ __global__ void __launch_bounds__(kThreads)
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncells) return;
     const int64_t nc = g.ncells;
-    for (int s = 0; s < g.max_xcell; ++s) {
-        const int64_t a = c + nc * s;
-        const bool kept = id_self(ids[a], a);
-        for (int k = 0; k < P.n; ++k) P.pre[k][a] = kept ? P.post[k][a] : 0.0;
+    const int M = g.max_xcell;
+    // U slots at a time: their ids, then per array their values, are loaded together
+    // (the loop is bound by load latency, not by bandwidth)
+    constexpr int U = 4;
+    for (int s0 = 0; s0 < M; s0 += U) {
+        bool kept[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t a = c + nc * (s0 + u);
+            kept[u] = s0 + u < M && id_self(ids[s0 + u < M ? a : c], a);
+        }
+        for (int k = 0; k < P.n; ++k) {
+            double v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) v[u] = kept[u] ? P.post[k][c + nc * (s0 + u)] : 0.0;
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (s0 + u < M) P.pre[k][c + nc * (s0 + u)] = v[u];
+        }
     }
     if (!copies || !srcflag[c]) return;
     const int64_t ns = nc * g.max_xcell;
     const int64_t cx = c % g.n[0], cy = c / g.n[0];
-    for (int64_t y = max(cy - kInjectReach, (int64_t)0); y <= min(cy + kInjectReach, g.n[1] - 1); ++y)
-        for (int64_t x = max(cx - kInjectReach, (int64_t)0); x <= min(cx + kInjectReach, g.n[0] - 1); ++x) {
-            const int64_t w = x + g.n[0] * y;
-            uint64_t m = inj[w];
+    constexpr int RW = 2 * kInjectReach + 1;  // window width
+    const int64_t x0 = cx - kInjectReach;
+    for (int64_t y = max(cy - kInjectReach, (int64_t)0); y <= min(cy + kInjectReach, g.n[1] - 1); ++y) {
+        // the injected-slot masks of one window row, loaded together
+        uint64_t row[RW];
+#pragma unroll
+        for (int j = 0; j < RW; ++j) {
+            const int64_t x = x0 + j;
+            row[j] = (x >= 0 && x < g.n[0]) ? inj[x + g.n[0] * y] : 0ull;
+        }
+#pragma unroll
+        for (int j = 0; j < RW; ++j) {
+            const int64_t w = (x0 + j) + g.n[0] * y;
+            uint64_t m = row[j];
             while (m) {
                 const int s = __ffsll((long long)m) - 1;
                 m &= m - 1;
@@ -220,6 +254,7 @@ __global__ void __launch_bounds__(kThreads)
                     if ((copies >> k) & 1u) P.pre[k][src] += P.post[k][b];
             }
         }
+    }
 }
 
 // --------------------------------------------------------- advection step

@@ -422,6 +422,14 @@ def test_misfit_gradient_is_reproducible_and_checkpoint_independent():
     for a, b, c in zip(gV1 + (gT1.data,), gV2 + (gT2.data,), gV3 + (gT3.data,)):
         assert torch.equal(a, b), "gradients differ between two identical runs"
         assert torch.equal(a, c), "gradients depend on the checkpoint spacing"
+    # how many trailing segments keep their records (the others run again) changes nothing
+    assert A.kept_segments(p, method, nsteps, 4) == 3  # all of them, at this size
+    for K in (1, 2):
+        lk, gVk, gTk = A.misfit_gradient(p, method, V, dt, nsteps, T0, target, checkpoint_every=4,
+                                         record_segments=K)
+        assert lk == l1
+        for a, b in zip(gV1 + (gT1.data,), gVk + (gTk.data,)):
+            assert torch.equal(a, b), f"gradients depend on the segments kept ({K})"
 
 
 def test_pic_misfit_autograd():
