@@ -263,9 +263,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             S.m.code[a] = code;
         }
     };
-    // Two particles per lane at a time: the loads of both are in flight
-    // before either is classified (the kernel is bound by load latency).
-    constexpr int B = 2;
+    // Four particles per lane at a time: the loads of all are in flight
+    // before any is classified (the kernel is bound by load latency; four
+    // measured faster than two here, while the FP64 kernel keeps two).
+    constexpr int B = 4;
     for (int k0 = lane; k0 < K; k0 += 32 * B) {
         int sl[B], ll[B];
         int64_t al[B];
