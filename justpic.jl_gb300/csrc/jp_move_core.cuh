@@ -264,9 +264,12 @@ static __global__ void __launch_bounds__(kAllocThreads)
             Lc &= ~bit;
             continue;
         }
+        // (a slot sits in one per-target mask; the clamp only keeps the shared-memory
+        // index in range should the masks ever be inconsistent)
         const int code = refill ? CENTER
-                                : (((P0 & bit) ? 1 : 0) | ((P1 & bit) ? 2 : 0) | ((P2 & bit) ? 4 : 0) |
-                                   ((P3 & bit) ? 8 : 0));
+                                : min(((P0 & bit) ? 1 : 0) | ((P1 & bit) ? 2 : 0) | ((P2 & bit) ? 4 : 0) |
+                                          ((P3 & bit) ? 8 : 0),
+                                      8);
         const bool unstable = refill || (unst & bit) != 0;
         // remove the particle from its slot (move_safe.jl:110-112)
         Lc &= ~bit;
