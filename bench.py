@@ -90,7 +90,7 @@ DRAM_BYTES_PER_PARTICLE_2D_F64 = {
     "particle2grid!": 673.6e6 / 5.790e6,
     "advection!": 306.2e6 / 5.790e6,
     "grid2particle!": 309.5e6 / 5.790e6,
-    "move_particles!": 1555.2e6 / 5.790e6,
+    "move_particles!": (444.8e6 + 9 * 14.8e6 + 923.5e6) / 5.790e6,  # classify + 9 colour passes + apply
     "inject_particles!": 333.1e6 / 5.790e6,
 }
 
