@@ -83,7 +83,8 @@ def algorithmic_bytes(op, N, nf, m, slots_per_live, grid_bytes_per_live, field_b
 
 # DRAM bytes per live particle of each call, FP64 form, 2D, one particle field:
 # dram__bytes_read.sum + dram__bytes_write.sum of the call's kernels in one ncu
-# capture of a 512x512-cell C2 case (5.79M particles; profiles/c2_fp64_kernels_512.md),
+# capture of a 512x512-cell C2 case (5.79M particles; profiles/c2_fp64_kernels_512.md,
+# the move's kernels profiles/move_kernels_512.md),
 # divided by its particle count. Traffic grows with the particle count, so the
 # bench scales it by the live particles of its own run.
 DRAM_BYTES_PER_PARTICLE_2D_F64 = {
