@@ -193,8 +193,9 @@ static __global__ void __launch_bounds__(kAllocThreads)
     move_allocate_2d(DevGrid g, MoveView S, int o0, int o1, int64_t m0, int64_t m1)
 {
     constexpr int CENTER = 4;
-    // [neighbour][thread]: a warp's 64-bit accesses are conflict-free whatever neighbour each lane picks
-    __shared__ uint64_t sL[9][kAllocThreads], sR[9][kAllocThreads], sU[9][kAllocThreads];
+    // [neighbour][thread]: a warp's 64-bit accesses are conflict-free whatever neighbour each lane picks.
+    // A neighbour's R mask is not read during the walk: it is formed at the write-back (below).
+    __shared__ uint64_t sL[9][kAllocThreads], sU[9][kAllocThreads];
     const int tid = threadIdx.x;
     const int64_t t = (int64_t)blockIdx.x * kAllocThreads + tid;
     if (t >= m0 * m1) return;
@@ -217,7 +218,7 @@ static __global__ void __launch_bounds__(kAllocThreads)
     const uint64_t U0 = S.U(sc);
     if (Mv == 0 && U0 == 0) return;
     uint64_t Lc = S.L(sc), Rc = S.R(sc), Uc = U0;
-    uint64_t nl[9], nr[9], nu[9], tm[10];
+    uint64_t nl[9], nu[9], tm[10];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         if (k == CENTER) continue;
@@ -225,7 +226,6 @@ static __global__ void __launch_bounds__(kAllocThreads)
         const bool in = jx >= 0 && jy >= 0 && jx < nx && jy < g.n[1];
         const int64_t jc = jx + nx * jy;
         nl[k] = in ? S.L(jc) : 0;
-        nr[k] = in ? S.R(jc) : 0;
         nu[k] = in ? S.U(jc) : 0;
     }
 #pragma unroll
@@ -234,7 +234,6 @@ static __global__ void __launch_bounds__(kAllocThreads)
     for (int k = 0; k < 9; ++k) {
         if (k == CENTER) continue;
         sL[k][tid] = nl[k];
-        sR[k][tid] = nr[k];
         sU[k][tid] = nu[k];
     }
     // bit j of a slot's destination code in plane j; movers with no destination leave the domain
@@ -291,9 +290,10 @@ static __global__ void __launch_bounds__(kAllocThreads)
                 Uc &= ~fb;
             }
         } else {
+            // a free slot has its R and U bits clear (U within R within L): a stable
+            // particle leaves U as it is, and R gains the slot at the write-back
             sL[code][tid] = tL | fb;
-            sR[code][tid] |= fb;
-            sU[code][tid] = unstable ? (sU[code][tid] | fb) : (sU[code][tid] & ~fb);
+            if (unstable) sU[code][tid] |= fb;
             touched |= 1u << code;
         }
         const int s = __ffsll((long long)bit) - 1, f = __ffsll((long long)fb) - 1;
@@ -308,11 +308,15 @@ static __global__ void __launch_bounds__(kAllocThreads)
     S.L(sc) = Lc;
     S.R(sc) = Rc;
     S.U(sc) = Uc;
-    for (uint32_t m = touched; m; m &= m - 1) {
-        const int k = __ffs(m) - 1;
+    // a neighbour only gained slots in this walk: R = R before | the slots L gained
+    // (its R and L in memory are still those before the walk: this thread alone writes them)
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        if (k == CENTER || !((touched >> k) & 1u)) continue;
         const int64_t jc = sc + (k % 3 - 1) + nx * (k / 3 - 1);
-        S.L(jc) = sL[k][tid];
-        S.R(jc) = sR[k][tid];
+        const uint64_t Lf = sL[k][tid];
+        S.R(jc) = S.R(jc) | (Lf & ~nl[k]);
+        S.L(jc) = Lf;
         S.U(jc) = sU[k][tid];
     }
 }
