@@ -67,7 +67,11 @@ inline size_t move_shadow_offset(const DevGrid& g)
 // disjoint, so every mask touched here belongs to exactly one thread. The
 // destination codes and the masks of every neighbour the walk will touch are
 // loaded up front (independent loads), the walk then runs on thread-local
-// copies, and the touched masks are written back at the end.
+// copies, and the touched masks are written back at the end. As in the 2D
+// pass below: the slots still to visit are a mask; the centre cell's masks
+// stay in registers; a neighbour's R mask is formed at the write-back (a free
+// slot has its R and U bits clear, so R gains exactly the slots L gained) and
+// its U mask changes only for unstable insertions.
 template <int DIM>
 __global__ void __launch_bounds__(kAllocThreads)
     move_allocate(DevGrid g, MoveView S, int o0, int o1, int o2, int64_t m0, int64_t m1, int64_t m2)
@@ -88,79 +92,16 @@ __global__ void __launch_bounds__(kAllocThreads)
     const uint64_t Mv = S.M(sc);
     const uint64_t U0 = S.U(sc);
     if (Mv == 0 && U0 == 0) return;
-    uint64_t nL[NB], nR[NB], nU[NB];
+    uint64_t nL[NB], nU[NB];
     uint8_t codes[64];
-    nL[CENTER] = S.L(sc);
-    nR[CENTER] = S.R(sc);
-    nU[CENTER] = U0;
-    uint32_t touched = 1u << CENTER;
+    uint64_t Lc = S.L(sc), Rc = S.R(sc), Uc = U0;
+    uint32_t touched = 0;  // neighbours (not the centre) the walk may change
     // codes of the original movers (slots not refilled by an earlier pass)
-    uint64_t orig_movers = Mv & ~nR[CENTER];
-    for (uint64_t m = orig_movers; m; m &= m - 1) {
+    for (uint64_t m = Mv & ~Rc; m; m &= m - 1) {
         const int s = __ffsll((long long)m) - 1;
         const uint8_t cb = S.code[sc + nc * s];
         codes[s] = cb;
-        if (cb != kCodeExit) touched |= 1u << (cb & 0x1F);
-    }
-    for (uint32_t m = touched & ~(1u << CENTER); m; m &= m - 1) {
-        const int nb = __ffs(m) - 1;
-        int off[3];
-        nb_offset<DIM>(nb, off);
-        const int64_t J[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
-        const int64_t jc = cell_linear<DIM>(g, J);
-        nL[nb] = S.L(jc);
-        nR[nb] = S.R(jc);
-        nU[nb] = S.U(jc);
-    }
-    const int nslot = g.max_xcell;
-    const uint64_t valid = nslot == 64 ? ~0ull : ((1ull << nslot) - 1);
-    int sp = 0;  // starting_point (move_safe.jl:83)
-    int cur = 0;
-    while (cur < nslot) {
-        const uint64_t L = nL[CENTER], R = nR[CENTER], U = nU[CENTER];
-        const uint64_t cand = L & ((Mv & ~R) | (R & U)) & (~0ull << cur);
-        if (!cand) break;
-        const int s = __ffsll((long long)cand) - 1;
-        cur = s + 1;
-        const uint64_t bit = 1ull << s;
-        int code;
-        bool unstable;
-        const bool from_refill = (R & bit) != 0;
-        uint16_t tag = 0;
-        if (from_refill) {
-            code = CENTER;
-            unstable = true;
-            tag = S.orig[sc + nc * s];
-        } else {
-            const uint8_t cb = codes[s];
-            if (cb == kCodeExit) {  // left the domain (or moved too far): cleared
-                nL[CENTER] = L & ~bit;
-                continue;
-            }
-            code = cb & 0x1F;
-            unstable = (cb & kCodeUnstable) != 0;
-            int off[3];
-            nb_offset<DIM>(code, off);
-            const int back[3] = {-off[0], -off[1], -off[2]};
-            tag = (uint16_t)(nb_code<DIM>(back) | (s << 5));
-        }
-        // remove the particle from its slot (move_safe.jl:110-112)
-        nL[CENTER] = L & ~bit;
-        nR[CENTER] = R & ~bit;
-        nU[CENTER] = U & ~bit;
-        // find_free_memory(starting_point, ...) (move_safe.jl:192-197)
-        const uint64_t freem = ~nL[code] & valid & (~0ull << sp);
-        if (!freem) continue;  // dropped: no free slot at or after starting_point
-        const int f = __ffsll((long long)freem) - 1;
-        sp = f;
-        const uint64_t fb = 1ull << f;
-        nL[code] |= fb;
-        nR[code] |= fb;
-        nU[code] = unstable ? (nU[code] | fb) : (nU[code] & ~fb);
-        int off[3];
-        nb_offset<DIM>(code, off);
-        const int64_t T[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
-        S.orig[cell_linear<DIM>(g, T) + nc * f] = tag;
+        if (cb != kCodeExit && (cb & 0x1F) != CENTER) touched |= 1u << (cb & 0x1F);
     }
     for (uint32_t m = touched; m; m &= m - 1) {
         const int nb = __ffs(m) - 1;
@@ -168,8 +109,81 @@ __global__ void __launch_bounds__(kAllocThreads)
         nb_offset<DIM>(nb, off);
         const int64_t J[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
         const int64_t jc = cell_linear<DIM>(g, J);
+        nL[nb] = S.L(jc);
+        nU[nb] = S.U(jc);
+    }
+    const int nslot = g.max_xcell;
+    const uint64_t valid = nslot == 64 ? ~0ull : ((1ull << nslot) - 1);
+    // the reference's candidates: live slots that are original movers, or refilled
+    // by an earlier pass and not strictly inside; a particle put back into the
+    // centre cell ahead of the walk is added
+    uint64_t todo = Lc & ((Mv & ~Rc) | (Rc & Uc));
+    uint64_t from_sp = valid;  // slots at or after starting_point (move_safe.jl:83)
+    while (todo) {
+        const uint64_t bit = todo & (0ull - todo);
+        todo ^= bit;
+        const int s = __ffsll((long long)bit) - 1;
+        int code;
+        bool unstable;
+        uint16_t tag;
+        if (Rc & bit) {  // refilled by an earlier pass and not strictly inside: walked again
+            code = CENTER;
+            unstable = true;
+            tag = S.orig[sc + nc * s];
+        } else {
+            const uint8_t cb = codes[s];
+            if (cb == kCodeExit) {  // left the domain (or moved too far): cleared
+                Lc &= ~bit;
+                continue;
+            }
+            code = min((int)(cb & 0x1F), NB - 1);
+            unstable = (cb & kCodeUnstable) != 0;
+            int off[3];
+            nb_offset<DIM>(code, off);
+            const int back[3] = {-off[0], -off[1], -off[2]};
+            tag = (uint16_t)(nb_code<DIM>(back) | (s << 5));
+        }
+        // remove the particle from its slot (move_safe.jl:110-112)
+        Lc &= ~bit;
+        Rc &= ~bit;
+        Uc &= ~bit;
+        // find_free_memory(starting_point, ...) (move_safe.jl:192-197)
+        const uint64_t tL = code == CENTER ? Lc : nL[code];
+        const uint64_t freem = ~tL & from_sp;
+        if (!freem) continue;  // dropped: no free slot at or after starting_point
+        const uint64_t fb = freem & (0ull - freem);
+        from_sp = valid & ~(fb - 1);
+        if (code == CENTER) {
+            Lc |= fb;
+            Rc |= fb;
+            if (unstable) {
+                Uc |= fb;
+                if (fb > bit) todo |= fb;  // ahead of the walk: visited again
+            } else {
+                Uc &= ~fb;
+            }
+        } else {
+            nL[code] = tL | fb;
+            if (unstable) nU[code] |= fb;
+        }
+        const int f = __ffsll((long long)fb) - 1;
+        int off[3];
+        nb_offset<DIM>(code, off);
+        const int64_t T[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
+        S.orig[cell_linear<DIM>(g, T) + nc * f] = tag;
+    }
+    S.L(sc) = Lc;
+    S.R(sc) = Rc;
+    S.U(sc) = Uc;
+    // a neighbour only gained slots in this walk: R = R before | the slots L gained
+    for (uint32_t m = touched; m; m &= m - 1) {
+        const int nb = __ffs(m) - 1;
+        int off[3];
+        nb_offset<DIM>(nb, off);
+        const int64_t J[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
+        const int64_t jc = cell_linear<DIM>(g, J);
+        S.R(jc) = S.R(jc) | (nL[nb] & ~S.L(jc));
         S.L(jc) = nL[nb];
-        S.R(jc) = nR[nb];
         S.U(jc) = nU[nb];
     }
 }
