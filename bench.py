@@ -660,6 +660,7 @@ def run_adjoint(args):
                                              checkpoint_every=k)
         grad1 = lambda: A.misfit_gradient_f32(p, xi, method, V32, dt, nsteps, T0f, tgt32,  # noqa: E731
                                               checkpoint_every=k, record_segments=1)
+        kept = A.kept_segments_f32(p, nsteps, k)
     for _ in range(max(1, min(args.warmup, 3))):
         fwd()
         grad()
@@ -706,7 +707,7 @@ def run_adjoint(args):
         "workload": DESC["C5"] if args.ni is None else DESC["C5"] + f" (resized to {args.ni})",
         "live_particles": live, "steps": nsteps, "checkpoint_every": k, "loss": loss,
         "forward_s": t_fwd, "forward_plus_gradient_s": t_grad, "gradient_cost_vs_forward": t_grad / t_fwd,
-        "records_kept_segments": kept if args.form == "f64" else None,
+        "records_kept_segments": kept,
         "records": "checkpoints every checkpoint_every steps; the records of the last records_kept_segments "
                    "segments stay in HBM (budget 64 GB), every other segment is run again from its checkpoint",
         "gradient_cost_vs_forward_one_segment_kept": t_grad1 / t_fwd,

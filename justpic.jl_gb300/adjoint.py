@@ -620,6 +620,16 @@ def _recorded_step_f32(p: Particles, xi, method, V, dt, fields, inject: bool):
     return X, idx, dest, ids
 
 
+def kept_segments_f32(particles: Particles, nsteps: int, checkpoint_every: int, budget_bytes: int = 64 << 30) -> int:
+    """kept_segments for misfit_gradient_f32, whose recorded step keeps the
+    FP32 offsets, the occupancy, the slot map and the int32 source ids."""
+    k = max(1, int(checkpoint_every))
+    per_step = particles.index.data.numel() * (2 * 4 + 1 + 4 + 4)
+    nseg = max(1, -(-nsteps // k))
+    cap = min(int(budget_bytes), torch.cuda.mem_get_info()[0] // 2)
+    return int(max(1, min(nseg, cap // max(1, k * per_step))))
+
+
 def misfit_gradient_f32(particles: Particles, xi, method, V, dt, nsteps: int, T0: CellArray, target: torch.Tensor,
                         checkpoint_every: int = 10, inject: bool = True, record_segments: int = None):
     """The FP32 (split-precision) variant of misfit_gradient: the run uses the
@@ -630,13 +640,7 @@ def misfit_gradient_f32(particles: Particles, xi, method, V, dt, nsteps: int, T0
     from .split import advection_f32_, grid_field_f32, inject_particles_f32_, move_particles_f32_
     _require_2d(particles)
     k = max(1, int(checkpoint_every))
-    if record_segments is None:
-        # per recorded step: the FP32 offsets, the occupancy, the slot map and the int32 source ids
-        per_step = particles.index.data.numel() * (2 * 4 + 1 + 4 + 4)
-        nseg = max(1, -(-nsteps // k))
-        cap = min(64 << 30, torch.cuda.mem_get_info()[0] // 2)
-        record_segments = max(1, min(nseg, cap // max(1, k * per_step)))
-    K = max(1, int(record_segments))
+    K = kept_segments_f32(particles, nsteps, k) if record_segments is None else max(1, int(record_segments))
     start = _save_f32(particles, xi)
     T = CellArray(T0.data.clone(), T0.ni)
     shape = _vertex_shape(particles)
@@ -694,7 +698,7 @@ def misfit_gradient_f32(particles: Particles, xi, method, V, dt, nsteps: int, T0
 
 __all__ = ["particle2grid_with_weights_", "particle2grid_vjp_", "grid2particle_vjp_", "advection_vjp_",
            "move_permutation", "permute_vjp_", "slot_ids", "inject_vjp_", "run_forward", "reverse_sweep",
-           "record_step_bytes", "kept_segments",
+           "record_step_bytes", "kept_segments", "kept_segments_f32",
            "misfit", "misfit_gradient", "misfit_value", "forward_field", "misfit_difference", "PICMisfit", "Grid2Particle", "Particle2Grid",
            "AdvectionStep", "particle2grid_f32_with_weights_", "particle2grid_vjp_f32_", "advection_vjp_f32_",
            "slot_ids_i32", "inject_vjp_i32_", "misfit_gradient_f32"]
