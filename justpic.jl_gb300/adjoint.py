@@ -256,12 +256,7 @@ def run_forward(particles: Particles, method, V, dt, nsteps: int, T: CellArray, 
     K = record_segments if record_segments is not None else (1 if record_last_segment else 0)
     cps, recs = [], []
     k = checkpoint_every
-    if K <= 0:
-        first = nsteps
-    elif k and nsteps:
-        first = max(0, ((nsteps - 1) // k - (K - 1)) * k)  # start of the K-th segment from the end
-    else:
-        first = 0
+    first = first_recorded_step(nsteps, k, K)
     for n in range(nsteps):
         if k and n % k == 0:
             cps.append(_save(particles))
@@ -270,6 +265,19 @@ def run_forward(particles: Particles, method, V, dt, nsteps: int, T: CellArray, 
         else:
             _step(particles, method, V, dt, (T,), inject)
     return (cps, recs) if K > 0 else cps
+
+
+def first_recorded_step(nsteps: int, checkpoint_every: int, segments: int) -> int:
+    """The first step whose record is kept when the records of the last
+    ``segments`` segments of ``checkpoint_every`` steps are kept (the start of
+    the segments-th segment from the end; nsteps when none are kept, 0 without
+    checkpoints)."""
+    if segments <= 0 or nsteps <= 0:
+        return max(0, nsteps)
+    if not checkpoint_every:
+        return 0
+    k = int(checkpoint_every)
+    return max(0, ((nsteps - 1) // k - (segments - 1)) * k)
 
 
 def record_step_bytes(particles: Particles, method) -> int:
@@ -647,7 +655,7 @@ def misfit_gradient_f32(particles: Particles, xi, method, V, dt, nsteps: int, T0
     try:
         with _deferred(particles):
             cps, last = [], []
-            first = max(0, ((nsteps - 1) // k - (K - 1)) * k) if nsteps else 0  # first step recorded
+            first = first_recorded_step(nsteps, k, K)
             for n in range(nsteps):
                 if n % k == 0:
                     cps.append(_save_f32(particles, xi))
@@ -698,7 +706,7 @@ def misfit_gradient_f32(particles: Particles, xi, method, V, dt, nsteps: int, T0
 
 __all__ = ["particle2grid_with_weights_", "particle2grid_vjp_", "grid2particle_vjp_", "advection_vjp_",
            "move_permutation", "permute_vjp_", "slot_ids", "inject_vjp_", "run_forward", "reverse_sweep",
-           "record_step_bytes", "kept_segments", "kept_segments_f32",
+           "record_step_bytes", "kept_segments", "kept_segments_f32", "first_recorded_step",
            "misfit", "misfit_gradient", "misfit_value", "forward_field", "misfit_difference", "PICMisfit", "Grid2Particle", "Particle2Grid",
            "AdvectionStep", "particle2grid_f32_with_weights_", "particle2grid_vjp_f32_", "advection_vjp_f32_",
            "slot_ids_i32", "inject_vjp_i32_", "misfit_gradient_f32"]
