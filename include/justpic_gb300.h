@@ -139,11 +139,12 @@ int jp_move_particles(jp_particles* p, double* const coords[3], uint8_t* index,
 
 /*
  * move_particles! for callers that cannot allocate device memory. It has no
- * counterpart in the reference; it exists for code that must not call
- * cudaMalloc while it runs: a step recorded into a CUDA graph under stream
- * capture (where allocation calls are refused), a time-stepping loop that
- * cannot afford the device-wide synchronisation an allocation may cause, or an
- * application whose device memory is all handed out by its own pool.
+ * counterpart in the reference. Some host programs may not call cudaMalloc
+ * once their time loop runs: an application whose device memory is all
+ * handed out up front by its own pool or by a framework that owns the GPU, or
+ * a loop that cannot absorb the device-wide synchronisation an allocation may
+ * cause. jp_move_particles allocates its scratch on a container's first move,
+ * so those callers use this entry point instead.
  *
  * Same arguments and results as jp_move_particles, but the scratch memory the
  * relocation needs (64-bit occupancy masks per cell, a code, an origin tag and
@@ -153,11 +154,14 @@ int jp_move_particles(jp_particles* p, double* const coords[3], uint8_t* index,
  * (120 bytes per cell in 2D, 40 in 3D, rounded up to a multiple of 256, plus (8*s+3) bytes
  * per slot with s = ndim+nargs, 4 when that is 3) is rejected with
  * JP_ERR_INVALID_ARGUMENT and a message naming the sizes; use
- * jp_move_particles there. The first call on a device looks up the array's
- * device address (and may load the library's device code), so make that first
- * call before any stream capture. All calls share the array and leave their
- * contents in it; nothing needs to start at zero. Calls whose kernels overlap
- * on the GPU (e.g. on two streams) race on the array.
+ * jp_move_particles there. Containers of more than 64 slots per cell need no
+ * scratch (they run the per-cell schedule) and are never rejected for size.
+ * The first call on a device looks up the array's device address (and may
+ * load the library's device code), so make that first call before any stream
+ * capture. All calls share the array and leave their contents in it; nothing
+ * needs to start at zero. Calls whose kernels overlap on the GPU (e.g. on two
+ * streams) race on the array. The call does not touch the container's own
+ * move record, so a jp_move_permutation after it is refused.
  */
 #define JP_NOALLOC_SCRATCH_BYTES (32u << 20)
 int jp_move_particles_noalloc(jp_particles* p, double* const coords[3], uint8_t* index,

@@ -366,7 +366,9 @@ int jp_move_particles_noalloc(jp_particles* P, double* const coords[3], uint8_t*
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles_noalloc: bad particle field list");
     for (int k = 0; k < nargs; ++k)
         if (!args[k]) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_particles_noalloc: null field");
-    const size_t need = jp::move_scratch_bytes(P->g, jp::shadow_stride(P->g.ndim + nargs));
+    // cells of more than 64 slots run the per-cell schedule, which needs no scratch
+    const size_t need =
+        P->g.max_xcell > 64 ? 0 : jp::move_scratch_bytes(P->g, jp::shadow_stride(P->g.ndim + nargs));
     if (need > jp::kNoAllocScratchBytes)
         return fail(JP_ERR_INVALID_ARGUMENT,
                     "jp_move_particles_noalloc: this container needs " + std::to_string(need) +
@@ -519,7 +521,10 @@ int jp_move_permutation(jp_particles* P, int32_t* dest)
 {
     JP_REQUIRE_NARROW(P, "jp_move_permutation");
     if (!P || !dest) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: null pointer");
-    if (!P->move.rec) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: no move_particles call to replay");
+    if (!P->move.rec || !P->move.replayable)
+        return fail(JP_ERR_INVALID_ARGUMENT,
+                    "jp_move_permutation: the container's last move left no record to replay (no move yet, or it "
+                    "was a jp_move_particles_noalloc call)");
     if (!slots_fit_int32(P)) return fail(JP_ERR_INVALID_ARGUMENT, "jp_move_permutation: more than 2^31 slots");
     return finish(P, jp::launch_move_permutation(P, dest), "jp_move_permutation");
 }

@@ -844,6 +844,7 @@ cudaError_t launch_move_f32(jp_particles* P, float* const xi[3], uint8_t* index,
     // FP32 records (4 bytes per value) fit in the scratch sized for FP64 records
     cudaError_t e = ensure_move_scratch(P, shadow_stride(N + nargs));
     if (e != cudaSuccess) return e;
+    P->move.replayable = 1;
     XiF Xi{{xi[0], xi[1], N == 3 ? xi[2] : nullptr}};
     ArgsF A{};
     A.n = nargs;

@@ -61,6 +61,10 @@ struct MoveScratch {
     double* shadow = nullptr; // movers' coordinates and fields, per component
     int shadow_comps = 0;
     size_t bytes = 0;
+    // the masks and origin tags above describe the container's last move (set by
+    // the moves that use this scratch, cleared by any move that does not), so
+    // jp_move_permutation can rebuild that move's permutation from them
+    int replayable = 0;
 };
 
 struct InjectScratch {

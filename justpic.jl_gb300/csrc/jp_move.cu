@@ -32,6 +32,7 @@
 
 #include <climits>
 #include <limits>
+#include <mutex>
 
 #include "jp_internal.cuh"
 #include "jp_move_core.cuh"
@@ -1242,6 +1243,7 @@ cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index
     const int N = P->g.ndim;
     cudaError_t e = ensure_move_scratch(P, shadow_stride(N + nargs));
     if (e != cudaSuccess) return e;
+    P->move.replayable = 1;
     Coords X{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};
     Args A{};
     A.n = nargs;
@@ -1397,6 +1399,7 @@ static __device__ __align__(256) unsigned char g_move_scratch[kNoAllocScratchByt
 
 namespace {
 constexpr int kMaxDevices = 64;
+std::mutex g_move_scratch_mutex;             // guards the table below (host threads may call concurrently)
 void* g_move_scratch_addr[kMaxDevices] = {};  // device address of g_move_scratch, per device
 }  // namespace
 
@@ -1411,13 +1414,18 @@ size_t move_scratch_bytes(const DevGrid& g, int comps)
 // for a host-side shadow. The first call on each device (with that device
 // current) asks the runtime for the real address and keeps it; this may load
 // the library's device image, so that first call should happen before any
-// stream capture.
+// stream capture. The table is filled under a mutex, so host threads calling
+// at the same time get the same address. The address belongs to the device's
+// current context: after cudaDeviceReset the library's device image is loaded
+// again and may sit elsewhere, so a process that resets a device must not use
+// this entry point on that device afterwards.
 static cudaError_t move_scratch_address(void** out)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_move_scratch_mutex);
     if (!g_move_scratch_addr[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_move_scratch);
@@ -1431,6 +1439,9 @@ static cudaError_t move_scratch_address(void** out)
 cudaError_t launch_move_noalloc(jp_particles* P, double* const coords[3], uint8_t* index, double* const* args,
                                 int nargs)
 {
+    // this move leaves the container's own move record untouched: it no longer
+    // describes the last move, so jp_move_permutation must not replay it
+    P->move.replayable = 0;
     if (P->g.max_xcell > 64) return launch_move_wide(P, coords, index, args, nargs);  // needs no scratch
     const int N = P->g.ndim;
     void* scratch = nullptr;

@@ -1,13 +1,12 @@
-"""jp_move_particles_noalloc: move_particles! for callers that cannot allocate
-device memory while they run (a step recorded under CUDA stream capture, a
-loop that cannot absorb the synchronisation an allocation may cause, an
-application whose device memory is owned by its own pool). The entry point
-takes its scratch from a fixed device array inside the library instead of
-cudaMalloc, so it is checked here, through the C ABI, against the ordinary
-jp_move_particles on identical inputs, for two calls in a row (the second call
-reuses the array the first one left behind). This file is collected last so
-that a run stopping at the first failure has already run every other test;
-it also passes on its own in a fresh process."""
+"""jp_move_particles_noalloc: move_particles! for host programs that may not
+call cudaMalloc once their time loop runs (device memory handed out up front by
+their own pool, or no room for the synchronisation an allocation may cause).
+The entry point takes its scratch from a fixed device array inside the library
+instead of cudaMalloc, so it is checked here, through the C ABI, against the
+ordinary jp_move_particles on identical inputs, for two calls in a row (the
+second call reuses the array the first one left behind). This file is
+collected last so that a run stopping at the first failure has already run
+every other test; it also passes on its own in a fresh process."""
 import ctypes
 
 import numpy as np
@@ -63,3 +62,41 @@ def test_noalloc_rejects_a_grid_beyond_its_buffer():
     rc = _noalloc_move(p, (f,))
     assert rc == jp._native.JP_ERR_INVALID_ARGUMENT
     assert "fixed buffer" in jp._native.last_error()
+
+
+def test_noalloc_move_is_not_replayed_by_move_permutation():
+    """The call leaves the container's own move record alone, so a later
+    jp_move_permutation must refuse instead of replaying an older move."""
+    from justpic_gb300 import adjoint as A
+
+    g, a, b, fa, fb = _pair((40, 36))
+    V = W.stream_velocity(g)
+    Vd = tuple(jp.TA("CUDA")(v) for v in V)
+    dt = W.cfl_dt(g, V)
+    jp.advection_(b, jp.RungeKutta2(), Vd, dt)
+    jp.move_particles_(b, (fb,))  # an ordinary move: its record can be replayed
+    A.move_permutation(b)
+    jp.advection_(b, jp.RungeKutta2(), Vd, dt)
+    assert _noalloc_move(b, (fb,)) == 0, jp._native.last_error()
+    with pytest.raises(Exception, match="no record to replay"):
+        A.move_permutation(b)
+
+
+def test_noalloc_wide_cells_beyond_the_buffer_size():
+    """Cells of more than 64 slots run the per-cell schedule, which uses no
+    scratch: a grid whose masked scratch would exceed the buffer is accepted
+    and moves exactly like jp_move_particles."""
+    g = W.grid((128, 128))  # 16384 cells x 80 slots: ~48 MB if it needed the masked scratch
+    a = jp.init_particles(jp.CUDABackend, 60, 80, 50, *g["grid_v"])
+    b = jp.init_particles(jp.CUDABackend, 60, 80, 50, *g["grid_v"])
+    assert a.max_xcell > 64
+    V = W.stream_velocity(g)
+    Vd = tuple(jp.TA("CUDA")(v) for v in V)
+    dt = W.cfl_dt(g, V)
+    jp.advection_(a, jp.RungeKutta2(), Vd, dt)
+    jp.advection_(b, jp.RungeKutta2(), Vd, dt)
+    jp.move_particles_(a, ())
+    assert _noalloc_move(b, ()) == 0, jp._native.last_error()
+    assert np.array_equal(a.index.numpy(), b.index.numpy())
+    for d in range(2):
+        assert_bits_equal(a.coords[d].numpy(), b.coords[d].numpy(), f"coords[{d}]")
