@@ -83,10 +83,9 @@ def algorithmic_bytes(op, N, nf, m, slots_per_live, grid_bytes_per_live, field_b
 
 # DRAM bytes per live particle of each call, FP64 form, 2D, one particle field:
 # dram__bytes_read.sum + dram__bytes_write.sum of the call's kernels in one ncu
-# capture of a 512x512-cell C2 case (5.79M particles; profiles/c2_fp64_kernels_512.md,
-# the move's kernels profiles/move_kernels_512.md),
-# divided by its particle count. Traffic grows with the particle count, so the
-# bench scales it by the live particles of its own run.
+# capture of a 512x512-cell C2 case (5.79M particles), divided by its particle
+# count. Traffic grows with the particle count, so the bench scales it by the
+# live particles of its own run.
 DRAM_BYTES_PER_PARTICLE_2D_F64 = {
     "particle2grid!": 673.6e6 / 5.790e6,
     "advection!": 306.2e6 / 5.790e6,
@@ -247,6 +246,23 @@ def movers_fraction(p, torch):
     return int((out & idx).sum()) / max(1, live)
 
 
+def workload_config(args, f32=False):
+    """The ``config`` object of a bench line: what defines the workload, the
+    same in this arm and in the reference arm."""
+    cfg = _setup_cfg(args.workload, args.ni)
+    rk4 = args.method == "rk4" or (args.method is None and cfg["method"] == "RK4")
+    desc = DESC[args.workload] if args.ni is None else DESC[args.workload] + f" (resized to {args.ni} cells per axis)"
+    return {
+        "workload": desc,
+        "form": "split precision (FP32 cell offset)" if f32 else "FP64",
+        "integrator": "RungeKutta4" if rk4 else "RungeKutta2",
+        "cells": list(cfg["grid"]["ni"]),
+        "particles_per_cell": [cfg["nxcell"], cfg["max_xcell"], cfg["min_xcell"]],
+        "dt": cfg["dt"],
+        "l2": "inputs larger than L2 (the coordinate arrays alone exceed 129 MB)",
+    }
+
+
 def _setup_cfg(workload, ni):
     from justpic_gb300 import workloads as W
     base = W.CONFIGS[workload]["ni"]
@@ -351,6 +367,7 @@ def run_ours(args, form=None, minimal=False):
     for _ in range(args.warmup):
         step()
     jp.synchronize(p)
+    jp.move_counts(p, clear=True)
     live0 = int(p.index.data.sum())
     events = [[[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)] for _ in ops]
               for _ in range(args.steps)]
@@ -365,6 +382,7 @@ def run_ours(args, form=None, minimal=False):
         torch.cuda.synchronize()
     jp.synchronize(p)
     _barrier(world)
+    removed = jp.move_counts(p, clear=True)
     live1 = int(p.index.data.sum())
     live = 0.5 * (live0 + live1)
     elapsed_rank = t0.elapsed_time(t1) / 1e3
@@ -374,7 +392,7 @@ def run_ours(args, form=None, minimal=False):
              for i, op in enumerate(ops)}
     if minimal:
         return {"value": value, "ms_per_step": 1e3 * elapsed / args.steps,
-                "per_call_ms": op_ms, "clocks": clocks.summary()}
+                "per_call_ms": op_ms, "clocks": clocks.summary(), "move_removed": removed}
 
     # ---- end to end through the public API (synchronous, host buffers) ----
     jp.set_synchronous(p, True)
@@ -437,18 +455,9 @@ def run_ours(args, form=None, minimal=False):
         "vs_baseline": None,
         "dtype": "f32 offsets + int32 cell (FP64 renormalisation and p2g sums)" if f32 else "f64",
         "data": "synthetic (seeded analytic flow; the reference publishes no dataset)",
-        "config": {
-            "form": "split precision (FP32 cell offset)" if f32 else "FP64",
-            "integrator": type(method).__name__,
-            "workload": DESC[args.workload] if args.ni is None else DESC[args.workload] + f" (resized to {args.ni} "
-                                                                                         "cells per axis)",
-            "cells": list(p.ni),
-            "live_particles": live,
-            "dt": dt,
-            "movers_fraction": m,
-            "l2": "inputs larger than L2 (the coordinate arrays alone exceed 129 MB)",
-            "parallelism": "independent replicas" if world > 1 else "single GPU",
-        },
+        "config": workload_config(args, f32),
+        "workload_stats": {"live_particles": live, "movers_fraction": m,
+                           "parallelism": "independent replicas" if world > 1 else "single GPU"},
         "per_call_ms": op_ms,
         "algorithmic_bytes_per_particle": bpp,
         "step_algorithmic_gbs": step_gbs,
@@ -475,6 +484,9 @@ def run_ours(args, form=None, minimal=False):
             "mode": "public API, synchronous calls; velocity grids in and (with fields) the vertex field out each step",
         },
         "gpu_launches": sum(launches(op, N) for op in ops) * args.steps,
+        "move_removed": dict(removed, steps=args.steps,
+                             note="particles move_particles! removed over the timed steps: left the domain, moved "
+                                  "more than one cell (dropped), no free slot in the new cell (dropped)"),
         "clocks": clocks.summary(),
     }
     if not f32 and N == 2 and not args.no_split:
@@ -805,7 +817,7 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded analytic flow; the reference publishes no dataset)",
-        "config": {"workload": DESC[args.workload]},
+        "config": workload_config(args),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{n} of {args.steps} requested full steps timed (capped at {budget:.0f} s); "
                                    "FP64 C restatement of JustPIC's CPU path (Julia is not installed)"},

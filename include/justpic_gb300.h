@@ -94,6 +94,16 @@ int jp_set_synchronous(jp_particles* p, int32_t synchronous);
 int jp_synchronize(jp_particles* p);
 /* Sticky warning bits (JP_WARN_*) since the last call with clear = 1. */
 int jp_get_warnings(jp_particles* p, uint32_t* bits, int32_t clear);
+
+/*
+ * Particles removed by move_particles! calls since the last call with
+ * clear = 1 (no reference counterpart; the reference removes them silently,
+ * src/Particles/move_safe.jl:96-117): counts[0] left the domain, counts[1]
+ * moved more than one cell in a step and were dropped, counts[2] found no free
+ * slot at or after the walk's starting point in their new cell. Waits for the
+ * container's stream.
+ */
+int jp_get_move_counts(jp_particles* p, uint64_t counts[3], int32_t clear);
 /* Number of inject calls so far: the `call` word of the injection RNG counter. */
 int jp_get_rng_counter(const jp_particles* p, uint64_t* counter);
 int jp_set_rng_counter(jp_particles* p, uint64_t counter);

@@ -26,6 +26,7 @@ from .api import (  # noqa: F401
     update_phase_ratios_,
     inject_particles_,
     inject_particles_phase_,
+    move_counts,
     move_particles_,
     particle2grid_,
     set_synchronous,

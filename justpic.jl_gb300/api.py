@@ -74,6 +74,17 @@ def synchronize(p: Particles) -> None:
         _warn_bits(bits.value)
 
 
+def move_counts(p: Particles, clear: bool = False) -> dict:
+    """Particles removed by move_particles! since the last clearing call: those
+    that left the domain, those that moved more than one cell in a step
+    (dropped), and those whose new cell had no free slot at or after the
+    walk's starting point (dropped, as in src/Particles/move_safe.jl:113-114).
+    Waits for the container's stream."""
+    out = (ctypes.c_uint64 * 3)()
+    check(_native.load().jp_get_move_counts(p.handle, out, 1 if clear else 0), "move_counts")
+    return {"left_domain": int(out[0]), "moved_too_far": int(out[1]), "no_free_slot": int(out[2])}
+
+
 def _coords(p: Particles) -> P3:
     return P3(*[c.data_ptr() for c in p.coords], *([None] * (3 - p.ndim)))
 

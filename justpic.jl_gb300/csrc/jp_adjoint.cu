@@ -68,11 +68,13 @@ __global__ void __launch_bounds__(kThreads) perm_scatter(DevGrid g, MoveView S, 
         const int s = __ffsll((long long)R) - 1;
         R &= R - 1;
         const int64_t a = c + nc * s;
-        const uint16_t tag = S.orig[a];
+        const uint16_t tag = S.orig[a];  // source cell's neighbour code, the mover's rank there
         int off[3];
         nb_offset<DIM>(tag & 0x1F, off);
         const int64_t J[3] = {I[0] + off[0], I[1] + off[1], DIM == 3 ? I[2] + off[2] : 0};
-        dest[cell_linear<DIM>(g, J) + nc * (tag >> 5)] = (int32_t)a;  // each origin has one destination
+        const int64_t src = cell_linear<DIM>(g, J);
+        const int s_src = nth_set_bit64(S.M(src), tag >> 5);
+        dest[src + nc * s_src] = (int32_t)a;  // each origin has one destination
     }
 }
 
@@ -1139,7 +1141,7 @@ cudaError_t launch_move_permutation(jp_particles* P, int32_t* dest)
     const MoveScratch& m = P->move;
     if (!m.rec) return cudaErrorInvalidValue;
     const unsigned nb = grid_blocks(P->g.ncells);
-    MoveView S{m.rec, P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, 0};
+    MoveView S{m.rec, P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, 0, P->g.max_xcell};
     perm_init<<<nb, kThreads, 0, P->stream>>>(P->g, S, dest);
     if (P->g.ndim == 2)
         perm_scatter<2><<<nb, kThreads, 0, P->stream>>>(P->g, S, dest);

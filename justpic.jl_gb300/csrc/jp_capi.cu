@@ -200,6 +200,8 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
         e = cudaMemcpy(P->dev_block, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&P->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(P->d_err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&g.counts, 3 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(g.counts, 0, 3 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMallocHost(&P->h_err, sizeof(int));
     if (e != cudaSuccess) {
         int rc = cuda_fail(e, "jp_particles_create");
@@ -228,6 +230,7 @@ int jp_particles_destroy(jp_particles* P)
     if (!P) return JP_OK;
     cudaFree(P->dev_block);
     cudaFree(P->d_err);
+    cudaFree(P->g.counts);
     if (P->h_err) cudaFreeHost(P->h_err);
     cudaFree(P->move.rec);  // one allocation holds all move scratch
     cudaFree(P->inject.counts);  // counters and lists share one allocation
@@ -290,6 +293,18 @@ int jp_get_warnings(jp_particles* P, uint32_t* bits, int32_t clear)
     if (!P || !bits) return fail(JP_ERR_INVALID_ARGUMENT, "null argument");
     *bits = P->warnings;
     if (clear) P->warnings = 0;
+    return JP_OK;
+}
+
+int jp_get_move_counts(jp_particles* P, uint64_t counts[3], int32_t clear)
+{
+    if (!P || !counts) return fail(JP_ERR_INVALID_ARGUMENT, "null argument");
+    unsigned long long h[3] = {0, 0, 0};
+    cudaError_t e = cudaMemcpyAsync(h, P->g.counts, sizeof(h), cudaMemcpyDeviceToHost, P->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+    if (e == cudaSuccess && clear) e = cudaMemsetAsync(P->g.counts, 0, sizeof(h), P->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "jp_get_move_counts");
+    for (int k = 0; k < 3; ++k) counts[k] = h[k];
     return JP_OK;
 }
 

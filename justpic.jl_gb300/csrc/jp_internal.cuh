@@ -51,6 +51,9 @@ struct DevGrid {
     const double* dxc[3];  // their spacing (di.center) per interval, n[d] - 1
     const double* ixc[3];  // 1/spacing
     double idmin[3];       // 1 / smallest vertex spacing per axis (grid_size, the FLIP transfer's di)
+    // move_particles! counts since the last jp_get_move_counts with clear: particles that
+    // left the domain, moved more than one cell (dropped), found no free slot (dropped)
+    unsigned long long* counts;
 };
 
 // Scratch owned by a container for move_particles! (allocated on first use).

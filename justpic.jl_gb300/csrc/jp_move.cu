@@ -68,157 +68,148 @@ __device__ __forceinline__ int64_t find_cell_key(double px, long long kp, const 
 }
 
 // -------------------------------------------------------------- classify
+// One thread per cell, a warp on 32 consecutive cells: the warp walks the slot
+// rows up to its highest live slot, so each row of each array is one coalesced
+// access, with four rows in flight per lane. A mover's record (coordinates,
+// then fields) goes to the next record of its own cell, so a cell's movers sit
+// together; all masks are built in registers and stored once.
 template <int DIM>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+__global__ void __launch_bounds__(kThreads)
     move_classify(DevGrid g, Coords X, const uint8_t* __restrict__ index, Args A, MoveView S, int* d_err)
 {
-    __shared__ SlotList lists[kWarpsPerBlock];
-    __shared__ long long cellk[kWarpsPerBlock][32][2 * DIM];  // keys of corner and corner + dx
-    __shared__ int cellI[kWarpsPerBlock][32][3];
-    __shared__ unsigned long long movers[kWarpsPerBlock][32];
-    constexpr int NT = DIM == 2 ? kTargetMasks2D : 1;
-    __shared__ unsigned long long tmask[kWarpsPerBlock][32][NT];  // 2D: movers per target, unstable ones
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
-    if (c0 >= g.ncells) return;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nc = g.ncells;
+    const bool valid = c < nc;
     const int M = g.max_xcell;
-    {
-        int64_t I[3];
-        cell_coords(g, min(c0 + lane, nc - 1), I);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            const double lo = ldg(g.xv[d] + I[d]);
-            cellk[w][lane][d] = okey(lo);
-            cellk[w][lane][DIM + d] = okey(lo + ldg(g.dxv[d] + I[d]));  // xv + dx (isincell)
-            cellI[w][lane][d] = (int)I[d];
-        }
-        movers[w][lane] = 0;
-#pragma unroll
-        for (int k = 0; k < NT; ++k) tmask[w][lane][k] = 0;
-    }
-    long long kdlo[3], kdhi[3];
+    int64_t I[3];
+    cell_coords(g, valid ? c : nc - 1, I);
+    long long klo[DIM], khi[DIM], kdlo[DIM], kdhi[DIM];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
+        const double lo = ldg(g.xv[d] + I[d]);
+        klo[d] = okey(lo);
+        khi[d] = okey(lo + ldg(g.dxv[d] + I[d]));  // xv + dx (isincell)
         kdlo[d] = okey(g.dom_lo[d]);
         kdhi[d] = okey(g.dom_hi[d]);
     }
-    uint64_t L;
-    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &L);
-    int errs = 0;
-    const bool rec4 = S.comps == 4;
-    // one live particle: p its coordinates, fv its fields (records of 4 values)
-    auto classify_one = [&](int s, int l, int64_t a, const double* p, const double* fv) {
-        long long kp[3];
-        bool pnan = false;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            kp[d] = okey(p[d]);
-            pnan |= is_nan_bits(p[d]);
-        }
-        bool in = !pnan;  // isincell, strict (src/Particles/utils.jl:7-15)
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) in = in & (cellk[w][l][d] < kp[d]) & (kp[d] < cellk[w][l][DIM + d]);
-        // The shadow copy. A record of 4 values is exactly one 32-byte sector:
-        // it is written whole (padding included) in one access, and only for
-        // movers (the apply stage gathers nothing else). Smaller or larger
-        // records are written for every live slot, so that the records of
-        // neighbouring slots fill whole sectors instead of partial ones that L2
-        // would first have to read back from DRAM.
-        if (rec4) {
-            if (!in) {
-                double v[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) v[d] = p[d];
-#pragma unroll
-                for (int j = 0; j < 4 - DIM; ++j) v[DIM + j] = fv[j];
-                store_rec4(S.shadow + a * 4, v);
-            }
-        } else {
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) S.shadow[a * S.comps + d] = p[d];
-            for (int j = 0; j < A.n; ++j) S.shadow[a * S.comps + DIM + j] = A.a[j][a];
-        }
-        if (in) {  // move_safe.jl:93
-            if (DIM == 3) S.code[a] = kCodeStay;
-            return;
-        }
-        atomicOr(&movers[w][l], 1ull << s);
-        bool inside = !pnan;  // indomain, strict (move_safe.jl:199-206)
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) inside = inside & (kdlo[d] < kp[d]) & (kp[d] < kdhi[d]);
-        uint8_t code = kCodeExit;
-        if (inside) {
-            int off[3] = {0, 0, 0};
-            bool far = false, inT = true;
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const int I = cellI[w][l][d];
-                const int64_t T = find_cell_key(p[d], kp[d], g.xv[d], g.n[d] + 1, I, &errs);
-                off[d] = (int)(T - I);
-                far |= (off[d] > 1) | (off[d] < -1);
-                const double lo = ldg(g.xv[d] + T);
-                inT = inT & (okey(lo) < kp[d]) & (kp[d] < okey(lo + ldg(g.dxv[d] + T)));
-            }
-            if (far) {
-                errs |= kWarnFarMove;
-            } else {
-                code = (uint8_t)nb_code<DIM>(off);
-                if (!inT) code |= kCodeUnstable;
-            }
-        }
-        if (DIM == 2) {
-            if (code != kCodeExit) {
-                atomicOr(&tmask[w][l][code & 0x1F], 1ull << s);
-                if (code & kCodeUnstable) atomicOr(&tmask[w][l][NT - 1], 1ull << s);
-            }
-        } else {
-            S.code[a] = code;
-        }
-    };
-    // Two particles per lane at a time: the loads of both are in flight
-    // before either is classified (the kernel is bound by load latency).
-    constexpr int B = 2;
-    for (int k0 = lane; k0 < K; k0 += 32 * B) {
-        int sl[B], ll[B];
-        int64_t al[B];
-        double pl[B][3], fl[B][4 - DIM];
-        bool has[B];
+    uint64_t L = 0;
+    if (valid) {
+#pragma unroll 8
+        for (int s = 0; s < M; ++s) L |= (uint64_t)(index[c + nc * s] != 0) << s;
+    }
+    const int hi = (int)__reduce_max_sync(0xffffffffu, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
+    uint64_t Mv = 0, P0 = 0, P1 = 0, P2 = 0, P3 = 0, RT = 0, UN = 0;
+    int rank = 0, n_exit = 0, n_far = 0, errs = 0;
+    const int comps = S.comps;
+    double* rec = S.shadow + S.record(valid ? c : 0, 0);
+    constexpr int B = 4;
+    for (int s0 = 0; s0 < hi; s0 += B) {
+        double p[B][DIM];
+        bool lv[B];
 #pragma unroll
         for (int u = 0; u < B; ++u) {
-            const int k = k0 + 32 * u;
-            has[u] = k < K;
-            sl[u] = 0;
-            ll[u] = 0;
-            if (has[u]) slot_item(lists[w], M, k, &sl[u], &ll[u]);
-            al[u] = c0 + ll[u] + nc * sl[u];
+            const int s = s0 + u;
+            lv[u] = s < hi && ((L >> s) & 1);
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) pl[u][d] = has[u] ? X.c[d][al[u]] : 0.0;
-#pragma unroll
-            for (int j = 0; j < 4 - DIM; ++j) fl[u][j] = (has[u] && rec4 && j < A.n) ? A.a[j][al[u]] : 0.0;
+            for (int d = 0; d < DIM; ++d) p[u][d] = lv[u] ? X.c[d][c + nc * s] : 0.0;
         }
 #pragma unroll
-        for (int u = 0; u < B; ++u)
-            if (has[u]) classify_one(sl[u], ll[u], al[u], pl[u], fl[u]);
+        for (int u = 0; u < B; ++u) {
+            if (!lv[u]) continue;
+            const int s = s0 + u;
+            const int64_t a = c + nc * s;
+            long long kp[DIM];
+            bool pnan = false;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                kp[d] = okey(p[u][d]);
+                pnan |= is_nan_bits(p[u][d]);
+            }
+            bool in = !pnan;  // isincell, strict (src/Particles/utils.jl:7-15)
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) in = in & (klo[d] < kp[d]) & (kp[d] < khi[d]);
+            if (in) continue;  // move_safe.jl:93
+            const uint64_t bit = 1ull << s;
+            Mv |= bit;
+            const int r = rank++;
+            bool inside = !pnan;  // indomain, strict (move_safe.jl:199-206)
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) inside = inside & (kdlo[d] < kp[d]) & (kp[d] < kdhi[d]);
+            uint8_t code = kCodeExit;
+            if (inside) {
+                int off[3] = {0, 0, 0};
+                bool far = false, inT = true;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const int64_t T = find_cell_key(p[u][d], kp[d], g.xv[d], g.n[d] + 1, I[d], &errs);
+                    off[d] = (int)(T - I[d]);
+                    far |= (off[d] > 1) | (off[d] < -1);
+                    const double lo = ldg(g.xv[d] + T);
+                    inT = inT & (okey(lo) < kp[d]) & (kp[d] < okey(lo + ldg(g.dxv[d] + T)));
+                }
+                if (far) {
+                    errs |= kWarnFarMove;
+                    ++n_far;
+                } else {
+                    code = (uint8_t)nb_code<DIM>(off);
+                    if (!inT) code |= kCodeUnstable;
+                }
+            } else {
+                ++n_exit;
+            }
+            if (DIM == 3) S.code[a] = code;
+            if (code == kCodeExit) continue;  // removed: no record needed
+            if (DIM == 2) {
+                const int k = code & 0x1F;
+                P0 |= (k & 1) ? bit : 0ull;
+                P1 |= (k & 2) ? bit : 0ull;
+                P2 |= (k & 4) ? bit : 0ull;
+                P3 |= (k & 8) ? bit : 0ull;
+                RT |= bit;
+                if (code & kCodeUnstable) UN |= bit;
+            }
+            // the record: one 32- or 16-byte store when it has 4 or 2 values
+            double* rp = rec + (int64_t)r * comps;
+            if (comps == 4) {
+                double v[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) v[d] = p[u][d];
+#pragma unroll
+                for (int j = 0; j < 4 - DIM; ++j)
+                    if (j < A.n) v[DIM + j] = A.a[j][a];
+                store_rec4(rp, v);
+            } else if (comps == 2) {
+                *reinterpret_cast<double2*>(rp) = make_double2(p[u][0], p[u][1]);
+            } else {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) rp[d] = p[u][d];
+                for (int j = 0; j < A.n; ++j) rp[DIM + j] = A.a[j][a];
+            }
+        }
     }
-    __syncwarp();
-    const int64_t c = c0 + lane;
-    if (c < nc) {
+    if (valid) {
         S.L(c) = L;
         S.R(c) = 0;
         S.U(c) = 0;
         S.L0(c) = L;
-        S.M(c) = movers[w][lane];
-        if (DIM == 2)
-#pragma unroll
-            for (int k = 0; k < NT; ++k) S.T(c, k) = tmask[w][lane][k];
+        S.M(c) = Mv;
+        if (DIM == 2) {
+            S.P(c, 0) = P0;
+            S.P(c, 1) = P1;
+            S.P(c, 2) = P2;
+            S.P(c, 3) = P3;
+            S.RT(c) = RT;
+            S.UN(c) = UN;
+        }
     }
+    add_move_counts(g.counts, n_exit, n_far, 0);
     raise_err(d_err, errs);
 }
 
 // ----------------------------------------------------------------- apply
 // Slot-major over a warp's 32 cells: at each slot the lanes whose slot changed
-// store together, so every 32-byte sector is written in one go.
+// store together, so every 32-byte sector is written in one go. A refilled
+// slot gathers its record from the source cell named by its origin tag.
 template <int DIM>
 __global__ void __launch_bounds__(kThreads)
     move_apply(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, MoveView S)
@@ -246,19 +237,23 @@ __global__ void __launch_bounds__(kThreads)
             int off[3];
             nb_offset<DIM>(tag & 0x1F, off);
             const int64_t J[3] = {I[0] + off[0], I[1] + off[1], DIM == 3 ? I[2] + off[2] : 0};
-            const int64_t b = cell_linear<DIM>(g, J) + nc * (tag >> 5);
+            const double* rp = S.shadow + S.record(cell_linear<DIM>(g, J), tag >> 5);
             if (S.comps == 4) {  // the whole record in one 32-byte load
                 double v[4];
-                load_rec4(S.shadow + b * 4, v);
+                load_rec4(rp, v);
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) X.c[d][a] = v[d];
 #pragma unroll
                 for (int k = 0; k < 4 - DIM; ++k)
                     if (k < A.n) A.a[k][a] = v[DIM + k];
+            } else if (S.comps == 2) {
+                const double2 v = *reinterpret_cast<const double2*>(rp);
+                X.c[0][a] = v.x;
+                X.c[1][a] = v.y;
             } else {
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) X.c[d][a] = S.shadow[b * S.comps + d];
-                for (int k = 0; k < A.n; ++k) A.a[k][a] = S.shadow[b * S.comps + DIM + k];
+                for (int d = 0; d < DIM; ++d) X.c[d][a] = rp[d];
+                for (int k = 0; k < A.n; ++k) A.a[k][a] = rp[DIM + k];
             }
             index[a] = 1;
         } else {
@@ -979,7 +974,7 @@ __global__ void __launch_bounds__(kThreads)
         corner[d] = ldg(g.xv[d] + I[d]);
         dx[d] = ldg(g.dxv[d] + I[d]);
     }
-    int errs = 0;
+    int errs = 0, n_exit = 0, n_far = 0, n_full = 0;
     int sp = 0;  // starting_point
     for (int ip = 0; ip < M; ++ip) {
         const int64_t a = c + nc * ip;
@@ -996,6 +991,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
             for (int d = 0; d < DIM; ++d) X.c[d][a] = CUDART_NAN;
             for (int k = 0; k < A.n; ++k) A.a[k][a] = CUDART_NAN;
+            ++n_exit;
             continue;
         }
         int64_t T[3] = {0, 0, 0};
@@ -1013,6 +1009,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int k = 0; k < A.n; ++k) A.a[k][a] = CUDART_NAN;
         if (far) {  // the reference's colour passes race here; the particle is dropped
             errs |= kWarnFarMove;
+            ++n_far;
             continue;
         }
         const int64_t tc = cell_linear<DIM>(g, T);
@@ -1022,13 +1019,21 @@ __global__ void __launch_bounds__(kThreads)
                 fr = i;
                 break;
             }
-        if (fr < 0) continue;  // target cell full: dropped
+        if (fr < 0) {  // target cell full: dropped
+            ++n_full;
+            continue;
+        }
         sp = fr;
         const int64_t b = tc + nc * fr;
         index[b] = 1;
 #pragma unroll
         for (int d = 0; d < DIM; ++d) X.c[d][b] = p[d];
         for (int k = 0; k < A.n; ++k) A.a[k][b] = cached[k];
+    }
+    if ((n_exit | n_far | n_full) && g.counts) {
+        if (n_exit) atomicAdd(g.counts + 0, (unsigned long long)n_exit);
+        if (n_far) atomicAdd(g.counts + 1, (unsigned long long)n_far);
+        if (n_full) atomicAdd(g.counts + 2, (unsigned long long)n_full);
     }
     raise_err(d_err, errs);
 }
@@ -1249,17 +1254,16 @@ cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index
     A.n = nargs;
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
     const MoveScratch& m = P->move;
-    MoveView S{m.rec, P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, shadow_stride(N + nargs)};
+    MoveView S{m.rec,    P->g.ncells, m.code, m.orig, m.shadow, P->g.ncells * P->g.max_xcell, shadow_stride(N + nargs),
+               P->g.max_xcell};
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(P->g.ncells);
-    const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
-    const int ntw = 32 * kWarpsPerBlock;
     if (N == 2) {
-        move_classify<2><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        move_classify<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S, P->d_err);
         launch_allocate_passes(P->g, S, st);
         move_apply<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     } else {
-        move_classify<3><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        move_classify<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S, P->d_err);
         launch_allocate_passes(P->g, S, st);
         move_apply<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     }
@@ -1458,20 +1462,19 @@ cudaError_t launch_move_noalloc(jp_particles* P, double* const coords[3], uint8_
     S.code = (uint8_t*)((char*)S.orig + ns * sizeof(uint16_t));
     S.nslots = ns;
     S.comps = shadow_stride(N + nargs);
+    S.mx = P->g.max_xcell;
     Coords X{{coords[0], coords[1], N == 3 ? coords[2] : nullptr}};
     Args A{};
     A.n = nargs;
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(nc);
-    const unsigned nbw = grid_blocks(nc, 32 * kWarpsPerBlock);
-    const int ntw = 32 * kWarpsPerBlock;
     if (N == 2) {
-        move_classify<2><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        move_classify<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S, P->d_err);
         launch_allocate_passes(P->g, S, st);
         move_apply<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     } else {
-        move_classify<3><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        move_classify<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S, P->d_err);
         launch_allocate_passes(P->g, S, st);
         move_apply<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     }

@@ -12,11 +12,18 @@ constexpr int kAllocThreads = 64;  // small blocks spread the sparse colour pass
 // Per-cell 64-bit slot masks, one array of ncells words each (a warp's
 // accesses to one mask are coalesced): the occupancy L, the refilled slots R,
 // the refilled slots whose particle is not strictly inside U, the occupancy
-// before the move L0 and the movers M; in 2D also the movers bound for each
-// of the 9 neighbours and the movers not strictly inside their new cell.
-constexpr int kRecWords2D = 15;
+// before the move L0 and the movers M; in 2D also the movers' destinations as
+// four bit planes of their neighbour code (bit j of the code of slot s is bit
+// s of plane j), the movers that have a destination (the others leave the
+// domain) and the movers not strictly inside their new cell.
+constexpr int kRecWords2D = 11;
 constexpr int kRecWords3D = 5;
 
+// Shadow records: the movers of cell c, in slot order, are records
+// c * max_xcell + 0, 1, 2, ... (the rank of a mover is the number of movers
+// in lower slots of its cell), so a cell's movers sit together. An origin tag
+// names a refilled slot's particle by the neighbour code of its source cell
+// (bits 0..4) and its rank there (bits 5..10).
 struct MoveView {
     uint64_t* rec;  // the mask arrays, one after the other
     int64_t nc;     // cells (the length of each mask array)
@@ -25,16 +32,46 @@ struct MoveView {
     double* shadow;
     int64_t nslots;
     int comps;  // stride of the shadow records: DIM coordinates, then the fields (records are interleaved)
+    int mx;     // max_xcell: records per cell
     __device__ __forceinline__ uint64_t& L(int64_t c) const { return rec[c]; }
     __device__ __forceinline__ uint64_t& R(int64_t c) const { return rec[nc + c]; }
     __device__ __forceinline__ uint64_t& U(int64_t c) const { return rec[2 * nc + c]; }
     __device__ __forceinline__ uint64_t& L0(int64_t c) const { return rec[3 * nc + c]; }
     __device__ __forceinline__ uint64_t& M(int64_t c) const { return rec[4 * nc + c]; }
-    // 2D: k < 9 movers bound for neighbour k, k = 9 movers not strictly inside their new cell
-    __device__ __forceinline__ uint64_t& T(int64_t c, int k) const { return rec[(5 + k) * nc + c]; }
+    // 2D: bit plane j < 4 of the movers' neighbour codes, the routed movers, the unstable ones
+    __device__ __forceinline__ uint64_t& P(int64_t c, int j) const { return rec[(5 + j) * nc + c]; }
+    __device__ __forceinline__ uint64_t& RT(int64_t c) const { return rec[9 * nc + c]; }
+    __device__ __forceinline__ uint64_t& UN(int64_t c) const { return rec[10 * nc + c]; }
+    // first value of the record of rank r of cell c
+    __device__ __forceinline__ int64_t record(int64_t c, int r) const { return (c * mx + r) * comps; }
 };
 
-constexpr int kTargetMasks2D = 10;
+__device__ __forceinline__ uint16_t make_tag(int code, int rank) { return (uint16_t)(code | (rank << 5)); }
+
+// position of the n-th set bit (n from 0) of a 64-bit mask
+__device__ __forceinline__ int nth_set_bit64(uint64_t m, int n)
+{
+    const uint32_t lo = (uint32_t)m;
+    const int cl = __popc(lo);
+    return n < cl ? nth_set_bit(lo, n) : 32 + nth_set_bit((uint32_t)(m >> 32), n - cl);
+}
+
+// Per-launch counts of the move, added to the container's counters: [0]
+// particles that left the domain, [1] particles that moved more than one cell
+// (dropped), [2] particles dropped because their new cell had no free slot at
+// or after the walk's starting point.
+__device__ __forceinline__ void add_move_counts(unsigned long long* counts, int n_exit, int n_far, int n_full)
+{
+    const unsigned full = 0xffffffffu;
+    n_exit = __reduce_add_sync(full, n_exit);
+    n_far = __reduce_add_sync(full, n_far);
+    n_full = __reduce_add_sync(full, n_full);
+    if ((threadIdx.x & 31) == 0 && counts) {
+        if (n_exit) atomicAdd(counts + 0, (unsigned long long)n_exit);
+        if (n_far) atomicAdd(counts + 1, (unsigned long long)n_far);
+        if (n_full) atomicAdd(counts + 2, (unsigned long long)n_full);
+    }
+}
 
 // One 32-byte shadow record (4 doubles) in a single 256-bit access: a gather
 // of a record is one sector request instead of one per value. p must be
@@ -119,6 +156,7 @@ __global__ void __launch_bounds__(kAllocThreads)
     // centre cell ahead of the walk is added
     uint64_t todo = Lc & ((Mv & ~Rc) | (Rc & Uc));
     uint64_t from_sp = valid;  // slots at or after starting_point (move_safe.jl:83)
+    int n_full = 0;
     while (todo) {
         const uint64_t bit = todo & (0ull - todo);
         todo ^= bit;
@@ -141,7 +179,7 @@ __global__ void __launch_bounds__(kAllocThreads)
             int off[3];
             nb_offset<DIM>(code, off);
             const int back[3] = {-off[0], -off[1], -off[2]};
-            tag = (uint16_t)(nb_code<DIM>(back) | (s << 5));
+            tag = make_tag(nb_code<DIM>(back), __popcll(Mv & (bit - 1)));
         }
         // remove the particle from its slot (move_safe.jl:110-112)
         Lc &= ~bit;
@@ -150,7 +188,10 @@ __global__ void __launch_bounds__(kAllocThreads)
         // find_free_memory(starting_point, ...) (move_safe.jl:192-197)
         const uint64_t tL = code == CENTER ? Lc : nL[code];
         const uint64_t freem = ~tL & from_sp;
-        if (!freem) continue;  // dropped: no free slot at or after starting_point
+        if (!freem) {  // dropped: no free slot at or after starting_point
+            ++n_full;
+            continue;
+        }
         const uint64_t fb = freem & (0ull - freem);
         from_sp = valid & ~(fb - 1);
         if (code == CENTER) {
@@ -175,6 +216,7 @@ __global__ void __launch_bounds__(kAllocThreads)
     S.L(sc) = Lc;
     S.R(sc) = Rc;
     S.U(sc) = Uc;
+    if (n_full && g.counts) atomicAdd(g.counts + 2, (unsigned long long)n_full);
     // a neighbour only gained slots in this walk: R = R before | the slots L gained
     for (uint32_t m = touched; m; m &= m - 1) {
         const int nb = __ffs(m) - 1;
@@ -194,8 +236,8 @@ __global__ void __launch_bounds__(kAllocThreads)
 //  * the slots still to visit are a mask (the candidates of the reference's
 //    slot loop; a particle put back into the centre cell ahead of the walk
 //    is added to it), popped lowest bit first;
-//  * the destination of a slot comes from four bit planes of the nine
-//    per-target masks written by the classify stage (no per-slot table);
+//  * the destination of a slot comes from the four bit planes of the
+//    movers' neighbour codes written by the classify stage (no per-slot table);
 //  * "first free slot at or after starting_point" is the lowest set bit of
 //    the free mask under a running mask of the slots >= starting_point;
 //  * the centre cell's masks stay in registers, the eight neighbours' sit in
@@ -232,7 +274,7 @@ static __global__ void __launch_bounds__(kAllocThreads)
     const uint64_t U0 = S.U(sc);
     if (Mv == 0 && U0 == 0) return;
     uint64_t Lc = S.L(sc), Rc = S.R(sc), Uc = U0;
-    uint64_t nl[9], nu[9], tm[10];
+    uint64_t nl[9], nu[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         if (k == CENTER) continue;
@@ -242,26 +284,16 @@ static __global__ void __launch_bounds__(kAllocThreads)
         nl[k] = in ? S.L(jc) : 0;
         nu[k] = in ? S.U(jc) : 0;
     }
-#pragma unroll
-    for (int k = 0; k < 10; ++k) tm[k] = S.T(sc, k);
+    // bit j of a slot's destination code in plane j; movers with no destination leave the domain
+    const uint64_t P0 = S.P(sc, 0), P1 = S.P(sc, 1), P2 = S.P(sc, 2), P3 = S.P(sc, 3);
+    const uint64_t routed = S.RT(sc), unst = S.UN(sc);
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         if (k == CENTER) continue;
         sL[k][tid] = nl[k];
         sU[k][tid] = nu[k];
     }
-    // bit j of a slot's destination code in plane j; movers with no destination leave the domain
-    uint64_t P0 = 0, P1 = 0, P2 = 0, P3 = 0, routed = 0;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        routed |= tm[k];
-        if (k & 1) P0 |= tm[k];
-        if (k & 2) P1 |= tm[k];
-        if (k & 4) P2 |= tm[k];
-        if (k & 8) P3 |= tm[k];
-    }
     const uint64_t exits = Mv & ~routed;
-    const uint64_t unst = tm[9];
     const int nslot = g.max_xcell;
     const uint64_t valid = nslot == 64 ? ~0ull : ((1ull << nslot) - 1);
     uint32_t touched = 0;  // neighbours (not the centre) whose masks changed
@@ -269,6 +301,7 @@ static __global__ void __launch_bounds__(kAllocThreads)
     // refilled by an earlier pass and not strictly inside
     uint64_t todo = Lc & ((Mv & ~Rc) | (Rc & Uc));
     uint64_t from_sp = valid;  // slots at or after starting_point (move_safe.jl:83)
+    int n_full = 0;
     while (todo) {
         const uint64_t bit = todo & (0ull - todo);
         todo ^= bit;
@@ -291,7 +324,10 @@ static __global__ void __launch_bounds__(kAllocThreads)
         // find_free_memory(starting_point, ...) (move_safe.jl:192-197)
         const uint64_t tL = code == CENTER ? Lc : sL[code][tid];
         const uint64_t freem = ~tL & from_sp;
-        if (!freem) continue;  // dropped: no free slot at or after starting_point
+        if (!freem) {  // dropped: no free slot at or after starting_point
+            ++n_full;
+            continue;
+        }
         const uint64_t fb = freem & (0ull - freem);
         from_sp = valid & ~(fb - 1);
         if (code == CENTER) {
@@ -315,13 +351,14 @@ static __global__ void __launch_bounds__(kAllocThreads)
         if (refill)
             tag = S.orig[sc + nc * s];
         else
-            tag = (uint16_t)((8 - code) | (s << 5));  // 8 - code: the neighbour code of the way back
+            tag = make_tag(8 - code, __popcll(Mv & (bit - 1)));  // 8 - code: the neighbour code of the way back
         const int dy = code / 3 - 1, dx = code - 3 * (dy + 1) - 1;
         S.orig[sc + dx + nx * dy + nc * f] = tag;
     }
     S.L(sc) = Lc;
     S.R(sc) = Rc;
     S.U(sc) = Uc;
+    if (n_full && g.counts) atomicAdd(g.counts + 2, (unsigned long long)n_full);
     // a neighbour only gained slots in this walk: R = R before | the slots L gained
     // (its R and L in memory are still those before the walk: this thread alone writes them)
 #pragma unroll

@@ -85,11 +85,50 @@ def test_move_full_cells_drop_like_reference():
     V = W.stream_velocity(g)
     pair.g2p(0, W.linear_T(g, 0))
     dt = W.cfl_dt(g, V)
+    full = 0
     for step in range(6):
         pair.advection("rk2_23", V, dt)
+        before = int(pair.p.index.numpy().sum())
+        jp.move_counts(pair.p, clear=True)
         pair.move()
         pair.assert_same(f"overflow move step {step}")
+        counts = jp.move_counts(pair.p)
+        # every particle the move removed is counted once
+        assert before - int(pair.p.index.numpy().sum()) == sum(counts.values()), counts
+        full += counts["no_free_slot"]
     assert pair.p.index.numpy().sum() < pair.o.ncells * pair.o.nxcell  # particles were dropped
+    assert full > 0
+
+
+@pytest.mark.parametrize("ni", [(16, 16), (7, 6, 5)])
+def test_move_counts_name_every_removed_particle(ni):
+    """A step of three CFL widths: some particles leave the domain, some move
+    more than one cell; move_counts tells them apart like a host check of the
+    positions does, and the move still matches the oracle."""
+    pair, g = _setup(ni)
+    N = len(ni)
+    V = W.stream_velocity(g) if N == 2 else W.stream_velocity_3d(g)
+    pair.advection("rk2", V, 3 * W.cfl_dt(g, V))
+    idx = pair.p.index.numpy().astype(bool)
+    X = [pair.p.coords[d].numpy() for d in range(N)]
+    cells = np.arange(idx.shape[1])
+    inside = np.ones_like(idx)
+    far = np.zeros_like(idx)
+    stride = 1
+    for d in range(N):
+        I = (cells // stride) % ni[d]
+        stride *= ni[d]
+        with np.errstate(invalid="ignore"):
+            inside &= (X[d] > 0.0) & (X[d] < 1.0)
+            T = np.floor(np.where(np.isfinite(X[d]), X[d], 0.0) * ni[d])
+        far |= np.abs(T - I[None, :]) > 1
+    jp.move_counts(pair.p, clear=True)
+    with pytest.warns(RuntimeWarning):
+        pair.move()
+    pair.assert_same("move after a long step")
+    counts = jp.move_counts(pair.p)
+    assert counts["left_domain"] == int((idx & ~inside).sum())
+    assert counts["moved_too_far"] == int((idx & inside & far).sum()) > 0
 
 
 @pytest.mark.parametrize("ni", [(12, 12), (5, 6, 4)])
