@@ -93,6 +93,8 @@ DRAM_BYTES_PER_PARTICLE_2D_F64 = {
     "move_particles!": (444.8e6 + 9 * 14.8e6 + 923.5e6) / 5.790e6,  # classify + 9 colour passes + apply
     "inject_particles!": 333.1e6 / 5.790e6,
 }
+# the same for the split-precision form (FP32 offsets and fields)
+DRAM_BYTES_PER_PARTICLE_2D_F32 = {}
 
 
 def fp64_instructions(op, N, method):
@@ -390,9 +392,36 @@ def run_ours(args, form=None, minimal=False):
     value = job_throughput(live * args.steps, elapsed_rank, world)
     op_ms = {op: float(np.mean([events[k][i][0].elapsed_time(events[k][i][1]) for k in range(args.steps)]))
              for i, op in enumerate(ops)}
+    # ---- roofline of the dominant call ----
+    peak, peak_kind = _peaks()
+    nvel_bytes = sum(v.size * 8 for v in cfg["V"])
+    slots_per_live = p.max_xcell * int(np.prod(p.ni)) / live
+    gb = nvel_bytes / live
+    fb = T.numel() * 8 / live
+    vb = 4 if f32 else 8  # bytes per value of coordinates/offsets and fields
+    bpp = {op: algorithmic_bytes(op, N, nf, m, slots_per_live, gb * vb / 8, fb * vb / 8, vb) for op in ops}
+    dom = max(op_ms, key=op_ms.get)
+    achieved = bpp[dom] * live / (op_ms[dom] / 1e3) / 1e9
+    step_bytes = sum(bpp.values()) * live
+    step_gbs = step_bytes / (elapsed / args.steps) / 1e9
+    traffic_table = DRAM_BYTES_PER_PARTICLE_2D_F32 if f32 else DRAM_BYTES_PER_PARTICLE_2D_F64
+    roofline = {
+        "bound": "hbm",
+        "kernel": dom,
+        "achieved": achieved,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+        "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
+        else "fallback 6.8 TB/s",
+        "traffic": (traffic_table[dom] * live / 1e9 if (N == 2 and nf == 1 and dom in traffic_table) else None),
+        "traffic_unit": "GB per launch, from ncu dram bytes of a 512^2 capture scaled by particle count",
+        "per_call_frac": {op: bpp[op] * live / (op_ms[op] / 1e3) / 1e9 / peak for op in ops},
+    }
     if minimal:
         return {"value": value, "ms_per_step": 1e3 * elapsed / args.steps,
-                "per_call_ms": op_ms, "clocks": clocks.summary(), "move_removed": removed}
+                "per_call_ms": op_ms, "clocks": clocks.summary(), "move_removed": removed,
+                "algorithmic_bytes_per_particle": bpp, "step_algorithmic_gbs": step_gbs, "roofline": roofline}
 
     # ---- end to end through the public API (synchronous, host buffers) ----
     jp.set_synchronous(p, True)
@@ -418,18 +447,6 @@ def run_ours(args, form=None, minimal=False):
     Vcur[0] = V
     e2e_value = job_throughput(live * e2e_steps, e2e_time, world)
 
-    # ---- roofline of the dominant call ----
-    peak, peak_kind = _peaks()
-    nvel_bytes = sum(v.size * 8 for v in cfg["V"])
-    slots_per_live = p.max_xcell * int(np.prod(p.ni)) / live
-    gb = nvel_bytes / live
-    fb = T.numel() * 8 / live
-    vb = 4 if f32 else 8  # bytes per value of coordinates/offsets and fields
-    bpp = {op: algorithmic_bytes(op, N, nf, m, slots_per_live, gb * vb / 8, fb * vb / 8, vb) for op in ops}
-    dom = max(op_ms, key=op_ms.get)
-    achieved = bpp[dom] * live / (op_ms[dom] / 1e3) / 1e9
-    step_bytes = sum(bpp.values()) * live
-    step_gbs = step_bytes / (elapsed / args.steps) / 1e9
     # the interpolating kernels are bound by GB300's FP64 issue rate (2 lanes per clock
     # per SM), not by HBM: their FP64 instruction rate against that peak at the sampled clock
     fp64_roof = None
@@ -462,19 +479,7 @@ def run_ours(args, form=None, minimal=False):
         "algorithmic_bytes_per_particle": bpp,
         "step_algorithmic_gbs": step_gbs,
         "fp64_roofline": fp64_roof,
-        "roofline": {
-            "bound": "hbm",
-            "kernel": dom,
-            "achieved": achieved,
-            "peak": peak,
-            "unit": "GB/s",
-            "frac": achieved / peak,
-            "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
-            else "fallback 6.8 TB/s",
-            "traffic": (DRAM_BYTES_PER_PARTICLE_2D_F64[dom] * live / 1e9
-                        if (N == 2 and not f32 and nf == 1) else None),
-            "traffic_unit": "GB per launch, from ncu dram bytes of a 512^2 capture scaled by particle count",
-        },
+        "roofline": roofline,
         "e2e": {
             "value": e2e_value,
             "unit": UNIT,
@@ -500,6 +505,8 @@ def run_ours(args, form=None, minimal=False):
             cmp_steps = 100
             sp["error_vs_fp64"] = run_compare(args, steps=cmp_steps, quiet=True)
         result["split_precision"] = sp
+    if rank == 0 and world == 1 and args.workload == "C2" and args.ni is None and not args.no_extra:
+        result.update(run_c4_c5(args))
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)
     if world > 1:
@@ -608,10 +615,10 @@ def run_compare(args, steps=None, quiet=False):
     print(json.dumps(out))
 
 
-def run_adjoint(args):
+def run_adjoint(args, quiet=False):
     """C5: cost of the checkpointed gradient against the forward run alone,
     and central finite differences (h = 1e-6) on --fd-nodes random velocity
-    nodes, each formed vertex by vertex."""
+    nodes, each formed vertex by vertex. Printed, or returned when ``quiet``."""
     import torch
 
     import justpic_gb300 as jp
@@ -714,7 +721,7 @@ def run_adjoint(args):
             "active": "|fd| >= 1e-3 of max |dL/dV|",
             "pairs_adjoint_fd": [[float(a), float(f)] for a, f in checked[:8]],
         })
-    print(json.dumps({
+    out = {
         "form": "split precision (FP32 offsets, FP64 cotangents)" if args.form == "f32" else "FP64",
         "workload": DESC["C5"] if args.ni is None else DESC["C5"] + f" (resized to {args.ni})",
         "live_particles": live, "steps": nsteps, "checkpoint_every": k, "loss": loss,
@@ -726,7 +733,51 @@ def run_adjoint(args):
         "forward_particle_steps_per_s": live * nsteps / t_fwd,
         "max_abs_gradient": gmax,
         "fd_check": fd_out,
-    }))
+    }
+    if quiet:
+        return out
+    print(json.dumps(out))
+
+
+def run_c4_c5(args):
+    """The figures of the other two GPU configurations, added to the default
+    line: C4 (2048^2, RK4, both forms, a short timed window each, and the
+    position error of the split form after 750 RK2 steps of the miniapp cycle
+    against the FP64 form) and C5 (the adjoint's cost against its forward run,
+    FP64 and FP32 variants)."""
+    import torch
+
+    c4 = argparse.Namespace(**vars(args))
+    c4.workload, c4.ni, c4.method, c4.steps, c4.warmup = "C4", None, None, 10, 3
+    f64 = run_ours(c4, "f64", True)
+    torch.cuda.empty_cache()
+    f32 = run_ours(c4, "f32", True)
+    torch.cuda.empty_cache()
+    rk2 = argparse.Namespace(**vars(c4))
+    rk2.method = "rk2"
+    err = run_compare(rk2, steps=750, quiet=True)
+    torch.cuda.empty_cache()
+    out = {"C4": {
+        "workload": DESC["C4"],
+        "timed_steps": c4.steps,
+        "fp64": {k: f64[k] for k in ("value", "ms_per_step", "per_call_ms", "roofline")},
+        "split": {k: f32[k] for k in ("value", "ms_per_step", "per_call_ms", "roofline")},
+        "speedup_split_vs_fp64": f32["value"] / f64["value"],
+        "error_after_750_rk2_steps": err,
+    }}
+    c5 = argparse.Namespace(**vars(args))
+    c5.workload, c5.ni, c5.adjoint_steps, c5.fd_nodes, c5.steps, c5.warmup = "C5", None, 0, 0, 5, 3
+    keys = ("forward_s", "forward_plus_gradient_s", "gradient_cost_vs_forward",
+            "gradient_cost_vs_forward_one_segment_kept", "records_kept_segments", "live_particles", "steps",
+            "checkpoint_every")
+    c5.form = "f64"
+    a64 = run_adjoint(c5, quiet=True)
+    torch.cuda.empty_cache()
+    c5.form = "f32"
+    a32 = run_adjoint(c5, quiet=True)
+    torch.cuda.empty_cache()
+    out["C5"] = {"workload": DESC["C5"], "fp64": {k: a64[k] for k in keys}, "fp32": {k: a32[k] for k in keys}}
+    return out
 
 
 def _cpu_setup(workload):
@@ -842,6 +893,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-split", action="store_true",
                     help="FP64 line without the split-precision timing and error added to it")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default line without the C4 (both forms) and C5 (adjoint) figures")
     ap.add_argument("--adjoint-steps", type=int, default=0,
                     help="C5: steps of the run (default: the workload's 100)")
     ap.add_argument("--fd-nodes", type=int, default=0,

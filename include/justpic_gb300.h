@@ -209,6 +209,25 @@ int jp_particle2grid(jp_particles* p, double* F, const double* Fp, const double*
                      const uint8_t* index);
 
 /*
+ * The tuple forms, nfields (1 to JP_MAX_ARGS) fields in one call; the
+ * coordinates and the weights are read and formed once for all fields.
+ * jp_grid2particle_n: grid2particle!(Fp::NTuple, F::NTuple, particles)
+ *   (src/Interpolations/grid_to_particle.jl:84-103): live particles with a NaN
+ *   coordinate are skipped, as in the reference's tuple kernel.
+ * jp_particle2grid_n: particle2grid!(F::NTuple, Fp::NTuple, particles)
+ *   (src/Interpolations/particle_to_grid.jl:70-109 (2D), 153-199 (3D)): the
+ *   scalar form's weights and order, one weighted sum per field, each
+ *   normalised as wF * inv(w). (The reference's own tuple kernels stop for
+ *   more than one field: the 2D one indexes a scalar accumulator with the
+ *   field number, the 3D one reads an undefined slot variable; these are the
+ *   sums both spell out.)
+ */
+int jp_grid2particle_n(jp_particles* p, double* const* Fp, const double* const* F, int32_t nfields,
+                       const double* const coords[3], const uint8_t* index);
+int jp_particle2grid_n(jp_particles* p, double* const* F, const double* const* Fp, int32_t nfields,
+                       const double* const coords[3], const uint8_t* index);
+
+/*
  * Transfers beside the hot path, on the same layout (FP64, 2D and 3D):
  * grid2particle_flip!(Fp, xvi, F, F0, particles; α)
  *   (src/Interpolations/grid_to_particle.jl:125-170) with xvi = the container's

@@ -67,6 +67,10 @@ SIGNATURES = [
     ("jp_synchronize", ctypes.c_int, [ctypes.c_void_p]),
     ("jp_get_warnings", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), ctypes.c_int32]),
     ("jp_get_move_counts", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64 * 3, ctypes.c_int32]),
+    ("jp_grid2particle_n", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, P3, ctypes.c_void_p]),
+    ("jp_particle2grid_n", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, P3, ctypes.c_void_p]),
     ("jp_get_rng_counter", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     ("jp_set_rng_counter", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     ("jp_last_error", ctypes.c_char_p, []),

@@ -203,8 +203,31 @@ def _vertex_shape(p: Particles):
     return tuple(n + 1 for n in p.ni)
 
 
-def grid2particle_(Fp: CellArray, F: torch.Tensor, particles: Particles) -> None:
-    """``grid2particle!(Fp, F, particles)``: vertex field -> particles."""
+def _field_lists(a, b, what):
+    a, b = tuple(a), tuple(b)
+    if len(a) != len(b) or not 1 <= len(a) <= _native.JP_MAX_ARGS:
+        raise ArgumentError(f"{what}: the two tuples need the same length, 1 to {_native.JP_MAX_ARGS} fields")
+    return a, b
+
+
+def _ptr_array(xs):
+    return (ctypes.c_void_p * len(xs))(*[x.data_ptr() for x in xs])
+
+
+def grid2particle_(Fp, F, particles: Particles) -> None:
+    """``grid2particle!(Fp, F, particles)``: vertex field -> particles. With
+    tuples ``Fp`` and ``F`` the tuple form (grid_to_particle.jl:84-103): all
+    fields in one call, live particles with a NaN coordinate skipped."""
+    if isinstance(Fp, (tuple, list)):
+        Fps, Fs = _field_lists(Fp, F, "grid2particle!")
+        for k, (fp, f) in enumerate(zip(Fps, Fs)):
+            _check_cellarray(particles, fp, f"Fp[{k}]")
+            _check_grid(f, _vertex_shape(particles), f"F[{k}]")
+        _bind_stream(particles)
+        rc = _native.load().jp_grid2particle_n(particles.handle, _ptr_array(Fps), _ptr_array(Fs), len(Fs),
+                                               _coords(particles), particles.index.data_ptr())
+        _finish(particles, rc, "grid2particle!")
+        return
     _check_cellarray(particles, Fp, "Fp")
     _check_grid(F, _vertex_shape(particles), "F")
     _bind_stream(particles)
@@ -213,8 +236,20 @@ def grid2particle_(Fp: CellArray, F: torch.Tensor, particles: Particles) -> None
     _finish(particles, rc, "grid2particle!")
 
 
-def particle2grid_(F: torch.Tensor, Fp: CellArray, particles: Particles) -> None:
-    """``particle2grid!(F, Fp, particles)``: particles -> vertex field."""
+def particle2grid_(F, Fp, particles: Particles) -> None:
+    """``particle2grid!(F, Fp, particles)``: particles -> vertex field. With
+    tuples ``F`` and ``Fp`` the tuple form (particle_to_grid.jl:70-109,
+    153-199): the weights are formed once for all fields."""
+    if isinstance(F, (tuple, list)):
+        Fs, Fps = _field_lists(F, Fp, "particle2grid!")
+        for k, (f, fp) in enumerate(zip(Fs, Fps)):
+            _check_cellarray(particles, fp, f"Fp[{k}]")
+            _check_grid(f, _vertex_shape(particles), f"F[{k}]")
+        _bind_stream(particles)
+        rc = _native.load().jp_particle2grid_n(particles.handle, _ptr_array(Fs), _ptr_array(Fps), len(Fs),
+                                               _coords(particles), particles.index.data_ptr())
+        _finish(particles, rc, "particle2grid!")
+        return
     _check_cellarray(particles, Fp, "Fp")
     _check_grid(F, _vertex_shape(particles), "F")
     _bind_stream(particles)

@@ -839,4 +839,33 @@ int jp_particle2grid(jp_particles* P, double* F, const double* Fp, const double*
     return finish(P, jp::launch_p2g(P, F, Fp, coords, index), "jp_particle2grid");
 }
 
+static int check_field_lists(const void* const* a, const void* const* b, int32_t nfields, const char* what)
+{
+    if (nfields < 1 || nfields > JP_MAX_ARGS || !a || !b)
+        return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": bad field list (1 to JP_MAX_ARGS fields)");
+    for (int k = 0; k < nfields; ++k)
+        if (!a[k] || !b[k]) return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": null field");
+    return JP_OK;
+}
+
+int jp_particle2grid_n(jp_particles* P, double* const* F, const double* const* Fp, int32_t nfields,
+                       const double* const coords[3], const uint8_t* index)
+{
+    if (!P || !index || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_n: null pointer");
+    int rc = check_field_lists((const void* const*)F, (const void* const*)Fp, nfields, "jp_particle2grid_n");
+    if (rc) return rc;
+    return finish(P, jp::launch_p2g_n(P, F, Fp, nfields, coords, index), "jp_particle2grid_n");
+}
+
+int jp_grid2particle_n(jp_particles* P, double* const* Fp, const double* const* F, int32_t nfields,
+                       const double* const coords[3], const uint8_t* index)
+{
+    if (!P || !index || !check_coords(P, (const void* const*)coords))
+        return fail(JP_ERR_INVALID_ARGUMENT, "jp_grid2particle_n: null pointer");
+    int rc = check_field_lists((const void* const*)Fp, (const void* const*)F, nfields, "jp_grid2particle_n");
+    if (rc) return rc;
+    return finish(P, jp::launch_g2p_n(P, Fp, F, nfields, coords, index), "jp_grid2particle_n");
+}
+
 }  // extern "C"

@@ -614,8 +614,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 }
 
 // ------------------------------------------------------- particle2grid!
-// Same marching scheme and accumulation order as the FP64 kernel; weights in
-// FP32, their sums (and the weighted field sums) at FP64 accuracy: within one
+// The FP64 form's accumulation order (per vertex: cells with the offsets of
+// the last axis outermost, x innermost, slots in order); weights in FP32, their sums (and the weighted field sums) at FP64 accuracy: within one
 // cell the terms are summed as compensated FP32 pairs (error-free TwoSum and
 // TwoProduct, Knuth / Dekker), and each cell's pair is added to the vertex's
 // FP64 accumulators. For the <= 64 terms of a cell the pair keeps the sum to
@@ -647,128 +647,217 @@ __device__ __forceinline__ void csum_add_prod(CSum& s, float a, float b)
 
 __device__ __forceinline__ double csum_value(const CSum& s) { return (double)s.h + (double)s.l; }
 
-template <int DIM>
-__device__ __forceinline__ void p2g_cell_f32(int64_t c, uint64_t mask, int64_t nc, const float* kc, const float* kn,
-                                             bool do_cur, bool do_nxt, const float* dx,
-                                             const float* __restrict__ Fp, const CXiF& Xi, double& w_c, double& wF_c,
-                                             double& w_n, double& wF_n)
+// Cell-centric form of the same sums: one lane per cell, a warp on 32
+// consecutive cells of a cell row (lane 0 is the column to the left of the
+// warp's vertex columns), marching up the rows of a band. The warp walks each
+// cell row's slot rows up to its highest live slot (coalesced rows, four in
+// flight per lane), so every particle is read once per band; per particle it
+// forms the weights of the cell's 2^N corners and adds them to one compensated
+// pair per corner, in slot order (the pair of a (vertex, cell)). A vertex then
+// adds its cells' pairs in the reference's cell order in FP64: the lower
+// corners of a cell row finish the vertex row below it, the upper corners
+// start the row above. No cell is read again for each of its vertices.
+__device__ __forceinline__ float p2g_w_f32(float qx, float e) { return __frcp_rn(fmaf(e, e, qx)); }
+
+static __global__ void __launch_bounds__(kThreads)
+    p2g_f32_cells2d(DevGrid g, F32Params P, float* __restrict__ F, const float* __restrict__ Fp, CXiF Xi,
+                    const uint8_t* __restrict__ index, int chunk, double* __restrict__ Wout)
 {
-    CSum sw_c, sF_c, sw_n, sF_n;
-    while (mask) {
-        const int s = __ffsll((long long)mask) - 1;
-        mask &= mask - 1;
-        const int64_t a = c + nc * s;
-        float xi[3];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t n0 = g.n[0], n1 = g.n[1], V0 = n0 + 1, nc = g.ncells;
+    const int64_t wcols = (V0 + 30) / 31;
+    const int64_t band = warp / wcols, wc = warp - band * wcols;
+    const int64_t r0 = band * chunk;
+    if (r0 > n1) return;  // the whole warp
+    const int64_t r1 = min(r0 + (int64_t)chunk, n1 + 1);  // vertex rows [r0, r1)
+    const int64_t ci = wc * 31 + lane - 1;                 // this lane's cell column
+    const bool col_ok = ci >= 0 && ci < n0;
+    const bool out_ok = lane >= 1 && ci < V0;             // lanes 1..31 own vertex column ci
+    const int M = g.max_xcell;
+    const float dx = P.dx[0], dy = P.dx[1];
+    double w_acc = 0.0, f_acc = 0.0;  // the vertex (ci, cr) being summed
+    for (int64_t cr = r0 - 1; cr < r1; ++cr) {
+        const bool cell_ok = col_ok && cr >= 0 && cr < n1;
+        const int64_t c = cell_ok ? ci + n0 * cr : 0;
+        const uint64_t L = cell_ok ? live_mask(index, c, nc, M) : 0;
+        const int hi = (int)__reduce_max_sync(full, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
+        // corners (0,0), (1,0), (0,1), (1,1) of the cell in cell units
+        CSum w00, f00, w10, f10, w01, f01, w11, f11;
+        constexpr int B = 4;
+        for (int s0 = 0; s0 < hi; s0 += B) {
+            float x[B], y[B], f[B];
+            bool lv[B];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) xi[d] = Xi.x[d][a];
-        const float f = Fp[a];
-        if (do_cur) {
-            float ss = 0.0f;
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const float e = (kc[d] - xi[d]) * dx[d];
-                ss = fmaf(e, e, ss);
+            for (int u = 0; u < B; ++u) {
+                const int s = s0 + u;
+                lv[u] = s < hi && ((L >> s) & 1);
+                const int64_t a = c + nc * s;
+                x[u] = lv[u] ? Xi.x[0][a] : 0.0f;
+                y[u] = lv[u] ? Xi.x[1][a] : 0.0f;
+                f[u] = lv[u] ? Fp[a] : 0.0f;
             }
-            const float wi = __frcp_rn(ss);
-            csum_add(sw_c, wi);
-            csum_add_prod(sF_c, wi, f);
-        }
-        if (do_nxt) {
-            float ss = 0.0f;
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const float e = (kn[d] - xi[d]) * dx[d];
-                ss = fmaf(e, e, ss);
+            for (int u = 0; u < B; ++u) {
+                if (!lv[u]) continue;
+                // distance^2 = fmaf(ey, ey, ex * ex), e = (corner - xi) * dx per axis
+                const float ex0 = (0.0f - x[u]) * dx, ex1 = (1.0f - x[u]) * dx;
+                const float ey0 = (0.0f - y[u]) * dy, ey1 = (1.0f - y[u]) * dy;
+                const float qx0 = fmaf(ex0, ex0, 0.0f), qx1 = fmaf(ex1, ex1, 0.0f);
+                const float a00 = p2g_w_f32(qx0, ey0), a10 = p2g_w_f32(qx1, ey0);
+                const float a01 = p2g_w_f32(qx0, ey1), a11 = p2g_w_f32(qx1, ey1);
+                csum_add(w00, a00);
+                csum_add_prod(f00, a00, f[u]);
+                csum_add(w10, a10);
+                csum_add_prod(f10, a10, f[u]);
+                csum_add(w01, a01);
+                csum_add_prod(f01, a01, f[u]);
+                csum_add(w11, a11);
+                csum_add_prod(f11, a11, f[u]);
             }
-            const float wi = __frcp_rn(ss);
-            csum_add(sw_n, wi);
-            csum_add_prod(sF_n, wi, f);
         }
-    }
-    if (do_cur) {
-        w_c += csum_value(sw_c);
-        wF_c += csum_value(sF_c);
-    }
-    if (do_nxt) {
-        w_n += csum_value(sw_n);
-        wF_n += csum_value(sF_n);
+        // vertex (ci, cr), the lower side of this cell row: its cells (ci-1, cr-1) and (ci, cr-1) are in
+        // the accumulators; (ci-1, cr) [corner (1,0) of the lane to the left] and (ci, cr) [corner (0,0)] follow
+        const double lw10 = __shfl_up_sync(full, csum_value(w10), 1), lf10 = __shfl_up_sync(full, csum_value(f10), 1);
+        if (cr >= r0) {
+            w_acc += lw10;
+            f_acc += lf10;
+            w_acc += csum_value(w00);
+            f_acc += csum_value(f00);
+            if (out_ok) {
+                const int64_t v = ci + V0 * cr;
+                F[v] = (float)(f_acc / w_acc);
+                if (Wout) Wout[v] = w_acc;
+            }
+        }
+        // vertex (ci, cr + 1), the upper side: (ci-1, cr) [corner (1,1) to the left], then (ci, cr) [corner (0,1)]
+        const double lw11 = __shfl_up_sync(full, csum_value(w11), 1), lf11 = __shfl_up_sync(full, csum_value(f11), 1);
+        w_acc = 0.0 + lw11;
+        f_acc = 0.0 + lf11;
+        w_acc += csum_value(w01);
+        f_acc += csum_value(f01);
     }
 }
 
-template <int DIM>
-__global__ void __launch_bounds__(kThreads)
-    p2g_f32_kernel(DevGrid g, F32Params P, float* __restrict__ F, const float* __restrict__ Fp, CXiF Xi,
-                   const uint8_t* __restrict__ index, int chunk, int64_t nthreads, double* __restrict__ Wout)
+// The 3D cell-centric sums: a block of 8 warps covers 8 consecutive cell rows
+// along y (warp 0 the row below the block's vertex rows), each warp 32 cells
+// along x (lane 0 the column to the left), marching up a band of z rows. Each
+// lane forms its cell's 8 corner pairs per z row; a vertex adds, per z row in
+// the reference's order, the pairs of its cells (i-1, j-1), (i, j-1) (from the
+// warp below, through shared memory), (i-1, j) (the lane to the left) and
+// (i, j) (its own): the lower corners finish the vertex row of this z row, the
+// upper corners start the next one.
+static __global__ void __launch_bounds__(kThreads)
+    p2g_f32_cells3d(DevGrid g, F32Params P, float* __restrict__ F, const float* __restrict__ Fp, CXiF Xi,
+                    const uint8_t* __restrict__ index, int band, double* __restrict__ Wout)
 {
-    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
-    constexpr int LAST = DIM - 1;
-    const int64_t nlast = g.n[LAST];
-    const int64_t cols = DIM == 2 ? V0 : V0 * V1;
-    const int64_t nc = g.ncells;
+    // the corners (cx, 1, cz) of every lane's cell, as (w, wF): [warp][lane][cx][cz][2]
+    __shared__ double up[kWarpsPerBlock][32][2][2][2];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t n0 = g.n[0], n1 = g.n[1], n2 = g.n[2], V0 = n0 + 1, V1 = n1 + 1, nc = g.ncells;
+    const int64_t wcols = (V0 + 30) / 31, jgroups = (V1 + 6) / 7;
+    const int64_t b = blockIdx.x;
+    const int64_t wc = b % wcols, jg = (b / wcols) % jgroups, kb = b / (wcols * jgroups);
+    const int64_t r0 = kb * band;
+    if (r0 > n2) return;  // the whole block
+    const int64_t r1 = min(r0 + (int64_t)band, n2 + 1);  // vertex rows along z: [r0, r1)
+    const int64_t ci = wc * 31 + lane - 1, cj = jg * 7 + w - 1;
+    const bool colrow_ok = ci >= 0 && ci < n0 && cj >= 0 && cj < n1;
+    const bool out_ok = lane >= 1 && w >= 1 && ci < V0 && cj < V1;  // vertex (ci, cj, .)
     const int M = g.max_xcell;
-    const bool active = t < nthreads;
-    const int64_t col = active ? t % cols : 0;
-    const int64_t q = active ? t / cols : 0;
-    const int64_t r0 = q * chunk;
-    const int64_t r1 = active ? min(r0 + (int64_t)chunk, nlast + 1) : r0;
-    const int64_t i = col % V0;
-    const int64_t j = DIM == 3 ? col / V0 : 0;
-    const bool has_i0 = i >= 1, has_i1 = i < g.n[0];
-    const bool has_j0 = DIM == 2 || j >= 1, has_j1 = DIM == 2 || j < g.n[1];
-    auto cell = [&](int di, int dj, int64_t r) -> int64_t {
-        return DIM == 2 ? (i + di) + g.n[0] * r : (i + di) + g.n[0] * ((j + dj) + g.n[1] * r);
-    };
-    // vertex position relative to a cell's lower-left corner, in cell units:
-    // the own cell (i, j) sees the vertex at 0, the cell to the left at 1, ...
-    auto row = [&](int64_t r, bool do_cur, bool do_nxt, double& w_c, double& wF_c, double& w_n, double& wF_n) {
-        const bool rok = active && r >= 0 && r < nlast;
-        const uint64_t m_own = (rok && has_i1 && has_j1) ? live_mask(index, cell(0, 0, r), nc, M) : 0;
-        uint64_t m_left = __shfl_up_sync(0xffffffffu, m_own, 1);
-        if (lane == 0 && rok && has_i0 && has_j1) m_left = live_mask(index, cell(-1, 0, r), nc, M);
-        if (!(rok && has_i0 && has_j1)) m_left = 0;
-        // the current vertex row is the cell row's lower side (0), the next one its upper side (1)
-        float kc[3], kn[3];
-        if (DIM == 3) {
-            const uint64_t mb0 = (rok && has_i0 && has_j0) ? live_mask(index, cell(-1, -1, r), nc, M) : 0;
-            const uint64_t mb1 = (rok && has_i1 && has_j0) ? live_mask(index, cell(0, -1, r), nc, M) : 0;
-            kc[1] = kn[1] = 1.0f;
-            kc[2] = 0.0f;
-            kn[2] = 1.0f;
-            kc[0] = kn[0] = 1.0f;
-            if (mb0) p2g_cell_f32<DIM>(cell(-1, -1, r), mb0, nc, kc, kn, do_cur, do_nxt, P.dx, Fp, Xi, w_c, wF_c, w_n, wF_n);
-            kc[0] = kn[0] = 0.0f;
-            if (mb1) p2g_cell_f32<DIM>(cell(0, -1, r), mb1, nc, kc, kn, do_cur, do_nxt, P.dx, Fp, Xi, w_c, wF_c, w_n, wF_n);
-            kc[1] = kn[1] = 0.0f;
-        } else {
-            kc[1] = 0.0f;
-            kn[1] = 1.0f;
+    const float dx = P.dx[0], dy = P.dx[1], dz = P.dx[2];
+    double w_acc = 0.0, f_acc = 0.0;
+    for (int64_t cr = r0 - 1; cr < r1; ++cr) {
+        const bool cell_ok = colrow_ok && cr >= 0 && cr < n2;
+        const int64_t c = cell_ok ? ci + n0 * (cj + n1 * cr) : 0;
+        const uint64_t L = cell_ok ? live_mask(index, c, nc, M) : 0;
+        const int hi = (int)__reduce_max_sync(full, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
+        CSum cw[2][2][2], cf[2][2][2];  // [cx][cy][cz]
+        constexpr int B = 4;
+        for (int s0 = 0; s0 < hi; s0 += B) {
+            float x[B], y[B], z[B], f[B];
+            bool lv[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                const int s = s0 + u;
+                lv[u] = s < hi && ((L >> s) & 1);
+                const int64_t a = c + nc * s;
+                x[u] = lv[u] ? Xi.x[0][a] : 0.0f;
+                y[u] = lv[u] ? Xi.x[1][a] : 0.0f;
+                z[u] = lv[u] ? Xi.x[2][a] : 0.0f;
+                f[u] = lv[u] ? Fp[a] : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                if (!lv[u]) continue;
+                float qx[2], ey[2], ez[2];
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const float ex = ((float)k - x[u]) * dx;
+                    qx[k] = fmaf(ex, ex, 0.0f);
+                    ey[k] = ((float)k - y[u]) * dy;
+                    ez[k] = ((float)k - z[u]) * dz;
+                }
+#pragma unroll
+                for (int kx = 0; kx < 2; ++kx)
+#pragma unroll
+                    for (int ky = 0; ky < 2; ++ky) {
+                        const float qxy = fmaf(ey[ky], ey[ky], qx[kx]);
+#pragma unroll
+                        for (int kz = 0; kz < 2; ++kz) {
+                            const float wi = __frcp_rn(fmaf(ez[kz], ez[kz], qxy));
+                            csum_add(cw[kx][ky][kz], wi);
+                            csum_add_prod(cf[kx][ky][kz], wi, f[u]);
+                        }
+                    }
+            }
         }
-        kc[0] = kn[0] = 1.0f;
-        if (m_left) p2g_cell_f32<DIM>(cell(-1, 0, r), m_left, nc, kc, kn, do_cur, do_nxt, P.dx, Fp, Xi, w_c, wF_c, w_n, wF_n);
-        kc[0] = kn[0] = 0.0f;
-        if (m_own) p2g_cell_f32<DIM>(cell(0, 0, r), m_own, nc, kc, kn, do_cur, do_nxt, P.dx, Fp, Xi, w_c, wF_c, w_n, wF_n);
-    };
-    double w_c = 0.0, wF_c = 0.0, w_n = 0.0, wF_n = 0.0;
-    {
-        double wd = 0.0, wFd = 0.0;
-        row(r0 - 1, false, true, wd, wFd, w_c, wF_c);
-    }
-    for (int k = 0; k < chunk; ++k) {
-        const int64_t r = r0 + k;
-        const bool vok = r < r1;
-        const bool has_next = r + 1 < r1;
-        w_n = 0.0;
-        wF_n = 0.0;
-        row(vok ? r : -1, vok, has_next, w_c, wF_c, w_n, wF_n);
-        if (vok) {
-            const int64_t v = DIM == 2 ? i + V0 * r : i + V0 * (j + V1 * r);
-            F[v] = (float)(wF_c / w_c);
-            if (Wout) Wout[v] = w_c;
+#pragma unroll
+        for (int kx = 0; kx < 2; ++kx)
+#pragma unroll
+            for (int kz = 0; kz < 2; ++kz) {
+                up[w][lane][kx][kz][0] = csum_value(cw[kx][1][kz]);
+                up[w][lane][kx][kz][1] = csum_value(cf[kx][1][kz]);
+            }
+        __syncthreads();
+        const int wb = w >= 1 ? w - 1 : 0, lb = lane >= 1 ? lane - 1 : 0;
+#pragma unroll
+        for (int kz = 0; kz < 2; ++kz) {
+            // cells (i-1, j-1), (i, j-1), (i-1, j), (i, j) of this z row, lower (kz = 0) or upper (kz = 1) corners
+            const double a_w = up[wb][lb][1][kz][0], a_f = up[wb][lb][1][kz][1];
+            const double b_w = up[wb][lane][0][kz][0], b_f = up[wb][lane][0][kz][1];
+            const double c_w = __shfl_up_sync(full, csum_value(cw[1][0][kz]), 1);
+            const double c_f = __shfl_up_sync(full, csum_value(cf[1][0][kz]), 1);
+            if (kz == 0) {
+                if (cr >= r0) {
+                    w_acc += a_w;
+                    f_acc += a_f;
+                    w_acc += b_w;
+                    f_acc += b_f;
+                    w_acc += c_w;
+                    f_acc += c_f;
+                    w_acc += csum_value(cw[0][0][0]);
+                    f_acc += csum_value(cf[0][0][0]);
+                    if (out_ok) {
+                        const int64_t v = ci + V0 * (cj + V1 * cr);
+                        F[v] = (float)(f_acc / w_acc);
+                        if (Wout) Wout[v] = w_acc;
+                    }
+                }
+            } else {
+                w_acc = 0.0 + a_w;
+                f_acc = 0.0 + a_f;
+                w_acc += b_w;
+                f_acc += b_f;
+                w_acc += c_w;
+                f_acc += c_f;
+                w_acc += csum_value(cw[0][0][1]);
+                f_acc += csum_value(cf[0][0][1]);
+            }
         }
-        w_c = w_n;
-        wF_c = wF_n;
+        __syncthreads();  // the next z row overwrites `up`
     }
 }
 
@@ -931,17 +1020,23 @@ cudaError_t launch_p2g_f32(jp_particles* P, float* F, const float* Fp, const flo
     CXiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
     const F32Params prm = make_params(P, 0.5, 0.0);
     const int64_t V0 = P->g.n[0] + 1, V1 = P->g.n[1] + 1;
-    const int64_t cols = d3 ? V0 * V1 : V0;
     const int64_t rows = P->g.n[d3 ? 2 : 1] + 1;
-    const int64_t want = 152LL * 2048;
-    int chunk = (int)((cols * rows) / want);
-    chunk = chunk < 2 ? 2 : (chunk > 16 ? 16 : chunk);
-    const int64_t nthreads = cols * ((rows + chunk - 1) / chunk);
-    const unsigned nb = grid_blocks(nthreads);
-    if (!d3)
-        p2g_f32_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, chunk, nthreads, W);
-    else
-        p2g_f32_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, chunk, nthreads, W);
+    if (!d3) {
+        // cell-centric: warps of 31 vertex columns (+ one cell column to the left) over bands of
+        // `band` vertex rows; bands as long as still leave about 4096 warps
+        const int64_t wcols = (V0 + 30) / 31;
+        int band = (int)((wcols * rows) / 4096);
+        band = band < 4 ? 4 : (band > 32 ? 32 : band);
+        const int64_t warps = wcols * ((rows + band - 1) / band);
+        p2g_f32_cells2d<<<grid_blocks(warps * 32), kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, band, W);
+    } else {
+        // blocks of 31 x 7 vertex columns over bands of z rows, as long as still leave about 1024 blocks
+        const int64_t wcols = (V0 + 30) / 31, jgroups = (V1 + 6) / 7;
+        int band = (int)((wcols * jgroups * rows) / 1024);
+        band = band < 4 ? 4 : (band > 32 ? 32 : band);
+        const int64_t blocks = wcols * jgroups * ((rows + band - 1) / band);
+        p2g_f32_cells3d<<<(unsigned)blocks, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, band, W);
+    }
     return cudaGetLastError();
 }
 

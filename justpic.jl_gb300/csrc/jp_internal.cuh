@@ -365,6 +365,11 @@ cudaError_t launch_advection_vjp_recorded(jp_particles* P, int method, double al
                                           const uint8_t* index, double* const lam[3], double* const gV[3]);
 cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
                        const uint8_t* index, double* W = nullptr);
+// the tuple forms of particle2grid! and grid2particle! (nf fields)
+cudaError_t launch_p2g_n(jp_particles* P, double* const* F, const double* const* Fp, int nf,
+                         const double* const coords[3], const uint8_t* index);
+cudaError_t launch_g2p_n(jp_particles* P, double* const* Fp, const double* const* F, int nf,
+                         const double* const coords[3], const uint8_t* index);
 
 // adjoint (jp_adjoint.cu), 2D
 cudaError_t launch_move_permutation(jp_particles* P, int32_t* dest);

@@ -434,6 +434,80 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     }
 }
 
+constexpr int kFieldsPerLaunchG2P = 4;
+
+// grid2particle! with a tuple of fields (src/Interpolations/grid_to_particle.jl:
+// 84-103): a live particle with a NaN coordinate is skipped; every other one
+// forms its normalised coordinates once and interpolates each field's corner
+// values (loaded through the read-only cache: the warp's particles share the
+// corners of its 32 cells).
+struct G2PFields {
+    const double* f[kFieldsPerLaunchG2P];
+    double* fp[kFieldsPerLaunchG2P];
+};
+
+template <int DIM, int NF>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    g2p_n_kernel(DevGrid g, G2PFields GF, CCoords X, const uint8_t* __restrict__ index)
+{
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ double cellx[kWarpsPerBlock][32][2 * DIM];
+    __shared__ int64_t cellb[kWarpsPerBlock][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1, SZ = V0 * V1;
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+        cellb[w][lane] = I[0] + V0 * (I[1] + (DIM == 3 ? V1 * I[2] : 0));
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            cellx[w][lane][d] = ldg(g.xv[d] + I[d]);
+            cellx[w][lane][DIM + d] = ldg(g.ixv[d] + I[d]);
+        }
+    }
+    for (int s0 = 0; s0 < M; s0 += 64) {  // slots in chunks of 64
+        const int Mc = min(64, M - s0);
+        uint64_t mine;
+        const int K = build_slot_list(lists[w], index + nc * s0, c0, nc, Mc, lane, &mine);
+        for (int k = lane; k < K; k += 32) {
+            int s, l;
+            slot_item(lists[w], Mc, k, &s, &l);
+            const int64_t a = c0 + l + nc * (s0 + s);
+            double t[3];
+            bool nan = false;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const double x = X.c[d][a];
+                nan |= is_nan_bits(x);
+                t[d] = (x - cellx[w][l][d]) * cellx[w][l][DIM + d];
+            }
+            if (nan) continue;  // any(isnan, pᵢ) && continue
+            const int64_t b = cellb[w][l];
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                const double* F = GF.f[f];
+                double v[8];
+                v[0] = ldg(F + b);
+                v[1] = ldg(F + b + 1);
+                v[2] = ldg(F + b + V0);
+                v[3] = ldg(F + b + V0 + 1);
+                if (DIM == 3) {
+                    v[4] = ldg(F + b + SZ);
+                    v[5] = ldg(F + b + SZ + 1);
+                    v[6] = ldg(F + b + SZ + V0);
+                    v[7] = ldg(F + b + SZ + V0 + 1);
+                }
+                GF.fp[f][a] = lerpN<DIM>(v, t);
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // ------------------------------------------------------- particle2grid!
 // src/Interpolations/particle_to_grid.jl:37-68 (2D), :113-151 (3D).
 // One thread per vertex column marching along the last axis over `chunk`
@@ -444,11 +518,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 // cell is walked through its 64-bit live mask, so no lane spends FP64 issue
 // slots on empty slots; the mask of the left neighbour cell comes from the
 // neighbouring lane. The loop trip count is the same for every lane of a warp.
-template <int DIM>
+// Fields of a particle2grid! call: one for the scalar form, up to four per
+// launch for the tuple form (particle_to_grid.jl:70-109, 153-199).
+constexpr int kFieldsPerLaunch = 4;
+struct P2GFields {
+    const double* fp[kFieldsPerLaunch];
+    double* f[kFieldsPerLaunch];
+};
+
+template <int DIM, int NF>
 __device__ __forceinline__ void p2g_cell(int64_t c, uint64_t mask, int64_t nc, const double* q_cur,
-                                         const double* q_nxt, bool do_cur, bool do_nxt,
-                                         const double* __restrict__ Fp, const CCoords& X, double& w_c,
-                                         double& wF_c, double& w_n, double& wF_n)
+                                         const double* q_nxt, bool do_cur, bool do_nxt, const P2GFields& PF,
+                                         const CCoords& X, double& w_c, double* wF_c, double& w_n, double* wF_n)
 {
     while (mask) {
         const int s = __ffsll((long long)mask) - 1;
@@ -457,7 +538,9 @@ __device__ __forceinline__ void p2g_cell(int64_t c, uint64_t mask, int64_t nc, c
         double p[3];
 #pragma unroll
         for (int d = 0; d < DIM; ++d) p[d] = X.c[d][a];
-        const double f = Fp[a];
+        double f[NF];
+#pragma unroll
+        for (int k = 0; k < NF; ++k) f[k] = PF.fp[k][a];
         // the two vertices share the column (x in 2D, x and y in 3D): those terms of
         // distance(xv, p)^2 = ((x - px)^2 + (y - py)^2) [+ (z - pz)^2] are formed once
         const double dx = q_cur[0] - p[0];
@@ -475,20 +558,25 @@ __device__ __forceinline__ void p2g_cell(int64_t c, uint64_t mask, int64_t nc, c
         if (do_cur) {
             const double wi = inv_dist2(shared + ec * ec);  // inv(distance^2), particle_to_grid.jl:203-205
             w_c += wi;
-            wF_c = fma(wi, f, wF_c);
+#pragma unroll
+            for (int k = 0; k < NF; ++k) wF_c[k] = fma(wi, f[k], wF_c[k]);
         }
         if (do_nxt) {
             const double wi = inv_dist2(shared + en * en);
             w_n += wi;
-            wF_n = fma(wi, f, wF_n);
+#pragma unroll
+            for (int k = 0; k < NF; ++k) wF_n[k] = fma(wi, f[k], wF_n[k]);
         }
     }
 }
 
-template <int DIM>
+// TUPLE: the tuple form's normalisation, F[k] = wF[k] * inv(w) for every field
+// (particle_to_grid.jl:103-108, 193-198); otherwise the scalar form's wF / w in
+// 2D (:67) and wF * inv(w) in 3D (:150).
+template <int DIM, int NF, bool TUPLE>
 __global__ void __launch_bounds__(kThreads)
-    p2g_kernel(DevGrid g, double* __restrict__ F, const double* __restrict__ Fp, CCoords X,
-               const uint8_t* __restrict__ index, int chunk, int64_t nthreads, double* __restrict__ Wout)
+    p2g_kernel(DevGrid g, P2GFields PF, CCoords X, const uint8_t* __restrict__ index, int chunk, int64_t nthreads,
+               double* __restrict__ Wout)
 {
     const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -516,7 +604,7 @@ __global__ void __launch_bounds__(kThreads)
         return DIM == 2 ? (i + di) + g.n[0] * r : (i + di) + g.n[0] * ((j + dj) + g.n[1] * r);
     };
     // accumulate row r into (cur, nxt): cells in reference order
-    auto row = [&](int64_t r, bool do_cur, bool do_nxt, double& w_c, double& wF_c, double& w_n, double& wF_n) {
+    auto row = [&](int64_t r, bool do_cur, bool do_nxt, double& w_c, double* wF_c, double& w_n, double* wF_n) {
         const bool rok = active && r >= 0 && r < nlast;
         // own cell (i, j, r) and its left neighbour (i-1, j, r) from the lane to the left
         const uint64_t m_own = (rok && has_i1 && has_j1) ? live_mask(index, cell(0, 0, r), nc, M) : 0;
@@ -527,18 +615,22 @@ __global__ void __launch_bounds__(kThreads)
             // row j-1 first (joffset = -1), then row j
             const uint64_t mb0 = (rok && has_i0 && has_j0) ? live_mask(index, cell(-1, -1, r), nc, M) : 0;
             const uint64_t mb1 = (rok && has_i1 && has_j0) ? live_mask(index, cell(0, -1, r), nc, M) : 0;
-            if (mb0) p2g_cell<DIM>(cell(-1, -1, r), mb0, nc, q_cur, q_nxt, do_cur, do_nxt, Fp, X, w_c, wF_c, w_n, wF_n);
-            if (mb1) p2g_cell<DIM>(cell(0, -1, r), mb1, nc, q_cur, q_nxt, do_cur, do_nxt, Fp, X, w_c, wF_c, w_n, wF_n);
+            if (mb0) p2g_cell<DIM, NF>(cell(-1, -1, r), mb0, nc, q_cur, q_nxt, do_cur, do_nxt, PF, X, w_c, wF_c, w_n, wF_n);
+            if (mb1) p2g_cell<DIM, NF>(cell(0, -1, r), mb1, nc, q_cur, q_nxt, do_cur, do_nxt, PF, X, w_c, wF_c, w_n, wF_n);
         }
-        if (m_left) p2g_cell<DIM>(cell(-1, 0, r), m_left, nc, q_cur, q_nxt, do_cur, do_nxt, Fp, X, w_c, wF_c, w_n, wF_n);
-        if (m_own) p2g_cell<DIM>(cell(0, 0, r), m_own, nc, q_cur, q_nxt, do_cur, do_nxt, Fp, X, w_c, wF_c, w_n, wF_n);
+        if (m_left) p2g_cell<DIM, NF>(cell(-1, 0, r), m_left, nc, q_cur, q_nxt, do_cur, do_nxt, PF, X, w_c, wF_c, w_n, wF_n);
+        if (m_own) p2g_cell<DIM, NF>(cell(0, 0, r), m_own, nc, q_cur, q_nxt, do_cur, do_nxt, PF, X, w_c, wF_c, w_n, wF_n);
     };
 
-    double w_c = 0.0, wF_c = 0.0, w_n = 0.0, wF_n = 0.0;
+    double w_c = 0.0, w_n = 0.0, wF_c[NF], wF_n[NF];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) wF_c[k] = wF_n[k] = 0.0;
     // prologue: row r0-1 is the lower half of vertex r0's stencil
     if (active && r0 >= 1) q_nxt[LAST] = ldg(g.xv[LAST] + r0);
     {
-        double wd = 0.0, wFd = 0.0;
+        double wd = 0.0, wFd[NF];
+#pragma unroll
+        for (int k = 0; k < NF; ++k) wFd[k] = 0.0;
         row(r0 - 1, false, true, wd, wFd, w_c, wF_c);
     }
     for (int k = 0; k < chunk; ++k) {
@@ -548,25 +640,33 @@ __global__ void __launch_bounds__(kThreads)
         if (vok) q_cur[LAST] = ldg(g.xv[LAST] + r);
         if (has_next) q_nxt[LAST] = ldg(g.xv[LAST] + r + 1);
         w_n = 0.0;
-        wF_n = 0.0;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) wF_n[f] = 0.0;
         row(vok ? r : -1, vok, has_next, w_c, wF_c, w_n, wF_n);
         if (vok) {
             const int64_t v = DIM == 2 ? i + V0 * r : i + V0 * (j + V1 * r);
-            F[v] = DIM == 2 ? wF_c / w_c : wF_c * __drcp_rn(w_c);
+            if (TUPLE || DIM == 3) {
+                const double iw = __drcp_rn(w_c);
+#pragma unroll
+                for (int f = 0; f < NF; ++f) PF.f[f][v] = wF_c[f] * iw;
+            } else {
+                PF.f[0][v] = wF_c[0] / w_c;
+            }
             if (Wout) Wout[v] = w_c;  // weight sums, kept for the adjoint
         }
         w_c = w_n;
-        wF_c = wF_n;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) wF_c[f] = wF_n[f];
     }
 }
 
 // particle2grid! for cells of more than 64 slots: one thread per vertex, the
 // cells of its stencil and their slots in the reference's order (the same sums
 // as p2g_kernel, without the per-cell bit masks).
-template <int DIM>
+template <int DIM, bool TUPLE>
 __global__ void __launch_bounds__(kThreads)
-    p2g_wide_kernel(DevGrid g, double* __restrict__ F, const double* __restrict__ Fp, CCoords X,
-                    const uint8_t* __restrict__ index, double* __restrict__ Wout)
+    p2g_wide_kernel(DevGrid g, P2GFields PF, int nf, CCoords X, const uint8_t* __restrict__ index,
+                    double* __restrict__ Wout)
 {
     const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1, V2 = DIM == 3 ? g.n[2] + 1 : 1;
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -577,7 +677,7 @@ __global__ void __launch_bounds__(kThreads)
     q[0] = ldg(g.xv[0] + i);
     q[1] = ldg(g.xv[1] + j);
     q[2] = DIM == 3 ? ldg(g.xv[2] + k) : 0.0;
-    double w = 0.0, wF = 0.0;
+    double w = 0.0, wF[kFieldsPerLaunch] = {0.0, 0.0, 0.0, 0.0};
     for (int ko = (DIM == 3 ? -1 : 0); ko <= 0; ++ko) {
         const int64_t kc = k + ko;
         if (DIM == 3 && !(0 <= kc && kc < g.n[2])) continue;
@@ -601,12 +701,21 @@ __global__ void __launch_bounds__(kThreads)
                     }
                     const double wi = inv_dist2(ss);
                     w += wi;
-                    wF = fma(wi, Fp[a], wF);
+#pragma unroll
+                    for (int f = 0; f < kFieldsPerLaunch; ++f)
+                        if (f < nf) wF[f] = fma(wi, PF.fp[f][a], wF[f]);
                 }
             }
         }
     }
-    F[v] = DIM == 2 ? wF / w : wF * __drcp_rn(w);
+    if (TUPLE || DIM == 3) {
+        const double iw = __drcp_rn(w);
+#pragma unroll
+        for (int f = 0; f < kFieldsPerLaunch; ++f)
+            if (f < nf) PF.f[f][v] = wF[f] * iw;
+    } else {
+        PF.f[0][v] = wF[0] / w;
+    }
     if (Wout) Wout[v] = w;
 }
 
@@ -750,20 +859,15 @@ cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const doubl
     return cudaGetLastError();
 }
 
-cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
-                       const uint8_t* index, double* W)
+// particle2grid! of nf fields (nf > 1 or tuple: the tuple form), fields in
+// launches of at most four; every launch forms the same weights in the same
+// order, so the result does not depend on how the fields are grouped
+static cudaError_t p2g_launch(jp_particles* P, double* const* F, const double* const* Fp, int nf, bool tuple,
+                              const double* const coords[3], const uint8_t* index, double* W)
 {
     const bool d3 = P->g.ndim == 3;
     CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
     const int64_t V0 = P->g.n[0] + 1, V1 = P->g.n[1] + 1;
-    if (P->g.max_xcell > 64) {
-        const unsigned nbw = grid_blocks(V0 * V1 * (d3 ? P->g.n[2] + 1 : 1));
-        if (!d3)
-            p2g_wide_kernel<2><<<nbw, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, W);
-        else
-            p2g_wide_kernel<3><<<nbw, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, W);
-        return cudaGetLastError();
-    }
     const int64_t cols = d3 ? V0 * V1 : V0;
     const int64_t rows = P->g.n[d3 ? 2 : 1] + 1;
     // rows per thread: long enough to amortise the prologue row, short enough
@@ -773,11 +877,83 @@ cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const doubl
     chunk = chunk < 2 ? 2 : (chunk > 16 ? 16 : chunk);
     const int64_t nthreads = cols * ((rows + chunk - 1) / chunk);
     const unsigned nb = grid_blocks(nthreads);
-    if (!d3)
-        p2g_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk, nthreads, W);
-    else
-        p2g_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, F, Fp, X, index, chunk, nthreads, W);
+    const unsigned nbw = grid_blocks(V0 * V1 * (d3 ? P->g.n[2] + 1 : 1));
+    for (int f0 = 0; f0 < nf; f0 += kFieldsPerLaunch) {
+        const int n = nf - f0 < kFieldsPerLaunch ? nf - f0 : kFieldsPerLaunch;
+        P2GFields PF{};
+        for (int k = 0; k < n; ++k) {
+            PF.fp[k] = Fp[f0 + k];
+            PF.f[k] = F[f0 + k];
+        }
+        double* Wk = f0 == 0 ? W : nullptr;
+        cudaStream_t st = P->stream;
+        if (P->g.max_xcell > 64) {
+            if (!d3)
+                tuple ? p2g_wide_kernel<2, true><<<nbw, kThreads, 0, st>>>(P->g, PF, n, X, index, Wk)
+                      : p2g_wide_kernel<2, false><<<nbw, kThreads, 0, st>>>(P->g, PF, n, X, index, Wk);
+            else
+                p2g_wide_kernel<3, true><<<nbw, kThreads, 0, st>>>(P->g, PF, n, X, index, Wk);
+            continue;
+        }
+#define JP_P2G(D, NF, T) p2g_kernel<D, NF, T><<<nb, kThreads, 0, st>>>(P->g, PF, X, index, chunk, nthreads, Wk)
+        if (!d3) {
+            if (!tuple) JP_P2G(2, 1, false);
+            else if (n == 1) JP_P2G(2, 1, true);
+            else if (n == 2) JP_P2G(2, 2, true);
+            else if (n == 3) JP_P2G(2, 3, true);
+            else JP_P2G(2, 4, true);
+        } else {
+            if (n == 1) JP_P2G(3, 1, true);
+            else if (n == 2) JP_P2G(3, 2, true);
+            else if (n == 3) JP_P2G(3, 3, true);
+            else JP_P2G(3, 4, true);
+        }
+#undef JP_P2G
+    }
     return cudaGetLastError();
+}
+
+cudaError_t launch_p2g(jp_particles* P, double* F, const double* Fp, const double* const coords[3],
+                       const uint8_t* index, double* W)
+{
+    return p2g_launch(P, &F, &Fp, 1, false, coords, index, W);
+}
+
+cudaError_t launch_g2p_n(jp_particles* P, double* const* Fp, const double* const* F, int nf,
+                         const double* const coords[3], const uint8_t* index)
+{
+    const bool d3 = P->g.ndim == 3;
+    CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
+    const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const int nt = 32 * kWarpsPerBlock;
+    for (int f0 = 0; f0 < nf; f0 += kFieldsPerLaunchG2P) {
+        const int n = nf - f0 < kFieldsPerLaunchG2P ? nf - f0 : kFieldsPerLaunchG2P;
+        G2PFields GF{};
+        for (int k = 0; k < n; ++k) {
+            GF.f[k] = F[f0 + k];
+            GF.fp[k] = Fp[f0 + k];
+        }
+#define JP_G2P(D, NF) g2p_n_kernel<D, NF><<<nb, nt, 0, P->stream>>>(P->g, GF, X, index)
+        if (!d3) {
+            if (n == 1) JP_G2P(2, 1);
+            else if (n == 2) JP_G2P(2, 2);
+            else if (n == 3) JP_G2P(2, 3);
+            else JP_G2P(2, 4);
+        } else {
+            if (n == 1) JP_G2P(3, 1);
+            else if (n == 2) JP_G2P(3, 2);
+            else if (n == 3) JP_G2P(3, 3);
+            else JP_G2P(3, 4);
+        }
+#undef JP_G2P
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_p2g_n(jp_particles* P, double* const* F, const double* const* Fp, int nf,
+                         const double* const coords[3], const uint8_t* index)
+{
+    return p2g_launch(P, F, Fp, nf, true, coords, index, nullptr);
 }
 
 }  // namespace jp

@@ -1327,6 +1327,120 @@ void jpo_particle2grid(const jpo_grid* g, double* F, const double* Fp,
     }
 }
 
+/*
+ * particle2grid! with a tuple of fields (src/Interpolations/particle_to_grid.jl:
+ * 70-109 in 2D, 153-199 in 3D): the scalar form's cells, slots and weights
+ * (inv(distance^2)), one weighted sum per field, ωxF[j] = muladd(ω_i, Fp[j],
+ * ωxF[j]) in slot order, then F[j] = ωxF[j] * inv(ω) for every field (2D and
+ * 3D alike). The reference's tuple kernels themselves stop on their first
+ * particle for more than one field: the 2D one starts ωxF as one number and
+ * indexes it with the field number (a bounds error from the second field on),
+ * the 3D one reads Fp[j][i, ...] with `i` undefined in that scope (its slot
+ * variable is `ip`). These sums are what both spell out: a separate
+ * accumulator per field, starting at zero.
+ */
+void jpo_particle2grid_n(const jpo_grid* g, double* const* F, const double* const* Fp, int nf,
+                         const double* const coords[3], const uint8_t* index)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int64_t V0 = g->n[0] + 1, V1 = g->n[1] + 1, V2 = N == 3 ? g->n[2] + 1 : 1;
+    const int64_t nv = V0 * V1 * V2;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t v = 0; v < nv; ++v) {
+        const int64_t i = v % V0, j = (v / V0) % V1, k = v / (V0 * V1);
+        const double xq = g->xv[0][i], yq = g->xv[1][j], zq = N == 3 ? g->xv[2][k] : 0.0;
+        double w = 0.0, wF[JPO_MAX_FIELDS];
+        for (int f = 0; f < nf; ++f) wF[f] = 0.0;
+        const int kmin = N == 3 ? -1 : 0;
+        for (int ko = kmin; ko <= 0; ++ko) {
+            const int64_t kc = k + ko;
+            if (N == 3 && !(0 <= kc && kc < g->n[2])) continue;
+            for (int jo = -1; jo <= 0; ++jo) {
+                const int64_t jc = j + jo;
+                if (!(0 <= jc && jc < g->n[1])) continue;
+                for (int io = -1; io <= 0; ++io) {
+                    const int64_t ic = i + io;
+                    if (!(0 <= ic && ic < g->n[0])) continue;
+                    const int64_t c = ic + g->n[0] * (jc + g->n[1] * (N == 3 ? kc : 0));
+                    for (int s = 0; s < M; ++s) {
+                        const int64_t a = c + nc * s;
+                        if (!index[a]) continue;
+                        double ss;
+                        const double ddx = xq - coords[0][a];
+                        const double ddy = yq - coords[1][a];
+                        if (N == 2) {
+                            ss = ddx * ddx + ddy * ddy;
+                        } else {
+                            const double ddz = zq - coords[2][a];
+                            ss = (ddx * ddx + ddy * ddy) + ddz * ddz;
+                        }
+                        const double dist = sqrt(ss);
+                        const double wi = 1.0 / (dist * dist);
+                        w += wi;
+                        for (int f = 0; f < nf; ++f) wF[f] = fma(wi, Fp[f][a], wF[f]);
+                    }
+                }
+            }
+        }
+        const double iw = 1.0 / w;
+        for (int f = 0; f < nf; ++f) F[f][v] = wF[f] * iw;
+    }
+}
+
+/*
+ * grid2particle! with a tuple of fields (src/Interpolations/grid_to_particle.jl:
+ * 84-103, through _grid2particle at :235-250): a live particle with a NaN
+ * coordinate is skipped (any(isnan, pᵢ)); every other one gets, for each field,
+ * the N-linear interpolation of that field's cell corners at
+ * t = (p - x_corner) * inv(di).
+ */
+void jpo_grid2particle_n(const jpo_grid* g, double* const* Fp, const double* const* F, int nf,
+                         const double* const coords[3], const uint8_t* index)
+{
+    const int N = g->ndim;
+    const int64_t nc = g->ncells;
+    const int M = g->max_xcell;
+    const int64_t V0 = g->n[0] + 1, V1 = g->n[1] + 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+    for (int64_t c = 0; c < nc; ++c) {
+        int64_t I[3];
+        cell_coords(g, c, I);
+        double x0[3], dx[3];
+        for (int d = 0; d < N; ++d) {
+            x0[d] = g->xv[d][I[d]];
+            dx[d] = g->dxv[d][I[d]];
+        }
+        const int64_t b = I[0] + V0 * (I[1] + (N == 3 ? V1 * I[2] : 0));
+        const int64_t sz = V0 * V1;
+        for (int s = 0; s < M; ++s) {
+            const int64_t a = c + nc * s;
+            if (!index[a]) continue;
+            int nan = 0;
+            for (int d = 0; d < N; ++d) nan |= isnan(coords[d][a]);
+            if (nan) continue;
+            double t[3];
+            for (int d = 0; d < N; ++d) t[d] = (coords[d][a] - x0[d]) * (1.0 / dx[d]);
+            for (int f = 0; f < nf; ++f) {
+                const double* Ff = F[f];
+                double v[8];
+                v[0] = Ff[b];
+                v[1] = Ff[b + 1];
+                v[2] = Ff[b + V0];
+                v[3] = Ff[b + V0 + 1];
+                if (N == 3) {
+                    v[4] = Ff[b + sz];
+                    v[5] = Ff[b + sz + 1];
+                    v[6] = Ff[b + sz + V0];
+                    v[7] = Ff[b + sz + V0 + 1];
+                }
+                Fp[f][a] = lerpN(N, v, t);
+            }
+        }
+    }
+}
+
 double jpo_rand(uint64_t seed, uint32_t stream, uint32_t call, uint64_t cell, uint32_t slot,
                 uint32_t dim)
 {

@@ -88,6 +88,15 @@ void jpo_grid2particle(const jpo_grid* g, double* Fp, const double* F,
 void jpo_particle2grid(const jpo_grid* g, double* F, const double* Fp,
                        const double* const coords[3], const uint8_t* index);
 
+/* tuple forms (at most JPO_MAX_FIELDS fields): particle2grid!(F::NTuple, Fp::NTuple, particles),
+   src/Interpolations/particle_to_grid.jl:70-109, 153-199; grid2particle!(Fp::NTuple, F::NTuple, particles),
+   src/Interpolations/grid_to_particle.jl:84-103 */
+#define JPO_MAX_FIELDS 16
+void jpo_particle2grid_n(const jpo_grid* g, double* const* F, const double* const* Fp, int nf,
+                         const double* const coords[3], const uint8_t* index);
+void jpo_grid2particle_n(const jpo_grid* g, double* const* Fp, const double* const* F, int nf,
+                         const double* const coords[3], const uint8_t* index);
+
 /* grid2particle_flip!: src/Interpolations/grid_to_particle.jl:125-170 */
 void jpo_grid2particle_flip(const jpo_grid* g, double* Fp, const double* F, const double* F0, double alpha,
                             const double* const coords[3], const uint8_t* index);

@@ -90,6 +90,8 @@ def lib():
         L.jpo_particle2grid.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3, ctypes.c_void_p]
         L.jpo_grid2particle_flip.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
                                              P3, ctypes.c_void_p]
+        L.jpo_particle2grid_n.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, P3, ctypes.c_void_p]
+        L.jpo_grid2particle_n.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, P3, ctypes.c_void_p]
         L.jpo_centroid2particle.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3]
         L.jpo_particle2centroid.argtypes = [G, ctypes.c_void_p, ctypes.c_void_p, P3]
         L.jpo_phase_ratios_center.argtypes = [G, ctypes.c_int, ctypes.c_void_p, P3, ctypes.c_void_p]
@@ -278,6 +280,23 @@ class OracleParticles:
     def particle2grid(self, F, Fp):
         assert F.flags.f_contiguous and F.dtype == np.float64
         lib().jpo_particle2grid(ctypes.byref(self._g), _ptr(F), _ptr(Fp), self._p3(self.coords), _ptr(self.index))
+
+    def particle2grid_n(self, Fs, Fps):
+        """particle2grid!(F::NTuple, Fp::NTuple, particles) on lists of fields."""
+        assert len(Fs) == len(Fps) and 1 <= len(Fs) <= 16
+        for F in Fs:
+            assert F.flags.f_contiguous and F.dtype == np.float64
+        dst = (ctypes.c_void_p * len(Fs))(*[_ptr(F) for F in Fs])
+        src = (ctypes.c_void_p * len(Fps))(*[_ptr(f) for f in Fps])
+        lib().jpo_particle2grid_n(ctypes.byref(self._g), dst, src, len(Fs), self._p3(self.coords), _ptr(self.index))
+
+    def grid2particle_n(self, Fps, Fs):
+        """grid2particle!(Fp::NTuple, F::NTuple, particles) on lists of fields."""
+        assert len(Fs) == len(Fps) and 1 <= len(Fs) <= 16
+        Fs = [np.asfortranarray(F, dtype=np.float64) for F in Fs]
+        dst = (ctypes.c_void_p * len(Fps))(*[_ptr(f) for f in Fps])
+        src = (ctypes.c_void_p * len(Fs))(*[_ptr(F) for F in Fs])
+        lib().jpo_grid2particle_n(ctypes.byref(self._g), dst, src, len(Fs), self._p3(self.coords), _ptr(self.index))
 
     # -- the adjacent transfers -------------------------------------------
     def grid2particle_flip(self, Fp, F, F0, alpha=0.0):

@@ -7,7 +7,10 @@ Tolerances (written here, asserted below):
   * one RK2 step: 1e-5 cell widths;
   * 60 RK2 steps of advection + move: 1e-4 cell widths for every particle
     present in both runs (tracked by id);
-  * particle2grid: 1e-5 relative to the field's range.
+  * particle2grid: 1e-5 relative to the field's range against the FP64 form;
+    1e-6 of the field's largest value against the same inverse-distance sums
+    formed on the host in FP64 from the FP32 offsets (the kernel sums FP32
+    weights in compensated pairs).
 """
 import numpy as np
 import pytest
@@ -154,3 +157,38 @@ def test_injection_refills_depleted_quadrants():
     inq = live & (x0 > 0) & (x0 < 0.5) & (x1 > 0) & (x1 < 0.5)
     assert np.all(inq.sum(axis=0) >= 2), "every cell's first quadrant holds at least min_xcell / 4 particles"
     assert np.all(np.isfinite(T.numpy()[live]))
+
+
+@pytest.mark.parametrize("ni", [(37, 29), (9, 7, 6)])
+def test_particle2grid_f32_against_host_sums(ni):
+    """Every vertex: sum_p w_p F_p / sum_p w_p over the particles of its 2^N
+    cells, w_p = 1 / |vertex - particle|^2 with the distance in physical units
+    formed from the FP32 offsets, summed on the host in FP64."""
+    g = W.grid(ni)
+    N = len(ni)
+    p = jp.init_particles(jp.CUDABackend, 24, 48, 12, *g["grid_v"])
+    xi = jp.init_offsets(p)
+    T = W.gaussian_T(g, center=(0.5,) * N, width2=0.05)
+    pT, = jp.init_cell_arrays_f32(p, 1)
+    jp.grid2particle_f32_(pT, jp.TA("CUDA")(T).float(), p, xi)
+    F = jp.grid_field_f32(T.shape)
+    jp.particle2grid_f32_(F, pT, p, xi)
+    live = p.index.numpy().astype(bool)
+    X = [xi[d].numpy().astype(np.float64) for d in range(N)]
+    f = pT.numpy().astype(np.float64)
+    dx = np.asarray(g["dx"])
+    cells = np.arange(live.shape[1])
+    I = [(cells // int(np.prod(ni[:d]))) % ni[d] for d in range(N)]
+    W_ = np.zeros(T.shape)
+    WF = np.zeros(T.shape)
+    for corner in np.ndindex(*(2,) * N):
+        d2 = sum(((corner[d] - X[d]) * np.float32(dx[d])) ** 2 for d in range(N))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            w = np.where(live, 1.0 / d2, 0.0)
+        v = tuple(np.broadcast_to(I[d] + corner[d], live.shape)[live] for d in range(N))
+        np.add.at(W_, v, w[live])
+        np.add.at(WF, v, (w * np.where(live, f, 0.0))[live])
+    ref = WF / W_
+    got = F.cpu().numpy().astype(np.float64)
+    assert np.all(W_ > 0)
+    assert np.max(np.abs(got - ref)) < 1e-6 * np.max(np.abs(ref))

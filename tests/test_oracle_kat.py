@@ -357,3 +357,33 @@ def test_phase_ratios_midpoints_against_loops():
                                    err_msg=name)
         s = ref[name].sum(axis=0)
         assert np.all((np.abs(s - 1) < 1e-12) | (s == 0))
+
+
+def test_oracle_tuple_forms_match_the_scalar_forms():
+    """The oracle's tuple grid2particle! equals the scalar one field by field;
+    its tuple particle2grid! equals the scalar one in 3D (both normalise by
+    wF * inv(w)) and differs from the 2D scalar form (wF / w) by at most one
+    rounding."""
+    for ni in [(9, 7), (4, 5, 3)]:
+        g = W.grid(ni)
+        grids = tuple(tuple(np.asarray(x) for x in comp) for comp in g["grid_v"])
+        o = O.OracleParticles(grids, 24, 48, 12, uniform=True)
+        o.init_particles()
+        Fs = [W.gaussian_T(g, center=(0.4,) * len(ni)), W.linear_T(g, 0)]
+        tup = [o.cell_array() for _ in Fs]
+        o.grid2particle_n(tup, Fs)
+        live = o.index.astype(bool)
+        for k, F in enumerate(Fs):
+            one = o.cell_array()
+            o.grid2particle(one, F)
+            assert np.array_equal(one[live], tup[k][live])
+        shape = tuple(n + 1 for n in ni)
+        Gt = [np.asfortranarray(np.zeros(shape)) for _ in Fs]
+        o.particle2grid_n(Gt, tup)
+        for k in range(len(Fs)):
+            Gs = np.asfortranarray(np.zeros(shape))
+            o.particle2grid(Gs, tup[k])
+            if len(ni) == 3:
+                assert np.array_equal(Gs, Gt[k])
+            else:
+                assert np.all(np.abs(Gs - Gt[k]) <= np.spacing(np.abs(Gs)))
