@@ -83,54 +83,61 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------- advection
-template <int DIM, int METHOD>
-__device__ __forceinline__ void advect_f32(const DevGrid& g, const CVelF& V, const F32Params& P, const int* I,
-                                           const float* x0, float* x)
+// sample(c, x): velocity component c at offset x of the particle's cell
+template <int DIM, int METHOD, class Sample>
+__device__ __forceinline__ void advect_f32(const F32Params& P, const float* x0, float* x, Sample sample)
 {
     float v0[3], v1[3], q[3];
     if (METHOD == JP_RUNGE_KUTTA2) {
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) v0[c] = velocity_f32<DIM>(g, c, I, x0, V.v[c]);
+        for (int c = 0; c < DIM; ++c) v0[c] = sample(c, x0);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) q[d] = fmaf(P.aw[d], v0[d], x0[d]);
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) v1[c] = velocity_f32<DIM>(g, c, I, q, V.v[c]);
+        for (int c = 0; c < DIM; ++c) v1[c] = sample(c, q);
 #pragma unroll
         for (int d = 0; d < DIM; ++d)
             x[d] = P.half ? fmaf(P.w[d], v1[d], x0[d]) : fmaf(P.w[d], fmaf(P.ca, v0[d], P.cb * v1[d]), x0[d]);
     } else if (METHOD == JP_RUNGE_KUTTA4) {
         float k1[3], k2[3], k3[3], k4[3];
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) k1[c] = velocity_f32<DIM>(g, c, I, x0, V.v[c]);
+        for (int c = 0; c < DIM; ++c) k1[c] = sample(c, x0);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) q[d] = fmaf(0.5f * P.w[d], k1[d], x0[d]);
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) k2[c] = velocity_f32<DIM>(g, c, I, q, V.v[c]);
+        for (int c = 0; c < DIM; ++c) k2[c] = sample(c, q);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) q[d] = fmaf(0.5f * P.w[d], k2[d], x0[d]);
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) k3[c] = velocity_f32<DIM>(g, c, I, q, V.v[c]);
+        for (int c = 0; c < DIM; ++c) k3[c] = sample(c, q);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) q[d] = fmaf(P.w[d], k3[d], x0[d]);
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) k4[c] = velocity_f32<DIM>(g, c, I, q, V.v[c]);
+        for (int c = 0; c < DIM; ++c) k4[c] = sample(c, q);
 #pragma unroll
         for (int d = 0; d < DIM; ++d)
             x[d] = fmaf(P.w[d] * (1.0f / 6.0f), (k1[d] + 2.0f * k2[d]) + (2.0f * k3[d] + k4[d]), x0[d]);
     } else {
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) v0[c] = velocity_f32<DIM>(g, c, I, x0, V.v[c]);
+        for (int c = 0; c < DIM; ++c) v0[c] = sample(c, x0);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) x[d] = fmaf(P.w[d], v0[d], x0[d]);
     }
 }
 
+// A warp takes 32 consecutive cells and their live particles in slot-major
+// order. In 2D, when the 32 cells lie in one cell row, the warp first copies
+// the window of both velocity grids around them into shared memory (coalesced
+// rows): the stage points' bilinear samples then read shared memory instead of
+// gathering through L1 (whose tag lookups, about six distinct lines per warp
+// load, bound the kernel); a sample outside the window reads global memory.
 template <int DIM, int METHOD>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     advect_f32_kernel(DevGrid g, CVelF V, F32Params P, XiF Xi, const uint8_t* __restrict__ index)
 {
     __shared__ SlotList lists[kWarpsPerBlock];
     __shared__ int cellI[kWarpsPerBlock][32][3];
+    __shared__ float vwin[DIM == 2 ? kWarpsPerBlock : 1][2][kWinY][kWinX];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
     if (c0 >= g.ncells) return;
@@ -142,19 +149,65 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 #pragma unroll
         for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
     }
+    int wx0 = 0, wy0 = 0;
+    bool use_win = false;
+    if (DIM == 2) {
+        const int64_t n0 = g.n[0];
+        const int64_t r0 = c0 / n0, r1 = min(c0 + 31, nc - 1) / n0;
+        use_win = r0 == r1;
+        if (use_win) {
+            wx0 = (int)(c0 - r0 * n0) - 1;
+            wy0 = (int)r0 - 1;
+#pragma unroll
+            for (int comp = 0; comp < 2; ++comp) {
+                const int64_t L0 = g.nvel[comp][0], L1 = g.nvel[comp][1];
+                for (int e = lane; e < kWinX * kWinY; e += 32) {
+                    const int ox = e % kWinX, oy = e / kWinX;
+                    const int64_t gx = wx0 + ox, gy = wy0 + oy;
+                    const bool in = gx >= 0 && gx < L0 && gy >= 0 && gy < L1;
+                    vwin[DIM == 2 ? w : 0][comp][oy][ox] = in ? __ldg(V.v[comp] + gx + L0 * gy) : 0.0f;
+                }
+            }
+        }
+    }
     uint64_t mine;
-    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
-    for (int k = lane; k < K; k += 32) {
-        int s, l;
-        slot_item(lists[w], M, k, &s, &l);
-        const int64_t a = c0 + l + nc * s;
-        const int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
-        float x0[3], x[3];
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);  // ends with a __syncwarp
+    // two particles per lane at a time: both loads are in flight before either is advected
+    constexpr int B = 2;
+    for (int k0 = lane; k0 < K; k0 += 32 * B) {
+        int ll[B];
+        int64_t al[B];
+        float x0[B][3];
+        bool has[B];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) x0[d] = Xi.x[d][a];
-        advect_f32<DIM, METHOD>(g, V, P, I, x0, x);
+        for (int u = 0; u < B; ++u) {
+            const int k = k0 + 32 * u;
+            int s = 0;
+            ll[u] = 0;
+            has[u] = k < K;
+            if (has[u]) slot_item(lists[w], M, k, &s, &ll[u]);
+            al[u] = c0 + ll[u] + nc * s;
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) Xi.x[d][a] = x[d];
+            for (int d = 0; d < DIM; ++d) x0[u][d] = has[u] ? Xi.x[d][al[u]] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            if (!has[u]) continue;
+            const int l = ll[u];
+            const int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
+            float x[3];
+            if (DIM == 2) {
+                const float* wb = use_win ? &vwin[DIM == 2 ? w : 0][0][0][0] : nullptr;
+                advect_f32<DIM, METHOD>(P, x0[u], x, [&](int c, const float* xi) {
+                    return velocity_f32_win(g, c, I, xi, V.v[c], wb ? wb + c * kWinX * kWinY : nullptr, wx0, wy0);
+                });
+            } else {
+                advect_f32<DIM, METHOD>(P, x0[u], x,
+                                        [&](int c, const float* xi) { return velocity_f32<DIM>(g, c, I, xi, V.v[c]); });
+            }
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) Xi.x[d][al[u]] = x[d];
+        }
     }
 }
 
@@ -570,23 +623,24 @@ __global__ void inject_pass_f32(DevGrid g, F32Params P, XiF Xi, uint8_t* __restr
 }
 
 // ------------------------------------------------------- grid2particle!
+// One thread per cell (its corner values in registers), a warp on 32
+// consecutive cells walking the slot rows up to its highest live slot, four
+// rows in flight per lane: every load and store is a coalesced row access.
 template <int DIM>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+__global__ void __launch_bounds__(kThreads)
     g2p_f32_kernel(DevGrid g, float* __restrict__ Fp, const float* __restrict__ F, CXiF Xi,
                    const uint8_t* __restrict__ index)
 {
-    __shared__ SlotList lists[kWarpsPerBlock];
-    __shared__ float cellv[kWarpsPerBlock][32][1 << DIM];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
-    if (c0 >= g.ncells) return;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nc = g.ncells;
+    const bool valid = c < nc;
     const int M = g.max_xcell;
+    float cv[1 << DIM];
+    uint64_t L = 0;
     {
         int64_t I[3];
-        cell_coords(g, min(c0 + lane, nc - 1), I);
+        cell_coords(g, valid ? c : nc - 1, I);
         const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
-        float* cv = cellv[w][lane];
         const float* b = F + I[0] + V0 * (I[1] + (DIM == 3 ? V1 * I[2] : 0));
         cv[0] = __ldg(b);
         cv[1] = __ldg(b + 1);
@@ -599,17 +653,23 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             cv[6] = __ldg(b + sz + V0);
             cv[7] = __ldg(b + sz + V0 + 1);
         }
+        if (valid) L = live_mask(index, c, nc, M);
     }
-    uint64_t mine;
-    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
-    for (int k = lane; k < K; k += 32) {
-        int s, l;
-        slot_item(lists[w], M, k, &s, &l);
-        const int64_t a = c0 + l + nc * s;
-        float t[3];
+    const int hi = (int)__reduce_max_sync(0xffffffffu, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
+    constexpr int B = 4;
+    for (int s0 = 0; s0 < hi; s0 += B) {
+        float t[B][3];
+        bool lv[B];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) t[d] = Xi.x[d][a];
-        Fp[a] = lerpNf<DIM>(cellv[w][l], t);
+        for (int u = 0; u < B; ++u) {
+            const int s = s0 + u;
+            lv[u] = s < hi && ((L >> s) & 1);
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) t[u][d] = lv[u] ? Xi.x[d][c + nc * s] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (lv[u]) Fp[c + nc * (s0 + u)] = lerpNf<DIM>(cv, t[u]);
     }
 }
 
@@ -1004,12 +1064,11 @@ cudaError_t launch_g2p_f32(jp_particles* P, float* Fp, const float* F, const flo
 {
     const bool d3 = P->g.ndim == 3;
     CXiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
-    const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
-    const int nt = 32 * kWarpsPerBlock;
+    const unsigned nb = grid_blocks(P->g.ncells);
     if (!d3)
-        g2p_f32_kernel<2><<<nb, nt, 0, P->stream>>>(P->g, Fp, F, Xi, index);
+        g2p_f32_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, Xi, index);
     else
-        g2p_f32_kernel<3><<<nb, nt, 0, P->stream>>>(P->g, Fp, F, Xi, index);
+        g2p_f32_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, Xi, index);
     return cudaGetLastError();
 }
 
