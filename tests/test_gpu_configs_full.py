@@ -91,8 +91,8 @@ def test_c1_full_size_750_steps():
             fp.assert_same(f"C1 step {step}")
     counts = jp.move_counts(fp.p)
     assert counts["moved_too_far"] == 0, counts
-    # the stream-function cells are closed: particles stay in the unit square
-    assert int(fp.o.index.sum()) > 0.9 * live0
+    # C1 has no injection: every particle the run lost was removed by a move, and counted
+    assert live0 - int(fp.o.index.sum()) == counts["left_domain"] + counts["no_free_slot"]
 
 
 def test_c2_full_size_miniapp_cycle():
