@@ -217,122 +217,148 @@ struct MoveViewF {
     float* shadow;  // interleaved records: DIM offsets, then the fields
 };
 
-// One thread per cell, a warp on 32 consecutive cells walking the slot rows up
-// to its highest live slot (coalesced rows, four in flight per lane), as in
-// the FP64 form; movers' records go to their own cell's next record.
+// The FP64 classify's scheme (slot-major live particles over the lanes, loads
+// of a batch in flight together, records written after a warp barrier at
+// their cell's next record), four particles per lane in flight.
 template <int DIM>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
     move_classify_f32(DevGrid g, XiF Xi, const uint8_t* __restrict__ index, ArgsF A, MoveViewF S, int* d_err)
 {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ int cellI[kWarpsPerBlock][32][3];
+    __shared__ unsigned long long movers[kWarpsPerBlock][32];
+    constexpr int NT = DIM == 2 ? 5 : 1;  // 2D: the four destination planes, routed
+    __shared__ unsigned long long tmask[kWarpsPerBlock][NT][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
     const int64_t nc = g.ncells;
-    const bool valid = c < nc;
     const int M = g.max_xcell;
-    int64_t I[3];
-    cell_coords(g, valid ? c : nc - 1, I);
-    uint64_t L = 0;
-    if (valid) {
-#pragma unroll 8
-        for (int s = 0; s < M; ++s) L |= (uint64_t)(index[c + nc * s] != 0) << s;
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
+        movers[w][lane] = 0;
+#pragma unroll
+        for (int k = 0; k < NT; ++k) tmask[w][k][lane] = 0;
     }
-    const int hi = (int)__reduce_max_sync(0xffffffffu, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
-    uint64_t Mv = 0, P0 = 0, P1 = 0, P2 = 0, P3 = 0, RT = 0;
-    int rank = 0, n_exit = 0, n_far = 0;
-    int errs = 0;
+    uint64_t L;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &L);
     const int comps = S.m.comps;
-    float* rec = S.shadow + S.m.record(valid ? c : 0, 0);
+    const bool whole = comps == 4;
+    int errs = 0, n_exit = 0, n_far = 0;
+    // one live particle: its destination code (kCodeStay, kCodeExit or a neighbour
+    // code) and, for a mover, its re-normalised offsets in v
+    auto classify_one = [&](int s, int l, int64_t a, const float* xi, float* v) -> uint8_t {
+        bool out = false;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) out |= !(xi[d] >= 0.0f && xi[d] < 1.0f);
+        if (!out) return kCodeStay;
+        const unsigned long long bit = 1ull << s;
+        atomicOr(&movers[w][l], bit);
+        int off[3] = {0, 0, 0};
+        bool inside = true, far = false;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            if (!(fabsf(xi[d]) < 1e6f)) {  // NaN / Inf: left the domain
+                inside = false;
+                continue;
+            }
+            const float fl = floorf(xi[d]);
+            const int o = (int)fl;
+            const int T = cellI[w][l][d] + o;
+            inside &= T >= 0 && T < g.n[d];
+            far |= o > 1 || o < -1;
+            off[d] = o;
+            // re-normalised offset in the target cell, kept below 1. xi - fl is one
+            // correctly rounded FP32 subtraction: for fl = 1 it is exact (Sterbenz), for
+            // fl = -1 the exact 1 + xi fits FP64 whenever it does not round to 1.0f in FP32
+            // either, so this equals the FP64 difference rounded to FP32 (the particles
+            // moving farther are dropped) without the FP64 pipe
+            const float rr = xi[d] - fl;
+            v[d] = rr < 1.0f ? rr : 0x1.fffffep-1f;
+        }
+        uint8_t code = kCodeExit;
+        if (!inside) {
+            ++n_exit;
+        } else if (far) {
+            errs |= kWarnFarMove;
+            ++n_far;
+        } else {
+            code = (uint8_t)nb_code<DIM>(off);
+        }
+        if (DIM == 2) {
+            if (code != kCodeExit) {
+                if (code & 1) atomicOr(&tmask[w][0][l], bit);
+                if (code & 2) atomicOr(&tmask[w][1][l], bit);
+                if (code & 4) atomicOr(&tmask[w][2][l], bit);
+                if (code & 8) atomicOr(&tmask[w][3][l], bit);
+                atomicOr(&tmask[w][4][l], bit);
+            }
+        } else {
+            S.m.code[a] = code;
+        }
+        return code;
+    };
     constexpr int B = 4;
-    for (int s0 = 0; s0 < hi; s0 += B) {
-        float x[B][DIM];
-        bool lv[B];
+    for (int k0 = lane; k0 < K; k0 += 32 * B) {
+        int sl[B], ll[B];
+        int64_t al[B];
+        float xl[B][3], fl[B][4 - DIM], vl[B][4];
+        bool has[B];
+        uint8_t code[B];
 #pragma unroll
         for (int u = 0; u < B; ++u) {
-            const int s = s0 + u;
-            lv[u] = s < hi && ((L >> s) & 1);
+            const int k = k0 + 32 * u;
+            has[u] = k < K;
+            sl[u] = 0;
+            ll[u] = 0;
+            if (has[u]) slot_item(lists[w], M, k, &sl[u], &ll[u]);
+            al[u] = c0 + ll[u] + nc * sl[u];
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) x[u][d] = lv[u] ? Xi.x[d][c + nc * s] : 0.0f;
+            for (int d = 0; d < DIM; ++d) xl[u][d] = has[u] ? Xi.x[d][al[u]] : 0.0f;
+#pragma unroll
+            for (int j = 0; j < 4 - DIM; ++j) fl[u][j] = (has[u] && whole && j < A.n) ? A.a[j][al[u]] : 0.0f;
         }
 #pragma unroll
         for (int u = 0; u < B; ++u) {
-            if (!lv[u]) continue;
-            const int s = s0 + u;
-            const int64_t a = c + nc * s;
-            bool out = false;
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) out |= !(x[u][d] >= 0.0f && x[u][d] < 1.0f);
-            if (!out) continue;
-            const uint64_t bit = 1ull << s;
-            Mv |= bit;
-            const int r = rank++;
-            int off[3] = {0, 0, 0};
-            float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            bool inside = true, far = false;
+            for (int j = 0; j < 4; ++j) vl[u][j] = 0.0f;
+            code[u] = has[u] ? classify_one(sl[u], ll[u], al[u], xl[u], vl[u]) : kCodeStay;
+        }
+        __syncwarp();  // every mover bit of this batch is set
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const float xd = x[u][d];
-                if (!(fabsf(xd) < 1e6f)) {  // NaN / Inf: left the domain
-                    inside = false;
-                    continue;
-                }
-                const float fl = floorf(xd);
-                const int o = (int)fl;
-                const int T = (int)I[d] + o;
-                inside &= T >= 0 && T < g.n[d];
-                far |= o > 1 || o < -1;
-                off[d] = o;
-                // re-normalised offset in the target cell, kept below 1. xi - fl is one
-                // correctly rounded FP32 subtraction: for fl = 1 it is exact (Sterbenz), for
-                // fl = -1 the exact 1 + xi fits FP64 whenever it does not round to 1.0f in FP32
-                // either, so this equals the FP64 difference rounded to FP32 (the particles
-                // moving farther are dropped) without the FP64 pipe
-                const float rr = xd - fl;
-                v[d] = rr < 1.0f ? rr : 0x1.fffffep-1f;
-            }
-            uint8_t code = kCodeExit;
-            if (!inside) {
-                ++n_exit;
-            } else if (far) {
-                errs |= kWarnFarMove;
-                ++n_far;
-            } else {
-                code = (uint8_t)nb_code<DIM>(off);
-            }
-            if (DIM == 3) S.m.code[a] = code;
-            if (code == kCodeExit) continue;  // removed: no record needed
-            if (DIM == 2) {
-                P0 |= (code & 1) ? bit : 0ull;
-                P1 |= (code & 2) ? bit : 0ull;
-                P2 |= (code & 4) ? bit : 0ull;
-                P3 |= (code & 8) ? bit : 0ull;
-                RT |= bit;
-            }
-            float* rp = rec + (int64_t)r * comps;
-            if (comps == 4) {
+        for (int u = 0; u < B; ++u) {
+            if (code[u] == kCodeStay || code[u] == kCodeExit) continue;
+            const int l = ll[u];
+            const int r = __popcll(movers[w][l] & ((1ull << sl[u]) - 1));
+            float* rp = S.shadow + S.m.record(c0 + l, r);
+            if (whole) {
 #pragma unroll
-                for (int j = 0; j < 4 - DIM; ++j)
-                    if (j < A.n) v[DIM + j] = A.a[j][a];
-                *reinterpret_cast<float4*>(rp) = make_float4(v[0], v[1], v[2], v[3]);
+                for (int j = 0; j < 4 - DIM; ++j) vl[u][DIM + j] = fl[u][j];
+                *reinterpret_cast<float4*>(rp) = make_float4(vl[u][0], vl[u][1], vl[u][2], vl[u][3]);
             } else if (comps == 2) {
-                *reinterpret_cast<float2*>(rp) = make_float2(v[0], v[1]);
+                *reinterpret_cast<float2*>(rp) = make_float2(vl[u][0], vl[u][1]);
             } else {
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) rp[d] = v[d];
-                for (int j = 0; j < A.n; ++j) rp[DIM + j] = A.a[j][a];
+                for (int d = 0; d < DIM; ++d) rp[d] = vl[u][d];
+                for (int j = 0; j < A.n; ++j) rp[DIM + j] = A.a[j][al[u]];
             }
         }
     }
-    if (valid) {
+    __syncwarp();
+    const int64_t c = c0 + lane;
+    if (c < nc) {
         S.m.L(c) = L;
         S.m.R(c) = 0;
         S.m.U(c) = 0;
         S.m.L0(c) = L;
-        S.m.M(c) = Mv;
+        S.m.M(c) = movers[w][lane];
         if (DIM == 2) {
-            S.m.P(c, 0) = P0;
-            S.m.P(c, 1) = P1;
-            S.m.P(c, 2) = P2;
-            S.m.P(c, 3) = P3;
-            S.m.RT(c) = RT;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) S.m.P(c, j) = tmask[w][j][lane];
+            S.m.RT(c) = tmask[w][4][lane];
             S.m.UN(c) = 0;  // a renormalised offset lies inside its new cell
         }
     }
@@ -992,12 +1018,14 @@ cudaError_t launch_move_f32(jp_particles* P, float* const xi[3], uint8_t* index,
     S.shadow = (float*)m.shadow;
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(P->g.ncells);
+    const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const int ntw = 32 * kWarpsPerBlock;
     if (N == 2) {
-        move_classify_f32<2><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S, P->d_err);
+        move_classify_f32<2><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, P->d_err);
         launch_allocate_passes(P->g, S.m, st);
         move_apply_f32<2><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S);
     } else {
-        move_classify_f32<3><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S, P->d_err);
+        move_classify_f32<3><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, P->d_err);
         launch_allocate_passes(P->g, S.m, st);
         move_apply_f32<3><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S);
     }

@@ -68,138 +68,168 @@ __device__ __forceinline__ int64_t find_cell_key(double px, long long kp, const 
 }
 
 // -------------------------------------------------------------- classify
-// One thread per cell, a warp on 32 consecutive cells: the warp walks the slot
-// rows up to its highest live slot, so each row of each array is one coalesced
-// access, with four rows in flight per lane. A mover's record (coordinates,
-// then fields) goes to the next record of its own cell, so a cell's movers sit
-// together; all masks are built in registers and stored once.
+// A warp covers 32 consecutive cells and spreads their live particles over its
+// lanes in slot-major order (full lanes whatever the occupancy), two particles
+// per lane in flight: coordinates and fields are loaded together, then the
+// particles are classified (their movers' bits and destination planes go to
+// the cells' masks in shared memory), and after a warp barrier each routed
+// mover writes its record to its cell's next records: its rank is the number of
+// movers in lower slots of its cell, all of which lie in this or an earlier
+// batch (slot-major order).
 template <int DIM>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
     move_classify(DevGrid g, Coords X, const uint8_t* __restrict__ index, Args A, MoveView S, int* d_err)
 {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ long long cellk[kWarpsPerBlock][32][2 * DIM];  // keys of corner and corner + dx
+    __shared__ int cellI[kWarpsPerBlock][32][3];
+    __shared__ unsigned long long movers[kWarpsPerBlock][32];
+    constexpr int NT = DIM == 2 ? 6 : 1;  // 2D: the four destination planes, routed, unstable
+    __shared__ unsigned long long tmask[kWarpsPerBlock][NT][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
     const int64_t nc = g.ncells;
-    const bool valid = c < nc;
     const int M = g.max_xcell;
-    int64_t I[3];
-    cell_coords(g, valid ? c : nc - 1, I);
-    long long klo[DIM], khi[DIM], kdlo[DIM], kdhi[DIM];
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            const double lo = ldg(g.xv[d] + I[d]);
+            cellk[w][lane][d] = okey(lo);
+            cellk[w][lane][DIM + d] = okey(lo + ldg(g.dxv[d] + I[d]));  // xv + dx (isincell)
+            cellI[w][lane][d] = (int)I[d];
+        }
+        movers[w][lane] = 0;
+#pragma unroll
+        for (int k = 0; k < NT; ++k) tmask[w][k][lane] = 0;
+    }
+    long long kdlo[3], kdhi[3];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        const double lo = ldg(g.xv[d] + I[d]);
-        klo[d] = okey(lo);
-        khi[d] = okey(lo + ldg(g.dxv[d] + I[d]));  // xv + dx (isincell)
         kdlo[d] = okey(g.dom_lo[d]);
         kdhi[d] = okey(g.dom_hi[d]);
     }
-    uint64_t L = 0;
-    if (valid) {
-#pragma unroll 8
-        for (int s = 0; s < M; ++s) L |= (uint64_t)(index[c + nc * s] != 0) << s;
-    }
-    const int hi = (int)__reduce_max_sync(0xffffffffu, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
-    uint64_t Mv = 0, P0 = 0, P1 = 0, P2 = 0, P3 = 0, RT = 0, UN = 0;
-    int rank = 0, n_exit = 0, n_far = 0, errs = 0;
+    uint64_t L;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &L);
+    int errs = 0, n_exit = 0, n_far = 0;
     const int comps = S.comps;
-    double* rec = S.shadow + S.record(valid ? c : 0, 0);
-    constexpr int B = 4;
-    for (int s0 = 0; s0 < hi; s0 += B) {
-        double p[B][DIM];
-        bool lv[B];
+    const bool rec4 = comps == 4;
+    // classify one live particle (coordinates p): its destination code, kCodeExit when it leaves
+    auto classify_one = [&](int s, int l, int64_t a, const double* p) -> uint8_t {
+        long long kp[3];
+        bool pnan = false;
 #pragma unroll
-        for (int u = 0; u < B; ++u) {
-            const int s = s0 + u;
-            lv[u] = s < hi && ((L >> s) & 1);
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) p[u][d] = lv[u] ? X.c[d][c + nc * s] : 0.0;
+        for (int d = 0; d < DIM; ++d) {
+            kp[d] = okey(p[d]);
+            pnan |= is_nan_bits(p[d]);
         }
+        bool in = !pnan;  // isincell, strict (src/Particles/utils.jl:7-15)
 #pragma unroll
-        for (int u = 0; u < B; ++u) {
-            if (!lv[u]) continue;
-            const int s = s0 + u;
-            const int64_t a = c + nc * s;
-            long long kp[DIM];
-            bool pnan = false;
+        for (int d = 0; d < DIM; ++d) in = in & (cellk[w][l][d] < kp[d]) & (kp[d] < cellk[w][l][DIM + d]);
+        if (in) return kCodeStay;  // move_safe.jl:93
+        const unsigned long long bit = 1ull << s;
+        atomicOr(&movers[w][l], bit);
+        bool inside = !pnan;  // indomain, strict (move_safe.jl:199-206)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) inside = inside & (kdlo[d] < kp[d]) & (kp[d] < kdhi[d]);
+        uint8_t code = kCodeExit;
+        if (inside) {
+            int off[3] = {0, 0, 0};
+            bool far = false, inT = true;
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
-                kp[d] = okey(p[u][d]);
-                pnan |= is_nan_bits(p[u][d]);
+                const int I = cellI[w][l][d];
+                const int64_t T = find_cell_key(p[d], kp[d], g.xv[d], g.n[d] + 1, I, &errs);
+                off[d] = (int)(T - I);
+                far |= (off[d] > 1) | (off[d] < -1);
+                const double lo = ldg(g.xv[d] + T);
+                inT = inT & (okey(lo) < kp[d]) & (kp[d] < okey(lo + ldg(g.dxv[d] + T)));
             }
-            bool in = !pnan;  // isincell, strict (src/Particles/utils.jl:7-15)
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) in = in & (klo[d] < kp[d]) & (kp[d] < khi[d]);
-            if (in) continue;  // move_safe.jl:93
-            const uint64_t bit = 1ull << s;
-            Mv |= bit;
-            const int r = rank++;
-            bool inside = !pnan;  // indomain, strict (move_safe.jl:199-206)
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) inside = inside & (kdlo[d] < kp[d]) & (kp[d] < kdhi[d]);
-            uint8_t code = kCodeExit;
-            if (inside) {
-                int off[3] = {0, 0, 0};
-                bool far = false, inT = true;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) {
-                    const int64_t T = find_cell_key(p[u][d], kp[d], g.xv[d], g.n[d] + 1, I[d], &errs);
-                    off[d] = (int)(T - I[d]);
-                    far |= (off[d] > 1) | (off[d] < -1);
-                    const double lo = ldg(g.xv[d] + T);
-                    inT = inT & (okey(lo) < kp[d]) & (kp[d] < okey(lo + ldg(g.dxv[d] + T)));
-                }
-                if (far) {
-                    errs |= kWarnFarMove;
-                    ++n_far;
-                } else {
-                    code = (uint8_t)nb_code<DIM>(off);
-                    if (!inT) code |= kCodeUnstable;
-                }
+            if (far) {
+                errs |= kWarnFarMove;
+                ++n_far;
             } else {
-                ++n_exit;
+                code = (uint8_t)nb_code<DIM>(off);
+                if (!inT) code |= kCodeUnstable;
             }
-            if (DIM == 3) S.code[a] = code;
-            if (code == kCodeExit) continue;  // removed: no record needed
-            if (DIM == 2) {
+        } else {
+            ++n_exit;
+        }
+        if (DIM == 2) {
+            if (code != kCodeExit) {
                 const int k = code & 0x1F;
-                P0 |= (k & 1) ? bit : 0ull;
-                P1 |= (k & 2) ? bit : 0ull;
-                P2 |= (k & 4) ? bit : 0ull;
-                P3 |= (k & 8) ? bit : 0ull;
-                RT |= bit;
-                if (code & kCodeUnstable) UN |= bit;
+                if (k & 1) atomicOr(&tmask[w][0][l], bit);
+                if (k & 2) atomicOr(&tmask[w][1][l], bit);
+                if (k & 4) atomicOr(&tmask[w][2][l], bit);
+                if (k & 8) atomicOr(&tmask[w][3][l], bit);
+                atomicOr(&tmask[w][4][l], bit);
+                if (code & kCodeUnstable) atomicOr(&tmask[w][5][l], bit);
             }
-            // the record: one 32- or 16-byte store when it has 4 or 2 values
-            double* rp = rec + (int64_t)r * comps;
-            if (comps == 4) {
+        } else {
+            S.code[a] = code;
+        }
+        return code;
+    };
+    constexpr int B = 2;
+    for (int k0 = lane; k0 < K; k0 += 32 * B) {
+        int sl[B], ll[B];
+        int64_t al[B];
+        double pl[B][3], fl[B][4 - DIM];
+        bool has[B];
+        uint8_t code[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int k = k0 + 32 * u;
+            has[u] = k < K;
+            sl[u] = 0;
+            ll[u] = 0;
+            if (has[u]) slot_item(lists[w], M, k, &sl[u], &ll[u]);
+            al[u] = c0 + ll[u] + nc * sl[u];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) pl[u][d] = has[u] ? X.c[d][al[u]] : 0.0;
+#pragma unroll
+            for (int j = 0; j < 4 - DIM; ++j) fl[u][j] = (has[u] && rec4 && j < A.n) ? A.a[j][al[u]] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) code[u] = has[u] ? classify_one(sl[u], ll[u], al[u], pl[u]) : kCodeStay;
+        __syncwarp();  // every mover bit of this batch is set
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            if (code[u] == kCodeStay || code[u] == kCodeExit) continue;
+            const int l = ll[u];
+            const int r = __popcll(movers[w][l] & ((1ull << sl[u]) - 1));
+            double* rp = S.shadow + S.record(c0 + l, r);
+            if (rec4) {  // the whole record in one 32-byte store
                 double v[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) v[d] = p[u][d];
+                for (int d = 0; d < DIM; ++d) v[d] = pl[u][d];
 #pragma unroll
-                for (int j = 0; j < 4 - DIM; ++j)
-                    if (j < A.n) v[DIM + j] = A.a[j][a];
+                for (int j = 0; j < 4 - DIM; ++j) v[DIM + j] = fl[u][j];
                 store_rec4(rp, v);
             } else if (comps == 2) {
-                *reinterpret_cast<double2*>(rp) = make_double2(p[u][0], p[u][1]);
+                *reinterpret_cast<double2*>(rp) = make_double2(pl[u][0], pl[u][1]);
             } else {
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) rp[d] = p[u][d];
-                for (int j = 0; j < A.n; ++j) rp[DIM + j] = A.a[j][a];
+                for (int d = 0; d < DIM; ++d) rp[d] = pl[u][d];
+                for (int j = 0; j < A.n; ++j) rp[DIM + j] = A.a[j][al[u]];
             }
         }
     }
-    if (valid) {
+    __syncwarp();
+    const int64_t c = c0 + lane;
+    if (c < nc) {
         S.L(c) = L;
         S.R(c) = 0;
         S.U(c) = 0;
         S.L0(c) = L;
-        S.M(c) = Mv;
+        S.M(c) = movers[w][lane];
         if (DIM == 2) {
-            S.P(c, 0) = P0;
-            S.P(c, 1) = P1;
-            S.P(c, 2) = P2;
-            S.P(c, 3) = P3;
-            S.RT(c) = RT;
-            S.UN(c) = UN;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) S.P(c, j) = tmask[w][j][lane];
+            S.RT(c) = tmask[w][4][lane];
+            S.UN(c) = tmask[w][5][lane];
         }
     }
     add_move_counts(g.counts, n_exit, n_far, 0);
@@ -1258,12 +1288,14 @@ cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index
                P->g.max_xcell};
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(P->g.ncells);
+    const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    const int ntw = 32 * kWarpsPerBlock;
     if (N == 2) {
-        move_classify<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        move_classify<2><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
         launch_allocate_passes(P->g, S, st);
         move_apply<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     } else {
-        move_classify<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        move_classify<3><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
         launch_allocate_passes(P->g, S, st);
         move_apply<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     }
@@ -1469,12 +1501,14 @@ cudaError_t launch_move_noalloc(jp_particles* P, double* const coords[3], uint8_
     for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
     cudaStream_t st = P->stream;
     const unsigned nb = grid_blocks(nc);
+    const unsigned nbw = grid_blocks(nc, 32 * kWarpsPerBlock);
+    const int ntw = 32 * kWarpsPerBlock;
     if (N == 2) {
-        move_classify<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        move_classify<2><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
         launch_allocate_passes(P->g, S, st);
         move_apply<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     } else {
-        move_classify<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S, P->d_err);
+        move_classify<3><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
         launch_allocate_passes(P->g, S, st);
         move_apply<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     }
