@@ -126,18 +126,13 @@ __device__ __forceinline__ void advect_f32(const F32Params& P, const float* x0, 
 }
 
 // A warp takes 32 consecutive cells and their live particles in slot-major
-// order. In 2D, when the 32 cells lie in one cell row, the warp first copies
-// the window of both velocity grids around them into shared memory (coalesced
-// rows): the stage points' bilinear samples then read shared memory instead of
-// gathering through L1 (whose tag lookups, about six distinct lines per warp
-// load, bound the kernel); a sample outside the window reads global memory.
+// order (full lanes whatever the occupancy).
 template <int DIM, int METHOD>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     advect_f32_kernel(DevGrid g, CVelF V, F32Params P, XiF Xi, const uint8_t* __restrict__ index)
 {
     __shared__ SlotList lists[kWarpsPerBlock];
     __shared__ int cellI[kWarpsPerBlock][32][3];
-    __shared__ float vwin[DIM == 2 ? kWarpsPerBlock : 1][2][kWinY][kWinX];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
     if (c0 >= g.ncells) return;
@@ -149,65 +144,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 #pragma unroll
         for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
     }
-    int wx0 = 0, wy0 = 0;
-    bool use_win = false;
-    if (DIM == 2) {
-        const int64_t n0 = g.n[0];
-        const int64_t r0 = c0 / n0, r1 = min(c0 + 31, nc - 1) / n0;
-        use_win = r0 == r1;
-        if (use_win) {
-            wx0 = (int)(c0 - r0 * n0) - 1;
-            wy0 = (int)r0 - 1;
-#pragma unroll
-            for (int comp = 0; comp < 2; ++comp) {
-                const int64_t L0 = g.nvel[comp][0], L1 = g.nvel[comp][1];
-                for (int e = lane; e < kWinX * kWinY; e += 32) {
-                    const int ox = e % kWinX, oy = e / kWinX;
-                    const int64_t gx = wx0 + ox, gy = wy0 + oy;
-                    const bool in = gx >= 0 && gx < L0 && gy >= 0 && gy < L1;
-                    vwin[DIM == 2 ? w : 0][comp][oy][ox] = in ? __ldg(V.v[comp] + gx + L0 * gy) : 0.0f;
-                }
-            }
-        }
-    }
     uint64_t mine;
-    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);  // ends with a __syncwarp
-    // two particles per lane at a time: both loads are in flight before either is advected
-    constexpr int B = 2;
-    for (int k0 = lane; k0 < K; k0 += 32 * B) {
-        int ll[B];
-        int64_t al[B];
-        float x0[B][3];
-        bool has[B];
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        const int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
+        float x0[3], x[3];
 #pragma unroll
-        for (int u = 0; u < B; ++u) {
-            const int k = k0 + 32 * u;
-            int s = 0;
-            ll[u] = 0;
-            has[u] = k < K;
-            if (has[u]) slot_item(lists[w], M, k, &s, &ll[u]);
-            al[u] = c0 + ll[u] + nc * s;
+        for (int d = 0; d < DIM; ++d) x0[d] = Xi.x[d][a];
+        advect_f32<DIM, METHOD>(P, x0, x, [&](int c, const float* xi) { return velocity_f32<DIM>(g, c, I, xi, V.v[c]); });
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) x0[u][d] = has[u] ? Xi.x[d][al[u]] : 0.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < B; ++u) {
-            if (!has[u]) continue;
-            const int l = ll[u];
-            const int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
-            float x[3];
-            if (DIM == 2) {
-                const float* wb = use_win ? &vwin[DIM == 2 ? w : 0][0][0][0] : nullptr;
-                advect_f32<DIM, METHOD>(P, x0[u], x, [&](int c, const float* xi) {
-                    return velocity_f32_win(g, c, I, xi, V.v[c], wb ? wb + c * kWinX * kWinY : nullptr, wx0, wy0);
-                });
-            } else {
-                advect_f32<DIM, METHOD>(P, x0[u], x,
-                                        [&](int c, const float* xi) { return velocity_f32<DIM>(g, c, I, xi, V.v[c]); });
-            }
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) Xi.x[d][al[u]] = x[d];
-        }
+        for (int d = 0; d < DIM; ++d) Xi.x[d][a] = x[d];
     }
 }
 

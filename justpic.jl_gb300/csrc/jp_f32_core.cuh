@@ -91,54 +91,6 @@ __device__ __forceinline__ float velocity_f32(const DevGrid& g, int comp, const 
     return lerpNf<DIM>(v, t);
 }
 
-// A warp's window of the 2D velocity grids in shared memory: nodes
-// [wx0, wx0 + kWinX) x [wy0, wy0 + kWinY) of each component, which holds every
-// node a stage point within one cell of the warp's 32 cells (one cell row) can
-// reach.
-constexpr int kWinX = 36, kWinY = 5;
-
-// velocity_f32 (2D) reading the four nodes from the window when they lie in it,
-// else from global memory: the same node values, so the same result
-__device__ __forceinline__ float velocity_f32_win(const DevGrid& g, int comp, const int* I, const float* xi,
-                                                  const float* __restrict__ V, const float* win, int wx0, int wy0)
-{
-    int k[2];
-    float t[2];
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-        const float y = (d == comp) ? xi[d] : xi[d] + 0.5f;
-        if (!(fabsf(y) < 1e6f)) return CUDART_INF_F;
-        const float fl = floorf(y);
-        int kk = I[d] + (int)fl;
-        float tt = y - fl;
-        const int L = (int)g.nvel[comp][d];
-        if (kk == L - 1 && tt == 0.0f) {
-            kk = L - 2;
-            tt = 1.0f;
-        }
-        if (kk < 0 || kk > L - 2) return CUDART_INF_F;
-        k[d] = kk;
-        t[d] = tt;
-    }
-    float v[4];
-    const int ox = k[0] - wx0, oy = k[1] - wy0;
-    if (win && ox >= 0 && ox + 1 < kWinX && oy >= 0 && oy + 1 < kWinY) {
-        const float* b = win + ox + kWinX * oy;
-        v[0] = b[0];
-        v[1] = b[1];
-        v[2] = b[kWinX];
-        v[3] = b[kWinX + 1];
-    } else {
-        const int64_t L0 = g.nvel[comp][0];
-        const float* b = V + k[0] + L0 * k[1];
-        v[0] = __ldg(b);
-        v[1] = __ldg(b + 1);
-        v[2] = __ldg(b + L0);
-        v[3] = __ldg(b + L0 + 1);
-    }
-    return lerpNf<2>(v, t);
-}
-
 inline F32Params make_params(const jp_particles* P, double alpha, double dt)
 {
     F32Params p{};
