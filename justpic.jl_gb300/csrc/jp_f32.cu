@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     __shared__ SlotList lists[kWarpsPerBlock];
     __shared__ int cellI[kWarpsPerBlock][32][3];
     __shared__ unsigned long long movers[kWarpsPerBlock][32];
-    constexpr int NT = DIM == 2 ? 5 : 1;  // 2D: the four destination planes, routed
+    constexpr int NT = DIM == 2 ? 9 : 1;  // 2D: movers bound for each of the 9 neighbours
     __shared__ unsigned long long tmask[kWarpsPerBlock][NT][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
@@ -238,13 +238,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             code = (uint8_t)nb_code<DIM>(off);
         }
         if (DIM == 2) {
-            if (code != kCodeExit) {
-                if (code & 1) atomicOr(&tmask[w][0][l], bit);
-                if (code & 2) atomicOr(&tmask[w][1][l], bit);
-                if (code & 4) atomicOr(&tmask[w][2][l], bit);
-                if (code & 8) atomicOr(&tmask[w][3][l], bit);
-                atomicOr(&tmask[w][4][l], bit);
-            }
+            if (code != kCodeExit) atomicOr(&tmask[w][code][l], bit);
         } else {
             S.m.code[a] = code;
         }
@@ -304,10 +298,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.m.U(c) = 0;
         S.m.L0(c) = L;
         S.m.M(c) = movers[w][lane];
-        if (DIM == 2) {
+        if (DIM == 2) {  // bit j of a mover's neighbour code in plane j
+            uint64_t P[4] = {0, 0, 0, 0}, RT = 0;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) S.m.P(c, j) = tmask[w][j][lane];
-            S.m.RT(c) = tmask[w][4][lane];
+            for (int k = 0; k < 9; ++k) {
+                const uint64_t t = tmask[w][k][lane];
+                RT |= t;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if ((k >> j) & 1) P[j] |= t;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) S.m.P(c, j) = P[j];
+            S.m.RT(c) = RT;
             S.m.UN(c) = 0;  // a renormalised offset lies inside its new cell
         }
     }
@@ -334,9 +337,21 @@ __global__ void __launch_bounds__(kThreads)
     int64_t I[3] = {0, 0, 0};
     if (valid) cell_coords(g, c, I);
     const int comps = S.m.comps;
+    const int lane = threadIdx.x & 31;
+    const uint64_t empty = ~(L0 | L);
+    // whole sectors where the values are known, as in the FP64 apply (8 offsets per sector)
     for (int s = 0; s < (int)hi_any; ++s) {
-        if (!((changed >> s) & 1)) continue;
+        const bool chg = (changed >> s) & 1;
+        const uint32_t row = __ballot_sync(0xffffffffu, chg);
+        if (!row) continue;
         const int64_t a = c + nc * s;
+        if (valid) index[a] = (uint8_t)((L >> s) & 1);
+        if (!chg) {
+            if (valid && ((empty >> s) & 1) && (row & sector_lanes(a, lane, 8)))
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) Xi.x[d][a] = CUDART_NAN_F;
+            continue;
+        }
         if ((R >> s) & 1) {
             const uint16_t tag = S.m.orig[a];
             int off[3];
@@ -360,12 +375,10 @@ __global__ void __launch_bounds__(kThreads)
                 for (int d = 0; d < DIM; ++d) Xi.x[d][a] = rec[d];
                 for (int k = 0; k < A.n; ++k) A.a[k][a] = rec[DIM + k];
             }
-            index[a] = 1;
         } else {
 #pragma unroll
             for (int d = 0; d < DIM; ++d) Xi.x[d][a] = CUDART_NAN_F;
             for (int k = 0; k < A.n; ++k) A.a[k][a] = CUDART_NAN_F;
-            index[a] = 0;
         }
     }
 }

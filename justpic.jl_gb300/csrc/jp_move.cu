@@ -71,8 +71,8 @@ __device__ __forceinline__ int64_t find_cell_key(double px, long long kp, const 
 // A warp covers 32 consecutive cells and spreads their live particles over its
 // lanes in slot-major order (full lanes whatever the occupancy), two particles
 // per lane in flight: coordinates and fields are loaded together, then the
-// particles are classified (their movers' bits and destination planes go to
-// the cells' masks in shared memory), and after a warp barrier each routed
+// particles are classified (their movers' bits go to per-target masks in
+// shared memory, one atomic each), and after a warp barrier each routed
 // mover writes its record to its cell's next records: its rank is the number of
 // movers in lower slots of its cell, all of which lie in this or an earlier
 // batch (slot-major order).
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     __shared__ long long cellk[kWarpsPerBlock][32][2 * DIM];  // keys of corner and corner + dx
     __shared__ int cellI[kWarpsPerBlock][32][3];
     __shared__ unsigned long long movers[kWarpsPerBlock][32];
-    constexpr int NT = DIM == 2 ? 6 : 1;  // 2D: the four destination planes, routed, unstable
+    constexpr int NT = DIM == 2 ? 10 : 1;  // 2D: movers bound for each of the 9 neighbours, unstable ones
     __shared__ unsigned long long tmask[kWarpsPerBlock][NT][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
@@ -159,13 +159,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         }
         if (DIM == 2) {
             if (code != kCodeExit) {
-                const int k = code & 0x1F;
-                if (k & 1) atomicOr(&tmask[w][0][l], bit);
-                if (k & 2) atomicOr(&tmask[w][1][l], bit);
-                if (k & 4) atomicOr(&tmask[w][2][l], bit);
-                if (k & 8) atomicOr(&tmask[w][3][l], bit);
-                atomicOr(&tmask[w][4][l], bit);
-                if (code & kCodeUnstable) atomicOr(&tmask[w][5][l], bit);
+                atomicOr(&tmask[w][code & 0x1F][l], bit);
+                if (code & kCodeUnstable) atomicOr(&tmask[w][9][l], bit);
             }
         } else {
             S.code[a] = code;
@@ -225,11 +220,20 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.U(c) = 0;
         S.L0(c) = L;
         S.M(c) = movers[w][lane];
-        if (DIM == 2) {
+        if (DIM == 2) {  // bit j of a mover's neighbour code in plane j
+            uint64_t P[4] = {0, 0, 0, 0}, RT = 0;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) S.P(c, j) = tmask[w][j][lane];
-            S.RT(c) = tmask[w][4][lane];
-            S.UN(c) = tmask[w][5][lane];
+            for (int k = 0; k < 9; ++k) {
+                const uint64_t t = tmask[w][k][lane];
+                RT |= t;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if ((k >> j) & 1) P[j] |= t;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) S.P(c, j) = P[j];
+            S.RT(c) = RT;
+            S.UN(c) = tmask[w][9][lane];
         }
     }
     add_move_counts(g.counts, n_exit, n_far, 0);
@@ -238,8 +242,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 
 // ----------------------------------------------------------------- apply
 // Slot-major over a warp's 32 cells: at each slot the lanes whose slot changed
-// store together, so every 32-byte sector is written in one go. A refilled
-// slot gathers its record from the source cell named by its origin tag.
+// store together. A refilled slot gathers its record from the source cell
+// named by its origin tag. A sector only partly written is read back from DRAM
+// by L2, so the stores complete sectors with values already known: every lane
+// writes its occupancy byte of a row that changed anywhere, and an empty slot
+// that stays empty next to a changed one rewrites its coordinates' NaN (empty
+// slots always hold NaN coordinates). Live slots that stay are not touched.
 template <int DIM>
 __global__ void __launch_bounds__(kThreads)
     move_apply(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, MoveView S)
@@ -259,9 +267,20 @@ __global__ void __launch_bounds__(kThreads)
     if (hi_any == 0) return;
     int64_t I[3] = {0, 0, 0};
     if (valid) cell_coords(g, c, I);
+    const int lane = threadIdx.x & 31;
+    const uint64_t empty = ~(L0 | L);
     for (int s = 0; s < (int)hi_any; ++s) {
-        if (!((changed >> s) & 1)) continue;
+        const bool chg = (changed >> s) & 1;
+        const uint32_t row = __ballot_sync(0xffffffffu, chg);
+        if (!row) continue;
         const int64_t a = c + nc * s;
+        if (valid) index[a] = (uint8_t)((L >> s) & 1);
+        if (!chg) {
+            if (valid && ((empty >> s) & 1) && (row & sector_lanes(a, lane, 4)))
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) X.c[d][a] = CUDART_NAN;
+            continue;
+        }
         if ((R >> s) & 1) {
             const uint16_t tag = S.orig[a];
             int off[3];
@@ -285,12 +304,10 @@ __global__ void __launch_bounds__(kThreads)
                 for (int d = 0; d < DIM; ++d) X.c[d][a] = rp[d];
                 for (int k = 0; k < A.n; ++k) A.a[k][a] = rp[DIM + k];
             }
-            index[a] = 1;
         } else {
 #pragma unroll
             for (int d = 0; d < DIM; ++d) X.c[d][a] = CUDART_NAN;
             for (int k = 0; k < A.n; ++k) A.a[k][a] = CUDART_NAN;
-            index[a] = 0;
         }
     }
 }
