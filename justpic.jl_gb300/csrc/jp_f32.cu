@@ -337,21 +337,9 @@ __global__ void __launch_bounds__(kThreads)
     int64_t I[3] = {0, 0, 0};
     if (valid) cell_coords(g, c, I);
     const int comps = S.m.comps;
-    const int lane = threadIdx.x & 31;
-    const uint64_t empty = ~(L0 | L);
-    // whole sectors where the values are known, as in the FP64 apply (8 offsets per sector)
     for (int s = 0; s < (int)hi_any; ++s) {
-        const bool chg = (changed >> s) & 1;
-        const uint32_t row = __ballot_sync(0xffffffffu, chg);
-        if (!row) continue;
+        if (!((changed >> s) & 1)) continue;
         const int64_t a = c + nc * s;
-        if (valid) index[a] = (uint8_t)((L >> s) & 1);
-        if (!chg) {
-            if (valid && ((empty >> s) & 1) && (row & sector_lanes(a, lane, 8)))
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) Xi.x[d][a] = CUDART_NAN_F;
-            continue;
-        }
         if ((R >> s) & 1) {
             const uint16_t tag = S.m.orig[a];
             int off[3];
@@ -375,10 +363,12 @@ __global__ void __launch_bounds__(kThreads)
                 for (int d = 0; d < DIM; ++d) Xi.x[d][a] = rec[d];
                 for (int k = 0; k < A.n; ++k) A.a[k][a] = rec[DIM + k];
             }
+            index[a] = 1;
         } else {
 #pragma unroll
             for (int d = 0; d < DIM; ++d) Xi.x[d][a] = CUDART_NAN_F;
             for (int k = 0; k < A.n; ++k) A.a[k][a] = CUDART_NAN_F;
+            index[a] = 0;
         }
     }
 }

@@ -242,12 +242,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 
 // ----------------------------------------------------------------- apply
 // Slot-major over a warp's 32 cells: at each slot the lanes whose slot changed
-// store together. A refilled slot gathers its record from the source cell
-// named by its origin tag. A sector only partly written is read back from DRAM
-// by L2, so the stores complete sectors with values already known: every lane
-// writes its occupancy byte of a row that changed anywhere, and an empty slot
-// that stays empty next to a changed one rewrites its coordinates' NaN (empty
-// slots always hold NaN coordinates). Live slots that stay are not touched.
+// store together, so every 32-byte sector is written in one go. A refilled
+// slot gathers its record from the source cell named by its origin tag.
 template <int DIM>
 __global__ void __launch_bounds__(kThreads)
     move_apply(DevGrid g, Coords X, uint8_t* __restrict__ index, Args A, MoveView S)
@@ -267,20 +263,9 @@ __global__ void __launch_bounds__(kThreads)
     if (hi_any == 0) return;
     int64_t I[3] = {0, 0, 0};
     if (valid) cell_coords(g, c, I);
-    const int lane = threadIdx.x & 31;
-    const uint64_t empty = ~(L0 | L);
     for (int s = 0; s < (int)hi_any; ++s) {
-        const bool chg = (changed >> s) & 1;
-        const uint32_t row = __ballot_sync(0xffffffffu, chg);
-        if (!row) continue;
+        if (!((changed >> s) & 1)) continue;
         const int64_t a = c + nc * s;
-        if (valid) index[a] = (uint8_t)((L >> s) & 1);
-        if (!chg) {
-            if (valid && ((empty >> s) & 1) && (row & sector_lanes(a, lane, 4)))
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) X.c[d][a] = CUDART_NAN;
-            continue;
-        }
         if ((R >> s) & 1) {
             const uint16_t tag = S.orig[a];
             int off[3];
@@ -304,10 +289,12 @@ __global__ void __launch_bounds__(kThreads)
                 for (int d = 0; d < DIM; ++d) X.c[d][a] = rp[d];
                 for (int k = 0; k < A.n; ++k) A.a[k][a] = rp[DIM + k];
             }
+            index[a] = 1;
         } else {
 #pragma unroll
             for (int d = 0; d < DIM; ++d) X.c[d][a] = CUDART_NAN;
             for (int k = 0; k < A.n; ++k) A.a[k][a] = CUDART_NAN;
+            index[a] = 0;
         }
     }
 }

@@ -48,16 +48,6 @@ struct MoveView {
 
 __device__ __forceinline__ uint16_t make_tag(int code, int rank) { return (uint16_t)(code | (rank << 5)); }
 
-// The lanes of a warp on consecutive cells whose elements of slot row a share
-// this lane's 32-byte sector (`per` elements per sector, the array assumed to
-// start on a sector boundary; used only to choose which sectors to complete).
-__device__ __forceinline__ uint32_t sector_lanes(int64_t a, int lane, int per)
-{
-    const int first = lane - (int)(a & (int64_t)(per - 1));
-    const int lo = first < 0 ? 0 : first, hi = first + per - 1 > 31 ? 31 : first + per - 1;
-    const uint32_t upto = hi == 31 ? 0xffffffffu : ((1u << (hi + 1)) - 1u);
-    return upto & ~((1u << lo) - 1u);
-}
 
 // position of the n-th set bit (n from 0) of a 64-bit mask
 __device__ __forceinline__ int nth_set_bit64(uint64_t m, int n)
