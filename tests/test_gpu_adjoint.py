@@ -72,6 +72,13 @@ def test_advection_vjp_matches_fd(method):
         jp.advection_(p, pm, Vd, dt)
         return [c.data.cpu().numpy().copy() for c in p.coords]
 
+    # A particle whose stage point leaves a velocity grid's limits is sent to Inf
+    # (src/Particles/Advection/advection.jl:104-108) whatever the perturbation: it
+    # carries no derivative and the adjoint gives it none. Such particles (and the
+    # empty slots, NaN) are left out of the finite differences explicitly.
+    base = forward(V)
+    on_grid = live.cpu().numpy() & np.isfinite(base[0]) & np.isfinite(base[1])
+    lam_np = [np.where(on_grid, l, 0.0) for l in lam_np]
     lam = [torch.from_numpy(l).cuda() for l in lam_np]
     gV = tuple(jp.grid_field(v.shape) for v in Vh)
     A.advection_vjp_(p, pm, V, dt, X0, A._Idx(p.index.data), lam, gV)
@@ -84,13 +91,13 @@ def test_advection_vjp_matches_fd(method):
             Vp[c][node] += h
             Vm[c][node] -= h
             xp, xm = forward(_dev(Vp)), forward(_dev(Vm))
-            fd.append(sum(np.sum((xp[d] - xm[d])[live.cpu().numpy()] * lam_np[d][live.cpu().numpy()])
-                          for d in range(2)) / (2 * h))
+            assert all(np.all(np.isfinite(x[d][on_grid])) for x in (xp, xm) for d in range(2))
+            fd.append(sum(np.sum((xp[d][on_grid] - xm[d][on_grid]) * lam_np[d][on_grid]) for d in range(2)) / (2 * h))
             adj.append(gV[c].cpu().numpy()[node])
         _close(adj, fd, f"{method} dL/dV{'xy'[c]}")
     # positions
     hx = 1e-9
-    slots = np.argwhere(live.cpu().numpy())
+    slots = np.argwhere(on_grid)
     sel = slots[rng.choice(len(slots), 12, replace=False)]
     lam0 = [l.cpu().numpy() for l in lam]
     for d in range(2):
