@@ -81,20 +81,27 @@ def algorithmic_bytes(op, N, nf, m, slots_per_live, grid_bytes_per_live, field_b
     raise KeyError(op)
 
 
-# DRAM bytes per live particle of each call, FP64 form, 2D, one particle field:
-# dram__bytes_read.sum + dram__bytes_write.sum of the call's kernels in one ncu
-# capture of a 512x512-cell C2 case (5.79M particles), divided by its particle
+# DRAM bytes per live particle of each call, 2D, one particle field:
+# dram__bytes_read.sum + dram__bytes_write.sum of the call's kernels (move:
+# classify + 9 colour passes + apply; injection: flag + 4 passes) in one ncu
+# capture of a 512x512-cell C2 case (5.77M particles), divided by its particle
 # count. Traffic grows with the particle count, so the bench scales it by the
-# live particles of its own run.
+# live particles of its own run. FP64 form:
 DRAM_BYTES_PER_PARTICLE_2D_F64 = {
-    "particle2grid!": 673.6e6 / 5.790e6,
-    "advection!": 306.2e6 / 5.790e6,
-    "grid2particle!": 309.5e6 / 5.790e6,
-    "move_particles!": (444.8e6 + 9 * 14.8e6 + 923.5e6) / 5.790e6,  # classify + 9 colour passes + apply
-    "inject_particles!": 333.1e6 / 5.790e6,
+    "particle2grid!": 103.05,
+    "advection!": 47.57,
+    "grid2particle!": 46.87,
+    "move_particles!": 192.40,
+    "inject_particles!": 55.83,
 }
-# the same for the split-precision form (FP32 offsets and fields)
-DRAM_BYTES_PER_PARTICLE_2D_F32 = {}
+# the split-precision form (FP32 offsets and fields)
+DRAM_BYTES_PER_PARTICLE_2D_F32 = {
+    "particle2grid!": 29.17,
+    "advection!": 21.10,
+    "grid2particle!": 23.63,
+    "move_particles!": 115.83,
+    "inject_particles!": 54.02,
+}
 
 
 def fp64_instructions(op, N, method):

@@ -161,7 +161,7 @@ int jp_move_particles(jp_particles* p, double* const coords[3], uint8_t* index,
  * a shadow record per slot) comes from one fixed device array of
  * JP_NOALLOC_SCRATCH_BYTES that is part of the library: every GPU on which the
  * library is loaded holds it until the process exits. A container needing more
- * (120 bytes per cell in 2D, 40 in 3D, rounded up to a multiple of 256, plus (8*s+3) bytes
+ * (88 bytes per cell in 2D, 40 in 3D, rounded up to a multiple of 256, plus (8*s+3) bytes
  * per slot with s = ndim+nargs, 4 when that is 3) is rejected with
  * JP_ERR_INVALID_ARGUMENT and a message naming the sizes; use
  * jp_move_particles there. Containers of more than 64 slots per cell need no

@@ -32,6 +32,7 @@ from .api import (  # noqa: F401
     set_synchronous,
     synchronize,
 )
+from .halo import CartesianGrid, update_cell_halo_  # noqa: F401
 from .integrators import AbstractAdvectionIntegrator, Euler, RungeKutta2, RungeKutta4  # noqa: F401
 from .particles import (  # noqa: F401
     DEFAULT_SEED,
