@@ -325,6 +325,9 @@ int jp_particle2centroid(jp_particles* p, double* F, const double* Fp, const dou
  *   before the injection and 0 for injected ones; for the arrays k whose bit is
  *   set in `copies`, each existing slot also receives post[k] of the slots
  *   injected from it (set the bits of particle fields, not of positions).
+ *   With pre[k] == post[k] for every array it works in place: only the sources
+ *   receive their copies' cotangents and the injected slots keep their values,
+ *   which a following jp_permute_vjp never reads.
  * jp_advection_vjp: one advection! step (same method, alpha, V, dt) taken
  *   from coords (the positions BEFORE the step): lam holds dL/dX after the step
  *   on entry and dL/dX before it on return; dL/dV is ADDED to gV. Fails with

@@ -166,7 +166,10 @@ def slot_ids(particles: Particles, index=None) -> CellArray:
 def inject_vjp_(particles: Particles, ids: CellArray, post, pre, copies) -> None:
     """Replay of an inject_particles! call traced with ``ids``. ``copies``:
     True/False for every array, or one flag per array (True for particle
-    fields, whose values injected particles copied; False for positions)."""
+    fields, whose values injected particles copied; False for positions).
+    With ``pre`` the same arrays as ``post`` it works in place: the sources
+    gather their copies' cotangents, the injected slots keep theirs (a
+    following permute_vjp_ reads only the slots that existed before)."""
     _require_2d(particles)
     post, pre = list(post), list(pre)
     flags = [bool(copies)] * len(post) if isinstance(copies, bool) else [bool(c) for c in copies]
@@ -324,13 +327,11 @@ def reverse_sweep(particles: Particles, method, V, dt, nsteps: int, checkpoints,
             _restore(particles, checkpoints[seg])
             recs = [_recorded_step(particles, method, V, dt, (), inject) for _ in range(n0, n1)]
         for X, idx, dest, ids in reversed(recs):
-            if ids is not None:
-                inject_vjp_(particles, ids, lam + [gT], tmp_x + [tmp_t], copies=(False, False, True))
-                permute_vjp_(particles, dest, tmp_x + [tmp_t], lam + [gT])
-            else:
-                permute_vjp_(particles, dest, lam + [gT], tmp_x + [tmp_t])
-                lam, tmp_x = tmp_x, lam
-                gT, tmp_t = tmp_t, gT
+            if ids is not None:  # in place: the sources gather their copies' field cotangents
+                inject_vjp_(particles, ids, lam + [gT], lam + [gT], copies=(False, False, True))
+            permute_vjp_(particles, dest, lam + [gT], tmp_x + [tmp_t])
+            lam, tmp_x = tmp_x, lam
+            gT, tmp_t = tmp_t, gT
             advection_vjp_recorded_(particles, method, dt, X, _Idx(idx), lam, gV)
     _restore(particles, checkpoints[0])
     ni = particles.ni
@@ -691,13 +692,11 @@ def misfit_gradient_f32(particles: Particles, xi, method, V, dt, nsteps: int, T0
                     _restore_f32(particles, xi, cps[seg])
                     recs = [_recorded_step_f32(particles, xi, method, V, dt, (), inject) for _ in range(n0, n1)]
                 for X, idx, dest, ids in reversed(recs):
-                    if ids is not None:
-                        inject_vjp_i32_(particles, ids, lam + [gTd], tmp_x + [tmp_t], copies=(False, False, True))
-                        permute_vjp_(particles, dest, tmp_x + [tmp_t], lam + [gTd])
-                    else:
-                        permute_vjp_(particles, dest, lam + [gTd], tmp_x + [tmp_t])
-                        lam, tmp_x = tmp_x, lam
-                        gTd, tmp_t = tmp_t, gTd
+                    if ids is not None:  # in place, as in misfit_gradient's sweep
+                        inject_vjp_i32_(particles, ids, lam + [gTd], lam + [gTd], copies=(False, False, True))
+                    permute_vjp_(particles, dest, lam + [gTd], tmp_x + [tmp_t])
+                    lam, tmp_x = tmp_x, lam
+                    gTd, tmp_t = tmp_t, gTd
                     advection_vjp_f32_(particles, method, V, dt, X, _Idx(idx), lam, gV)
     finally:
         _restore_f32(particles, xi, start)

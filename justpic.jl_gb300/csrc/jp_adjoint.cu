@@ -197,6 +197,44 @@ __global__ void __launch_bounds__(kThreads)
     raise_err(d_err, errs);
 }
 
+// Source cell c adds to pre[k][src] (arrays k in `copies`) post[k][b] of every
+// slot b injected from one of its slots: cells of the window in order (y outer,
+// x inner), slots ascending.
+template <typename IdT>
+__device__ __forceinline__ void gather_copies(const DevGrid& g, const IdT* __restrict__ ids,
+                                              const uint64_t* __restrict__ inj, const PermArrays& P,
+                                              unsigned copies, int64_t c)
+{
+    const int64_t nc = g.ncells;
+    const int64_t ns = nc * g.max_xcell;
+    const int64_t cx = c % g.n[0], cy = c / g.n[0];
+    constexpr int RW = 2 * kInjectReach + 1;  // window width
+    const int64_t x0 = cx - kInjectReach;
+    for (int64_t y = max(cy - kInjectReach, (int64_t)0); y <= min(cy + kInjectReach, g.n[1] - 1); ++y) {
+        // the injected-slot masks of one window row, loaded together
+        uint64_t row[RW];
+#pragma unroll
+        for (int j = 0; j < RW; ++j) {
+            const int64_t x = x0 + j;
+            row[j] = (x >= 0 && x < g.n[0]) ? inj[x + g.n[0] * y] : 0ull;
+        }
+#pragma unroll
+        for (int j = 0; j < RW; ++j) {
+            const int64_t w = (x0 + j) + g.n[0] * y;
+            uint64_t m = row[j];
+            while (m) {
+                const int s = __ffsll((long long)m) - 1;
+                m &= m - 1;
+                const int64_t b = w + nc * s;
+                const int64_t src = id_slot(ids[b], ns);  // a slot index: inject_mask_kernel checked it
+                if (src % nc != c) continue;
+                for (int k = 0; k < P.n; ++k)
+                    if ((copies >> k) & 1u) P.pre[k][src] += P.post[k][b];
+            }
+        }
+    }
+}
+
 // pre[k][a] = post[k][a] for slots that existed before the injection (id ==
 // own slot), 0 otherwise; for the arrays k in the `copies` bit mask, a
 // pre-existing slot also collects post[k][b] of every slot b injected from it,
@@ -230,33 +268,21 @@ __global__ void __launch_bounds__(kThreads)
         }
     }
     if (!copies || !srcflag[c]) return;
-    const int64_t ns = nc * g.max_xcell;
-    const int64_t cx = c % g.n[0], cy = c / g.n[0];
-    constexpr int RW = 2 * kInjectReach + 1;  // window width
-    const int64_t x0 = cx - kInjectReach;
-    for (int64_t y = max(cy - kInjectReach, (int64_t)0); y <= min(cy + kInjectReach, g.n[1] - 1); ++y) {
-        // the injected-slot masks of one window row, loaded together
-        uint64_t row[RW];
-#pragma unroll
-        for (int j = 0; j < RW; ++j) {
-            const int64_t x = x0 + j;
-            row[j] = (x >= 0 && x < g.n[0]) ? inj[x + g.n[0] * y] : 0ull;
-        }
-#pragma unroll
-        for (int j = 0; j < RW; ++j) {
-            const int64_t w = (x0 + j) + g.n[0] * y;
-            uint64_t m = row[j];
-            while (m) {
-                const int s = __ffsll((long long)m) - 1;
-                m &= m - 1;
-                const int64_t b = w + nc * s;
-                const int64_t src = id_slot(ids[b], ns);  // a slot index: inject_mask_kernel checked it
-                if (src % nc != c) continue;
-                for (int k = 0; k < P.n; ++k)
-                    if ((copies >> k) & 1u) P.pre[k][src] += P.post[k][b];
-            }
-        }
-    }
+    gather_copies(g, ids, inj, P, copies, c);
+}
+
+// The in-place form (pre == post): only the sources gather their copies'
+// cotangents. The slots the injection filled keep their values: the move's
+// transpose that follows reads only the slots that existed before the
+// injection, and those are the ones this leaves as they were (plus the copies).
+template <typename IdT>
+__global__ void __launch_bounds__(kThreads)
+    inject_vjp_inplace_kernel(DevGrid g, const IdT* __restrict__ ids, const uint64_t* __restrict__ inj,
+                              const unsigned* __restrict__ srcflag, PermArrays P, unsigned copies)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells || !srcflag[c]) return;
+    gather_copies(g, ids, inj, P, copies, c);
 }
 
 // --------------------------------------------------------- advection step
@@ -692,9 +718,11 @@ constexpr int kDepThreads = 128;
 
 // Deposit: one thread per owning cell adds its particles' staged samples, in
 // slot order, to the cell's 40 window partial sums (shared memory), then
-// writes them out for the node gather. The lanes of a warp walk the slots
-// together (up to the highest live slot of the warp), so every load of the
-// staged arrays is coalesced across the warp's 32 cells.
+// writes them out for the node gather. Each lane takes its own cell's live
+// slots in order (the warp runs as many rounds as its fullest cell has
+// particles, not as its highest live slot): the kernel is bound by FP64 issue,
+// and a lane idling on an empty slot row wastes it. The k-th live slots of
+// neighbouring cells mostly share a row, so the staged loads stay close.
 template <int NQ>
 __global__ void __launch_bounds__(kDepThreads)
     deposit_kernel(DevGrid g, const uint8_t* __restrict__ index, Staging stg, double* __restrict__ parts)
@@ -706,10 +734,10 @@ __global__ void __launch_bounds__(kDepThreads)
     const int64_t ns = stg.nslots;
     const int t = threadIdx.x;
     for (int k = 0; k < kWinParts; ++k) part[k][t] = 0.0;
-    const uint64_t m = valid ? live_mask(index, c, nc, g.max_xcell) : 0;
-    const uint32_t hi = __reduce_max_sync(0xffffffffu, m ? 64u - (uint32_t)__clzll((long long)m) : 0u);
-    for (int s = 0; s < (int)hi; ++s) {
-        if (!((m >> s) & 1)) continue;
+    uint64_t m = valid ? live_mask(index, c, nc, g.max_xcell) : 0;
+    while (m) {
+        const int s = __ffsll((long long)m) - 1;
+        m &= m - 1;
         const int64_t a = c + nc * s;
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
@@ -1190,13 +1218,20 @@ static cudaError_t inject_vjp(jp_particles* P, const IdT* ids, const double* con
     cudaError_t e = ensure_adjoint_scratch(P);
     if (e != cudaSuccess) return e;
     const unsigned nb = grid_blocks(P->g.ncells);
+    const bool inplace = n > 0 && post[0] == pre[0];  // the C ABI checked that all or none alias
     if (copies) {
         e = cudaMemsetAsync(adj_srcflag(P), 0, (size_t)P->g.ncells * sizeof(unsigned), P->stream);
         if (e != cudaSuccess) return e;
         inject_mask_kernel<IdT><<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), adj_srcflag(P), P->d_err);
     }
-    inject_vjp_kernel<IdT><<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), adj_srcflag(P),
-                                                           perm_arrays(post, pre, n), copies);
+    if (inplace) {
+        if (copies)
+            inject_vjp_inplace_kernel<IdT><<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), adj_srcflag(P),
+                                                                           perm_arrays(post, pre, n), copies);
+    } else {
+        inject_vjp_kernel<IdT><<<nb, kThreads, 0, P->stream>>>(P->g, ids, adj_inj(P), adj_srcflag(P),
+                                                               perm_arrays(post, pre, n), copies);
+    }
     return cudaGetLastError();
 }
 

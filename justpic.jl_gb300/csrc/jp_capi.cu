@@ -569,9 +569,10 @@ int jp_inject_vjp(jp_particles* P, const double* ids, const double* const* post,
     if (!P || !ids || !post || !pre || n < 0 || n > 8)
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp: bad arguments");
     if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp: the adjoint is built for 2D");
+    // in place (pre[k] == post[k] for every array) or out of place (no array aliased)
     for (int k = 0; k < n; ++k)
-        if (!post[k] || !pre[k] || post[k] == pre[k])
-            return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp: null or aliased array");
+        if (!post[k] || !pre[k] || (post[k] == pre[k]) != (post[0] == pre[0]))
+            return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp: null array, or only some arrays aliased");
     return finish(P, jp::launch_inject_vjp(P, ids, post, pre, n, (unsigned)copies & ((1u << n) - 1u)),
                   "jp_inject_vjp");
 }
@@ -656,9 +657,10 @@ int jp_inject_vjp_i32(jp_particles* P, const int32_t* ids, const double* const* 
     if (!P || !ids || !post || !pre || n < 0 || n > 8)
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp_i32: bad arguments");
     if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp_i32: the adjoint is built for 2D");
+    // in place (pre[k] == post[k] for every array) or out of place (no array aliased)
     for (int k = 0; k < n; ++k)
-        if (!post[k] || !pre[k] || post[k] == pre[k])
-            return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp_i32: null or aliased array");
+        if (!post[k] || !pre[k] || (post[k] == pre[k]) != (post[0] == pre[0]))
+            return fail(JP_ERR_INVALID_ARGUMENT, "jp_inject_vjp_i32: null array, or only some arrays aliased");
     return finish(P, jp::launch_inject_vjp_i32(P, ids, post, pre, n, (unsigned)copies & ((1u << n) - 1u)),
                   "jp_inject_vjp_i32");
 }

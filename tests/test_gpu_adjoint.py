@@ -343,6 +343,15 @@ def test_inject_ids_name_the_sources():
     ref_t = ref_x.reshape(-1).copy()
     np.add.at(ref_t, src, pn[new])
     np.testing.assert_allclose(pre_t.cpu().numpy().reshape(-1), ref_t, rtol=1e-14, atol=1e-300)
+    # in place: the slots that existed before the injection get the same values as
+    # out of place (bit for bit); the injected ones keep theirs
+    inp = [post.clone(), post.clone()]
+    A.inject_vjp_(p, ids, inp, inp, copies=(False, True))
+    assert torch.equal(inp[0][torch.from_numpy(live0).cuda()], pre_x[torch.from_numpy(live0).cuda()])
+    assert torch.equal(inp[1][torch.from_numpy(live0).cuda()], pre_t[torch.from_numpy(live0).cuda()])
+    assert torch.equal(inp[1][torch.from_numpy(new).cuda()], post[torch.from_numpy(new).cuda()])
+    with pytest.raises(jp.ArgumentError):
+        A.inject_vjp_(p, ids, [post, post], [post, torch.empty_like(post)], copies=True)
 
 
 # ------------------------------------------------------------ whole run
