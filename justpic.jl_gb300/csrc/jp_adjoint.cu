@@ -718,11 +718,9 @@ constexpr int kDepThreads = 128;
 
 // Deposit: one thread per owning cell adds its particles' staged samples, in
 // slot order, to the cell's 40 window partial sums (shared memory), then
-// writes them out for the node gather. Each lane takes its own cell's live
-// slots in order (the warp runs as many rounds as its fullest cell has
-// particles, not as its highest live slot): the kernel is bound by FP64 issue,
-// and a lane idling on an empty slot row wastes it. The k-th live slots of
-// neighbouring cells mostly share a row, so the staged loads stay close.
+// writes them out for the node gather. The lanes of a warp walk the slots
+// together (up to the highest live slot of the warp), so every load of the
+// staged arrays is coalesced across the warp's 32 cells.
 template <int NQ>
 __global__ void __launch_bounds__(kDepThreads)
     deposit_kernel(DevGrid g, const uint8_t* __restrict__ index, Staging stg, double* __restrict__ parts)
@@ -734,10 +732,10 @@ __global__ void __launch_bounds__(kDepThreads)
     const int64_t ns = stg.nslots;
     const int t = threadIdx.x;
     for (int k = 0; k < kWinParts; ++k) part[k][t] = 0.0;
-    uint64_t m = valid ? live_mask(index, c, nc, g.max_xcell) : 0;
-    while (m) {
-        const int s = __ffsll((long long)m) - 1;
-        m &= m - 1;
+    const uint64_t m = valid ? live_mask(index, c, nc, g.max_xcell) : 0;
+    const uint32_t hi = __reduce_max_sync(0xffffffffu, m ? 64u - (uint32_t)__clzll((long long)m) : 0u);
+    for (int s = 0; s < (int)hi; ++s) {
+        if (!((m >> s) & 1)) continue;
         const int64_t a = c + nc * s;
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
