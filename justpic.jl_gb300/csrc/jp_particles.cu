@@ -586,30 +586,13 @@ __global__ void __launch_bounds__(kThreads)
     const int64_t cols = DIM == 2 ? V0 : V0 * V1;
     const int64_t nc = g.ncells;
     const int M = g.max_xcell;
-    // 2D: a warp takes 32 consecutive vertex columns. 3D: a warp takes a tile of
-    // 8 x 4 vertex columns (lane = x + 8 y), so the four vertex columns reading a
-    // cell of a row sit in one warp (the cell's particles are loaded once into L1
-    // for all of them) and the neighbouring cells' masks come from the lanes.
-    int64_t i, j, q;
-    bool active;
-    if (DIM == 2) {
-        active = t < nthreads;
-        const int64_t col = active ? t % cols : 0;
-        q = active ? t / cols : 0;
-        i = col % V0;
-        j = 0;
-    } else {
-        const int64_t tx = (V0 + 7) >> 3, ty = (V1 + 3) >> 2, tiles = tx * ty;
-        const int64_t warp = t >> 5;
-        const int64_t tile = warp % tiles;
-        q = warp / tiles;
-        i = (tile % tx) * 8 + (lane & 7);
-        j = (tile / tx) * 4 + (lane >> 3);
-        active = t < nthreads && i < V0 && j < V1;
-        if (!active) i = j = 0;
-    }
+    const bool active = t < nthreads;
+    const int64_t col = active ? t % cols : 0;
+    const int64_t q = active ? t / cols : 0;
     const int64_t r0 = q * chunk;
     const int64_t r1 = active ? min(r0 + (int64_t)chunk, nlast + 1) : r0;
+    const int64_t i = col % V0;
+    const int64_t j = DIM == 3 ? col / V0 : 0;
     const bool has_i0 = i >= 1, has_i1 = i < g.n[0];          // cells i-1 and i exist
     const bool has_j0 = DIM == 2 || j >= 1, has_j1 = DIM == 2 || j < g.n[1];
     double q_cur[3] = {0.0, 0.0, 0.0}, q_nxt[3] = {0.0, 0.0, 0.0};
@@ -625,22 +608,13 @@ __global__ void __launch_bounds__(kThreads)
         const bool rok = active && r >= 0 && r < nlast;
         // own cell (i, j, r) and its left neighbour (i-1, j, r) from the lane to the left
         const uint64_t m_own = (rok && has_i1 && has_j1) ? live_mask(index, cell(0, 0, r), nc, M) : 0;
-        // the lane to the left holds vertex column i-1 (2D: lanes 1..31; 3D: x > 0 in the tile)
-        const bool left_in_warp = DIM == 2 ? lane != 0 : (lane & 7) != 0;
         uint64_t m_left = __shfl_up_sync(0xffffffffu, m_own, 1);
-        if (!left_in_warp && rok && has_i0 && has_j1) m_left = live_mask(index, cell(-1, 0, r), nc, M);
+        if (lane == 0 && rok && has_i0 && has_j1) m_left = live_mask(index, cell(-1, 0, r), nc, M);
         if (!(rok && has_i0 && has_j1)) m_left = 0;
         if (DIM == 3) {
-            // row j-1 first (joffset = -1), then row j; from the tile row below when it is in the warp
-            const bool below_in_warp = (lane >> 3) != 0;
-            uint64_t mb1 = __shfl_up_sync(0xffffffffu, m_own, 8);
-            uint64_t mb0 = __shfl_up_sync(0xffffffffu, m_left, 8);
-            if (!below_in_warp) {
-                mb1 = (rok && has_i1 && has_j0) ? live_mask(index, cell(0, -1, r), nc, M) : 0;
-                mb0 = (rok && has_i0 && has_j0) ? live_mask(index, cell(-1, -1, r), nc, M) : 0;
-            }
-            if (!(rok && has_i1 && has_j0)) mb1 = 0;
-            if (!(rok && has_i0 && has_j0)) mb0 = 0;
+            // row j-1 first (joffset = -1), then row j
+            const uint64_t mb0 = (rok && has_i0 && has_j0) ? live_mask(index, cell(-1, -1, r), nc, M) : 0;
+            const uint64_t mb1 = (rok && has_i1 && has_j0) ? live_mask(index, cell(0, -1, r), nc, M) : 0;
             if (mb0) p2g_cell<DIM, NF>(cell(-1, -1, r), mb0, nc, q_cur, q_nxt, do_cur, do_nxt, PF, X, w_c, wF_c, w_n, wF_n);
             if (mb1) p2g_cell<DIM, NF>(cell(0, -1, r), mb1, nc, q_cur, q_nxt, do_cur, do_nxt, PF, X, w_c, wF_c, w_n, wF_n);
         }
@@ -901,8 +875,7 @@ static cudaError_t p2g_launch(jp_particles* P, double* const* F, const double* c
     const int64_t want = 152LL * 2048;
     int chunk = (int)((cols * rows) / want);
     chunk = chunk < 2 ? 2 : (chunk > 16 ? 16 : chunk);
-    const int64_t nchunks = (rows + chunk - 1) / chunk;
-    const int64_t nthreads = d3 ? 32 * ((V0 + 7) / 8) * ((V1 + 3) / 4) * nchunks : cols * nchunks;
+    const int64_t nthreads = cols * ((rows + chunk - 1) / chunk);
     const unsigned nb = grid_blocks(nthreads);
     const unsigned nbw = grid_blocks(V0 * V1 * (d3 ? P->g.n[2] + 1 : 1));
     for (int f0 = 0; f0 < nf; f0 += kFieldsPerLaunch) {
