@@ -841,13 +841,28 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, METHOD == JP_RUNGE_KUTTA4
     const int64_t ns = stg.nslots;
     const double wd[2] = {(double)P.w[0], (double)P.w[1]}, awd[2] = {(double)P.aw[0], (double)P.aw[1]};
     int errs = 0;
+    // the next particle's offsets and cotangents are loaded while this one is worked on
+    auto fetch = [&](int kk, int64_t& a, int& l, float* x0, double* lam) {
+        int s;
+        slot_item(lists[w], M, kk, &s, &l);
+        a = c0 + l + nc * s;
+        x0[0] = Xi.x[0][a];
+        x0[1] = Xi.x[1][a];
+        lam[0] = Lam.c[0][a];
+        lam[1] = Lam.c[1][a];
+    };
+    int64_t na = 0;
+    int nl = 0;
+    float nx0[2] = {0.0f, 0.0f};
+    double nlam[2] = {0.0, 0.0};
+    if (lane < K) fetch(lane, na, nl, nx0, nlam);
     for (int k = lane; k < K; k += 32) {
-        int s, l;
-        slot_item(lists[w], M, k, &s, &l);
-        const int64_t a = c0 + l + nc * s;
+        const int64_t a = na;
+        const int l = nl;
+        const float x0[2] = {nx0[0], nx0[1]};
+        const double lam[2] = {nlam[0], nlam[1]};
+        if (k + 32 < K) fetch(k + 32, na, nl, nx0, nlam);
         const int I[2] = {cellI[w][l][0], cellI[w][l][1]};
-        const float x0[2] = {Xi.x[0][a], Xi.x[1][a]};
-        const double lam[2] = {Lam.c[0][a], Lam.c[1][a]};
         SampF S[NS][2];
         bool ok = true;
 #pragma unroll
