@@ -32,6 +32,8 @@ struct F32Params {
     float aw[3];   // alpha * dt / dx
     float ca, cb;  // RK2 blend for alpha != 1/2
     int half;
+    int uniform;   // one spacing per axis: dx, w and aw above hold for every cell
+    F32Axes ax;    // per-cell tables (any grid)
 };
 
 __device__ __forceinline__ float lerpf1(float t, float v0, float v1) { return fmaf(t, v1, fmaf(-t, v0, v0)); }
@@ -104,6 +106,8 @@ inline F32Params make_params(const jp_particles* P, double alpha, double dt)
     p.ca = (float)std::fma(-0.5, ia, 1.0);
     p.cb = (float)(0.5 * ia);
     p.half = alpha == 0.5;
+    p.uniform = P->g.uniform;
+    p.ax = P->f32ax;
     return p;
 }
 

@@ -56,6 +56,24 @@ struct DevGrid {
     unsigned long long* counts;
 };
 
+// Per-cell spacing tables of the split-precision form, one array per axis
+// (n[d] entries), built at container creation; on a uniform grid every width
+// ratio is exactly 1. w / aw are written by each advection call (dt / dx[i],
+// alpha dt / dx[i]) when the grid is not uniform.
+struct F32Axes {
+    const float* dxf[3];              // cell widths dx[i]
+    const float* nbl[3];              // dx[i-1] / dx[i] (1 at the first cell)
+    const float* nbr[3];              // dx[i+1] / dx[i] (1 at the last cell)
+    const float* tol[3];              // dx[i] / dx[i-1]: cell i's units -> cell i-1's (1 at the first cell)
+    const float* tor[3];              // dx[i] / dx[i+1]: cell i's units -> cell i+1's (1 at the last cell)
+    const float* cl[3];               // dx[i] / (spacing of the centred nodes left of cell i's centre)
+    const float* cr[3];               // dx[i] / (spacing of the centred nodes right of it)
+    const double* tol64[3];           // the same ratios in FP64 (cell-crossing renormalisation)
+    const double* tor64[3];
+    float* wf[3];                     // per call: dt / dx[i]
+    float* awf[3];                    // per call: alpha dt / dx[i]
+};
+
 // Scratch owned by a container for move_particles! (allocated on first use).
 struct MoveScratch {
     uint64_t* rec = nullptr;  // the per-cell 64-bit slot mask arrays (layout: MoveView)
@@ -93,6 +111,8 @@ struct jp_particles {
     uint64_t inject_calls = 0;
     double dx_host[3] = {1.0, 1.0, 1.0};  // spacing per axis (uniform grids) for the split-precision form
     int staggered_std = 0;                // velocity grids have the standard ghost-node staggering
+    float* f32_block = nullptr;           // the split-precision form's per-cell tables (F32Axes)
+    jp::F32Axes f32ax{};
     int centres_ok = 0;                   // the centre grids have one node per cell and >= 2 nodes per axis
     jp::MoveScratch move;
     jp::InjectScratch inject;
