@@ -384,10 +384,14 @@ int jp_particle2grid_vjp_f32(jp_particles* p, const float* F, const double* W, c
  * slot (an implicit int32 index) plus an FP32 offset xi in [0, 1)^N in units
  * of the cell spacing, stored in the same blocklength-0 layout as the
  * coordinates (4 bytes per value). Velocity fields, particle fields and vertex
- * fields are FP32; FP64 is used only to re-normalise (cell, offset) when a
- * particle changes cell and for the weight sums of particle2grid. Uniform
- * (range) grids only. Semantics in cell units: a particle belongs to its cell
- * when 0 <= xi < 1; move_particles sends it to cell + floor(xi) with the same
+ * fields are FP32; FP64 is used for the weight sums of particle2grid. Grids:
+ * uniform, or with spacing that varies (per-cell width tables built by
+ * jp_particles_create), in both cases with the standard staggering of the
+ * velocity components (the vertex grid along the component's axis; the cell
+ * midpoints plus one ghost node at each end along the others); other grids get
+ * JP_ERR_INVALID_ARGUMENT. Semantics in cell units: a particle belongs to its
+ * cell when 0 <= xi < 1; move_particles sends it to cell + floor(xi) (the
+ * offset scaled to the new cell's width where widths differ) with the same
  * colour-pass slot allocation as the FP64 form; the other rules follow the
  * FP64 form (see jp_f32.cu). Error against the FP64 form is measured by the
  * tests and the bench.

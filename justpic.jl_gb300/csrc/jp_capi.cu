@@ -175,9 +175,10 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
         for (int64_t i = 1; i < g.n[d]; ++i) dm = (x[i + 1] - x[i]) < dm ? (x[i + 1] - x[i]) : dm;
         g.idmin[d] = 1.0 / std::fabs(dm);
     }
-    // The split-precision form samples velocities in cell units and assumes the
-    // standard staggering: component c on the vertices along axis c and on the
-    // ghost-expanded cell centres (vertex origin - dx/2 + k*dx) along the others.
+    // The split-precision form samples velocities in cell units. Its fast path
+    // takes uniform grids with the standard staggering: component c on the
+    // vertices along axis c and on the ghost-expanded cell centres (vertex origin
+    // - dx/2 + k*dx) along the others.
     P->staggered_std = grid->uniform ? 1 : 0;
     for (int c = 0; c < N && P->staggered_std; ++c)
         for (int d = 0; d < N && P->staggered_std; ++d) {
@@ -195,9 +196,73 @@ int jp_particles_create(jp_particles** out, const jp_grid_desc* grid, int32_t nx
                     break;
                 }
         }
+    // Otherwise (spacing that varies, or other ghost nodes) the form runs on per-cell
+    // tables when the staggering is the standard one on that grid: component c on
+    // the vertex grid along axis c; along the others the cell midpoints, with one
+    // ghost node below the first vertex and one above the last, the same nodes for
+    // every component.
+    std::vector<float> ftab;
+    size_t ftab_off[7][3] = {};
+    P->f32_cells = 0;
+    if (!P->staggered_std) {
+        bool ok = true;
+        for (int d = 0; d < N && ok; ++d) {
+            const double* xv = grid->xi_vel[d][d];
+            const int64_t n = g.n[d];
+            const double* z0 = nullptr;
+            for (int c = 0; c < N && ok; ++c) {
+                if (c == d) continue;
+                const double* z = grid->xi_vel[c][d];
+                if (grid->n_vel[c][d] != n + 2 || !(z[0] < xv[0]) || !(z[n + 1] > xv[n])) {
+                    ok = false;
+                    break;
+                }
+                for (int64_t k = 0; k < n && ok; ++k) {
+                    const double h = xv[k + 1] - xv[k];
+                    ok = std::fabs(z[k + 1] - 0.5 * (xv[k] + xv[k + 1])) <= 1e-9 * h * (double)(n + 1);
+                }
+                if (ok && z0)
+                    ok = std::fabs(z[0] - z0[0]) <= 1e-9 * (xv[1] - xv[0]) &&
+                         std::fabs(z[n + 1] - z0[n + 1]) <= 1e-9 * (xv[n] - xv[n - 1]);
+                if (!z0) z0 = z;
+            }
+            if (!ok || !z0) break;
+            // tables of axis d: widths, neighbour ratios, centred-node spacings (from z0)
+            std::vector<double> h((size_t)n);
+            for (int64_t k = 0; k < n; ++k) h[k] = xv[k + 1] - xv[k];
+            for (int t = 0; t < 7; ++t) {
+                ftab_off[t][d] = ftab.size();
+                for (int64_t k = 0; k < n; ++k) {
+                    double v = 1.0;
+                    switch (t) {
+                        case 0: v = h[k]; break;
+                        case 1: v = k > 0 ? h[k - 1] / h[k] : 1.0; break;
+                        case 2: v = k + 1 < n ? h[k + 1] / h[k] : 1.0; break;
+                        case 3: v = k > 0 ? h[k] / h[k - 1] : 1.0; break;
+                        case 4: v = k + 1 < n ? h[k] / h[k + 1] : 1.0; break;
+                        case 5: v = h[k] / (z0[k + 1] - z0[k]); break;
+                        default: v = h[k] / (z0[k + 2] - z0[k + 1]); break;
+                    }
+                    ftab.push_back((float)v);
+                }
+            }
+        }
+        P->f32_cells = ok ? 1 : 0;
+    }
     cudaError_t e = cudaMalloc(&P->dev_block, host.size() * sizeof(double));
     if (e == cudaSuccess)
         e = cudaMemcpy(P->dev_block, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && P->f32_cells) {
+        e = cudaMalloc(&P->f32_block, ftab.size() * sizeof(float));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(P->f32_block, ftab.data(), ftab.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            const float** tabs[7] = {P->f32ax.dxf, P->f32ax.nbl, P->f32ax.nbr, P->f32ax.tol,
+                                     P->f32ax.tor, P->f32ax.cl,  P->f32ax.cr};
+            for (int t = 0; t < 7; ++t)
+                for (int d = 0; d < N; ++d) tabs[t][d] = P->f32_block + ftab_off[t][d];
+        }
+    }
     if (e == cudaSuccess) e = cudaMalloc(&P->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(P->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&g.counts, 3 * sizeof(unsigned long long));
@@ -229,6 +294,7 @@ int jp_particles_destroy(jp_particles* P)
 {
     if (!P) return JP_OK;
     cudaFree(P->dev_block);
+    cudaFree(P->f32_block);
     cudaFree(P->d_err);
     cudaFree(P->g.counts);
     if (P->h_err) cudaFreeHost(P->h_err);
@@ -433,10 +499,11 @@ int jp_inject_particles_phase(jp_particles* P, double* const coords[3], uint8_t*
 static int check_f32(const jp_particles* P, const void* const* xi, const void* index, const char* what)
 {
     if (!P || !index || !check_coords(P, xi)) return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": null pointer");
-    if (!P->g.uniform || !P->staggered_std)
+    if (!P->staggered_std && !P->f32_cells)
         return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) +
-                                                 ": the FP32 cell-offset form needs uniform (range) grids with the "
-                                                 "standard ghost-node staggering of the velocity components");
+                                                 ": the FP32 cell-offset form needs the standard staggering of the "
+                                                 "velocity components (vertex grid along the component's axis, cell "
+                                                 "midpoints plus one ghost node at each end along the others)");
     return JP_OK;
 }
 

@@ -4,19 +4,24 @@
 // CellArray slot belongs to one cell) plus an FP32 offset xi in [0, 1)^N in
 // units of that cell's spacing, so round-off scales with the cell width and not
 // with the domain. Velocities, interpolation weights and Runge-Kutta stages
-// are FP32; FP64 is kept for the re-normalisation of (cell, offset) when a
-// particle changes cell and for the weight sums of particle2grid!. Uniform
-// grids only (every spacing is one number per axis). The form has no reference
-// counterpart: its error is stated against the FP64 form on the same seeded run.
+// are FP32; FP64 is kept for the weight sums of particle2grid!. On a uniform
+// grid every spacing is one number per axis; on a grid whose spacing varies
+// the kernels read per-cell tables of widths and width ratios (F32Axes), and
+// offsets carried across a face are converted to the new cell's units. The
+// form has no reference counterpart: its error is stated against the FP64 form
+// on the same seeded run.
 //
 // Semantics in cell units (FP64 form: the reference's rules):
 //   * a particle belongs to its cell when 0 <= xi < 1 on every axis;
 //   * velocity component c is sampled on its staggered grid: along its own
 //     axis the nodes are the cell vertices (node k at k), along the others the
-//     ghost-expanded centres (node k at k - 1/2); outside a grid's limits the
-//     sample is Inf, as in the reference;
+//     ghost-expanded centres (node k at k - 1/2; on a grid whose spacing
+//     varies, the cell midpoints and the grid's own ghost nodes); outside a
+//     grid's limits the sample is Inf, as in the reference;
 //   * move_particles! sends a particle to cell + floor(xi) with
-//     xi - floor(xi) (computed in FP64, kept below 1), with the reference's
+//     xi - floor(xi) (one FP32 operation, kept below 1; scaled to the new
+//     cell's width where the spacing varies, and dropped as a move of more
+//     than one cell if it then lies outside that cell), with the reference's
 //     colour-pass slot allocation (shared allocate stage);
 //   * inject_particles! follows the reference's quadrant walk; new offsets are
 //     quadrant corner + 1/2 * (0.05 + 0.95 r) and the nearest neighbour is the
@@ -83,56 +88,54 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------- advection
-// sample(c, x): velocity component c at offset x of the particle's cell
+// sample(x, v): every velocity component at offset x of the particle's cell;
+// w / aw: dt / dx and alpha dt / dx of that cell per axis
 template <int DIM, int METHOD, class Sample>
-__device__ __forceinline__ void advect_f32(const F32Params& P, const float* x0, float* x, Sample sample)
+__device__ __forceinline__ void advect_f32(const F32Params& P, const float* w, const float* aw, const float* x0,
+                                           float* x, Sample sample)
 {
     float v0[3], v1[3], q[3];
     if (METHOD == JP_RUNGE_KUTTA2) {
+        sample(x0, v0);
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) v0[c] = sample(c, x0);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) q[d] = fmaf(P.aw[d], v0[d], x0[d]);
-#pragma unroll
-        for (int c = 0; c < DIM; ++c) v1[c] = sample(c, q);
+        for (int d = 0; d < DIM; ++d) q[d] = fmaf(aw[d], v0[d], x0[d]);
+        sample(q, v1);
 #pragma unroll
         for (int d = 0; d < DIM; ++d)
-            x[d] = P.half ? fmaf(P.w[d], v1[d], x0[d]) : fmaf(P.w[d], fmaf(P.ca, v0[d], P.cb * v1[d]), x0[d]);
+            x[d] = P.half ? fmaf(w[d], v1[d], x0[d]) : fmaf(w[d], fmaf(P.ca, v0[d], P.cb * v1[d]), x0[d]);
     } else if (METHOD == JP_RUNGE_KUTTA4) {
         float k1[3], k2[3], k3[3], k4[3];
+        sample(x0, k1);
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) k1[c] = sample(c, x0);
+        for (int d = 0; d < DIM; ++d) q[d] = fmaf(0.5f * w[d], k1[d], x0[d]);
+        sample(q, k2);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) q[d] = fmaf(0.5f * P.w[d], k1[d], x0[d]);
+        for (int d = 0; d < DIM; ++d) q[d] = fmaf(0.5f * w[d], k2[d], x0[d]);
+        sample(q, k3);
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) k2[c] = sample(c, q);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) q[d] = fmaf(0.5f * P.w[d], k2[d], x0[d]);
-#pragma unroll
-        for (int c = 0; c < DIM; ++c) k3[c] = sample(c, q);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) q[d] = fmaf(P.w[d], k3[d], x0[d]);
-#pragma unroll
-        for (int c = 0; c < DIM; ++c) k4[c] = sample(c, q);
+        for (int d = 0; d < DIM; ++d) q[d] = fmaf(w[d], k3[d], x0[d]);
+        sample(q, k4);
 #pragma unroll
         for (int d = 0; d < DIM; ++d)
-            x[d] = fmaf(P.w[d] * (1.0f / 6.0f), (k1[d] + 2.0f * k2[d]) + (2.0f * k3[d] + k4[d]), x0[d]);
+            x[d] = fmaf(w[d] * (1.0f / 6.0f), (k1[d] + 2.0f * k2[d]) + (2.0f * k3[d] + k4[d]), x0[d]);
     } else {
+        sample(x0, v0);
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) v0[c] = sample(c, x0);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) x[d] = fmaf(P.w[d], v0[d], x0[d]);
+        for (int d = 0; d < DIM; ++d) x[d] = fmaf(w[d], v0[d], x0[d]);
     }
 }
 
 // A warp takes 32 consecutive cells and their live particles in slot-major
-// order (full lanes whatever the occupancy).
-template <int DIM, int METHOD>
+// order (full lanes whatever the occupancy). CELLS: the grid's spacing varies;
+// each cell's steps are dt and alpha dt times the container's 1/dx[i] (one
+// FP64 product per cell and axis), its samples walk the per-cell tables.
+template <int DIM, int METHOD, bool CELLS>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     advect_f32_kernel(DevGrid g, CVelF V, F32Params P, XiF Xi, const uint8_t* __restrict__ index)
 {
     __shared__ SlotList lists[kWarpsPerBlock];
     __shared__ int cellI[kWarpsPerBlock][32][3];
+    __shared__ float cellW[CELLS ? kWarpsPerBlock : 1][32][2 * DIM];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
     if (c0 >= g.ncells) return;
@@ -143,6 +146,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         cell_coords(g, min(c0 + lane, nc - 1), I);
 #pragma unroll
         for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
+        if (CELLS) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const double ix = ldg(g.ixv[d] + I[d]);
+                cellW[w][lane][d] = (float)(P.dt * ix);
+                cellW[w][lane][DIM + d] = (float)(P.adt * ix);
+            }
+        }
     }
     uint64_t mine;
     const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
@@ -154,7 +165,21 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         float x0[3], x[3];
 #pragma unroll
         for (int d = 0; d < DIM; ++d) x0[d] = Xi.x[d][a];
-        advect_f32<DIM, METHOD>(P, x0, x, [&](int c, const float* xi) { return velocity_f32<DIM>(g, c, I, xi, V.v[c]); });
+        if (CELLS) {
+            float wc[3], awc[3];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                wc[d] = cellW[w][l][d];
+                awc[d] = cellW[w][l][DIM + d];
+            }
+            advect_f32<DIM, METHOD>(P, wc, awc, x0, x,
+                                    [&](const float* xi, float* v) { velocity_f32_cells<DIM>(g, P.ax, I, xi, V, v); });
+        } else {
+            advect_f32<DIM, METHOD>(P, P.w, P.aw, x0, x, [&](const float* xi, float* v) {
+#pragma unroll
+                for (int c = 0; c < DIM; ++c) v[c] = velocity_f32<DIM>(g, c, I, xi, V.v[c]);
+            });
+        }
 #pragma unroll
         for (int d = 0; d < DIM; ++d) Xi.x[d][a] = x[d];
     }
@@ -168,10 +193,14 @@ struct MoveViewF {
 
 // The FP64 classify's scheme (slot-major live particles over the lanes, loads
 // of a batch in flight together, records written after a warp barrier at
-// their cell's next record), four particles per lane in flight.
-template <int DIM>
+// their cell's next record), four particles per lane in flight. CELLS: the
+// grid's spacing varies; an offset carried into a neighbour is converted to
+// that cell's units (tables tor / tol), and a particle whose converted offset
+// still lies outside the neighbour has moved more than one cell.
+template <int DIM, bool CELLS>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
-    move_classify_f32(DevGrid g, XiF Xi, const uint8_t* __restrict__ index, ArgsF A, MoveViewF S, int* d_err)
+    move_classify_f32(DevGrid g, XiF Xi, const uint8_t* __restrict__ index, ArgsF A, MoveViewF S, F32Axes ax,
+                      int* d_err)
 {
     __shared__ SlotList lists[kWarpsPerBlock];
     __shared__ int cellI[kWarpsPerBlock][32][3];
@@ -215,17 +244,24 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
                 continue;
             }
             const float fl = floorf(xi[d]);
-            const int o = (int)fl;
-            const int T = cellI[w][l][d] + o;
-            inside &= T >= 0 && T < g.n[d];
-            far |= o > 1 || o < -1;
-            off[d] = o;
+            int o = (int)fl;
             // re-normalised offset in the target cell, kept below 1. xi - fl is one
             // correctly rounded FP32 subtraction: for fl = 1 it is exact (Sterbenz), for
             // fl = -1 the exact 1 + xi fits FP64 whenever it does not round to 1.0f in FP32
             // either, so this equals the FP64 difference rounded to FP32 (the particles
             // moving farther are dropped) without the FP64 pipe
-            const float rr = xi[d] - fl;
+            float rr = xi[d] - fl;
+            if (CELLS && o == 1) {  // (xi - 1) dx[i] / dx[i+1]
+                rr = (xi[d] - 1.0f) * __ldg(ax.tor[d] + cellI[w][l][d]);
+                if (!(rr < 1.0f)) o = 2;
+            } else if (CELLS && o == -1) {  // 1 + xi dx[i] / dx[i-1]
+                rr = fmaf(xi[d], __ldg(ax.tol[d] + cellI[w][l][d]), 1.0f);
+                if (rr < 0.0f) o = -2;
+            }
+            const int T = cellI[w][l][d] + o;
+            inside &= T >= 0 && T < g.n[d];
+            far |= o > 1 || o < -1;
+            off[d] = o;
             v[d] = rr < 1.0f ? rr : 0x1.fffffep-1f;
         }
         uint8_t code = kCodeExit;
@@ -443,6 +479,14 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
     const int ncand = NB * M;
     int64_t I[3];
     cell_coords(g, c, I);
+    // this cell's widths and its neighbours' widths in its units (1 on a uniform grid)
+    float h[3], rl[3], rh[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        h[d] = P.cells ? __ldg(P.ax.dxf[d] + I[d]) : P.dx[d];
+        rl[d] = P.cells ? __ldg(P.ax.nbl[d] + I[d]) : 1.0f;
+        rh[d] = P.cells ? __ldg(P.ax.nbr[d] + I[d]) : 1.0f;
+    }
     // Stage positions in cell units relative to this cell's lower-left vertex.
     // Occupancy from the flag pass's per-cell masks (one load per neighbour
     // cell); the offsets of the live candidates are loaded in batches with all
@@ -480,9 +524,11 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
             if (o >= ncand) continue;
             const int nb = o / M;
             const int off[3] = {nb % 3 - 1, (nb / 3) % 3 - 1, DIM == 3 ? nb / 9 - 1 : 0};
-            if (lv[u]) {
+            if (lv[u]) {  // x of cell i-1 -> (x - 1) dx[i-1] / dx[i]; of cell i+1 -> 1 + x dx[i+1] / dx[i]
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) r[d][o] = (float)off[d] + xs[u][d];
+                for (int d = 0; d < DIM; ++d)
+                    r[d][o] = off[d] < 0 ? (xs[u][d] - 1.0f) * rl[d]
+                                         : (off[d] > 0 ? fmaf(xs[u][d], rh[d], 1.0f) : xs[u][d]);
             }
             live[o] = lv[u] ? 1 : 0;
         }
@@ -537,7 +583,7 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
                 float ss = 0.0f;
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) {
-                    const float e = (r[d][o] - pn[d]) * P.dx[d];
+                    const float e = (r[d][o] - pn[d]) * h[d];
                     ss = fmaf(e, e, ss);
                 }
                 if (ss < best) {  // NaN never wins
@@ -714,10 +760,11 @@ static __global__ void __launch_bounds__(kThreads)
     const bool col_ok = ci >= 0 && ci < n0;
     const bool out_ok = lane >= 1 && ci < V0;             // lanes 1..31 own vertex column ci
     const int M = g.max_xcell;
-    const float dx = P.dx[0], dy = P.dx[1];
+    const float dx = P.cells && col_ok ? __ldg(P.ax.dxf[0] + ci) : P.dx[0];
     double w_acc = 0.0, f_acc = 0.0;  // the vertex (ci, cr) being summed
     for (int64_t cr = r0 - 1; cr < r1; ++cr) {
         const bool cell_ok = col_ok && cr >= 0 && cr < n1;
+        const float dy = P.cells && cr >= 0 && cr < n1 ? __ldg(P.ax.dxf[1] + cr) : P.dx[1];
         const int64_t c = cell_ok ? ci + n0 * cr : 0;
         const uint64_t L = cell_ok ? live_mask(index, c, nc, M) : 0;
         const int hi = (int)__reduce_max_sync(full, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
@@ -805,10 +852,12 @@ static __global__ void __launch_bounds__(kThreads)
     const bool colrow_ok = ci >= 0 && ci < n0 && cj >= 0 && cj < n1;
     const bool out_ok = lane >= 1 && w >= 1 && ci < V0 && cj < V1;  // vertex (ci, cj, .)
     const int M = g.max_xcell;
-    const float dx = P.dx[0], dy = P.dx[1], dz = P.dx[2];
+    const float dx = P.cells && ci >= 0 && ci < n0 ? __ldg(P.ax.dxf[0] + ci) : P.dx[0];
+    const float dy = P.cells && cj >= 0 && cj < n1 ? __ldg(P.ax.dxf[1] + cj) : P.dx[1];
     double w_acc = 0.0, f_acc = 0.0;
     for (int64_t cr = r0 - 1; cr < r1; ++cr) {
         const bool cell_ok = colrow_ok && cr >= 0 && cr < n2;
+        const float dz = P.cells && cr >= 0 && cr < n2 ? __ldg(P.ax.dxf[2] + cr) : P.dx[2];
         const int64_t c = cell_ok ? ci + n0 * (cj + n1 * cr) : 0;
         const uint64_t L = cell_ok ? live_mask(index, c, nc, M) : 0;
         const int hi = (int)__reduce_max_sync(full, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
@@ -938,7 +987,9 @@ cudaError_t launch_advection_f32(jp_particles* P, int method, double alpha, cons
     const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
     const int nt = 32 * kWarpsPerBlock;
     cudaStream_t s = P->stream;
-#define JP_ADVF(D, M) advect_f32_kernel<D, M><<<nb, nt, 0, s>>>(P->g, Vv, prm, Xi, index)
+#define JP_ADVF(D, M)                                                                 \
+    (prm.cells ? advect_f32_kernel<D, M, true><<<nb, nt, 0, s>>>(P->g, Vv, prm, Xi, index) \
+               : advect_f32_kernel<D, M, false><<<nb, nt, 0, s>>>(P->g, Vv, prm, Xi, index))
     if (!d3) {
         if (method == JP_RUNGE_KUTTA2) JP_ADVF(2, JP_RUNGE_KUTTA2);
         else if (method == JP_RUNGE_KUTTA4) JP_ADVF(2, JP_RUNGE_KUTTA4);
@@ -972,12 +1023,19 @@ cudaError_t launch_move_f32(jp_particles* P, float* const xi[3], uint8_t* index,
     const unsigned nb = grid_blocks(P->g.ncells);
     const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
     const int ntw = 32 * kWarpsPerBlock;
+    const F32Axes& ax = P->f32ax;
     if (N == 2) {
-        move_classify_f32<2><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, P->d_err);
+        if (P->f32_cells)
+            move_classify_f32<2, true><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, ax, P->d_err);
+        else
+            move_classify_f32<2, false><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, ax, P->d_err);
         launch_allocate_passes(P->g, S.m, st);
         move_apply_f32<2><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S);
     } else {
-        move_classify_f32<3><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, P->d_err);
+        if (P->f32_cells)
+            move_classify_f32<3, true><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, ax, P->d_err);
+        else
+            move_classify_f32<3, false><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, ax, P->d_err);
         launch_allocate_passes(P->g, S.m, st);
         move_apply_f32<3><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S);
     }

@@ -32,8 +32,9 @@ struct F32Params {
     float aw[3];   // alpha * dt / dx
     float ca, cb;  // RK2 blend for alpha != 1/2
     int half;
-    int uniform;   // one spacing per axis: dx, w and aw above hold for every cell
-    F32Axes ax;    // per-cell tables (any grid)
+    int cells;     // spacing varies: per-cell tables (ax) and per-cell steps (dt, adt times 1/dx[i])
+    double dt, adt;
+    F32Axes ax;
 };
 
 __device__ __forceinline__ float lerpf1(float t, float v0, float v1) { return fmaf(t, v1, fmaf(-t, v0, v0)); }
@@ -93,6 +94,92 @@ __device__ __forceinline__ float velocity_f32(const DevGrid& g, int comp, const 
     return lerpNf<DIM>(v, t);
 }
 
+// The same samples on a grid whose spacing varies (per-cell tables): every
+// component of the velocity at offset xi of cell I (xi in cell I's units, any
+// value). Per axis the point is first carried into the cell that holds it (a
+// walk of at most kWalkCells cells, never past the first or last cell), then
+// component c takes, along its own axis, the vertex interval of that cell and,
+// along the others, the interval of the centred nodes around the point: the
+// cell's centre sits at offset 1/2, its neighbours' centres (or the ghost
+// nodes at the ends) at the spacings of tables cl / cr. Outside a grid's
+// limits (or for a point farther than the walk) the sample is Inf.
+constexpr int kWalkCells = 8;
+
+template <int DIM>
+__device__ __forceinline__ void velocity_f32_cells(const DevGrid& g, const F32Axes& ax, const int* I,
+                                                   const float* xi, const CVelF& V, float* out)
+{
+    int k[3];
+    float u[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        int kk = I[d];
+        float uu = xi[d];
+        const int n = (int)g.n[d];
+        for (int it = 0; it < kWalkCells; ++it) {
+            if (uu >= 1.0f && kk < n - 1) {
+                uu = (uu - 1.0f) * __ldg(ax.tor[d] + kk);
+                ++kk;
+            } else if (uu < 0.0f && kk > 0) {
+                uu = fmaf(uu, __ldg(ax.tol[d] + kk), 1.0f);
+                --kk;
+            } else {
+                break;
+            }
+        }
+        if ((uu >= 1.0f && kk < n - 1) || (uu < 0.0f && kk > 0)) uu = CUDART_NAN_F;  // farther than the walk
+        k[d] = kk;
+        u[d] = uu;
+    }
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+        int kn[3];
+        float t[3];
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            if (d == c) {  // vertex nodes: interval k, t = u
+                kn[d] = k[d];
+                t[d] = u[d];
+            } else if (u[d] >= 0.5f) {  // centred nodes k+1 (the centre) and k+2
+                kn[d] = k[d] + 1;
+                t[d] = (u[d] - 0.5f) * __ldg(ax.cr[d] + k[d]);
+            } else {  // centred nodes k and k+1 (the centre)
+                kn[d] = k[d];
+                t[d] = fmaf(u[d] - 0.5f, __ldg(ax.cl[d] + k[d]), 1.0f);
+            }
+            ok &= t[d] >= 0.0f && t[d] <= 1.0f;  // false for NaN
+        }
+        if (!ok) {
+            out[c] = CUDART_INF_F;
+            continue;
+        }
+        const float* Vc = V.v[c];
+        const int64_t L0 = g.nvel[c][0];
+        float v[8];
+        if (DIM == 2) {
+            const float* b = Vc + kn[0] + L0 * kn[1];
+            v[0] = __ldg(b);
+            v[1] = __ldg(b + 1);
+            v[2] = __ldg(b + L0);
+            v[3] = __ldg(b + L0 + 1);
+        } else {
+            const int64_t L1 = g.nvel[c][1];
+            const int64_t sz = L0 * L1;
+            const float* b = Vc + kn[0] + L0 * (kn[1] + L1 * (int64_t)kn[2]);
+            v[0] = __ldg(b);
+            v[1] = __ldg(b + 1);
+            v[2] = __ldg(b + L0);
+            v[3] = __ldg(b + L0 + 1);
+            v[4] = __ldg(b + sz);
+            v[5] = __ldg(b + sz + 1);
+            v[6] = __ldg(b + sz + L0);
+            v[7] = __ldg(b + sz + L0 + 1);
+        }
+        out[c] = lerpNf<DIM>(v, t);
+    }
+}
+
 inline F32Params make_params(const jp_particles* P, double alpha, double dt)
 {
     F32Params p{};
@@ -106,7 +193,9 @@ inline F32Params make_params(const jp_particles* P, double alpha, double dt)
     p.ca = (float)std::fma(-0.5, ia, 1.0);
     p.cb = (float)(0.5 * ia);
     p.half = alpha == 0.5;
-    p.uniform = P->g.uniform;
+    p.cells = P->f32_cells;
+    p.dt = dt;
+    p.adt = alpha * dt;
     p.ax = P->f32ax;
     return p;
 }

@@ -56,22 +56,17 @@ struct DevGrid {
     unsigned long long* counts;
 };
 
-// Per-cell spacing tables of the split-precision form, one array per axis
-// (n[d] entries), built at container creation; on a uniform grid every width
-// ratio is exactly 1. w / aw are written by each advection call (dt / dx[i],
-// alpha dt / dx[i]) when the grid is not uniform.
+// Per-cell spacing tables of the split-precision form on grids whose spacing
+// varies (one array of n[d] entries per axis and table, built at container
+// creation). Ratios past the ends of an axis are 1.
 struct F32Axes {
-    const float* dxf[3];              // cell widths dx[i]
-    const float* nbl[3];              // dx[i-1] / dx[i] (1 at the first cell)
-    const float* nbr[3];              // dx[i+1] / dx[i] (1 at the last cell)
-    const float* tol[3];              // dx[i] / dx[i-1]: cell i's units -> cell i-1's (1 at the first cell)
-    const float* tor[3];              // dx[i] / dx[i+1]: cell i's units -> cell i+1's (1 at the last cell)
-    const float* cl[3];               // dx[i] / (spacing of the centred nodes left of cell i's centre)
-    const float* cr[3];               // dx[i] / (spacing of the centred nodes right of it)
-    const double* tol64[3];           // the same ratios in FP64 (cell-crossing renormalisation)
-    const double* tor64[3];
-    float* wf[3];                     // per call: dt / dx[i]
-    float* awf[3];                    // per call: alpha dt / dx[i]
+    const float* dxf[3];  // cell widths dx[i]
+    const float* nbl[3];  // dx[i-1] / dx[i]: a length in cell i-1's units -> cell i's
+    const float* nbr[3];  // dx[i+1] / dx[i]
+    const float* tol[3];  // dx[i] / dx[i-1]: a length in cell i's units -> cell i-1's
+    const float* tor[3];  // dx[i] / dx[i+1]
+    const float* cl[3];   // dx[i] / (distance from the centred node left of cell i's centre to that centre)
+    const float* cr[3];   // dx[i] / (distance from cell i's centre to the centred node right of it)
 };
 
 // Scratch owned by a container for move_particles! (allocated on first use).
@@ -110,8 +105,9 @@ struct jp_particles {
     uint32_t warnings = 0;
     uint64_t inject_calls = 0;
     double dx_host[3] = {1.0, 1.0, 1.0};  // spacing per axis (uniform grids) for the split-precision form
-    int staggered_std = 0;                // velocity grids have the standard ghost-node staggering
-    float* f32_block = nullptr;           // the split-precision form's per-cell tables (F32Axes)
+    int staggered_std = 0;                // uniform grids with ghost nodes half a cell out (the fast split form)
+    int f32_cells = 0;                    // the split-precision form runs on per-cell spacing tables
+    float* f32_block = nullptr;           // those tables (F32Axes), one allocation
     jp::F32Axes f32ax{};
     int centres_ok = 0;                   // the centre grids have one node per cell and >= 2 nodes per axis
     jp::MoveScratch move;

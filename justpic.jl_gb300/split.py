@@ -6,7 +6,9 @@ injection counter are shared with the FP64 form).
 into FP32 offsets in cell units; the ``*_f32_`` functions mirror the FP64 API
 (``advection_f32_(particles, xi, method, V32, dt)`` etc.) with FP32 velocity,
 particle and vertex fields. ``coords_from_offsets(particles, xi)`` returns
-FP64 coordinates for output. Uniform (``LinRange``) grids only.
+FP64 coordinates for output. Uniform (``LinRange``) grids and vector grids
+with the standard staggering (cell midpoints plus one ghost node at each end
+for the centred axes); the container decides at creation.
 """
 from __future__ import annotations
 
