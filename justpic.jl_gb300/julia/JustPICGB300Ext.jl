@@ -224,7 +224,8 @@ end
 
 # ---- split-precision form (no reference counterpart) ----------------------
 # Float32 offsets xi[d] in [0, 1) in the CellArray layout; the cell of a slot
-# is implicit. Uniform grids with the standard ghost-node staggering only.
+# is implicit. Uniform and vector grids with the standard staggering (cell
+# midpoints plus one ghost node at each end along the centred axes).
 offsets!(xi, p::GP) = check(ccall((:jp_offsets_from_coords, lib), Cint,
     (Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}),
     handle(p).ptr, ptrs3(p.coords), ptr(p.index), ptrs3(xi)))
