@@ -21,9 +21,8 @@
  *
  * Limits: ndim 2 or 3; 1 <= max_xcell <= JP_MAX_XCELL (cells above 64 slots
  * run the reference's own per-cell schedule for move_particles! and
- * inject_particles!, and the split-precision form and the adjoint need
- * max_xcell <= 64); at most JP_MAX_ARGS particle fields per call; grids
- * strictly increasing.
+ * inject_particles!, in both forms; the adjoint needs max_xcell <= 64); at
+ * most JP_MAX_ARGS particle fields per call; grids strictly increasing.
  */
 #ifndef JUSTPIC_GB300_H
 #define JUSTPIC_GB300_H

@@ -18,7 +18,7 @@ int fail(int code, const std::string& msg)
     return code;
 }
 
-// the split-precision form and the adjoint keep 64-bit slot masks: cells of at most 64 slots
+// the adjoint keeps 64-bit slot masks: cells of at most 64 slots
 #define JP_REQUIRE_NARROW(P, what)                                                                        \
     do {                                                                                                  \
         if ((P) && (P)->g.max_xcell > 64)                                                                 \
@@ -509,7 +509,6 @@ static int check_f32(const jp_particles* P, const void* const* xi, const void* i
 
 int jp_offsets_from_coords(jp_particles* P, const double* const coords[3], const uint8_t* index, float* const xi[3])
 {
-    JP_REQUIRE_NARROW(P, "jp_offsets_from_coords");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_offsets_from_coords");
     if (rc) return rc;
     if (!check_coords(P, (const void* const*)coords))
@@ -519,7 +518,6 @@ int jp_offsets_from_coords(jp_particles* P, const double* const coords[3], const
 
 int jp_coords_from_offsets(jp_particles* P, const float* const xi[3], const uint8_t* index, double* const coords[3])
 {
-    JP_REQUIRE_NARROW(P, "jp_coords_from_offsets");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_coords_from_offsets");
     if (rc) return rc;
     if (!check_coords(P, (const void* const*)coords))
@@ -530,7 +528,6 @@ int jp_coords_from_offsets(jp_particles* P, const float* const xi[3], const uint
 int jp_advection_f32(jp_particles* P, int32_t method, double alpha, const float* const V[3], double dt,
                      float* const xi[3], const uint8_t* index)
 {
-    JP_REQUIRE_NARROW(P, "jp_advection_f32");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_advection_f32");
     if (rc) return rc;
     if (!check_coords(P, (const void* const*)V)) return fail(JP_ERR_INVALID_ARGUMENT, "jp_advection_f32: null velocity");
@@ -543,7 +540,6 @@ int jp_advection_f32(jp_particles* P, int32_t method, double alpha, const float*
 
 int jp_move_particles_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int32_t nargs)
 {
-    JP_REQUIRE_NARROW(P, "jp_move_particles_f32");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_move_particles_f32");
     if (rc) return rc;
     if (nargs < 0 || nargs > JP_MAX_ARGS || (nargs > 0 && !args))
@@ -555,7 +551,6 @@ int jp_move_particles_f32(jp_particles* P, float* const xi[3], uint8_t* index, f
 
 int jp_inject_particles_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int32_t nargs)
 {
-    JP_REQUIRE_NARROW(P, "jp_inject_particles_f32");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_inject_particles_f32");
     if (rc) return rc;
     if (nargs < 0 || nargs > JP_MAX_ARGS || (nargs > 0 && !args))
@@ -569,7 +564,6 @@ int jp_inject_particles_f32(jp_particles* P, float* const xi[3], uint8_t* index,
 
 int jp_grid2particle_f32(jp_particles* P, float* Fp, const float* F, const float* const xi[3], const uint8_t* index)
 {
-    JP_REQUIRE_NARROW(P, "jp_grid2particle_f32");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_grid2particle_f32");
     if (rc) return rc;
     if (!Fp || !F) return fail(JP_ERR_INVALID_ARGUMENT, "jp_grid2particle_f32: null field");
@@ -578,7 +572,6 @@ int jp_grid2particle_f32(jp_particles* P, float* Fp, const float* F, const float
 
 int jp_particle2grid_f32(jp_particles* P, float* F, const float* Fp, const float* const xi[3], const uint8_t* index)
 {
-    JP_REQUIRE_NARROW(P, "jp_particle2grid_f32");
     int rc = check_f32(P, (const void* const*)xi, index, "jp_particle2grid_f32");
     if (rc) return rc;
     if (!Fp || !F) return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_f32: null field");

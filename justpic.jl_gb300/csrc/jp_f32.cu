@@ -129,7 +129,7 @@ __device__ __forceinline__ void advect_f32(const F32Params& P, const float* w, c
 // order (full lanes whatever the occupancy). CELLS: the grid's spacing varies;
 // each cell's steps are dt and alpha dt times the container's 1/dx[i] (one
 // FP64 product per cell and axis), its samples walk the per-cell tables.
-template <int DIM, int METHOD, bool CELLS>
+template <int DIM, int METHOD, bool CELLS, bool WIDE>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     advect_f32_kernel(DevGrid g, CVelF V, F32Params P, XiF Xi, const uint8_t* __restrict__ index)
 {
@@ -155,33 +155,37 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             }
         }
     }
-    uint64_t mine;
-    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
-    for (int k = lane; k < K; k += 32) {
-        int s, l;
-        slot_item(lists[w], M, k, &s, &l);
-        const int64_t a = c0 + l + nc * s;
-        const int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
-        float x0[3], x[3];
+    for (int s0 = 0; s0 < (WIDE ? M : 1); s0 += 64) {  // WIDE: slots in chunks of 64 (max_xcell > 64)
+        const int Mc = min(64, M - s0);
+        uint64_t mine;
+        const int K = build_slot_list(lists[w], index + nc * s0, c0, nc, Mc, lane, &mine);
+        for (int k = lane; k < K; k += 32) {
+            int s, l;
+            slot_item(lists[w], Mc, k, &s, &l);
+            const int64_t a = c0 + l + nc * (s0 + s);
+            const int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
+            float x0[3], x[3];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) x0[d] = Xi.x[d][a];
-        if (CELLS) {
-            float wc[3], awc[3];
+            for (int d = 0; d < DIM; ++d) x0[d] = Xi.x[d][a];
+            if (CELLS) {
+                float wc[3], awc[3];
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                wc[d] = cellW[w][l][d];
-                awc[d] = cellW[w][l][DIM + d];
+                for (int d = 0; d < DIM; ++d) {
+                    wc[d] = cellW[w][l][d];
+                    awc[d] = cellW[w][l][DIM + d];
+                }
+                advect_f32<DIM, METHOD>(P, wc, awc, x0, x,
+                                        [&](const float* xi, float* v) { velocity_f32_cells<DIM>(g, P.ax, I, xi, V, v); });
+            } else {
+                advect_f32<DIM, METHOD>(P, P.w, P.aw, x0, x, [&](const float* xi, float* v) {
+#pragma unroll
+                    for (int c = 0; c < DIM; ++c) v[c] = velocity_f32<DIM>(g, c, I, xi, V.v[c]);
+                });
             }
-            advect_f32<DIM, METHOD>(P, wc, awc, x0, x,
-                                    [&](const float* xi, float* v) { velocity_f32_cells<DIM>(g, P.ax, I, xi, V, v); });
-        } else {
-            advect_f32<DIM, METHOD>(P, P.w, P.aw, x0, x, [&](const float* xi, float* v) {
 #pragma unroll
-                for (int c = 0; c < DIM; ++c) v[c] = velocity_f32<DIM>(g, c, I, xi, V.v[c]);
-            });
+            for (int d = 0; d < DIM; ++d) Xi.x[d][a] = x[d];
         }
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) Xi.x[d][a] = x[d];
+        if (WIDE) __syncwarp();  // the next chunk rebuilds the warp's list
     }
 }
 
@@ -191,12 +195,52 @@ struct MoveViewF {
     float* shadow;  // interleaved records: DIM offsets, then the fields
 };
 
+// Destination of a particle at offset xi of cell I (xi outside [0, 1) on some
+// axis): the neighbour offset per axis and the re-normalised offset in that
+// cell, kept below 1. xi - floor(xi) is one correctly rounded FP32
+// subtraction: for floor = 1 it is exact (Sterbenz), for floor = -1 the exact
+// 1 + xi fits FP64 whenever it does not round to 1.0f in FP32 either, so this
+// equals the FP64 difference rounded to FP32 without the FP64 pipe. CELLS:
+// the grid's spacing varies; an offset carried into a neighbour is converted
+// to that cell's units (tables tor / tol), and one that still lies outside
+// the neighbour has moved more than one cell. inside: the destination is a
+// cell of the grid (false for NaN / Inf offsets: left the domain); far: it is
+// more than one cell away (the particle is dropped).
+template <int DIM, bool CELLS>
+__device__ __forceinline__ void offset_destination(const DevGrid& g, const F32Axes& ax, const int* I,
+                                                   const float* xi, float* v, int* off, bool* inside, bool* far)
+{
+    bool in = true, fr = false;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        off[d] = 0;
+        if (!(fabsf(xi[d]) < 1e6f)) {  // NaN / Inf: left the domain
+            in = false;
+            continue;
+        }
+        const float fl = floorf(xi[d]);
+        int o = (int)fl;
+        float rr = xi[d] - fl;
+        if (CELLS && o == 1) {  // (xi - 1) dx[i] / dx[i+1]
+            rr = (xi[d] - 1.0f) * __ldg(ax.tor[d] + I[d]);
+            if (!(rr < 1.0f)) o = 2;
+        } else if (CELLS && o == -1) {  // 1 + xi dx[i] / dx[i-1]
+            rr = fmaf(xi[d], __ldg(ax.tol[d] + I[d]), 1.0f);
+            if (rr < 0.0f) o = -2;
+        }
+        const int T = I[d] + o;
+        in &= T >= 0 && T < g.n[d];
+        fr |= o > 1 || o < -1;
+        off[d] = o;
+        v[d] = rr < 1.0f ? rr : 0x1.fffffep-1f;
+    }
+    *inside = in;
+    *far = fr;
+}
+
 // The FP64 classify's scheme (slot-major live particles over the lanes, loads
 // of a batch in flight together, records written after a warp barrier at
-// their cell's next record), four particles per lane in flight. CELLS: the
-// grid's spacing varies; an offset carried into a neighbour is converted to
-// that cell's units (tables tor / tol), and a particle whose converted offset
-// still lies outside the neighbour has moved more than one cell.
+// their cell's next record), four particles per lane in flight.
 template <int DIM, bool CELLS>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     move_classify_f32(DevGrid g, XiF Xi, const uint8_t* __restrict__ index, ArgsF A, MoveViewF S, F32Axes ax,
@@ -235,35 +279,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         if (!out) return kCodeStay;
         const unsigned long long bit = 1ull << s;
         atomicOr(&movers[w][l], bit);
-        int off[3] = {0, 0, 0};
-        bool inside = true, far = false;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            if (!(fabsf(xi[d]) < 1e6f)) {  // NaN / Inf: left the domain
-                inside = false;
-                continue;
-            }
-            const float fl = floorf(xi[d]);
-            int o = (int)fl;
-            // re-normalised offset in the target cell, kept below 1. xi - fl is one
-            // correctly rounded FP32 subtraction: for fl = 1 it is exact (Sterbenz), for
-            // fl = -1 the exact 1 + xi fits FP64 whenever it does not round to 1.0f in FP32
-            // either, so this equals the FP64 difference rounded to FP32 (the particles
-            // moving farther are dropped) without the FP64 pipe
-            float rr = xi[d] - fl;
-            if (CELLS && o == 1) {  // (xi - 1) dx[i] / dx[i+1]
-                rr = (xi[d] - 1.0f) * __ldg(ax.tor[d] + cellI[w][l][d]);
-                if (!(rr < 1.0f)) o = 2;
-            } else if (CELLS && o == -1) {  // 1 + xi dx[i] / dx[i-1]
-                rr = fmaf(xi[d], __ldg(ax.tol[d] + cellI[w][l][d]), 1.0f);
-                if (rr < 0.0f) o = -2;
-            }
-            const int T = cellI[w][l][d] + o;
-            inside &= T >= 0 && T < g.n[d];
-            far |= o > 1 || o < -1;
-            off[d] = o;
-            v[d] = rr < 1.0f ? rr : 0x1.fffffep-1f;
-        }
+        int off[3];
+        bool inside, far;
+        const int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
+        offset_destination<DIM, CELLS>(g, ax, I, xi, v, off, &inside, &far);
         uint8_t code = kCodeExit;
         if (!inside) {
             ++n_exit;
@@ -650,7 +669,7 @@ __global__ void inject_pass_f32(DevGrid g, F32Params P, XiF Xi, uint8_t* __restr
 // One thread per cell (its corner values in registers), a warp on 32
 // consecutive cells walking the slot rows up to its highest live slot, four
 // rows in flight per lane: every load and store is a coalesced row access.
-template <int DIM>
+template <int DIM, bool WIDE>
 __global__ void __launch_bounds__(kThreads)
     g2p_f32_kernel(DevGrid g, float* __restrict__ Fp, const float* __restrict__ F, CXiF Xi,
                    const uint8_t* __restrict__ index)
@@ -677,23 +696,25 @@ __global__ void __launch_bounds__(kThreads)
             cv[6] = __ldg(b + sz + V0);
             cv[7] = __ldg(b + sz + V0 + 1);
         }
-        if (valid) L = live_mask(index, c, nc, M);
     }
-    const int hi = (int)__reduce_max_sync(0xffffffffu, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
-    constexpr int B = 4;
-    for (int s0 = 0; s0 < hi; s0 += B) {
-        float t[B][3];
-        bool lv[B];
+    for (int q0 = 0; q0 < (WIDE ? M : 1); q0 += 64) {  // WIDE: slots in chunks of 64 (max_xcell > 64)
+        if (valid) L = live_mask(index + nc * q0, c, nc, min(64, M - q0));
+        const int hi = (int)__reduce_max_sync(0xffffffffu, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
+        constexpr int B = 4;
+        for (int s0 = 0; s0 < hi; s0 += B) {
+            float t[B][3];
+            bool lv[B];
 #pragma unroll
-        for (int u = 0; u < B; ++u) {
-            const int s = s0 + u;
-            lv[u] = s < hi && ((L >> s) & 1);
+            for (int u = 0; u < B; ++u) {
+                const int s = s0 + u;
+                lv[u] = s < hi && ((L >> s) & 1);
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) t[u][d] = lv[u] ? Xi.x[d][c + nc * s] : 0.0f;
+                for (int d = 0; d < DIM; ++d) t[u][d] = lv[u] ? Xi.x[d][c + nc * (q0 + s)] : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (lv[u]) Fp[c + nc * (q0 + s0 + u)] = lerpNf<DIM>(cv, t[u]);
         }
-#pragma unroll
-        for (int u = 0; u < B; ++u)
-            if (lv[u]) Fp[c + nc * (s0 + u)] = lerpNf<DIM>(cv, t[u]);
     }
 }
 
@@ -743,7 +764,8 @@ __device__ __forceinline__ double csum_value(const CSum& s) { return (double)s.h
 // start the row above. No cell is read again for each of its vertices.
 __device__ __forceinline__ float p2g_w_f32(float qx, float e) { return __frcp_rn(fmaf(e, e, qx)); }
 
-static __global__ void __launch_bounds__(kThreads)
+template <bool WIDE>
+__global__ void __launch_bounds__(kThreads)
     p2g_f32_cells2d(DevGrid g, F32Params P, float* __restrict__ F, const float* __restrict__ Fp, CXiF Xi,
                     const uint8_t* __restrict__ index, int chunk, double* __restrict__ Wout)
 {
@@ -766,40 +788,42 @@ static __global__ void __launch_bounds__(kThreads)
         const bool cell_ok = col_ok && cr >= 0 && cr < n1;
         const float dy = P.cells && cr >= 0 && cr < n1 ? __ldg(P.ax.dxf[1] + cr) : P.dx[1];
         const int64_t c = cell_ok ? ci + n0 * cr : 0;
-        const uint64_t L = cell_ok ? live_mask(index, c, nc, M) : 0;
-        const int hi = (int)__reduce_max_sync(full, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
         // corners (0,0), (1,0), (0,1), (1,1) of the cell in cell units
         CSum w00, f00, w10, f10, w01, f01, w11, f11;
-        constexpr int B = 4;
-        for (int s0 = 0; s0 < hi; s0 += B) {
-            float x[B], y[B], f[B];
-            bool lv[B];
+        for (int q0 = 0; q0 < (WIDE ? M : 1); q0 += 64) {  // WIDE: slots in chunks of 64 (max_xcell > 64)
+            const uint64_t L = cell_ok ? live_mask(index + nc * q0, c, nc, min(64, M - q0)) : 0;
+            const int hi = (int)__reduce_max_sync(full, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
+            constexpr int B = 4;
+            for (int s0 = 0; s0 < hi; s0 += B) {
+                float x[B], y[B], f[B];
+                bool lv[B];
 #pragma unroll
-            for (int u = 0; u < B; ++u) {
-                const int s = s0 + u;
-                lv[u] = s < hi && ((L >> s) & 1);
-                const int64_t a = c + nc * s;
-                x[u] = lv[u] ? Xi.x[0][a] : 0.0f;
-                y[u] = lv[u] ? Xi.x[1][a] : 0.0f;
-                f[u] = lv[u] ? Fp[a] : 0.0f;
-            }
+                for (int u = 0; u < B; ++u) {
+                    const int s = s0 + u;
+                    lv[u] = s < hi && ((L >> s) & 1);
+                    const int64_t a = c + nc * (q0 + s);
+                    x[u] = lv[u] ? Xi.x[0][a] : 0.0f;
+                    y[u] = lv[u] ? Xi.x[1][a] : 0.0f;
+                    f[u] = lv[u] ? Fp[a] : 0.0f;
+                }
 #pragma unroll
-            for (int u = 0; u < B; ++u) {
-                if (!lv[u]) continue;
-                // distance^2 = fmaf(ey, ey, ex * ex), e = (corner - xi) * dx per axis
-                const float ex0 = (0.0f - x[u]) * dx, ex1 = (1.0f - x[u]) * dx;
-                const float ey0 = (0.0f - y[u]) * dy, ey1 = (1.0f - y[u]) * dy;
-                const float qx0 = fmaf(ex0, ex0, 0.0f), qx1 = fmaf(ex1, ex1, 0.0f);
-                const float a00 = p2g_w_f32(qx0, ey0), a10 = p2g_w_f32(qx1, ey0);
-                const float a01 = p2g_w_f32(qx0, ey1), a11 = p2g_w_f32(qx1, ey1);
-                csum_add(w00, a00);
-                csum_add_prod(f00, a00, f[u]);
-                csum_add(w10, a10);
-                csum_add_prod(f10, a10, f[u]);
-                csum_add(w01, a01);
-                csum_add_prod(f01, a01, f[u]);
-                csum_add(w11, a11);
-                csum_add_prod(f11, a11, f[u]);
+                for (int u = 0; u < B; ++u) {
+                    if (!lv[u]) continue;
+                    // distance^2 = fmaf(ey, ey, ex * ex), e = (corner - xi) * dx per axis
+                    const float ex0 = (0.0f - x[u]) * dx, ex1 = (1.0f - x[u]) * dx;
+                    const float ey0 = (0.0f - y[u]) * dy, ey1 = (1.0f - y[u]) * dy;
+                    const float qx0 = fmaf(ex0, ex0, 0.0f), qx1 = fmaf(ex1, ex1, 0.0f);
+                    const float a00 = p2g_w_f32(qx0, ey0), a10 = p2g_w_f32(qx1, ey0);
+                    const float a01 = p2g_w_f32(qx0, ey1), a11 = p2g_w_f32(qx1, ey1);
+                    csum_add(w00, a00);
+                    csum_add_prod(f00, a00, f[u]);
+                    csum_add(w10, a10);
+                    csum_add_prod(f10, a10, f[u]);
+                    csum_add(w01, a01);
+                    csum_add_prod(f01, a01, f[u]);
+                    csum_add(w11, a11);
+                    csum_add_prod(f11, a11, f[u]);
+                }
             }
         }
         // vertex (ci, cr), the lower side of this cell row: its cells (ci-1, cr-1) and (ci, cr-1) are in
@@ -833,7 +857,8 @@ static __global__ void __launch_bounds__(kThreads)
 // warp below, through shared memory), (i-1, j) (the lane to the left) and
 // (i, j) (its own): the lower corners finish the vertex row of this z row, the
 // upper corners start the next one.
-static __global__ void __launch_bounds__(kThreads)
+template <bool WIDE>
+__global__ void __launch_bounds__(kThreads)
     p2g_f32_cells3d(DevGrid g, F32Params P, float* __restrict__ F, const float* __restrict__ Fp, CXiF Xi,
                     const uint8_t* __restrict__ index, int band, double* __restrict__ Wout)
 {
@@ -859,46 +884,48 @@ static __global__ void __launch_bounds__(kThreads)
         const bool cell_ok = colrow_ok && cr >= 0 && cr < n2;
         const float dz = P.cells && cr >= 0 && cr < n2 ? __ldg(P.ax.dxf[2] + cr) : P.dx[2];
         const int64_t c = cell_ok ? ci + n0 * (cj + n1 * cr) : 0;
-        const uint64_t L = cell_ok ? live_mask(index, c, nc, M) : 0;
-        const int hi = (int)__reduce_max_sync(full, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
         CSum cw[2][2][2], cf[2][2][2];  // [cx][cy][cz]
-        constexpr int B = 4;
-        for (int s0 = 0; s0 < hi; s0 += B) {
-            float x[B], y[B], z[B], f[B];
-            bool lv[B];
+        for (int q0 = 0; q0 < (WIDE ? M : 1); q0 += 64) {  // WIDE: slots in chunks of 64 (max_xcell > 64)
+            const uint64_t L = cell_ok ? live_mask(index + nc * q0, c, nc, min(64, M - q0)) : 0;
+            const int hi = (int)__reduce_max_sync(full, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
+            constexpr int B = 4;
+            for (int s0 = 0; s0 < hi; s0 += B) {
+                float x[B], y[B], z[B], f[B];
+                bool lv[B];
 #pragma unroll
-            for (int u = 0; u < B; ++u) {
-                const int s = s0 + u;
-                lv[u] = s < hi && ((L >> s) & 1);
-                const int64_t a = c + nc * s;
-                x[u] = lv[u] ? Xi.x[0][a] : 0.0f;
-                y[u] = lv[u] ? Xi.x[1][a] : 0.0f;
-                z[u] = lv[u] ? Xi.x[2][a] : 0.0f;
-                f[u] = lv[u] ? Fp[a] : 0.0f;
-            }
-#pragma unroll
-            for (int u = 0; u < B; ++u) {
-                if (!lv[u]) continue;
-                float qx[2], ey[2], ez[2];
-#pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                    const float ex = ((float)k - x[u]) * dx;
-                    qx[k] = fmaf(ex, ex, 0.0f);
-                    ey[k] = ((float)k - y[u]) * dy;
-                    ez[k] = ((float)k - z[u]) * dz;
+                for (int u = 0; u < B; ++u) {
+                    const int s = s0 + u;
+                    lv[u] = s < hi && ((L >> s) & 1);
+                    const int64_t a = c + nc * (q0 + s);
+                    x[u] = lv[u] ? Xi.x[0][a] : 0.0f;
+                    y[u] = lv[u] ? Xi.x[1][a] : 0.0f;
+                    z[u] = lv[u] ? Xi.x[2][a] : 0.0f;
+                    f[u] = lv[u] ? Fp[a] : 0.0f;
                 }
 #pragma unroll
-                for (int kx = 0; kx < 2; ++kx)
+                for (int u = 0; u < B; ++u) {
+                    if (!lv[u]) continue;
+                    float qx[2], ey[2], ez[2];
 #pragma unroll
-                    for (int ky = 0; ky < 2; ++ky) {
-                        const float qxy = fmaf(ey[ky], ey[ky], qx[kx]);
-#pragma unroll
-                        for (int kz = 0; kz < 2; ++kz) {
-                            const float wi = __frcp_rn(fmaf(ez[kz], ez[kz], qxy));
-                            csum_add(cw[kx][ky][kz], wi);
-                            csum_add_prod(cf[kx][ky][kz], wi, f[u]);
-                        }
+                    for (int k = 0; k < 2; ++k) {
+                        const float ex = ((float)k - x[u]) * dx;
+                        qx[k] = fmaf(ex, ex, 0.0f);
+                        ey[k] = ((float)k - y[u]) * dy;
+                        ez[k] = ((float)k - z[u]) * dz;
                     }
+#pragma unroll
+                    for (int kx = 0; kx < 2; ++kx)
+#pragma unroll
+                        for (int ky = 0; ky < 2; ++ky) {
+                            const float qxy = fmaf(ey[ky], ey[ky], qx[kx]);
+#pragma unroll
+                            for (int kz = 0; kz < 2; ++kz) {
+                                const float wi = __frcp_rn(fmaf(ez[kz], ez[kz], qxy));
+                                csum_add(cw[kx][ky][kz], wi);
+                                csum_add_prod(cf[kx][ky][kz], wi, f[u]);
+                            }
+                        }
+                }
             }
         }
 #pragma unroll
@@ -948,6 +975,236 @@ static __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// ------------------------------------------------- cells above 64 slots
+// Containers with max_xcell > 64 do not fit the 64-bit slot masks of the
+// move and injection kernels above. They run the colour passes directly, as
+// the FP64 form does for such cells: move_particles! with one thread per cell
+// walking its slots in order (the starting point of the free-slot search
+// carried across the cell's movers), inject_particles! with one warp per cell
+// (quadrant counts, free slots and the nearest-neighbour search shared by the
+// warp). Same rules and results as the kernels above.
+template <int DIM, bool CELLS>
+__global__ void __launch_bounds__(kThreads)
+    move_wide_f32(DevGrid g, XiF Xi, uint8_t* __restrict__ index, ArgsF A, F32Axes ax, int pass, int* d_err)
+{
+    int64_t ncol[3] = {1, 1, 1}, off[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ncol[d] = (g.n[d] + 2) / 3;
+    if (DIM == 2) {
+        off[0] = pass / 3;
+        off[1] = pass % 3;
+    } else {
+        off[0] = pass / 9;
+        off[1] = (pass / 3) % 3;
+        off[2] = pass % 3;
+    }
+    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= ncol[0] * ncol[1] * ncol[2]) return;
+    const int64_t J[3] = {w % ncol[0], (w / ncol[0]) % ncol[1], w / (ncol[0] * ncol[1])};
+    int I[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const int64_t i = 3 * J[d] + off[d];
+        if (i >= g.n[d]) return;
+        I[d] = (int)i;
+    }
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    const int64_t I64[3] = {I[0], I[1], I[2]};
+    const int64_t c = cell_linear<DIM>(g, I64);
+    int errs = 0, n_exit = 0, n_far = 0, n_full = 0;
+    int sp = 0;  // starting point of the free-slot search
+    for (int ip = 0; ip < M; ++ip) {
+        const int64_t a = c + nc * ip;
+        if (!index[a]) continue;
+        float xi[3];
+        bool out = false;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            xi[d] = Xi.x[d][a];
+            out |= !(xi[d] >= 0.0f && xi[d] < 1.0f);
+        }
+        if (!out) continue;
+        float v[3];
+        int o[3];
+        bool inside, far;
+        offset_destination<DIM, CELLS>(g, ax, I, xi, v, o, &inside, &far);
+        float cached[JP_MAX_ARGS];
+        for (int k = 0; k < A.n; ++k) cached[k] = A.a[k][a];
+        index[a] = 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) Xi.x[d][a] = CUDART_NAN_F;
+        for (int k = 0; k < A.n; ++k) A.a[k][a] = CUDART_NAN_F;
+        if (!inside) {
+            ++n_exit;
+            continue;
+        }
+        if (far) {
+            errs |= kWarnFarMove;
+            ++n_far;
+            continue;
+        }
+        const int64_t T[3] = {I[0] + o[0], I[1] + o[1], DIM == 3 ? I[2] + o[2] : 0};
+        const int64_t tc = cell_linear<DIM>(g, T);
+        int fr = -1;
+        for (int i = sp; i < M; ++i)
+            if (!index[tc + nc * i]) {
+                fr = i;
+                break;
+            }
+        if (fr < 0) {  // target cell full: dropped
+            ++n_full;
+            continue;
+        }
+        sp = fr;
+        const int64_t b = tc + nc * fr;
+        index[b] = 1;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) Xi.x[d][b] = v[d];
+        for (int k = 0; k < A.n; ++k) A.a[k][b] = cached[k];
+    }
+    if ((n_exit | n_far | n_full) && g.counts) {
+        if (n_exit) atomicAdd(g.counts + 0, (unsigned long long)n_exit);
+        if (n_far) atomicAdd(g.counts + 1, (unsigned long long)n_far);
+        if (n_full) atomicAdd(g.counts + 2, (unsigned long long)n_full);
+    }
+    raise_err(d_err, errs);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    inject_wide_f32(DevGrid g, F32Params P, XiF Xi, uint8_t* __restrict__ index, ArgsF A, int pass, uint32_t call,
+                    int* d_err)
+{
+    int64_t ncol[3] = {1, 1, 1}, off[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ncol[d] = (g.n[d] + 1) / 2;
+    if (DIM == 2) {
+        off[0] = pass / 2;
+        off[1] = pass % 2;
+    } else {
+        off[0] = pass / 4;
+        off[1] = (pass / 2) % 2;
+        off[2] = pass % 2;
+    }
+    const int lane = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= ncol[0] * ncol[1] * ncol[2]) return;
+    const int64_t J[3] = {w % ncol[0], (w / ncol[0]) % ncol[1], w / (ncol[0] * ncol[1])};
+    int64_t I[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        I[d] = 2 * J[d] + off[d];
+        if (I[d] >= g.n[d]) return;  // the same for the whole warp
+    }
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    constexpr int NB = DIM == 2 ? 9 : 27;
+    constexpr int CENTER = DIM == 2 ? 4 : 13;
+    const int64_t c = cell_linear<DIM>(g, I);
+    float h[3], rl[3], rh[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        h[d] = P.cells ? __ldg(P.ax.dxf[d] + I[d]) : P.dx[d];
+        rl[d] = P.cells ? __ldg(P.ax.nbl[d] + I[d]) : 1.0f;
+        rh[d] = P.cells ? __ldg(P.ax.nbr[d] + I[d]) : 1.0f;
+    }
+    const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
+    int errs = 0;
+    for (int q = 0; q < (1 << DIM); ++q) {
+        float qc[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) qc[d] = 0.5f * (float)((q >> d) & 1);
+        int cnt = 0;
+        for (int s = lane; s < M; s += 32) {
+            const int64_t a = c + nc * s;
+            if (!index[a]) continue;
+            bool in = true;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const float x = Xi.x[d][a];
+                in = in && x > qc[d] && x < qc[d] + 0.5f;
+            }
+            cnt += in ? 1 : 0;
+        }
+        int count = __reduce_add_sync(0xffffffffu, cnt);
+        if (count >= min_xq) break;
+        bool done = false;
+        for (int base = 0; base < M && !done; base += 32) {
+            const int s = base + lane;
+            uint32_t freem = __ballot_sync(0xffffffffu, s < M && !index[c + nc * s]);
+            while (freem) {
+                const int i = base + __ffs(freem) - 1;
+                freem &= freem - 1;
+                ++count;
+                float pn[3];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const float u = jp_rand_uniform_f32(g.seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)i,
+                                                        (uint32_t)d);
+                    pn[d] = qc[d] + 0.5f * fmaf(0.95f, u, 0.05f);
+                }
+                const int64_t ai = c + nc * i;
+                if (lane == 0) {
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) Xi.x[d][ai] = pn[d];
+                    index[ai] = 1;
+                }
+                __syncwarp();
+                // nearest: first minimum of the FP32 squared physical distance in candidate order
+                float best = CUDART_INF_F;
+                int bo = 0x7fffffff;
+                for (int o = lane; o < NB * M; o += 32) {
+                    const int nb = o / M, sl = o - nb * M;
+                    if (nb == CENTER && sl == i) continue;
+                    const int ox[3] = {nb % 3 - 1, (nb / 3) % 3 - 1, DIM == 3 ? nb / 9 - 1 : 0};
+                    const int64_t K[3] = {I[0] + ox[0], I[1] + ox[1], I[2] + ox[2]};
+                    if (K[0] < 0 || K[1] < 0 || K[0] >= g.n[0] || K[1] >= g.n[1]) continue;
+                    if (DIM == 3 && (K[2] < 0 || K[2] >= g.n[2])) continue;
+                    const int64_t b = cell_linear<DIM>(g, K) + nc * sl;
+                    if (!index[b]) continue;
+                    float ss = 0.0f;
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) {
+                        const float x = Xi.x[d][b];
+                        const float r = ox[d] < 0 ? (x - 1.0f) * rl[d] : (ox[d] > 0 ? fmaf(x, rh[d], 1.0f) : x);
+                        const float e = (r - pn[d]) * h[d];
+                        ss = fmaf(e, e, ss);
+                    }
+                    if (ss < best) {  // NaN never wins
+                        best = ss;
+                        bo = o;
+                    }
+                }
+#pragma unroll
+                for (int sh = 16; sh > 0; sh >>= 1) {
+                    const float ob = __shfl_xor_sync(0xffffffffu, best, sh);
+                    const int oo = __shfl_xor_sync(0xffffffffu, bo, sh);
+                    if (ob < best || (ob == best && oo < bo)) {
+                        best = ob;
+                        bo = oo;
+                    }
+                }
+                if (bo != 0x7fffffff) {
+                    const int nb = bo / M, sl = bo - nb * M;
+                    const int64_t K[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1,
+                                          DIM == 3 ? I[2] + nb / 9 - 1 : 0};
+                    const int64_t src = cell_linear<DIM>(g, K) + nc * sl;
+                    for (int k = lane; k < A.n; k += 32) A.a[k][ai] = A.a[k][src];
+                } else if (A.n > 0) {
+                    errs |= kWarnNoNeighbour;
+                }
+                __syncwarp();
+                if (count >= min_xq) {
+                    done = true;
+                    break;
+                }
+            }
+        }
+    }
+    raise_err(d_err, errs);
+}
+
 // ------------------------------------------------------------ launchers
 cudaError_t launch_to_offsets(jp_particles* P, const double* const coords[3], const uint8_t* index,
                               float* const xi[3])
@@ -984,12 +1241,15 @@ cudaError_t launch_advection_f32(jp_particles* P, int method, double alpha, cons
     XiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
     CVelF Vv{{V[0], V[1], d3 ? V[2] : nullptr}};
     const F32Params prm = make_params(P, alpha, dt);
+    const bool wide = P->g.max_xcell > 64;
     const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
     const int nt = 32 * kWarpsPerBlock;
     cudaStream_t s = P->stream;
-#define JP_ADVF(D, M)                                                                 \
-    (prm.cells ? advect_f32_kernel<D, M, true><<<nb, nt, 0, s>>>(P->g, Vv, prm, Xi, index) \
-               : advect_f32_kernel<D, M, false><<<nb, nt, 0, s>>>(P->g, Vv, prm, Xi, index))
+#define JP_ADVF(D, M)                                                                              \
+    (wide ? (prm.cells ? advect_f32_kernel<D, M, true, true><<<nb, nt, 0, s>>>(P->g, Vv, prm, Xi, index)   \
+                       : advect_f32_kernel<D, M, false, true><<<nb, nt, 0, s>>>(P->g, Vv, prm, Xi, index)) \
+          : (prm.cells ? advect_f32_kernel<D, M, true, false><<<nb, nt, 0, s>>>(P->g, Vv, prm, Xi, index)  \
+                       : advect_f32_kernel<D, M, false, false><<<nb, nt, 0, s>>>(P->g, Vv, prm, Xi, index)))
     if (!d3) {
         if (method == JP_RUNGE_KUTTA2) JP_ADVF(2, JP_RUNGE_KUTTA2);
         else if (method == JP_RUNGE_KUTTA4) JP_ADVF(2, JP_RUNGE_KUTTA4);
@@ -1003,8 +1263,39 @@ cudaError_t launch_advection_f32(jp_particles* P, int method, double alpha, cons
     return cudaGetLastError();
 }
 
+static cudaError_t launch_move_wide_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args,
+                                        int nargs)
+{
+    const int N = P->g.ndim;
+    P->move.replayable = 0;  // this move leaves no record in the container's scratch
+    XiF Xi{{xi[0], xi[1], N == 3 ? xi[2] : nullptr}};
+    ArgsF A{};
+    A.n = nargs;
+    for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
+    int64_t cols = 1;
+    for (int d = 0; d < N; ++d) cols *= (P->g.n[d] + 2) / 3;
+    const unsigned nb = grid_blocks(cols);
+    const F32Axes& ax = P->f32ax;
+    const bool cells = P->f32_cells != 0;
+    for (int pass = 0; pass < (N == 2 ? 9 : 27); ++pass) {
+        if (N == 2) {
+            if (cells)
+                move_wide_f32<2, true><<<nb, kThreads, 0, P->stream>>>(P->g, Xi, index, A, ax, pass, P->d_err);
+            else
+                move_wide_f32<2, false><<<nb, kThreads, 0, P->stream>>>(P->g, Xi, index, A, ax, pass, P->d_err);
+        } else {
+            if (cells)
+                move_wide_f32<3, true><<<nb, kThreads, 0, P->stream>>>(P->g, Xi, index, A, ax, pass, P->d_err);
+            else
+                move_wide_f32<3, false><<<nb, kThreads, 0, P->stream>>>(P->g, Xi, index, A, ax, pass, P->d_err);
+        }
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_move_f32(jp_particles* P, float* const xi[3], uint8_t* index, float* const* args, int nargs)
 {
+    if (P->g.max_xcell > 64) return launch_move_wide_f32(P, xi, index, args, nargs);  // needs no scratch
     const int N = P->g.ndim;
     // FP32 records (4 bytes per value) fit in the scratch sized for FP64 records
     cudaError_t e = ensure_move_scratch(P, shadow_stride(N + nargs));
@@ -1047,6 +1338,25 @@ cudaError_t launch_inject_f32(jp_particles* P, float* const xi[3], uint8_t* inde
 {
     const int N = P->g.ndim;
     const int64_t nc = P->g.ncells;
+    if (P->g.max_xcell > 64) {  // one warp per cell of each colour, no flag pass
+        XiF Xi{{xi[0], xi[1], N == 3 ? xi[2] : nullptr}};
+        ArgsF A{};
+        A.n = nargs;
+        for (int k = 0; k < nargs; ++k) A.a[k] = args[k];
+        const F32Params prm = make_params(P, 0.5, 0.0);
+        int64_t cols = 1;
+        for (int d = 0; d < N; ++d) cols *= (P->g.n[d] + 1) / 2;
+        const unsigned nb = grid_blocks(cols * 32, 32 * kWarpsPerBlock);
+        for (int pass = 0; pass < (1 << N); ++pass) {
+            if (N == 2)
+                inject_wide_f32<2><<<nb, 32 * kWarpsPerBlock, 0, P->stream>>>(P->g, prm, Xi, index, A, pass, call,
+                                                                              P->d_err);
+            else
+                inject_wide_f32<3><<<nb, 32 * kWarpsPerBlock, 0, P->stream>>>(P->g, prm, Xi, index, A, pass, call,
+                                                                              P->d_err);
+        }
+        return cudaGetLastError();
+    }
     {
         cudaError_t e = ensure_inject_scratch(P);
         if (e != cudaSuccess) return e;
@@ -1103,10 +1413,13 @@ cudaError_t launch_g2p_f32(jp_particles* P, float* Fp, const float* F, const flo
     const bool d3 = P->g.ndim == 3;
     CXiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
     const unsigned nb = grid_blocks(P->g.ncells);
+    const bool wide = P->g.max_xcell > 64;
     if (!d3)
-        g2p_f32_kernel<2><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, Xi, index);
+        wide ? g2p_f32_kernel<2, true><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, Xi, index)
+             : g2p_f32_kernel<2, false><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, Xi, index);
     else
-        g2p_f32_kernel<3><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, Xi, index);
+        wide ? g2p_f32_kernel<3, true><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, Xi, index)
+             : g2p_f32_kernel<3, false><<<nb, kThreads, 0, P->stream>>>(P->g, Fp, F, Xi, index);
     return cudaGetLastError();
 }
 
@@ -1116,6 +1429,7 @@ cudaError_t launch_p2g_f32(jp_particles* P, float* F, const float* Fp, const flo
     const bool d3 = P->g.ndim == 3;
     CXiF Xi{{xi[0], xi[1], d3 ? xi[2] : nullptr}};
     const F32Params prm = make_params(P, 0.5, 0.0);
+    const bool wide = P->g.max_xcell > 64;
     const int64_t V0 = P->g.n[0] + 1, V1 = P->g.n[1] + 1;
     const int64_t rows = P->g.n[d3 ? 2 : 1] + 1;
     if (!d3) {
@@ -1125,14 +1439,22 @@ cudaError_t launch_p2g_f32(jp_particles* P, float* F, const float* Fp, const flo
         int band = (int)((wcols * rows) / 4096);
         band = band < 4 ? 4 : (band > 32 ? 32 : band);
         const int64_t warps = wcols * ((rows + band - 1) / band);
-        p2g_f32_cells2d<<<grid_blocks(warps * 32), kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, band, W);
+        if (wide)
+            p2g_f32_cells2d<true><<<grid_blocks(warps * 32), kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index,
+                                                                                       band, W);
+        else
+            p2g_f32_cells2d<false><<<grid_blocks(warps * 32), kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index,
+                                                                                        band, W);
     } else {
         // blocks of 31 x 7 vertex columns over bands of z rows, as long as still leave about 1024 blocks
         const int64_t wcols = (V0 + 30) / 31, jgroups = (V1 + 6) / 7;
         int band = (int)((wcols * jgroups * rows) / 1024);
         band = band < 4 ? 4 : (band > 32 ? 32 : band);
         const int64_t blocks = wcols * jgroups * ((rows + band - 1) / band);
-        p2g_f32_cells3d<<<(unsigned)blocks, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, band, W);
+        if (wide)
+            p2g_f32_cells3d<true><<<(unsigned)blocks, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, band, W);
+        else
+            p2g_f32_cells3d<false><<<(unsigned)blocks, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, band, W);
     }
     return cudaGetLastError();
 }

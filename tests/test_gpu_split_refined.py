@@ -14,6 +14,9 @@ cell width h:
     sums formed on the host in FP64 from the FP32 offsets and the per-cell
     widths;
   * injection: every cell's first quadrant holds min_xcell / 2^N particles.
+
+Cells wider than 64 slots (uniform and refined) run the wide move and
+injection kernels; they are held to the same bounds and to determinism.
 """
 import numpy as np
 import pytest
@@ -197,6 +200,86 @@ def test_injection_refills_depleted_quadrants_refined(ni):
     assert np.all(np.isfinite(T.numpy()[live]))
     # injected particles copy the field of a particle of the 3^N neighbourhood: all ones here
     assert np.all(T.numpy()[live] == 1.0)
+
+
+@pytest.mark.parametrize("ni,refined", [((24, 20), False), ((20, 16), True), ((8, 7, 6), False), ((7, 6, 6), True)])
+def test_wide_cells_against_fp64(ni, refined):
+    """Cells of more than 64 slots (the reference's 3D miniapps use 125 / 150 /
+    100): the split form's wide move and injection kernels, 10 cycles of
+    advection + move + inject + grid2particle against the FP64 form; position
+    error 2e-4 h by id, offsets inside their cells, particle counts within 1%,
+    and the move and injection rules the same as the narrow kernels'
+    (deterministic: two runs bit-identical)."""
+    g = refined_grid(ni) if refined else W.grid(ni)
+    N = len(ni)
+    nxcell, max_xcell, min_xcell = (90, 120, 60) if N == 2 else (125, 150, 100)
+    a, b = _pair(g, nxcell, max_xcell, min_xcell)
+    c = jp.init_particles(jp.CUDABackend, nxcell, max_xcell, min_xcell, *g["grid_v"])
+    V = _velocity(g)
+    dt = W.cfl_dt(g, V, 0.5)
+    Va = tuple(jp.TA("CUDA")(v) for v in V)
+    Vb = tuple(jp.TA("CUDA")(v).float() for v in V)
+    ida, _, _ = _ids(a)
+    _, hib, lob = _ids(b)
+    fa = jp.CellArray(ida, a.ni)
+    fb = (jp.CellArray(hib.contiguous(), b.ni), jp.CellArray(lob.contiguous(), b.ni))
+    fc = (jp.CellArray(hib.clone(), c.ni), jp.CellArray(lob.clone(), c.ni))
+    xb, xc = jp.init_offsets(b), jp.init_offsets(c)
+    for _ in range(10):
+        jp.advection_(a, jp.RungeKutta2(), Va, dt)
+        jp.move_particles_(a, (fa,))
+        for p, x, f in ((b, xb, fb), (c, xc, fc)):
+            jp.advection_f32_(p, x, jp.RungeKutta2(), Vb, dt)
+            jp.move_particles_f32_(p, x, f)
+    assert torch.equal(b.index.data, c.index.data)
+    for d in range(N):
+        assert torch.equal(xb[d].data.nan_to_num(-7.0), xc[d].data.nan_to_num(-7.0))
+    live_a = a.index.numpy().astype(bool)
+    ids_a = fa.numpy()[live_a].astype(np.int64)
+    pa = np.stack([q.numpy()[live_a] for q in a.coords], axis=1)
+    live_b = b.index.numpy().astype(bool)
+    ids_b = fb[0].numpy()[live_b].astype(np.int64) * 4096 + fb[1].numpy()[live_b].astype(np.int64)
+    back = jp.coords_from_offsets(b, xb)
+    pb = np.stack([q.numpy()[live_b] for q in back], axis=1)
+    assert abs(len(ids_b) - len(ids_a)) <= 0.01 * len(ids_a)
+    common, ia, ib = np.intersect1d(ids_a, ids_b, return_indices=True)
+    assert len(common) > 0.95 * len(ids_a)
+    err = np.abs(pa[ia] - pb[ib]) / np.asarray(g["dx"])[None, :]
+    assert err.max() < 2e-4, f"max error {err.max():.3g} smallest cell widths"
+    for d in range(N):
+        x = xb[d].numpy()[live_b]
+        assert np.all((x >= 0) & (x < 1))
+    # injection into depleted wide cells: the first quadrant refilled, fields copied from neighbours
+    T, = jp.init_cell_arrays_f32(b, 1)
+    T.data[b.index.data.bool()] = 1.0
+    kill = (torch.rand(b.index.data.shape, device="cuda", generator=torch.Generator("cuda").manual_seed(3)) < 0.8)
+    kill &= b.index.data.bool()
+    b.index.data[kill] = 0
+    for d in range(N):
+        xb[d].data[kill] = float("nan")
+    jp.inject_particles_f32_(b, xb, (T,))
+    live = b.index.numpy().astype(bool)
+    inq = live.copy()
+    for d in range(N):
+        x = xb[d].numpy()
+        inq &= (x > 0) & (x < 0.5)
+    min_q = (min_xcell + (1 << N) - 1) >> N
+    assert np.all(inq.sum(axis=0) >= min_q)
+    assert np.all(T.numpy()[live] == 1.0)
+    # grid2particle / particle2grid over the wide slot rows against the FP64 form
+    Tg = W.gaussian_T(g, center=(0.5,) * N, width2=0.05)
+    pa2, = jp.init_cell_arrays(a, 1)
+    jp.grid2particle_(pa2, jp.TA("CUDA")(Tg), a)
+    xa = jp.init_offsets(a)
+    pf, = jp.init_cell_arrays_f32(a, 1)
+    jp.grid2particle_f32_(pf, jp.TA("CUDA")(Tg).float(), a, xa)
+    la = a.index.numpy().astype(bool)
+    rng = Tg.max() - Tg.min()
+    assert np.abs(pa2.numpy()[la] - pf.numpy()[la]).max() < 1e-6 * rng
+    Fa, Fb = jp.grid_field(Tg.shape), jp.grid_field_f32(Tg.shape)
+    jp.particle2grid_(Fa, pa2, a)
+    jp.particle2grid_f32_(Fb, pf, a, xa)
+    assert np.abs(Fa.cpu().numpy() - Fb.cpu().numpy()).max() < 1e-5 * rng
 
 
 def test_other_staggering_is_refused():

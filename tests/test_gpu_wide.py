@@ -101,8 +101,11 @@ def test_phase_ratios_3d_reference_test_size():
         np.testing.assert_allclose(s, 1.0, rtol=1e-12, err_msg=name)
 
 
-def test_wide_cells_rejected_by_narrow_entry_points():
+def test_wide_cells_rejected_by_the_adjoint():
+    """The adjoint keeps 64-bit slot masks; wider cells are refused at the boundary."""
+    from justpic_gb300 import adjoint as A
+
     g = W.grid((8, 8))
     p = jp.init_particles(jp.CUDABackend, 60, 80, 50, *g["grid_v"])
     with pytest.raises(jp.ArgumentError):
-        jp.init_offsets(p)
+        A.slot_ids(p)

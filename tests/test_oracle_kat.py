@@ -215,6 +215,38 @@ def test_advection_2d_refined_miniapp():
     assert refined_grid  # imported helper used by the GPU tests too
 
 
+def _miniapp_3d_refined_grid():
+    """The refined 9^3 grid of test/test_3D.jl:388-399 (cell midpoints, expand_range ghosts)."""
+    from _harness import expand_vector
+    xv = np.array([0.0, 0.04, 0.09, 0.16, 0.25, 0.37, 0.52, 0.68, 0.84, 1.0])
+    yv = np.array([0.0, 0.05, 0.11, 0.2, 0.31, 0.44, 0.58, 0.73, 0.87, 1.0])
+    zv = np.array([0.0, 0.03, 0.08, 0.15, 0.26, 0.4, 0.56, 0.72, 0.88, 1.0])
+    xvi = (xv, yv, zv)
+    ext = tuple(expand_vector(0.5 * (x[1:] + x[:-1])) for x in xvi)
+    grid_v = tuple(tuple(xvi[d] if d == c else ext[d] for d in range(3)) for c in range(3))
+    return {"ndim": 3, "ni": (9, 9, 9), "xv": xvi, "grid_v": grid_v,
+            "dx": tuple(float(np.min(np.diff(x))) for x in xvi)}
+
+
+def miniapp_3d_inputs(g):
+    """test/test_3D.jl:357-368, 401-415: the x-z stream function velocity on the
+    staggered grids, T = z on the vertices, dt = min(dx_min / max|V|) / 4."""
+    V = W.stream_velocity_3d(g)
+    T = W.on_grid(lambda x, y, z: z + 0 * x + 0 * y, g["xv"])
+    dt = min(g["dx"][d] / float(np.max(np.abs(V[d]))) for d in range(3) if np.max(np.abs(V[d])) > 0) / 4
+    return V, T, dt
+
+
+def test_advection_3d_refined_miniapp():
+    # test_3D.jl:387-432 and :445-453: 125/150/100 particles per cell (cells wider
+    # than 64 slots), 5 cycles of particle2grid!, RK2 advection!, move_particles!,
+    # inject_particles!, grid2particle!; relative change of sum(T) below 1e-1
+    g = _miniapp_3d_refined_grid()
+    V, T, dt = miniapp_3d_inputs(g)
+    err = _miniapp(g, V, T, dt, 5, 0.5, nxcell=125, max_xcell=150, min_xcell=100, uniform=False)
+    assert np.isfinite(err) and err < 1e-1
+
+
 def test_rotating_circle_miniapp():
     # test_2D.jl:599-653 (rotation of a disc; 100 steps of dt = 200)
     n = 256
