@@ -757,6 +757,61 @@ __global__ void __launch_bounds__(kDepThreads)
         for (int k = 0; k < kWinParts; ++k) parts[k * nc + c] = part[k][t];
 }
 
+// s += x with the rounding error kept in s.y (TwoSum; needs -fmad=false)
+__device__ __forceinline__ void csum2_add(float2& s, float x)
+{
+    const float t = s.x + x;
+    const float bp = t - s.x;
+    const float err = (s.x - (t - bp)) + (x - bp);
+    s.x = t;
+    s.y += err;
+}
+
+// The deposit of the split-precision form: its staged coordinates are the
+// forward's FP32 interpolation coordinates (t in FP32, exact) and its staged
+// cotangents are rounded to FP32, so the bilinear terms are formed in FP32
+// and summed per window part as compensated FP32 pairs, in the same slot
+// order as deposit_kernel; each pair becomes one FP64 partial sum at the end.
+// The FP64 pipe (1/64 of the FP32 rate, and idle for the lanes on empty
+// slots) is left to the per-cell write-out.
+template <int NQ>
+__global__ void __launch_bounds__(kDepThreads)
+    deposit_f32_kernel(DevGrid g, const uint8_t* __restrict__ index, Staging stg, double* __restrict__ parts)
+{
+    __shared__ float2 part[kWinParts][kDepThreads];
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nc = g.ncells;
+    const bool valid = c < nc;
+    const int64_t ns = stg.nslots;
+    const int t = threadIdx.x;
+    const float* tf = reinterpret_cast<const float*>(stg.t);
+    const float* gkf = reinterpret_cast<const float*>(stg.gk);
+    for (int k = 0; k < kWinParts; ++k) part[k][t] = make_float2(0.0f, 0.0f);
+    const uint64_t m = valid ? live_mask(index, c, nc, g.max_xcell) : 0;
+    const uint32_t hi = __reduce_max_sync(0xffffffffu, m ? 64u - (uint32_t)__clzll((long long)m) : 0u);
+    for (int s = 0; s < (int)hi; ++s) {
+        if (!((m >> s) & 1)) continue;
+        const int64_t a = c + nc * s;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const uint8_t wv = stg.win[q * ns + a];
+            if (wv == 0xFF) continue;
+            const int cc = q & 1;
+            const int NX = win_nx(cc);
+            const int b = (cc == 0 ? 0 : 20) + (wv & 0xF) + NX * (wv >> 4);
+            const float tx = tf[(2 * q) * ns + a], ty = tf[(2 * q + 1) * ns + a];
+            const float gq = gkf[q * ns + a];
+            const float g0 = gq * (1.0f - ty), g1 = gq * ty;
+            csum2_add(part[b][t], g0 * (1.0f - tx));
+            csum2_add(part[b + 1][t], g0 * tx);
+            csum2_add(part[b + NX][t], g1 * (1.0f - tx));
+            csum2_add(part[b + NX + 1][t], g1 * tx);
+        }
+    }
+    if (valid)
+        for (int k = 0; k < kWinParts; ++k) parts[k * nc + c] = (double)part[k][t].x + (double)part[k][t].y;
+}
+
 // ------------------------------------------- split-precision form (FP32)
 // Velocity sample of the FP32 form (velocity_f32's cell and local
 // coordinates, in cell units) with its gradient with respect to the offset.
@@ -816,7 +871,8 @@ __device__ __forceinline__ void jt_f(const SampF* s, const double* g, double* ou
 // Replay kernel of the FP32 form: the stages of advect_f32 (offsets in cell
 // units, FP32, the same operations), then the same reverse sweep as the FP64
 // kernel with the per-axis step w = dt/dx, carried out in FP64; lam is
-// dL/d(offset). The staged samples feed the same deposit and node gather.
+// dL/d(offset). The staged samples (FP32 coordinates and cotangents) feed
+// deposit_f32_kernel and the same node gather.
 template <int METHOD>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, METHOD == JP_RUNGE_KUTTA4 ? 2 : 3)
     advect_vjp_f32_kernel(DevGrid g, const float* __restrict__ V0, const float* __restrict__ V1, F32Params P,
@@ -840,6 +896,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, METHOD == JP_RUNGE_KUTTA4
     const float* Vc[2] = {V0, V1};
     const int64_t ns = stg.nslots;
     const double wd[2] = {(double)P.w[0], (double)P.w[1]}, awd[2] = {(double)P.aw[0], (double)P.aw[1]};
+    float* tf = reinterpret_cast<float*>(stg.t);
+    float* gkf = reinterpret_cast<float*>(stg.gk);
     int errs = 0;
     // the next particle's offsets and cotangents are loaded while this one is worked on
     auto fetch = [&](int kk, int64_t& a, int& l, float* x0, double* lam) {
@@ -943,9 +1001,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, METHOD == JP_RUNGE_KUTTA4
                 const bool in = ox >= 0 && ox <= win_nx(cc) - 2 && oy >= 0 && oy <= win_ny(cc) - 2;
                 if (!in) errs |= kErrAdjointWindow;
                 stg.win[j * ns + a] = in ? (uint8_t)(ox | (oy << 4)) : (uint8_t)0xFF;
-                stg.t[(2 * j) * ns + a] = (double)S[q][cc].t[0];
-                stg.t[(2 * j + 1) * ns + a] = (double)S[q][cc].t[1];
-                stg.gk[j * ns + a] = gk[q][cc];
+                tf[(2 * j) * ns + a] = S[q][cc].t[0];  // FP32 staging (deposit_f32_kernel)
+                tf[(2 * j + 1) * ns + a] = S[q][cc].t[1];
+                gkf[j * ns + a] = (float)gk[q][cc];
             }
     }
     raise_err(d_err, errs);
@@ -1387,13 +1445,13 @@ cudaError_t launch_advection_vjp_f32(jp_particles* P, int method, double alpha, 
     const int nt = 32 * kWarpsPerBlock;
     if (method == JP_RUNGE_KUTTA2) {
         advect_vjp_f32_kernel<JP_RUNGE_KUTTA2><<<nb, nt, 0, st>>>(P->g, V[0], V[1], prm, X, index, L, stg, P->d_err);
-        deposit_kernel<4><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
+        deposit_f32_kernel<4><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
     } else if (method == JP_RUNGE_KUTTA4) {
         advect_vjp_f32_kernel<JP_RUNGE_KUTTA4><<<nb, nt, 0, st>>>(P->g, V[0], V[1], prm, X, index, L, stg, P->d_err);
-        deposit_kernel<8><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
+        deposit_f32_kernel<8><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
     } else {
         advect_vjp_f32_kernel<JP_EULER><<<nb, nt, 0, st>>>(P->g, V[0], V[1], prm, X, index, L, stg, P->d_err);
-        deposit_kernel<2><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
+        deposit_f32_kernel<2><<<nd, kDepThreads, 0, st>>>(P->g, index, stg, adj_parts(P));
     }
     for (int c = 0; c < 2; ++c) {
         const int64_t nn = P->g.nvel[c][0] * P->g.nvel[c][1];
