@@ -167,7 +167,9 @@ int jp_move_particles(jp_particles* p, double* const coords[3], uint8_t* index,
  * scratch (they run the per-cell schedule) and are never rejected for size.
  * The first call on a device looks up the array's device address (and may
  * load the library's device code), so make that first call before any stream
- * capture. All calls share the array and leave their contents in it; nothing
+ * capture; the address is kept for the process and does not survive a
+ * cudaDeviceReset, after which this entry point must not be used on that
+ * device. All calls share the array and leave their contents in it; nothing
  * needs to start at zero. Calls whose kernels overlap on the GPU (e.g. on two
  * streams) race on the array. The call does not touch the container's own
  * move record, so a jp_move_permutation after it is refused.
