@@ -486,11 +486,23 @@ __host__ __device__ __forceinline__ size_t hood_bytes_f32(int M)
     return (bytes + 15) & ~(size_t)15;
 }
 
+// One flagged cell per warp. The cell's own particles are staged in shared
+// memory (offsets in its units); a neighbour cell is staged only when a new
+// particle's search needs it. The nearest neighbour of a new particle is the
+// first minimum of the FP32 squared physical distance in candidate order
+// (neighbour cells k -> j -> i, slots in order): the search scans the own
+// cell, then every neighbour whose lower bound (the gap from the new particle
+// to that neighbour's side of the cell, per axis, squared and summed, less a
+// relative 2^-18 for the rounding of the candidates' own distances) does not
+// exceed the best squared distance found there. A skipped neighbour holds no
+// candidate at or below that distance, so the minimum and its tie order are
+// those of the full scan.
 template <int DIM>
 __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const XiF& Xi,
                                      uint8_t* __restrict__ index, uint64_t* lm, const ArgsF& A, uint32_t call,
                                      int64_t c, float* const* r, uint8_t* live, int lane, int* errs)
 {
+    const unsigned full = 0xffffffffu;
     const int64_t nc = g.ncells;
     const int M = g.max_xcell;
     constexpr int NB = DIM == 2 ? 9 : 27;
@@ -506,14 +518,15 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
         rl[d] = P.cells ? __ldg(P.ax.nbl[d] + I[d]) : 1.0f;
         rh[d] = P.cells ? __ldg(P.ax.nbr[d] + I[d]) : 1.0f;
     }
-    // Stage positions in cell units relative to this cell's lower-left vertex.
-    // Occupancy from the flag pass's per-cell masks (one load per neighbour
-    // cell); the offsets of the live candidates are loaded in batches with all
-    // loads of a batch in flight together.
+    // lane nb < NB: neighbour nb's cell and occupancy (the flag pass's per-cell masks)
     int64_t nbc = 0;
     uint64_t nbm = 0;
+    int nbo[3] = {0, 0, 0};
     if (lane < NB) {
-        const int64_t J[3] = {I[0] + lane % 3 - 1, I[1] + (lane / 3) % 3 - 1, DIM == 3 ? I[2] + lane / 9 - 1 : 0};
+        nbo[0] = lane % 3 - 1;
+        nbo[1] = (lane / 3) % 3 - 1;
+        nbo[2] = DIM == 3 ? lane / 9 - 1 : 0;
+        const int64_t J[3] = {I[0] + nbo[0], I[1] + nbo[1], DIM == 3 ? I[2] + nbo[2] : 0};
         const bool ok = J[0] >= 0 && J[1] >= 0 && J[0] < g.n[0] && J[1] < g.n[1] &&
                         (DIM == 2 || (J[2] >= 0 && J[2] < g.n[2]));
         if (ok) {
@@ -521,38 +534,82 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
             nbm = lm[nbc];
         }
     }
-    constexpr int B = 8;
-    for (int bo = 0; bo < ncand; bo += 32 * B) {
-        float xs[B][DIM];
-        bool lv[B];
+    // Stage the neighbours in `want` (a warp-uniform set): positions in this cell's
+    // units, loads of a batch in flight together, rounds holding no wanted cell skipped.
+    auto stage = [&](uint32_t want) {
+        constexpr int B = 8;
+        for (int bo = 0; bo < ncand; bo += 32 * B) {
+            const int nlo = bo / M, nhi = min(NB - 1, (bo + 32 * B - 1) / M);
+            if (!((want >> nlo) & (0xffffffffu >> (31 - (nhi - nlo))))) continue;
+            float xs[B][DIM];
+            bool lv[B], in[B];
 #pragma unroll
-        for (int u = 0; u < B; ++u) {
-            const int o = bo + 32 * u + lane;
-            const int nb = o / M, s = o - nb * M;
-            const uint64_t m = __shfl_sync(0xffffffffu, nbm, nb < NB ? nb : 0);
-            const int64_t cc = __shfl_sync(0xffffffffu, nbc, nb < NB ? nb : 0);
-            lv[u] = o < ncand && ((m >> s) & 1ull);
-            if (lv[u]) {
+            for (int u = 0; u < B; ++u) {
+                const int o = bo + 32 * u + lane;
+                const int nb = o / M, sl = o - nb * M;
+                const uint64_t m = __shfl_sync(full, nbm, nb < NB ? nb : 0);
+                const int64_t cc = __shfl_sync(full, nbc, nb < NB ? nb : 0);
+                in[u] = o < ncand && ((want >> nb) & 1u);
+                lv[u] = in[u] && ((m >> sl) & 1ull);
+                if (lv[u]) {
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) xs[u][d] = Xi.x[d][cc + nc * s];
+                    for (int d = 0; d < DIM; ++d) xs[u][d] = Xi.x[d][cc + nc * sl];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                if (!in[u]) continue;
+                const int o = bo + 32 * u + lane;
+                const int nb = o / M;
+                const int off[3] = {nb % 3 - 1, (nb / 3) % 3 - 1, DIM == 3 ? nb / 9 - 1 : 0};
+                if (lv[u]) {  // x of cell i-1 -> (x - 1) dx[i-1] / dx[i]; of cell i+1 -> 1 + x dx[i+1] / dx[i]
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                        r[d][o] = off[d] < 0 ? (xs[u][d] - 1.0f) * rl[d]
+                                             : (off[d] > 0 ? fmaf(xs[u][d], rh[d], 1.0f) : xs[u][d]);
+                }
+                live[o] = lv[u] ? 1 : 0;
+            }
+        }
+        __syncwarp();
+    };
+    // lexicographic (squared distance, candidate) minimum over the neighbours in `set`
+    auto scan = [&](uint32_t set, const float* pn, int self, float& best, int& bo) {
+        float lb = CUDART_INF_F;
+        int lo = 0x7fffffff;
+        for (uint32_t m = set; m; m &= m - 1) {
+            const int nb = __ffs(m) - 1;
+            for (int sl = lane; sl < M; sl += 32) {
+                const int o = nb * M + sl;
+                if (!live[o] || o == self) continue;
+                float ss = 0.0f;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const float e = (r[d][o] - pn[d]) * h[d];
+                    ss = fmaf(e, e, ss);
+                }
+                if (ss < lb || (ss == lb && o < lo)) {  // NaN never wins
+                    lb = ss;
+                    lo = o;
+                }
             }
         }
 #pragma unroll
-        for (int u = 0; u < B; ++u) {
-            const int o = bo + 32 * u + lane;
-            if (o >= ncand) continue;
-            const int nb = o / M;
-            const int off[3] = {nb % 3 - 1, (nb / 3) % 3 - 1, DIM == 3 ? nb / 9 - 1 : 0};
-            if (lv[u]) {  // x of cell i-1 -> (x - 1) dx[i-1] / dx[i]; of cell i+1 -> 1 + x dx[i+1] / dx[i]
-#pragma unroll
-                for (int d = 0; d < DIM; ++d)
-                    r[d][o] = off[d] < 0 ? (xs[u][d] - 1.0f) * rl[d]
-                                         : (off[d] > 0 ? fmaf(xs[u][d], rh[d], 1.0f) : xs[u][d]);
+        for (int sh = 16; sh > 0; sh >>= 1) {
+            const float ob = __shfl_xor_sync(full, lb, sh);
+            const int oo = __shfl_xor_sync(full, lo, sh);
+            if (ob < lb || (ob == lb && oo < lo)) {
+                lb = ob;
+                lo = oo;
             }
-            live[o] = lv[u] ? 1 : 0;
         }
-    }
-    __syncwarp();
+        if (lb < best || (lb == best && lo < bo)) {
+            best = lb;
+            bo = lo;
+        }
+    };
+    uint32_t staged = 1u << CENTER;
+    stage(staged);
     const int min_xq = (g.min_xcell + (1 << DIM) - 1) >> DIM;
     const int base = CENTER * M;
     for (int q = 0; q < (1 << DIM); ++q) {
@@ -567,11 +624,11 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
             for (int d = 0; d < DIM; ++d) in = in && r[d][base + s] > qc[d] && r[d][base + s] < qc[d] + 0.5f;
             cnt += in ? 1 : 0;
         }
-        int count = __reduce_add_sync(0xffffffffu, cnt);
+        int count = __reduce_add_sync(full, cnt);
         if (count >= min_xq) break;
         const bool f0 = lane < M && !live[base + lane];
         const bool f1 = lane + 32 < M && !live[base + lane + 32];
-        uint64_t freem = (uint64_t)__ballot_sync(0xffffffffu, f0) | ((uint64_t)__ballot_sync(0xffffffffu, f1) << 32);
+        uint64_t freem = (uint64_t)__ballot_sync(full, f0) | ((uint64_t)__ballot_sync(full, f1) << 32);
         while (freem) {
             const int i = __ffsll((long long)freem) - 1;
             freem &= freem - 1;
@@ -594,35 +651,32 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
                 live[base + i] = 1;
             }
             __syncwarp();
-            // nearest: first minimum of the FP32 squared physical distance in candidate order
             float best = CUDART_INF_F;
             int bo = 0x7fffffff;
-            for (int o = lane; o < ncand; o += 32) {
-                if (!live[o] || o == base + i) continue;
-                float ss = 0.0f;
+            scan(1u << CENTER, pn, base + i, best, bo);
+            // the neighbours that may hold a candidate at or below the best so far: pn lies in
+            // (0, 1) on every axis, so the gap to neighbour side -1 is pn, to side +1 is 1 - pn
+            bool need = false;
+            if (lane < NB && lane != CENTER && nbm != 0) {
+                float lbd = 0.0f;
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) {
-                    const float e = (r[d][o] - pn[d]) * h[d];
-                    ss = fmaf(e, e, ss);
+                    const float gap = nbo[d] < 0 ? pn[d] : (nbo[d] > 0 ? 1.0f - pn[d] : 0.0f);
+                    const float e = gap * h[d];
+                    lbd = fmaf(e, e, lbd);
                 }
-                if (ss < best) {  // NaN never wins
-                    best = ss;
-                    bo = o;
-                }
+                need = lbd * (1.0f - 0x1p-18f) <= best;
             }
-#pragma unroll
-            for (int sh = 16; sh > 0; sh >>= 1) {
-                const float ob = __shfl_xor_sync(0xffffffffu, best, sh);
-                const int oo = __shfl_xor_sync(0xffffffffu, bo, sh);
-                if (ob < best || (ob == best && oo < bo)) {
-                    best = ob;
-                    bo = oo;
-                }
+            const uint32_t S = __ballot_sync(full, need);
+            if (S & ~staged) {
+                stage(S & ~staged);
+                staged |= S;
             }
+            scan(S, pn, base + i, best, bo);
             if (bo != 0x7fffffff) {
-                const int nb = bo / M, s = bo - nb * M;
+                const int nb = bo / M, sl = bo - nb * M;
                 const int64_t J[3] = {I[0] + nb % 3 - 1, I[1] + (nb / 3) % 3 - 1, DIM == 3 ? I[2] + nb / 9 - 1 : 0};
-                const int64_t src = cell_linear<DIM>(g, J) + nc * s;
+                const int64_t src = cell_linear<DIM>(g, J) + nc * sl;
                 for (int k = lane; k < A.n; k += 32) A.a[k][ai] = A.a[k][src];
             } else if (A.n > 0) {
                 *errs |= kWarnNoNeighbour;
@@ -635,7 +689,7 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
     __syncwarp();
     const bool o0 = lane < M && live[base + lane];
     const bool o1 = lane + 32 < M && live[base + lane + 32];
-    const uint64_t own = (uint64_t)__ballot_sync(0xffffffffu, o0) | ((uint64_t)__ballot_sync(0xffffffffu, o1) << 32);
+    const uint64_t own = (uint64_t)__ballot_sync(full, o0) | ((uint64_t)__ballot_sync(full, o1) << 32);
     if (lane == 0) lm[c] = own;
 }
 
