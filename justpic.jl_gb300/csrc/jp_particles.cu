@@ -862,6 +862,54 @@ cudaError_t launch_g2p(jp_particles* P, double* Fp, const double* F, const doubl
 // particle2grid! of nf fields (nf > 1 or tuple: the tuple form), fields in
 // launches of at most four; every launch forms the same weights in the same
 // order, so the result does not depend on how the fields are grouped
+// Launch shape of p2g_kernel: `chunk` vertex rows per thread along the last
+// axis. Each thread also walks the cell row below its first vertex row, so
+// short chunks repeat work, and the threads run in waves of what the GPU holds
+// at once (SMs x resident blocks of this kernel x block size): a last wave
+// filled only in part leaves SMs idle while it runs, and under about one and a
+// half waves the SMs run short of warps to hide the loads' latency. The chunk
+// is the one (3..16 rows) that minimises (chunk + 1/2) x the number of waves
+// among those giving at least 1.5 waves, else 2 (small grids: as many threads
+// as possible); on one GB300 this picks 4 rows at 1024^2 and 5 at 128^3, the
+// fastest or within 3% of the fastest of a measured sweep over 2..16. Results
+// do not depend on it: every vertex sums its cells in the same order whatever
+// the chunk.
+struct P2GShape {
+    int chunk;
+    int64_t threads;
+    unsigned blocks;
+};
+
+template <int DIM, int NF, bool TUPLE>
+static P2GShape p2g_shape(int64_t cols, int64_t rows)
+{
+    static const double resident = [] {  // threads of this kernel the GPU holds at once
+        int dev = 0, sms = 0, bps = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, p2g_kernel<DIM, NF, TUPLE>, kThreads, 0) !=
+                cudaSuccess ||
+            sms <= 0 || bps <= 0) {
+            cudaGetLastError();
+            return 152.0 * 1024.0;
+        }
+        return (double)sms * bps * kThreads;
+    }();
+    int chunk = 2;
+    double best = 0.0;
+    for (int c = 3; c <= 16; ++c) {
+        const double waves = (double)(cols * ((rows + c - 1) / c)) / resident;
+        if (waves < 1.5) continue;
+        const double cost = (c + 0.5) * std::ceil(waves);
+        if (chunk == 2 || cost < best) {
+            chunk = c;
+            best = cost;
+        }
+    }
+    const int64_t threads = cols * ((rows + chunk - 1) / chunk);
+    return P2GShape{chunk, threads, grid_blocks(threads)};
+}
+
 static cudaError_t p2g_launch(jp_particles* P, double* const* F, const double* const* Fp, int nf, bool tuple,
                               const double* const coords[3], const uint8_t* index, double* W)
 {
@@ -870,13 +918,6 @@ static cudaError_t p2g_launch(jp_particles* P, double* const* F, const double* c
     const int64_t V0 = P->g.n[0] + 1, V1 = P->g.n[1] + 1;
     const int64_t cols = d3 ? V0 * V1 : V0;
     const int64_t rows = P->g.n[d3 ? 2 : 1] + 1;
-    // rows per thread: long enough to amortise the prologue row, short enough
-    // to give every SM about 2048 threads
-    const int64_t want = 152LL * 2048;
-    int chunk = (int)((cols * rows) / want);
-    chunk = chunk < 2 ? 2 : (chunk > 16 ? 16 : chunk);
-    const int64_t nthreads = cols * ((rows + chunk - 1) / chunk);
-    const unsigned nb = grid_blocks(nthreads);
     const unsigned nbw = grid_blocks(V0 * V1 * (d3 ? P->g.n[2] + 1 : 1));
     for (int f0 = 0; f0 < nf; f0 += kFieldsPerLaunch) {
         const int n = nf - f0 < kFieldsPerLaunch ? nf - f0 : kFieldsPerLaunch;
@@ -895,7 +936,11 @@ static cudaError_t p2g_launch(jp_particles* P, double* const* F, const double* c
                 p2g_wide_kernel<3, true><<<nbw, kThreads, 0, st>>>(P->g, PF, n, X, index, Wk);
             continue;
         }
-#define JP_P2G(D, NF, T) p2g_kernel<D, NF, T><<<nb, kThreads, 0, st>>>(P->g, PF, X, index, chunk, nthreads, Wk)
+#define JP_P2G(D, NF, T)                                                                                    \
+    do {                                                                                                    \
+        const P2GShape sh = p2g_shape<D, NF, T>(cols, rows);                                                \
+        p2g_kernel<D, NF, T><<<sh.blocks, kThreads, 0, st>>>(P->g, PF, X, index, sh.chunk, sh.threads, Wk); \
+    } while (0)
         if (!d3) {
             if (!tuple) JP_P2G(2, 1, false);
             else if (n == 1) JP_P2G(2, 1, true);
