@@ -1488,10 +1488,11 @@ cudaError_t launch_p2g_f32(jp_particles* P, float* F, const float* Fp, const flo
     const int64_t rows = P->g.n[d3 ? 2 : 1] + 1;
     if (!d3) {
         // cell-centric: warps of 31 vertex columns (+ one cell column to the left) over bands of
-        // `band` vertex rows; bands as long as still leave about 4096 warps
+        // `band` vertex rows; bands as long as still leave about 4096 warps, 4 to 8 rows (a sweep
+        // of 2..32 on one GB300: 8 the fastest at 1024^2, within 1% of the fastest at 2048^2)
         const int64_t wcols = (V0 + 30) / 31;
         int band = (int)((wcols * rows) / 4096);
-        band = band < 4 ? 4 : (band > 32 ? 32 : band);
+        band = band < 4 ? 4 : (band > 8 ? 8 : band);
         const int64_t warps = wcols * ((rows + band - 1) / band);
         if (wide)
             p2g_f32_cells2d<true><<<grid_blocks(warps * 32), kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index,
@@ -1500,10 +1501,11 @@ cudaError_t launch_p2g_f32(jp_particles* P, float* F, const float* Fp, const flo
             p2g_f32_cells2d<false><<<grid_blocks(warps * 32), kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index,
                                                                                         band, W);
     } else {
-        // blocks of 31 x 7 vertex columns over bands of z rows, as long as still leave about 1024 blocks
+        // blocks of 31 x 7 vertex columns over bands of z rows, as long as still leave about 1024
+        // blocks, 4 to 8 rows (8 the fastest of a sweep of 2..32 at 128^3)
         const int64_t wcols = (V0 + 30) / 31, jgroups = (V1 + 6) / 7;
         int band = (int)((wcols * jgroups * rows) / 1024);
-        band = band < 4 ? 4 : (band > 32 ? 32 : band);
+        band = band < 4 ? 4 : (band > 8 ? 8 : band);
         const int64_t blocks = wcols * jgroups * ((rows + band - 1) / band);
         if (wide)
             p2g_f32_cells3d<true><<<(unsigned)blocks, kThreads, 0, P->stream>>>(P->g, prm, F, Fp, Xi, index, band, W);
