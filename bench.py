@@ -88,19 +88,19 @@ def algorithmic_bytes(op, N, nf, m, slots_per_live, grid_bytes_per_live, field_b
 # count. Traffic grows with the particle count, so the bench scales it by the
 # live particles of its own run. FP64 form:
 DRAM_BYTES_PER_PARTICLE_2D_F64 = {
-    "particle2grid!": 103.05,
-    "advection!": 47.57,
+    "particle2grid!": 103.07,
+    "advection!": 47.59,
     "grid2particle!": 46.87,
-    "move_particles!": 192.40,
-    "inject_particles!": 55.83,
+    "move_particles!": 163.91,
+    "inject_particles!": 55.82,
 }
 # the split-precision form (FP32 offsets and fields)
 DRAM_BYTES_PER_PARTICLE_2D_F32 = {
-    "particle2grid!": 29.17,
-    "advection!": 21.10,
-    "grid2particle!": 23.63,
+    "particle2grid!": 29.16,
+    "advection!": 21.07,
+    "grid2particle!": 23.62,
     "move_particles!": 115.83,
-    "inject_particles!": 54.02,
+    "inject_particles!": 31.15,
 }
 
 
