@@ -298,6 +298,7 @@ int jp_particles_destroy(jp_particles* P)
     cudaFree(P->d_err);
     cudaFree(P->g.counts);
     if (P->h_err) cudaFreeHost(P->h_err);
+    if (P->move.passes) cudaGraphExecDestroy(P->move.passes);
     cudaFree(P->move.rec);  // one allocation holds all move scratch
     cudaFree(P->inject.counts);  // counters and lists share one allocation
     cudaFree(P->adj_rec);

@@ -1374,14 +1374,16 @@ cudaError_t launch_move_f32(jp_particles* P, float* const xi[3], uint8_t* index,
             move_classify_f32<2, true><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, ax, P->d_err);
         else
             move_classify_f32<2, false><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, ax, P->d_err);
-        launch_allocate_passes(P->g, S.m, st);
+        e = run_allocate_passes(P, S.m, st);
+        if (e != cudaSuccess) return e;
         move_apply_f32<2><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S);
     } else {
         if (P->f32_cells)
             move_classify_f32<3, true><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, ax, P->d_err);
         else
             move_classify_f32<3, false><<<nbw, ntw, 0, st>>>(P->g, Xi, index, A, S, ax, P->d_err);
-        launch_allocate_passes(P->g, S.m, st);
+        e = run_allocate_passes(P, S.m, st);
+        if (e != cudaSuccess) return e;
         move_apply_f32<3><<<nb, kThreads, 0, st>>>(P->g, Xi, index, A, S);
     }
     return cudaGetLastError();

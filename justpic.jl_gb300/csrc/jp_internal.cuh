@@ -81,6 +81,10 @@ struct MoveScratch {
     // the moves that use this scratch, cleared by any move that does not), so
     // jp_move_permutation can rebuild that move's permutation from them
     int replayable = 0;
+    // the colour passes of a move on this scratch, captured once as a CUDA graph
+    // (their arguments depend only on the container and the scratch's address)
+    cudaGraphExec_t passes = nullptr;
+    const void* passes_key = nullptr;
 };
 
 struct InjectScratch {
@@ -410,6 +414,8 @@ cudaError_t ensure_move_scratch(jp_particles* P, int comps);
 inline int shadow_stride(int comps) { return comps == 3 ? 4 : comps; }
 struct MoveView;
 void launch_allocate_passes(const DevGrid& g, const MoveView& S, cudaStream_t st);
+// the same passes of a move on the container's own scratch, replayed from a CUDA graph
+cudaError_t run_allocate_passes(jp_particles* P, const MoveView& S, cudaStream_t st);
 
 // split-precision form (jp_f32.cu)
 cudaError_t launch_to_offsets(jp_particles* P, const double* const coords[3], const uint8_t* index,

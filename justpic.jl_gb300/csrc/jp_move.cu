@@ -1231,6 +1231,7 @@ cudaError_t ensure_move_scratch(jp_particles* P, int comps)
     if (m.rec) {
         cudaError_t e = cudaStreamSynchronize(P->stream);
         if (e != cudaSuccess) return e;
+        if (m.passes) cudaGraphExecDestroy(m.passes);
         cudaFree(m.rec);
         m = MoveScratch();
     }
@@ -1294,15 +1295,17 @@ cudaError_t launch_move(jp_particles* P, double* const coords[3], uint8_t* index
     const unsigned nb = grid_blocks(P->g.ncells);
     const unsigned nbw = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
     const int ntw = 32 * kWarpsPerBlock;
+    cudaError_t e2 = cudaSuccess;
     if (N == 2) {
         move_classify<2><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
-        launch_allocate_passes(P->g, S, st);
+        e2 = run_allocate_passes(P, S, st);
         move_apply<2><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     } else {
         move_classify<3><<<nbw, ntw, 0, st>>>(P->g, X, index, A, S, P->d_err);
-        launch_allocate_passes(P->g, S, st);
+        e2 = run_allocate_passes(P, S, st);
         move_apply<3><<<nb, kThreads, 0, st>>>(P->g, X, index, A, S);
     }
+    if (e2 != cudaSuccess) return e2;
     return cudaGetLastError();
 }
 
@@ -1320,6 +1323,50 @@ void launch_allocate_passes(const DevGrid& g, const MoveView& S, cudaStream_t st
             move_allocate<3><<<nbp, kAllocThreads, 0, st>>>(g, S, pass / 9, (pass / 3) % 3, pass % 3, mc[0],
                                                             mc[1], mc[2]);
     }
+}
+
+// The colour passes are 3^N short launches whose time is mostly one thread's
+// walk, so the gaps between launches count. Their arguments never change for
+// a container's scratch: the first move captures them on a private stream into
+// a graph, later moves launch that graph on the caller's stream (one launch
+// instead of 9 or 27). A stream that is itself being captured (a caller
+// building its own graph) gets the plain launches; so does any failure to
+// capture or instantiate.
+cudaError_t run_allocate_passes(jp_particles* P, const MoveView& S, cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        launch_allocate_passes(P->g, S, st);
+        return cudaGetLastError();
+    }
+    MoveScratch& m = P->move;
+    if (m.passes && m.passes_key != (const void*)S.rec) {
+        cudaGraphExecDestroy(m.passes);
+        m.passes = nullptr;
+    }
+    if (!m.passes) {
+        cudaStream_t cap = nullptr;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        bool ok = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) == cudaSuccess;
+        if (ok) ok = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            launch_allocate_passes(P->g, S, cap);
+            ok = cudaStreamEndCapture(cap, &graph) == cudaSuccess && graph;
+        }
+        if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+        if (graph) cudaGraphDestroy(graph);
+        if (cap) cudaStreamDestroy(cap);
+        cudaGetLastError();
+        if (!ok) {
+            launch_allocate_passes(P->g, S, st);
+            return cudaGetLastError();
+        }
+        m.passes = exec;
+        m.passes_key = S.rec;
+    }
+    return cudaGraphLaunch(m.passes, st);
 }
 
 template <bool PHASE>
