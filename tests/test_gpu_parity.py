@@ -78,6 +78,24 @@ def test_move_particles_bit_exact(ni, refined):
         pair.assert_same(f"move step {step}")
 
 
+@pytest.mark.parametrize("ni", [(12, 10), (5, 6, 4)])
+def test_move_after_scratch_grows_bit_exact(ni):
+    """The colour passes are captured once per container into a CUDA graph over
+    the container's move scratch; a move with more particle fields reallocates
+    that scratch, and the passes must be captured again."""
+    g = W.grid(ni)
+    pair = Pair(g, 24, 48, 12, nfields=4)
+    V = W.stream_velocity(g) if len(ni) == 2 else W.stream_velocity_3d(g)
+    dt = W.cfl_dt(g, V)
+    for k in range(4):
+        pair.g2p(k, W.linear_T(g, k % len(ni)))
+    for step, nf in enumerate([0, 1, 4, 1, 0]):  # no fields, then more (the scratch grows), then fewer
+        pair.advection("rk2", V, dt)
+        pair.o.move_particles(pair.of[:nf])
+        jp.move_particles_(pair.p, tuple(pair.pf[:nf]))
+        pair.assert_same(f"move step {step} with {nf} fields")
+
+
 def test_move_full_cells_drop_like_reference():
     # tiny capacity: relocation overflows, the first-free-slot-after-starting_point
     # rule decides who is dropped (move_safe.jl:115-117)
