@@ -944,7 +944,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int q0 = 0; q0 < (WIDE ? M : 1); q0 += 64) {  // WIDE: slots in chunks of 64 (max_xcell > 64)
             const uint64_t L = cell_ok ? live_mask(index + nc * q0, c, nc, min(64, M - q0)) : 0;
             const int hi = (int)__reduce_max_sync(full, L ? 64u - (uint32_t)__clzll((long long)L) : 0u);
-            constexpr int B = 4;
+            constexpr int B = 2;  // rows in flight per lane (2 measured 6% faster than 4 at 128^3)
             for (int s0 = 0; s0 < hi; s0 += B) {
                 float x[B], y[B], z[B], f[B];
                 bool lv[B];
