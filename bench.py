@@ -81,26 +81,24 @@ def algorithmic_bytes(op, N, nf, m, slots_per_live, grid_bytes_per_live, field_b
     raise KeyError(op)
 
 
-# DRAM bytes per live particle of each call, 2D, one particle field:
-# dram__bytes_read.sum + dram__bytes_write.sum of the call's kernels (move:
-# classify + 9 colour passes + apply; injection: flag + 4 passes) in one ncu
-# capture of a 512x512-cell C2 case (5.77M particles), divided by its particle
-# count. Traffic grows with the particle count, so the bench scales it by the
-# live particles of its own run. FP64 form:
-DRAM_BYTES_PER_PARTICLE_2D_F64 = {
-    "particle2grid!": 103.07,
-    "advection!": 47.59,
-    "grid2particle!": 46.87,
-    "move_particles!": 163.91,
-    "inject_particles!": 55.82,
-}
-# the split-precision form (FP32 offsets and fields)
-DRAM_BYTES_PER_PARTICLE_2D_F32 = {
-    "particle2grid!": 29.16,
-    "advection!": 21.07,
-    "grid2particle!": 23.62,
-    "move_particles!": 115.83,
-    "inject_particles!": 31.15,
+# DRAM bytes per live particle of each call: dram__bytes_read.sum +
+# dram__bytes_write.sum of the call's kernels (move: classify + colour passes +
+# apply; injection: flag + colour passes), averaged over the calls of one ncu
+# launch-list capture of the workload at its own size (one pass; ncu flushes L2
+# before each launch) and divided by its live particles. The bench multiplies
+# by the live particles of its own run; C4 (2048^2, the same calls as C2) takes
+# the C2 figures, a resized workload (--ni) its own workload's.
+DRAM_BYTES_PER_PARTICLE = {
+    ("C1", "f64"): {"advection!": 31.9, "move_particles!": 93.3},
+    ("C1", "f32"): {"advection!": 17.4, "move_particles!": 57.7},
+    ("C2", "f64"): {"particle2grid!": 99.3, "advection!": 56.9, "grid2particle!": 54.0, "move_particles!": 219.3,
+                    "inject_particles!": 60.7},
+    ("C2", "f32"): {"particle2grid!": 28.4, "advection!": 29.4, "grid2particle!": 29.2, "move_particles!": 141.0,
+                    "inject_particles!": 38.0},
+    ("C3", "f64"): {"particle2grid!": 254.8, "advection!": 76.3, "move_particles!": 231.0,
+                    "inject_particles!": 190.1},
+    ("C3", "f32"): {"particle2grid!": 33.2, "advection!": 40.8, "move_particles!": 153.7,
+                    "inject_particles!": 130.4},
 }
 
 
@@ -437,7 +435,8 @@ def run_ours(args, form=None, minimal=False):
     achieved = bpp[dom] * live / (op_ms[dom] / 1e3) / 1e9
     step_bytes = sum(bpp.values()) * live
     step_gbs = step_bytes / (elapsed / args.steps) / 1e9
-    traffic_table = DRAM_BYTES_PER_PARTICLE_2D_F32 if f32 else DRAM_BYTES_PER_PARTICLE_2D_F64
+    traffic_table = DRAM_BYTES_PER_PARTICLE.get(("C2" if args.workload == "C4" else args.workload,
+                                                 "f32" if f32 else "f64"), {})
     roofline = {
         "bound": "hbm",
         "kernel": dom,
@@ -447,8 +446,9 @@ def run_ours(args, form=None, minimal=False):
         "frac": achieved / peak,
         "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
         else "fallback 6.8 TB/s",
-        "traffic": (traffic_table[dom] * live / 1e9 if (N == 2 and nf == 1 and dom in traffic_table) else None),
-        "traffic_unit": "GB per launch, from ncu dram bytes of a 512^2 capture scaled by particle count",
+        "traffic": traffic_table[dom] * live / 1e9 if dom in traffic_table else None,
+        "traffic_unit": "GB per call, from an ncu capture of the workload at its own size (C4: of C2), "
+                        "bytes per particle x this run's live particles",
         "per_call_frac": {op: bpp[op] * live / (op_ms[op] / 1e3) / 1e9 / peak for op in ops},
     }
     if minimal:
