@@ -141,7 +141,12 @@ int jp_advection_mqs(jp_particles* p, int32_t method, double alpha, const double
 /*
  * move_particles! (src/Particles/move_safe.jl:21-125): relocate particles that
  * left their cell, carrying the nargs particle fields args[0..nargs-1]. Slot
- * allocation reproduces the reference's colour passes exactly.
+ * allocation reproduces the reference's colour passes exactly. The first move
+ * of a container allocates its scratch and captures the colour passes into a
+ * CUDA graph on a private stream; later moves launch that graph on the
+ * container's stream (a stream that is being captured by the caller gets the
+ * plain launches instead; the scratch allocation itself is not allowed inside
+ * a capture, so make the first move before capturing).
  */
 int jp_move_particles(jp_particles* p, double* const coords[3], uint8_t* index,
                       double* const* args, int32_t nargs);
