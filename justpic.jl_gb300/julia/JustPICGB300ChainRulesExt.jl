@@ -1,5 +1,6 @@
-# JustPICGB300ChainRulesExt: a ChainRulesCore rrule for a run of the
-# particle-in-cell loop with a particle2grid! misfit, over the library's
+# JustPICGB300ChainRulesExt: ChainRulesCore rrules for a run of the
+# particle-in-cell loop with a particle2grid! misfit and for single calls
+# (grid2particle!, particle2grid!, one advection! step), over the library's
 # vector-Jacobian entry points (include/justpic_gb300.h, "adjoint"). No
 # counterpart in the reference (ChainRulesCore is not one of its
 # dependencies); it is the Julia form of the reverse sweep in
@@ -139,6 +140,87 @@ function ChainRulesCore.rrule(::typeof(misfit_run), p::GP, method, V, T0, target
                 NoTangent())
     end
     return loss, pullback
+end
+
+# ---- per-call rules (the Julia form of Grid2Particle, Particle2Grid and
+# AdvectionStep in justpic.jl_gb300/adjoint.py): functional forms on the raw
+# arrays (a CellArray's data in its slot layout, grid fields, coordinates),
+# positions fixed for the transfers. 2D and 3D for the transfers; the
+# advection step is 2D like the rest of the adjoint.
+
+# Fp (slot data) = grid2particle!(Fp, F, p) on a fresh array
+function grid2particle_data(F::CuArray{Float64}, p::GP)
+    Fp, = JustPIC.init_cell_arrays(p, Val(1))
+    JustPIC.grid2particle!(Fp, F, p)
+    return Fp.data
+end
+
+function ChainRulesCore.rrule(::typeof(grid2particle_data), F::CuArray{Float64}, p::GP)
+    Fp = grid2particle_data(F, p)
+    function pullback(ΔFp)
+        gF = zero(F)
+        g = CuArray{Float64}(unthunk(ΔFp))
+        check(ccall((:jp_grid2particle_vjp, lib), Cint,
+            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid},
+             NTuple{3, Ptr{Cvoid}}),
+            handle(p).ptr, ptr(F), ptr(g), ptrs3(p.coords), ptr(p.index), ptr(gF), (C_NULL, C_NULL, C_NULL)))
+        return NoTangent(), gF, NoTangent()
+    end
+    return Fp, pullback
+end
+
+# F (vertex field) = particle2grid!(F, Fp, p) from slot data Fp
+function particle2grid_data(Fp::CuArray{Float64}, p::GP)
+    T, = JustPIC.init_cell_arrays(p, Val(1))
+    copyto!(T.data, Fp)
+    F, _ = particle2grid_with_weights(T, p)
+    return F
+end
+
+function ChainRulesCore.rrule(::typeof(particle2grid_data), Fp::CuArray{Float64}, p::GP)
+    T, = JustPIC.init_cell_arrays(p, Val(1))
+    copyto!(T.data, Fp)
+    F, W = particle2grid_with_weights(T, p)
+    function pullback(ΔF)
+        gT = zero(T)
+        g = CuArray{Float64}(unthunk(ΔF))
+        check(ccall((:jp_particle2grid_vjp, lib), Cint,
+            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid},
+             Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}),
+            handle(p).ptr, ptr(F), ptr(W), ptr(T), ptrs3(p.coords), ptr(p.index), ptr(g), ptr(gT),
+            (C_NULL, C_NULL, C_NULL)))
+        return NoTangent(), gT.data, NoTangent()
+    end
+    return F, pullback
+end
+
+# X' = one advection! step of the positions X (a tuple of coordinate data
+# arrays in the slot layout) through the velocity grids V; p supplies the grid
+# and the occupancy, and its own coordinates are left as they were
+function advection_step(X::Tuple, V::Tuple, p::GP, method, dt)
+    saved = map(c -> copy(c.data), p.coords)
+    foreach((c, x) -> copyto!(c.data, x), p.coords, X)
+    JustPIC.advection!(p, method, V, dt)
+    out = map(c -> copy(c.data), p.coords)
+    foreach((c, x) -> copyto!(c.data, x), p.coords, saved)
+    return out
+end
+
+function ChainRulesCore.rrule(::typeof(advection_step), X::Tuple, V::Tuple, p::GP, method, dt)
+    out = advection_step(X, V, p, method, dt)
+    X0 = map(copy, X)
+    idx = copy(p.index.data)
+    function pullback(ΔX)
+        lam = map(d -> CuArray{Float64}(unthunk(d)), unthunk(ΔX))  # dL/dX' in, dL/dX out
+        gV = map(zero, V)
+        check(ccall((:jp_advection_vjp, lib), Cint,
+            (Ptr{Cvoid}, Int32, Float64, NTuple{3, Ptr{Cvoid}}, Float64, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid},
+             NTuple{3, Ptr{Cvoid}}, NTuple{3, Ptr{Cvoid}}),
+            handle(p).ptr, code(method), alpha(method), ptrs3(V), Float64(dt), ptrs3(X0), ptr(idx),
+            ptrs3(lam), ptrs3(gV)))
+        return NoTangent(), Tuple(lam), Tuple(gV), NoTangent(), NoTangent(), NoTangent()
+    end
+    return out, pullback
 end
 
 end  # module

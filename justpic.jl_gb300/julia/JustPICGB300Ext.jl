@@ -133,6 +133,22 @@ function move_particles!(p::GP, args)
     return warn_bits(p)
 end
 
+# move_particles! for host loops that may not allocate device memory once they
+# run (jp_move_particles_noalloc: scratch from a fixed array in the library)
+function move_particles_noalloc!(p::GP, args)
+    a = ptrvec(args)
+    check(ccall((:jp_move_particles_noalloc, lib), Cint,
+        (Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Int32),
+        handle(p).ptr, ptrs3(p.coords), ptr(p.index), a, length(a)))
+    return warn_bits(p)
+end
+
+# calls are synchronous by default, as launch! is; turn that off to queue a
+# time step and wait once (synchronize raises any device-side error)
+synchronous!(p::GP, on::Bool) =
+    check(ccall((:jp_set_synchronous, lib), Cint, (Ptr{Cvoid}, Int32), handle(p).ptr, Int32(on)))
+synchronize(p::GP) = (check(ccall((:jp_synchronize, lib), Cint, (Ptr{Cvoid},), handle(p).ptr)); warn_bits(p))
+
 function inject_particles!(p::GP, args)
     a = ptrvec(args)
     check(ccall((:jp_inject_particles, lib), Cint,
