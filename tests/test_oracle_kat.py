@@ -66,6 +66,23 @@ def test_bisection_closed_interval_and_ties():
     assert O.bisection(x[4], x, 3)[0] == 3
 
 
+def test_cell_index_bounds_like_the_reference():
+    """test/test_2D.jl:143-167: for points drawn in [0, 1] on range(0, 1, 11)
+    and in [-1, 0] on range(-1, 0, 11), the cell found satisfies
+    x[i] <= p < x[i + 1]; the same on a refined vector axis. The oracle's cell
+    search (find_parent_cell_bisection, from any seed cell) is the one the
+    kernels use."""
+    rng = np.random.default_rng(5)
+    axes = [np.linspace(0.0, 1.0, 11), np.linspace(-1.0, 0.0, 11),
+            np.concatenate([[0.0], np.cumsum(1.0 + 0.35 * rng.uniform(-1, 1, 10))]) / 10.0]
+    axes[2] = axes[2] / axes[2][-1]
+    for x in axes:
+        for px in rng.uniform(x[0], x[-1], 200):
+            for seed in (0, 4, len(x) - 2):
+                i, err = O.bisection(px, x, seed)
+                assert err == 0 and x[i] <= px < x[i + 1], (px, i, seed)
+
+
 def test_bisection_is_bounded():
     x = np.linspace(0.0, 1.0, 11)
     s, err = O.bisection(float("nan"), x, 3)
