@@ -311,8 +311,10 @@ int jp_cellarray_permute(jp_particles* p, const void* src, void* dst, int64_t nn
 int jp_particle2centroid(jp_particles* p, double* F, const double* Fp, const double* const coords[3]);
 
 /*
- * Adjoint (vector-Jacobian products) of the FP64 path, 2D only. No
- * counterpart in the reference: it is what a ChainRulesCore rrule of the
+ * Adjoint (vector-Jacobian products) of the FP64 path, 2D; the grid
+ * transfers (jp_particle2grid_with_weights, jp_particle2grid_vjp,
+ * jp_grid2particle_vjp) in 2D and 3D. max_xcell <= 64. No counterpart in
+ * the reference: it is what a ChainRulesCore rrule of the
  * Julia API calls. Gradient arrays share the layout of the values they
  * belong to. Transposes are gathers with a fixed summation order: results are
  * reproducible run to run. Particle relocation is replayed as integer data

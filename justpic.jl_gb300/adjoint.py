@@ -1,5 +1,5 @@
-"""Adjoint of the FP64 hot path in 2D: vector-Jacobian products of one
-advection! step, grid2particle! and particle2grid!, replay of the relocation
+"""Adjoint of the FP64 hot path: vector-Jacobian products of one
+advection! step (2D), grid2particle! and particle2grid! (2D and 3D), replay of the relocation
 done by move_particles!/inject_particles!, and a checkpointed reverse sweep
 over a whole run.
 
@@ -70,8 +70,7 @@ def particle2grid_with_weights_(F: torch.Tensor, W: torch.Tensor, Fp: CellArray,
 def particle2grid_vjp_(gFp: CellArray, gX, gF: torch.Tensor, F: torch.Tensor, W: torch.Tensor, Fp: CellArray,
                        particles: Particles, coords=None, index=None) -> None:
     """Adds dL/dFp to gFp and (if gX is not None) dL/dX to gX, from gF = dL/dF
-    of ``particle2grid!(F, Fp, particles)`` (F, W: its outputs)."""
-    _require_2d(particles)
+    of ``particle2grid!(F, Fp, particles)`` (F, W: its outputs). 2D and 3D."""
     coords = coords if coords is not None else particles.coords
     index = index if index is not None else particles.index
     _bind_stream(particles)
@@ -83,8 +82,7 @@ def particle2grid_vjp_(gFp: CellArray, gX, gF: torch.Tensor, F: torch.Tensor, W:
 
 def grid2particle_vjp_(gF, gX, gFp: CellArray, F, particles: Particles, coords=None, index=None) -> None:
     """Adds dL/dF to gF (if not None) and dL/dX to gX (if not None), from
-    gFp = dL/dFp of ``grid2particle!(Fp, F, particles)``."""
-    _require_2d(particles)
+    gFp = dL/dFp of ``grid2particle!(Fp, F, particles)``. 2D and 3D."""
     coords = coords if coords is not None else particles.coords
     index = index if index is not None else particles.index
     _bind_stream(particles)

@@ -1197,6 +1197,136 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// ----------------------------------------------- the transfers in 3D
+// The same products over the 8 corners of a cell. The forward weight is
+// inv((dx^2 + dy^2) + dz^2) with d = vertex - particle, as particle2grid! forms
+// it in 3D; corners are taken x fastest, then y, then z.
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    p2g_vjp_kernel3(DevGrid g, const double* __restrict__ F, const double* __restrict__ W,
+                    const double* __restrict__ Fp, CCoords X, const uint8_t* __restrict__ index,
+                    const double* __restrict__ gF, double* __restrict__ gFp, Coords gX)
+{
+    __shared__ SlotList lists[kWarpsPerBlock];
+    __shared__ int cellI[kWarpsPerBlock][32][3];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c0 = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32;
+    if (c0 >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    const int M = g.max_xcell;
+    {
+        int64_t I[3];
+        cell_coords(g, min(c0 + lane, nc - 1), I);
+        for (int d = 0; d < 3; ++d) cellI[w][lane][d] = (int)I[d];
+    }
+    uint64_t mine;
+    const int K = build_slot_list(lists[w], index, c0, nc, M, lane, &mine);
+    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
+    for (int k = lane; k < K; k += 32) {
+        int s, l;
+        slot_item(lists[w], M, k, &s, &l);
+        const int64_t a = c0 + l + nc * s;
+        const int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
+        const double p[3] = {X.c[0][a], X.c[1][a], X.c[2][a]};
+        const double f = Fp[a];
+        double gf = 0.0, gx[3] = {0.0, 0.0, 0.0};
+        for (int q = 0; q < 8; ++q) {
+            const int o[3] = {q & 1, (q >> 1) & 1, q >> 2};
+            const int64_t v = (I[0] + o[0]) + V0 * ((I[1] + o[1]) + V1 * (int64_t)(I[2] + o[2]));
+            double e[3];
+            for (int d = 0; d < 3; ++d) e[d] = ldg(g.xv[d] + I[d] + o[d]) - p[d];
+            const double wi = inv_dist2((e[0] * e[0] + e[1] * e[1]) + e[2] * e[2]);
+            const double r = ldg(gF + v) / ldg(W + v);
+            gf = fma(r, wi, gf);
+            const double qd = r * (f - ldg(F + v)) * 2.0 * wi * wi;
+            for (int d = 0; d < 3; ++d) gx[d] = fma(qd, e[d], gx[d]);
+        }
+        gFp[a] += gf;
+        if (gX.c[0])
+            for (int d = 0; d < 3; ++d) gX.c[d][a] += gx[d];
+    }
+}
+
+// dL/dF_v of grid2particle! in 3D: the (up to) eight cells around v, z outer,
+// then y, then x, slots ascending; weight = product of the per-axis linear weights.
+__global__ void __launch_bounds__(kThreads)
+    g2p_vjp_kernel3(DevGrid g, const double* __restrict__ gFp, CCoords X, const uint8_t* __restrict__ index,
+                    double* __restrict__ gF)
+{
+    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1, V2 = g.n[2] + 1;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= V0 * V1 * V2) return;
+    const int64_t i = t % V0, j = (t / V0) % V1, kz = t / (V0 * V1);
+    const int64_t nc = g.ncells;
+    double acc = 0.0;
+    for (int64_t cz = kz - 1; cz <= kz; ++cz) {
+        if (cz < 0 || cz >= g.n[2]) continue;
+        for (int64_t cy = j - 1; cy <= j; ++cy) {
+            if (cy < 0 || cy >= g.n[1]) continue;
+            for (int64_t cx = i - 1; cx <= i; ++cx) {
+                if (cx < 0 || cx >= g.n[0]) continue;
+                const int64_t c = cx + g.n[0] * (cy + g.n[1] * cz);
+                const double x0 = ldg(g.xv[0] + cx), y0 = ldg(g.xv[1] + cy), z0 = ldg(g.xv[2] + cz);
+                const double ixx = ldg(g.ixv[0] + cx), iyy = ldg(g.ixv[1] + cy), izz = ldg(g.ixv[2] + cz);
+                uint64_t m = live_mask(index, c, nc, g.max_xcell);
+                while (m) {
+                    const int s = __ffsll((long long)m) - 1;
+                    m &= m - 1;
+                    const int64_t a = c + nc * s;
+                    const double tx = (X.c[0][a] - x0) * ixx, ty = (X.c[1][a] - y0) * iyy,
+                                 tz = (X.c[2][a] - z0) * izz;
+                    const double fx = cx == i ? 1.0 - tx : tx;
+                    const double fy = cy == j ? 1.0 - ty : ty;
+                    const double fz = cz == kz ? 1.0 - tz : tz;
+                    acc = fma(gFp[a], fx * fy * fz, acc);
+                }
+            }
+        }
+    }
+    gF[t] += acc;
+}
+
+// dL/dx_i += gFp_i * grad(trilinear F)(x_i): along axis d, the differences of
+// the corner values across d weighted by the other two axes' linear weights.
+__global__ void __launch_bounds__(kThreads)
+    g2p_vjp_pos_kernel3(DevGrid g, const double* __restrict__ F, const double* __restrict__ gFp, CCoords X,
+                        const uint8_t* __restrict__ index, Coords gX)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncells) return;
+    const int64_t nc = g.ncells;
+    int64_t I[3];
+    cell_coords(g, c, I);
+    const int64_t V0 = g.n[0] + 1, V1 = g.n[1] + 1;
+    const double* b = F + I[0] + V0 * (I[1] + V1 * I[2]);
+    double f[8];  // corner q = x + 2 y + 4 z
+    for (int q = 0; q < 8; ++q) f[q] = ldg(b + (q & 1) + V0 * ((q >> 1) & 1) + V0 * V1 * (q >> 2));
+    double x0[3], ix[3];
+    for (int d = 0; d < 3; ++d) {
+        x0[d] = ldg(g.xv[d] + I[d]);
+        ix[d] = ldg(g.ixv[d] + I[d]);
+    }
+    uint64_t m = live_mask(index, c, nc, g.max_xcell);
+    while (m) {
+        const int s = __ffsll((long long)m) - 1;
+        m &= m - 1;
+        const int64_t a = c + nc * s;
+        double t[3];
+        for (int d = 0; d < 3; ++d) t[d] = (X.c[d][a] - x0[d]) * ix[d];
+        const double gp = gFp[a];
+        for (int d = 0; d < 3; ++d) {
+            const int e1 = d == 0 ? 1 : 0, e2 = d == 2 ? 1 : 2;  // the other two axes
+            double acc = 0.0;
+            for (int q = 0; q < 8; ++q) {
+                if (!((q >> d) & 1)) continue;
+                const double w1 = (q >> e1) & 1 ? t[e1] : 1.0 - t[e1];
+                const double w2 = (q >> e2) & 1 ? t[e2] : 1.0 - t[e2];
+                acc = fma(f[q] - f[q - (1 << d)], w1 * w2, acc);
+            }
+            gX.c[d][a] += gp * acc * ix[d];
+        }
+    }
+}
+
 // ------------------------------------------------------------ launchers
 // Adjoint scratch: the 40 window partial sums and the injected-slot mask per
 // cell, then the per-slot staging of up to 8 velocity samples (RK4).
@@ -1476,16 +1606,32 @@ cudaError_t launch_p2g_vjp(jp_particles* P, const double* F, const double* W, co
                            const double* const coords[3], const uint8_t* index, const double* gF, double* gFp,
                            double* const gX[3])
 {
-    CCoords X{{coords[0], coords[1], nullptr}};
-    Coords G{{gX ? gX[0] : nullptr, gX ? gX[1] : nullptr, nullptr}};
-    p2g_vjp_kernel<<<grid_blocks(P->g.ncells, 32 * kWarpsPerBlock), 32 * kWarpsPerBlock, 0, P->stream>>>(
-        P->g, F, W, Fp, X, index, gF, gFp, G);
+    const bool d3 = P->g.ndim == 3;
+    CCoords X{{coords[0], coords[1], d3 ? coords[2] : nullptr}};
+    Coords G{{gX ? gX[0] : nullptr, gX ? gX[1] : nullptr, gX && d3 ? gX[2] : nullptr}};
+    const unsigned nb = grid_blocks(P->g.ncells, 32 * kWarpsPerBlock);
+    if (d3)
+        p2g_vjp_kernel3<<<nb, 32 * kWarpsPerBlock, 0, P->stream>>>(P->g, F, W, Fp, X, index, gF, gFp, G);
+    else
+        p2g_vjp_kernel<<<nb, 32 * kWarpsPerBlock, 0, P->stream>>>(P->g, F, W, Fp, X, index, gF, gFp, G);
     return cudaGetLastError();
 }
 
 cudaError_t launch_g2p_vjp(jp_particles* P, const double* F, const double* gFp, const double* const coords[3],
                            const uint8_t* index, double* gF, double* const gX[3])
 {
+    if (P->g.ndim == 3) {
+        CCoords X{{coords[0], coords[1], coords[2]}};
+        if (gF) {
+            const int64_t nv = (P->g.n[0] + 1) * (P->g.n[1] + 1) * (P->g.n[2] + 1);
+            g2p_vjp_kernel3<<<grid_blocks(nv), kThreads, 0, P->stream>>>(P->g, gFp, X, index, gF);
+        }
+        if (gX) {
+            Coords G{{gX[0], gX[1], gX[2]}};
+            g2p_vjp_pos_kernel3<<<grid_blocks(P->g.ncells), kThreads, 0, P->stream>>>(P->g, F, gFp, X, index, G);
+        }
+        return cudaGetLastError();
+    }
     CCoords X{{coords[0], coords[1], nullptr}};
     if (gF) {
         const int64_t nv = (P->g.n[0] + 1) * (P->g.n[1] + 1);

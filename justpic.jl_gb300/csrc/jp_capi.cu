@@ -579,12 +579,14 @@ int jp_particle2grid_f32(jp_particles* P, float* F, const float* Fp, const float
     return finish(P, jp::launch_p2g_f32(P, F, Fp, xi, index), "jp_particle2grid_f32");
 }
 
-// ---- adjoint (2D, FP64) -----------------------------------------------
-static int check_adj(const jp_particles* P, const void* const* coords, const void* index, const char* what)
+// ---- adjoint (FP64; the grid transfers in 2D and 3D, the rest in 2D) ----
+static int check_adj(const jp_particles* P, const void* const* coords, const void* index, const char* what,
+                     bool any_dim = false)
 {
     if (!P || !index || !check_coords(P, coords))
         return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": null pointer");
-    if (P->g.ndim != 2) return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": the adjoint is built for 2D");
+    if (!any_dim && P->g.ndim != 2)
+        return fail(JP_ERR_INVALID_ARGUMENT, std::string(what) + ": the adjoint is built for 2D");
     return JP_OK;
 }
 
@@ -667,7 +669,7 @@ int jp_particle2grid_vjp(jp_particles* P, const double* F, const double* W, cons
                          double* const gX[3])
 {
     JP_REQUIRE_NARROW(P, "jp_particle2grid_vjp");
-    int rc = check_adj(P, (const void* const*)coords, index, "jp_particle2grid_vjp");
+    int rc = check_adj(P, (const void* const*)coords, index, "jp_particle2grid_vjp", true);
     if (rc) return rc;
     if (!F || !W || !Fp || !gF || !gFp || (gX && !check_coords(P, (const void* const*)gX)))
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_particle2grid_vjp: null pointer");
@@ -678,7 +680,7 @@ int jp_grid2particle_vjp(jp_particles* P, const double* F, const double* gFp, co
                          const uint8_t* index, double* gF, double* const gX[3])
 {
     JP_REQUIRE_NARROW(P, "jp_grid2particle_vjp");
-    int rc = check_adj(P, (const void* const*)coords, index, "jp_grid2particle_vjp");
+    int rc = check_adj(P, (const void* const*)coords, index, "jp_grid2particle_vjp", true);
     if (rc) return rc;
     if (!gFp || (gX && (!F || !check_coords(P, (const void* const*)gX))))
         return fail(JP_ERR_INVALID_ARGUMENT, "jp_grid2particle_vjp: null pointer");

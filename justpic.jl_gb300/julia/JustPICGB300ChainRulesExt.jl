@@ -44,11 +44,11 @@ record_bytes(p, method) = (n = Ref{UInt64}(0);
                 handle(p).ptr, code(method), n)); n[])
 
 advection_record!(p, method, V, dt, rec::CuArray{UInt8}) = check(ccall((:jp_advection_record, lib), Cint,
-    (Ptr{Cvoid}, Int32, Float64, NTuple{3, Ptr{Cvoid}}, Float64, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid}),
+    (Ptr{Cvoid}, Int32, Float64, Ptr{Ptr{Cvoid}}, Float64, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid}),
     handle(p).ptr, code(method), alpha(method), ptrs3(V), Float64(dt), ptrs3(p.coords), ptr(p.index), pointer(rec)))
 
 vjp_advection!(p, method, dt, rec, idx, lam, gV) = check(ccall((:jp_advection_vjp_recorded, lib), Cint,
-    (Ptr{Cvoid}, Int32, Float64, Float64, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, NTuple{3, Ptr{Cvoid}}),
+    (Ptr{Cvoid}, Int32, Float64, Float64, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}),
     handle(p).ptr, code(method), alpha(method), Float64(dt), pointer(rec), pointer(idx), ptrs3(lam), ptrs3(gV)))
 
 move_permutation!(dest::CuArray{Int32}, p) =
@@ -69,14 +69,14 @@ function particle2grid_with_weights(T, p)
     F = CUDA.zeros(Float64, length.(p.xvi)...)
     W = similar(F)
     check(ccall((:jp_particle2grid_with_weights, lib), Cint,
-        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
         handle(p).ptr, ptr(F), ptr(W), ptr(T), ptrs3(p.coords), ptr(p.index)))
     return F, W
 end
 
 particle2grid_vjp!(gT, gX, gF, F, W, T, p) = check(ccall((:jp_particle2grid_vjp, lib), Cint,
-    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
-     NTuple{3, Ptr{Cvoid}}),
+    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
+     Ptr{Ptr{Cvoid}}),
     handle(p).ptr, ptr(F), ptr(W), ptr(T), ptrs3(p.coords), ptr(p.index), ptr(gF), ptr(gT), ptrs3(gX)))
 
 # ---- the differentiated function and its rule
@@ -161,9 +161,9 @@ function ChainRulesCore.rrule(::typeof(grid2particle_data), F::CuArray{Float64},
         gF = zero(F)
         g = CuArray{Float64}(unthunk(ΔFp))
         check(ccall((:jp_grid2particle_vjp, lib), Cint,
-            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid},
-             NTuple{3, Ptr{Cvoid}}),
-            handle(p).ptr, ptr(F), ptr(g), ptrs3(p.coords), ptr(p.index), ptr(gF), (C_NULL, C_NULL, C_NULL)))
+            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid},
+             Ptr{Ptr{Cvoid}}),
+            handle(p).ptr, ptr(F), ptr(g), ptrs3(p.coords), ptr(p.index), ptr(gF), C_NULL))
         return NoTangent(), gF, NoTangent()
     end
     return Fp, pullback
@@ -185,10 +185,10 @@ function ChainRulesCore.rrule(::typeof(particle2grid_data), Fp::CuArray{Float64}
         gT = zero(T)
         g = CuArray{Float64}(unthunk(ΔF))
         check(ccall((:jp_particle2grid_vjp, lib), Cint,
-            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid},
-             Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}),
+            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid},
+             Ptr{Cvoid}, Ptr{Ptr{Cvoid}}),
             handle(p).ptr, ptr(F), ptr(W), ptr(T), ptrs3(p.coords), ptr(p.index), ptr(g), ptr(gT),
-            (C_NULL, C_NULL, C_NULL)))
+            C_NULL))
         return NoTangent(), gT.data, NoTangent()
     end
     return F, pullback
@@ -214,8 +214,8 @@ function ChainRulesCore.rrule(::typeof(advection_step), X::Tuple, V::Tuple, p::G
         lam = map(d -> CuArray{Float64}(unthunk(d)), unthunk(ΔX))  # dL/dX' in, dL/dX out
         gV = map(zero, V)
         check(ccall((:jp_advection_vjp, lib), Cint,
-            (Ptr{Cvoid}, Int32, Float64, NTuple{3, Ptr{Cvoid}}, Float64, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid},
-             NTuple{3, Ptr{Cvoid}}, NTuple{3, Ptr{Cvoid}}),
+            (Ptr{Cvoid}, Int32, Float64, Ptr{Ptr{Cvoid}}, Float64, Ptr{Ptr{Cvoid}}, Ptr{Cvoid},
+             Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}),
             handle(p).ptr, code(method), alpha(method), ptrs3(V), Float64(dt), ptrs3(X0), ptr(idx),
             ptrs3(lam), ptrs3(gV)))
         return NoTangent(), Tuple(lam), Tuple(gV), NoTangent(), NoTangent(), NoTangent()

@@ -50,7 +50,9 @@ end
 
 ptr(A::CellArray) = reinterpret(Ptr{Cvoid}, pointer(A.data))
 ptr(A::CuArray) = reinterpret(Ptr{Cvoid}, pointer(A))
-ptrs3(t) = ntuple(i -> i <= length(t) ? ptr(t[i]) : C_NULL, 3)
+# the C ABI's `const double* const coords[3]` is a pointer to three pointers:
+# a Vector (rooted by ccall for the call), NULL past the grid's dimension
+ptrs3(t) = Ptr{Cvoid}[i <= length(t) ? ptr(t[i]) : C_NULL for i in 1:3]
 ptrvec(t) = Ptr{Cvoid}[ptr(x) for x in t]
 
 code(::Euler) = JP_EULER
@@ -96,7 +98,7 @@ function init_particles(::Type{GB300Backend}, nxcell, max_xcell, min_xcell, xi_v
                   q.xci, q.xvi, q.xi_vel)
     h = create_handle(xi_vel, nxcell, max_xcell, min_xcell, UInt64(seed))
     HANDLES[p] = h
-    check(ccall((:jp_init_particles, lib), Cint, (Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+    check(ccall((:jp_init_particles, lib), Cint, (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
         h.ptr, ptrs3(p.coords), ptr(p.index)))
     return p
 end
@@ -120,7 +122,7 @@ for (f, sym) in ((:advection!, :jp_advection), (:advection_LinP!, :jp_advection_
                  (:advection_MQS!, :jp_advection_mqs))
     @eval function $f(p::GP, method::JustPIC.AbstractAdvectionIntegrator, V, dt)
         check(ccall(($(QuoteNode(sym)), lib), Cint,
-            (Ptr{Cvoid}, Int32, Float64, NTuple{3, Ptr{Cvoid}}, Float64, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+            (Ptr{Cvoid}, Int32, Float64, Ptr{Ptr{Cvoid}}, Float64, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
             handle(p).ptr, code(method), alpha(method), ptrs3(V), Float64(dt), ptrs3(p.coords), ptr(p.index)))
     end
 end
@@ -128,7 +130,7 @@ end
 function move_particles!(p::GP, args)
     a = ptrvec(args)
     check(ccall((:jp_move_particles, lib), Cint,
-        (Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Int32),
+        (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Int32),
         handle(p).ptr, ptrs3(p.coords), ptr(p.index), a, length(a)))
     return warn_bits(p)
 end
@@ -138,7 +140,7 @@ end
 function move_particles_noalloc!(p::GP, args)
     a = ptrvec(args)
     check(ccall((:jp_move_particles_noalloc, lib), Cint,
-        (Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Int32),
+        (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Int32),
         handle(p).ptr, ptrs3(p.coords), ptr(p.index), a, length(a)))
     return warn_bits(p)
 end
@@ -152,30 +154,30 @@ synchronize(p::GP) = (check(ccall((:jp_synchronize, lib), Cint, (Ptr{Cvoid},), h
 function inject_particles!(p::GP, args)
     a = ptrvec(args)
     check(ccall((:jp_inject_particles, lib), Cint,
-        (Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Int32),
+        (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Int32),
         handle(p).ptr, ptrs3(p.coords), ptr(p.index), a, length(a)))
     return warn_bits(p)
 end
 
 grid2particle!(Fp, F, p::GP) =
     check(ccall((:jp_grid2particle, lib), Cint,
-        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
         handle(p).ptr, ptr(Fp), ptr(F), ptrs3(p.coords), ptr(p.index)))
 
 particle2grid!(F, Fp, p::GP) =
     check(ccall((:jp_particle2grid, lib), Cint,
-        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
         handle(p).ptr, ptr(F), ptr(Fp), ptrs3(p.coords), ptr(p.index)))
 
 # the tuple forms (grid_to_particle.jl:84-103, particle_to_grid.jl:70-109, 153-199)
 grid2particle!(Fp::NTuple{N}, F::NTuple{N}, p::GP) where {N} =
     check(ccall((:jp_grid2particle_n, lib), Cint,
-        (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Int32, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+        (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Int32, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
         handle(p).ptr, ptrvec(Fp), ptrvec(F), Int32(N), ptrs3(p.coords), ptr(p.index)))
 
 particle2grid!(F::NTuple{N}, Fp::NTuple{N}, p::GP) where {N} =
     check(ccall((:jp_particle2grid_n, lib), Cint,
-        (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Int32, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+        (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Int32, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
         handle(p).ptr, ptrvec(F), ptrvec(Fp), Int32(N), ptrs3(p.coords), ptr(p.index)))
 
 """Particles removed by move_particles! since the last call with clear:
@@ -192,7 +194,7 @@ function inject_particles_phase!(p::GP, phases, args, fields)
     a, f = ptrvec(args), ptrvec(fields)
     centred = Int32[size(x) == size(p.index) for x in fields]  # cell-centred vs vertex fields
     check(ccall((:jp_inject_particles_phase, lib), Cint,
-        (Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}},
+        (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}},
          Ptr{Int32}, Int32),
         handle(p).ptr, ptrs3(p.coords), ptr(p.index), ptr(phases), a, f, centred, length(a)))
     return warn_bits(p)
@@ -204,27 +206,27 @@ function update_phase_ratios!(pr::JustPIC.PhaseRatios, p::GP, xci, xvi, phases)
     n = Int32(JustPIC.numphases(pr))
     faces = length(p.coords) == 2 ? (ptr(pr.Vx), ptr(pr.Vy), C_NULL) : (ptr(pr.Vx), ptr(pr.Vy), ptr(pr.Vz))
     check(ccall((:jp_phase_ratios, lib), Cint,
-        (Ptr{Cvoid}, Int32, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}),
+        (Ptr{Cvoid}, Int32, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}),
         handle(p).ptr, n, ptr(phases), ptrs3(p.coords), ptr(pr.center), ptr(pr.vertex), faces))
     length(p.coords) == 3 && check(ccall((:jp_phase_ratios_midpoints, lib), Cint,
-        (Ptr{Cvoid}, Int32, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, NTuple{3, Ptr{Cvoid}}),
+        (Ptr{Cvoid}, Int32, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}),
         handle(p).ptr, n, ptr(phases), ptrs3(p.coords), (ptr(pr.xy), ptr(pr.yz), ptr(pr.xz))))
     return nothing
 end
 
 grid2particle_flip!(Fp, xvi, F, F0, p::GP; α = 0.0) =
     check(ccall((:jp_grid2particle_flip, lib), Cint,
-        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Float64, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Float64, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
         handle(p).ptr, ptr(Fp), ptr(F), ptr(F0), Float64(α), ptrs3(p.coords), ptr(p.index)))
 
 centroid2particle!(Fp, xci, F, p::GP) =
     check(ccall((:jp_centroid2particle, lib), Cint,
-        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}),
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}),
         handle(p).ptr, ptr(Fp), ptr(F), ptrs3(p.coords)))
 
 particle2centroid!(F, Fp, xci, p::GP) =
     check(ccall((:jp_particle2centroid, lib), Cint,
-        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}),
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}),
         handle(p).ptr, ptr(F), ptr(Fp), ptrs3(p.coords)))
 
 # Array(CellArray) of a GPU CellArray: the (3, 2, 1) permute on the device,
@@ -243,33 +245,33 @@ end
 # is implicit. Uniform and vector grids with the standard staggering (cell
 # midpoints plus one ghost node at each end along the centred axes).
 offsets!(xi, p::GP) = check(ccall((:jp_offsets_from_coords, lib), Cint,
-    (Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}),
+    (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}),
     handle(p).ptr, ptrs3(p.coords), ptr(p.index), ptrs3(xi)))
 
 coords!(p::GP, xi) = check(ccall((:jp_coords_from_offsets, lib), Cint,
-    (Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}),
+    (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}),
     handle(p).ptr, ptrs3(xi), ptr(p.index), ptrs3(p.coords)))
 
 advection_f32!(p::GP, xi, method, V, dt) = check(ccall((:jp_advection_f32, lib), Cint,
-    (Ptr{Cvoid}, Int32, Float64, NTuple{3, Ptr{Cvoid}}, Float64, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+    (Ptr{Cvoid}, Int32, Float64, Ptr{Ptr{Cvoid}}, Float64, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
     handle(p).ptr, code(method), alpha(method), ptrs3(V), Float64(dt), ptrs3(xi), ptr(p.index)))
 
 for (f, sym) in ((:move_particles_f32!, :jp_move_particles_f32), (:inject_particles_f32!, :jp_inject_particles_f32))
     @eval function $f(p::GP, xi, args)
         a = ptrvec(args)
         check(ccall(($(QuoteNode(sym)), lib), Cint,
-            (Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Int32),
+            (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Int32),
             handle(p).ptr, ptrs3(xi), ptr(p.index), a, length(a)))
         return warn_bits(p)
     end
 end
 
 grid2particle_f32!(Fp, F, p::GP, xi) = check(ccall((:jp_grid2particle_f32, lib), Cint,
-    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
     handle(p).ptr, ptr(Fp), ptr(F), ptrs3(xi), ptr(p.index)))
 
 particle2grid_f32!(F, Fp, p::GP, xi) = check(ccall((:jp_particle2grid_f32, lib), Cint,
-    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, NTuple{3, Ptr{Cvoid}}, Ptr{Cvoid}),
+    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Cvoid}),
     handle(p).ptr, ptr(F), ptr(Fp), ptrs3(xi), ptr(p.index)))
 
 end  # module
