@@ -631,17 +631,25 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
         const bool f0 = lane < M && !live[base + lane];
         const bool f1 = lane + 32 < M && !live[base + lane + 32];
         uint64_t freem = (uint64_t)__ballot_sync(full, f0) | ((uint64_t)__ballot_sync(full, f1) << 32);
+        constexpr int SPB = 32 / DIM;  // new particles per batch of draws
+        int k = 0;
+        float ub = 0.0f;
         while (freem) {
+            if (k % SPB == 0)
+                ub = batch_draws<DIM, float>(freem, lane, [&](int slot, int d) {
+                    return jp_rand_uniform_f32(g.seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)slot,
+                                               (uint32_t)d);
+                });
             const int i = __ffsll((long long)freem) - 1;
             freem &= freem - 1;
             ++count;
             float pn[3];
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
-                const float u = jp_rand_uniform_f32(g.seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)i,
-                                                    (uint32_t)d);
+                const float u = __shfl_sync(full, ub, (k % SPB) * DIM + d);
                 pn[d] = qc[d] + 0.5f * fmaf(0.95f, u, 0.05f);
             }
+            ++k;
             const int64_t ai = c + nc * i;
             if (lane == 0) {
 #pragma unroll
@@ -695,9 +703,11 @@ __device__ void inject_cell_warp_f32(const DevGrid& g, const F32Params& P, const
     if (lane == 0) lm[c] = own;
 }
 
+// A colour pass: warps take the colour's flagged cells in turn.
 template <int DIM>
-__global__ void inject_pass_f32(DevGrid g, F32Params P, XiF Xi, uint8_t* __restrict__ index, ArgsF A,
-                                InjectListsF Ls, int col, uint32_t call, int* d_err)
+__device__ __forceinline__ void inject_pass_f32_body(const DevGrid& g, const F32Params& P, const XiF& Xi,
+                                                     uint8_t* __restrict__ index, const ArgsF& A,
+                                                     const InjectListsF& Ls, int col, uint32_t call, int* d_err)
 {
     extern __shared__ __align__(16) unsigned char smem_f32[];
     const int lane = threadIdx.x & 31;
@@ -719,6 +729,23 @@ __global__ void inject_pass_f32(DevGrid g, F32Params P, XiF Xi, uint8_t* __restr
         __syncwarp();
     }
     raise_err(d_err, errs);
+}
+
+// 3D: three blocks of four warps per SM, held there by the shared-memory staging
+template <int DIM>
+__global__ void inject_pass_f32(DevGrid g, F32Params P, XiF Xi, uint8_t* __restrict__ index, ArgsF A,
+                                InjectListsF Ls, int col, uint32_t call, int* d_err)
+{
+    inject_pass_f32_body<DIM>(g, P, Xi, index, A, Ls, col, call, d_err);
+}
+
+// 2D: five blocks of four warps per SM (the registers of the walk allow 21 warps)
+template <>
+__global__ void __launch_bounds__(128, 5)
+    inject_pass_f32<2>(DevGrid g, F32Params P, XiF Xi, uint8_t* __restrict__ index, ArgsF A, InjectListsF Ls,
+                       int col, uint32_t call, int* d_err)
+{
+    inject_pass_f32_body<2>(g, P, Xi, index, A, Ls, col, call, d_err);
 }
 
 // ------------------------------------------------------- grid2particle!

@@ -242,6 +242,22 @@ __device__ __forceinline__ void raise_err(int* d_err, int bits)
     if (bits) atomicOr(d_err, bits);
 }
 
+// ---- injection draws, a batch per warp ----------------------------------
+// A cell's new particles take the free slots lowest first, each with DIM
+// draws that depend only on (slot, axis). Instead of every lane drawing every
+// value, lane l draws axis l % DIM of the (l / DIM)-th lowest slot of `free`
+// (32 / DIM slots per batch; 0 for lanes past the batch or the free slots);
+// new particle k of the batch reads its axis d from lane k * DIM + d.
+template <int DIM, typename T, typename Draw>
+__device__ __forceinline__ T batch_draws(uint64_t free, int lane, Draw draw)
+{
+    const int j = lane / DIM, d = lane - j * DIM;
+    if (j >= 32 / DIM) return T(0);
+    uint64_t m = free;
+    for (int t = 0; t < j && m; ++t) m &= m - 1;
+    return m ? draw(__ffsll((long long)m) - 1, d) : T(0);
+}
+
 // ---- exact IEEE comparisons on the integer pipe ------------------------
 // GB300 issues FP64 instructions (compares included) at a small fraction of
 // its integer rate, so range tests use an order-preserving integer key of

@@ -761,17 +761,25 @@ __device__ void inject_cell_pruned(const DevGrid& g, const Coords& X, uint8_t* _
             break;                // injection.jl:100
         }
         uint64_t freem = ~ownm & (M == 64 ? ~0ull : ((1ull << M) - 1));
+        constexpr int SPB = 32 / DIM;  // new particles per batch of draws
+        int k = 0;
+        double ub = 0.0;
         while (freem) {
+            if (k % SPB == 0)
+                ub = batch_draws<DIM, double>(freem, lane, [&](int slot, int d) {
+                    return jp_rand_uniform(g.seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)slot,
+                                           (uint32_t)d);
+                });
             const int i = __ffsll((long long)freem) - 1;
             freem &= freem - 1;
             ++count;
             double pn[3];
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
-                const double r = jp_rand_uniform(g.seed, JP_RNG_STREAM_INJECT, call, (uint64_t)c, (uint32_t)i,
-                                                 (uint32_t)d);
+                const double r = __shfl_sync(0xffffffffu, ub, (k % SPB) * DIM + d);
                 pn[d] = qc[d] + dq[d] * fma(0.95, r, 0.05);  // new_particle, injection.jl:411-417
             }
+            ++k;
             const int64_t ai = c + nc * i;
             long long pnI[3] = {0, 0, 0};
             bool pn_fixed = true;
