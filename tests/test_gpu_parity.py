@@ -174,6 +174,22 @@ def test_inject_particles_bit_exact(ni):
     pair.assert_same("inject twice")
 
 
+@pytest.mark.parametrize("ni,min_xcell", [((6, 5), 200), ((4, 3, 3), 500)])
+def test_inject_many_per_quadrant_bit_exact(ni, min_xcell):
+    """A min_xcell above max_xcell (the reference does not bound it) makes the first
+    quadrant take every free slot of a cell: more new particles than one batch of
+    the warp's draws holds (16 in 2D, 10 in 3D)."""
+    pair, g = _setup(ni, nxcell=4 if len(ni) == 2 else 8, max_xcell=64, min_xcell=min_xcell)
+    pair.g2p(0, W.gaussian_T(g))
+    pair.assert_same("before inject")
+    pair.inject()
+    pair.assert_same("inject")
+    live = pair.o.index.astype(bool)
+    assert live.sum(axis=0).min() == 64  # every free slot was filled
+    pair.inject()
+    pair.assert_same("inject twice")
+
+
 @pytest.mark.parametrize("ni,refined", [((8, 8), False), ((10, 7), True), ((4, 4, 4), False), ((5, 3, 4), True)])
 def test_grid2particle_bit_exact(ni, refined):
     pair, g = _setup(ni, refined=refined)

@@ -123,11 +123,17 @@ def host_inject(ni, index, xi, field, widths, uniform, min_xcell, seed, call):
                         break
 
 
-@pytest.mark.parametrize("ni,refined", [((12, 10), False), ((11, 9), True), ((6, 5, 4), False), ((5, 5, 4), True)])
-def test_split_injection_matches_exhaustive_host_search(ni, refined):
+CASES = [((12, 10), False, None), ((11, 9), True, None), ((6, 5, 4), False, None), ((5, 5, 4), True, None),
+         # min_xcell above max_xcell: a quadrant fills every free slot, more new particles
+         # than one batch of the warp's draws holds (16 in 2D, 10 in 3D)
+         ((4, 3), False, (4, 64, 200)), ((3, 2, 2), True, (8, 64, 500))]
+
+
+@pytest.mark.parametrize("ni,refined,caps", CASES)
+def test_split_injection_matches_exhaustive_host_search(ni, refined, caps):
     g = refined_grid(ni) if refined else W.grid(ni)
     N = len(ni)
-    nxcell, max_xcell, min_xcell = (16, 40, 12) if N == 2 else (16, 40, 16)
+    nxcell, max_xcell, min_xcell = caps or ((16, 40, 12) if N == 2 else (16, 40, 16))
     p = jp.init_particles(jp.CUDABackend, nxcell, max_xcell, min_xcell, *g["grid_v"], seed=7)
     xi = jp.init_offsets(p)
     T, = jp.init_cell_arrays_f32(p, 1)
