@@ -1328,7 +1328,7 @@ void launch_allocate_passes(const DevGrid& g, const MoveView& S, cudaStream_t st
             move_allocate_2d<<<nbp, kAllocThreads, 0, st>>>(g, S, pass / 3, pass % 3, mc[0], mc[1]);
     } else {
         for (int pass = 0; pass < 27; ++pass)  // i outer, k inner (move_safe.jl:39)
-            move_allocate<3><<<nbp, kAllocThreads, 0, st>>>(g, S, pass / 9, (pass / 3) % 3, pass % 3, mc[0],
+            move_allocate_3d<<<nbp, kAllocThreads, 0, st>>>(g, S, pass / 9, (pass / 3) % 3, pass % 3, mc[0],
                                                             mc[1], mc[2]);
     }
 }

@@ -101,54 +101,80 @@ inline size_t move_shadow_offset(const DevGrid& g)
 }
 
 // -------------------------------------------------------------- allocate
-// One colour pass of move_particles!: sources 3*J + o, neighbourhoods
+// One colour pass of move_particles! in 3D: sources 3*J + o, neighbourhoods
 // disjoint, so every mask touched here belongs to exactly one thread. The
-// destination codes and the masks of every neighbour the walk will touch are
-// loaded up front (independent loads), the walk then runs on thread-local
-// copies, and the touched masks are written back at the end. As in the 2D
-// pass below: the slots still to visit are a mask; the centre cell's masks
-// stay in registers; a neighbour's R mask is formed at the write-back (a free
-// slot has its R and U bits clear, so R gains exactly the slots L gained) and
-// its U mask changes only for unstable insertions.
-template <int DIM>
-__global__ void __launch_bounds__(kAllocThreads)
-    move_allocate(DevGrid g, MoveView S, int o0, int o1, int o2, int64_t m0, int64_t m1, int64_t m2)
+// walk is the 2D pass's (below), on 27 neighbours:
+//  * the destination codes of the source's original movers are read four
+//    loads at a time and kept as five bit planes (bit j of slot s's code in
+//    plane j), with the movers that leave and those not strictly inside their
+//    new cell as two more masks: no per-slot table in local memory;
+//  * the masks of the neighbours the walk may touch are loaded together and
+//    kept in the thread's own column of shared memory (27 x 64 threads x 2
+//    words: one indexed access per step, conflict-free);
+//  * the slots still to visit are a mask; the centre cell's masks stay in
+//    registers; a neighbour's R mask is formed at the write-back (a free slot
+//    has its R and U bits clear, so R gains exactly the slots L gained) and
+//    its U mask changes only for unstable insertions.
+static __global__ void __launch_bounds__(kAllocThreads)
+    move_allocate_3d(DevGrid g, MoveView S, int o0, int o1, int o2, int64_t m0, int64_t m1, int64_t m2)
 {
-    constexpr int NB = DIM == 2 ? 9 : 27;
-    constexpr int CENTER = DIM == 2 ? 4 : 13;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    constexpr int NB = 27;
+    constexpr int CENTER = 13;
+    __shared__ uint64_t sL[NB][kAllocThreads], sU[NB][kAllocThreads];
+    const int tid = threadIdx.x;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + tid;
     if (t >= m0 * m1 * m2) return;
     int64_t idx[3];
     idx[0] = 3 * (t % m0) + o0;
     idx[1] = 3 * ((t / m0) % m1) + o1;
-    idx[2] = DIM == 3 ? 3 * (t / (m0 * m1)) + o2 : 0;
+    idx[2] = 3 * (t / (m0 * m1)) + o2;
 #pragma unroll
-    for (int d = 0; d < DIM; ++d)
+    for (int d = 0; d < 3; ++d)
         if (idx[d] >= g.n[d]) return;
     const int64_t nc = g.ncells;
-    const int64_t sc = cell_linear<DIM>(g, idx);
+    const int64_t sc = cell_linear<3>(g, idx);
     const uint64_t Mv = S.M(sc);
     const uint64_t U0 = S.U(sc);
     if (Mv == 0 && U0 == 0) return;
-    uint64_t nL[NB], nU[NB];
-    uint8_t codes[64];
     uint64_t Lc = S.L(sc), Rc = S.R(sc), Uc = U0;
+    // the original movers' codes (slots not refilled by an earlier pass)
+    uint64_t P0 = 0, P1 = 0, P2 = 0, P3 = 0, P4 = 0, exits = 0, unst = 0;
     uint32_t touched = 0;  // neighbours (not the centre) the walk may change
-    // codes of the original movers (slots not refilled by an earlier pass)
-    for (uint64_t m = Mv & ~Rc; m; m &= m - 1) {
-        const int s = __ffsll((long long)m) - 1;
-        const uint8_t cb = S.code[sc + nc * s];
-        codes[s] = cb;
-        if (cb != kCodeExit && (cb & 0x1F) != CENTER) touched |= 1u << (cb & 0x1F);
+    for (uint64_t m = Mv & ~Rc; m;) {
+        int sl[4];
+        uint8_t cb[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            sl[u] = m ? __ffsll((long long)m) - 1 : -1;
+            m &= m - 1;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) cb[u] = sl[u] >= 0 ? S.code[sc + nc * sl[u]] : kCodeExit;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (sl[u] < 0) continue;
+            const uint64_t bit = 1ull << sl[u];
+            if (cb[u] == kCodeExit) {
+                exits |= bit;
+                continue;
+            }
+            const int code = min((int)(cb[u] & 0x1F), NB - 1);
+            if (code & 1) P0 |= bit;
+            if (code & 2) P1 |= bit;
+            if (code & 4) P2 |= bit;
+            if (code & 8) P3 |= bit;
+            if (code & 16) P4 |= bit;
+            if (cb[u] & kCodeUnstable) unst |= bit;
+            if (code != CENTER) touched |= 1u << code;
+        }
     }
-    for (uint32_t m = touched; m; m &= m - 1) {
-        const int nb = __ffs(m) - 1;
-        int off[3];
-        nb_offset<DIM>(nb, off);
-        const int64_t J[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
-        const int64_t jc = cell_linear<DIM>(g, J);
-        nL[nb] = S.L(jc);
-        nU[nb] = S.U(jc);
+    const int64_t n0 = g.n[0], n01 = g.n[0] * g.n[1];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+        if (k == CENTER || !((touched >> k) & 1u)) continue;
+        const int64_t jc = sc + (k % 3 - 1) + n0 * ((k / 3) % 3 - 1) + n01 * (k / 9 - 1);
+        sL[k][tid] = S.L(jc);
+        sU[k][tid] = S.U(jc);
     }
     const int nslot = g.max_xcell;
     const uint64_t valid = nslot == 64 ? ~0ull : ((1ull << nslot) - 1);
@@ -162,32 +188,23 @@ __global__ void __launch_bounds__(kAllocThreads)
         const uint64_t bit = todo & (0ull - todo);
         todo ^= bit;
         const int s = __ffsll((long long)bit) - 1;
-        int code;
-        bool unstable;
-        uint16_t tag;
-        if (Rc & bit) {  // refilled by an earlier pass and not strictly inside: walked again
-            code = CENTER;
-            unstable = true;
-            tag = S.orig[sc + nc * s];
-        } else {
-            const uint8_t cb = codes[s];
-            if (cb == kCodeExit) {  // left the domain (or moved too far): cleared
-                Lc &= ~bit;
-                continue;
-            }
-            code = min((int)(cb & 0x1F), NB - 1);
-            unstable = (cb & kCodeUnstable) != 0;
-            int off[3];
-            nb_offset<DIM>(code, off);
-            const int back[3] = {-off[0], -off[1], -off[2]};
-            tag = make_tag(nb_code<DIM>(back), __popcll(Mv & (bit - 1)));
+        const bool refill = (Rc & bit) != 0;  // refilled by an earlier pass: walked again, into the centre
+        if (!refill && (exits & bit)) {  // left the domain (or moved too far): cleared
+            Lc &= ~bit;
+            continue;
         }
+        const int code = refill ? CENTER
+                                : ((P0 & bit) ? 1 : 0) | ((P1 & bit) ? 2 : 0) | ((P2 & bit) ? 4 : 0) |
+                                      ((P3 & bit) ? 8 : 0) | ((P4 & bit) ? 16 : 0);
+        const bool unstable = refill || (unst & bit) != 0;
+        const uint16_t tag = refill ? S.orig[sc + nc * s]
+                                    : make_tag(NB - 1 - code, __popcll(Mv & (bit - 1)));  // the way back
         // remove the particle from its slot (move_safe.jl:110-112)
         Lc &= ~bit;
         Rc &= ~bit;
         Uc &= ~bit;
         // find_free_memory(starting_point, ...) (move_safe.jl:192-197)
-        const uint64_t tL = code == CENTER ? Lc : nL[code];
+        const uint64_t tL = code == CENTER ? Lc : sL[code][tid];
         const uint64_t freem = ~tL & from_sp;
         if (!freem) {  // dropped: no free slot at or after starting_point
             ++n_full;
@@ -205,29 +222,26 @@ __global__ void __launch_bounds__(kAllocThreads)
                 Uc &= ~fb;
             }
         } else {
-            nL[code] = tL | fb;
-            if (unstable) nU[code] |= fb;
+            sL[code][tid] = tL | fb;
+            if (unstable) sU[code][tid] |= fb;
         }
         const int f = __ffsll((long long)fb) - 1;
-        int off[3];
-        nb_offset<DIM>(code, off);
-        const int64_t T[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
-        S.orig[cell_linear<DIM>(g, T) + nc * f] = tag;
+        const int64_t tc = sc + (code % 3 - 1) + n0 * ((code / 3) % 3 - 1) + n01 * (code / 9 - 1);
+        S.orig[tc + nc * f] = tag;
     }
     S.L(sc) = Lc;
     S.R(sc) = Rc;
     S.U(sc) = Uc;
     if (n_full && g.counts) atomicAdd(g.counts + 2, (unsigned long long)n_full);
     // a neighbour only gained slots in this walk: R = R before | the slots L gained
+    // (its R and L in memory are still those before the walk: this thread alone writes them)
     for (uint32_t m = touched; m; m &= m - 1) {
-        const int nb = __ffs(m) - 1;
-        int off[3];
-        nb_offset<DIM>(nb, off);
-        const int64_t J[3] = {idx[0] + off[0], idx[1] + off[1], DIM == 3 ? idx[2] + off[2] : 0};
-        const int64_t jc = cell_linear<DIM>(g, J);
-        S.R(jc) = S.R(jc) | (nL[nb] & ~S.L(jc));
-        S.L(jc) = nL[nb];
-        S.U(jc) = nU[nb];
+        const int k = __ffs(m) - 1;
+        const int64_t jc = sc + (k % 3 - 1) + n0 * ((k / 3) % 3 - 1) + n01 * (k / 9 - 1);
+        const uint64_t Lf = sL[k][tid];
+        S.R(jc) = S.R(jc) | (Lf & ~S.L(jc));
+        S.L(jc) = Lf;
+        S.U(jc) = sU[k][tid];
     }
 }
 
@@ -245,7 +259,6 @@ __global__ void __launch_bounds__(kAllocThreads)
 //    the thread's own column of shared memory (one indexed access, no select
 //    over the neighbours), all global loads are issued before the first
 //    shared-memory store.
-// Same walk, same result as move_allocate<2>.
 static __global__ void __launch_bounds__(kAllocThreads)
     move_allocate_2d(DevGrid g, MoveView S, int o0, int o1, int64_t m0, int64_t m1)
 {
