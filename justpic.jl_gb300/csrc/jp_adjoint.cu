@@ -1049,7 +1049,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
                 float ss = 0.0f;
                 ss = fmaf(ex, ex, ss);
                 ss = fmaf(ey, ey, ss);
-                const double wi = (double)__frcp_rn(ss);
+                const double wi = (double)p2g_weight_f32(ss);
                 const double r = ldg(gF + v) / ldg(W + v);
                 gf = fma(r, wi, gf);
                 const double q = r * (f - (double)__ldg(F + v)) * 2.0 * wi * wi;

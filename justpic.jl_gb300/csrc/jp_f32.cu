@@ -845,7 +845,7 @@ __device__ __forceinline__ double csum_value(const CSum& s) { return (double)s.h
 // adds its cells' pairs in the reference's cell order in FP64: the lower
 // corners of a cell row finish the vertex row below it, the upper corners
 // start the row above. No cell is read again for each of its vertices.
-__device__ __forceinline__ float p2g_w_f32(float qx, float e) { return __frcp_rn(fmaf(e, e, qx)); }
+__device__ __forceinline__ float p2g_w_f32(float qx, float e) { return p2g_weight_f32(fmaf(e, e, qx)); }
 
 template <bool WIDE>
 __global__ void __launch_bounds__(kThreads)
@@ -1003,7 +1003,7 @@ __global__ void __launch_bounds__(kThreads)
                             const float qxy = fmaf(ey[ky], ey[ky], qx[kx]);
 #pragma unroll
                             for (int kz = 0; kz < 2; ++kz) {
-                                const float wi = __frcp_rn(fmaf(ez[kz], ez[kz], qxy));
+                                const float wi = p2g_weight_f32(fmaf(ez[kz], ez[kz], qxy));
                                 csum_add(cw[kx][ky][kz], wi);
                                 csum_add_prod(cf[kx][ky][kz], wi, f[u]);
                             }

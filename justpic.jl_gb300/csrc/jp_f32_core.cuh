@@ -200,4 +200,16 @@ inline F32Params make_params(const jp_particles* P, double alpha, double dt)
     return p;
 }
 
+// particle2grid! weight of the split form, 1 / distance^2 in FP32: the
+// special-function unit's reciprocal (rcp.approx.f32, one instruction instead
+// of the correctly rounded sequence; deterministic, its error of the order of
+// the FP32 distance's own rounding). The forward sums and the adjoint use it
+// alike.
+__device__ __forceinline__ float p2g_weight_f32(float ss)
+{
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(ss));
+    return r;
+}
+
 }  // namespace jp
