@@ -453,16 +453,26 @@ __global__ void __launch_bounds__(kThreads)
         // the cell's occupancy mask, kept for the passes' neighbourhood staging
         const uint64_t live = live_mask(index, c, nc, g.max_xcell);
         Ls.lm[c] = live;
-        int count = 0;
-        for (uint64_t m = live; m && count < min_xq; m &= m - 1) {
-            const int64_t a = c + nc * (__ffsll((long long)m) - 1);
-            bool in = true;
+        int count = 0;  // live particles in the first quadrant, counted until min_xq is reached
+        constexpr int B = 4;  // slots per step, their loads in flight together
+        for (uint64_t m = live; m && count < min_xq;) {
+            float xs[B][DIM];
+            bool lv[B];
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const float x = Xi.x[d][a];
-                in = in && x > 0.0f && x < 0.5f;
+            for (int u = 0; u < B; ++u) {
+                lv[u] = m != 0;
+                const int64_t a = c + nc * (lv[u] ? __ffsll((long long)m) - 1 : 0);
+                m &= m - 1;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) xs[u][d] = lv[u] ? Xi.x[d][a] : 0.0f;
             }
-            count += in ? 1 : 0;
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                bool in = lv[u];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) in = in && xs[u][d] > 0.0f && xs[u][d] < 0.5f;
+                count += in ? 1 : 0;
+            }
         }
         flag = count < min_xq;
     }

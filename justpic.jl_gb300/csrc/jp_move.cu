@@ -351,26 +351,38 @@ __global__ void __launch_bounds__(kThreads)
     long long blo[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, bhi[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
     int cq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const int smax = __reduce_max_sync(0xffffffffu, live ? 64 - __clzll((long long)live) : 0);
-    for (int s = 0; s < smax; ++s) {
-        if (!((live >> s) & 1ull)) continue;
-        const int64_t a = c + nc * s;
-        unsigned in0 = 0, in1 = 0;
+    constexpr int B = 4;  // slots per step, their loads in flight together
+    for (int s0 = 0; s0 < smax; s0 += B) {
+        double xs[B][DIM];
+        bool lv[B];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            const double x = X.c[d][a];
-            const bool ok = !is_nan_bits(x);
-            const long long k = okey(x);
-            if (ok) {
-                blo[d] = min(blo[d], k);
-                bhi[d] = max(bhi[d], k);
-            }
-            in0 |= (unsigned)(ok & (klo[0][d] < k) & (k < khi[0][d])) << d;
-            in1 |= (unsigned)(ok & (klo[1][d] < k) & (k < khi[1][d])) << d;
+        for (int u = 0; u < B; ++u) {
+            const int s = s0 + u;
+            lv[u] = s < smax && ((live >> s) & 1ull);
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) xs[u][d] = lv[u] ? X.c[d][c + nc * s] : 0.0;
         }
-        constexpr unsigned full = (1u << DIM) - 1u;
 #pragma unroll
-        for (int q = 0; q < (PHASE ? (1 << DIM) : 1); ++q)  // quadrant q: upper half where bit d of q is set
-            cq[q] += (((in1 & (unsigned)q) | (in0 & ~(unsigned)q & full)) == full) ? 1 : 0;
+        for (int u = 0; u < B; ++u) {
+            if (!lv[u]) continue;
+            unsigned in0 = 0, in1 = 0;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const double x = xs[u][d];
+                const bool ok = !is_nan_bits(x);
+                const long long k = okey(x);
+                if (ok) {
+                    blo[d] = min(blo[d], k);
+                    bhi[d] = max(bhi[d], k);
+                }
+                in0 |= (unsigned)(ok & (klo[0][d] < k) & (k < khi[0][d])) << d;
+                in1 |= (unsigned)(ok & (klo[1][d] < k) & (k < khi[1][d])) << d;
+            }
+            constexpr unsigned full = (1u << DIM) - 1u;
+#pragma unroll
+            for (int q = 0; q < (PHASE ? (1 << DIM) : 1); ++q)  // quadrant q: upper half where bit d of q is set
+                cq[q] += (((in1 & (unsigned)q) | (in0 & ~(unsigned)q & full)) == full) ? 1 : 0;
+        }
     }
     bool flag = false;
     if (valid) {
