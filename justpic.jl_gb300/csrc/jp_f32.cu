@@ -951,7 +951,7 @@ __global__ void __launch_bounds__(kThreads)
 // (i, j) (its own): the lower corners finish the vertex row of this z row, the
 // upper corners start the next one.
 template <bool WIDE>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
     p2g_f32_cells3d(DevGrid g, F32Params P, float* __restrict__ F, const float* __restrict__ Fp, CXiF Xi,
                     const uint8_t* __restrict__ index, int band, double* __restrict__ Wout)
 {
