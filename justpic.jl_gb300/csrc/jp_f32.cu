@@ -392,6 +392,57 @@ __global__ void __launch_bounds__(kThreads)
     int64_t I[3] = {0, 0, 0};
     if (valid) cell_coords(g, c, I);
     const int comps = S.m.comps;
+    if (comps == 4 || comps == 2) {
+        // four slot rows per step, the warp still on the same row at a time (stores of
+        // one row share sectors); the rows' origin tags, then their records, are
+        // loaded together, so a step waits for two loads instead of two per row
+        constexpr int B = 4;
+        for (int s0 = 0; s0 < (int)hi_any; s0 += B) {
+            bool ch[B], rf[B];
+            uint16_t tag[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                const int s = s0 + u;
+                ch[u] = s < (int)hi_any && ((changed >> s) & 1);
+                rf[u] = ch[u] && ((R >> s) & 1);
+                tag[u] = rf[u] ? S.m.orig[c + nc * s] : (uint16_t)0;
+            }
+            float v[B][4];
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) v[u][k] = CUDART_NAN_F;  // a vacated slot
+                if (!rf[u]) continue;
+                int off[3];
+                nb_offset<DIM>(tag[u] & 0x1F, off);
+                const int64_t J[3] = {I[0] + off[0], I[1] + off[1], DIM == 3 ? I[2] + off[2] : 0};
+                const float* rec = S.shadow + S.m.record(cell_linear<DIM>(g, J), tag[u] >> 5);
+                if (comps == 4) {
+                    const float4 r4 = *reinterpret_cast<const float4*>(rec);
+                    v[u][0] = r4.x;
+                    v[u][1] = r4.y;
+                    v[u][2] = r4.z;
+                    v[u][3] = r4.w;
+                } else {
+                    const float2 r2 = *reinterpret_cast<const float2*>(rec);
+                    v[u][0] = r2.x;
+                    v[u][1] = r2.y;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                if (!ch[u]) continue;
+                const int64_t a = c + nc * (s0 + u);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) Xi.x[d][a] = v[u][d];
+#pragma unroll
+                for (int k = 0; k < 4 - DIM; ++k)
+                    if (k < A.n) A.a[k][a] = v[u][DIM + k];
+                index[a] = rf[u] ? 1 : 0;
+            }
+        }
+        return;
+    }
     for (int s = 0; s < (int)hi_any; ++s) {
         if (!((changed >> s) & 1)) continue;
         const int64_t a = c + nc * s;
