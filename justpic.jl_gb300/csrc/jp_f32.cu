@@ -393,10 +393,10 @@ __global__ void __launch_bounds__(kThreads)
     if (valid) cell_coords(g, c, I);
     const int comps = S.m.comps;
     if (comps == 4 || comps == 2) {
-        // four slot rows per step, the warp still on the same row at a time (stores of
+        // eight slot rows per step, the warp still on the same row at a time (stores of
         // one row share sectors); the rows' origin tags, then their records, are
         // loaded together, so a step waits for two loads instead of two per row
-        constexpr int B = 4;
+        constexpr int B = 8;
         for (int s0 = 0; s0 < (int)hi_any; s0 += B) {
             bool ch[B], rf[B];
             uint16_t tag[B];

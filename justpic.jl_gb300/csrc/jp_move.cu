@@ -264,9 +264,10 @@ __global__ void __launch_bounds__(kThreads)
     int64_t I[3] = {0, 0, 0};
     if (valid) cell_coords(g, c, I);
     if (S.comps == 4 || S.comps == 2) {
-        // four slot rows per step, the warp still on the same row at a time (stores of
-        // one row share sectors); the rows' origin tags, then their records, are
-        // loaded together, so a step waits for two loads instead of two per row
+        // four slot rows per step (eight hold 100 registers for the same time), the warp
+        // still on the same row at a time (stores of one row share sectors); the rows'
+        // origin tags, then their records, are loaded together, so a step waits for two
+        // loads instead of two per row
         constexpr int B = 4;
         for (int s0 = 0; s0 < (int)hi_any; s0 += B) {
             bool ch[B], rf[B];
