@@ -89,16 +89,16 @@ def algorithmic_bytes(op, N, nf, m, slots_per_live, grid_bytes_per_live, field_b
 # by the live particles of its own run; C4 (2048^2, the same calls as C2) takes
 # the C2 figures, a resized workload (--ni) its own workload's.
 DRAM_BYTES_PER_PARTICLE = {
-    ("C1", "f64"): {"advection!": 31.9, "move_particles!": 93.3},
-    ("C1", "f32"): {"advection!": 17.4, "move_particles!": 57.7},
-    ("C2", "f64"): {"particle2grid!": 99.3, "advection!": 56.9, "grid2particle!": 54.0, "move_particles!": 219.3,
-                    "inject_particles!": 60.7},
-    ("C2", "f32"): {"particle2grid!": 28.4, "advection!": 29.4, "grid2particle!": 29.2, "move_particles!": 141.0,
-                    "inject_particles!": 38.0},
-    ("C3", "f64"): {"particle2grid!": 254.8, "advection!": 76.3, "move_particles!": 231.0,
-                    "inject_particles!": 190.1},
-    ("C3", "f32"): {"particle2grid!": 33.2, "advection!": 40.8, "move_particles!": 153.7,
-                    "inject_particles!": 130.4},
+    ("C1", "f64"): {"advection!": 31.9, "move_particles!": 90.6},
+    ("C1", "f32"): {"advection!": 17.4, "move_particles!": 54.8},
+    ("C2", "f64"): {"particle2grid!": 99.3, "advection!": 56.9, "grid2particle!": 54.0, "move_particles!": 216.1,
+                    "inject_particles!": 60.5},
+    ("C2", "f32"): {"particle2grid!": 28.4, "advection!": 29.4, "grid2particle!": 29.2, "move_particles!": 139.0,
+                    "inject_particles!": 38.7},
+    ("C3", "f64"): {"particle2grid!": 254.7, "advection!": 76.3, "move_particles!": 219.0,
+                    "inject_particles!": 188.7},
+    ("C3", "f32"): {"particle2grid!": 37.2, "advection!": 40.8, "move_particles!": 142.0,
+                    "inject_particles!": 129.9},
 }
 
 
