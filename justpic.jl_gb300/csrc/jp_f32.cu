@@ -159,9 +159,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         const int Mc = min(64, M - s0);
         uint64_t mine;
         const int K = build_slot_list(lists[w], index + nc * s0, c0, nc, Mc, lane, &mine);
+        int row = 0;
         for (int k = lane; k < K; k += 32) {
             int s, l;
-            slot_item(lists[w], Mc, k, &s, &l);
+            slot_item_next(lists[w], Mc, k, &row, &s, &l);
             const int64_t a = c0 + l + nc * (s0 + s);
             const int I[3] = {cellI[w][l][0], cellI[w][l][1], cellI[w][l][2]};
             float x0[3], x[3];
@@ -300,6 +301,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         return code;
     };
     constexpr int B = 4;
+    int row = 0;
     for (int k0 = lane; k0 < K; k0 += 32 * B) {
         int sl[B], ll[B];
         int64_t al[B];
@@ -312,7 +314,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             has[u] = k < K;
             sl[u] = 0;
             ll[u] = 0;
-            if (has[u]) slot_item(lists[w], M, k, &sl[u], &ll[u]);
+            if (has[u]) slot_item_next(lists[w], M, k, &row, &sl[u], &ll[u]);
             al[u] = c0 + ll[u] + nc * sl[u];
 #pragma unroll
             for (int d = 0; d < DIM; ++d) xl[u][d] = has[u] ? Xi.x[d][al[u]] : 0.0f;

@@ -346,6 +346,19 @@ __device__ __forceinline__ void slot_item(const SlotList& Lst, int M, int k, int
     *lane = nth_set_bit(Lst.mask[lo], k - Lst.pre[lo]);
 }
 
+// slot_item for a lane whose items k only increase (k, k + 32, ...): the row
+// of item k is searched forward from the row of the lane's previous item
+// (*row, 0 before the first), a few rows back, instead of bisected over all
+// rows. Same answer: the last row s with pre[s] <= k.
+__device__ __forceinline__ void slot_item_next(const SlotList& Lst, int M, int k, int* row, int* slot, int* lane)
+{
+    int s = *row;
+    while (s + 1 < M && Lst.pre[s + 1] <= k) ++s;
+    *row = s;
+    *slot = s;
+    *lane = nth_set_bit(Lst.mask[s], k - Lst.pre[s]);
+}
+
 constexpr int kWarpsPerBlock = 8;
 
 // 64-bit occupancy mask of cell c (bit s = slot s is live)
