@@ -802,9 +802,10 @@ __global__ void inject_pass_f32(DevGrid g, F32Params P, XiF Xi, uint8_t* __restr
     inject_pass_f32_body<DIM>(g, P, Xi, index, A, Ls, col, call, d_err);
 }
 
-// 2D: five blocks of four warps per SM (the registers of the walk allow 21 warps)
+// 2D: six blocks of four warps per SM (80 registers, no spills; a sweep of 5..8 blocks
+// at C2 gave 0.374, 0.364, 0.363, 0.364 ms per call)
 template <>
-__global__ void __launch_bounds__(128, 5)
+__global__ void __launch_bounds__(128, 6)
     inject_pass_f32<2>(DevGrid g, F32Params P, XiF Xi, uint8_t* __restrict__ index, ArgsF A, InjectListsF Ls,
                        int col, uint32_t call, int* d_err)
 {
