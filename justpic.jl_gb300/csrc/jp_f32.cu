@@ -507,7 +507,7 @@ __global__ void __launch_bounds__(kThreads)
         const uint64_t live = live_mask(index, c, nc, g.max_xcell);
         Ls.lm[c] = live;
         int count = 0;  // live particles in the first quadrant, counted until min_xq is reached
-        constexpr int B = 4;  // slots per step, their loads in flight together
+        constexpr int B = 8;  // slots per step, their loads in flight together (4: 3% slower at C3)
         for (uint64_t m = live; m && count < min_xq;) {
             float xs[B][DIM];
             bool lv[B];
