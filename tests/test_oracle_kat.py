@@ -436,3 +436,41 @@ def test_oracle_tuple_forms_match_the_scalar_forms():
                 assert np.array_equal(Gs, Gt[k])
             else:
                 assert np.all(np.abs(Gs - Gt[k]) <= np.spacing(np.abs(Gs)))
+
+
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_particle2grid_jvp_matches_oracle_fd(ndim):
+    """The oracle's dual-number particle2grid! (the checker of the grid transfers'
+    adjoint) against central differences of its own forward: a random tangent of
+    the field and of every coordinate, compared vertex by vertex."""
+    g = W.grid((5, 4) if ndim == 2 else (4, 3, 3))
+    P = _oracle_particles(g, 8, 16, 4)
+    T = W.gaussian_T(g, width2=0.05)
+    pT = P.cell_array()
+    P.grid2particle(pT, T)
+    live = P.index.astype(bool)
+    rng = np.random.default_rng(3)
+    dT = np.where(live, rng.standard_normal(live.shape), 0.0)
+    dX = [np.where(live, rng.standard_normal(live.shape), 0.0) for _ in range(ndim)]
+    shape = tuple(n + 1 for n in g["ni"])
+    F = np.asfortranarray(np.zeros(shape))
+    dF = np.asfortranarray(np.zeros(shape))
+    P.particle2grid_jvp(F, dF, pT, dT, [np.ascontiguousarray(x) for x in dX])
+    F0 = np.asfortranarray(np.zeros(shape))
+    P.particle2grid(F0, pT)
+    np.testing.assert_array_equal(F, F0)  # the dual run's values are the forward's
+    x0 = [c.copy() for c in P.coords]
+    h = 1e-6
+
+    def forward(sign):
+        for d in range(ndim):
+            P.coords[d][...] = x0[d] + sign * h * dX[d]
+        Fs = np.asfortranarray(np.zeros(shape))
+        P.particle2grid(Fs, np.where(live, pT + sign * h * dT, pT))
+        return Fs
+
+    fd = (forward(1.0) - forward(-1.0)) / (2 * h)
+    for d in range(ndim):
+        P.coords[d][...] = x0[d]
+    scale = np.max(np.abs(dF))
+    np.testing.assert_allclose(dF, fd, rtol=1e-5, atol=1e-6 * scale)
