@@ -69,21 +69,53 @@ def julia_shape(t):
             "UInt8": "u8"}.get(t, t)
 
 
+def _types_after(text, start):
+    i, depth = start, 1
+    while depth:
+        depth += {"(": 1, ")": -1}.get(text[i], 0)
+        i += 1
+    return _split_top(" ".join(text[start:i - 1].split()))
+
+
 def ccalls():
+    """(file, line, entry point, argument types) of every ccall: the literal ones,
+    and those an `@eval` loop generates (`for (f, sym) in ((:f, :jp_x), ...)`
+    around `ccall(($(QuoteNode(sym)), lib), ...)`), once per symbol."""
     out = []
     for fn in sorted(os.listdir(JULIA)):
         if not fn.endswith(".jl"):
             continue
         text = open(os.path.join(JULIA, fn)).read()
         for m in re.finditer(r"ccall\(\(:(jp_[a-z0-9_]+),\s*lib\),\s*\w+,\s*\(", text):
-            i, depth = m.end(), 1
-            while depth:
-                depth += {"(": 1, ")": -1}.get(text[i], 0)
-                i += 1
-            types = _split_top(" ".join(text[m.end():i - 1].split()))
             line = text.count("\n", 0, m.start()) + 1
-            out.append((fn, line, m.group(1), types))
+            out.append((fn, line, m.group(1), _types_after(text, m.end())))
+        for loop in re.finditer(r"for \(f, sym\) in \(((?:[^()]|\([^()]*\))*)\)", text):
+            syms = re.findall(r":(jp_[a-z0-9_]+)", loop.group(1))
+            m = re.compile(r"ccall\(\(\$\(QuoteNode\(sym\)\),\s*lib\),\s*\w+,\s*\(").search(text, loop.end())
+            assert m and syms, f"{fn}: a generated ccall loop the test cannot read"
+            line = text.count("\n", 0, m.start()) + 1
+            for sym in syms:
+                out.append((fn, line, sym, _types_after(text, m.end())))
     return out
+
+
+# entry points the Julia sources leave to other callers, with the reason
+NOT_BOUND = {
+    "jp_particles_info": "the extension keeps the sizes in its Particles object",
+    "jp_selftest_weight": "a test of the library's weight arithmetic (tests/test_gpu_weight.py)",
+    "jp_advection_vjp_f32": "the FP32-offset adjoint is driven from Python (adjoint.py)",
+    "jp_inject_vjp_i32": "the FP32-offset adjoint is driven from Python (adjoint.py)",
+    "jp_particle2grid_f32_with_weights": "the FP32-offset adjoint is driven from Python (adjoint.py)",
+    "jp_particle2grid_vjp_f32": "the FP32-offset adjoint is driven from Python (adjoint.py)",
+    "jp_slot_ids_i32": "the FP32-offset adjoint is driven from Python (adjoint.py)",
+}
+
+
+def test_every_entry_point_is_bound_or_accounted_for():
+    bound = {name for _, _, name, _ in ccalls()}
+    missing = sorted(set(prototypes()) - bound - set(NOT_BOUND))
+    assert not missing, f"header entry points with no ccall in the Julia sources: {missing}"
+    assert not (bound & set(NOT_BOUND)), "an entry point listed as not bound has a ccall"
 
 
 def test_julia_sources_have_ccalls():
